@@ -1,0 +1,132 @@
+"""ctypes mirror of include/gb_goldstein.h (structs, constants) and helpers that
+fill them from a :class:`cgenie_gb300.grid.Member`.
+
+The structs carry what the reference's ``tstepo`` reads from module state
+(src/goldstein/goldstein_lib.f90:6-180): dimensions, namelist switches and
+grid metrics.  Pointers in ``GbGrid`` reference numpy arrays that the caller
+must keep alive for the duration of the C call (``GridRefs`` does that).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+GB_GO_OK = 0
+GB_GO_EINVAL = -1
+GB_GO_EUNSUPPORTED = -2
+GB_GO_ECUDA = -3
+GB_GO_ENOMEM = -4
+GB_GO_ENOTREADY = -5
+GB_GO_EDEVICE = -6
+GB_GO_ERANGE = -7
+GB_GO_ENONFINITE = -8
+
+GB_GO_FP64 = 0
+GB_GO_FP32FLUX = 1
+GB_GO_MAX_K = 64
+GB_GO_MAX_L = 128
+
+ERRNAMES = {
+    GB_GO_EINVAL: "EINVAL", GB_GO_EUNSUPPORTED: "EUNSUPPORTED", GB_GO_ECUDA: "ECUDA",
+    GB_GO_ENOMEM: "ENOMEM", GB_GO_ENOTREADY: "ENOTREADY", GB_GO_EDEVICE: "EDEVICE",
+    GB_GO_ERANGE: "ERANGE", GB_GO_ENONFINITE: "ENONFINITE",
+}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class GbDims(C.Structure):
+    _fields_ = [("maxi", C.c_int32), ("maxj", C.c_int32), ("maxk", C.c_int32), ("maxl", C.c_int32)]
+
+
+class GbParams(C.Structure):
+    _fields_ = [
+        ("diff", C.c_double * 2),
+        ("ec", C.c_double * 5),
+        ("ediff0", C.c_double),
+        ("ediffpow2", C.c_double),
+        ("dsc", C.c_double),
+        ("ieos", C.c_int32),
+        ("iediff", C.c_int32),
+        ("ediffpow2i", C.c_int32),
+        ("iconv", C.c_int32),
+        ("imld", C.c_int32),
+        ("diso", C.c_int32),
+        ("precision", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class GbGrid(C.Structure):
+    _fields_ = [
+        ("rc", _dp), ("rc2", _dp), ("cv", _dp),
+        ("cv2", _dp), ("dsv", _dp), ("rdsv", _dp),
+        ("ds", _dp), ("rds", _dp),
+        ("dz", _dp), ("dza", _dp), ("rdz", _dp), ("rdza", _dp), ("zro", _dp), ("dt", _dp),
+        ("zw", _dp),
+        ("ssmax", _dp),
+        ("ediff1", _dp),
+        ("diffmax", _dp),
+        ("k1", _ip),
+        ("dphi", C.c_double), ("rdphi", C.c_double),
+    ]
+
+
+class GbEnsTuning(C.Structure):
+    _fields_ = [("tile_i", C.c_int32), ("tile_j", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("use_graph", C.c_int32)]
+
+
+def dptr(a: np.ndarray):
+    """Pointer to a contiguous float64 numpy array (None -> NULL)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(_ip)
+
+
+class GridRefs:
+    """Owns contiguous copies of a member's metric arrays and the ctypes structs
+    that point at them."""
+
+    def __init__(self, m, *, diso=None, ieos=None, iconv=None, iediff=None, precision=GB_GO_FP64):
+        cfg = m.cfg
+        self.arrays = {}
+        for name in ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza",
+                     "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
+            self.arrays[name] = np.ascontiguousarray(getattr(m, name), dtype=np.float64)
+        self.arrays["k1"] = np.ascontiguousarray(m.k1, dtype=np.int32)
+        self.dims = GbDims(m.maxi, m.maxj, m.maxk, m.maxl)
+        p = GbParams()
+        p.diff[0], p.diff[1] = float(m.diff[0]), float(m.diff[1])
+        for n in range(5):
+            p.ec[n] = float(m.ec[n])
+        p.ediff0 = float(m.ediff0)
+        p.ediffpow2 = float(m.ediffpow2)
+        p.dsc = 5.0e3
+        p.ieos = int(cfg.ieos if ieos is None else ieos)
+        p.iediff = int(cfg.iediff if iediff is None else iediff)
+        p.ediffpow2i = int(m.ediffpow2i)
+        p.iconv = int(cfg.iconv if iconv is None else iconv)
+        p.imld = 0
+        p.diso = int(bool(cfg.diso if diso is None else diso))
+        p.precision = int(precision)
+        p.reserved = 0
+        self.params = p
+        g = GbGrid()
+        for name in ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza",
+                     "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
+            setattr(g, name, dptr(self.arrays[name]))
+        g.k1 = iptr(self.arrays["k1"])
+        g.dphi = float(m.dphi)
+        g.rdphi = float(m.rdphi)
+        self.grid = g

@@ -1,0 +1,219 @@
+/*
+ * gb_goldstein.h -- C-ABI of the GB300 GOLDSTEIN ocean tracer timestep.
+ *
+ * This library replaces the body of the reference's `SUBROUTINE tstepo`
+ * (src/goldstein/goldstein.f90:2280-2432) together with the routines it calls:
+ * `tstepo_flux` (:2436-2642, including the `diso` isoneutral branch :2561-2624),
+ * `co` (:2657-2777), `coshuffle` (:2781-2841), `eos` (:3048-3061) and `eosd`
+ * (:3064-3082).  The reference routine takes no arguments and works on SAVE'd
+ * module state declared in src/goldstein/goldstein_lib.f90:6-180; here that state
+ * is passed once through plain C structs and pointers, and kept resident on the
+ * GPU between calls.  A Fortran caller binds these symbols with ISO_C_BINDING
+ * (`BIND(C, NAME=...)`, `TYPE(c_ptr), VALUE`), the same pattern the reference
+ * already uses for its ITT shim (src/utils/itt_fortran.f90:1-44).
+ *
+ * Conventions
+ * -----------
+ *  - Every array argument is a pointer to the FIRST element of the Fortran array
+ *    (its declared lower bound), column-major, REAL(8) = double, INTEGER = int32_t.
+ *  - Index maps (i, j, k counted from the Fortran lower bound, halos included):
+ *      ts(l,i,j,k), ts1(l,i,j,k): (maxl, 0:maxi+1, 0:maxj+1, 0:maxk+1)
+ *          offset = (l-1) + maxl*(i + (maxi+2)*(j + (maxj+2)*k))
+ *      u(c,i,j,k):   (3, 0:maxi, 0:maxj, 1:maxk)
+ *          offset = (c-1) + 3*(i + (maxi+1)*(j + (maxj+1)*(k-1)))
+ *      rho(i,j,k):   (0:maxi+1, 0:maxj+1, 0:maxk)
+ *          offset = i + (maxi+2)*(j + (maxj+2)*k)
+ *      k1(i,j):      (0:maxi+1, 0:maxj+1)      offset = i + (maxi+2)*j
+ *      cost(i,j), icosd(i,j): (1:maxi, 1:maxj) offset = (i-1) + maxi*(j-1)
+ *  - A column (i,j) is wet iff k1(i,j) <= maxk; level k=1 is the deepest and
+ *    k=maxk the surface.  Rows j=0 and j=maxj+1 must be land, and k1 must be
+ *    periodic in i (k1(0,j)=k1(maxi,j), k1(maxi+1,j)=k1(1,j)), as the reference
+ *    enforces when it reads the .k1 file (goldstein.f90:1111-1118).
+ *  - Return value: 0 on success, a negative GB_GO_E* code on failure;
+ *    gb_go_errstr() turns it into text.  The reference aborts through
+ *    `die` -> write_status('ERRORED') -> STOP (src/wrappers/genie_util.f90:14-30);
+ *    the Fortran shim is expected to do that on a non-zero return.
+ *  - Ownership: the caller owns every host array; the library copies what it
+ *    needs during the call and never keeps or frees a caller pointer.
+ *  - A handle is not thread-safe; use one handle per host thread.
+ */
+#ifndef GB_GOLDSTEIN_H
+#define GB_GOLDSTEIN_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_GO_ABI_VERSION 1
+
+/* Error codes. */
+#define GB_GO_OK            0
+#define GB_GO_EINVAL       -1   /* bad argument (NULL pointer, size, flag value) */
+#define GB_GO_EUNSUPPORTED -2   /* option combination not implemented (e.g. imld=1) */
+#define GB_GO_ECUDA        -3   /* a CUDA runtime call failed */
+#define GB_GO_ENOMEM       -4   /* device allocation failed or over the memory budget */
+#define GB_GO_ENOTREADY    -5   /* state/velocity not uploaded yet */
+#define GB_GO_EDEVICE      -6   /* a kernel reported an error status (see detail) */
+#define GB_GO_ERANGE       -7   /* a size exceeds a compiled-in limit */
+#define GB_GO_ENONFINITE   -8   /* non-finite tracer value detected (blow-up guard) */
+
+/* Precision of the flux arithmetic. */
+#define GB_GO_FP64         0    /* plain form: every operation in IEEE double, no FMA
+                                   contraction, in the reference order; bit-identical to
+                                   the reference arithmetic */
+#define GB_GO_FP32FLUX     1    /* face fluxes in FP32, tracer state and its update in
+                                   FP64; inventories in compensated FP64 */
+
+/* Largest supported vertical level count and tracer count. */
+#define GB_GO_MAX_K        64
+#define GB_GO_MAX_L        128
+
+typedef struct gb_go_dims {
+    int32_t maxi;   /* longitudes (dim_GOLDSTEINNLONS) */
+    int32_t maxj;   /* latitudes  (dim_GOLDSTEINNLATS) */
+    int32_t maxk;   /* levels     (dim_GOLDSTEINNLEVS), 2..GB_GO_MAX_K */
+    int32_t maxl;   /* tracers    (dim_GOLDSTEINNTRACS), 2..GB_GO_MAX_L; l=1 is T, l=2 is S */
+} gb_go_dims;
+
+/* Namelist-derived switches and coefficients read by tstepo
+ * (ini_gold_nml, goldstein.f90:596-622; defaults goldstein-defaults.nml). */
+typedef struct gb_go_params {
+    double  diff[2];      /* nondimensional diffusivities after goldstein.f90:1406-1407 */
+    double  ec[5];        /* equation-of-state coefficients, goldstein.f90:1063-1075 */
+    double  ediff0;       /* nondimensional, after ediff (goldstein.f90:2946) */
+    double  ediffpow2;    /* exponent used when ediffpow2i is neither 0, 1 nor 2 */
+    double  dsc;          /* depth scale (goldstein_lib.f90:51), used by co when iconv=1 */
+    int32_t ieos;         /* 0: no thermobaricity; 1: ec(5)*t*z term */
+    int32_t iediff;       /* 0: uniform diff(2); 1 or 2: ediff1/diffmax profile */
+    int32_t ediffpow2i;   /* 0, 1, 2 or any other value for the general power */
+    int32_t iconv;        /* 0: co only; 1: coshuffle before co */
+    int32_t imld;         /* must be 0: the Kraus-Turner branch is not provided */
+    int32_t diso;         /* non-zero: isoneutral (Redi) branch on */
+    int32_t precision;    /* GB_GO_FP64 or GB_GO_FP32FLUX */
+    int32_t reserved;     /* must be 0 */
+} gb_go_params;
+
+/* Grid metrics (goldstein.f90:908-1076, 2057-2070).  Lower bounds in brackets. */
+typedef struct gb_go_grid {
+    const double  *rc, *rc2, *cv;        /* [0:maxj]   */
+    const double  *cv2, *dsv, *rdsv;     /* [1:maxj-1] */
+    const double  *ds, *rds;             /* [1:maxj]   */
+    const double  *dz, *dza, *rdz, *rdza, *zro, *dt;  /* [1:maxk] */
+    const double  *zw;                   /* [0:maxk]   */
+    const double  *ssmax;                /* [1:maxk-1], read when diso != 0 */
+    const double  *ediff1;               /* (1:maxi,1:maxj,1:maxk-1), read when iediff is 1 or 2 */
+    const double  *diffmax;              /* [1:maxk], read when iediff is 1 or 2 */
+    const int32_t *k1;                   /* (0:maxi+1, 0:maxj+1) */
+    double dphi, rdphi;
+} gb_go_grid;
+
+typedef struct gb_go_handle gb_go_handle;
+
+/* ---- single grid: drop-in for `CALL tstepo` (goldstein.f90:235) ------------- */
+
+/* Validate the configuration, copy grid/params to the device, allocate resident
+ * state.  `device` selects the CUDA device (-1 = current). */
+int  gb_go_create(const gb_go_dims *dims, const gb_go_params *params,
+                  const gb_go_grid *grid, int device, gb_go_handle **out);
+void gb_go_destroy(gb_go_handle *h);
+
+/* Use this CUDA stream (a cudaStream_t; NULL = the handle's own stream) for
+ * every later call on the handle. */
+int  gb_go_set_stream(gb_go_handle *h, void *cuda_stream);
+
+/* Upload ts, ts1 (full halo'd arrays, including the surface-forcing slot
+ * ts(:,:,:,maxk+1)) and rho.  Replaces the per-step copy-in at
+ * goldstein.f90:176-187; call it at coupling intervals only. */
+int  gb_go_upload_state(gb_go_handle *h, const double *ts, const double *ts1,
+                        const double *rho);
+
+/* Surface forcing slot ts(1:maxl, 0:maxi+1, 0:maxj+1, maxk+1) (one contiguous
+ * level of ts), written by step_goldstein at goldstein.f90:167-170. */
+int  gb_go_set_forcing(gb_go_handle *h, const double *ts_top);
+
+/* Velocities u(3, 0:maxi, 0:maxj, 1:maxk) from velc (goldstein.f90:3668-3678). */
+int  gb_go_set_velocity(gb_go_handle *h, const double *u);
+
+/* Convection diagnostics cost(maxi,maxj) (passed back in from BIOGEM at
+ * goldstein.f90:99) and icosd(maxi,maxj).  Either may be NULL. */
+int  gb_go_set_diag(gb_go_handle *h, const double *cost, const int32_t *icosd);
+
+/* Advance `nsteps` tracer timesteps on the device (tstepo repeated). */
+int  gb_go_tstepo(gb_go_handle *h, int32_t nsteps);
+
+/* Copy the state back (the copy-out at goldstein.f90:443-450), at coupling
+ * intervals.  Any pointer may be NULL to skip that array.  dmax and limps
+ * are the diagnostics of the last step (goldstein.f90:2459, 2598-2608). */
+int  gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *rho,
+                    double *cost, int32_t *icosd, double *dmax, int32_t *limps);
+
+/* Per-tracer inventory sum over wet cells of ts(l,i,j,k)*ds(j)*dz(k)
+ * (the weighting of the reference's conservation diagnostic,
+ * goldstein.f90:458-478), computed on the device in FP64 with compensated
+ * (Neumaier) summation.  `out` has maxl entries. */
+int  gb_go_inventory(gb_go_handle *h, double *out);
+
+/* Wait for all work queued on the handle's stream. */
+int  gb_go_sync(gb_go_handle *h);
+
+/* Text for an error code; the handle's last detailed message. */
+const char *gb_go_errstr(int code);
+const char *gb_go_last_error(const gb_go_handle *h);
+
+/* Number of CUDA kernels this library launched in this process (all handles). */
+uint64_t gb_go_kernel_launch_count(void);
+
+/* ---- ensembles: many independent grids advanced by one batched launch -------
+ * No counterpart in the reference (a single serial run).  Members may differ in
+ * every dimension and parameter; they are packed into one work list and stepped
+ * together by a persistent kernel.  Members can be added and removed between
+ * steps (continuous batching). */
+
+typedef struct gb_ens gb_ens;
+
+typedef struct gb_ens_tuning {
+    int32_t tile_i, tile_j;   /* columns per work item (0 = autotuned default) */
+    int32_t ctas_per_sm;      /* persistent CTAs per SM (0 = default) */
+    int32_t use_graph;        /* capture a multi-step launch in a CUDA graph */
+} gb_ens_tuning;
+
+int  gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out);
+void gb_ens_destroy(gb_ens *e);
+int  gb_ens_set_tuning(gb_ens *e, const gb_ens_tuning *t);
+int  gb_ens_set_stream(gb_ens *e, void *cuda_stream);
+
+/* Bytes of device memory one member of this shape needs. */
+size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params);
+
+/* Add a member: copies grid/params and the initial ts (full halo'd array,
+ * also used as ts1), u and forcing slot; returns its id in *member_id.
+ * GB_GO_ENOMEM when it does not fit in the budget. */
+int  gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params,
+                const gb_go_grid *grid, const double *ts, const double *u,
+                int32_t *member_id);
+int  gb_ens_remove(gb_ens *e, int32_t member_id);
+
+/* Advance every active member by `nsteps` steps. */
+int  gb_ens_step(gb_ens *e, int32_t nsteps);
+
+/* Advance only members whose remaining-step counter is positive, decrementing
+ * it; members reaching zero stop advancing.  Used by the serving loop. */
+int  gb_ens_set_remaining(gb_ens *e, int32_t member_id, int64_t steps);
+int  gb_ens_step_remaining(gb_ens *e, int32_t nsteps);
+int  gb_ens_remaining(gb_ens *e, int32_t member_id, int64_t *steps);
+
+int  gb_ens_download(gb_ens *e, int32_t member_id, double *ts, double *rho,
+                     double *cost);
+int  gb_ens_inventory(gb_ens *e, int32_t member_id, double *out);
+int  gb_ens_status(gb_ens *e, int32_t member_id, int32_t *status);
+int  gb_ens_sync(gb_ens *e);
+int  gb_ens_count(gb_ens *e, int32_t *active, size_t *bytes_in_use);
+const char *gb_ens_last_error(const gb_ens *e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB_GOLDSTEIN_H */
