@@ -1,0 +1,563 @@
+// C-ABI of the GB300 GOLDSTEIN tracer step (include/gb_goldstein.h): one grid,
+// device-resident state, drop-in for `CALL tstepo` (goldstein.f90:235).
+#include "gb_internal.h"
+#include "gb_fp32.h"
+#include "../../include/gb_goldstein.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace gbgo;
+
+static std::atomic<uint64_t> g_launches{0};
+
+namespace gbgo {
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}
+
+struct gb_go_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    Dims d{};
+    PhysParams p{};
+    int precision = GB_GO_FP64;
+    int tile_i = 4, tile_j = 4;
+    double *ts_buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    double *ts_static = nullptr, *ts1_static = nullptr, *top = nullptr, *rho = nullptr, *u = nullptr;
+    double *cost = nullptr;
+    int32_t *icosd = nullptr;
+    unsigned long long *diag = nullptr;  // two slots of {dmax bits, limps}
+    int slot = 0;
+    double *metrics = nullptr;
+    int32_t *k1 = nullptr;
+    double *ediff1 = nullptr;
+    double *stage = nullptr;
+    double *inv_part = nullptr;
+    int inv_blocks = 0;
+    Metrics m{};
+    std::vector<int32_t> k1_host;
+    bool state_ready = false, vel_ready = false;
+    long long steps_since_upload = 0;
+    std::string last_error;
+    Fp32Member f32{};   // FP32-flux path data
+};
+
+static const char *kErrText[] = {
+    "ok", "invalid argument", "unsupported option", "CUDA error", "out of memory",
+    "state or velocity not uploaded", "device-side error", "size beyond compiled-in limit",
+    "non-finite tracer value",
+};
+
+extern "C" const char *gb_go_errstr(int code)
+{
+    int c = -code;
+    if (c < 0 || c > 8) return "unknown error";
+    return kErrText[c];
+}
+
+extern "C" const char *gb_go_last_error(const gb_go_handle *h) { return h ? h->last_error.c_str() : ""; }
+
+extern "C" uint64_t gb_go_kernel_launch_count(void) { return g_launches.load(); }
+
+static int fail(gb_go_handle *h, int code, const std::string &msg)
+{
+    if (h) h->last_error = msg;
+    return code;
+}
+
+static int cuda_fail(gb_go_handle *h, cudaError_t e, const char *what)
+{
+    return fail(h, GB_GO_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(h, call)                                  \
+    do {                                                   \
+        cudaError_t _e = (call);                           \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, #call); \
+    } while (0)
+
+namespace gbgo {
+
+int validate_config(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid, std::string &msg)
+{
+    if (!dims || !params || !grid) { msg = "NULL dims/params/grid"; return GB_GO_EINVAL; }
+    if (dims->maxi < 2 || dims->maxj < 2 || dims->maxk < 2 || dims->maxl < 2) {
+        msg = "dimensions must be >= 2 (maxl >= 2: T and S are read by the equation of state)";
+        return GB_GO_EINVAL;
+    }
+    if (dims->maxk > GB_GO_MAX_K || dims->maxl > GB_GO_MAX_L) {
+        msg = "maxk > GB_GO_MAX_K or maxl > GB_GO_MAX_L";
+        return GB_GO_ERANGE;
+    }
+    if ((long long)dims->maxi * dims->maxj > (1LL << 28)) { msg = "grid too large"; return GB_GO_ERANGE; }
+    if (params->imld != 0) { msg = "imld=1 (Kraus-Turner mixed layer) is not provided"; return GB_GO_EUNSUPPORTED; }
+    if (params->ieos != 0 && params->ieos != 1) { msg = "ieos must be 0 or 1"; return GB_GO_EINVAL; }
+    if (params->iconv != 0 && params->iconv != 1) { msg = "iconv must be 0 or 1"; return GB_GO_EINVAL; }
+    if (params->iediff < 0) { msg = "iediff must be >= 0"; return GB_GO_EINVAL; }
+    if (params->precision != GB_GO_FP64 && params->precision != GB_GO_FP32FLUX) {
+        msg = "precision must be GB_GO_FP64 or GB_GO_FP32FLUX";
+        return GB_GO_EINVAL;
+    }
+    if (params->reserved != 0) { msg = "reserved must be 0"; return GB_GO_EINVAL; }
+    if (!(params->diff[0] != 0.0)) { msg = "diff(1) must be non-zero"; return GB_GO_EINVAL; }
+    const gb_go_grid *g = grid;
+    if (!g->k1 || !g->rc || !g->rc2 || !g->cv || !g->cv2 || !g->dsv || !g->rdsv || !g->ds || !g->rds || !g->dz ||
+        !g->dza || !g->rdz || !g->rdza || !g->zro || !g->dt || !g->zw) {
+        msg = "NULL grid metric";
+        return GB_GO_EINVAL;
+    }
+    if (params->diso && !g->ssmax) { msg = "diso needs ssmax"; return GB_GO_EINVAL; }
+    if (params->iediff > 0 && params->iediff < 3 && (!g->ediff1 || !g->diffmax)) {
+        msg = "iediff 1/2 needs ediff1 and diffmax";
+        return GB_GO_EINVAL;
+    }
+    const int NI = dims->maxi + 2, NJ = dims->maxj + 2;
+    for (int i = 0; i < NI; ++i) {
+        if (g->k1[i] <= dims->maxk || g->k1[i + (size_t)NI * (NJ - 1)] <= dims->maxk) {
+            msg = "k1 rows j=0 and j=maxj+1 must be land (k1 > maxk)";
+            return GB_GO_EINVAL;
+        }
+    }
+    for (int j = 0; j < NJ; ++j) {
+        const int32_t *row = g->k1 + (size_t)NI * j;
+        if (row[0] != row[dims->maxi] || row[NI - 1] != row[1]) {
+            msg = "k1 must be periodic in i: k1(0,j)=k1(maxi,j), k1(maxi+1,j)=k1(1,j)";
+            return GB_GO_EINVAL;
+        }
+        for (int i = 0; i < NI; ++i) {
+            if (row[i] < 1) { msg = "k1 must be >= 1"; return GB_GO_EINVAL; }
+        }
+    }
+    return GB_GO_OK;
+}
+
+// Fortran-indexed metric blob: 8 j-arrays of maxj+2 entries then 9 k-arrays of maxk+2.
+void build_metric_blob(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *g, std::vector<double> &blob)
+{
+    const int nj = dims->maxj + 2, nk = dims->maxk + 2, maxj = dims->maxj, maxk = dims->maxk;
+    blob.assign((size_t)8 * nj + (size_t)9 * nk, 0.0);
+    double *b = blob.data();
+    double *rc = b, *rc2 = b + nj, *cv = b + 2 * nj, *cv2 = b + 3 * nj, *dsv = b + 4 * nj, *rdsv = b + 5 * nj,
+           *ds = b + 6 * nj, *rds = b + 7 * nj;
+    double *kb = b + 8 * nj;
+    double *dz = kb, *dza = kb + nk, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk, *dt = kb + 5 * nk,
+           *zw = kb + 6 * nk, *ssmax = kb + 7 * nk, *diffmax = kb + 8 * nk;
+    for (int j = 0; j <= maxj; ++j) { rc[j] = g->rc[j]; rc2[j] = g->rc2[j]; cv[j] = g->cv[j]; }
+    for (int j = 1; j <= maxj - 1; ++j) { cv2[j] = g->cv2[j - 1]; dsv[j] = g->dsv[j - 1]; rdsv[j] = g->rdsv[j - 1]; }
+    for (int j = 1; j <= maxj; ++j) { ds[j] = g->ds[j - 1]; rds[j] = g->rds[j - 1]; }
+    for (int k = 1; k <= maxk; ++k) {
+        dz[k] = g->dz[k - 1]; dza[k] = g->dza[k - 1]; rdz[k] = g->rdz[k - 1]; rdza[k] = g->rdza[k - 1];
+        zro[k] = g->zro[k - 1]; dt[k] = g->dt[k - 1];
+    }
+    for (int k = 0; k <= maxk; ++k) zw[k] = g->zw[k];
+    if (params->diso && g->ssmax)
+        for (int k = 1; k <= maxk - 1; ++k) ssmax[k] = g->ssmax[k - 1];
+    if (params->iediff > 0 && params->iediff < 3 && g->diffmax)
+        for (int k = 1; k <= maxk; ++k) diffmax[k] = g->diffmax[k - 1];
+}
+
+Metrics metrics_from_blob(const double *b, const int32_t *k1, const double *ediff1, int maxj, int maxk)
+{
+    const int nj = maxj + 2, nk = maxk + 2;
+    Metrics m{};
+    m.rc = b; m.rc2 = b + nj; m.cv = b + 2 * nj; m.cv2 = b + 3 * nj; m.dsv = b + 4 * nj; m.rdsv = b + 5 * nj;
+    m.ds = b + 6 * nj; m.rds = b + 7 * nj;
+    const double *kb = b + 8 * nj;
+    m.dz = kb; m.dza = kb + nk; m.rdz = kb + 2 * nk; m.rdza = kb + 3 * nk; m.zro = kb + 4 * nk; m.dt = kb + 5 * nk;
+    m.zw = kb + 6 * nk; m.ssmax = kb + 7 * nk; m.diffmax = kb + 8 * nk;
+    m.ediff1 = ediff1;
+    m.k1 = k1;
+    return m;
+}
+
+PhysParams phys_from(const gb_go_params *pp, const gb_go_grid *g)
+{
+    PhysParams p{};
+    p.diff1 = pp->diff[0];
+    p.diff2 = pp->diff[1];
+    for (int n = 0; n < 5; ++n) p.ec[n] = pp->ec[n];
+    p.ediff0 = pp->ediff0;
+    p.ediffpow2 = pp->ediffpow2;
+    p.dsc = pp->dsc;
+    p.dphi = g->dphi;
+    p.rdphi = g->rdphi;
+    p.ieos = pp->ieos;
+    p.iediff = (pp->iediff > 0 && pp->iediff < 3) ? pp->iediff : 0;
+    p.ediffpow2i = pp->ediffpow2i;
+    p.iconv = pp->iconv;
+    p.diso = pp->diso ? 1 : 0;
+    return p;
+}
+
+}  // namespace gbgo
+
+// ---------------------------------------------------------------------------
+// auxiliary kernels
+
+// out = stat; wet interior cells (and, for ts1, wet halo columns) from cur.
+__global__ void k_merge_download(double *out, const double *stat, const double *cur, Dims d, const int32_t *k1,
+                                 int with_halo, int use_cur)
+{
+    const size_t ncell = (size_t)d.NI * d.NJ * (d.maxk + 2);
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % d.NI);
+        const int j = (int)((c / d.NI) % d.NJ);
+        const int k = (int)(c / ((size_t)d.NI * d.NJ));
+        bool take = false;
+        if (use_cur && k >= 1 && k <= d.maxk && j >= 1 && j <= d.maxj) {
+            const int kk = k1[i + d.NI * j];
+            if (i >= 1 && i <= d.maxi) take = k >= kk;
+            else if (with_halo) take = k >= kk;
+        }
+        const double *src = take ? cur : stat;
+        for (int l = 0; l < d.L; ++l) out[c * d.L + l] = src[c * d.L + l];
+    }
+}
+
+// Per-tracer Neumaier partial sums of ts*ds(j)*dz(k) over wet interior cells.
+__global__ void k_inventory_partial(const double *ts, Dims d, Metrics m, double *part)
+{
+    const int l = blockIdx.y;
+    const size_t ncol = (size_t)d.maxi * d.maxj;
+    const size_t ncell = ncol * d.maxk;
+    double s = 0.0, comp = 0.0;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % d.maxi) + 1;
+        const int j = (int)((c / d.maxi) % d.maxj) + 1;
+        const int k = (int)(c / ncol) + 1;
+        if (k < m.k1[i + d.NI * j]) continue;
+        const double x = __dmul_rn(__dmul_rn(ts[ts_index(d, l, i, j, k)], m.ds[j]), m.dz[k]);
+        const double t = __dadd_rn(s, x);
+        if (fabs(s) >= fabs(x)) comp = __dadd_rn(comp, __dadd_rn(__dadd_rn(s, -t), x));
+        else comp = __dadd_rn(comp, __dadd_rn(__dadd_rn(x, -t), s));
+        s = t;
+    }
+    __shared__ double ss[256], sc[256];
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = comp;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0.0, Cc = 0.0;
+        for (int n = 0; n < blockDim.x; ++n) {
+            const double x = ss[n];
+            const double t = __dadd_rn(S, x);
+            if (fabs(S) >= fabs(x)) Cc = __dadd_rn(Cc, __dadd_rn(__dadd_rn(S, -t), x));
+            else Cc = __dadd_rn(Cc, __dadd_rn(__dadd_rn(x, -t), S));
+            S = t;
+            Cc = __dadd_rn(Cc, sc[n]);
+        }
+        part[2 * ((size_t)l * gridDim.x + blockIdx.x)] = S;
+        part[2 * ((size_t)l * gridDim.x + blockIdx.x) + 1] = Cc;
+    }
+}
+
+__global__ void k_inventory_final(const double *part, int nblk, int L, double *out)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= L) return;
+    double S = 0.0, Cc = 0.0;
+    for (int n = 0; n < nblk; ++n) {
+        const double x = part[2 * ((size_t)l * nblk + n)];
+        const double t = __dadd_rn(S, x);
+        if (fabs(S) >= fabs(x)) Cc = __dadd_rn(Cc, __dadd_rn(__dadd_rn(S, -t), x));
+        else Cc = __dadd_rn(Cc, __dadd_rn(__dadd_rn(x, -t), S));
+        S = t;
+        Cc = __dadd_rn(Cc, part[2 * ((size_t)l * nblk + n) + 1]);
+    }
+    out[l] = __dadd_rn(S, Cc);
+}
+
+// ---------------------------------------------------------------------------
+
+static void free_handle(gb_go_handle *h)
+{
+    if (!h) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->ts_buf[0]); cudaFree(h->ts_buf[1]);
+    cudaFree(h->ts_static); cudaFree(h->ts1_static); cudaFree(h->top); cudaFree(h->rho); cudaFree(h->u);
+    cudaFree(h->cost); cudaFree(h->icosd); cudaFree(h->diag); cudaFree(h->metrics); cudaFree(h->k1);
+    cudaFree(h->ediff1); cudaFree(h->stage); cudaFree(h->inv_part);
+    fp32_member_free(&h->f32);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete h;
+}
+
+extern "C" int gb_go_create(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid, int device,
+                            gb_go_handle **out)
+{
+    if (!out) return GB_GO_EINVAL;
+    *out = nullptr;
+    std::string msg;
+    int rc = validate_config(dims, params, grid, msg);
+    if (rc) {
+        fprintf(stderr, "gb_go_create: %s\n", msg.c_str());
+        return rc;
+    }
+    gb_go_handle *h = new (std::nothrow) gb_go_handle();
+    if (!h) return GB_GO_ENOMEM;
+    if (device < 0) {
+        if (cudaGetDevice(&h->device) != cudaSuccess) { delete h; return GB_GO_ECUDA; }
+    } else {
+        h->device = device;
+    }
+    if (cudaSetDevice(h->device) != cudaSuccess) { delete h; return GB_GO_ECUDA; }
+    h->d.maxi = dims->maxi; h->d.maxj = dims->maxj; h->d.maxk = dims->maxk; h->d.L = dims->maxl;
+    h->d.NI = dims->maxi + 2; h->d.NJ = dims->maxj + 2;
+    h->p = phys_from(params, grid);
+    h->precision = params->precision;
+    step_fp64_tile(dims->maxk, &h->tile_i, &h->tile_j);
+
+    const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
+    const size_t ntop = (size_t)h->d.L * h->d.NI * h->d.NJ;
+    const size_t nrho = (size_t)h->d.NI * h->d.NJ * (h->d.maxk + 1);
+    const size_t nu = (size_t)3 * (h->d.maxi + 1) * (h->d.maxj + 1) * h->d.maxk;
+    const size_t ncol = (size_t)h->d.maxi * h->d.maxj;
+    std::vector<double> blob;
+    build_metric_blob(dims, params, grid, blob);
+    h->inv_blocks = 64;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        h->stream = h->own_stream;
+        e = cudaMalloc(&h->ts_buf[0], nts * sizeof(double));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&h->ts_buf[1], nts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->ts_static, nts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->ts1_static, nts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->stage, nts * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->top, ntop * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->rho, nrho * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->u, nu * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->cost, ncol * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->icosd, ncol * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&h->diag, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&h->metrics, blob.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->k1, (size_t)h->d.NI * h->d.NJ * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&h->inv_part, (size_t)2 * h->inv_blocks * h->d.L * sizeof(double));
+    const bool need_ediff = params->iediff > 0 && params->iediff < 3;
+    const size_t ned = (size_t)h->d.maxi * h->d.maxj * (h->d.maxk - 1);
+    if (e == cudaSuccess && need_ediff) e = cudaMalloc(&h->ediff1, ned * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->metrics, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->k1, grid->k1, (size_t)h->d.NI * h->d.NJ * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && need_ediff) e = cudaMemcpyAsync(h->ediff1, grid->ediff1, ned * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->diag, 0, 4 * sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->cost, 0, ncol * sizeof(double), h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->icosd, 0, ncol * sizeof(int32_t), h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->u, 0, nu * sizeof(double), h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "gb_go_create: %s\n", cudaGetErrorString(e));
+        int code = (e == cudaErrorMemoryAllocation) ? GB_GO_ENOMEM : GB_GO_ECUDA;
+        free_handle(h);
+        return code;
+    }
+    h->k1_host.assign(grid->k1, grid->k1 + (size_t)h->d.NI * h->d.NJ);
+    h->m = metrics_from_blob(h->metrics, h->k1, h->ediff1, h->d.maxj, h->d.maxk);
+    if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_init(&h->f32, h->d, h->p, h->m, blob, h->k1_host.data(), h->stream, msg);
+        if (r) {
+            fprintf(stderr, "gb_go_create: %s\n", msg.c_str());
+            free_handle(h);
+            return r;
+        }
+    }
+    *out = h;
+    return GB_GO_OK;
+}
+
+extern "C" void gb_go_destroy(gb_go_handle *h) { free_handle(h); }
+
+extern "C" int gb_go_set_stream(gb_go_handle *h, void *cuda_stream)
+{
+    if (!h) return GB_GO_EINVAL;
+    h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const double *ts1, const double *rho)
+{
+    if (!h || !ts || !ts1 || !rho) return fail(h, GB_GO_EINVAL, "upload_state: NULL array");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
+    const size_t ntop = (size_t)h->d.L * h->d.NI * h->d.NJ;
+    const size_t nrho = (size_t)h->d.NI * h->d.NJ * (h->d.maxk + 1);
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_static, ts, nts * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts1_static, ts1, nts * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_buf[0], h->ts1_static, nts * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_buf[1], h->ts_static, nts * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->top, h->ts_static + ntop * (h->d.maxk + 1), ntop * sizeof(double),
+                                cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->rho, rho, nrho * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->cur = 0;
+    h->state_ready = true;
+    h->steps_since_upload = 0;
+    if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_upload(&h->f32, h->ts_buf[0], h->ts_static, h->stream);
+        if (r) return fail(h, r, "fp32 upload failed");
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_set_forcing(gb_go_handle *h, const double *ts_top)
+{
+    if (!h || !ts_top) return fail(h, GB_GO_EINVAL, "set_forcing: NULL array");
+    if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "set_forcing before upload_state");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t ntop = (size_t)h->d.L * h->d.NI * h->d.NJ;
+    CUDA_TRY(h, cudaMemcpyAsync(h->top, ts_top, ntop * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_static + ntop * (h->d.maxk + 1), h->top, ntop * sizeof(double),
+                                cudaMemcpyDeviceToDevice, h->stream));
+    if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_set_top(&h->f32, h->top, h->stream);
+        if (r) return fail(h, r, "fp32 set_forcing failed");
+    }
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_set_velocity(gb_go_handle *h, const double *u)
+{
+    if (!h || !u) return fail(h, GB_GO_EINVAL, "set_velocity: NULL array");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t nu = (size_t)3 * (h->d.maxi + 1) * (h->d.maxj + 1) * h->d.maxk;
+    CUDA_TRY(h, cudaMemcpyAsync(h->u, u, nu * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_set_velocity(&h->f32, h->u, h->stream);
+        if (r) return fail(h, r, "fp32 set_velocity failed");
+    }
+    h->vel_ready = true;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_set_diag(gb_go_handle *h, const double *cost, const int32_t *icosd)
+{
+    if (!h) return GB_GO_EINVAL;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t ncol = (size_t)h->d.maxi * h->d.maxj;
+    if (cost) CUDA_TRY(h, cudaMemcpyAsync(h->cost, cost, ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (icosd) CUDA_TRY(h, cudaMemcpyAsync(h->icosd, icosd, ncol * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_tstepo(gb_go_handle *h, int32_t nsteps)
+{
+    if (!h || nsteps < 0) return fail(h, GB_GO_EINVAL, "tstepo: bad arguments");
+    if (!h->state_ready || !h->vel_ready) return fail(h, GB_GO_ENOTREADY, "tstepo before upload_state/set_velocity");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_step(&h->f32, h->ts_buf, &h->cur, h->rho, h->ts_static, h->cost, h->icosd,
+                                 h->diag, &h->slot, nsteps, h->stream);
+        if (r) return fail(h, r, "fp32 step launch failed");
+        h->steps_since_upload += nsteps;
+        return GB_GO_OK;
+    }
+    StepArgs a{};
+    a.d = h->d;
+    a.p = h->p;
+    a.m = h->m;
+    a.ts_static = h->ts_static;
+    a.top = h->top;
+    a.rho = h->rho;
+    a.u = h->u;
+    a.cost = h->cost;
+    a.icosd = h->icosd;
+    a.tile_i = h->tile_i;
+    a.tile_j = h->tile_j;
+    a.tiles_i = (h->d.maxi + h->tile_i - 1) / h->tile_i;
+    for (int s = 0; s < nsteps; ++s) {
+        a.ts1 = h->ts_buf[h->cur];
+        a.ts = h->ts_buf[1 - h->cur];
+        a.diag = h->diag + 2 * h->slot;
+        a.diag_next = h->diag + 2 * (1 - h->slot);
+        if (launch_step_fp64(a, h->stream)) return cuda_fail(h, cudaGetLastError(), "step_fp64 launch");
+        count_launches(1);
+        h->cur = 1 - h->cur;
+        h->slot = 1 - h->slot;
+        ++h->steps_since_upload;
+    }
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *rho, double *cost, int32_t *icosd,
+                              double *dmax, int32_t *limps)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "download before upload_state");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
+    const size_t nrho = (size_t)h->d.NI * h->d.NJ * (h->d.maxk + 1);
+    const size_t ncol = (size_t)h->d.maxi * h->d.maxj;
+    const int use_cur = h->steps_since_upload > 0 ? 1 : 0;
+    const double *curbuf = h->ts_buf[h->cur];
+    if (h->precision == GB_GO_FP32FLUX && use_cur) {
+        int r = fp32_member_export(&h->f32, h->ts_buf[h->cur], h->rho, h->ts_static, h->stream);
+        if (r) return fail(h, r, "fp32 export failed");
+    }
+    const size_t ncell = (size_t)h->d.NI * h->d.NJ * (h->d.maxk + 2);
+    const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 4096);
+    if (ts) {
+        k_merge_download<<<blocks, 256, 0, h->stream>>>(h->stage, h->ts_static, curbuf, h->d, h->k1, 0, use_cur);
+        count_launches(1);
+        CUDA_TRY(h, cudaGetLastError());
+        CUDA_TRY(h, cudaMemcpyAsync(ts, h->stage, nts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    if (ts1) {
+        k_merge_download<<<blocks, 256, 0, h->stream>>>(h->stage, h->ts1_static, curbuf, h->d, h->k1, 1, use_cur);
+        count_launches(1);
+        CUDA_TRY(h, cudaGetLastError());
+        CUDA_TRY(h, cudaMemcpyAsync(ts1, h->stage, nts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (rho) CUDA_TRY(h, cudaMemcpyAsync(rho, h->rho, nrho * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (cost) CUDA_TRY(h, cudaMemcpyAsync(cost, h->cost, ncol * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (icosd) CUDA_TRY(h, cudaMemcpyAsync(icosd, h->icosd, ncol * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    unsigned long long dg[2] = {0, 0};
+    if ((dmax || limps) && h->steps_since_upload > 0)
+        CUDA_TRY(h, cudaMemcpyAsync(dg, h->diag + 2 * (1 - h->slot), sizeof(dg), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (dmax) {
+        double v;
+        std::memcpy(&v, &dg[0], sizeof(v));
+        *dmax = v;
+    }
+    if (limps) *limps = h->p.diso ? (int32_t)dg[1] : 0;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_inventory(gb_go_handle *h, double *out)
+{
+    if (!h || !out) return GB_GO_EINVAL;
+    if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "inventory before upload_state");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const double *src = h->ts_buf[h->cur];
+    if (h->steps_since_upload == 0) src = h->ts_static;
+    dim3 grid(h->inv_blocks, h->d.L);
+    k_inventory_partial<<<grid, 256, 0, h->stream>>>(src, h->d, h->m, h->inv_part);
+    k_inventory_final<<<(h->d.L + 63) / 64, 64, 0, h->stream>>>(h->inv_part, h->inv_blocks, h->d.L, h->stage);
+    count_launches(2);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->stage, h->d.L * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_sync(gb_go_handle *h)
+{
+    if (!h) return GB_GO_EINVAL;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}

@@ -1,0 +1,83 @@
+// Internal definitions shared by the GOLDSTEIN GB300 kernels and the C-ABI.
+//
+// Device layout (one grid):
+//   state buffers  ts[2]      (maxl, 0:maxi+1, 0:maxj+1, 0:maxk+1) FP64, the
+//                             Fortran layout of ts/ts1, ping-ponged: a step reads
+//                             buffer `cur` (the reference's ts1) and writes the other
+//                             one (the reference's ts), so the reference's closing
+//                             ts1 = ts copy (goldstein.f90:2423-2431) disappears.
+//   ts_static/ts1_static      the uploaded ts/ts1: land cells, halo rows, level 0 and
+//                             the forcing level keep their uploaded values exactly as
+//                             the reference leaves them untouched.
+//   top                       forcing level ts(:, :, :, maxk+1)
+//   rho                       (0:maxi+1, 0:maxj+1, 0:maxk)
+//   u                         (3, 0:maxi, 0:maxj, 1:maxk)
+//   k1                        (0:maxi+1, 0:maxj+1) int32
+//   metrics                   one blob; j-arrays hold maxj+2 entries and k-arrays maxk+2
+//                             entries, both indexed by the Fortran index.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace gbgo {
+
+constexpr int kMaxK = 64;
+
+// Fortran-indexed metric pointers (device).
+struct Metrics {
+    const double *rc, *rc2, *cv, *cv2, *dsv, *rdsv, *ds, *rds;      // [0 .. maxj+1]
+    const double *dz, *dza, *rdz, *rdza, *zro, *dt, *zw, *ssmax, *diffmax;  // [0 .. maxk+1]
+    const double *ediff1;                                           // (maxi, maxj, maxk-1)
+    const int32_t *k1;                                              // (maxi+2, maxj+2)
+};
+
+struct Dims {
+    int maxi, maxj, maxk, L;
+    int NI, NJ;          // maxi+2, maxj+2
+};
+
+struct PhysParams {
+    double diff1, diff2;
+    double ec[5];
+    double ediff0, ediffpow2, dsc;
+    double dphi, rdphi;
+    int ieos, iediff, ediffpow2i, iconv, diso;
+};
+
+// Arguments of one FP64 step launch.
+struct StepArgs {
+    Dims d;
+    PhysParams p;
+    Metrics m;
+    const double *ts1;        // read buffer (old state)
+    double *ts;               // write buffer (new state)
+    const double *ts_static;  // uploaded ts: land / level-0 values
+    const double *top;        // forcing level (L, NI, NJ)
+    double *rho;
+    const double *u;
+    double *cost;
+    int32_t *icosd;
+    unsigned long long *diag;       // [0] dmax bits, [1] limps  (this step)
+    unsigned long long *diag_next;  // zeroed by block 0 for the next step
+    int tile_i, tile_j, tiles_i;
+};
+
+__host__ __device__ inline size_t ts_index(const Dims &d, int l, int i, int j, int k)
+{
+    return (size_t)l + (size_t)d.L * ((size_t)i + (size_t)d.NI * ((size_t)j + (size_t)d.NJ * (size_t)k));
+}
+__host__ __device__ inline size_t u_index(const Dims &d, int c, int i, int j, int k)
+{
+    return (size_t)c + 3 * ((size_t)i + (size_t)(d.maxi + 1) * ((size_t)j + (size_t)(d.maxj + 1) * (size_t)(k - 1)));
+}
+__host__ __device__ inline size_t rho_index(const Dims &d, int i, int j, int k)
+{
+    return (size_t)i + (size_t)d.NI * ((size_t)j + (size_t)d.NJ * (size_t)k);
+}
+
+// Launchers (tstep_fp64.cu)
+int launch_step_fp64(const StepArgs &a, void *stream);
+void step_fp64_tile(int maxk, int *tile_i, int *tile_j);
+
+}  // namespace gbgo

@@ -1,0 +1,201 @@
+"""Host-side mirror of the reference's tracer-step interface over the C-ABI.
+
+The reference calls ``CALL tstepo`` (src/goldstein/goldstein.f90:235) on SAVE'd
+module arrays; :class:`Goldstein` holds the same arrays (``ts``, ``ts1``,
+``rho``, ``u``, ``cost``, ``icosd`` in Fortran layout) and forwards them to
+libgb_goldstein.so, where the state stays resident on the GPU between
+``tstepo()`` calls and is copied back only by :meth:`Goldstein.download` (the
+coupling-interval copy of goldstein.f90:443-450).
+
+There is no CPU fallback: importing works without a GPU, but creating a
+:class:`Goldstein` requires the CUDA library and a device, and raises otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import abi
+from .abi import GbDims, GbEnsTuning, GbGrid, GbParams, GridRefs, dptr, iptr
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgb_goldstein.so")
+
+# every exported entry point of include/gb_goldstein.h
+EXPORTED = [
+    "gb_go_create", "gb_go_destroy", "gb_go_set_stream", "gb_go_upload_state", "gb_go_set_forcing",
+    "gb_go_set_velocity", "gb_go_set_diag", "gb_go_tstepo", "gb_go_download", "gb_go_inventory",
+    "gb_go_sync", "gb_go_errstr", "gb_go_last_error", "gb_go_kernel_launch_count",
+    "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
+    "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
+    "gb_ens_remaining", "gb_ens_download", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
+    "gb_ens_count", "gb_ens_last_error",
+]
+
+_lib = None
+
+
+class GoldsteinError(RuntimeError):
+    def __init__(self, code: int, what: str, detail: str = ""):
+        self.code = code
+        name = abi.ERRNAMES.get(code, str(code))
+        super().__init__(f"{what} failed: {name} ({code}) {detail}".rstrip())
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libgb_goldstein.so (built by cgenie_gb300.build).  Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} (run `python -m cgenie_gb300.build`)")
+    L = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    dp = P(C.c_double)
+    ip = P(C.c_int32)
+    L.gb_go_create.argtypes = [P(GbDims), P(GbParams), P(GbGrid), C.c_int, P(vp)]
+    L.gb_go_destroy.argtypes = [vp]
+    L.gb_go_destroy.restype = None
+    L.gb_go_set_stream.argtypes = [vp, vp]
+    L.gb_go_upload_state.argtypes = [vp, dp, dp, dp]
+    L.gb_go_set_forcing.argtypes = [vp, dp]
+    L.gb_go_set_velocity.argtypes = [vp, dp]
+    L.gb_go_set_diag.argtypes = [vp, dp, ip]
+    L.gb_go_tstepo.argtypes = [vp, C.c_int32]
+    L.gb_go_download.argtypes = [vp, dp, dp, dp, dp, ip, dp, ip]
+    L.gb_go_inventory.argtypes = [vp, dp]
+    L.gb_go_sync.argtypes = [vp]
+    L.gb_go_errstr.argtypes = [C.c_int]
+    L.gb_go_errstr.restype = C.c_char_p
+    L.gb_go_last_error.argtypes = [vp]
+    L.gb_go_last_error.restype = C.c_char_p
+    L.gb_go_kernel_launch_count.argtypes = []
+    L.gb_go_kernel_launch_count.restype = C.c_uint64
+    L.gb_ens_create.argtypes = [C.c_int, C.c_size_t, P(vp)]
+    L.gb_ens_destroy.argtypes = [vp]
+    L.gb_ens_destroy.restype = None
+    L.gb_ens_set_tuning.argtypes = [vp, P(GbEnsTuning)]
+    L.gb_ens_set_stream.argtypes = [vp, vp]
+    L.gb_ens_member_bytes.argtypes = [P(GbDims), P(GbParams)]
+    L.gb_ens_member_bytes.restype = C.c_size_t
+    L.gb_ens_add.argtypes = [vp, P(GbDims), P(GbParams), P(GbGrid), dp, dp, ip]
+    L.gb_ens_remove.argtypes = [vp, C.c_int32]
+    L.gb_ens_step.argtypes = [vp, C.c_int32]
+    L.gb_ens_set_remaining.argtypes = [vp, C.c_int32, C.c_int64]
+    L.gb_ens_step_remaining.argtypes = [vp, C.c_int32]
+    L.gb_ens_remaining.argtypes = [vp, C.c_int32, P(C.c_int64)]
+    L.gb_ens_download.argtypes = [vp, C.c_int32, dp, dp, dp]
+    L.gb_ens_inventory.argtypes = [vp, C.c_int32, dp]
+    L.gb_ens_status.argtypes = [vp, C.c_int32, ip]
+    L.gb_ens_sync.argtypes = [vp]
+    L.gb_ens_count.argtypes = [vp, ip, P(C.c_size_t)]
+    L.gb_ens_last_error.argtypes = [vp]
+    L.gb_ens_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def kernel_launch_count() -> int:
+    return int(load_library().gb_go_kernel_launch_count())
+
+
+class Goldstein:
+    """One GOLDSTEIN grid with device-resident tracer state.
+
+    Mirrors the reference's call sequence in step_goldstein
+    (goldstein.f90:167-187, 235, 443-450): set the forcing slot and the
+    velocities, call :meth:`tstepo`, and copy back at coupling intervals.
+    """
+
+    def __init__(self, member, *, precision: int = abi.GB_GO_FP64, device: int = -1,
+                 diso=None, ieos=None, iconv=None, iediff=None, stream: Optional[int] = None):
+        self.lib = load_library()
+        self.m = member
+        self.refs = GridRefs(member, diso=diso, ieos=ieos, iconv=iconv, iediff=iediff, precision=precision)
+        h = C.c_void_p()
+        rc = self.lib.gb_go_create(C.byref(self.refs.dims), C.byref(self.refs.params), C.byref(self.refs.grid),
+                                   int(device), C.byref(h))
+        if rc != 0:
+            raise GoldsteinError(rc, "gb_go_create")
+        self.h = h
+        if stream is not None:
+            self._check(self.lib.gb_go_set_stream(self.h, C.c_void_p(stream)), "gb_go_set_stream")
+
+    # -- plumbing
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            detail = self.lib.gb_go_last_error(self.h).decode() if self.h else ""
+            raise GoldsteinError(rc, what, detail)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_go_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream: Optional[int]):
+        self._check(self.lib.gb_go_set_stream(self.h, C.c_void_p(stream or 0)), "gb_go_set_stream")
+
+    # -- the reference's data movement
+    def upload_state(self, ts=None, ts1=None, rho=None):
+        m = self.m
+        ts = np.ascontiguousarray(m.ts if ts is None else ts, dtype=np.float64)
+        ts1 = np.ascontiguousarray(m.ts1 if ts1 is None else ts1, dtype=np.float64)
+        rho = np.ascontiguousarray(m.rho if rho is None else rho, dtype=np.float64)
+        self._check(self.lib.gb_go_upload_state(self.h, dptr(ts), dptr(ts1), dptr(rho)), "gb_go_upload_state")
+
+    def set_forcing(self, top):
+        top = np.ascontiguousarray(top, dtype=np.float64)
+        self._check(self.lib.gb_go_set_forcing(self.h, dptr(top)), "gb_go_set_forcing")
+
+    def set_velocity(self, u=None):
+        u = np.ascontiguousarray(self.m.u if u is None else u, dtype=np.float64)
+        self._check(self.lib.gb_go_set_velocity(self.h, dptr(u)), "gb_go_set_velocity")
+
+    def set_diag(self, cost=None, icosd=None):
+        c = None if cost is None else np.ascontiguousarray(cost, dtype=np.float64)
+        i = None if icosd is None else np.ascontiguousarray(icosd, dtype=np.int32)
+        self._check(self.lib.gb_go_set_diag(self.h, dptr(c), iptr(i)), "gb_go_set_diag")
+
+    def tstepo(self, nsteps: int = 1):
+        self._check(self.lib.gb_go_tstepo(self.h, int(nsteps)), "gb_go_tstepo")
+
+    def sync(self):
+        self._check(self.lib.gb_go_sync(self.h), "gb_go_sync")
+
+    def download(self):
+        """Return dict(ts, ts1, rho, cost, icosd, dmax, limps) in Fortran layout."""
+        m = self.m
+        ts = np.empty_like(m.ts)
+        ts1 = np.empty_like(m.ts1)
+        rho = np.empty_like(m.rho)
+        cost = np.empty_like(m.cost)
+        icosd = np.empty_like(m.icosd)
+        dmax = C.c_double()
+        limps = C.c_int32()
+        self._check(self.lib.gb_go_download(self.h, dptr(ts), dptr(ts1), dptr(rho), dptr(cost), iptr(icosd),
+                                            C.byref(dmax), C.byref(limps)), "gb_go_download")
+        return dict(ts=ts, ts1=ts1, rho=rho, cost=cost, icosd=icosd, dmax=dmax.value, limps=limps.value)
+
+    def inventory(self) -> np.ndarray:
+        out = np.zeros(self.m.maxl)
+        self._check(self.lib.gb_go_inventory(self.h, dptr(out)), "gb_go_inventory")
+        return out
+
+
+def new_member_run(member, **kw) -> Goldstein:
+    """Create a handle, upload the member's state and velocities."""
+    g = Goldstein(member, **kw)
+    g.upload_state()
+    g.set_velocity()
+    g.set_diag(member.cost, member.icosd)
+    return g

@@ -1,0 +1,52 @@
+"""CPU checks of the boundary: the library loads and exports every symbol the
+header declares; ctypes struct layouts match the header; host-side validation."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from cgenie_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "gb_goldstein.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_(?:go|ens)_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_all_header_symbols():
+    from cgenie_gb300 import build, goldstein
+    path = build.build()
+    lib = C.CDLL(path)
+    names = header_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(goldstein.EXPORTED) == names
+
+
+def test_struct_layouts():
+    assert C.sizeof(abi.GbDims) == 16
+    # 2+5 doubles, 3 doubles, 8 int32
+    assert C.sizeof(abi.GbParams) == (7 + 3) * 8 + 8 * 4
+    assert C.sizeof(abi.GbGrid) == 19 * 8 + 2 * 8
+    assert C.sizeof(abi.GbEnsTuning) == 16
+
+
+def test_errstr_without_gpu():
+    from cgenie_gb300 import build, goldstein
+    build.build()
+    lib = goldstein.load_library()
+    assert lib.gb_go_errstr(0) == b"ok"
+    assert lib.gb_go_errstr(abi.GB_GO_EINVAL) == b"invalid argument"
+    assert lib.gb_go_errstr(-99) == b"unknown error"
+
+
+def test_oracle_header_cites_reference():
+    src = open(os.path.join(ROOT, "oracle", "goldstein_oracle.c")).read()
+    assert "ORACLE -- test infrastructure only" in src
+    assert "goldstein.f90:2436-2642" in src
+    assert "parity unpinned" in src
