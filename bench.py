@@ -196,7 +196,10 @@ def main():
 
     w = WORKLOADS[args.workload]
     m = grid.make_member(getattr(grid, w["factory"])())
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the legacy default stream's handle is 0, which the C-ABI
+    # reads as "the handle's own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     g = new_member_run(m, device=local, stream=stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 

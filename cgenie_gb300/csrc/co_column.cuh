@@ -1,0 +1,139 @@
+// Convective adjustment of one water column in IEEE double with explicit
+// round-to-nearest intrinsics (no contraction whatever the compile flags), so
+// the FP32-flux form applies the reference's exact co/coshuffle arithmetic to
+// its FP64 state.
+//   co         src/goldstein/goldstein.f90:2657-2777
+//   coshuffle  src/goldstein/goldstein.f90:2781-2841
+//   eos        src/goldstein/goldstein.f90:3048-3061
+//
+// `Col` provides:  double T(int l, int lev) const;  void setT(int l, int lev, double v);
+//                  double &R(int lev);   (rho of this column, levels 0..maxk)
+#pragma once
+
+#include "gb_internal.h"
+
+namespace gbgo {
+
+struct EosCoef {
+    double ec[5];
+    int ieos;
+};
+
+__device__ __forceinline__ double eos_rn(const EosCoef &c, double t, double s, double z)
+{
+    const double tt = __dmul_rn(t, t);
+    double r = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c.ec[0], t), __dmul_rn(c.ec[1], s)), __dmul_rn(c.ec[2], tt)),
+                         __dmul_rn(c.ec[3], __dmul_rn(tt, t)));
+    if (c.ieos != 0) r = __dadd_rn(r, __dmul_rn(__dmul_rn(c.ec[4], t), z));
+    return r;
+}
+
+// coshuffle for one wet column; returns icosd of the column
+template <class Col>
+__device__ int coshuffle_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const double *dz, const double *rdz,
+                            const double *zw)
+{
+    int icos = 0;
+    int k0 = 0, ipass = 0;
+    while (k0 < maxk && ipass < maxk) {
+        ipass = ipass + 1;
+        int k = maxk - 1;
+        if (ec.ieos != 0) {
+            col.R(maxk) = eos_rn(ec, col.T(0, maxk), col.T(1, maxk), zw[k]);
+            col.R(k) = eos_rn(ec, col.T(0, k), col.T(1, k), zw[k]);
+        }
+        while ((col.R(maxk) > col.R(k)) && (k >= k1)) {
+            k = k - 1;
+            if (ec.ieos != 0) {
+                col.R(maxk) = eos_rn(ec, col.T(0, maxk), col.T(1, maxk), zw[k]);
+                col.R(k) = eos_rn(ec, col.T(0, k), col.T(1, k), zw[k]);
+            }
+        }
+        k0 = k + 1;
+        if (k0 < maxk) {
+            const double dzt = dz[maxk];
+            for (int l = 0; l < L; ++l) {
+                const double tv_temp = col.T(l, maxk);
+                for (int kk = maxk; kk >= k0 + 1; --kk) {
+                    const double v = __dmul_rn(
+                        __dadd_rn(__dmul_rn(__dadd_rn(dz[kk], -dzt), col.T(l, kk)), __dmul_rn(dzt, col.T(l, kk - 1))),
+                        rdz[kk]);
+                    col.setT(l, kk, v);
+                }
+                const double v0 = __dmul_rn(
+                    __dadd_rn(__dmul_rn(__dadd_rn(dz[k0], -dzt), col.T(l, k0)), __dmul_rn(dzt, tv_temp)), rdz[k0]);
+                col.setT(l, k0, v0);
+            }
+            for (int kk = k0; kk <= maxk; ++kk) col.R(kk) = eos_rn(ec, col.T(0, kk), col.T(1, kk), zw[maxk - 1]);
+            if (maxk - k0 > icos) icos = maxk - k0;
+        }
+    }
+    return icos;
+}
+
+// co main loop + fill for one wet column; returns the number of filled levels
+template <class Col>
+__device__ int co_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const double *dz, const double *zw)
+{
+    int kk[kMaxK + 1];
+    double dzm[kMaxK + 1];
+    kk[k1 - 1] = 0;
+    for (int m = k1; m <= maxk; ++m) {
+        kk[m] = m;
+        dzm[m] = dz[m];
+    }
+    auto refresh = [&](int x, int y) {
+        if (ec.ieos != 0) {
+            col.R(kk[x]) = eos_rn(ec, col.T(0, kk[x]), col.T(1, kk[x]), zw[kk[y]]);
+            col.R(kk[y]) = eos_rn(ec, col.T(0, kk[y]), col.T(1, kk[y]), zw[kk[y]]);
+        }
+    };
+    int m = maxk, lastmix = 0;
+    while (kk[m - 1] > 0 || (lastmix != 0 && kk[m] != maxk)) {
+        refresh(m, m - 1);
+        if (col.R(kk[m]) < col.R(kk[m - 1]) || kk[m - 1] == 0) {
+            if (lastmix == 0 || kk[m] == maxk) m = m - 1;
+            else m = m + 1;
+            lastmix = 0;
+        } else {
+            lastmix = 1;
+            int n = m - 1;
+            refresh(n, n - 1);
+            while (kk[n - 1] > 0 && col.R(kk[n]) >= col.R(kk[n - 1])) {
+                n = n - 1;
+                refresh(n, n - 1);
+            }
+            const int km = kk[m];
+            const double d0 = dzm[km];
+            double dtot = d0;
+            for (int ni = 1; ni <= m - n; ++ni) dtot = __dadd_rn(dtot, dzm[kk[m - ni]]);
+            for (int l = 0; l < L; ++l) {
+                double s = __dmul_rn(col.T(l, km), d0);
+                for (int ni = 1; ni <= m - n; ++ni) s = __dadd_rn(s, __dmul_rn(col.T(l, kk[m - ni]), dzm[kk[m - ni]]));
+                col.setT(l, km, __ddiv_rn(s, dtot));
+            }
+            dzm[km] = dtot;
+            col.R(km) = eos_rn(ec, col.T(0, km), col.T(1, km), zw[kk[m - 1]]);
+            int ni = m - 1;
+            while (kk[ni + 1] > 0) {
+                kk[ni] = kk[ni - m + n];
+                ni = ni - 1;
+            }
+        }
+    }
+    int filled = 0;
+    m = maxk - 1;
+    for (int n = maxk - 1; n >= k1; --n) {
+        if (n > kk[m]) {
+            const int src = kk[m + 1];
+            for (int l = 0; l < L; ++l) col.setT(l, n, col.T(l, src));
+            col.R(n) = eos_rn(ec, col.T(0, n), col.T(1, n), zw[kk[n - 1]]);
+            filled = filled + 1;
+        } else {
+            m = m - 1;
+        }
+    }
+    return filled;
+}
+
+}  // namespace gbgo

@@ -1,5 +1,5 @@
-// FP32-flux / FP64-state form of the tracer step (one grid, and the
-// per-member data the batched ensemble kernel reads).
+// FP32-flux / FP64-state form of the tracer step, for one grid and for the
+// batched ensemble (a single grid is a batch of one member).
 #pragma once
 
 #include "gb_internal.h"
@@ -11,20 +11,94 @@
 
 namespace gbgo {
 
+constexpr int kFp32MaxL = 32;   // tracers per member supported by the FP32-flux kernel
+constexpr int kFp32Threads = 128;
+
+// Per-member descriptor read by the batched kernel (device memory).
+struct MemberDesc {
+    int maxi, maxj, maxk, L;
+    int NI, NJ, diso, ieos;
+    int iconv, status_idx, parity, pad0;
+    long long stop_step;        // the member advances while step < stop_step
+    double dt, dphi, rdphi, diff1;
+    double ec[5];
+    double dsc;
+    double *buf[2];             // state ping-pong, Fortran layout with halos
+    const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
+    const float *coef;          // 6 floats per interior cell: Ae Be An Bn Aa Ba (transfer coefficients)
+    const double *rvol;         // 1/(dphi*ds(j)*dz(k)), index (j-1) + maxj*(k-1)
+    const float *gtop;          // forcing transfer dt*dphi*ds(j)*ts(l,i,j,maxk+1), index l + L*((i-1)+maxi*(j-1))
+    const int32_t *k1;          // (maxi+2, maxj+2)
+    const int32_t *scale;       // per tracer power-of-two exponent of the fixed-point transfers
+    const double *mk;           // FP64 k metrics, Fortran-indexed, 4 arrays of maxk+2: dz, rdz, zw, zro
+    const float *fj;            // FP32 j metrics, 4 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), ds(j)*dt*dphi, unused
+    const float *fk;            // FP32 k metrics, 3 arrays of maxk+2: rdza, zw, ssmax
+    double *cost;
+    int32_t *icosd;
+    unsigned long long *diag;   // two slots {dmax bits, limps}; step n uses slot n & 1 and clears
+                                // slot (n+1) & 1 for the next step
+    unsigned int *status;       // bit0 non-finite, bit1 transfer range exceeded
+};
+
+// Host-side owner of one member's FP32-path device data.
+struct Fp32Data {
+    MemberDesc host{};          // descriptor contents (device pointers)
+    MemberDesc *dev = nullptr;  // device copy when used alone
+    float *coef = nullptr;
+    double *rvol = nullptr;
+    float *gtop = nullptr;
+    int32_t *scale = nullptr;
+    double *mk = nullptr;
+    float *fj = nullptr, *fk = nullptr;
+    unsigned int *status = nullptr;
+    unsigned long long *diag = nullptr;
+    int4 *items = nullptr;      // work items when stepped alone
+    int nitems = 0;
+    long long *step_ctr = nullptr;
+    std::vector<int32_t> scale_host;
+    std::vector<float> gtop_host_unscaled;
+    double cmax = 0.0;          // max over faces of |A|+|B|
+    int tile_i = 16, tile_j = 8;
+    long long steps = 0;
+    long long step_host = 0;
+    bool desc_valid = false;
+};
+
 struct Fp32Member {
     bool ready = false;
-    void *impl = nullptr;   // owned device data, see tstep_fp32.cu
+    void *impl = nullptr;   // owner of the member's FP32-path data (tstep_fp32.cu)
 };
 
 int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Metrics &m,
                      const std::vector<double> &blob, const int32_t *k1_host, cudaStream_t s, std::string &msg);
 void fp32_member_free(Fp32Member *f);
-int fp32_member_upload(Fp32Member *f, const double *ts_cur, const double *ts_static, cudaStream_t s);
-int fp32_member_set_top(Fp32Member *f, const double *top, cudaStream_t s);
-int fp32_member_set_velocity(Fp32Member *f, const double *u, cudaStream_t s);
+// host pointers: the transfer scales and coefficients are built on the host
+int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, cudaStream_t s);
+int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s);
+int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s);
 int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, const double *ts_static, double *cost,
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s);
 int fp32_member_export(Fp32Member *f, const double *ts_cur, double *rho, const double *ts_static, cudaStream_t s);
+
+// shared by the single-grid path and the ensemble
+struct Fp32Static {
+    std::vector<float> coef;       // 6 per interior cell
+    std::vector<double> rvol;
+    std::vector<double> mk;
+    std::vector<float> fj, fk;
+    double cmax = 0.0;
+};
+void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const int32_t *k1,
+                       const double *u_host, Fp32Static &out);
+void fp32_scales(const Dims &d, const int32_t *k1, const double *ts_host, double cmax, const float *gtop_unscaled,
+                 std::vector<int32_t> &scale);
+void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top_host,
+               std::vector<float> &gtop);
+int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int lmax, int smem_bytes,
+                const long long *step_ctr, int rel, cudaStream_t s);
+int fp32_smem_bytes(int tile_i, int tile_j, int L);
+void fp32_default_tile(int maxi, int maxj, int *ti, int *tj);
+int fp32_export(const MemberDesc &md, const double *cur, double *rho, cudaStream_t s);
 
 void count_launches(uint64_t n);
 

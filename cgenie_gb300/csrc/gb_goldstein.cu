@@ -402,10 +402,11 @@ extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const doubl
                                 cudaMemcpyDeviceToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->rho, rho, nrho * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     h->cur = 0;
+    h->slot = 0;
     h->state_ready = true;
     h->steps_since_upload = 0;
     if (h->precision == GB_GO_FP32FLUX) {
-        int r = fp32_member_upload(&h->f32, h->ts_buf[0], h->ts_static, h->stream);
+        int r = fp32_member_upload(&h->f32, ts1, ts, h->stream);
         if (r) return fail(h, r, "fp32 upload failed");
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -422,7 +423,7 @@ extern "C" int gb_go_set_forcing(gb_go_handle *h, const double *ts_top)
     CUDA_TRY(h, cudaMemcpyAsync(h->ts_static + ntop * (h->d.maxk + 1), h->top, ntop * sizeof(double),
                                 cudaMemcpyDeviceToDevice, h->stream));
     if (h->precision == GB_GO_FP32FLUX) {
-        int r = fp32_member_set_top(&h->f32, h->top, h->stream);
+        int r = fp32_member_set_top(&h->f32, ts_top, h->stream);
         if (r) return fail(h, r, "fp32 set_forcing failed");
     }
     return GB_GO_OK;
@@ -435,7 +436,7 @@ extern "C" int gb_go_set_velocity(gb_go_handle *h, const double *u)
     const size_t nu = (size_t)3 * (h->d.maxi + 1) * (h->d.maxj + 1) * h->d.maxk;
     CUDA_TRY(h, cudaMemcpyAsync(h->u, u, nu * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (h->precision == GB_GO_FP32FLUX) {
-        int r = fp32_member_set_velocity(&h->f32, h->u, h->stream);
+        int r = fp32_member_set_velocity(&h->f32, u, h->stream);
         if (r) return fail(h, r, "fp32 set_velocity failed");
     }
     h->vel_ready = true;

@@ -1,0 +1,116 @@
+"""Batched ensembles of GOLDSTEIN grids over the gb_ens_* C-ABI.
+
+Every member is an independent grid (its own dimensions, tracers, mask,
+velocities and diffusivities).  All active members advance together, one
+persistent FP32-flux launch per step; members can be added and retired between
+steps (continuous batching).  There is no counterpart in the reference, which
+runs a single grid serially; each member's arithmetic is the reference's
+tracer step in the split-precision form (FP32 transfers, FP64 state).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import abi
+from .abi import GbEnsTuning, GridRefs, dptr
+from .goldstein import GoldsteinError, load_library
+
+
+class Ensemble:
+    def __init__(self, device: int = -1, hbm_budget_bytes: int = 0, *, tile_i: int = 0, tile_j: int = 0,
+                 use_graph: bool = False, stream: Optional[int] = None):
+        self.lib = load_library()
+        e = C.c_void_p()
+        rc = self.lib.gb_ens_create(int(device), C.c_size_t(hbm_budget_bytes), C.byref(e))
+        if rc != 0:
+            raise GoldsteinError(rc, "gb_ens_create")
+        self.e = e
+        self.members = {}
+        self.set_tuning(tile_i=tile_i, tile_j=tile_j, use_graph=use_graph)
+        if stream is not None:
+            self._check(self.lib.gb_ens_set_stream(self.e, C.c_void_p(stream)), "gb_ens_set_stream")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            detail = self.lib.gb_ens_last_error(self.e).decode() if self.e else ""
+            raise GoldsteinError(rc, what, detail)
+
+    def set_tuning(self, tile_i=0, tile_j=0, ctas_per_sm=0, use_graph=False):
+        t = GbEnsTuning(int(tile_i), int(tile_j), int(ctas_per_sm), int(bool(use_graph)))
+        self._check(self.lib.gb_ens_set_tuning(self.e, C.byref(t)), "gb_ens_set_tuning")
+
+    def close(self):
+        if getattr(self, "e", None):
+            self.lib.gb_ens_destroy(self.e)
+            self.e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def member_bytes(member) -> int:
+        lib = load_library()
+        r = GridRefs(member)
+        return int(lib.gb_ens_member_bytes(C.byref(r.dims), C.byref(r.params)))
+
+    def add(self, member, steps: Optional[int] = None, **kw) -> int:
+        """Admit a member (its state ts is also the initial ts1); returns its id.
+        Raises GoldsteinError(GB_GO_ENOMEM) when it does not fit the HBM budget."""
+        r = GridRefs(member, precision=abi.GB_GO_FP32FLUX, **kw)
+        ts = np.ascontiguousarray(member.ts, dtype=np.float64)
+        u = np.ascontiguousarray(member.u, dtype=np.float64)
+        mid = C.c_int32()
+        self._check(self.lib.gb_ens_add(self.e, C.byref(r.dims), C.byref(r.params), C.byref(r.grid), dptr(ts),
+                                        dptr(u), C.byref(mid)), "gb_ens_add")
+        self.members[mid.value] = member
+        if steps is not None:
+            self.set_remaining(mid.value, steps)
+        return mid.value
+
+    def remove(self, mid: int):
+        self._check(self.lib.gb_ens_remove(self.e, int(mid)), "gb_ens_remove")
+        self.members.pop(mid, None)
+
+    def step(self, nsteps: int = 1):
+        self._check(self.lib.gb_ens_step(self.e, int(nsteps)), "gb_ens_step")
+
+    def set_remaining(self, mid: int, steps: int):
+        self._check(self.lib.gb_ens_set_remaining(self.e, int(mid), C.c_int64(int(steps))), "gb_ens_set_remaining")
+
+    def remaining(self, mid: int) -> int:
+        v = C.c_int64()
+        self._check(self.lib.gb_ens_remaining(self.e, int(mid), C.byref(v)), "gb_ens_remaining")
+        return int(v.value)
+
+    def download(self, mid: int) -> dict:
+        m = self.members[mid]
+        ts = np.empty_like(m.ts)
+        rho = np.empty_like(m.rho)
+        cost = np.empty_like(m.cost)
+        self._check(self.lib.gb_ens_download(self.e, int(mid), dptr(ts), dptr(rho), dptr(cost)), "gb_ens_download")
+        return dict(ts=ts, rho=rho, cost=cost)
+
+    def inventory(self, mid: int) -> np.ndarray:
+        out = np.zeros(self.members[mid].maxl)
+        self._check(self.lib.gb_ens_inventory(self.e, int(mid), dptr(out)), "gb_ens_inventory")
+        return out
+
+    def status(self, mid: int) -> int:
+        v = C.c_int32()
+        self._check(self.lib.gb_ens_status(self.e, int(mid), C.byref(v)), "gb_ens_status")
+        return int(v.value)
+
+    def sync(self):
+        self._check(self.lib.gb_ens_sync(self.e), "gb_ens_sync")
+
+    def count(self):
+        a = C.c_int32()
+        b = C.c_size_t()
+        self._check(self.lib.gb_ens_count(self.e, C.byref(a), C.byref(b)), "gb_ens_count")
+        return int(a.value), int(b.value)
