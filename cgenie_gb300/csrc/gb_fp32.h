@@ -30,7 +30,7 @@ struct MemberDesc {
     const float *gtop;          // forcing transfer dt*dphi*ds(j)*ts(l,i,j,maxk+1), index l + L*((i-1)+maxi*(j-1))
     const int32_t *k1;          // (maxi+2, maxj+2)
     const int32_t *scale;       // per tracer power-of-two exponent of the fixed-point transfers
-    const double *mk;           // FP64 k metrics, Fortran-indexed, 4 arrays of maxk+2: dz, rdz, zw, zro
+    const double *mk;           // FP64 k metrics, Fortran-indexed, 5 arrays of maxk+2: dz, rdz, zw, zro, rdza
     const float *fj;            // FP32 j metrics, 4 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), ds(j)*dt*dphi, unused
     const float *fk;            // FP32 k metrics, 3 arrays of maxk+2: rdza, zw, ssmax
     double *cost;

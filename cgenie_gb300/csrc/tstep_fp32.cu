@@ -227,45 +227,53 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                 float cC0 = Ba, cC1 = Aa, cW0 = 0.f, cE0 = 0.f, cS0 = 0.f, cN0 = 0.f, cW1 = 0.f, cE1 = 0.f, cS1 = 0.f,
                       cN1 = 0.f;
                 if (md.diso && !top) {
-                    const float sT = __int_as_float((127 - s_scale[0]) << 23);
-                    const float sS = __int_as_float((127 - s_scale[1]) << 23);
-                    auto TT = [&](const float *S, int cc) { return S[cc * LP + 0] * sT; };
-                    auto SS = [&](const float *S, int cc) { return S[cc * LP + 1] * sS; };
-                    const float t1 = TT(Sk, cidx), t2 = TT(Su, cidx), s1 = SS(Sk, cidx), s2 = SS(Su, cidx);
-                    const float rdza = fk[k], zwk = fk[fkn + k];
-                    const float tatw = 0.5f * (t1 + t2);
-                    float tec = -ecf[0] - ecf[2] * tatw * 2.0f - ecf[3] * tatw * tatw * 3.0f;
-                    if (md.ieos) tec -= ecf[4] * zwk;
-                    const float dzrho = (ecf[1] * (s2 - s1) - tec * (t2 - t1)) * rdza;
-                    if (dzrho < -1.0e-12f) {
+                    // Slopes need the density differences scc*dS - tec*dT, which cancel
+                    // strongly in weakly stratified water: they are formed in FP64 from
+                    // the FP64 state as differences of D = ec(2)*S - tec*T (tec of this
+                    // cell, as in goldstein.f90:2587-2588); the rest is FP32.
+                    const double *mk = md.mk;
+                    const int mkn = maxk + 2;
+                    auto ld = [&](int ii, int jj, int kk, int l) {
+                        return __ldg(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
+                    };
+                    const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
+                    const double s1 = ld(i, j, k, 1), s2 = ld(i, j, k + 1, 1);
+                    const double tatw = 0.5 * (t1 + t2);
+                    double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
+                    if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
+                    const double scc = md.ec[1];
+                    const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
+                    const double dzrho = (Dc1 - Dc0) * mk[4 * mkn + k];
+                    if (dzrho < -1.0e-12) {
                         iso = true;
-                        const float rdzrho = 1.0f / dzrho;
-                        const float scc = ecf[1];
+                        const float rdza = fk[k];
+                        const float dzf = (float)dzrho;
+                        const float rdzrho = 1.0f / dzf;
                         const float rcr = fj[j];                 // rc(j)*rdphi
-                        float dxr[4], dyr[4], mxf[4], myf[4];
+                        const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
+                        float dxr[4], dyr[4];
                         float tv1 = 0.0f;
 #pragma unroll
                         for (int knp = 0; knp <= 1; ++knp) {
-                            const float *S = knp ? Su : Sk;
+                            const double Dck = knp ? Dc1 : Dc0;
 #pragma unroll
                             for (int nnp = 0; nnp <= 1; ++nnp) {
                                 const int ina = nnp + 2 * knp;
                                 const int kk = k + knp;
                                 const int cx = cidx + (nnp ? 1 : -1);
                                 const int cy = cidx + (nnp ? nx : -nx);
-                                const bool mx = kk >= k1t[cx];
-                                const bool my = kk >= k1t[cy];
-                                const float cvr = fj[fjn + j - 1 + nnp];   // cv(j-1+nnp)*rdsv(j-1+nnp)
-                                mxf[ina] = mx ? rcr : 0.0f;
-                                myf[ina] = my ? cvr : 0.0f;
-                                const int cxa = nnp ? cx : cidx, cxb = nnp ? cidx : cx;
-                                const int cya = nnp ? cy : cidx, cyb = nnp ? cidx : cy;
-                                const float dxT = (TT(S, cxa) - TT(S, cxb)) * mxf[ina];
-                                const float dxS = (SS(S, cxa) - SS(S, cxb)) * mxf[ina];
-                                const float dyT = (TT(S, cya) - TT(S, cyb)) * myf[ina];
-                                const float dyS = (SS(S, cya) - SS(S, cyb)) * myf[ina];
-                                dxr[ina] = scc * dxS - tec * dxT;
-                                dyr[ina] = scc * dyS - tec * dyT;
+                                dxr[ina] = 0.0f;
+                                dyr[ina] = 0.0f;
+                                if (kk >= k1t[cx]) {
+                                    const int ii = nnp ? ip : im;
+                                    const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
+                                    dxr[ina] = (float)(nnp ? Dn - Dck : Dck - Dn) * rcr;
+                                }
+                                if (kk >= k1t[cy]) {
+                                    const int jj = nnp ? j + 1 : j - 1;
+                                    const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
+                                    dyr[ina] = (float)(nnp ? Dn - Dck : Dck - Dn) * fj[fjn + j - 1 + nnp];
+                                }
                                 tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
                             }
                         }
@@ -279,13 +287,19 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         }
                         const float tvd = tv1 * slim * (float)md.diff1 * rdza * (float)md.dt * rdza;
                         dmax_l = fmaxf(dmax_l, tvd);
-                        // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
+                        // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]; dxr/dyr already
+                        // carry the metric factors, masked corners are zero
                         const float c0 = fj[2 * fjn + j] * 0.25f * slim * (float)md.diff1 * rdzrho * rdzrho;
-                        const float two_dz = 2.0f * dzrho * c0;
-                        const float wx0 = two_dz * dxr[0] * mxf[0], wx1 = two_dz * dxr[1] * mxf[1];
-                        const float wx2 = two_dz * dxr[2] * mxf[2], wx3 = two_dz * dxr[3] * mxf[3];
-                        const float wy0 = two_dz * dyr[0] * myf[0], wy1 = two_dz * dyr[1] * myf[1];
-                        const float wy2 = two_dz * dyr[2] * myf[2], wy3 = two_dz * dyr[3] * myf[3];
+                        const float two_dz = 2.0f * dzf * c0;
+                        const float mx0 = (k >= k1t[cidx - 1]) ? rcr : 0.0f, mx1 = (k >= k1t[cidx + 1]) ? rcr : 0.0f;
+                        const float mx2 = (k + 1 >= k1t[cidx - 1]) ? rcr : 0.0f, mx3 = (k + 1 >= k1t[cidx + 1]) ? rcr : 0.0f;
+                        const float cvs = fj[fjn + j - 1], cvn = fj[fjn + j];
+                        const float my0 = (k >= k1t[cidx - nx]) ? cvs : 0.0f, my1 = (k >= k1t[cidx + nx]) ? cvn : 0.0f;
+                        const float my2 = (k + 1 >= k1t[cidx - nx]) ? cvs : 0.0f, my3 = (k + 1 >= k1t[cidx + nx]) ? cvn : 0.0f;
+                        const float wx0 = two_dz * dxr[0] * mx0, wx1 = two_dz * dxr[1] * mx1;
+                        const float wx2 = two_dz * dxr[2] * mx2, wx3 = two_dz * dxr[3] * mx3;
+                        const float wy0 = two_dz * dyr[0] * my0, wy1 = two_dz * dyr[1] * my1;
+                        const float wy2 = two_dz * dyr[2] * my2, wy3 = two_dz * dyr[3] * my3;
                         const float wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
                         cW0 = -wx0; cE0 = wx1; cW1 = -wx2; cE1 = wx3;
                         cS0 = -wy0; cN0 = wy1; cS1 = -wy2; cN1 = wy3;
@@ -509,12 +523,13 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
             }
         }
     }
-    out.mk.assign(4 * (size_t)nk, 0.0);
+    out.mk.assign(5 * (size_t)nk, 0.0);
     for (int k = 0; k <= maxk + 1; ++k) {
         out.mk[k] = dz[k];
         out.mk[nk + k] = rdz[k];
         out.mk[2 * nk + k] = zw[k];
         out.mk[3 * nk + k] = zro[k];
+        out.mk[4 * nk + k] = rdza[k];
     }
     out.fj.assign(4 * (size_t)nj, 0.0f);
     for (int j = 0; j <= maxj + 1; ++j) {
@@ -686,7 +701,7 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMalloc(&D.rvol, (size_t)d.maxj * d.maxk * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.gtop, (size_t)d.L * d.maxi * d.maxj * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.scale, (size_t)d.L * sizeof(int32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&D.mk, 4 * (size_t)nk * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&D.mk, 5 * (size_t)nk * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.fj, 4 * (size_t)nj * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.fk, 3 * (size_t)nk * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.status, sizeof(unsigned int));
