@@ -43,9 +43,10 @@ struct Member {
     size_t bytes = 0;
     // device
     double *buf0 = nullptr, *buf1 = nullptr, *ts_static = nullptr, *rho = nullptr, *stage = nullptr;
-    float *coef = nullptr, *gtop = nullptr, *fj = nullptr, *fk = nullptr;
-    double *rvol = nullptr, *mk = nullptr, *cost = nullptr, *dsj = nullptr;
+    float *coef = nullptr, *gtop = nullptr;
+    double *rvol = nullptr, *mk = nullptr, *mj = nullptr, *cost = nullptr, *dsj = nullptr;
     int32_t *k1 = nullptr, *scale = nullptr, *icosd = nullptr;
+    unsigned int *gmax = nullptr;         // per tracer, scale re-targeting
     unsigned long long *diag = nullptr;   // two slots {dmax bits, limps}
     unsigned int *status = nullptr;
     std::vector<double> ds_host;          // ds(0:maxj+1), for the inventory
@@ -100,7 +101,7 @@ static size_t member_bytes(const gb_go_dims *d)
     const size_t ncell = (size_t)d->maxi * d->maxj * d->maxk;
     const size_t ncol = (size_t)d->maxi * d->maxj;
     // two state buffers, uploaded copy, download stage, rho, coefficients, forcing, small arrays
-    return 4 * nts * 8 + nrho * 8 + 6 * ncell * 4 + ncol * d->maxl * 4 + (size_t)d->maxj * d->maxk * 8 +
+    return 4 * nts * 8 + nrho * 8 + 12 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
            ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + 4096;
 }
 
@@ -140,8 +141,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
 static void free_member(gb_ens *e, Member *m)
 {
     cudaStream_t s = e->stream;
-    void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->gtop, m->fj, m->fk,
-                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status};
+    void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->gtop, m->mj,
+                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
 }
@@ -235,8 +236,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = dalloc(e, &m->rho, nrho);
     if (x == cudaSuccess) x = dalloc(e, &m->coef, st.coef.size());
     if (x == cudaSuccess) x = dalloc(e, &m->gtop, gtop.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->fj, st.fj.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->fk, st.fk.size());
+    if (x == cudaSuccess) x = dalloc(e, &m->mj, st.mj.size());
     if (x == cudaSuccess) x = dalloc(e, &m->rvol, st.rvol.size());
     if (x == cudaSuccess) x = dalloc(e, &m->mk, st.mk.size());
     if (x == cudaSuccess) x = dalloc(e, &m->cost, ncol);
@@ -244,6 +244,8 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = dalloc(e, &m->k1, (size_t)m->d.NI * m->d.NJ);
     if (x == cudaSuccess) x = dalloc(e, &m->scale, scale.size());
     if (x == cudaSuccess) x = dalloc(e, &m->dsj, (size_t)dims->maxj + 2);
+    if (x == cudaSuccess) x = dalloc(e, &m->gmax, (size_t)dims->maxl);
+    if (x == cudaSuccess) x = cudaMemsetAsync(m->gmax, 0, (size_t)dims->maxl * sizeof(unsigned int), s);
     if (x == cudaSuccess) x = dalloc(e, &m->diag, 4);
     if (x == cudaSuccess) x = dalloc(e, &m->status, 1);
     m->ds_host.assign(blob.begin() + 6 * (dims->maxj + 2), blob.begin() + 7 * (dims->maxj + 2));
@@ -256,8 +258,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = cudaMemsetAsync(m->rho, 0, nrho * 8, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->coef, st.coef.data(), st.coef.size() * 4, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->gtop, gtop.data(), gtop.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->fj, st.fj.data(), st.fj.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->fk, st.fk.data(), st.fk.size() * 4, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->mj, st.mj.data(), st.mj.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->rvol, st.rvol.data(), st.rvol.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->mk, st.mk.data(), st.mk.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemsetAsync(m->cost, 0, ncol * 8, s);
@@ -279,8 +280,8 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.dsc = m->p.dsc;
     md.buf[0] = m->buf0; md.buf[1] = m->buf1;
     md.ts_static = m->ts_static; md.coef = m->coef; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
-    md.scale = m->scale; md.mk = m->mk; md.fj = m->fj; md.fk = m->fk; md.cost = m->cost; md.icosd = m->icosd;
-    md.diag = m->diag; md.status = m->status;
+    md.scale = m->scale; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
+    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission
@@ -375,10 +376,11 @@ static int launch_steps(gb_ens *e, int nsteps)
     cudaStream_t s = e->stream;
     for (int n = 0; n < nsteps; ++n) {
         int r = fp32_launch(e->descs, e->items, e->nitems, e->lmax, e->smem, e->step_ctr, n, s);
+        if (!r) r = fp32_rescale(e->descs, (int)e->members.size(), s);
         if (r) return efail(e, r, "fp32 batched launch failed");
     }
     k_add_step<<<1, 1, 0, s>>>(e->step_ctr, nsteps);
-    count_launches((uint64_t)nsteps + 1);
+    count_launches(2 * (uint64_t)nsteps + 1);
     return cudaGetLastError() == cudaSuccess ? GB_GO_OK : efail(e, GB_GO_ECUDA, "launch failed");
 }
 
@@ -414,7 +416,7 @@ extern "C" int gb_ens_step(gb_ens *e, int32_t nsteps)
             e->graph_steps = nsteps;
         }
         ETRY(e, cudaGraphLaunch(e->graph, e->stream));
-        count_launches((uint64_t)nsteps + 1);
+        count_launches(2 * (uint64_t)nsteps + 1);
     } else {
         int r = launch_steps(e, nsteps);
         if (r) return r;

@@ -25,14 +25,17 @@ struct MemberDesc {
     double dsc;
     double *buf[2];             // state ping-pong, Fortran layout with halos
     const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
-    const float *coef;          // 6 floats per interior cell: Ae Be An Bn Aa Ba (transfer coefficients)
+    const float *coef;          // 12 floats per interior cell: Ae Be An Bn Aa Ba as FP32, then their
+                                // FP64 remainders (the pair hi+lo carries the FP64 coefficient)
     const double *rvol;         // 1/(dphi*ds(j)*dz(k)), index (j-1) + maxj*(k-1)
-    const float *gtop;          // forcing transfer dt*dphi*ds(j)*ts(l,i,j,maxk+1), index l + L*((i-1)+maxi*(j-1))
+    const float *gtop;          // forcing transfer dt*dphi*ds(j)*ts(l,i,j,maxk+1): L+2 floats per column
+                                // ((i-1)+maxi*(j-1)): FP32 value of every tracer, then the lo parts of T, S
     const int32_t *k1;          // (maxi+2, maxj+2)
-    const int32_t *scale;       // per tracer power-of-two exponent of the fixed-point transfers
-    const double *mk;           // FP64 k metrics, Fortran-indexed, 5 arrays of maxk+2: dz, rdz, zw, zro, rdza
-    const float *fj;            // FP32 j metrics, 4 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), ds(j)*dt*dphi, unused
-    const float *fk;            // FP32 k metrics, 3 arrays of maxk+2: rdza, zw, ssmax
+    int32_t *scale;             // per tracer power-of-two exponent of the fixed-point transfers; re-targeted
+                                // between steps from gmax so the largest transfer sits near 2^26
+    unsigned int *gmax;         // per tracer: largest |scaled transfer| of the step (FP32 bits)
+    const double *mk;           // FP64 k metrics, Fortran-indexed, 6 arrays of maxk+2: dz, rdz, zw, zro, rdza, ssmax
+    const double *mj;           // FP64 j metrics, 3 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), dt*dphi*ds(j)
     double *cost;
     int32_t *icosd;
     unsigned long long *diag;   // two slots {dmax bits, limps}; step n uses slot n & 1 and clears
@@ -48,8 +51,8 @@ struct Fp32Data {
     double *rvol = nullptr;
     float *gtop = nullptr;
     int32_t *scale = nullptr;
-    double *mk = nullptr;
-    float *fj = nullptr, *fk = nullptr;
+    unsigned int *gmax = nullptr;
+    double *mk = nullptr, *mj = nullptr;
     unsigned int *status = nullptr;
     unsigned long long *diag = nullptr;
     int4 *items = nullptr;      // work items when stepped alone
@@ -82,10 +85,9 @@ int fp32_member_export(Fp32Member *f, const double *ts_cur, double *rho, const d
 
 // shared by the single-grid path and the ensemble
 struct Fp32Static {
-    std::vector<float> coef;       // 6 per interior cell
+    std::vector<float> coef;       // 12 per interior cell
     std::vector<double> rvol;
-    std::vector<double> mk;
-    std::vector<float> fj, fk;
+    std::vector<double> mk, mj;
     double cmax = 0.0;
 };
 void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const int32_t *k1,
@@ -99,6 +101,8 @@ int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int lmax
 int fp32_smem_bytes(int tile_i, int tile_j, int L);
 void fp32_default_tile(int maxi, int maxj, int *ti, int *tj);
 int fp32_export(const MemberDesc &md, const double *cur, double *rho, cudaStream_t s);
+// re-target the fixed-point scales of `n` members after a step (stream order)
+int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s);
 
 void count_launches(uint64_t n);
 

@@ -3,24 +3,31 @@
 // The arithmetic of src/goldstein/goldstein.f90:2436-2642 (tstepo_flux) is
 // rewritten per face as a linear transfer G = A*T_neighbour + B*T_centre with
 // tracer-independent coefficients (upstream weights, masks and the metric
-// factors dt*area folded in, built once per velocity field); the isoneutral
-// term of the vertical face (goldstein.f90:2561-2624) becomes a 10-point
-// stencil whose coefficients are built per cell and step from T and S.
+// factors dt*area folded in, built once per velocity field in FP64 and kept as
+// an FP32 pair hi+lo); the isoneutral term of the vertical face
+// (goldstein.f90:2561-2624) becomes a 10-point stencil whose coefficients are
+// built per cell and step in FP64 from the FP64 state.
 //
-// Split precision with exact conservation: face transfers are evaluated in FP32
-// on tracer values scaled by a per-tracer power of two, rounded once to int32
-// (F2I), and the SAME integer is subtracted from one cell and added to the
-// other, so the integer budget of every step telescopes exactly.  The FP64
-// state is then updated with one FMA: T += (sum of integer transfers)*2^-s / V.
-// The FP64 <-> FP32/int conversions are done with integer bit operations, so a
-// tracer-cell update costs one instruction of GB300's slow FP64 pipe.
+// Two precision classes share the launch:
+//  * T and S (l = 1, 2), the tracers that decide convection through the
+//    equation of state, use double-float (FP32 pair) transfers on the FP32
+//    pipe, ~1e-14 relative, so convective decisions follow the FP64 reference;
+//  * every other tracer uses FP32 transfers on values scaled by a per-tracer
+//    power of two, rounded once to int32 (F2I).  The SAME integer is taken from
+//    one cell and given to the other, so the budget telescopes exactly.
+// The FP64 state is then updated with one FMA per tracer-cell.  FP64 <-> FP32
+// and int -> FP64 conversions use integer bit operations: GB300's FP64 pipe
+// (and its hardware conversions) run at ~2 ops/clk/SM.
 //
 // Convective adjustment (goldstein.f90:2657-2841) runs in exact FP64 on columns
 // that an FP32 density prescreen cannot prove statically stable.
 //
 // Mapping: a CTA of 128 threads takes work items (member, TX x TY column tile)
-// from a host-built list; each thread owns one column and marches k upward,
-// with FP32 slabs of levels k and k+1 (plus the k+2 prefetch) in shared memory.
+// from a host-built list.  Each level k of a tile: cp.async brings the FP64 slab
+// of level k+2 (with a one-cell halo) into shared memory while threads (one per
+// column) compute the integer / double-float transfers of level k from scaled
+// FP32 slabs of levels k and k+1; then the tile's FP64 state of level k is
+// updated row by row with coalesced loads and stores.
 #include "gb_fp32.h"
 #include "co_column.cuh"
 #include "../../include/gb_goldstein.h"
@@ -46,6 +53,17 @@ __device__ __forceinline__ float d2f_scaled(double x, int s)
     return __uint_as_float(f | (hi & 0x80000000u));
 }
 
+// (double)f * 2^-s exactly (FP32 zero and subnormals give 0)
+__device__ __forceinline__ double f2d_scaled(float f, int s)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned a = b & 0x7fffffffu;
+    const unsigned hi = (b & 0x80000000u) | ((a >> 3) + ((unsigned)(896 - s) << 20));
+    const unsigned lo = a << 29;
+    const double r = __hiloint2double((int)hi, (int)lo);
+    return a < 0x00800000u ? 0.0 : r;
+}
+
 // (double)q * 2^-s exactly
 __device__ __forceinline__ double i2d_scaled(int q, int s)
 {
@@ -56,6 +74,51 @@ __device__ __forceinline__ double i2d_scaled(int q, int s)
     const unsigned lo = m << 20;
     const double r = __hiloint2double((int)hi, (int)lo);
     return q == 0 ? 0.0 : r;
+}
+
+// ---------------------------------------------------------------------------
+// double-float (unevaluated FP32 pair) arithmetic
+
+struct dflt {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dflt df_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ dflt df_fast(float a, float b)
+{
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ dflt df_add(dflt a, dflt b)
+{
+    const dflt s = df_two_sum(a.hi, b.hi);
+    return df_fast(s.hi, (a.lo + b.lo) + s.lo);
+}
+
+__device__ __forceinline__ dflt df_sub(dflt a, dflt b) { return df_add(a, dflt{-b.hi, -b.lo}); }
+
+// A*X + B*Y
+__device__ __forceinline__ dflt df_dot2(dflt A, dflt X, dflt B, dflt Y)
+{
+    const float p1 = A.hi * X.hi, p2 = B.hi * Y.hi;
+    const float e1 = fmaf(A.hi, X.hi, -p1), e2 = fmaf(B.hi, Y.hi, -p2);
+    const dflt s = df_two_sum(p1, p2);
+    const float t = fmaf(A.hi, X.lo, fmaf(A.lo, X.hi, fmaf(B.hi, Y.lo, B.lo * Y.hi)));
+    return df_fast(s.hi, ((e1 + e2) + t) + s.lo);
+}
+
+// FP64 value as a double-float (hi truncated, lo the rest)
+__device__ __forceinline__ dflt df_split(double x)
+{
+    const float h = d2f_scaled(x, 0);
+    return {h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
 }
 
 __device__ __forceinline__ float eos_f(const float ec[5], float t, float s)
@@ -81,20 +144,56 @@ struct Fp32Col {
 // ---------------------------------------------------------------------------
 // the step kernel
 
-struct SmemLayout {
-    int nx, ny, LP;      // slab extents (TX+2, TY+2) and padded tracer stride
-    int slab;            // floats per slab
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Dynamic shared memory of one work item (byte offsets, 16-byte aligned).
+struct Fp32Smem {
+    int stage;   // double[nc*L]   FP64 slab in flight (cp.async)
+    int f0, f1;  // float[nc*LP]   scaled FP32 slabs of levels k and k+1 (hi parts for T,S)
+    int g0, g1;  // float[nc*2]    lo parts of T and S for the two slabs
+    int qb, qs;  // int[nin*LP]    bottom-face carry, per-level transfer sum (tracers >= 3)
+    int qbd, qsd;// float[nin*4]   the same for T and S as double-floats
+    int tsn;     // float[nin*2]   new T and S of the level just updated
+    int k1t;     // int[nc]        k1 with a one-cell halo
+    int total;
 };
 
-template <int LMAX>
-__global__ void __launch_bounds__(kFp32Threads, 3)
+__host__ __device__ inline Fp32Smem fp32_smem_layout(int TX, int TY, int L)
+{
+    const int nc = (TX + 2) * (TY + 2), LP = L | 1, nin = TX * TY;
+    Fp32Smem s;
+    int o = 0;
+    s.stage = o; o += (nc * L * 8 + 15) & ~15;
+    s.f0 = o; o += (nc * LP * 4 + 15) & ~15;
+    s.f1 = o; o += (nc * LP * 4 + 15) & ~15;
+    s.g0 = o; o += (nc * 2 * 4 + 15) & ~15;
+    s.g1 = o; o += (nc * 2 * 4 + 15) & ~15;
+    s.qb = o; o += (nin * LP * 4 + 15) & ~15;
+    s.qs = o; o += (nin * LP * 4 + 15) & ~15;
+    s.qbd = o; o += (nin * 4 * 4 + 15) & ~15;
+    s.qsd = o; o += (nin * 4 * 4 + 15) & ~15;
+    s.tsn = o; o += (nin * 2 * 4 + 15) & ~15;
+    s.k1t = o; o += (nc * 4 + 15) & ~15;
+    s.total = o;
+    return s;
+}
+
+__global__ void __launch_bounds__(kFp32Threads, 4)
 k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
             const long long *__restrict__ step_ctr, int rel)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_kstart;
-    __shared__ int s_scale[LMAX];
+    __shared__ int s_scale[kFp32MaxL];
+    __shared__ unsigned int s_gmax[kFp32MaxL];
     const int t = threadIdx.x;
+    const int warp = t >> 5, lane = t & 31, nwarp = blockDim.x >> 5;
     const long long step = *step_ctr + rel;
 
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -110,18 +209,29 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             dn[1] = 0ull;
         }
         const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
-        const int nx = TX + 2, ny = TY + 2;
-        const int LP = L | 1;
-        const int slabf = nx * ny * LP;
-        int *k1t = reinterpret_cast<int *>(smraw);
-        float *slab0 = reinterpret_cast<float *>(smraw + ((nx * ny * 4 + 15) & ~15));
+        const int nx = TX + 2, ny = TY + 2, nc = nx * ny, LP = L | 1, nin = TX * TY;
+        const Fp32Smem lay = fp32_smem_layout(TX, TY, L);
+        double *stage = reinterpret_cast<double *>(smraw + lay.stage);
+        float *F0 = reinterpret_cast<float *>(smraw + lay.f0);
+        float *F1 = reinterpret_cast<float *>(smraw + lay.f1);
+        float *G0 = reinterpret_cast<float *>(smraw + lay.g0);
+        float *G1 = reinterpret_cast<float *>(smraw + lay.g1);
+        int *QB = reinterpret_cast<int *>(smraw + lay.qb);
+        int *QS = reinterpret_cast<int *>(smraw + lay.qs);
+        float *QBD = reinterpret_cast<float *>(smraw + lay.qbd);
+        float *QSD = reinterpret_cast<float *>(smraw + lay.qsd);
+        float *TSN = reinterpret_cast<float *>(smraw + lay.tsn);
+        int *k1t = reinterpret_cast<int *>(smraw + lay.k1t);
         const int par = (int)((step + md.parity) & 1);
         const double *__restrict__ R = md.buf[par];
         double *__restrict__ W = md.buf[par ^ 1];
+        const double *mk = md.mk;
+        const double *mj = md.mj;
+        const int mkn = maxk + 2, mjn = maxj + 2;
 
-        // k1 tile with a one-column halo (periodic in i), land outside
+        // k1 tile with a one-column halo (periodic in i), land outside the grid
         if (t == 0) s_kstart = 1 << 20;
-        for (int e = t; e < nx * ny; e += blockDim.x) {
+        for (int e = t; e < nc; e += blockDim.x) {
             const int c = e % nx, r = e / nx;
             int gi = i0 - 1 + c, gj = j0 - 1 + r;
             int v = maxk + 1;
@@ -132,12 +242,18 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             }
             k1t[e] = v;
         }
-        for (int l = t; l < L; l += blockDim.x) s_scale[l] = md.scale[l];
+        for (int l = t; l < L; l += blockDim.x) {
+            s_scale[l] = md.scale[l];
+            s_gmax[l] = 0u;
+        }
+        for (int e = t; e < nin * LP; e += blockDim.x) QB[e] = 0;
+        for (int e = t; e < nin * 4; e += blockDim.x) QBD[e] = 0.0f;
         __syncthreads();
         const int ti = t % TX, tj = t / TX;
         const int i = i0 + ti, j = j0 + tj;
-        const bool inside = (t < TX * TY) && (i <= maxi) && (j <= maxj);
+        const bool inside = (t < nin) && (i <= maxi) && (j <= maxj);
         const int cidx = (tj + 1) * nx + (ti + 1);
+        const int cell = tj * TX + ti;
         const int k1c = inside ? k1t[cidx] : maxk + 1;
         if (inside && k1c <= maxk) atomicMin(&s_kstart, k1c);
         __syncthreads();
@@ -147,30 +263,28 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             continue;
         }
 
-        // slab loader: level `lev` into ring slot `slot`
-        auto load_slab = [&](int lev, int slot) {
-            float *S = slab0 + (size_t)slot * slabf;
-            const int warp = t >> 5, lane = t & 31, nwarp = blockDim.x >> 5;
-            const int rowlen = nx * L;
+        // cp.async the FP64 slab of level `lev` (rows of the tile plus halo) into stage
+        auto issue = [&](int lev) {
             const int dc = 32 / L, dl = 32 % L;
+            const int rowlen = nx * L;
             for (int r = warp; r < ny; r += nwarp) {
                 const int gj = j0 - 1 + r;
-                float *Srow = S + r * nx * LP;
+                double *Srow = stage + (size_t)r * rowlen;
                 if (gj > maxj + 1) {
-                    for (int e = lane; e < nx * LP; e += 32) Srow[e] = 0.0f;
+                    for (int e = lane; e < rowlen; e += 32) Srow[e] = 0.0;
                     continue;
                 }
                 const size_t rowbase = (size_t)NI * ((size_t)gj + (size_t)NJ * (size_t)lev);
                 int c = lane / L, l = lane % L;
                 for (int e = lane; e < rowlen; e += 32) {
                     int gi = i0 - 1 + c;
-                    float v = 0.0f;
                     if (gi <= maxi + 1) {
                         if (gi == 0) gi = maxi;
                         else if (gi == maxi + 1) gi = 1;
-                        v = d2f_scaled(__ldg(R + ((size_t)gi + rowbase) * L + l), s_scale[l]);
+                        cp_async8(Srow + e, R + ((size_t)gi + rowbase) * L + l);
+                    } else {
+                        Srow[e] = 0.0;
                     }
-                    Srow[c * LP + l] = v;
                     c += dc;
                     l += dl;
                     if (l >= L) {
@@ -179,12 +293,28 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     }
                 }
             }
+            cp_async_commit();
         };
-
-        // per-tracer carry of the bottom-face transfer (the top face of the level below)
-        int qb[LMAX];
-#pragma unroll
-        for (int l = 0; l < LMAX; ++l) qb[l] = 0;
+        // stage -> FP32 slab scaled by 2^s_l (tracer stride LP, odd: no bank conflicts);
+        // T and S also keep the truncated remainder as an FP32 lo part
+        auto convert = [&](float *dst, float *dlo) {
+            const int total = nc * L;
+            const int dc = kFp32Threads / L, dl = kFp32Threads % L;
+            int c = t / L, l = t % L;
+            for (int e = t; e < total; e += kFp32Threads) {
+                const double x = stage[e];
+                const int sl = s_scale[l];
+                const float h = d2f_scaled(x, sl);
+                dst[c * LP + l] = h;
+                if (l < 2) dlo[c * 2 + l] = d2f_scaled(x - f2d_scaled(h, sl), sl);
+                c += dc;
+                l += dl;
+                if (l >= L) {
+                    l -= L;
+                    c += 1;
+                }
+            }
+        };
 
         float ecf[5];
         for (int n = 0; n < 5; ++n) ecf[n] = (float)md.ec[n];
@@ -192,47 +322,70 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         bool unstable = false;
         float gmax = 0.0f;
         bool nonfinite = false;
-        float dmax_l = 0.0f;
+        double dmax_l = 0.0;
         unsigned limps_l = 0;
-        const float *fj = md.fj;
-        const float *fk = md.fk;
-        const int fjn = maxj + 2, fkn = maxk + 2;
 
-        load_slab(kstart, kstart % 3);
-        if (kstart + 1 <= maxk) load_slab(kstart + 1, (kstart + 1) % 3);
+        auto prescreen = [&](int lev) {
+            // FP32 density of the updated level vs the level below: a column is left to
+            // the exact co unless every pair is stable by a margin above FP32 error
+            const float tf = TSN[cell * 2 + 0], sf = TSN[cell * 2 + 1];
+            const float rf = eos_f(ecf, tf, sf);
+            if (lev > k1c) {
+                const float margin = 2.0e-6f * (fabsf(rf) + fabsf(rho_prev) + fabsf(ecf[0] * tf) +
+                                                fabsf(ecf[1] * sf) + fabsf(ecf[2] * tf * tf) +
+                                                fabsf(ecf[3] * tf * tf * tf)) + 1.0e-30f;
+                if (!(rho_prev - rf > margin)) unstable = true;
+            }
+            rho_prev = rf;
+        };
+
+        issue(kstart);
+        cp_async_wait_all();
         __syncthreads();
+        convert((kstart & 1) ? F1 : F0, (kstart & 1) ? G1 : G0);
+        __syncthreads();
+        if (kstart + 1 <= maxk) {
+            issue(kstart + 1);
+            cp_async_wait_all();
+            __syncthreads();
+            convert(((kstart + 1) & 1) ? F1 : F0, ((kstart + 1) & 1) ? G1 : G0);
+            __syncthreads();
+        }
+        if (kstart + 2 <= maxk) issue(kstart + 2);
 
         for (int k = kstart; k <= maxk; ++k) {
-            if (k + 2 <= maxk) load_slab(k + 2, (k + 2) % 3);
-            const float *Sk = slab0 + (size_t)(k % 3) * slabf;
-            const float *Su = slab0 + (size_t)((k + 1) % 3) * slabf;
+            const float *Sk = (k & 1) ? F1 : F0;
+            const float *Su = (k & 1) ? F0 : F1;
+            const float *SkL = (k & 1) ? G1 : G0;
+            const float *SuL = (k & 1) ? G0 : G1;
+            if (inside && k - 1 >= k1c && k - 1 >= kstart) prescreen(k - 1);
+            // ---- phase A: transfers of the cell's faces
             if (inside && k >= k1c) {
-                const size_t cell = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
-                const float *cf = md.coef + 6 * cell;
-                const float Ae = __ldg(cf + 0), Be = __ldg(cf + 1), An = __ldg(cf + 2), Bn = __ldg(cf + 3);
-                float Aa = __ldg(cf + 4), Ba = __ldg(cf + 5);
+                const size_t cl = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
+                const float *cf = md.coef + 12 * cl;
                 const int iw = (i == 1) ? maxi : i - 1;
-                const float *cw = md.coef + 6 * ((size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1)));
-                const float Aw = __ldg(cw + 0), Bw = __ldg(cw + 1);
-                float As = 0.0f, Bs = 0.0f;
+                const float *cw = md.coef + 12 * ((size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1)));
+                const dflt AeX = {__ldg(cf + 0), __ldg(cf + 6)}, BeX = {__ldg(cf + 1), __ldg(cf + 7)};
+                const dflt AnX = {__ldg(cf + 2), __ldg(cf + 8)}, BnX = {__ldg(cf + 3), __ldg(cf + 9)};
+                const dflt AaX = {__ldg(cf + 4), __ldg(cf + 10)}, BaX = {__ldg(cf + 5), __ldg(cf + 11)};
+                const dflt AwX = {__ldg(cw + 0), __ldg(cw + 6)}, BwX = {__ldg(cw + 1), __ldg(cw + 7)};
+                dflt AsX = {0.0f, 0.0f}, BsX = {0.0f, 0.0f};
                 if (j > 1) {
-                    const float *cs = md.coef + 6 * (cell - (size_t)maxi);
-                    As = __ldg(cs + 2);
-                    Bs = __ldg(cs + 3);
+                    const float *cs = md.coef + 12 * (cl - (size_t)maxi);
+                    AsX = {__ldg(cs + 2), __ldg(cs + 8)};
+                    BsX = {__ldg(cs + 3), __ldg(cs + 9)};
                 }
-                const double rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
                 const bool top = (k == maxk);
-                // isoneutral stencil of the top face (goldstein.f90:2561-2624), FP32
                 bool iso = false;
-                float cC0 = Ba, cC1 = Aa, cW0 = 0.f, cE0 = 0.f, cS0 = 0.f, cN0 = 0.f, cW1 = 0.f, cE1 = 0.f, cS1 = 0.f,
-                      cN1 = 0.f;
+                // top-face stencil: C1*T(k+1) + C0*T(k) (+ isoneutral corners)
+                dflt C1X = AaX, C0X = BaX;
+                dflt W0X = {0.f, 0.f}, E0X = {0.f, 0.f}, S0X = {0.f, 0.f}, N0X = {0.f, 0.f};
+                dflt W1X = {0.f, 0.f}, E1X = {0.f, 0.f}, S1X = {0.f, 0.f}, N1X = {0.f, 0.f};
                 if (md.diso && !top) {
-                    // Slopes need the density differences scc*dS - tec*dT, which cancel
-                    // strongly in weakly stratified water: they are formed in FP64 from
-                    // the FP64 state as differences of D = ec(2)*S - tec*T (tec of this
-                    // cell, as in goldstein.f90:2587-2588); the rest is FP32.
-                    const double *mk = md.mk;
-                    const int mkn = maxk + 2;
+                    // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
+                    // state: the density differences scc*dS - tec*dT cancel strongly in weakly
+                    // stratified water; they are differences of D = ec(2)*S - tec*T with the
+                    // cell's tec (goldstein.f90:2587-2588)
                     auto ld = [&](int ii, int jj, int kk, int l) {
                         return __ldg(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
                     };
@@ -243,16 +396,16 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
                     const double scc = md.ec[1];
                     const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
-                    const double dzrho = (Dc1 - Dc0) * mk[4 * mkn + k];
+                    const double rdza = mk[4 * mkn + k];
+                    const double dzrho = (Dc1 - Dc0) * rdza;
                     if (dzrho < -1.0e-12) {
                         iso = true;
-                        const float rdza = fk[k];
-                        const float dzf = (float)dzrho;
-                        const float rdzrho = 1.0f / dzf;
-                        const float rcr = fj[j];                 // rc(j)*rdphi
+                        const double rdzrho = 1.0 / dzrho;
+                        const double rcr = mj[j];                          // rc(j)*rdphi
+                        const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
                         const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
-                        float dxr[4], dyr[4];
-                        float tv1 = 0.0f;
+                        double dxr[4], dyr[4], mx[4], my[4];
+                        double tv1 = 0.0;
 #pragma unroll
                         for (int knp = 0; knp <= 1; ++knp) {
                             const double Dck = knp ? Dc1 : Dc0;
@@ -260,113 +413,184 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             for (int nnp = 0; nnp <= 1; ++nnp) {
                                 const int ina = nnp + 2 * knp;
                                 const int kk = k + knp;
-                                const int cx = cidx + (nnp ? 1 : -1);
-                                const int cy = cidx + (nnp ? nx : -nx);
-                                dxr[ina] = 0.0f;
-                                dyr[ina] = 0.0f;
-                                if (kk >= k1t[cx]) {
+                                const bool okx = kk >= k1t[cidx + (nnp ? 1 : -1)];
+                                const bool oky = kk >= k1t[cidx + (nnp ? nx : -nx)];
+                                mx[ina] = okx ? rcr : 0.0;
+                                my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
+                                dxr[ina] = 0.0;
+                                dyr[ina] = 0.0;
+                                if (okx) {
                                     const int ii = nnp ? ip : im;
                                     const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
-                                    dxr[ina] = (float)(nnp ? Dn - Dck : Dck - Dn) * rcr;
+                                    dxr[ina] = (nnp ? Dn - Dck : Dck - Dn) * rcr;
                                 }
-                                if (kk >= k1t[cy]) {
+                                if (oky) {
                                     const int jj = nnp ? j + 1 : j - 1;
                                     const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
-                                    dyr[ina] = (float)(nnp ? Dn - Dck : Dck - Dn) * fj[fjn + j - 1 + nnp];
+                                    dyr[ina] = (nnp ? Dn - Dck : Dck - Dn) * my[ina];
                                 }
                                 tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
                             }
                         }
-                        const float sum2 = tv1;
-                        tv1 = 0.25f * tv1 * rdzrho * rdzrho;
-                        const float ss = fk[2 * fkn + k];
-                        float slim = 1.0f;
+                        const double sum2 = tv1;
+                        tv1 = 0.25 * tv1 * rdzrho * rdzrho;
+                        const double ss = mk[5 * mkn + k];
+                        double slim = 1.0;
                         if (tv1 > ss) {
                             slim = ss * ss / (tv1 * tv1);
                             limps_l += 1;
                         }
-                        const float tvd = tv1 * slim * (float)md.diff1 * rdza * (float)md.dt * rdza;
-                        dmax_l = fmaxf(dmax_l, tvd);
-                        // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]; dxr/dyr already
-                        // carry the metric factors, masked corners are zero
-                        const float c0 = fj[2 * fjn + j] * 0.25f * slim * (float)md.diff1 * rdzrho * rdzrho;
-                        const float two_dz = 2.0f * dzf * c0;
-                        const float mx0 = (k >= k1t[cidx - 1]) ? rcr : 0.0f, mx1 = (k >= k1t[cidx + 1]) ? rcr : 0.0f;
-                        const float mx2 = (k + 1 >= k1t[cidx - 1]) ? rcr : 0.0f, mx3 = (k + 1 >= k1t[cidx + 1]) ? rcr : 0.0f;
-                        const float cvs = fj[fjn + j - 1], cvn = fj[fjn + j];
-                        const float my0 = (k >= k1t[cidx - nx]) ? cvs : 0.0f, my1 = (k >= k1t[cidx + nx]) ? cvn : 0.0f;
-                        const float my2 = (k + 1 >= k1t[cidx - nx]) ? cvs : 0.0f, my3 = (k + 1 >= k1t[cidx + nx]) ? cvn : 0.0f;
-                        const float wx0 = two_dz * dxr[0] * mx0, wx1 = two_dz * dxr[1] * mx1;
-                        const float wx2 = two_dz * dxr[2] * mx2, wx3 = two_dz * dxr[3] * mx3;
-                        const float wy0 = two_dz * dyr[0] * my0, wy1 = two_dz * dyr[1] * my1;
-                        const float wy2 = two_dz * dyr[2] * my2, wy3 = two_dz * dyr[3] * my3;
-                        const float wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
-                        cW0 = -wx0; cE0 = wx1; cW1 = -wx2; cE1 = wx3;
-                        cS0 = -wy0; cN0 = wy1; cS1 = -wy2; cN1 = wy3;
-                        cC0 += (wx0 - wx1) + (wy0 - wy1) - wz;
-                        cC1 += (wx2 - wx3) + (wy2 - wy3) + wz;
-                    }
-                }
-                const size_t base = (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)k));
-                const float *gt = md.gtop + (size_t)L * ((size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1));
-                double tn0 = 0.0, tn1 = 0.0;
+                        const double tvd = tv1 * slim * md.diff1 * rdza * md.dt * rdza;
+                        dmax_l = fmax(dmax_l, tvd);
+                        // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
+                        const double c0 = mj[2 * mjn + j] * 0.25 * slim * md.diff1 * rdzrho * rdzrho;
+                        const double two_dz = 2.0 * dzrho * c0;
+                        double wx[4], wy[4];
 #pragma unroll
-                for (int l = 0; l < LMAX; ++l) {
-                    if (l < L) {
-                        const int sl = s_scale[l];
-                        const float Tc = Sk[cidx * LP + l];
-                        const float TE = Sk[(cidx + 1) * LP + l];
-                        const float TW = Sk[(cidx - 1) * LP + l];
-                        const float TN = Sk[(cidx + nx) * LP + l];
-                        const float TS = Sk[(cidx - nx) * LP + l];
-                        const float ge = fmaf(Ae, TE, Be * Tc);
-                        const float gw = fmaf(Aw, Tc, Bw * TW);
-                        const float gn = fmaf(An, TN, Bn * Tc);
-                        const float gs = fmaf(As, Tc, Bs * TS);
-                        float ga;
-                        if (top) {
-                            ga = __ldg(gt + l) * __int_as_float((127 + sl) << 23);
-                        } else {
-                            const float TU = Su[cidx * LP + l];
-                            ga = fmaf(cC1, TU, cC0 * Tc);
-                            if (iso) {
-                                ga = fmaf(cW0, TW, ga);
-                                ga = fmaf(cE0, TE, ga);
-                                ga = fmaf(cS0, TS, ga);
-                                ga = fmaf(cN0, TN, ga);
-                                ga = fmaf(cW1, Su[(cidx - 1) * LP + l], ga);
-                                ga = fmaf(cE1, Su[(cidx + 1) * LP + l], ga);
-                                ga = fmaf(cS1, Su[(cidx - nx) * LP + l], ga);
-                                ga = fmaf(cN1, Su[(cidx + nx) * LP + l], ga);
-                            }
+                        for (int n = 0; n < 4; ++n) {
+                            wx[n] = two_dz * dxr[n] * mx[n];
+                            wy[n] = two_dz * dyr[n] * my[n];
                         }
-                        gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga))));
-                        const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
-                        const int qn = __float2int_rn(gn), qs = __float2int_rn(gs);
-                        const int qa = __float2int_rn(ga);
-                        const int sum = (qw - qe) + (qs - qn) + (qb[l] - qa);
-                        qb[l] = qa;
-                        const double told = __ldg(R + base + l);
-                        const double tnew = fma(i2d_scaled(sum, sl), rv, told);
-                        W[base + l] = tnew;
-                        if (((unsigned)__double2hiint(tnew) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
-                        if (l == 0) tn0 = tnew;
-                        if (l == 1) tn1 = tnew;
+                        const double wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
+                        const double c0d = f2d_scaled(BaX.hi, 0) + f2d_scaled(BaX.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
+                        const double c1d = f2d_scaled(AaX.hi, 0) + f2d_scaled(AaX.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
+                        C0X = df_split(c0d);
+                        C1X = df_split(c1d);
+                        W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
+                        S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
                     }
                 }
-                // FP32 density prescreen for the exact convective adjustment
-                const float tf = d2f_scaled(tn0, 0), sf = d2f_scaled(tn1, 0);
-                const float rf = eos_f(ecf, tf, sf);
-                if (k > k1c) {
-                    const float margin = 2.0e-6f * (fabsf(rf) + fabsf(rho_prev) + fabsf(ecf[0] * tf) +
-                                                    fabsf(ecf[1] * sf) + fabsf(ecf[2] * tf * tf) +
-                                                    fabsf(ecf[3] * tf * tf * tf)) + 1.0e-30f;
-                    if (!(rho_prev - rf > margin)) unstable = true;
+                const float *gt = md.gtop + (size_t)(L + 2) * ((size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1));
+
+                // T and S: double-float transfers
+#pragma unroll
+                for (int l = 0; l < 2; ++l) {
+                    const dflt Tc = {Sk[cidx * LP + l], SkL[cidx * 2 + l]};
+                    const dflt TE = {Sk[(cidx + 1) * LP + l], SkL[(cidx + 1) * 2 + l]};
+                    const dflt TW = {Sk[(cidx - 1) * LP + l], SkL[(cidx - 1) * 2 + l]};
+                    const dflt TN = {Sk[(cidx + nx) * LP + l], SkL[(cidx + nx) * 2 + l]};
+                    const dflt TS = {Sk[(cidx - nx) * LP + l], SkL[(cidx - nx) * 2 + l]};
+                    const dflt Ge = df_dot2(AeX, TE, BeX, Tc);
+                    const dflt Gw = df_dot2(AwX, Tc, BwX, TW);
+                    const dflt Gn = df_dot2(AnX, TN, BnX, Tc);
+                    const dflt Gs = df_dot2(AsX, Tc, BsX, TS);
+                    dflt Ga;
+                    if (top) {
+                        const float sc = __int_as_float((127 + s_scale[l]) << 23);
+                        Ga = {__ldg(gt + l) * sc, __ldg(gt + L + l) * sc};
+                    } else {
+                        const dflt TU = {Su[cidx * LP + l], SuL[cidx * 2 + l]};
+                        Ga = df_dot2(C1X, TU, C0X, Tc);
+                        if (iso) {
+                            Ga = df_add(Ga, df_dot2(W0X, TW, E0X, TE));
+                            Ga = df_add(Ga, df_dot2(S0X, TS, N0X, TN));
+                            const dflt TW1 = {Su[(cidx - 1) * LP + l], SuL[(cidx - 1) * 2 + l]};
+                            const dflt TE1 = {Su[(cidx + 1) * LP + l], SuL[(cidx + 1) * 2 + l]};
+                            const dflt TS1 = {Su[(cidx - nx) * LP + l], SuL[(cidx - nx) * 2 + l]};
+                            const dflt TN1 = {Su[(cidx + nx) * LP + l], SuL[(cidx + nx) * 2 + l]};
+                            Ga = df_add(Ga, df_dot2(W1X, TW1, E1X, TE1));
+                            Ga = df_add(Ga, df_dot2(S1X, TS1, N1X, TN1));
+                        }
+                    }
+                    float *qb = QBD + cell * 4 + 2 * l;
+                    const dflt Gb = {qb[0], qb[1]};
+                    const dflt sum = df_add(df_add(df_sub(Gw, Ge), df_sub(Gs, Gn)), df_sub(Gb, Ga));
+                    qb[0] = Ga.hi;
+                    qb[1] = Ga.lo;
+                    QSD[cell * 4 + 2 * l] = sum.hi;
+                    QSD[cell * 4 + 2 * l + 1] = sum.lo;
                 }
-                rho_prev = rf;
+                // other tracers: FP32 transfers rounded once to int32
+                const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
+                const float As = AsX.hi, Bs = BsX.hi;
+                const float cC0 = C0X.hi, cC1 = C1X.hi, cW0 = W0X.hi, cE0 = E0X.hi, cS0 = S0X.hi, cN0 = N0X.hi;
+                const float cW1 = W1X.hi, cE1 = E1X.hi, cS1 = S1X.hi, cN1 = N1X.hi;
+                int *qb = QB + cell * LP;
+                int *qs = QS + cell * LP;
+                const unsigned amask = __activemask();
+                for (int l = 2; l < L; ++l) {
+                    const float Tc = Sk[cidx * LP + l];
+                    const float TE = Sk[(cidx + 1) * LP + l];
+                    const float TW = Sk[(cidx - 1) * LP + l];
+                    const float TN = Sk[(cidx + nx) * LP + l];
+                    const float TS = Sk[(cidx - nx) * LP + l];
+                    const float ge = fmaf(Ae, TE, Be * Tc);
+                    const float gw = fmaf(Aw, Tc, Bw * TW);
+                    const float gn = fmaf(An, TN, Bn * Tc);
+                    const float gs = fmaf(As, Tc, Bs * TS);
+                    float ga;
+                    if (top) {
+                        ga = __ldg(gt + l) * __int_as_float((127 + s_scale[l]) << 23);
+                    } else {
+                        const float TU = Su[cidx * LP + l];
+                        ga = fmaf(cC1, TU, cC0 * Tc);
+                        if (iso) {
+                            ga = fmaf(cW0, TW, ga);
+                            ga = fmaf(cE0, TE, ga);
+                            ga = fmaf(cS0, TS, ga);
+                            ga = fmaf(cN0, TN, ga);
+                            ga = fmaf(cW1, Su[(cidx - 1) * LP + l], ga);
+                            ga = fmaf(cE1, Su[(cidx + 1) * LP + l], ga);
+                            ga = fmaf(cS1, Su[(cidx - nx) * LP + l], ga);
+                            ga = fmaf(cN1, Su[(cidx + nx) * LP + l], ga);
+                        }
+                    }
+                    const float gm = fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga)));
+                    gmax = fmaxf(gmax, gm);
+                    // per-tracer maximum for the next step's scale: one shared atomic per warp
+                    const unsigned wmax = __reduce_max_sync(amask, __float_as_uint(gm));
+                    if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[l], wmax);
+                    const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
+                    const int qn = __float2int_rn(gn), qs_ = __float2int_rn(gs);
+                    const int qa = __float2int_rn(ga);
+                    qs[l] = (qw - qe) + (qs_ - qn) + (qb[l] - qa);
+                    qb[l] = qa;
+                }
             }
+            cp_async_wait_all();
             __syncthreads();
+            // ---- phase B: FP64 update of the tile's wet cells at level k, row by row (coalesced)
+            {
+                const int rowlen = TX * L;
+                const int dc = 32 / L, dl = 32 % L;
+                for (int r = warp; r < TY; r += nwarp) {
+                    const int jr = j0 + r;
+                    if (jr > maxj) continue;
+                    const double rv = __ldg(md.rvol + (size_t)(jr - 1) + (size_t)maxj * (size_t)(k - 1));
+                    const size_t rowbase = (size_t)NI * ((size_t)jr + (size_t)NJ * (size_t)k);
+                    int c = lane / L, l = lane % L;
+                    for (int e = lane; e < rowlen; e += 32) {
+                        const int ic = i0 + c;
+                        if (ic <= maxi && k >= k1t[(r + 1) * nx + c + 1]) {
+                            const size_t g = ((size_t)ic + rowbase) * L + l;
+                            const double told = R[g];
+                            const int cc = r * TX + c;
+                            double dlt;
+                            if (l < 2) {
+                                const int sl = s_scale[l];
+                                dlt = f2d_scaled(QSD[cc * 4 + 2 * l], sl) + f2d_scaled(QSD[cc * 4 + 2 * l + 1], sl);
+                            } else {
+                                dlt = i2d_scaled(QS[cc * LP + l], s_scale[l]);
+                            }
+                            const double tnew = fma(dlt, rv, told);
+                            W[g] = tnew;
+                            if (((unsigned)__double2hiint(tnew) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
+                            if (l < 2) TSN[cc * 2 + l] = d2f_scaled(tnew, 0);
+                        }
+                        c += dc;
+                        l += dl;
+                        if (l >= L) {
+                            l -= L;
+                            c += 1;
+                        }
+                    }
+                }
+            }
+            if (k + 2 <= maxk) convert((k & 1) ? F1 : F0, (k & 1) ? G1 : G0);
+            __syncthreads();
+            if (k + 3 <= maxk) issue(k + 3);
         }
+        if (inside && maxk >= k1c) prescreen(maxk);
 
         // exact convective adjustment of columns that may be unstable
         if (inside && k1c <= maxk) {
@@ -384,8 +608,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                 EosCoef ec;
                 for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
                 ec.ieos = md.ieos;
-                const double *dz = md.mk, *rdz = md.mk + (maxk + 2), *zw = md.mk + 2 * (maxk + 2),
-                             *zro = md.mk + 3 * (maxk + 2);
+                const double *dz = mk, *rdz = mk + mkn, *zw = mk + 2 * mkn, *zro = mk + 3 * mkn;
                 col.rho[0] = 0.0;
                 for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
                 int icos = 0;
@@ -404,44 +627,63 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         }
         if (md.diso) {
             unsigned long long *dg = md.diag + 2 * (step & 1);
-            unsigned long long db = __double_as_longlong((double)dmax_l);
+            unsigned long long db = __double_as_longlong(dmax_l);
             if (db) atomicMax(&dg[0], db);
             if (limps_l) atomicAdd(&dg[1], (unsigned long long)limps_l);
         }
-        if (nonfinite || gmax > 3.0e8f) atomicOr(md.status, (nonfinite ? 1u : 0u) | (gmax > 3.0e8f ? 2u : 0u));
+        // a scaled transfer above 3.5e8 could overflow the int32 sum of six faces
+        if (nonfinite || gmax > 3.5e8f) atomicOr(md.status, (nonfinite ? 1u : 0u) | (gmax > 3.5e8f ? 2u : 0u));
         __syncthreads();
+        for (int l = 2 + t; l < L; l += blockDim.x)
+            if (s_gmax[l]) atomicMax(&md.gmax[l], s_gmax[l]);
     }
 }
 
-int fp32_smem_bytes(int tile_i, int tile_j, int L)
+// After a step: move each tracer's scale so that the step's largest transfer would
+// have landed in [2^25, 2^26); clear the maxima.  T and S (double-float) keep theirs.
+__global__ void k_rescale(const MemberDesc *__restrict__ mds, int n)
 {
-    const int nx = tile_i + 2, ny = tile_j + 2;
-    const int LP = L | 1;
-    return ((nx * ny * 4 + 15) & ~15) + 3 * nx * ny * LP * 4;
+    for (int m = blockIdx.x; m < n; m += gridDim.x) {
+        const MemberDesc &md = mds[m];
+        for (int l = 2 + threadIdx.x; l < md.L; l += blockDim.x) {
+            const unsigned gb = md.gmax[l];
+            if (gb == 0u) continue;
+            const int e = (int)((gb >> 23) & 0xff) - 127;      // floor(log2(max |scaled transfer|))
+            int s = md.scale[l] + (25 - e);
+            s = s < -120 ? -120 : (s > 120 ? 120 : s);
+            md.scale[l] = s;
+            md.gmax[l] = 0u;
+        }
+    }
 }
+
+int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    k_rescale<<<std::min(n, 1024), 32, 0, s>>>(descs, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+}
+
+int fp32_smem_bytes(int tile_i, int tile_j, int L) { return fp32_smem_layout(tile_i, tile_j, L).total; }
 
 int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int lmax, int smem_bytes,
                 const long long *step_ctr, int rel, cudaStream_t s)
 {
+    (void)lmax;
     static int nsm = 0;
     if (!nsm) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    auto go = [&](auto kern) -> int {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
-        if (per_sm < 1) per_sm = 1;
-        int grid = std::min(nitems, nsm * per_sm);
-        if (grid < 1) grid = 1;
-        kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel);
-        return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
-    };
-    if (lmax <= 8) return go(k_step_fp32<8>);
-    if (lmax <= 16) return go(k_step_fp32<16>);
-    return go(k_step_fp32<32>);
+    cudaFuncSetAttribute(k_step_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_fp32, kFp32Threads, smem_bytes);
+    if (per_sm < 1) per_sm = 1;
+    int grid = std::min(nitems, nsm * per_sm);
+    if (grid < 1) grid = 1;
+    k_step_fp32<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel);
+    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
 void fp32_default_tile(int maxi, int maxj, int *ti, int *tj)
@@ -483,7 +725,7 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     const double *dz = kb, *dza = kb + nk, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk,
                  *dt = kb + 5 * nk, *zw = kb + 6 * nk, *ssmax = kb + 7 * nk;
     const size_t ncell = (size_t)maxi * maxj * maxk;
-    out.coef.assign(6 * ncell, 0.0f);
+    out.coef.assign(12 * ncell, 0.0f);
     out.rvol.assign((size_t)maxj * maxk, 0.0);
     out.cmax = 0.0;
     auto U = [&](int c, int i, int j, int k) -> double {
@@ -494,71 +736,76 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
         for (int j = 1; j <= maxj; ++j) {
             out.rvol[(size_t)(j - 1) + (size_t)maxj * (k - 1)] = 1.0 / (p.dphi * ds[j] * dz[k]);
             for (int i = 1; i <= maxi; ++i) {
-                float *c = &out.coef[6 * ((size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1)))];
+                float *c = &out.coef[12 * ((size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1)))];
+                double cd[6] = {0, 0, 0, 0, 0, 0};
                 const int k1c = K1(i, j);
                 const int ie = (i == maxi) ? 1 : i + 1;
                 if (k >= std::max(k1c, K1(ie, j))) {
                     const double u1 = U(0, i, j, k);
                     const double pec = u1 * p.dphi / p.diff1, ups = pec / (2.0 + std::fabs(pec));
                     const double g = dt[k] * ds[j] * dz[k], a = u1 * rc[j];
-                    c[0] = (float)(g * (a * (1.0 - ups) * 0.5 - rc2[j] * p.diff1));
-                    c[1] = (float)(g * (a * (1.0 + ups) * 0.5 + rc2[j] * p.diff1));
+                    cd[0] = g * (a * (1.0 - ups) * 0.5 - rc2[j] * p.diff1);
+                    cd[1] = g * (a * (1.0 + ups) * 0.5 + rc2[j] * p.diff1);
                 }
                 if (k >= std::max(k1c, K1(i, j + 1))) {
                     const double u2 = U(1, i, j, k);
                     const double pec = u2 * dsv[std::min(j, maxj - 1)] / p.diff1, ups = pec / (2.0 + std::fabs(pec));
                     const double g = dt[k] * p.dphi * dz[k], a = cv[j] * u2;
-                    c[2] = (float)(g * (a * (1.0 - ups) * 0.5 - cv2[j] * p.diff1));
-                    c[3] = (float)(g * (a * (1.0 + ups) * 0.5 + cv2[j] * p.diff1));
+                    cd[2] = g * (a * (1.0 - ups) * 0.5 - cv2[j] * p.diff1);
+                    cd[3] = g * (a * (1.0 + ups) * 0.5 + cv2[j] * p.diff1);
                 }
                 if (k >= k1c && k < maxk) {
                     const double u3 = U(2, i, j, k);
                     const double pec = u3 * dza[k] / p.diff2, ups = pec / (2.0 + std::fabs(pec));
                     const double g = dt[k] * p.dphi * ds[j];
-                    c[4] = (float)(g * (u3 * (1.0 - ups) * 0.5 - rdza[k] * p.diff2));
-                    c[5] = (float)(g * (u3 * (1.0 + ups) * 0.5 + rdza[k] * p.diff2));
+                    cd[4] = g * (u3 * (1.0 - ups) * 0.5 - rdza[k] * p.diff2);
+                    cd[5] = g * (u3 * (1.0 + ups) * 0.5 + rdza[k] * p.diff2);
+                }
+                for (int n = 0; n < 6; ++n) {
+                    c[n] = (float)cd[n];
+                    c[6 + n] = (float)(cd[n] - (double)c[n]);
                 }
                 for (int f = 0; f < 3; ++f)
                     out.cmax = std::max(out.cmax, (double)std::fabs(c[2 * f]) + (double)std::fabs(c[2 * f + 1]));
             }
         }
     }
-    out.mk.assign(5 * (size_t)nk, 0.0);
+    out.mk.assign(6 * (size_t)nk, 0.0);
     for (int k = 0; k <= maxk + 1; ++k) {
         out.mk[k] = dz[k];
         out.mk[nk + k] = rdz[k];
         out.mk[2 * nk + k] = zw[k];
         out.mk[3 * nk + k] = zro[k];
         out.mk[4 * nk + k] = rdza[k];
+        out.mk[5 * nk + k] = ssmax[k];
     }
-    out.fj.assign(4 * (size_t)nj, 0.0f);
-    for (int j = 0; j <= maxj + 1; ++j) {
-        if (j <= maxj) out.fj[j] = (float)(rc[j] * p.rdphi);
-        if (j <= maxj) out.fj[nj + j] = (float)(cv[j] * rdsv[j]);
-        if (j >= 1 && j <= maxj) out.fj[2 * nj + j] = (float)(dt[1] * p.dphi * ds[j]);
-    }
-    out.fk.assign(3 * (size_t)nk, 0.0f);
-    for (int k = 0; k <= maxk + 1; ++k) {
-        out.fk[k] = (float)rdza[k];
-        out.fk[nk + k] = (float)zw[k];
-        out.fk[2 * nk + k] = (float)ssmax[k];
+    out.mj.assign(3 * (size_t)nj, 0.0);
+    for (int j = 0; j <= maxj; ++j) {
+        out.mj[j] = rc[j] * p.rdphi;
+        out.mj[nj + j] = cv[j] * rdsv[j];
+        if (j >= 1) out.mj[2 * nj + j] = dt[1] * p.dphi * ds[j];
     }
 }
 
 void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top,
                std::vector<float> &gtop)
 {
-    // transfer through the surface face: dt*dphi*ds(j)*ts(l,i,j,maxk+1)
+    // transfer through the surface face: dt*dphi*ds(j)*ts(l,i,j,maxk+1); per column the FP32
+    // value of every tracer, then the FP64 remainders of T and S
     const int maxi = d.maxi, maxj = d.maxj, L = d.L, NI = d.NI;
     const int nj = maxj + 2, nk = d.maxk + 2;
     const double *ds = blob.data() + 6 * nj;
     const double dt = blob.data()[8 * nj + 5 * nk + 1];
-    gtop.assign((size_t)L * maxi * maxj, 0.0f);
+    gtop.assign((size_t)(L + 2) * maxi * maxj, 0.0f);
     for (int j = 1; j <= maxj; ++j)
-        for (int i = 1; i <= maxi; ++i)
-            for (int l = 0; l < L; ++l)
-                gtop[(size_t)l + (size_t)L * ((size_t)(i - 1) + (size_t)maxi * (j - 1))] =
-                    (float)(dt * p.dphi * ds[j] * top[(size_t)l + (size_t)L * ((size_t)i + (size_t)NI * j)]);
+        for (int i = 1; i <= maxi; ++i) {
+            float *g = &gtop[(size_t)(L + 2) * ((size_t)(i - 1) + (size_t)maxi * (j - 1))];
+            for (int l = 0; l < L; ++l) {
+                const double v = dt * p.dphi * ds[j] * top[(size_t)l + (size_t)L * ((size_t)i + (size_t)NI * j)];
+                g[l] = (float)v;
+                if (l < 2) g[L + l] = (float)(v - (double)g[l]);
+            }
+        }
 }
 
 void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax, const float *gtop,
@@ -575,7 +822,7 @@ void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax
             }
     if (gtop)
         for (size_t n = 0; n < (size_t)maxi * maxj; ++n)
-            for (int l = 0; l < L; ++l) gmax[l] = std::max(gmax[l], (double)std::fabs(gtop[n * L + l]));
+            for (int l = 0; l < L; ++l) gmax[l] = std::max(gmax[l], (double)std::fabs(gtop[n * (L + 2) + l]));
     scale.assign(L, 0);
     for (int l = 0; l < L; ++l) {
         // largest transfer the step can produce: (|A|+|B|)*max|T| per face; the
@@ -697,13 +944,14 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     D.tile_i = ti;
     D.tile_j = tj;
     const size_t ncell = (size_t)d.maxi * d.maxj * d.maxk;
-    cudaError_t e = cudaMalloc(&D.coef, 6 * ncell * sizeof(float));
+    cudaError_t e = cudaMalloc(&D.coef, 12 * ncell * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.rvol, (size_t)d.maxj * d.maxk * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&D.gtop, (size_t)d.L * d.maxi * d.maxj * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&D.gtop, (size_t)(d.L + 2) * d.maxi * d.maxj * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.scale, (size_t)d.L * sizeof(int32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&D.mk, 5 * (size_t)nk * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&D.fj, 4 * (size_t)nj * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&D.fk, 3 * (size_t)nk * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&D.gmax, (size_t)d.L * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(D.gmax, 0, (size_t)d.L * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.mk, 6 * (size_t)nk * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&D.mj, 3 * (size_t)nj * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&D.dev, sizeof(MemberDesc));
     if (e == cudaSuccess) e = cudaMalloc(&D.step_ctr, sizeof(long long));
@@ -718,7 +966,7 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(D.status, 0, sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(D.gtop, 0, (size_t)d.L * d.maxi * d.maxj * sizeof(float), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.gtop, 0, (size_t)(d.L + 2) * d.maxi * d.maxj * sizeof(float), s);
     f->impl = h;
     f->ready = true;
     if (e != cudaSuccess) {
@@ -735,8 +983,8 @@ void fp32_member_free(Fp32Member *f)
     if (!f || !f->impl) return;
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
-    cudaFree(D.coef); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.mk); cudaFree(D.fj);
-    cudaFree(D.fk); cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr);
+    cudaFree(D.coef); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
+    cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr);
     delete h;
     f->impl = nullptr;
     f->ready = false;
@@ -786,8 +1034,7 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s
     cudaError_t e = cudaMemcpyAsync(D.coef, st.coef.data(), st.coef.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.rvol, st.rvol.data(), st.rvol.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.mk, st.mk.data(), st.mk.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(D.fj, st.fj.data(), st.fj.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(D.fk, st.fk.data(), st.fk.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(D.mj, st.mj.data(), st.mj.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_ok(e);
     h->have_vel = true;
@@ -813,8 +1060,8 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.buf[0] = ts_buf[0];
         md.buf[1] = ts_buf[1];
         md.ts_static = ts_static;
-        md.coef = D.coef; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale;
-        md.mk = D.mk; md.fj = D.fj; md.fk = D.fk; md.cost = cost; md.icosd = icosd;
+        md.coef = D.coef; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
+        md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
         md.status = D.status;
         md.diag = diag;
         if (cudaMemcpyAsync(D.dev, &md, sizeof(md), cudaMemcpyHostToDevice, s) != cudaSuccess) return GB_GO_ECUDA;
@@ -831,8 +1078,9 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         if (cudaMemsetAsync(diag + 2 * (step & 1), 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
             return GB_GO_ECUDA;
         int r = fp32_launch(D.dev, D.items, D.nitems, h->d.L, smem, D.step_ctr, n, s);
+        if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;
-        count_launches(1);
+        count_launches(2);
     }
     D.steps += nsteps;
     *cur = (int)(D.steps & 1);
