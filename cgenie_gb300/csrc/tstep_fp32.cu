@@ -152,39 +152,38 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Dynamic shared memory of one work item (byte offsets, 16-byte aligned).
+// Tracers per march of a tile: shared memory (and so CTAs per SM) scales with it.
+constexpr int kGroup = 8;
+
+// Dynamic shared memory of one work item, for tracer groups of up to kGroup
+// (byte offsets, 16-byte aligned).  ncp = nc | 1 (odd pitch: conflict-free).
 struct Fp32Smem {
-    int stage;   // double[nc*L]   FP64 slab in flight (cp.async)
-    int f0, f1;  // float[nc*LP]   scaled FP32 slabs of levels k and k+1 (hi parts for T,S)
-    int g0, g1;  // float[nc*2]    lo parts of T and S for the two slabs
-    int qb, qs;  // int[nin*LP]    bottom-face carry, per-level transfer sum (tracers >= 3)
-    int qbd, qsd;// float[nin*4]   the same for T and S as double-floats
-    int tsn;     // float[nin*2]   new T and S of the level just updated
-    int k1t;     // int[nc]        k1 with a one-cell halo
+    int stage;   // double[nc*G]      FP64 slab of one tracer group in flight (cp.async)
+    int f;       // float[3][G][ncp]  scaled FP32 slabs of levels k, k+1, k+2 (tracer-major)
+    int fl;      // float[3][2][ncp]  lo parts of T and S for the three slabs
+    int qb;      // int[G][nin]       bottom-face carry of the group's tracers
+    int qbd;     // float[2][2][nin]  the same for T and S as double-floats
+    int k1t;     // int[nc]           k1 with a one-cell halo
     int total;
 };
 
 __host__ __device__ inline Fp32Smem fp32_smem_layout(int TX, int TY, int L)
 {
-    const int nc = (TX + 2) * (TY + 2), LP = L | 1, nin = TX * TY;
+    const int nc = (TX + 2) * (TY + 2), ncp = nc | 1, nin = TX * TY;
+    const int G = L < kGroup ? L : kGroup;
     Fp32Smem s;
     int o = 0;
-    s.stage = o; o += (nc * L * 8 + 15) & ~15;
-    s.f0 = o; o += (nc * LP * 4 + 15) & ~15;
-    s.f1 = o; o += (nc * LP * 4 + 15) & ~15;
-    s.g0 = o; o += (nc * 2 * 4 + 15) & ~15;
-    s.g1 = o; o += (nc * 2 * 4 + 15) & ~15;
-    s.qb = o; o += (nin * LP * 4 + 15) & ~15;
-    s.qs = o; o += (nin * LP * 4 + 15) & ~15;
-    s.qbd = o; o += (nin * 4 * 4 + 15) & ~15;
-    s.qsd = o; o += (nin * 4 * 4 + 15) & ~15;
-    s.tsn = o; o += (nin * 2 * 4 + 15) & ~15;
+    s.stage = o; o += (nc * G * 8 + 15) & ~15;
+    s.f = o; o += (3 * G * ncp * 4 + 15) & ~15;
+    s.fl = o; o += (3 * 2 * ncp * 4 + 15) & ~15;
+    s.qb = o; o += (G * nin * 4 + 15) & ~15;
+    s.qbd = o; o += (4 * nin * 4 + 15) & ~15;
     s.k1t = o; o += (nc * 4 + 15) & ~15;
     s.total = o;
     return s;
 }
 
-__global__ void __launch_bounds__(kFp32Threads, 4)
+__global__ void __launch_bounds__(kFp32Threads, 5)
 k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
             const long long *__restrict__ step_ctr, int rel)
 {
@@ -195,6 +194,8 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
     const int t = threadIdx.x;
     const int warp = t >> 5, lane = t & 31, nwarp = blockDim.x >> 5;
     const long long step = *step_ctr + rel;
+    // every 4th step the per-tracer transfer maxima are gathered to re-target the scales
+    const bool track = (step & 3) == 0;
 
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int4 item = items[it];
@@ -209,18 +210,13 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             dn[1] = 0ull;
         }
         const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
-        const int nx = TX + 2, ny = TY + 2, nc = nx * ny, LP = L | 1, nin = TX * TY;
+        const int nx = TX + 2, ny = TY + 2, nc = nx * ny, ncp = nc | 1, nin = TX * TY;
         const Fp32Smem lay = fp32_smem_layout(TX, TY, L);
         double *stage = reinterpret_cast<double *>(smraw + lay.stage);
-        float *F0 = reinterpret_cast<float *>(smraw + lay.f0);
-        float *F1 = reinterpret_cast<float *>(smraw + lay.f1);
-        float *G0 = reinterpret_cast<float *>(smraw + lay.g0);
-        float *G1 = reinterpret_cast<float *>(smraw + lay.g1);
+        float *Fb = reinterpret_cast<float *>(smraw + lay.f);
+        float *FLb = reinterpret_cast<float *>(smraw + lay.fl);
         int *QB = reinterpret_cast<int *>(smraw + lay.qb);
-        int *QS = reinterpret_cast<int *>(smraw + lay.qs);
         float *QBD = reinterpret_cast<float *>(smraw + lay.qbd);
-        float *QSD = reinterpret_cast<float *>(smraw + lay.qsd);
-        float *TSN = reinterpret_cast<float *>(smraw + lay.tsn);
         int *k1t = reinterpret_cast<int *>(smraw + lay.k1t);
         const int par = (int)((step + md.parity) & 1);
         const double *__restrict__ R = md.buf[par];
@@ -228,6 +224,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         const double *mk = md.mk;
         const double *mj = md.mj;
         const int mkn = maxk + 2, mjn = maxj + 2;
+        const int Gmax = L < kGroup ? L : kGroup;
 
         // k1 tile with a one-column halo (periodic in i), land outside the grid
         if (t == 0) s_kstart = 1 << 20;
@@ -246,8 +243,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             s_scale[l] = md.scale[l];
             s_gmax[l] = 0u;
         }
-        for (int e = t; e < nin * LP; e += blockDim.x) QB[e] = 0;
-        for (int e = t; e < nin * 4; e += blockDim.x) QBD[e] = 0.0f;
         __syncthreads();
         const int ti = t % TX, tj = t / TX;
         const int i = i0 + ti, j = j0 + tj;
@@ -263,59 +258,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             continue;
         }
 
-        // cp.async the FP64 slab of level `lev` (rows of the tile plus halo) into stage
-        auto issue = [&](int lev) {
-            const int dc = 32 / L, dl = 32 % L;
-            const int rowlen = nx * L;
-            for (int r = warp; r < ny; r += nwarp) {
-                const int gj = j0 - 1 + r;
-                double *Srow = stage + (size_t)r * rowlen;
-                if (gj > maxj + 1) {
-                    for (int e = lane; e < rowlen; e += 32) Srow[e] = 0.0;
-                    continue;
-                }
-                const size_t rowbase = (size_t)NI * ((size_t)gj + (size_t)NJ * (size_t)lev);
-                int c = lane / L, l = lane % L;
-                for (int e = lane; e < rowlen; e += 32) {
-                    int gi = i0 - 1 + c;
-                    if (gi <= maxi + 1) {
-                        if (gi == 0) gi = maxi;
-                        else if (gi == maxi + 1) gi = 1;
-                        cp_async8(Srow + e, R + ((size_t)gi + rowbase) * L + l);
-                    } else {
-                        Srow[e] = 0.0;
-                    }
-                    c += dc;
-                    l += dl;
-                    if (l >= L) {
-                        l -= L;
-                        c += 1;
-                    }
-                }
-            }
-            cp_async_commit();
-        };
-        // stage -> FP32 slab scaled by 2^s_l (tracer stride LP, odd: no bank conflicts);
-        // T and S also keep the truncated remainder as an FP32 lo part
-        auto convert = [&](float *dst, float *dlo) {
-            const int total = nc * L;
-            const int dc = kFp32Threads / L, dl = kFp32Threads % L;
-            int c = t / L, l = t % L;
-            for (int e = t; e < total; e += kFp32Threads) {
-                const double x = stage[e];
-                const int sl = s_scale[l];
-                const float h = d2f_scaled(x, sl);
-                dst[c * LP + l] = h;
-                if (l < 2) dlo[c * 2 + l] = d2f_scaled(x - f2d_scaled(h, sl), sl);
-                c += dc;
-                l += dl;
-                if (l >= L) {
-                    l -= L;
-                    c += 1;
-                }
-            }
-        };
-
         float ecf[5];
         for (int n = 0; n < 5; ++n) ecf[n] = (float)md.ec[n];
         float rho_prev = 0.0f;
@@ -325,272 +267,290 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         double dmax_l = 0.0;
         unsigned limps_l = 0;
 
-        auto prescreen = [&](int lev) {
-            // FP32 density of the updated level vs the level below: a column is left to
-            // the exact co unless every pair is stable by a margin above FP32 error
-            const float tf = TSN[cell * 2 + 0], sf = TSN[cell * 2 + 1];
-            const float rf = eos_f(ecf, tf, sf);
-            if (lev > k1c) {
-                const float margin = 2.0e-6f * (fabsf(rf) + fabsf(rho_prev) + fabsf(ecf[0] * tf) +
-                                                fabsf(ecf[1] * sf) + fabsf(ecf[2] * tf * tf) +
-                                                fabsf(ecf[3] * tf * tf * tf)) + 1.0e-30f;
-                if (!(rho_prev - rf > margin)) unstable = true;
-            }
-            rho_prev = rf;
-        };
+        for (int g0 = 0; g0 < L; g0 += Gmax) {
+            const int gl = (L - g0) < Gmax ? (L - g0) : Gmax;
+            const bool ts_group = (g0 == 0);
 
-        issue(kstart);
-        cp_async_wait_all();
-        __syncthreads();
-        convert((kstart & 1) ? F1 : F0, (kstart & 1) ? G1 : G0);
-        __syncthreads();
-        if (kstart + 1 <= maxk) {
-            issue(kstart + 1);
-            cp_async_wait_all();
-            __syncthreads();
-            convert(((kstart + 1) & 1) ? F1 : F0, ((kstart + 1) & 1) ? G1 : G0);
-            __syncthreads();
-        }
-        if (kstart + 2 <= maxk) issue(kstart + 2);
-
-        for (int k = kstart; k <= maxk; ++k) {
-            const float *Sk = (k & 1) ? F1 : F0;
-            const float *Su = (k & 1) ? F0 : F1;
-            const float *SkL = (k & 1) ? G1 : G0;
-            const float *SuL = (k & 1) ? G0 : G1;
-            if (inside && k - 1 >= k1c && k - 1 >= kstart) prescreen(k - 1);
-            // ---- phase A: transfers of the cell's faces
-            if (inside && k >= k1c) {
-                const size_t cl = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
-                const float *cf = md.coef + 12 * cl;
-                const int iw = (i == 1) ? maxi : i - 1;
-                const float *cw = md.coef + 12 * ((size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1)));
-                const dflt AeX = {__ldg(cf + 0), __ldg(cf + 6)}, BeX = {__ldg(cf + 1), __ldg(cf + 7)};
-                const dflt AnX = {__ldg(cf + 2), __ldg(cf + 8)}, BnX = {__ldg(cf + 3), __ldg(cf + 9)};
-                const dflt AaX = {__ldg(cf + 4), __ldg(cf + 10)}, BaX = {__ldg(cf + 5), __ldg(cf + 11)};
-                const dflt AwX = {__ldg(cw + 0), __ldg(cw + 6)}, BwX = {__ldg(cw + 1), __ldg(cw + 7)};
-                dflt AsX = {0.0f, 0.0f}, BsX = {0.0f, 0.0f};
-                if (j > 1) {
-                    const float *cs = md.coef + 12 * (cl - (size_t)maxi);
-                    AsX = {__ldg(cs + 2), __ldg(cs + 8)};
-                    BsX = {__ldg(cs + 3), __ldg(cs + 9)};
-                }
-                const bool top = (k == maxk);
-                bool iso = false;
-                // top-face stencil: C1*T(k+1) + C0*T(k) (+ isoneutral corners)
-                dflt C1X = AaX, C0X = BaX;
-                dflt W0X = {0.f, 0.f}, E0X = {0.f, 0.f}, S0X = {0.f, 0.f}, N0X = {0.f, 0.f};
-                dflt W1X = {0.f, 0.f}, E1X = {0.f, 0.f}, S1X = {0.f, 0.f}, N1X = {0.f, 0.f};
-                if (md.diso && !top) {
-                    // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
-                    // state: the density differences scc*dS - tec*dT cancel strongly in weakly
-                    // stratified water; they are differences of D = ec(2)*S - tec*T with the
-                    // cell's tec (goldstein.f90:2587-2588)
-                    auto ld = [&](int ii, int jj, int kk, int l) {
-                        return __ldg(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
-                    };
-                    const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
-                    const double s1 = ld(i, j, k, 1), s2 = ld(i, j, k + 1, 1);
-                    const double tatw = 0.5 * (t1 + t2);
-                    double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
-                    if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
-                    const double scc = md.ec[1];
-                    const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
-                    const double rdza = mk[4 * mkn + k];
-                    const double dzrho = (Dc1 - Dc0) * rdza;
-                    if (dzrho < -1.0e-12) {
-                        iso = true;
-                        const double rdzrho = 1.0 / dzrho;
-                        const double rcr = mj[j];                          // rc(j)*rdphi
-                        const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
-                        const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
-                        double dxr[4], dyr[4], mx[4], my[4];
-                        double tv1 = 0.0;
-#pragma unroll
-                        for (int knp = 0; knp <= 1; ++knp) {
-                            const double Dck = knp ? Dc1 : Dc0;
-#pragma unroll
-                            for (int nnp = 0; nnp <= 1; ++nnp) {
-                                const int ina = nnp + 2 * knp;
-                                const int kk = k + knp;
-                                const bool okx = kk >= k1t[cidx + (nnp ? 1 : -1)];
-                                const bool oky = kk >= k1t[cidx + (nnp ? nx : -nx)];
-                                mx[ina] = okx ? rcr : 0.0;
-                                my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
-                                dxr[ina] = 0.0;
-                                dyr[ina] = 0.0;
-                                if (okx) {
-                                    const int ii = nnp ? ip : im;
-                                    const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
-                                    dxr[ina] = (nnp ? Dn - Dck : Dck - Dn) * rcr;
-                                }
-                                if (oky) {
-                                    const int jj = nnp ? j + 1 : j - 1;
-                                    const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
-                                    dyr[ina] = (nnp ? Dn - Dck : Dck - Dn) * my[ina];
-                                }
-                                tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
-                            }
-                        }
-                        const double sum2 = tv1;
-                        tv1 = 0.25 * tv1 * rdzrho * rdzrho;
-                        const double ss = mk[5 * mkn + k];
-                        double slim = 1.0;
-                        if (tv1 > ss) {
-                            slim = ss * ss / (tv1 * tv1);
-                            limps_l += 1;
-                        }
-                        const double tvd = tv1 * slim * md.diff1 * rdza * md.dt * rdza;
-                        dmax_l = fmax(dmax_l, tvd);
-                        // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
-                        const double c0 = mj[2 * mjn + j] * 0.25 * slim * md.diff1 * rdzrho * rdzrho;
-                        const double two_dz = 2.0 * dzrho * c0;
-                        double wx[4], wy[4];
-#pragma unroll
-                        for (int n = 0; n < 4; ++n) {
-                            wx[n] = two_dz * dxr[n] * mx[n];
-                            wy[n] = two_dz * dyr[n] * my[n];
-                        }
-                        const double wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
-                        const double c0d = f2d_scaled(BaX.hi, 0) + f2d_scaled(BaX.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
-                        const double c1d = f2d_scaled(AaX.hi, 0) + f2d_scaled(AaX.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
-                        C0X = df_split(c0d);
-                        C1X = df_split(c1d);
-                        W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
-                        S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
-                    }
-                }
-                const float *gt = md.gtop + (size_t)(L + 2) * ((size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1));
-
-                // T and S: double-float transfers
-#pragma unroll
-                for (int l = 0; l < 2; ++l) {
-                    const dflt Tc = {Sk[cidx * LP + l], SkL[cidx * 2 + l]};
-                    const dflt TE = {Sk[(cidx + 1) * LP + l], SkL[(cidx + 1) * 2 + l]};
-                    const dflt TW = {Sk[(cidx - 1) * LP + l], SkL[(cidx - 1) * 2 + l]};
-                    const dflt TN = {Sk[(cidx + nx) * LP + l], SkL[(cidx + nx) * 2 + l]};
-                    const dflt TS = {Sk[(cidx - nx) * LP + l], SkL[(cidx - nx) * 2 + l]};
-                    const dflt Ge = df_dot2(AeX, TE, BeX, Tc);
-                    const dflt Gw = df_dot2(AwX, Tc, BwX, TW);
-                    const dflt Gn = df_dot2(AnX, TN, BnX, Tc);
-                    const dflt Gs = df_dot2(AsX, Tc, BsX, TS);
-                    dflt Ga;
-                    if (top) {
-                        const float sc = __int_as_float((127 + s_scale[l]) << 23);
-                        Ga = {__ldg(gt + l) * sc, __ldg(gt + L + l) * sc};
-                    } else {
-                        const dflt TU = {Su[cidx * LP + l], SuL[cidx * 2 + l]};
-                        Ga = df_dot2(C1X, TU, C0X, Tc);
-                        if (iso) {
-                            Ga = df_add(Ga, df_dot2(W0X, TW, E0X, TE));
-                            Ga = df_add(Ga, df_dot2(S0X, TS, N0X, TN));
-                            const dflt TW1 = {Su[(cidx - 1) * LP + l], SuL[(cidx - 1) * 2 + l]};
-                            const dflt TE1 = {Su[(cidx + 1) * LP + l], SuL[(cidx + 1) * 2 + l]};
-                            const dflt TS1 = {Su[(cidx - nx) * LP + l], SuL[(cidx - nx) * 2 + l]};
-                            const dflt TN1 = {Su[(cidx + nx) * LP + l], SuL[(cidx + nx) * 2 + l]};
-                            Ga = df_add(Ga, df_dot2(W1X, TW1, E1X, TE1));
-                            Ga = df_add(Ga, df_dot2(S1X, TS1, N1X, TN1));
-                        }
-                    }
-                    float *qb = QBD + cell * 4 + 2 * l;
-                    const dflt Gb = {qb[0], qb[1]};
-                    const dflt sum = df_add(df_add(df_sub(Gw, Ge), df_sub(Gs, Gn)), df_sub(Gb, Ga));
-                    qb[0] = Ga.hi;
-                    qb[1] = Ga.lo;
-                    QSD[cell * 4 + 2 * l] = sum.hi;
-                    QSD[cell * 4 + 2 * l + 1] = sum.lo;
-                }
-                // other tracers: FP32 transfers rounded once to int32
-                const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
-                const float As = AsX.hi, Bs = BsX.hi;
-                const float cC0 = C0X.hi, cC1 = C1X.hi, cW0 = W0X.hi, cE0 = E0X.hi, cS0 = S0X.hi, cN0 = N0X.hi;
-                const float cW1 = W1X.hi, cE1 = E1X.hi, cS1 = S1X.hi, cN1 = N1X.hi;
-                int *qb = QB + cell * LP;
-                int *qs = QS + cell * LP;
-                const unsigned amask = __activemask();
-                for (int l = 2; l < L; ++l) {
-                    const float Tc = Sk[cidx * LP + l];
-                    const float TE = Sk[(cidx + 1) * LP + l];
-                    const float TW = Sk[(cidx - 1) * LP + l];
-                    const float TN = Sk[(cidx + nx) * LP + l];
-                    const float TS = Sk[(cidx - nx) * LP + l];
-                    const float ge = fmaf(Ae, TE, Be * Tc);
-                    const float gw = fmaf(Aw, Tc, Bw * TW);
-                    const float gn = fmaf(An, TN, Bn * Tc);
-                    const float gs = fmaf(As, Tc, Bs * TS);
-                    float ga;
-                    if (top) {
-                        ga = __ldg(gt + l) * __int_as_float((127 + s_scale[l]) << 23);
-                    } else {
-                        const float TU = Su[cidx * LP + l];
-                        ga = fmaf(cC1, TU, cC0 * Tc);
-                        if (iso) {
-                            ga = fmaf(cW0, TW, ga);
-                            ga = fmaf(cE0, TE, ga);
-                            ga = fmaf(cS0, TS, ga);
-                            ga = fmaf(cN0, TN, ga);
-                            ga = fmaf(cW1, Su[(cidx - 1) * LP + l], ga);
-                            ga = fmaf(cE1, Su[(cidx + 1) * LP + l], ga);
-                            ga = fmaf(cS1, Su[(cidx - nx) * LP + l], ga);
-                            ga = fmaf(cN1, Su[(cidx + nx) * LP + l], ga);
-                        }
-                    }
-                    const float gm = fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga)));
-                    gmax = fmaxf(gmax, gm);
-                    // per-tracer maximum for the next step's scale: one shared atomic per warp
-                    const unsigned wmax = __reduce_max_sync(amask, __float_as_uint(gm));
-                    if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[l], wmax);
-                    const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
-                    const int qn = __float2int_rn(gn), qs_ = __float2int_rn(gs);
-                    const int qa = __float2int_rn(ga);
-                    qs[l] = (qw - qe) + (qs_ - qn) + (qb[l] - qa);
-                    qb[l] = qa;
-                }
-            }
-            cp_async_wait_all();
-            __syncthreads();
-            // ---- phase B: FP64 update of the tile's wet cells at level k, row by row (coalesced)
-            {
-                const int rowlen = TX * L;
-                const int dc = 32 / L, dl = 32 % L;
-                for (int r = warp; r < TY; r += nwarp) {
-                    const int jr = j0 + r;
-                    if (jr > maxj) continue;
-                    const double rv = __ldg(md.rvol + (size_t)(jr - 1) + (size_t)maxj * (size_t)(k - 1));
-                    const size_t rowbase = (size_t)NI * ((size_t)jr + (size_t)NJ * (size_t)k);
-                    int c = lane / L, l = lane % L;
+            // Each thread owns a fixed set of slab elements (rows by warp, elements of the
+            // row by lane).  pump(cv, nx_lev): convert the thread's own staged elements of
+            // level cv into FP32 slot cv % 3 (its own cp.async copies are complete after
+            // cp.async.wait_all, so no block barrier guards the stage), then cp.async its
+            // elements of level nx_lev into the stage.  Land cells are zero-filled instead
+            // of copied: their values only ever meet zero coefficients.
+            auto pump = [&](int cv, int nx_lev) {
+                float *F = Fb + (size_t)(cv % 3) * gl * ncp;
+                float *FL = FLb + (size_t)(cv % 3) * 2 * ncp;
+                const int rowlen = nx * gl;
+                const int dc = 32 / gl, dl = 32 % gl;
+                for (int r = warp; r < ny; r += nwarp) {
+                    const int gj = j0 - 1 + r;
+                    double *Srow = stage + (size_t)r * rowlen;
+                    const int *krow = k1t + r * nx;
+                    const bool rowok = gj <= maxj + 1;
+                    const size_t rowbase = (size_t)NI * ((size_t)gj + (size_t)NJ * (size_t)nx_lev);
+                    int c = lane / gl, q = lane % gl;
                     for (int e = lane; e < rowlen; e += 32) {
-                        const int ic = i0 + c;
-                        if (ic <= maxi && k >= k1t[(r + 1) * nx + c + 1]) {
-                            const size_t g = ((size_t)ic + rowbase) * L + l;
-                            const double told = R[g];
-                            const int cc = r * TX + c;
-                            double dlt;
-                            if (l < 2) {
-                                const int sl = s_scale[l];
-                                dlt = f2d_scaled(QSD[cc * 4 + 2 * l], sl) + f2d_scaled(QSD[cc * 4 + 2 * l + 1], sl);
+                        if (cv >= 0) {
+                            const double x = Srow[e];
+                            const int sl = s_scale[g0 + q];
+                            const float h = d2f_scaled(x, sl);
+                            const int cc = r * nx + c;
+                            F[q * ncp + cc] = h;
+                            if (ts_group && q < 2) FL[q * ncp + cc] = d2f_scaled(x - f2d_scaled(h, sl), sl);
+                        }
+                        if (nx_lev >= 0) {
+                            int gi = i0 - 1 + c;
+                            if (rowok && gi <= maxi + 1 && nx_lev >= krow[c]) {
+                                if (gi == 0) gi = maxi;
+                                else if (gi == maxi + 1) gi = 1;
+                                cp_async8(Srow + e, R + ((size_t)gi + rowbase) * L + g0 + q);
                             } else {
-                                dlt = i2d_scaled(QS[cc * LP + l], s_scale[l]);
+                                Srow[e] = 0.0;
                             }
-                            const double tnew = fma(dlt, rv, told);
-                            W[g] = tnew;
-                            if (((unsigned)__double2hiint(tnew) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
-                            if (l < 2) TSN[cc * 2 + l] = d2f_scaled(tnew, 0);
                         }
                         c += dc;
-                        l += dl;
-                        if (l >= L) {
-                            l -= L;
+                        q += dl;
+                        if (q >= gl) {
+                            q -= gl;
                             c += 1;
                         }
                     }
                 }
+                cp_async_commit();
+            };
+
+            for (int e = t; e < gl * nin; e += blockDim.x) QB[e] = 0;
+            if (ts_group)
+                for (int e = t; e < 4 * nin; e += blockDim.x) QBD[e] = 0.0f;
+            // prologue: slabs kstart and kstart+1 converted, kstart+2 in flight
+            pump(-1, kstart);
+            cp_async_wait_all();
+            pump(kstart, kstart + 1 <= maxk ? kstart + 1 : -1);
+            if (kstart + 1 <= maxk) {
+                cp_async_wait_all();
+                pump(kstart + 1, kstart + 2 <= maxk ? kstart + 2 : -1);
             }
-            if (k + 2 <= maxk) convert((k & 1) ? F1 : F0, (k & 1) ? G1 : G0);
             __syncthreads();
-            if (k + 3 <= maxk) issue(k + 3);
+
+            for (int k = kstart; k <= maxk; ++k) {
+                const float *Sk = Fb + (size_t)(k % 3) * gl * ncp;
+                const float *Su = Fb + (size_t)((k + 1) % 3) * gl * ncp;
+                const float *SkL = FLb + (size_t)(k % 3) * 2 * ncp;
+                const float *SuL = FLb + (size_t)((k + 1) % 3) * 2 * ncp;
+                if (inside && k >= k1c) {
+                    const size_t cl = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
+                    const float *cf = md.coef + 12 * cl;
+                    const int iw = (i == 1) ? maxi : i - 1;
+                    const float *cw = md.coef + 12 * ((size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1)));
+                    const dflt AeX = {__ldg(cf + 0), __ldg(cf + 6)}, BeX = {__ldg(cf + 1), __ldg(cf + 7)};
+                    const dflt AnX = {__ldg(cf + 2), __ldg(cf + 8)}, BnX = {__ldg(cf + 3), __ldg(cf + 9)};
+                    const dflt AaX = {__ldg(cf + 4), __ldg(cf + 10)}, BaX = {__ldg(cf + 5), __ldg(cf + 11)};
+                    const dflt AwX = {__ldg(cw + 0), __ldg(cw + 6)}, BwX = {__ldg(cw + 1), __ldg(cw + 7)};
+                    dflt AsX = {0.0f, 0.0f}, BsX = {0.0f, 0.0f};
+                    if (j > 1) {
+                        const float *cs = md.coef + 12 * (cl - (size_t)maxi);
+                        AsX = {__ldg(cs + 2), __ldg(cs + 8)};
+                        BsX = {__ldg(cs + 3), __ldg(cs + 9)};
+                    }
+                    const bool top = (k == maxk);
+                    const double rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
+                    const size_t base = (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)k));
+                    const float *gt = md.gtop + (size_t)(L + 2) * ((size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1));
+                    bool iso = false;
+                    // top-face stencil: C1*T(k+1) + C0*T(k) (+ isoneutral corners)
+                    dflt C1X = AaX, C0X = BaX;
+                    dflt W0X = {0.f, 0.f}, E0X = {0.f, 0.f}, S0X = {0.f, 0.f}, N0X = {0.f, 0.f};
+                    dflt W1X = {0.f, 0.f}, E1X = {0.f, 0.f}, S1X = {0.f, 0.f}, N1X = {0.f, 0.f};
+                    if (md.diso && !top) {
+                        // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
+                        // state: the density differences scc*dS - tec*dT cancel strongly in weakly
+                        // stratified water; they are differences of D = ec(2)*S - tec*T with the
+                        // cell's tec (goldstein.f90:2587-2588)
+                        auto ld = [&](int ii, int jj, int kk, int l) {
+                            return __ldg(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
+                        };
+                        const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
+                        const double s1 = ld(i, j, k, 1), s2 = ld(i, j, k + 1, 1);
+                        const double tatw = 0.5 * (t1 + t2);
+                        double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
+                        if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
+                        const double scc = md.ec[1];
+                        const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
+                        const double rdza = mk[4 * mkn + k];
+                        const double dzrho = (Dc1 - Dc0) * rdza;
+                        if (dzrho < -1.0e-12) {
+                            iso = true;
+                            const double rdzrho = 1.0 / dzrho;
+                            const double rcr = mj[j];                          // rc(j)*rdphi
+                            const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
+                            const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
+                            double dxr[4], dyr[4], mx[4], my[4];
+                            double tv1 = 0.0;
+#pragma unroll
+                            for (int knp = 0; knp <= 1; ++knp) {
+                                const double Dck = knp ? Dc1 : Dc0;
+#pragma unroll
+                                for (int nnp = 0; nnp <= 1; ++nnp) {
+                                    const int ina = nnp + 2 * knp;
+                                    const int kk = k + knp;
+                                    const bool okx = kk >= k1t[cidx + (nnp ? 1 : -1)];
+                                    const bool oky = kk >= k1t[cidx + (nnp ? nx : -nx)];
+                                    mx[ina] = okx ? rcr : 0.0;
+                                    my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
+                                    dxr[ina] = 0.0;
+                                    dyr[ina] = 0.0;
+                                    if (okx) {
+                                        const int ii = nnp ? ip : im;
+                                        const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
+                                        dxr[ina] = (nnp ? Dn - Dck : Dck - Dn) * rcr;
+                                    }
+                                    if (oky) {
+                                        const int jj = nnp ? j + 1 : j - 1;
+                                        const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
+                                        dyr[ina] = (nnp ? Dn - Dck : Dck - Dn) * my[ina];
+                                    }
+                                    tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
+                                }
+                            }
+                            const double sum2 = tv1;
+                            tv1 = 0.25 * tv1 * rdzrho * rdzrho;
+                            const double ss = mk[5 * mkn + k];
+                            double slim = 1.0;
+                            if (tv1 > ss) {
+                                slim = ss * ss / (tv1 * tv1);
+                                if (ts_group) limps_l += 1;
+                            }
+                            if (ts_group) dmax_l = fmax(dmax_l, tv1 * slim * md.diff1 * rdza * md.dt * rdza);
+                            // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
+                            const double c0 = mj[2 * mjn + j] * 0.25 * slim * md.diff1 * rdzrho * rdzrho;
+                            const double two_dz = 2.0 * dzrho * c0;
+                            double wx[4], wy[4];
+#pragma unroll
+                            for (int n = 0; n < 4; ++n) {
+                                wx[n] = two_dz * dxr[n] * mx[n];
+                                wy[n] = two_dz * dyr[n] * my[n];
+                            }
+                            const double wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
+                            const double c0d = f2d_scaled(BaX.hi, 0) + f2d_scaled(BaX.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
+                            const double c1d = f2d_scaled(AaX.hi, 0) + f2d_scaled(AaX.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
+                            C0X = df_split(c0d);
+                            C1X = df_split(c1d);
+                            W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
+                            S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
+                        }
+                    }
+                    const int cE = cidx + 1, cW = cidx - 1, cN = cidx + nx, cS = cidx - nx;
+                    int q0 = 0;
+                    if (ts_group) {
+                        // T and S: double-float transfers, FP64 update
+                        double tn[2];
+#pragma unroll
+                        for (int l = 0; l < 2; ++l) {
+                            const float *F = Sk + l * ncp, *FL = SkL + l * ncp;
+                            const float *U = Su + l * ncp, *UL = SuL + l * ncp;
+                            const dflt Tc = {F[cidx], FL[cidx]}, TE = {F[cE], FL[cE]}, TW = {F[cW], FL[cW]};
+                            const dflt TN = {F[cN], FL[cN]}, TS = {F[cS], FL[cS]};
+                            const dflt Ge = df_dot2(AeX, TE, BeX, Tc);
+                            const dflt Gw = df_dot2(AwX, Tc, BwX, TW);
+                            const dflt Gn = df_dot2(AnX, TN, BnX, Tc);
+                            const dflt Gs = df_dot2(AsX, Tc, BsX, TS);
+                            const int sl = s_scale[l];
+                            dflt Ga;
+                            if (top) {
+                                const float sc = __int_as_float((127 + sl) << 23);
+                                Ga = {__ldg(gt + l) * sc, __ldg(gt + L + l) * sc};
+                            } else {
+                                Ga = df_dot2(C1X, dflt{U[cidx], UL[cidx]}, C0X, Tc);
+                                if (iso) {
+                                    Ga = df_add(Ga, df_dot2(W0X, TW, E0X, TE));
+                                    Ga = df_add(Ga, df_dot2(S0X, TS, N0X, TN));
+                                    Ga = df_add(Ga, df_dot2(W1X, dflt{U[cW], UL[cW]}, E1X, dflt{U[cE], UL[cE]}));
+                                    Ga = df_add(Ga, df_dot2(S1X, dflt{U[cS], UL[cS]}, N1X, dflt{U[cN], UL[cN]}));
+                                }
+                            }
+                            float *qb = QBD + (2 * l) * nin + cell;
+                            const dflt Gb = {qb[0], qb[nin]};
+                            const dflt sum = df_add(df_add(df_sub(Gw, Ge), df_sub(Gs, Gn)), df_sub(Gb, Ga));
+                            qb[0] = Ga.hi;
+                            qb[nin] = Ga.lo;
+                            const double dlt = f2d_scaled(sum.hi, sl) + f2d_scaled(sum.lo, sl);
+                            const double told = R[base + l];
+                            tn[l] = fma(dlt, rv, told);
+                            W[base + l] = tn[l];
+                            if (((unsigned)__double2hiint(tn[l]) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
+                        }
+                        // FP32 density prescreen for the exact convective adjustment
+                        const float tf = d2f_scaled(tn[0], 0), sf = d2f_scaled(tn[1], 0);
+                        const float rf = eos_f(ecf, tf, sf);
+                        if (k > k1c) {
+                            const float margin = 2.0e-6f * (fabsf(rf) + fabsf(rho_prev) + fabsf(ecf[0] * tf) +
+                                                            fabsf(ecf[1] * sf) + fabsf(ecf[2] * tf * tf) +
+                                                            fabsf(ecf[3] * tf * tf * tf)) + 1.0e-30f;
+                            if (!(rho_prev - rf > margin)) unstable = true;
+                        }
+                        rho_prev = rf;
+                        q0 = 2;
+                    }
+                    // other tracers: FP32 transfers rounded once to int32
+                    const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
+                    const float As = AsX.hi, Bs = BsX.hi;
+                    const float cC0 = C0X.hi, cC1 = C1X.hi, cW0 = W0X.hi, cE0 = E0X.hi, cS0 = S0X.hi, cN0 = N0X.hi;
+                    const float cW1 = W1X.hi, cE1 = E1X.hi, cS1 = S1X.hi, cN1 = N1X.hi;
+                    const unsigned amask = __activemask();
+                    for (int q = q0; q < gl; ++q) {
+                        const int l = g0 + q;
+                        const float *F = Sk + q * ncp;
+                        const float Tc = F[cidx], TE = F[cE], TW = F[cW], TN = F[cN], TS = F[cS];
+                        const float ge = fmaf(Ae, TE, Be * Tc);
+                        const float gw = fmaf(Aw, Tc, Bw * TW);
+                        const float gn = fmaf(An, TN, Bn * Tc);
+                        const float gs = fmaf(As, Tc, Bs * TS);
+                        const int sl = s_scale[l];
+                        float ga;
+                        if (top) {
+                            ga = __ldg(gt + l) * __int_as_float((127 + sl) << 23);
+                        } else {
+                            const float *U = Su + q * ncp;
+                            ga = fmaf(cC1, U[cidx], cC0 * Tc);
+                            if (iso) {
+                                ga = fmaf(cW0, TW, ga);
+                                ga = fmaf(cE0, TE, ga);
+                                ga = fmaf(cS0, TS, ga);
+                                ga = fmaf(cN0, TN, ga);
+                                ga = fmaf(cW1, U[cW], ga);
+                                ga = fmaf(cE1, U[cE], ga);
+                                ga = fmaf(cS1, U[cS], ga);
+                                ga = fmaf(cN1, U[cN], ga);
+                            }
+                        }
+                        if (track) {
+                            // per-tracer maximum for the scale of later steps: one shared atomic
+                            // per warp; also the int32 range check
+                            const float gm = fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga)));
+                            gmax = fmaxf(gmax, gm);
+                            const unsigned wmax = __reduce_max_sync(amask, __float_as_uint(gm));
+                            if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[l], wmax);
+                        }
+                        const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
+                        const int qn = __float2int_rn(gn), qs = __float2int_rn(gs);
+                        const int qa = __float2int_rn(ga);
+                        int *qbp = QB + q * nin + cell;
+                        const int sum = (qw - qe) + (qs - qn) + (*qbp - qa);
+                        *qbp = qa;
+                        const double told = R[base + l];
+                        const double tnew = fma(i2d_scaled(sum, sl), rv, told);
+                        W[base + l] = tnew;
+                        if (((unsigned)__double2hiint(tnew) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
+                    }
+                }
+                // the thread's own copies of level k+2 -> FP32 slot of k+2; start level k+3
+                if (k + 2 <= maxk) {
+                    cp_async_wait_all();
+                    pump(k + 2, k + 3 <= maxk ? k + 3 : -1);
+                }
+                __syncthreads();
+            }
         }
-        if (inside && maxk >= k1c) prescreen(maxk);
 
         // exact convective adjustment of columns that may be unstable
         if (inside && k1c <= maxk) {
@@ -634,13 +594,14 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         // a scaled transfer above 3.5e8 could overflow the int32 sum of six faces
         if (nonfinite || gmax > 3.5e8f) atomicOr(md.status, (nonfinite ? 1u : 0u) | (gmax > 3.5e8f ? 2u : 0u));
         __syncthreads();
-        for (int l = 2 + t; l < L; l += blockDim.x)
-            if (s_gmax[l]) atomicMax(&md.gmax[l], s_gmax[l]);
+        if (track)
+            for (int l = 2 + t; l < L; l += blockDim.x)
+                if (s_gmax[l]) atomicMax(&md.gmax[l], s_gmax[l]);
     }
 }
 
-// After a step: move each tracer's scale so that the step's largest transfer would
-// have landed in [2^25, 2^26); clear the maxima.  T and S (double-float) keep theirs.
+// After a tracking step: move each tracer's scale so that the step's largest transfer
+// would have landed in [2^25, 2^26); clear the maxima.  T and S (double-float) keep theirs.
 __global__ void k_rescale(const MemberDesc *__restrict__ mds, int n)
 {
     for (int m = blockIdx.x; m < n; m += gridDim.x) {

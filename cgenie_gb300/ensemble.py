@@ -29,6 +29,11 @@ class Ensemble:
             raise GoldsteinError(rc, "gb_ens_create")
         self.e = e
         self.members = {}
+        self.tile = (int(tile_i), int(tile_j))
+        self.use_graph = bool(use_graph)
+        self._current_tile = None
+        from .autotune import load_table
+        self.table = load_table()
         self.set_tuning(tile_i=tile_i, tile_j=tile_j, use_graph=use_graph)
         if stream is not None:
             self._check(self.lib.gb_ens_set_stream(self.e, C.c_void_p(stream)), "gb_ens_set_stream")
@@ -63,6 +68,14 @@ class Ensemble:
         """Admit a member (its state ts is also the initial ts1); returns its id.
         Raises GoldsteinError(GB_GO_ENOMEM) when it does not fit the HBM budget."""
         r = GridRefs(member, precision=abi.GB_GO_FP32FLUX, **kw)
+        # tile shape: the one given at construction, else the autotuned one for this grid shape
+        tile = self.tile
+        if tile == (0, 0):
+            from .autotune import lookup
+            tile = lookup(self.table, member.maxi, member.maxj, member.maxk) or (0, 0)
+        if tile != self._current_tile:
+            self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
+            self._current_tile = tile
         ts = np.ascontiguousarray(member.ts, dtype=np.float64)
         u = np.ascontiguousarray(member.u, dtype=np.float64)
         mid = C.c_int32()
