@@ -7,8 +7,9 @@ It follows the arithmetic of k_step_fp32 without the isoneutral branch:
 - other tracers are truncated to FP32 after scaling by 2^s_l, each face
   transfer is evaluated as an FMA of the FP32 coefficients and rounded to int32
   (half to even), and the FP64 state gets T += sum(q) * 2^-s_l / V;
-- after each step s_l moves so that the step's largest |scaled transfer| of a
-  wet cell would have landed in [2^25, 2^26);
+- after every 4th step (steps 0, 4, 8, ... since upload) s_l moves so that
+  that step's largest |scaled transfer| of a wet cell would have landed in
+  [2^25, 2^26);
 - convective adjustment uses the oracle's exact co.
 
 Used to tell the scheme's intrinsic error from kernel defects.
@@ -113,6 +114,7 @@ class Fp32Emulator:
             for j in range(m.maxj):
                 rv[k, j] = 1.0 / (m.dphi * m.ds[j] * m.dz[k])
         self.rv = rv
+        self.nstep = 0
 
     def step(self, n=1):
         import ctypes as C
@@ -182,7 +184,7 @@ class Fp32Emulator:
                         gmax = max(gmax, gm)
                     upd = self.ts[k, 1:-1, 1:-1, l] + (sm.astype(np.float64) / sc) * self.rv[k - 1][:, None]
                     new[k, 1:-1, 1:-1, l] = np.where(wet, upd, self.ts[k, 1:-1, 1:-1, l])
-                if gmax > 0:
+                if gmax > 0 and self.nstep % 4 == 0:
                     e = int(np.frexp(np.float32(gmax))[1]) - 1
                     self.s[l] = max(-120, min(120, self.s[l] + 25 - e))
             self.ts = new
@@ -192,3 +194,4 @@ class Fp32Emulator:
             r = self.refs
             self.oracle.lib().gbo_co(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), dptr(self.ts),
                                      dptr(self.rho), dptr(self.cost), iptr(self.icosd))
+            self.nstep += 1
