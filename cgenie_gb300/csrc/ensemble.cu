@@ -39,7 +39,6 @@ struct Member {
     Dims d{};
     PhysParams p{};
     double dt = 0.0;
-    int tile_i = 16, tile_j = 8;
     size_t bytes = 0;
     // device
     double *buf0 = nullptr, *buf1 = nullptr, *ts_static = nullptr, *rho = nullptr, *stage = nullptr;
@@ -49,6 +48,11 @@ struct Member {
     unsigned int *gmax = nullptr;         // per tracer, scale re-targeting
     unsigned long long *diag = nullptr;   // two slots {dmax bits, limps}
     unsigned int *status = nullptr;
+    int32_t *ptab = nullptr;              // patch tables
+    uint8_t *coflag = nullptr;            // per column: flagged for the exact convective adjustment
+    std::vector<int32_t> poff;            // per patch: word offset in ptab
+    std::vector<double> pcost;            // per patch: cell-updates per step
+    int max_slots = 1;
     std::vector<double> ds_host;          // ds(0:maxj+1), for the inventory
     MemberDesc desc{};
     long long start_step = 0;    // step index at admission (state in buf0)
@@ -71,8 +75,10 @@ struct gb_ens {
     MemberDesc *descs = nullptr;        // device, capacity cap_desc
     int cap_desc = 0;
     int4 *items = nullptr;              // device, capacity cap_items
-    int cap_items = 0, nitems = 0;
-    int lmax = 2, smem = 0;
+    int cap_items = 0, nitems = 0, nco = 0;
+    int max_slots = 1;
+    bool any_iso = false;               // some member has the isoneutral branch
+    int *work = nullptr;                // device work counters (two, by step parity)
     bool dirty = true;
     gb_ens_tuning tuning{0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
@@ -101,8 +107,9 @@ static size_t member_bytes(const gb_go_dims *d)
     const size_t ncell = (size_t)d->maxi * d->maxj * d->maxk;
     const size_t ncol = (size_t)d->maxi * d->maxj;
     // two state buffers, uploaded copy, download stage, rho, coefficients, forcing, small arrays
+    // patch tables: at most (31 + maxk) words per column
     return 4 * nts * 8 + nrho * 8 + 12 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
-           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + 4096;
+           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + 4096;
 }
 
 extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *) { return dims ? member_bytes(dims) : 0; }
@@ -130,6 +137,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
     }
     if (x == cudaSuccess) x = cudaMalloc(&e->step_ctr, sizeof(long long));
     if (x == cudaSuccess) x = cudaMemset(e->step_ctr, 0, sizeof(long long));
+    if (x == cudaSuccess) x = cudaMalloc(&e->work, 2 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMemset(e->work, 0, 2 * sizeof(int));
     if (x != cudaSuccess) {
         gb_ens_destroy(e);
         return x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
@@ -142,7 +151,8 @@ static void free_member(gb_ens *e, Member *m)
 {
     cudaStream_t s = e->stream;
     void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->gtop, m->mj,
-                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax};
+                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax,
+                    m->ptab, m->coflag};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
 }
@@ -156,6 +166,7 @@ extern "C" void gb_ens_destroy(gb_ens *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->graph) cudaGraphExecDestroy(e->graph);
     cudaFree(e->step_ctr);
+    cudaFree(e->work);
     cudaFree(e->descs);
     cudaFree(e->items);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
@@ -165,8 +176,10 @@ extern "C" void gb_ens_destroy(gb_ens *e)
 extern "C" int gb_ens_set_tuning(gb_ens *e, const gb_ens_tuning *t)
 {
     if (!e || !t) return GB_GO_EINVAL;
-    if (t->tile_i < 0 || t->tile_j < 0 || t->tile_i * t->tile_j > kFp32Threads || t->tile_i > 64 || t->tile_j > 64)
-        return efail(e, GB_GO_EINVAL, "tile must satisfy tile_i*tile_j <= 128, each <= 64");
+    // tile_i x tile_j: the patch rectangle asked for (0, 0: chosen per member); a rectangle
+    // over the kernel limits for a member falls back to the chosen one
+    if (t->tile_i < 0 || t->tile_j < 0 || t->tile_i > 4096 || t->tile_j > 4096)
+        return efail(e, GB_GO_EINVAL, "tile sizes must be in 0..4096");
     e->tuning = *t;
     e->dirty = true;
     return GB_GO_OK;
@@ -209,12 +222,13 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     m->p = phys_from(params, grid);
     m->dt = grid->dt[0];
     m->bytes = bytes;
-    if (e->tuning.tile_i > 0 && e->tuning.tile_j > 0) {
-        m->tile_i = e->tuning.tile_i;
-        m->tile_j = e->tuning.tile_j;
-    } else {
-        fp32_default_tile(dims->maxi, dims->maxj, &m->tile_i, &m->tile_j);
-    }
+    if (dims->maxk > kMaxK) return efail(e, GB_GO_ERANGE, "ensemble members have at most 64 levels");
+    PatchPlan plan;
+    if (fp32_plan_patches(m->d, grid->k1, e->tuning.tile_i, e->tuning.tile_j, plan) != GB_GO_OK)
+        return efail(e, GB_GO_ERANGE, "no patch shape fits the FP32-flux kernel limits");
+    m->poff = plan.offset;
+    m->pcost = plan.cost;
+    m->max_slots = plan.max_slots;
     std::vector<double> blob;
     build_metric_blob(dims, params, grid, blob);
     Fp32Static st;
@@ -248,6 +262,11 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = cudaMemsetAsync(m->gmax, 0, (size_t)dims->maxl * sizeof(unsigned int), s);
     if (x == cudaSuccess) x = dalloc(e, &m->diag, 4);
     if (x == cudaSuccess) x = dalloc(e, &m->status, 1);
+    if (x == cudaSuccess) x = dalloc(e, &m->ptab, std::max<size_t>(4, plan.words.size()));
+    if (x == cudaSuccess) x = dalloc(e, &m->coflag, ncol);
+    if (x == cudaSuccess) x = cudaMemsetAsync(m->coflag, 0, ncol, s);
+    if (x == cudaSuccess && !plan.words.empty())
+        x = cudaMemcpyAsync(m->ptab, plan.words.data(), plan.words.size() * 4, cudaMemcpyHostToDevice, s);
     m->ds_host.assign(blob.begin() + 6 * (dims->maxj + 2), blob.begin() + 7 * (dims->maxj + 2));
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->dsj, m->ds_host.data(), m->ds_host.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemsetAsync(m->diag, 0, 4 * sizeof(unsigned long long), s);
@@ -281,11 +300,12 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.buf[0] = m->buf0; md.buf[1] = m->buf1;
     md.ts_static = m->ts_static; md.coef = m->coef; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
     md.scale = m->scale; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
-    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax;
+    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab; md.coflag = m->coflag;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission
     md.stop_step = m->stop_step;
+    md.origin = e->step;
     long long wet = 0;
     for (int j = 1; j <= dims->maxj; ++j)
         for (int i = 1; i <= dims->maxi; ++i) {
@@ -326,8 +346,11 @@ static int rebuild(gb_ens *e)
         e->cap_desc = cap;
     }
     std::vector<MemberDesc> descs;
-    std::vector<std::pair<double, int4>> items;
-    int lmax = 2, smem = 0;
+    // members in decreasing order of work (longest first); a member's patches stay
+    // together so the ring columns one patch reads are in L2 from its neighbours
+    std::vector<std::pair<double, Member *>> order;
+    int max_slots = 1;
+    bool any_iso = false;
     int slot = 0;
     for (auto &kv : e->members) {
         Member *m = kv.second.get();
@@ -338,19 +361,26 @@ static int rebuild(gb_ens *e)
         md.stop_step = m->stop_step;
         md.status_idx = slot;
         descs.push_back(md);
-        const int ti = m->tile_i, tj = m->tile_j;
-        const int nti = (m->d.maxi + ti - 1) / ti, ntj = (m->d.maxj + tj - 1) / tj;
-        const double per = m->cost_est / (nti * ntj);
-        for (int b = 0; b < ntj; ++b)
-            for (int a = 0; a < nti; ++a) items.push_back({per, make_int4(slot, 1 + a * ti, 1 + b * tj, ti | (tj << 8))});
-        lmax = std::max(lmax, m->d.L);
-        smem = std::max(smem, fp32_smem_bytes(ti, tj, m->d.L));
+        double c = 0.0;
+        for (double v : m->pcost) c += v;
+        order.push_back({c, m});
+        max_slots = std::max(max_slots, m->max_slots);
+        any_iso = any_iso || m->desc.diso;
         ++slot;
     }
-    std::stable_sort(items.begin(), items.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    // transfer items (member, patch, group): the T-S group of every patch first (the longest
+    // items), then the other groups, each member's patches together; then co items (member, patch)
     std::vector<int4> it;
-    it.reserve(items.size());
-    for (auto &p : items) it.push_back(p.second);
+    int maxg = 1;
+    for (auto &o : order) maxg = std::max(maxg, fp32_group_count(o.second->d.L));
+    for (int g = 0; g < maxg; ++g)
+        for (auto &o : order)
+            if (g < fp32_group_count(o.second->d.L))
+                for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], g, 0));
+    const int nstep_items = (int)it.size();
+    for (auto &o : order)
+        for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], 0, 0));
     if ((int)it.size() > e->cap_items) {
         int cap = std::max(256, (int)(2 * it.size()));
         if (e->items) cudaFreeAsync(e->items, s);
@@ -360,9 +390,10 @@ static int rebuild(gb_ens *e)
     if (!descs.empty()) ETRY(e, cudaMemcpyAsync(e->descs, descs.data(), descs.size() * sizeof(MemberDesc), cudaMemcpyHostToDevice, s));
     if (!it.empty()) ETRY(e, cudaMemcpyAsync(e->items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
     ETRY(e, cudaStreamSynchronize(s));
-    e->nitems = (int)it.size();
-    e->lmax = lmax;
-    e->smem = smem;
+    e->nitems = nstep_items;
+    e->nco = (int)it.size() - nstep_items;
+    e->max_slots = max_slots;
+    e->any_iso = any_iso;
     e->dirty = false;
     if (e->graph) {
         cudaGraphExecDestroy(e->graph);
@@ -375,12 +406,13 @@ static int launch_steps(gb_ens *e, int nsteps)
 {
     cudaStream_t s = e->stream;
     for (int n = 0; n < nsteps; ++n) {
-        int r = fp32_launch(e->descs, e->items, e->nitems, e->lmax, e->smem, e->step_ctr, n, s);
+        int r = fp32_launch(e->descs, e->items, e->nitems, e->items + e->nitems, e->nco, e->max_slots, e->step_ctr, n,
+                            e->work, e->any_iso, s);
         if (!r) r = fp32_rescale(e->descs, (int)e->members.size(), s);
         if (r) return efail(e, r, "fp32 batched launch failed");
     }
     k_add_step<<<1, 1, 0, s>>>(e->step_ctr, nsteps);
-    count_launches(2 * (uint64_t)nsteps + 1);
+    count_launches(3 * (uint64_t)nsteps + 1);   // step, co, rescale per step; step counter
     return cudaGetLastError() == cudaSuccess ? GB_GO_OK : efail(e, GB_GO_ECUDA, "launch failed");
 }
 
@@ -416,7 +448,7 @@ extern "C" int gb_ens_step(gb_ens *e, int32_t nsteps)
             e->graph_steps = nsteps;
         }
         ETRY(e, cudaGraphLaunch(e->graph, e->stream));
-        count_launches(2 * (uint64_t)nsteps + 1);
+        count_launches(3 * (uint64_t)nsteps + 1);   // step, co, rescale per step; step counter
     } else {
         int r = launch_steps(e, nsteps);
         if (r) return r;
@@ -435,6 +467,8 @@ extern "C" int gb_ens_set_remaining(gb_ens *e, int32_t id, int64_t steps)
     const long long done_at = std::min(e->step, m->stop_step);
     const int curbuf = (int)((done_at + m->desc.parity) & 1);
     m->desc.parity = (int)((curbuf - (e->step & 1) + 2) & 1);
+    // keep the member's own step count running across a pause
+    m->desc.origin = e->step - (done_at - m->desc.origin);
     m->stop_step = e->step + steps;
     e->dirty = true;
     return GB_GO_OK;

@@ -22,12 +22,13 @@
 // Convective adjustment (goldstein.f90:2657-2841) runs in exact FP64 on columns
 // that an FP32 density prescreen cannot prove statically stable.
 //
-// Mapping: a CTA of 128 threads takes work items (member, TX x TY column tile)
-// from a host-built list.  Each level k of a tile: cp.async brings the FP64 slab
-// of level k+2 (with a one-cell halo) into shared memory while threads (one per
-// column) compute the integer / double-float transfers of level k from scaled
-// FP32 slabs of levels k and k+1; then the tile's FP64 state of level k is
-// updated row by row with coalesced loads and stores.
+// Mapping: persistent CTAs of 128 threads take work items (member, patch) from
+// a counter.  A patch is a rectangle of water columns with the ring of wet
+// neighbour columns around it, its columns sorted by k1 so that the wet cells
+// of each level form a prefix (land and the cells below the sea floor are never
+// loaded).  Per level, a memory phase with tracers innermost (coalesced FP64
+// loads and stores) converts and updates, and a compute phase with one thread
+// per column forms the transfers.
 #include "gb_fp32.h"
 #include "co_column.cuh"
 #include "../../include/gb_goldstein.h"
@@ -35,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -143,119 +145,165 @@ struct Fp32Col {
 
 // ---------------------------------------------------------------------------
 // the step kernel
+//
+// A work item is one patch of one member: a rectangle of water columns (periodic
+// in i) plus the ring of wet neighbour columns outside it.  Each column of the
+// patch (a "slot") belongs to one thread for the whole step: interior slots
+// first, then ring slots, each part sorted by k1, so the wet cells of a level are
+// two prefixes of the threads (land and cells below the sea floor are never
+// touched).  A work item is one tracer group of one patch, marched up in k.  At level k every slot's thread converts its FP64 values
+// of level k+1 (loaded one level earlier) into the scaled FP32 slab, starts the
+// loads of level k+2, and, after one barrier, each interior thread forms the
+// face transfers of level k from the slabs of k and k+1 (the bottom face carried
+// in registers) and writes its column's FP64 update.  Three slab buffers make one
+// barrier per level enough.  The group of T and S also flags the columns whose FP32
+// density profile may be unstable; k_co_fp32 then adjusts those columns exactly.
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-// Tracers per march of a tile: shared memory (and so CTAs per SM) scales with it.
+// Tracers per march of a patch.  Group 0 is T and S (double-float transfers, and the
+// convection prescreen); the other tracers form groups of at most kGroup.
 constexpr int kGroup = 8;
 
-// Dynamic shared memory of one work item, for tracer groups of up to kGroup
-// (byte offsets, 16-byte aligned).  ncp = nc | 1 (odd pitch: conflict-free).
+__host__ __device__ inline int fp32_ngroups(int L)
+{
+    return L <= 2 ? 1 : 1 + (L - 2 + kGroup - 1) / kGroup;
+}
+
+__host__ __device__ inline void fp32_group(int L, int g, int *g0, int *gl)
+{
+    if (g == 0) {
+        *g0 = 0;
+        *gl = 2;
+        return;
+    }
+    const int nb = L - 2, ngb = (nb + kGroup - 1) / kGroup;
+    const int base = nb / ngb, rem = nb % ngb, h = g - 1;
+    *gl = base + (h < rem ? 1 : 0);
+    *g0 = 2 + h * base + (h < rem ? h : rem);
+}
+// FP32 slab pitch per slot (kGroup tracers + 1: consecutive slots hit distinct banks)
+constexpr int kGP = 9;
+constexpr int kPatchHdr = 8;
+constexpr int kIcolWords = 8;
+
+// Dynamic shared memory for patches of up to P - 1 slots (slot P - 1 stays zero: the
+// neighbour of a column next to land).  Byte offsets, 16-byte aligned.
 struct Fp32Smem {
-    int stage;   // double[nc*G]      FP64 slab of one tracer group in flight (cp.async)
-    int f;       // float[3][G][ncp]  scaled FP32 slabs of levels k, k+1, k+2 (tracer-major)
-    int fl;      // float[3][2][ncp]  lo parts of T and S for the three slabs
-    int qb;      // int[G][nin]       bottom-face carry of the group's tracers
-    int qbd;     // float[2][2][nin]  the same for T and S as double-floats
-    int k1t;     // int[nc]           k1 with a one-cell halo
+    int slab;    // float[3][P][kGP]  scaled FP32 values of three levels
+    int slo;     // float[3][P][3]    lo parts of T and S for the same levels
     int total;
 };
 
-__host__ __device__ inline Fp32Smem fp32_smem_layout(int TX, int TY, int L)
+__host__ __device__ inline Fp32Smem fp32_smem_layout(int P)
 {
-    const int nc = (TX + 2) * (TY + 2), ncp = nc | 1, nin = TX * TY;
-    const int G = L < kGroup ? L : kGroup;
     Fp32Smem s;
     int o = 0;
-    s.stage = o; o += (nc * G * 8 + 15) & ~15;
-    s.f = o; o += (3 * G * ncp * 4 + 15) & ~15;
-    s.fl = o; o += (3 * 2 * ncp * 4 + 15) & ~15;
-    s.qb = o; o += (G * nin * 4 + 15) & ~15;
-    s.qbd = o; o += (4 * nin * 4 + 15) & ~15;
-    s.k1t = o; o += (nc * 4 + 15) & ~15;
+    s.slab = o; o += (3 * P * kGP * 4 + 15) & ~15;
+    s.slo = o; o += (3 * P * 3 * 4 + 15) & ~15;
     s.total = o;
     return s;
 }
 
-__global__ void __launch_bounds__(kFp32Threads, 5)
+__device__ __forceinline__ double ldg_d(const double *p) { return __ldg(p); }
+
+// ISO: the isoneutral branch is compiled in (members with diso); without it the kernel
+// needs fewer registers.  A work item is (member, patch table offset, tracer group).
+template <bool ISO>
+__global__ void __launch_bounds__(kFp32Threads, 4)
 k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
-            const long long *__restrict__ step_ctr, int rel)
+            const long long *__restrict__ step_ctr, int rel, int *__restrict__ work, int P)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ int s_kstart;
+    __shared__ int s_nki[kMaxK + 2], s_nkr[kMaxK + 2];
     __shared__ int s_scale[kFp32MaxL];
     __shared__ unsigned int s_gmax[kFp32MaxL];
+    __shared__ int s_it;
     const int t = threadIdx.x;
-    const int warp = t >> 5, lane = t & 31, nwarp = blockDim.x >> 5;
+    const int lane = t & 31;
     const long long step = *step_ctr + rel;
-    // every 4th step the per-tracer transfer maxima are gathered to re-target the scales
-    const bool track = (step & 3) == 0;
+    // the counter of the next step is free: this launch runs after the previous one ended
+    if (blockIdx.x == 0 && t == 0) work[(step + 1) & 1] = 0;
 
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const Fp32Smem lay = fp32_smem_layout(P);
+    float *slab = reinterpret_cast<float *>(smraw + lay.slab);
+    float *slo = reinterpret_cast<float *>(smraw + lay.slo);
+    const int zs = P - 1;
+    // Slab entries of slots not yet wet, and the zero slot, meet only zero coefficients; they
+    // must be finite, so the slabs start at zero (afterwards they only hold converted values).
+    for (int e = t; e < 3 * P * kGP; e += blockDim.x) slab[e] = 0.0f;
+    for (int e = t; e < 3 * P * 3; e += blockDim.x) slo[e] = 0.0f;
+
+    for (;;) {
+        if (t == 0) s_it = atomicAdd(&work[step & 1], 1);
+        __syncthreads();
+        const int it = s_it;
+        __syncthreads();
+        if (it >= nitems) break;
         const int4 item = items[it];
         const MemberDesc &md = mds[item.x];
         if (step >= md.stop_step) continue;   // uniform over the CTA
-        const int TX = item.w & 0xff, TY = (item.w >> 8) & 0xff;
-        const int i0 = item.y, j0 = item.z;
-        // the member's first tile clears the diagnostics slot of the next step
-        if (i0 == 1 && j0 == 1 && t == 0) {
+        const int32_t *__restrict__ tab = md.ptab + item.y;
+        const int ns = tab[0], ni = tab[1], kstart = tab[2], pidx = tab[3];
+        const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
+        const int32_t *__restrict__ tgoff = tab + kPatchHdr + 2 * (maxk + 2);
+        const int32_t *__restrict__ ticol = tab + ((kPatchHdr + 2 * (maxk + 2) + ns + 3) & ~3);
+        // every 4th step of the member's own the per-tracer transfer maxima are gathered
+        // to re-target the scales (a member's result does not depend on when it was admitted)
+        const bool track = ((step - md.origin) & 3) == 0;
+        // the member's first patch clears the diagnostics slot of the next step
+        if (pidx == 0 && t == 0) {
             unsigned long long *dn = md.diag + 2 * ((step + 1) & 1);
             dn[0] = 0ull;
             dn[1] = 0ull;
         }
-        const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
-        const int nx = TX + 2, ny = TY + 2, nc = nx * ny, ncp = nc | 1, nin = TX * TY;
-        const Fp32Smem lay = fp32_smem_layout(TX, TY, L);
-        double *stage = reinterpret_cast<double *>(smraw + lay.stage);
-        float *Fb = reinterpret_cast<float *>(smraw + lay.f);
-        float *FLb = reinterpret_cast<float *>(smraw + lay.fl);
-        int *QB = reinterpret_cast<int *>(smraw + lay.qb);
-        float *QBD = reinterpret_cast<float *>(smraw + lay.qbd);
-        int *k1t = reinterpret_cast<int *>(smraw + lay.k1t);
         const int par = (int)((step + md.parity) & 1);
         const double *__restrict__ R = md.buf[par];
         double *__restrict__ W = md.buf[par ^ 1];
+        const long long LNIJ = (long long)L * NI * NJ;
+        const size_t nij = (size_t)maxi * maxj;
         const double *mk = md.mk;
         const double *mj = md.mj;
         const int mkn = maxk + 2, mjn = maxj + 2;
-        const int Gmax = L < kGroup ? L : kGroup;
-
-        // k1 tile with a one-column halo (periodic in i), land outside the grid
-        if (t == 0) s_kstart = 1 << 20;
-        for (int e = t; e < nc; e += blockDim.x) {
-            const int c = e % nx, r = e / nx;
-            int gi = i0 - 1 + c, gj = j0 - 1 + r;
-            int v = maxk + 1;
-            if (gj <= maxj + 1 && gi <= maxi + 1) {
-                if (gi == 0) gi = maxi;
-                else if (gi == maxi + 1) gi = 1;
-                v = md.k1[gi + NI * gj];
-            }
-            k1t[e] = v;
-        }
         for (int l = t; l < L; l += blockDim.x) {
             s_scale[l] = md.scale[l];
             s_gmax[l] = 0u;
         }
+        for (int e = t; e < maxk + 2; e += blockDim.x) {
+            s_nki[e] = tab[kPatchHdr + e];
+            s_nkr[e] = tab[kPatchHdr + maxk + 2 + e];
+        }
+
+        // this thread's slot (t < ns): interior column (t < ni) or ring column
+        const bool own = t < ns;
+        const bool interior = t < ni;
+        const int goffs = own ? __ldg(tgoff + t) : 0;
+        int sE = zs, sW = zs, sN = zs, sS = zs, k1c = maxk + 1, i = 1, j = 1;
+        int cl0 = 0, cw0 = 0, k1nb = 0;
+        if (interior) {
+            const int4 w0 = __ldg(reinterpret_cast<const int4 *>(ticol + kIcolWords * t));
+            const int4 w1 = __ldg(reinterpret_cast<const int4 *>(ticol + kIcolWords * t + 4));
+            auto sl16 = [&](int v) { v &= 0xffff; return v == 0xffff ? zs : v; };
+            sE = sl16(w0.x >> 16);
+            sW = sl16(w0.y);
+            sN = sl16(w0.y >> 16);
+            sS = sl16(w0.z);
+            k1c = (w0.z >> 16) & 0xffff;
+            cl0 = w0.w;
+            i = w1.x & 0xffff;
+            j = (w1.x >> 16) & 0xffff;
+            k1nb = w1.y;
+            cw0 = w1.z;
+        }
+        // first level at which this slot is wet (ring slots: their k1, from the prefix tables)
         __syncthreads();
-        const int ti = t % TX, tj = t / TX;
-        const int i = i0 + ti, j = j0 + tj;
-        const bool inside = (t < nin) && (i <= maxi) && (j <= maxj);
-        const int cidx = (tj + 1) * nx + (ti + 1);
-        const int cell = tj * TX + ti;
-        const int k1c = inside ? k1t[cidx] : maxk + 1;
-        if (inside && k1c <= maxk) atomicMin(&s_kstart, k1c);
-        __syncthreads();
-        const int kstart = s_kstart;
-        if (kstart > maxk) {
-            __syncthreads();
-            continue;
+        int kown = maxk + 1;
+        if (own) {
+            if (interior) kown = k1c;
+            else
+                for (int k = kstart; k <= maxk; ++k)
+                    if (t - ni < s_nkr[k]) {
+                        kown = k;
+                        break;
+                    }
         }
 
         float ecf[5];
@@ -263,127 +311,126 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         float rho_prev = 0.0f;
         bool unstable = false;
         float gmax = 0.0f;
-        bool nonfinite = false;
+        unsigned hmax = 0u;
         double dmax_l = 0.0;
         unsigned limps_l = 0;
 
-        for (int g0 = 0; g0 < L; g0 += Gmax) {
-            const int gl = (L - g0) < Gmax ? (L - g0) : Gmax;
-            const bool ts_group = (g0 == 0);
+        {
+            int g0, gl;
+            fp32_group(L, item.z, &g0, &gl);
+            const bool ts_group = (item.z == 0);
+            int scl[kGroup];
+#pragma unroll
+            for (int q = 0; q < kGroup; ++q) scl[q] = q < gl ? s_scale[g0 + q] : 0;
 
-            // Each thread owns a fixed set of slab elements (rows by warp, elements of the
-            // row by lane).  pump(cv, nx_lev): convert the thread's own staged elements of
-            // level cv into FP32 slot cv % 3 (its own cp.async copies are complete after
-            // cp.async.wait_all, so no block barrier guards the stage), then cp.async its
-            // elements of level nx_lev into the stage.  Land cells are zero-filled instead
-            // of copied: their values only ever meet zero coefficients.
-            auto pump = [&](int cv, int nx_lev) {
-                float *F = Fb + (size_t)(cv % 3) * gl * ncp;
-                float *FL = FLb + (size_t)(cv % 3) * 2 * ncp;
-                const int rowlen = nx * gl;
-                const int dc = 32 / gl, dl = 32 % gl;
-                for (int r = warp; r < ny; r += nwarp) {
-                    const int gj = j0 - 1 + r;
-                    double *Srow = stage + (size_t)r * rowlen;
-                    const int *krow = k1t + r * nx;
-                    const bool rowok = gj <= maxj + 1;
-                    const size_t rowbase = (size_t)NI * ((size_t)gj + (size_t)NJ * (size_t)nx_lev);
-                    int c = lane / gl, q = lane % gl;
-                    for (int e = lane; e < rowlen; e += 32) {
-                        if (cv >= 0) {
-                            const double x = Srow[e];
-                            const int sl = s_scale[g0 + q];
-                            const float h = d2f_scaled(x, sl);
-                            const int cc = r * nx + c;
-                            F[q * ncp + cc] = h;
-                            if (ts_group && q < 2) FL[q * ncp + cc] = d2f_scaled(x - f2d_scaled(h, sl), sl);
-                        }
-                        if (nx_lev >= 0) {
-                            int gi = i0 - 1 + c;
-                            if (rowok && gi <= maxi + 1 && nx_lev >= krow[c]) {
-                                if (gi == 0) gi = maxi;
-                                else if (gi == maxi + 1) gi = 1;
-                                cp_async8(Srow + e, R + ((size_t)gi + rowbase) * L + g0 + q);
-                            } else {
-                                Srow[e] = 0.0;
-                            }
-                        }
-                        c += dc;
-                        q += dl;
-                        if (q >= gl) {
-                            q -= gl;
-                            c += 1;
-                        }
+            double xr[kGroup];
+            // this slot's FP64 values of level lev (if wet there) into xr
+            auto load_level = [&](int lev) {
+                if (lev >= kown) {
+                    const double *p = R + LNIJ * lev + goffs + g0;
+#pragma unroll
+                    for (int q = 0; q < kGroup; ++q)
+                        if (q < gl) xr[q] = ldg_d(p + q);
+                }
+            };
+            // xr (level lev) -> this slot's scaled FP32 slab entries of lev (and lo of T and S)
+            auto convert_level = [&](int lev, int buf) {
+                if (lev >= kown) {
+                    float *F = slab + (buf * P + t) * kGP;
+#pragma unroll
+                    for (int q = 0; q < kGroup; ++q) {
+                        if (q >= gl) continue;
+                        const float h = d2f_scaled(xr[q], scl[q]);
+                        F[q] = h;
+                        if (ts_group && q < 2) slo[(buf * P + t) * 3 + q] = d2f_scaled(xr[q] - f2d_scaled(h, scl[q]), scl[q]);
                     }
                 }
-                cp_async_commit();
             };
 
-            for (int e = t; e < gl * nin; e += blockDim.x) QB[e] = 0;
-            if (ts_group)
-                for (int e = t; e < 4 * nin; e += blockDim.x) QBD[e] = 0.0f;
-            // prologue: slabs kstart and kstart+1 converted, kstart+2 in flight
-            pump(-1, kstart);
-            cp_async_wait_all();
-            pump(kstart, kstart + 1 <= maxk ? kstart + 1 : -1);
-            if (kstart + 1 <= maxk) {
-                cp_async_wait_all();
-                pump(kstart + 1, kstart + 2 <= maxk ? kstart + 2 : -1);
-            }
-            __syncthreads();
+            int carry[kGroup];
+#pragma unroll
+            for (int q = 0; q < kGroup; ++q) carry[q] = 0;
+            dflt carryT[2] = {{0.f, 0.f}, {0.f, 0.f}};
+
+            // prologue: level kstart in the slab, kstart+1 in registers
+            int bk = kstart % 3;
+            load_level(kstart);
+            convert_level(kstart, bk);
+            if (kstart + 1 <= maxk) load_level(kstart + 1);
 
             for (int k = kstart; k <= maxk; ++k) {
-                const float *Sk = Fb + (size_t)(k % 3) * gl * ncp;
-                const float *Su = Fb + (size_t)((k + 1) % 3) * gl * ncp;
-                const float *SkL = FLb + (size_t)(k % 3) * 2 * ncp;
-                const float *SuL = FLb + (size_t)((k + 1) % 3) * 2 * ncp;
-                if (inside && k >= k1c) {
-                    const size_t cl = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
+                const int bk1 = bk == 2 ? 0 : bk + 1;
+                // ---- this slot: convert level k+1, start the loads of k+2
+                if (k + 1 <= maxk) {
+                    convert_level(k + 1, bk1);
+                    if (k + 2 <= maxk) load_level(k + 2);
+                }
+                __syncthreads();
+                // ---- interior column wet at k: transfers of level k and the FP64 update
+                if (interior && k >= k1c) {
+                    const double *Rk = R + LNIJ * k + goffs + g0;
+                    double *Wk = W + LNIJ * k + goffs + g0;
+                    const size_t cl = (size_t)cl0 + nij * (size_t)(k - 1);
                     const float *cf = md.coef + 12 * cl;
-                    const int iw = (i == 1) ? maxi : i - 1;
-                    const float *cw = md.coef + 12 * ((size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1)));
-                    const dflt AeX = {__ldg(cf + 0), __ldg(cf + 6)}, BeX = {__ldg(cf + 1), __ldg(cf + 7)};
-                    const dflt AnX = {__ldg(cf + 2), __ldg(cf + 8)}, BnX = {__ldg(cf + 3), __ldg(cf + 9)};
-                    const dflt AaX = {__ldg(cf + 4), __ldg(cf + 10)}, BaX = {__ldg(cf + 5), __ldg(cf + 11)};
-                    const dflt AwX = {__ldg(cw + 0), __ldg(cw + 6)}, BwX = {__ldg(cw + 1), __ldg(cw + 7)};
-                    dflt AsX = {0.0f, 0.0f}, BsX = {0.0f, 0.0f};
-                    if (j > 1) {
-                        const float *cs = md.coef + 12 * (cl - (size_t)maxi);
-                        AsX = {__ldg(cs + 2), __ldg(cs + 8)};
-                        BsX = {__ldg(cs + 3), __ldg(cs + 9)};
-                    }
-                    const bool top = (k == maxk);
+                    const float4 a4 = __ldg(reinterpret_cast<const float4 *>(cf));        // Ae Be An Bn
+                    const float2 a2 = __ldg(reinterpret_cast<const float2 *>(cf + 4));    // Aa Ba
+                    const float *cw = md.coef + 12 * ((size_t)cw0 + nij * (size_t)(k - 1));
+                    const float2 w2 = __ldg(reinterpret_cast<const float2 *>(cw));        // Ae Be of the west cell
+                    float2 s2 = make_float2(0.f, 0.f);
+                    if (j > 1) s2 = __ldg(reinterpret_cast<const float2 *>(cf - 12 * (size_t)maxi + 2));  // An Bn south
                     const double rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
-                    const size_t base = (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)k));
-                    const float *gt = md.gtop + (size_t)(L + 2) * ((size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1));
+                    const bool top = (k == maxk);
+                    const float *gt = md.gtop + (size_t)(L + 2) * (size_t)cl0;
+                    const float *Fk = slab + bk * P * kGP;
+                    const float *Fu = slab + bk1 * P * kGP;
+                    const float *pC = Fk + t * kGP, *pE = Fk + sE * kGP, *pW = Fk + sW * kGP;
+                    const float *pN = Fk + sN * kGP, *pS = Fk + sS * kGP, *pU = Fu + t * kGP;
+                    const int sC = t;
+
+                    // top-face stencil: C1*T(k+1) + C0*T(k) (+ isoneutral terms)
                     bool iso = false;
-                    // top-face stencil: C1*T(k+1) + C0*T(k) (+ isoneutral corners)
-                    dflt C1X = AaX, C0X = BaX;
+                    dflt C1X = {a2.x, 0.f}, C0X = {a2.y, 0.f};
                     dflt W0X = {0.f, 0.f}, E0X = {0.f, 0.f}, S0X = {0.f, 0.f}, N0X = {0.f, 0.f};
                     dflt W1X = {0.f, 0.f}, E1X = {0.f, 0.f}, S1X = {0.f, 0.f}, N1X = {0.f, 0.f};
-                    if (md.diso && !top) {
+                    dflt AeX = {a4.x, 0.f}, BeX = {a4.y, 0.f}, AnX = {a4.z, 0.f}, BnX = {a4.w, 0.f};
+                    dflt AwX = {w2.x, 0.f}, BwX = {w2.y, 0.f}, AsX = {s2.x, 0.f}, BsX = {s2.y, 0.f};
+                    if (ts_group || (ISO && md.diso && !top)) {
+                        // lo parts of the coefficients (T and S use the FP32 pair; the isoneutral
+                        // stencil is built from the FP64 coefficient)
+                        const float2 l2 = __ldg(reinterpret_cast<const float2 *>(cf + 6));   // lo Aa Ba
+                        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(cf + 8));   // lo Ae Be An Bn
+                        const float2 lw = __ldg(reinterpret_cast<const float2 *>(cw + 8));
+                        float2 ls = make_float2(0.f, 0.f);
+                        if (j > 1) ls = __ldg(reinterpret_cast<const float2 *>(cf - 12 * (size_t)maxi + 10));
+                        C1X.lo = l2.x; C0X.lo = l2.y;
+                        AeX.lo = l4.x; BeX.lo = l4.y; AnX.lo = l4.z; BnX.lo = l4.w;
+                        AwX.lo = lw.x; BwX.lo = lw.y; AsX.lo = ls.x; BsX.lo = ls.y;
+                    }
+                    if (ISO && md.diso && !top) {
                         // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
                         // state: the density differences scc*dS - tec*dT cancel strongly in weakly
                         // stratified water; they are differences of D = ec(2)*S - tec*T with the
                         // cell's tec (goldstein.f90:2587-2588)
                         auto ld = [&](int ii, int jj, int kk, int l) {
-                            return __ldg(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
+                            return ldg_d(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
                         };
                         const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
-                        const double s1 = ld(i, j, k, 1), s2 = ld(i, j, k + 1, 1);
+                        const double s1 = ld(i, j, k, 1), s2v = ld(i, j, k + 1, 1);
                         const double tatw = 0.5 * (t1 + t2);
                         double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
                         if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
                         const double scc = md.ec[1];
-                        const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
+                        const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2v - tec * t2;
                         const double rdza = mk[4 * mkn + k];
                         const double dzrho = (Dc1 - Dc0) * rdza;
                         if (dzrho < -1.0e-12) {
                             iso = true;
                             const double rdzrho = 1.0 / dzrho;
-                            const double rcr = mj[j];                          // rc(j)*rdphi
+                            const double rcr = mj[j];                                 // rc(j)*rdphi
                             const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
                             const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
+                            const int k1E = k1nb & 0xff, k1W = (k1nb >> 8) & 0xff, k1N = (k1nb >> 16) & 0xff,
+                                      k1S = (k1nb >> 24) & 0xff;
                             double dxr[4], dyr[4], mx[4], my[4];
                             double tv1 = 0.0;
 #pragma unroll
@@ -393,8 +440,8 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                                 for (int nnp = 0; nnp <= 1; ++nnp) {
                                     const int ina = nnp + 2 * knp;
                                     const int kk = k + knp;
-                                    const bool okx = kk >= k1t[cidx + (nnp ? 1 : -1)];
-                                    const bool oky = kk >= k1t[cidx + (nnp ? nx : -nx)];
+                                    const bool okx = kk >= (nnp ? k1E : k1W);
+                                    const bool oky = kk >= (nnp ? k1N : k1S);
                                     mx[ina] = okx ? rcr : 0.0;
                                     my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
                                     dxr[ina] = 0.0;
@@ -431,53 +478,65 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                                 wy[n] = two_dz * dyr[n] * my[n];
                             }
                             const double wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
-                            const double c0d = f2d_scaled(BaX.hi, 0) + f2d_scaled(BaX.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
-                            const double c1d = f2d_scaled(AaX.hi, 0) + f2d_scaled(AaX.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
-                            C0X = df_split(c0d);
-                            C1X = df_split(c1d);
-                            W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
-                            S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
+                            const double c0d = f2d_scaled(C0X.hi, 0) + f2d_scaled(C0X.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
+                            const double c1d = f2d_scaled(C1X.hi, 0) + f2d_scaled(C1X.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
+                            if (ts_group) {
+                                C0X = df_split(c0d);
+                                C1X = df_split(c1d);
+                                W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
+                                S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
+                            } else {
+                                // the other tracers use the FP32 part only (the FP32 part of the pair)
+                                C0X.hi = d2f_scaled(c0d, 0); C1X.hi = d2f_scaled(c1d, 0);
+                                W0X.hi = d2f_scaled(-wx[0], 0); E0X.hi = d2f_scaled(wx[1], 0);
+                                W1X.hi = d2f_scaled(-wx[2], 0); E1X.hi = d2f_scaled(wx[3], 0);
+                                S0X.hi = d2f_scaled(-wy[0], 0); N0X.hi = d2f_scaled(wy[1], 0);
+                                S1X.hi = d2f_scaled(-wy[2], 0); N1X.hi = d2f_scaled(wy[3], 0);
+                            }
                         }
                     }
-                    const int cE = cidx + 1, cW = cidx - 1, cN = cidx + nx, cS = cidx - nx;
-                    int q0 = 0;
+                    const float *pUE = Fu + sE * kGP, *pUW = Fu + sW * kGP, *pUN = Fu + sN * kGP, *pUS = Fu + sS * kGP;
+                    const unsigned amask = __activemask();
                     if (ts_group) {
                         // T and S: double-float transfers, FP64 update
+                        const float *Lk = slo + bk * P * 3, *Lu = slo + bk1 * P * 3;
                         double tn[2];
 #pragma unroll
                         for (int l = 0; l < 2; ++l) {
-                            const float *F = Sk + l * ncp, *FL = SkL + l * ncp;
-                            const float *U = Su + l * ncp, *UL = SuL + l * ncp;
-                            const dflt Tc = {F[cidx], FL[cidx]}, TE = {F[cE], FL[cE]}, TW = {F[cW], FL[cW]};
-                            const dflt TN = {F[cN], FL[cN]}, TS = {F[cS], FL[cS]};
-                            const dflt Ge = df_dot2(AeX, TE, BeX, Tc);
-                            const dflt Gw = df_dot2(AwX, Tc, BwX, TW);
-                            const dflt Gn = df_dot2(AnX, TN, BnX, Tc);
-                            const dflt Gs = df_dot2(AsX, Tc, BsX, TS);
-                            const int sl = s_scale[l];
+                            const double told = Rk[l];
+                            const dflt Tc = {pC[l], Lk[sC * 3 + l]};
+                            const int sl = scl[l];
+                            // sum = (Gw - Ge) + (Gs - Gn) + (Gb - Ga), faces formed as needed
+                            dflt sum;
+                            {
+                                const dflt TE = {pE[l], Lk[sE * 3 + l]}, TW = {pW[l], Lk[sW * 3 + l]};
+                                sum = df_sub(df_dot2(AwX, Tc, BwX, TW), df_dot2(AeX, TE, BeX, Tc));
+                            }
+                            {
+                                const dflt TN = {pN[l], Lk[sN * 3 + l]}, TS = {pS[l], Lk[sS * 3 + l]};
+                                sum = df_add(sum, df_sub(df_dot2(AsX, Tc, BsX, TS), df_dot2(AnX, TN, BnX, Tc)));
+                            }
                             dflt Ga;
                             if (top) {
                                 const float sc = __int_as_float((127 + sl) << 23);
                                 Ga = {__ldg(gt + l) * sc, __ldg(gt + L + l) * sc};
                             } else {
-                                Ga = df_dot2(C1X, dflt{U[cidx], UL[cidx]}, C0X, Tc);
-                                if (iso) {
+                                Ga = df_dot2(C1X, dflt{pU[l], Lu[sC * 3 + l]}, C0X, Tc);
+                                if (ISO && iso) {
+                                    const dflt TE = {pE[l], Lk[sE * 3 + l]}, TW = {pW[l], Lk[sW * 3 + l]};
+                                    const dflt TN = {pN[l], Lk[sN * 3 + l]}, TS = {pS[l], Lk[sS * 3 + l]};
                                     Ga = df_add(Ga, df_dot2(W0X, TW, E0X, TE));
                                     Ga = df_add(Ga, df_dot2(S0X, TS, N0X, TN));
-                                    Ga = df_add(Ga, df_dot2(W1X, dflt{U[cW], UL[cW]}, E1X, dflt{U[cE], UL[cE]}));
-                                    Ga = df_add(Ga, df_dot2(S1X, dflt{U[cS], UL[cS]}, N1X, dflt{U[cN], UL[cN]}));
+                                    Ga = df_add(Ga, df_dot2(W1X, dflt{pUW[l], Lu[sW * 3 + l]}, E1X, dflt{pUE[l], Lu[sE * 3 + l]}));
+                                    Ga = df_add(Ga, df_dot2(S1X, dflt{pUS[l], Lu[sS * 3 + l]}, N1X, dflt{pUN[l], Lu[sN * 3 + l]}));
                                 }
                             }
-                            float *qb = QBD + (2 * l) * nin + cell;
-                            const dflt Gb = {qb[0], qb[nin]};
-                            const dflt sum = df_add(df_add(df_sub(Gw, Ge), df_sub(Gs, Gn)), df_sub(Gb, Ga));
-                            qb[0] = Ga.hi;
-                            qb[nin] = Ga.lo;
+                            sum = df_add(sum, df_sub(carryT[l], Ga));
+                            carryT[l] = Ga;
                             const double dlt = f2d_scaled(sum.hi, sl) + f2d_scaled(sum.lo, sl);
-                            const double told = R[base + l];
                             tn[l] = fma(dlt, rv, told);
-                            W[base + l] = tn[l];
-                            if (((unsigned)__double2hiint(tn[l]) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
+                            Wk[l] = tn[l];
+                            hmax = max(hmax, (unsigned)__double2hiint(tn[l]) & 0x7fffffffu);
                         }
                         // FP32 density prescreen for the exact convective adjustment
                         const float tf = d2f_scaled(tn[0], 0), sf = d2f_scaled(tn[1], 0);
@@ -489,38 +548,36 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             if (!(rho_prev - rf > margin)) unstable = true;
                         }
                         rho_prev = rf;
-                        q0 = 2;
                     }
-                    // other tracers: FP32 transfers rounded once to int32
+                    // other tracers: FP32 transfers rounded once to int32, FP64 update
                     const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
                     const float As = AsX.hi, Bs = BsX.hi;
                     const float cC0 = C0X.hi, cC1 = C1X.hi, cW0 = W0X.hi, cE0 = E0X.hi, cS0 = S0X.hi, cN0 = N0X.hi;
                     const float cW1 = W1X.hi, cE1 = E1X.hi, cS1 = S1X.hi, cN1 = N1X.hi;
-                    const unsigned amask = __activemask();
-                    for (int q = q0; q < gl; ++q) {
-                        const int l = g0 + q;
-                        const float *F = Sk + q * ncp;
-                        const float Tc = F[cidx], TE = F[cE], TW = F[cW], TN = F[cN], TS = F[cS];
+                    const int q0 = ts_group ? 2 : 0;
+#pragma unroll
+                    for (int q = 0; q < kGroup; ++q) {
+                        if (q < q0 || q >= gl) continue;
+                        const double told = Rk[q];
+                        const float Tc = pC[q], TE = pE[q], TW = pW[q], TN = pN[q], TS = pS[q];
                         const float ge = fmaf(Ae, TE, Be * Tc);
                         const float gw = fmaf(Aw, Tc, Bw * TW);
                         const float gn = fmaf(An, TN, Bn * Tc);
                         const float gs = fmaf(As, Tc, Bs * TS);
-                        const int sl = s_scale[l];
                         float ga;
                         if (top) {
-                            ga = __ldg(gt + l) * __int_as_float((127 + sl) << 23);
+                            ga = __ldg(gt + g0 + q) * __int_as_float((127 + scl[q]) << 23);
                         } else {
-                            const float *U = Su + q * ncp;
-                            ga = fmaf(cC1, U[cidx], cC0 * Tc);
-                            if (iso) {
+                            ga = fmaf(cC1, pU[q], cC0 * Tc);
+                            if (ISO && iso) {
                                 ga = fmaf(cW0, TW, ga);
                                 ga = fmaf(cE0, TE, ga);
                                 ga = fmaf(cS0, TS, ga);
                                 ga = fmaf(cN0, TN, ga);
-                                ga = fmaf(cW1, U[cW], ga);
-                                ga = fmaf(cE1, U[cE], ga);
-                                ga = fmaf(cS1, U[cS], ga);
-                                ga = fmaf(cN1, U[cN], ga);
+                                ga = fmaf(cW1, pUW[q], ga);
+                                ga = fmaf(cE1, pUE[q], ga);
+                                ga = fmaf(cS1, pUS[q], ga);
+                                ga = fmaf(cN1, pUN[q], ga);
                             }
                         }
                         if (track) {
@@ -529,69 +586,34 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             const float gm = fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga)));
                             gmax = fmaxf(gmax, gm);
                             const unsigned wmax = __reduce_max_sync(amask, __float_as_uint(gm));
-                            if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[l], wmax);
+                            if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[g0 + q], wmax);
                         }
                         const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
                         const int qn = __float2int_rn(gn), qs = __float2int_rn(gs);
                         const int qa = __float2int_rn(ga);
-                        int *qbp = QB + q * nin + cell;
-                        const int sum = (qw - qe) + (qs - qn) + (*qbp - qa);
-                        *qbp = qa;
-                        const double told = R[base + l];
-                        const double tnew = fma(i2d_scaled(sum, sl), rv, told);
-                        W[base + l] = tnew;
-                        if (((unsigned)__double2hiint(tnew) & 0x7ff00000u) == 0x7ff00000u) nonfinite = true;
+                        const int sum = (qw - qe) + (qs - qn) + (carry[q] - qa);
+                        carry[q] = qa;
+                        const double tnew = fma(i2d_scaled(sum, scl[q]), rv, told);
+                        Wk[q] = tnew;
+                        hmax = max(hmax, (unsigned)__double2hiint(tnew) & 0x7fffffffu);
                     }
                 }
-                // the thread's own copies of level k+2 -> FP32 slot of k+2; start level k+3
-                if (k + 2 <= maxk) {
-                    cp_async_wait_all();
-                    pump(k + 2, k + 3 <= maxk ? k + 3 : -1);
-                }
-                __syncthreads();
+                bk = bk1;
             }
+            // the next item's prologue writes slab buffers the last levels read
+            __syncthreads();
         }
 
-        // exact convective adjustment of columns that may be unstable
-        if (inside && k1c <= maxk) {
-            const size_t c2 = (size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1);
-            if (unstable || md.iconv == 1 || md.ieos != 0) {
-                Fp32Col col;
-                col.w = W;
-                col.stat = md.ts_static;
-                col.L = L;
-                col.NI = NI;
-                col.NJ = NJ;
-                col.i = i;
-                col.j = j;
-                col.k1 = k1c;
-                EosCoef ec;
-                for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
-                ec.ieos = md.ieos;
-                const double *dz = mk, *rdz = mk + mkn, *zw = mk + 2 * mkn, *zro = mk + 3 * mkn;
-                col.rho[0] = 0.0;
-                for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
-                int icos = 0;
-                if (md.iconv == 1) icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
-                const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
-                if (md.iconv == 1) {
-                    if (filled > icos) icos = filled;
-                    md.icosd[c2] = icos;
-                    md.cost[c2] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
-                } else if (filled > 0) {
-                    double cst = md.cost[c2];
-                    for (int f = 0; f < filled; ++f) cst = __dadd_rn(cst, 1.0);
-                    md.cost[c2] = cst;
-                }
-            }
-        }
-        if (md.diso) {
+        // columns whose density profile may be unstable: exact convective adjustment next
+        if (item.z == 0 && interior) md.coflag[cl0] = unstable ? 1 : 0;
+        if (ISO && md.diso) {
             unsigned long long *dg = md.diag + 2 * (step & 1);
             unsigned long long db = __double_as_longlong(dmax_l);
             if (db) atomicMax(&dg[0], db);
             if (limps_l) atomicAdd(&dg[1], (unsigned long long)limps_l);
         }
         // a scaled transfer above 3.5e8 could overflow the int32 sum of six faces
+        const bool nonfinite = hmax >= 0x7ff00000u;
         if (nonfinite || gmax > 3.5e8f) atomicOr(md.status, (nonfinite ? 1u : 0u) | (gmax > 3.5e8f ? 2u : 0u));
         __syncthreads();
         if (track)
@@ -625,50 +647,275 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
-int fp32_smem_bytes(int tile_i, int tile_j, int L) { return fp32_smem_layout(tile_i, tile_j, L).total; }
-
-int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int lmax, int smem_bytes,
-                const long long *step_ctr, int rel, cudaStream_t s)
+// Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step flagged
+// (all columns with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  An item is
+// (member, patch table offset): thread t takes the patch's interior column t.
+__global__ void __launch_bounds__(kFp32Threads)
+k_co_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
+          const long long *__restrict__ step_ctr, int rel)
 {
-    (void)lmax;
+    const long long step = *step_ctr + rel;
+    const int t = threadIdx.x;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int4 item = items[it];
+        const MemberDesc &md = mds[item.x];
+        if (step >= md.stop_step) continue;
+        const int32_t *tab = md.ptab + item.y;
+        const int ns = tab[0], ni = tab[1], maxk = md.maxk;
+        if (t >= ni) continue;
+        const int32_t *ticol = tab + ((kPatchHdr + 2 * (maxk + 2) + ns + 3) & ~3) + kIcolWords * t;
+        const int k1c = (ticol[2] >> 16) & 0xffff, cl0 = ticol[3];
+        const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
+        if (!(md.coflag[cl0] || md.iconv == 1 || md.ieos != 0)) continue;
+        const int par = (int)((step + md.parity) & 1);
+        const int L = md.L, mkn = maxk + 2;
+        const double *mk = md.mk;
+        Fp32Col col;
+        col.w = md.buf[par ^ 1];
+        col.stat = md.ts_static;
+        col.L = L;
+        col.NI = md.NI;
+        col.NJ = md.NJ;
+        col.i = i;
+        col.j = j;
+        col.k1 = k1c;
+        EosCoef ec;
+        for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
+        ec.ieos = md.ieos;
+        const double *dz = mk, *rdz = mk + mkn, *zw = mk + 2 * mkn, *zro = mk + 3 * mkn;
+        col.rho[0] = 0.0;
+        for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
+        int icos = 0;
+        if (md.iconv == 1) icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
+        const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
+        if (md.iconv == 1) {
+            if (filled > icos) icos = filled;
+            md.icosd[cl0] = icos;
+            md.cost[cl0] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
+        } else if (filled > 0) {
+            double cst = md.cost[cl0];
+            for (int f = 0; f < filled; ++f) cst = __dadd_rn(cst, 1.0);
+            md.cost[cl0] = cst;
+        }
+    }
+}
+
+int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).total; }
+
+int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, const int4 *co_items, int nco,
+                int max_slots, const long long *step_ctr, int rel, int *work, bool iso, cudaStream_t s)
+{
     static int nsm = 0;
     if (!nsm) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    cudaFuncSetAttribute(k_step_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    const int P = max_slots + 1;
+    const int smem_bytes = fp32_smem_layout(P).total;
+    auto kern = iso ? k_step_fp32<true> : k_step_fp32<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_fp32, kFp32Threads, smem_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
     if (per_sm < 1) per_sm = 1;
     int grid = std::min(nitems, nsm * per_sm);
     if (grid < 1) grid = 1;
-    k_step_fp32<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel);
+    kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P);
+    k_co_fp32<<<std::max(1, std::min(nco, 4 * nsm)), kFp32Threads, 0, s>>>(descs, co_items, nco, step_ctr, rel);
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
-void fp32_default_tile(int maxi, int maxj, int *ti, int *tj)
+// ---------------------------------------------------------------------------
+// patch plan (host): rectangles of water columns, periodic in i, with the ring of
+// wet neighbour columns; slots sorted by k1 so the wet cells of a level are a prefix
+
+int fp32_group_count(int L) { return fp32_ngroups(L); }
+
+// one thread per slot; slot indices are 16-bit in the tables
+static int plan_cap_slots(int) { return kFp32Threads; }
+
+namespace {
+struct PatchShape {
+    std::vector<std::pair<int, int>> inner;   // (i, j) wet columns of the rectangle
+    std::vector<std::pair<int, int>> ring;    // wet neighbours outside it
+};
+}
+
+// Columns of rectangle [i0, i1] x [j0, j1] and its ring; false if over the kernel limits.
+static bool patch_shape(const Dims &d, const int32_t *k1, int i0, int i1, int j0, int j1, int cap, PatchShape &ps)
 {
-    // whole rows when the grid is narrow, else 32 x 4 (<= 128 threads, <= 64 wide)
-    int best_i = 16, best_j = 8;
-    double best = 1e30;
-    for (int tx = 4; tx <= 64; ++tx) {
-        for (int ty = 1; ty <= 32 && tx * ty <= kFp32Threads; ++ty) {
-            if (tx * ty < 64) continue;
-            const int nti = (maxi + tx - 1) / tx, ntj = (maxj + ty - 1) / ty;
-            // cost: halo'd slab cells loaded + idle threads
-            const double load = (double)nti * ntj * (tx + 2) * (ty + 2);
-            const double idle = (double)nti * ntj * tx * ty - (double)maxi * maxj;
-            const double c = load + 0.5 * idle;
-            if (c < best) {
-                best = c;
-                best_i = tx;
-                best_j = ty;
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
+    auto wet = [&](int i, int j) { return j >= 0 && j <= maxj + 1 && k1[i + (size_t)NI * j] <= maxk; };
+    auto inside = [&](int i, int j) { return i >= i0 && i <= i1 && j >= j0 && j <= j1; };
+    ps.inner.clear();
+    ps.ring.clear();
+    for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i)
+            if (wet(i, j)) ps.inner.push_back({i, j});
+    if ((int)ps.inner.size() > kFp32Threads) return false;
+    std::vector<char> seen((size_t)NI * (maxj + 2), 0);
+    for (auto &c : ps.inner) {
+        const int i = c.first, j = c.second;
+        const int nb[4][2] = {{i == maxi ? 1 : i + 1, j}, {i == 1 ? maxi : i - 1, j}, {i, j + 1}, {i, j - 1}};
+        for (auto &n : nb) {
+            if (n[1] < 0 || n[1] > maxj + 1 || inside(n[0], n[1]) || !wet(n[0], n[1])) continue;
+            char &s = seen[n[0] + (size_t)NI * n[1]];
+            if (!s) {
+                s = 1;
+                ps.ring.push_back({n[0], n[1]});
             }
         }
     }
-    *ti = best_i;
-    *tj = best_j;
+    return (int)(ps.inner.size() + ps.ring.size()) <= cap;
+}
+
+// Estimated issue cost of a tiling: per patch, level and tracer group, the warps that hold
+// wet interior slots (load, convert, transfers, update: ~60 instructions per tracer) and
+// wet ring slots (load and convert: ~10), plus a per-level overhead of the CTA.
+static double plan_cost(const Dims &d, const int32_t *k1, int tx, int ty, int cap, bool *ok)
+{
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
+    const int ng = (d.L + kGroup - 1) / kGroup;
+    const double per_t = (double)d.L / ng;
+    double cost = 0.0;
+    PatchShape ps;
+    std::vector<int> hi(maxk + 2), hr(maxk + 2);
+    *ok = true;
+    for (int j0 = 1; j0 <= maxj; j0 += ty)
+        for (int i0 = 1; i0 <= maxi; i0 += tx) {
+            if (!patch_shape(d, k1, i0, std::min(maxi, i0 + tx - 1), j0, std::min(maxj, j0 + ty - 1), cap, ps)) {
+                *ok = false;
+                return 0.0;
+            }
+            if (ps.inner.empty()) continue;
+            std::fill(hi.begin(), hi.end(), 0);
+            std::fill(hr.begin(), hr.end(), 0);
+            int kst = maxk + 1;
+            for (auto &c : ps.inner) {
+                const int kk = k1[c.first + (size_t)NI * c.second];
+                hi[kk] += 1;
+                kst = std::min(kst, kk);
+            }
+            for (auto &c : ps.ring) hr[std::max(kst, (int)k1[c.first + (size_t)NI * c.second])] += 1;
+            int ni = 0, nr = 0;
+            for (int k = 1; k <= maxk; ++k) {
+                ni += hi[k];
+                nr += hr[k];
+                if (k < kst) continue;
+                cost += ng * (std::ceil(ni / 32.0) * 32 * 60 * per_t + std::ceil(nr / 32.0) * 32 * 10 * per_t + 256 * 20);
+            }
+        }
+    return cost;
+}
+
+int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, PatchPlan &plan)
+{
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
+    const int cap = plan_cap_slots(d.L);
+    int best_tx = 0, best_ty = 0;
+    if (tile_i > 0 && tile_j > 0) {
+        bool ok = false;
+        plan_cost(d, k1, std::min(tile_i, maxi), std::min(tile_j, maxj), cap, &ok);
+        if (ok) {
+            best_tx = std::min(tile_i, maxi);
+            best_ty = std::min(tile_j, maxj);
+        }
+    }
+    if (!best_tx) {
+        double best = 1e300;
+        for (int tx = maxi; tx >= 1; --tx) {
+            // widths that split the rows evenly (or nearly)
+            const int nti = (maxi + tx - 1) / tx;
+            if (tx != (maxi + nti - 1) / nti) continue;
+            for (int ty = 1; ty <= maxj; ++ty) {
+                const int ntj = (maxj + ty - 1) / ty;
+                if (ty != (maxj + ntj - 1) / ntj) continue;
+                if (tx * ty > 4 * kFp32Threads) break;
+                bool ok = false;
+                const double c = plan_cost(d, k1, tx, ty, cap, &ok);
+                if (ok && c < best) {
+                    best = c;
+                    best_tx = tx;
+                    best_ty = ty;
+                }
+            }
+        }
+    }
+    if (!best_tx) return GB_GO_ERANGE;
+    plan.words.clear();
+    plan.offset.clear();
+    plan.cost.clear();
+    plan.max_slots = 1;
+    plan.tile_i = best_tx;
+    plan.tile_j = best_ty;
+    PatchShape ps;
+    int pidx = 0;
+    for (int j0 = 1; j0 <= maxj; j0 += best_ty)
+        for (int i0 = 1; i0 <= maxi; i0 += best_tx) {
+            patch_shape(d, k1, i0, std::min(maxi, i0 + best_tx - 1), j0, std::min(maxj, j0 + best_ty - 1), cap, ps);
+            if (ps.inner.empty()) continue;
+            struct Slot { int k1, j, i, inner; };
+            std::vector<Slot> sl;
+            for (auto &c : ps.inner) sl.push_back({k1[c.first + (size_t)NI * c.second], c.second, c.first, 1});
+            for (auto &c : ps.ring) sl.push_back({k1[c.first + (size_t)NI * c.second], c.second, c.first, 0});
+            // interior slots first, then the ring; each part by k1 (then row, column)
+            std::stable_sort(sl.begin(), sl.end(), [](const Slot &a, const Slot &b) {
+                if (a.inner != b.inner) return a.inner > b.inner;
+                if (a.k1 != b.k1) return a.k1 < b.k1;
+                if (a.j != b.j) return a.j < b.j;
+                return a.i < b.i;
+            });
+            const int ns = (int)sl.size(), ni = (int)ps.inner.size();
+            std::vector<int> slot_of((size_t)NI * (maxj + 2), -1);
+            for (int s = 0; s < ns; ++s) slot_of[sl[s].i + (size_t)NI * sl[s].j] = s;
+            int kst = maxk + 1;
+            for (auto &s : sl)
+                if (s.inner) kst = std::min(kst, s.k1);
+            const size_t off = plan.words.size();
+            plan.offset.push_back((int32_t)off);
+            std::vector<int32_t> w(kPatchHdr + 2 * (maxk + 2) + ns, 0);
+            w[0] = ns;
+            w[1] = ni;
+            w[2] = kst;
+            w[3] = pidx++;
+            for (int k = 0; k <= maxk + 1; ++k) {
+                int a = 0, r = 0;
+                for (auto &x : sl)
+                    if (x.k1 <= k) (x.inner ? a : r) += 1;
+                w[kPatchHdr + k] = a;
+                w[kPatchHdr + maxk + 2 + k] = r;
+            }
+            for (int s = 0; s < ns; ++s) w[kPatchHdr + 2 * (maxk + 2) + s] = d.L * (sl[s].i + NI * sl[s].j);
+            while (w.size() & 3) w.push_back(0);
+            auto nbslot = [&](int i, int j) -> int {
+                if (j < 0 || j > maxj + 1) return 0xffff;
+                const int s = slot_of[i + (size_t)NI * j];
+                return s < 0 ? 0xffff : s;
+            };
+            auto k1c8 = [&](int i, int j) -> int {
+                if (j < 0 || j > maxj + 1) return 255;
+                return std::min(255, (int)k1[i + (size_t)NI * j]);
+            };
+            double cost = 0.0;
+            for (int s = 0; s < ns; ++s) {
+                if (!sl[s].inner) continue;
+                const int i = sl[s].i, j = sl[s].j;
+                const int ie = i == maxi ? 1 : i + 1, iw = i == 1 ? maxi : i - 1;
+                w.push_back(s | (nbslot(ie, j) << 16));
+                w.push_back(nbslot(iw, j) | (nbslot(i, j + 1) << 16));
+                w.push_back(nbslot(i, j - 1) | (sl[s].k1 << 16));
+                w.push_back((i - 1) + maxi * (j - 1));
+                w.push_back(i | (j << 16));
+                w.push_back(k1c8(ie, j) | (k1c8(iw, j) << 8) | (k1c8(i, j + 1) << 16) | (k1c8(i, j - 1) << 24));
+                w.push_back((iw - 1) + maxi * (j - 1));
+                w.push_back(0);
+                cost += (double)(maxk - sl[s].k1 + 1) * d.L;
+            }
+            plan.words.insert(plan.words.end(), w.begin(), w.end());
+            plan.cost.push_back(cost);
+            plan.max_slots = std::max(plan.max_slots, ns);
+        }
+    return GB_GO_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -722,9 +969,10 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
                     cd[4] = g * (u3 * (1.0 - ups) * 0.5 - rdza[k] * p.diff2);
                     cd[5] = g * (u3 * (1.0 + ups) * 0.5 + rdza[k] * p.diff2);
                 }
+                // layout: Ae Be An Bn | Aa Ba, lo(Aa) lo(Ba) | lo(Ae) lo(Be) lo(An) lo(Bn)
                 for (int n = 0; n < 6; ++n) {
                     c[n] = (float)cd[n];
-                    c[6 + n] = (float)(cd[n] - (double)c[n]);
+                    c[n < 4 ? 8 + n : 2 + n] = (float)(cd[n] - (double)c[n]);
                 }
                 for (int f = 0; f < 3; ++f)
                     out.cmax = std::max(out.cmax, (double)std::fabs(c[2 * f]) + (double)std::fabs(c[2 * f + 1]));
@@ -888,10 +1136,13 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
             msg = "GB_GO_FP32FLUX needs the same dt on every level (the transfers are shared between levels)";
             return GB_GO_EUNSUPPORTED;
         }
-    int ti = 16, tj = 8;
-    fp32_default_tile(d.maxi, d.maxj, &ti, &tj);
-    if (fp32_smem_bytes(ti, tj, d.L) > 200 * 1024) {
-        msg = "tile does not fit in shared memory";
+    if (d.maxk > kMaxK) {
+        msg = "GB_GO_FP32FLUX supports at most 64 levels";
+        return GB_GO_ERANGE;
+    }
+    PatchPlan plan;
+    if (fp32_plan_patches(d, k1_host, 0, 0, plan) != GB_GO_OK) {
+        msg = "no patch shape fits the FP32-flux kernel limits";
         return GB_GO_ERANGE;
     }
     Fp32Host *h = new Fp32Host();
@@ -902,8 +1153,7 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     h->k1_dev = m.k1;
     h->dt = dtp[1];
     Fp32Data &D = h->data;
-    D.tile_i = ti;
-    D.tile_j = tj;
+    D.max_slots = plan.max_slots;
     const size_t ncell = (size_t)d.maxi * d.maxj * d.maxk;
     cudaError_t e = cudaMalloc(&D.coef, 12 * ncell * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.rvol, (size_t)d.maxj * d.maxk * sizeof(double));
@@ -916,14 +1166,25 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMalloc(&D.status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&D.dev, sizeof(MemberDesc));
     if (e == cudaSuccess) e = cudaMalloc(&D.step_ctr, sizeof(long long));
-    const int nti = (d.maxi + ti - 1) / ti, ntj = (d.maxj + tj - 1) / tj;
-    D.nitems = nti * ntj;
-    if (e == cudaSuccess) e = cudaMalloc(&D.items, (size_t)D.nitems * sizeof(int4));
+    const int ng = fp32_ngroups(d.L);
+    D.nitems = (int)plan.offset.size() * ng;
+    D.nco = (int)plan.offset.size();
+    if (e == cudaSuccess) e = cudaMalloc(&D.work, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(D.work, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.ptab, std::max<size_t>(1, plan.words.size()) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&D.coflag, (size_t)d.maxi * d.maxj);
+    if (e == cudaSuccess) e = cudaMemset(D.coflag, 0, (size_t)d.maxi * d.maxj);
+    if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems + D.nco) * sizeof(int4));
     if (e == cudaSuccess) {
+        // (patch, group) items, longest first (the group of T and S, then the others); then co items
         std::vector<int4> it;
-        for (int b = 0; b < ntj; ++b)
-            for (int a = 0; a < nti; ++a) it.push_back(make_int4(0, 1 + a * ti, 1 + b * tj, ti | (tj << 8)));
-        e = cudaMemcpyAsync(D.items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
+        for (int g = 0; g < ng; ++g)
+            for (size_t n = 0; n < plan.offset.size(); ++n) it.push_back(make_int4(0, plan.offset[n], g, 0));
+        for (size_t n = 0; n < plan.offset.size(); ++n) it.push_back(make_int4(0, plan.offset[n], 0, 0));
+        if (!plan.words.empty())
+            e = cudaMemcpyAsync(D.ptab, plan.words.data(), plan.words.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !it.empty())
+            e = cudaMemcpyAsync(D.items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(D.status, 0, sizeof(unsigned int), s);
@@ -945,7 +1206,8 @@ void fp32_member_free(Fp32Member *f)
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
     cudaFree(D.coef); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
-    cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr);
+    cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
+    cudaFree(D.coflag);
     delete h;
     f->impl = nullptr;
     f->ready = false;
@@ -1015,6 +1277,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.diso = h->p.diso; md.ieos = h->p.ieos; md.iconv = h->p.iconv;
         md.parity = 0;
         md.stop_step = (long long)1 << 62;
+        md.origin = 0;
         md.dt = h->dt; md.dphi = h->p.dphi; md.rdphi = h->p.rdphi; md.diff1 = h->p.diff1;
         for (int n = 0; n < 5; ++n) md.ec[n] = h->p.ec[n];
         md.dsc = h->p.dsc;
@@ -1023,6 +1286,8 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.ts_static = ts_static;
         md.coef = D.coef; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
         md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
+        md.ptab = D.ptab;
+        md.coflag = D.coflag;
         md.status = D.status;
         md.diag = diag;
         if (cudaMemcpyAsync(D.dev, &md, sizeof(md), cudaMemcpyHostToDevice, s) != cudaSuccess) return GB_GO_ECUDA;
@@ -1033,15 +1298,16 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
     D.step_host = D.steps;
     if (cudaMemcpyAsync(D.step_ctr, &D.step_host, sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess)
         return GB_GO_ECUDA;
-    const int smem = fp32_smem_bytes(D.tile_i, D.tile_j, h->d.L);
     for (int n = 0; n < nsteps; ++n) {
         const long long step = D.steps + n;
         if (cudaMemsetAsync(diag + 2 * (step & 1), 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
             return GB_GO_ECUDA;
-        int r = fp32_launch(D.dev, D.items, D.nitems, h->d.L, smem, D.step_ctr, n, s);
+        int r = D.nitems ? fp32_launch(D.dev, D.items, D.nitems, D.items + D.nitems, D.nco, D.max_slots, D.step_ctr, n,
+                                       D.work, h->p.diso != 0, s)
+                         : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;
-        count_launches(2);
+        count_launches(3);
     }
     D.steps += nsteps;
     *cur = (int)(D.steps & 1);
