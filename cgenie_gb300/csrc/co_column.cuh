@@ -136,4 +136,98 @@ __device__ int co_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const
     return filled;
 }
 
+// Working arrays of co_warp (one per warp, shared memory).
+struct CoWarpState {
+    int kk[kMaxK + 2];
+    double dzm[kMaxK + 1];
+    double rho[kMaxK + 1];
+};
+
+// co_rn with one warp per column: the tracers of the column are in shared memory,
+// tv[lev * 32 + l] for the wet levels, and lane l mixes and fills tracer l.  The levels
+// to merge (kk, dzm, rho in cs) are kept by lane 0 (densities of the first pass one lane
+// per level); every value is the one co_rn computes.  Returns the number of filled levels
+// (in every lane).
+__device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, int maxk, int L, int k1,
+                              const double *dz, const double *zro, const double *zw, int lane)
+{
+    int *kk = cs->kk;
+    double *dzm = cs->dzm, *rho = cs->rho;
+    auto T = [&](int l, int lev) { return tv[lev * 32 + l]; };
+    for (int lev = k1 + lane; lev <= maxk; lev += 32) {
+        rho[lev] = eos_rn(ec, T(0, lev), T(1, lev), zro[lev]);
+        kk[lev] = lev;
+        dzm[lev] = dz[lev];
+    }
+    if (lane == 0) {
+        rho[0] = 0.0;
+        kk[k1 - 1] = 0;
+    }
+    __syncwarp();
+    auto refresh = [&](int x, int y) {
+        if (ec.ieos != 0) {
+            if (lane == 0) {
+                rho[kk[x]] = eos_rn(ec, T(0, kk[x]), T(1, kk[x]), zw[kk[y]]);
+                rho[kk[y]] = eos_rn(ec, T(0, kk[y]), T(1, kk[y]), zw[kk[y]]);
+            }
+            __syncwarp();
+        }
+    };
+    // m, n, lastmix follow from the shared arrays, so they are the same in every lane
+    int m = maxk, lastmix = 0;
+    while (kk[m - 1] > 0 || (lastmix != 0 && kk[m] != maxk)) {
+        refresh(m, m - 1);
+        if (rho[kk[m]] < rho[kk[m - 1]] || kk[m - 1] == 0) {
+            if (lastmix == 0 || kk[m] == maxk) m = m - 1;
+            else m = m + 1;
+            lastmix = 0;
+        } else {
+            lastmix = 1;
+            int n = m - 1;
+            refresh(n, n - 1);
+            while (kk[n - 1] > 0 && rho[kk[n]] >= rho[kk[n - 1]]) {
+                n = n - 1;
+                refresh(n, n - 1);
+            }
+            const int km = kk[m];
+            const double d0 = dzm[km];
+            double dtot = d0;
+            if (lane == 0)
+                for (int ni = 1; ni <= m - n; ++ni) dtot = __dadd_rn(dtot, dzm[kk[m - ni]]);
+            dtot = __shfl_sync(0xffffffffu, dtot, 0);
+            if (lane < L) {
+                double s = __dmul_rn(T(lane, km), d0);
+                for (int ni = 1; ni <= m - n; ++ni) s = __dadd_rn(s, __dmul_rn(T(lane, kk[m - ni]), dzm[kk[m - ni]]));
+                tv[km * 32 + lane] = __ddiv_rn(s, dtot);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                dzm[km] = dtot;
+                rho[km] = eos_rn(ec, T(0, km), T(1, km), zw[kk[m - 1]]);
+                int ni = m - 1;
+                while (kk[ni + 1] > 0) {
+                    kk[ni] = kk[ni - m + n];
+                    ni = ni - 1;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    int filled = 0;
+    m = maxk - 1;
+    for (int n = maxk - 1; n >= k1; --n) {
+        if (n > kk[m]) {
+            const int src = kk[m + 1];
+            if (lane < L) tv[n * 32 + lane] = T(lane, src);
+            __syncwarp();
+            if (lane == 0) rho[n] = eos_rn(ec, T(0, n), T(1, n), zw[kk[n - 1]]);
+            __syncwarp();
+            filled = filled + 1;
+        } else {
+            m = m - 1;
+        }
+    }
+    return filled;
+}
+
 }  // namespace gbgo

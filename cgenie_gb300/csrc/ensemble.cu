@@ -42,14 +42,14 @@ struct Member {
     size_t bytes = 0;
     // device
     double *buf0 = nullptr, *buf1 = nullptr, *ts_static = nullptr, *rho = nullptr, *stage = nullptr;
-    float *coef = nullptr, *gtop = nullptr;
+    float *coef = nullptr, *coefl = nullptr, *gtop = nullptr;
     double *rvol = nullptr, *mk = nullptr, *mj = nullptr, *cost = nullptr, *dsj = nullptr;
     int32_t *k1 = nullptr, *scale = nullptr, *icosd = nullptr;
     unsigned int *gmax = nullptr;         // per tracer, scale re-targeting
     unsigned long long *diag = nullptr;   // two slots {dmax bits, limps}
     unsigned int *status = nullptr;
     int32_t *ptab = nullptr;              // patch tables
-    uint8_t *coflag = nullptr;            // per column: flagged for the exact convective adjustment
+    int wet_cols = 0;                     // wet columns (entries it may add to the co list)
     std::vector<int32_t> poff;            // per patch: word offset in ptab
     std::vector<double> pcost;            // per patch: cell-updates per step
     int max_slots = 1;
@@ -75,9 +75,13 @@ struct gb_ens {
     MemberDesc *descs = nullptr;        // device, capacity cap_desc
     int cap_desc = 0;
     int4 *items = nullptr;              // device, capacity cap_items
-    int cap_items = 0, nitems = 0, nco = 0;
+    int cap_items = 0, nitems = 0;
     int max_slots = 1;
     bool any_iso = false;               // some member has the isoneutral branch
+    int kmax = 1;                       // largest maxk of the members
+    int2 *colist = nullptr;             // columns listed for the exact convective adjustment
+    int *cocount = nullptr;             // two counters, by step parity
+    int cocap = 0;
     int *work = nullptr;                // device work counters (two, by step parity)
     bool dirty = true;
     gb_ens_tuning tuning{0, 0, 0, 0};
@@ -106,9 +110,10 @@ static size_t member_bytes(const gb_go_dims *d)
     const size_t nrho = (size_t)(d->maxi + 2) * (d->maxj + 2) * (d->maxk + 1);
     const size_t ncell = (size_t)d->maxi * d->maxj * d->maxk;
     const size_t ncol = (size_t)d->maxi * d->maxj;
-    // two state buffers, uploaded copy, download stage, rho, coefficients, forcing, small arrays
-    // patch tables: at most (31 + maxk) words per column
-    return 4 * nts * 8 + nrho * 8 + 12 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
+    // two group-planar state buffers, uploaded copy, download stage, rho, coefficients (FP32
+    // and remainders), forcing, small arrays; patch tables: at most (31 + maxk) words per column
+    const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
+    return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
            ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + 4096;
 }
 
@@ -139,6 +144,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
     if (x == cudaSuccess) x = cudaMemset(e->step_ctr, 0, sizeof(long long));
     if (x == cudaSuccess) x = cudaMalloc(&e->work, 2 * sizeof(int));
     if (x == cudaSuccess) x = cudaMemset(e->work, 0, 2 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 2 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 2 * sizeof(int));
     if (x != cudaSuccess) {
         gb_ens_destroy(e);
         return x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
@@ -150,9 +157,9 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
 static void free_member(gb_ens *e, Member *m)
 {
     cudaStream_t s = e->stream;
-    void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->gtop, m->mj,
+    void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->coefl, m->gtop, m->mj,
                     m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax,
-                    m->ptab, m->coflag};
+                    m->ptab};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
 }
@@ -167,6 +174,8 @@ extern "C" void gb_ens_destroy(gb_ens *e)
     if (e->graph) cudaGraphExecDestroy(e->graph);
     cudaFree(e->step_ctr);
     cudaFree(e->work);
+    cudaFree(e->cocount);
+    cudaFree(e->colist);
     cudaFree(e->descs);
     cudaFree(e->items);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
@@ -243,12 +252,14 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     const size_t nrho = (size_t)m->d.NI * m->d.NJ * (dims->maxk + 1);
     const size_t ncol = (size_t)dims->maxi * dims->maxj;
     cudaStream_t s = e->stream;
-    cudaError_t x = dalloc(e, &m->buf0, nts);
-    if (x == cudaSuccess) x = dalloc(e, &m->buf1, nts);
+    const size_t nplan = fp32_planar_size(m->d);
+    cudaError_t x = dalloc(e, &m->buf0, nplan);
+    if (x == cudaSuccess) x = dalloc(e, &m->buf1, nplan);
     if (x == cudaSuccess) x = dalloc(e, &m->ts_static, nts);
     if (x == cudaSuccess) x = dalloc(e, &m->stage, nts);
     if (x == cudaSuccess) x = dalloc(e, &m->rho, nrho);
     if (x == cudaSuccess) x = dalloc(e, &m->coef, st.coef.size());
+    if (x == cudaSuccess) x = dalloc(e, &m->coefl, st.coefl.size());
     if (x == cudaSuccess) x = dalloc(e, &m->gtop, gtop.size());
     if (x == cudaSuccess) x = dalloc(e, &m->mj, st.mj.size());
     if (x == cudaSuccess) x = dalloc(e, &m->rvol, st.rvol.size());
@@ -263,19 +274,20 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = dalloc(e, &m->diag, 4);
     if (x == cudaSuccess) x = dalloc(e, &m->status, 1);
     if (x == cudaSuccess) x = dalloc(e, &m->ptab, std::max<size_t>(4, plan.words.size()));
-    if (x == cudaSuccess) x = dalloc(e, &m->coflag, ncol);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->coflag, 0, ncol, s);
     if (x == cudaSuccess && !plan.words.empty())
         x = cudaMemcpyAsync(m->ptab, plan.words.data(), plan.words.size() * 4, cudaMemcpyHostToDevice, s);
     m->ds_host.assign(blob.begin() + 6 * (dims->maxj + 2), blob.begin() + 7 * (dims->maxj + 2));
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->dsj, m->ds_host.data(), m->ds_host.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemsetAsync(m->diag, 0, 4 * sizeof(unsigned long long), s);
     if (x == cudaSuccess) x = cudaMemsetAsync(m->status, 0, sizeof(unsigned int), s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->buf0, ts, nts * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, m->buf0, nts * 8, cudaMemcpyDeviceToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->buf1, m->buf0, nts * 8, cudaMemcpyDeviceToDevice, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, ts, nts * 8, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess && (fp32_to_planar(m->buf0, m->ts_static, m->d, s) || fp32_to_planar(m->buf1, m->ts_static, m->d, s))) {
+        const cudaError_t le = cudaGetLastError();
+        x = le != cudaSuccess ? le : cudaErrorLaunchFailure;
+    }
     if (x == cudaSuccess) x = cudaMemsetAsync(m->rho, 0, nrho * 8, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->coef, st.coef.data(), st.coef.size() * 4, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->coefl, st.coefl.data(), st.coefl.size() * 4, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->gtop, gtop.data(), gtop.size() * 4, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->mj, st.mj.data(), st.mj.size() * 8, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->rvol, st.rvol.data(), st.rvol.size() * 8, cudaMemcpyHostToDevice, s);
@@ -298,9 +310,9 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     for (int n = 0; n < 5; ++n) md.ec[n] = m->p.ec[n];
     md.dsc = m->p.dsc;
     md.buf[0] = m->buf0; md.buf[1] = m->buf1;
-    md.ts_static = m->ts_static; md.coef = m->coef; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
+    md.ts_static = m->ts_static; md.coef = m->coef; md.coefl = m->coefl; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
     md.scale = m->scale; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
-    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab; md.coflag = m->coflag;
+    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission
@@ -310,7 +322,10 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     for (int j = 1; j <= dims->maxj; ++j)
         for (int i = 1; i <= dims->maxi; ++i) {
             const int k1 = grid->k1[i + (size_t)m->d.NI * j];
-            if (k1 <= dims->maxk) wet += dims->maxk - k1 + 1;
+            if (k1 <= dims->maxk) {
+                wet += dims->maxk - k1 + 1;
+                m->wet_cols += 1;
+            }
         }
     m->cost_est = (double)wet * (dims->maxl + 4) * (params->diso ? 2.0 : 1.0);
     m->id = e->next_id++;
@@ -351,6 +366,7 @@ static int rebuild(gb_ens *e)
     std::vector<std::pair<double, Member *>> order;
     int max_slots = 1;
     bool any_iso = false;
+    int kmax = 1;
     int slot = 0;
     for (auto &kv : e->members) {
         Member *m = kv.second.get();
@@ -366,21 +382,20 @@ static int rebuild(gb_ens *e)
         order.push_back({c, m});
         max_slots = std::max(max_slots, m->max_slots);
         any_iso = any_iso || m->desc.diso;
+        kmax = std::max(kmax, m->d.maxk);
         ++slot;
     }
     std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
-    // transfer items (member, patch, group): the T-S group of every patch first (the longest
-    // items), then the other groups, each member's patches together; then co items (member, patch)
+    // transfer items (member, patch, group) with a patch's groups and a member's patches next to
+    // each other: items taken together share the coefficients and ring columns in L2.  The co
+    // column list holds at most every wet column of the batch.
     std::vector<int4> it;
-    int maxg = 1;
-    for (auto &o : order) maxg = std::max(maxg, fp32_group_count(o.second->d.L));
-    for (int g = 0; g < maxg; ++g)
-        for (auto &o : order)
-            if (g < fp32_group_count(o.second->d.L))
-                for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], g, 0));
-    const int nstep_items = (int)it.size();
     for (auto &o : order)
-        for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], 0, 0));
+        for (size_t n = 0; n < o.second->poff.size(); ++n)
+            for (int g = 0; g < fp32_group_count(o.second->d.L); ++g)
+                it.push_back(make_int4(o.second->slot, o.second->poff[n], g, 0));
+    int cocap = 0;
+    for (auto &o : order) cocap += o.second->wet_cols;
     if ((int)it.size() > e->cap_items) {
         int cap = std::max(256, (int)(2 * it.size()));
         if (e->items) cudaFreeAsync(e->items, s);
@@ -390,10 +405,16 @@ static int rebuild(gb_ens *e)
     if (!descs.empty()) ETRY(e, cudaMemcpyAsync(e->descs, descs.data(), descs.size() * sizeof(MemberDesc), cudaMemcpyHostToDevice, s));
     if (!it.empty()) ETRY(e, cudaMemcpyAsync(e->items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
     ETRY(e, cudaStreamSynchronize(s));
-    e->nitems = nstep_items;
-    e->nco = (int)it.size() - nstep_items;
+    e->nitems = (int)it.size();
+    if (cocap > e->cocap) {
+        if (e->colist) cudaFreeAsync(e->colist, s);
+        e->colist = nullptr;
+        ETRY(e, cudaMallocAsync(&e->colist, (size_t)cocap * sizeof(int2), s));
+        e->cocap = cocap;
+    }
     e->max_slots = max_slots;
     e->any_iso = any_iso;
+    e->kmax = kmax;
     e->dirty = false;
     if (e->graph) {
         cudaGraphExecDestroy(e->graph);
@@ -406,8 +427,8 @@ static int launch_steps(gb_ens *e, int nsteps)
 {
     cudaStream_t s = e->stream;
     for (int n = 0; n < nsteps; ++n) {
-        int r = fp32_launch(e->descs, e->items, e->nitems, e->items + e->nitems, e->nco, e->max_slots, e->step_ctr, n,
-                            e->work, e->any_iso, s);
+        int r = fp32_launch(e->descs, e->items, e->nitems, e->max_slots, e->kmax, e->step_ctr, n, e->work, e->colist,
+                            e->cocount, e->cocap, e->any_iso, s);
         if (!r) r = fp32_rescale(e->descs, (int)e->members.size(), s);
         if (r) return efail(e, r, "fp32 batched launch failed");
     }
@@ -491,6 +512,10 @@ static double *current_buffer(gb_ens *e, Member *m)
     return ((done_at + m->desc.parity) & 1) ? m->buf1 : m->buf0;
 }
 
+// The other ping-pong buffer: the next step overwrites every cell of it that anything reads,
+// so downloads use it as scratch for the Fortran-layout copy of the current state.
+static double *scratch_buffer(gb_ens *e, Member *m) { return current_buffer(e, m) == m->buf0 ? m->buf1 : m->buf0; }
+
 __global__ void k_merge_member(double *out, const double *stat, const double *cur, Dims d, const int32_t *k1)
 {
     const size_t ncell = (size_t)d.NI * d.NJ * (d.maxk + 2);
@@ -513,9 +538,9 @@ extern "C" int gb_ens_download(gb_ens *e, int32_t id, double *ts, double *rho, d
     Member *m = it->second.get();
     ETRY(e, cudaSetDevice(e->device));
     cudaStream_t s = e->stream;
-    double *cur = current_buffer(e, m);
+    double *cur = scratch_buffer(e, m);
     MemberDesc md = m->desc;
-    int r = fp32_export(md, cur, m->rho, s);
+    int r = fp32_export(md, current_buffer(e, m), cur, m->rho, s);
     if (r) return efail(e, r, "export failed");
     const size_t nts = (size_t)m->d.L * m->d.NI * m->d.NJ * (m->d.maxk + 2);
     if (ts) {
@@ -574,7 +599,9 @@ extern "C" int gb_ens_inventory(gb_ens *e, int32_t id, double *out)
     cudaStream_t s = e->stream;
     double *dout = nullptr;
     ETRY(e, cudaMallocAsync(&dout, m->d.L * sizeof(double), s));
-    k_member_inventory<<<m->d.L, 256, 0, s>>>(current_buffer(e, m), m->d, m->k1, m->mk, nullptr, m->dsj, dout);
+    double *fort = scratch_buffer(e, m);
+    if (fp32_from_planar(fort, current_buffer(e, m), m->d, s)) return efail(e, GB_GO_ECUDA, "export failed");
+    k_member_inventory<<<m->d.L, 256, 0, s>>>(fort, m->d, m->k1, m->mk, nullptr, m->dsj, dout);
     count_launches(1);
     ETRY(e, cudaMemcpyAsync(out, dout, m->d.L * sizeof(double), cudaMemcpyDeviceToHost, s));
     cudaFreeAsync(dout, s);

@@ -14,6 +14,57 @@ namespace gbgo {
 constexpr int kFp32MaxL = 32;   // tracers per member supported by the FP32-flux kernel
 constexpr int kFp32Threads = 128;   // CTA of the FP32-flux kernel: one thread per patch column
 
+// Tracer groups: group 0 is T and S (double-float transfers, convection flag); the other
+// tracers form groups of at most kGroup.  A work item of the step kernel is one group of
+// one patch.
+constexpr int kGroup = 8;
+
+__host__ __device__ inline int fp32_ngroups(int L)
+{
+    return L <= 2 ? 1 : 1 + (L - 2 + kGroup - 1) / kGroup;
+}
+
+// First tracer g0 and size gl of group g.
+__host__ __device__ inline void fp32_group(int L, int g, int *g0, int *gl)
+{
+    if (g == 0) {
+        *g0 = 0;
+        *gl = 2;
+        return;
+    }
+    const int nb = L - 2, ngb = (nb + kGroup - 1) / kGroup;
+    const int base = nb / ngb, rem = nb % ngb, h = g - 1;
+    *gl = base + (h < rem ? 1 : 0);
+    *g0 = 2 + h * base + (h < rem ? h : rem);
+}
+
+// Device-resident state of the FP32-flux path ("group-planar"): group g is a plane of
+// NI*NJ*(maxk+2) cells with gp = gl rounded up to even doubles per cell, so that a
+// group's values of one cell are contiguous and 16-byte aligned pairs:
+//   (l, i, j, k), l = g0 + q  ->  plane(g) * NIJK + (i + NI*(j + NJ*k)) * gp + q
+// plane(g) = sum of gp over the groups before g.  Fortran-layout arrays are converted
+// on upload and export only.
+__host__ __device__ inline void fp32_plane(int L, int g, int *g0, int *gl, int *gp, int *plane)
+{
+    fp32_group(L, g, g0, gl);
+    *gp = *gl + (*gl & 1);
+    int pl = 0;
+    for (int h = 0; h < g; ++h) {
+        int a, b;
+        fp32_group(L, h, &a, &b);
+        pl += b + (b & 1);
+    }
+    *plane = pl;
+}
+
+__host__ __device__ inline int fp32_planar_width(int L)
+{
+    int g0, gl, gp, pl;
+    const int ng = fp32_ngroups(L);
+    fp32_plane(L, ng - 1, &g0, &gl, &gp, &pl);
+    return pl + gp;
+}
+
 // Per-member descriptor read by the batched kernel (device memory).
 struct MemberDesc {
     int maxi, maxj, maxk, L;
@@ -25,10 +76,11 @@ struct MemberDesc {
     double dt, dphi, rdphi, diff1;
     double ec[5];
     double dsc;
-    double *buf[2];             // state ping-pong, Fortran layout with halos
+    double *buf[2];             // state ping-pong, group-planar layout (fp32_plane)
     const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
-    const float *coef;          // 12 floats per interior cell: Ae Be An Bn Aa Ba as FP32, then their
-                                // FP64 remainders (the pair hi+lo carries the FP64 coefficient)
+    const float *coef;          // 8 floats per interior cell: Ae Be An Bn Aa Ba as FP32, 0, 0
+    const float *coefl;         // 8 floats per interior cell: the FP64 remainders of the same (hi+lo
+                                // carries the FP64 coefficient; read by the T-S group only)
     const double *rvol;         // 1/(dphi*ds(j)*dz(k)), index (j-1) + maxj*(k-1)
     const float *gtop;          // forcing transfer dt*dphi*ds(j)*ts(l,i,j,maxk+1): L+2 floats per column
                                 // ((i-1)+maxi*(j-1)): FP32 value of every tracer, then the lo parts of T, S
@@ -43,15 +95,15 @@ struct MemberDesc {
     int32_t *icosd;
     unsigned long long *diag;   // two slots {dmax bits, limps}; step n uses slot n & 1 and clears
                                 // slot (n+1) & 1 for the next step
-    unsigned int *status;       // bit0 non-finite, bit1 transfer range exceeded
-    uint8_t *coflag;            // per column ((i-1) + maxi*(j-1)): density profile may be unstable
+    unsigned int *status;       // bit0 non-finite, bit1 transfer range exceeded, bit2 column list full
 };
 
 // Host-side owner of one member's FP32-path device data.
 struct Fp32Data {
     MemberDesc host{};          // descriptor contents (device pointers)
     MemberDesc *dev = nullptr;  // device copy when used alone
-    float *coef = nullptr;
+    float *coef = nullptr, *coefl = nullptr;
+    double *plan_buf[2] = {nullptr, nullptr};   // group-planar state ping-pong
     double *rvol = nullptr;
     float *gtop = nullptr;
     int32_t *scale = nullptr;
@@ -59,9 +111,11 @@ struct Fp32Data {
     double *mk = nullptr, *mj = nullptr;
     unsigned int *status = nullptr;
     unsigned long long *diag = nullptr;
-    int4 *items = nullptr;      // work items when stepped alone: (0, patch, group), then (0, patch) for co
-    int nitems = 0, nco = 0;
-    uint8_t *coflag = nullptr;
+    int4 *items = nullptr;      // work items when stepped alone: (0, patch, group)
+    int nitems = 0;
+    int2 *colist = nullptr;     // columns for the exact convective adjustment (capacity cocap)
+    int *cocount = nullptr;     // their count, two by step parity
+    int cocap = 0;
     int32_t *ptab = nullptr;    // patch tables
     int *work = nullptr;        // work counters (two, by step parity)
     int max_slots = 1;
@@ -82,17 +136,22 @@ struct Fp32Member {
 int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Metrics &m,
                      const std::vector<double> &blob, const int32_t *k1_host, cudaStream_t s, std::string &msg);
 void fp32_member_free(Fp32Member *f);
-// host pointers: the transfer scales and coefficients are built on the host
-int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, cudaStream_t s);
+// host pointers: the transfer scales and coefficients are built on the host; ts1_dev is the
+// uploaded ts1 on the device (Fortran layout), converted to the group-planar state
+int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, const double *ts1_dev, cudaStream_t s);
 int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s);
 int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s);
 int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, const double *ts_static, double *cost,
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s);
-int fp32_member_export(Fp32Member *f, const double *ts_cur, double *rho, const double *ts_static, cudaStream_t s);
+// current state -> ts_cur (Fortran layout, halo columns) and rho
+int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s);
+// current state -> dst (Fortran layout)
+int fp32_member_fortran(Fp32Member *f, double *dst, cudaStream_t s);
 
 // shared by the single-grid path and the ensemble
 struct Fp32Static {
-    std::vector<float> coef;       // 12 per interior cell
+    std::vector<float> coef;       // 8 per interior cell (FP32 parts)
+    std::vector<float> coefl;      // 8 per interior cell (remainders)
     std::vector<double> rvol;
     std::vector<double> mk, mj;
     double cmax = 0.0;
@@ -105,7 +164,7 @@ void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &bl
                std::vector<float> &gtop);
 // Patch plan of one member: the kernel's work items.  Word layout of one patch table:
 //   [ns, ni, kstart, patch index, 0, 0, 0, 0], nki[0..maxk+1] (interior slots with k1 <= k),
-//   nkr[0..maxk+1] (ring slots with k1 <= k), goff[ns] (L*(i + NI*j) of each slot; interior
+//   nkr[0..maxk+1] (ring slots with k1 <= k), goff[ns] (i + NI*j of each slot; interior
 //   slots 0..ni-1, then the ring), padding to 4 words,
 //   then 8 words per interior column (in slot order): slot | E << 16, W | N << 16,
 //   S | k1 << 16, (i-1) + maxi*(j-1), i | j << 16, neighbour k1 (E, W, N, S bytes),
@@ -120,13 +179,21 @@ struct PatchPlan {
 // tile_i/tile_j > 0 ask for that rectangle (if within the kernel limits), else the cheapest one
 int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, PatchPlan &plan);
 int fp32_group_count(int L);   // tracer groups (work items per patch): T and S, then groups of <= 8
-// One step of a batch: the transfer kernel over (member, patch, group) items, then the exact
-// convective adjustment over (member, patch) items.  iso: some member has the isoneutral
-// branch (selects the kernel instance that has it).
-int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, const int4 *co_items, int nco,
-                int max_slots, const long long *step_ctr, int rel, int *work, bool iso, cudaStream_t s);
+// Fortran layout (L, NI, NJ, maxk+2) <-> group-planar layout of the FP32-flux state
+int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s);
+int fp32_from_planar(double *fortran, const double *planar, const Dims &d, cudaStream_t s);
+inline size_t fp32_planar_size(const Dims &d) { return (size_t)fp32_planar_width(d.L) * d.NI * d.NJ * (d.maxk + 2); }
+// One step of a batch: the transfer kernel over (member, patch, group) items, which lists the
+// columns that need the exact convective adjustment (colist, count in cocount[step & 1],
+// capacity cocap: the wet columns of the batch), then the adjustment of those columns.
+// kmax: the largest maxk of the batch; iso: some member has the isoneutral branch (selects
+// the kernel instance that has it).
+int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int max_slots, int kmax,
+                const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap, bool iso,
+                cudaStream_t s);
 int fp32_smem_bytes(int max_slots);
-int fp32_export(const MemberDesc &md, const double *cur, double *rho, cudaStream_t s);
+// current state (group-planar) -> Fortran layout with halo columns, and rho
+int fp32_export(const MemberDesc &md, const double *planar, double *cur, double *rho, cudaStream_t s);
 // re-target the fixed-point scales of `n` members after a step (stream order)
 int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s);
 

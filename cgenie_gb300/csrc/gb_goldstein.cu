@@ -406,7 +406,7 @@ extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const doubl
     h->state_ready = true;
     h->steps_since_upload = 0;
     if (h->precision == GB_GO_FP32FLUX) {
-        int r = fp32_member_upload(&h->f32, ts1, ts, h->stream);
+        int r = fp32_member_upload(&h->f32, ts1, ts, h->ts_buf[0], h->stream);
         if (r) return fail(h, r, "fp32 upload failed");
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -545,6 +545,10 @@ extern "C" int gb_go_inventory(gb_go_handle *h, double *out)
     CUDA_TRY(h, cudaSetDevice(h->device));
     const double *src = h->ts_buf[h->cur];
     if (h->steps_since_upload == 0) src = h->ts_static;
+    else if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_fortran(&h->f32, h->ts_buf[h->cur], h->stream);
+        if (r) return fail(h, r, "fp32 export failed");
+    }
     dim3 grid(h->inv_blocks, h->d.L);
     k_inventory_partial<<<grid, 256, 0, h->stream>>>(src, h->d, h->m, h->inv_part);
     k_inventory_final<<<(h->d.L + 63) / 64, 64, 0, h->stream>>>(h->inv_part, h->inv_blocks, h->d.L, h->stage);

@@ -123,23 +123,49 @@ __device__ __forceinline__ dflt df_split(double x)
     return {h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
 }
 
-__device__ __forceinline__ float eos_f(const float ec[5], float t, float s)
+// density of the equation of state with the ieos = 0 terms, the arithmetic of eos_rn
+template <class MD>
+__device__ __forceinline__ double eos_md(const MD &md, double t, double s)
 {
-    return ec[0] * t + ec[1] * s + ec[2] * (t * t) + ec[3] * (t * t * t);
+    const double tt = __dmul_rn(t, t);
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(md.ec[0], t), __dmul_rn(md.ec[1], s)), __dmul_rn(md.ec[2], tt)),
+                     __dmul_rn(md.ec[3], __dmul_rn(tt, t)));
 }
 
-// column view used by the exact co on the FP64 state
+// column view used by the exact co: the group-planar FP64 state at and above k1,
+// the uploaded (Fortran-layout) state below
 struct Fp32Col {
     double *w;
     const double *stat;
-    int L, NI, NJ, i, j, k1;
+    int L, NI, NJ, nk, i, j, k1;
+    int pofs[kFp32MaxL];   // per tracer: plane * NIJK + q (l = g0 + q)
+    int gpl[kFp32MaxL];    // per tracer: gp of its group
     double rho[kMaxK + 1];
-    __device__ size_t idx(int l, int lev) const
+    __device__ void init_planes()
+    {
+        NIJK = (size_t)NI * NJ * (size_t)(nk);
+        const int ng = fp32_ngroups(L);
+        for (int g = 0; g < ng; ++g) {
+            int g0, gl, gp, pl;
+            fp32_plane(L, g, &g0, &gl, &gp, &pl);
+            for (int q = 0; q < gl; ++q) {
+                pofs[g0 + q] = pl;
+                gpl[g0 + q] = gp * 64 + q;
+            }
+        }
+    }
+    __device__ size_t widx(int l, int lev, size_t NIJK) const
+    {
+        const size_t cell = (size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)lev);
+        return (size_t)pofs[l] * NIJK + cell * (size_t)(gpl[l] >> 6) + (size_t)(gpl[l] & 63);
+    }
+    size_t NIJK;
+    __device__ size_t sidx(int l, int lev) const
     {
         return (size_t)l + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)lev));
     }
-    __device__ double T(int l, int lev) const { return lev >= k1 ? w[idx(l, lev)] : stat[idx(l, lev)]; }
-    __device__ void setT(int l, int lev, double v) { w[idx(l, lev)] = v; }
+    __device__ double T(int l, int lev) const { return lev >= k1 ? w[widx(l, lev, NIJK)] : stat[sidx(l, lev)]; }
+    __device__ void setT(int l, int lev, double v) { w[widx(l, lev, NIJK)] = v; }
     __device__ double &R(int lev) { return rho[lev]; }
 };
 
@@ -159,27 +185,6 @@ struct Fp32Col {
 // barrier per level enough.  The group of T and S also flags the columns whose FP32
 // density profile may be unstable; k_co_fp32 then adjusts those columns exactly.
 
-// Tracers per march of a patch.  Group 0 is T and S (double-float transfers, and the
-// convection prescreen); the other tracers form groups of at most kGroup.
-constexpr int kGroup = 8;
-
-__host__ __device__ inline int fp32_ngroups(int L)
-{
-    return L <= 2 ? 1 : 1 + (L - 2 + kGroup - 1) / kGroup;
-}
-
-__host__ __device__ inline void fp32_group(int L, int g, int *g0, int *gl)
-{
-    if (g == 0) {
-        *g0 = 0;
-        *gl = 2;
-        return;
-    }
-    const int nb = L - 2, ngb = (nb + kGroup - 1) / kGroup;
-    const int base = nb / ngb, rem = nb % ngb, h = g - 1;
-    *gl = base + (h < rem ? 1 : 0);
-    *g0 = 2 + h * base + (h < rem ? h : rem);
-}
 // FP32 slab pitch per slot (kGroup tracers + 1: consecutive slots hit distinct banks)
 constexpr int kGP = 9;
 constexpr int kPatchHdr = 8;
@@ -210,7 +215,8 @@ __device__ __forceinline__ double ldg_d(const double *p) { return __ldg(p); }
 template <bool ISO>
 __global__ void __launch_bounds__(kFp32Threads, 4)
 k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
-            const long long *__restrict__ step_ctr, int rel, int *__restrict__ work, int P)
+            const long long *__restrict__ step_ctr, int rel, int *__restrict__ work, int P,
+            int2 *__restrict__ colist, int *__restrict__ cocount, int cocap)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_nki[kMaxK + 2], s_nkr[kMaxK + 2];
@@ -258,7 +264,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         const int par = (int)((step + md.parity) & 1);
         const double *__restrict__ R = md.buf[par];
         double *__restrict__ W = md.buf[par ^ 1];
-        const long long LNIJ = (long long)L * NI * NJ;
         const size_t nij = (size_t)maxi * maxj;
         const double *mk = md.mk;
         const double *mj = md.mj;
@@ -306,9 +311,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     }
         }
 
-        float ecf[5];
-        for (int n = 0; n < 5; ++n) ecf[n] = (float)md.ec[n];
-        float rho_prev = 0.0f;
+        double rho_prev = 0.0;
         bool unstable = false;
         float gmax = 0.0f;
         unsigned hmax = 0u;
@@ -316,9 +319,12 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         unsigned limps_l = 0;
 
         {
-            int g0, gl;
-            fp32_group(L, item.z, &g0, &gl);
+            int g0, gl, gp, plane;
+            fp32_plane(L, item.z, &g0, &gl, &gp, &plane);
             const bool ts_group = (item.z == 0);
+            const long long NIJK = (long long)NI * NJ * (maxk + 2), NIJ = (long long)NI * NJ;
+            const double *__restrict__ Rg = R + NIJK * plane;
+            double *__restrict__ Wg = W + NIJK * plane;
             int scl[kGroup];
 #pragma unroll
             for (int q = 0; q < kGroup; ++q) scl[q] = q < gl ? s_scale[g0 + q] : 0;
@@ -327,10 +333,14 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             // this slot's FP64 values of level lev (if wet there) into xr
             auto load_level = [&](int lev) {
                 if (lev >= kown) {
-                    const double *p = R + LNIJ * lev + goffs + g0;
+                    const double2 *p = reinterpret_cast<const double2 *>(Rg + ((long long)goffs + NIJ * lev) * gp);
 #pragma unroll
-                    for (int q = 0; q < kGroup; ++q)
-                        if (q < gl) xr[q] = ldg_d(p + q);
+                    for (int m = 0; m < kGroup / 2; ++m)
+                        if (2 * m < gl) {
+                            const double2 v = __ldg(p + m);
+                            xr[2 * m] = v.x;
+                            xr[2 * m + 1] = v.y;
+                        }
                 }
             };
             // xr (level lev) -> this slot's scaled FP32 slab entries of lev (and lo of T and S)
@@ -368,16 +378,18 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                 __syncthreads();
                 // ---- interior column wet at k: transfers of level k and the FP64 update
                 if (interior && k >= k1c) {
-                    const double *Rk = R + LNIJ * k + goffs + g0;
-                    double *Wk = W + LNIJ * k + goffs + g0;
+                    const double2 *Rk = reinterpret_cast<const double2 *>(Rg + ((long long)goffs + NIJ * k) * gp);
+                    double2 *Wk = reinterpret_cast<double2 *>(Wg + ((long long)goffs + NIJ * k) * gp);
                     const size_t cl = (size_t)cl0 + nij * (size_t)(k - 1);
-                    const float *cf = md.coef + 12 * cl;
+                    const float *cf = md.coef + 8 * cl;
+                    const float *cfl = md.coefl + 8 * cl;
                     const float4 a4 = __ldg(reinterpret_cast<const float4 *>(cf));        // Ae Be An Bn
                     const float2 a2 = __ldg(reinterpret_cast<const float2 *>(cf + 4));    // Aa Ba
-                    const float *cw = md.coef + 12 * ((size_t)cw0 + nij * (size_t)(k - 1));
+                    const size_t cwi = 8 * ((size_t)cw0 + nij * (size_t)(k - 1));
+                    const float *cw = md.coef + cwi;
                     const float2 w2 = __ldg(reinterpret_cast<const float2 *>(cw));        // Ae Be of the west cell
                     float2 s2 = make_float2(0.f, 0.f);
-                    if (j > 1) s2 = __ldg(reinterpret_cast<const float2 *>(cf - 12 * (size_t)maxi + 2));  // An Bn south
+                    if (j > 1) s2 = __ldg(reinterpret_cast<const float2 *>(cf - 8 * (size_t)maxi + 2));  // An Bn south
                     const double rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
                     const bool top = (k == maxk);
                     const float *gt = md.gtop + (size_t)(L + 2) * (size_t)cl0;
@@ -397,11 +409,11 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     if (ts_group || (ISO && md.diso && !top)) {
                         // lo parts of the coefficients (T and S use the FP32 pair; the isoneutral
                         // stencil is built from the FP64 coefficient)
-                        const float2 l2 = __ldg(reinterpret_cast<const float2 *>(cf + 6));   // lo Aa Ba
-                        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(cf + 8));   // lo Ae Be An Bn
-                        const float2 lw = __ldg(reinterpret_cast<const float2 *>(cw + 8));
+                        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(cfl));      // lo Ae Be An Bn
+                        const float2 l2 = __ldg(reinterpret_cast<const float2 *>(cfl + 4));  // lo Aa Ba
+                        const float2 lw = __ldg(reinterpret_cast<const float2 *>(md.coefl + cwi));
                         float2 ls = make_float2(0.f, 0.f);
-                        if (j > 1) ls = __ldg(reinterpret_cast<const float2 *>(cf - 12 * (size_t)maxi + 10));
+                        if (j > 1) ls = __ldg(reinterpret_cast<const float2 *>(cfl - 8 * (size_t)maxi + 2));
                         C1X.lo = l2.x; C0X.lo = l2.y;
                         AeX.lo = l4.x; BeX.lo = l4.y; AnX.lo = l4.z; BnX.lo = l4.w;
                         AwX.lo = lw.x; BwX.lo = lw.y; AsX.lo = ls.x; BsX.lo = ls.y;
@@ -411,8 +423,9 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         // state: the density differences scc*dS - tec*dT cancel strongly in weakly
                         // stratified water; they are differences of D = ec(2)*S - tec*T with the
                         // cell's tec (goldstein.f90:2587-2588)
+                        // T and S are plane 0 of the group-planar state, two values per cell
                         auto ld = [&](int ii, int jj, int kk, int l) {
-                            return ldg_d(R + (size_t)L * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
+                            return ldg_d(R + 2 * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
                         };
                         const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
                         const double s1 = ld(i, j, k, 1), s2v = ld(i, j, k + 1, 1);
@@ -501,9 +514,10 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         // T and S: double-float transfers, FP64 update
                         const float *Lk = slo + bk * P * 3, *Lu = slo + bk1 * P * 3;
                         double tn[2];
+                        const double2 ts_old = __ldg(Rk);
 #pragma unroll
                         for (int l = 0; l < 2; ++l) {
-                            const double told = Rk[l];
+                            const double told = l ? ts_old.y : ts_old.x;
                             const dflt Tc = {pC[l], Lk[sC * 3 + l]};
                             const int sl = scl[l];
                             // sum = (Gw - Ge) + (Gs - Gn) + (Gb - Ga), faces formed as needed
@@ -535,30 +549,28 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             carryT[l] = Ga;
                             const double dlt = f2d_scaled(sum.hi, sl) + f2d_scaled(sum.lo, sl);
                             tn[l] = fma(dlt, rv, told);
-                            Wk[l] = tn[l];
                             hmax = max(hmax, (unsigned)__double2hiint(tn[l]) & 0x7fffffffu);
                         }
-                        // FP32 density prescreen for the exact convective adjustment
-                        const float tf = d2f_scaled(tn[0], 0), sf = d2f_scaled(tn[1], 0);
-                        const float rf = eos_f(ecf, tf, sf);
-                        if (k > k1c) {
-                            const float margin = 2.0e-6f * (fabsf(rf) + fabsf(rho_prev) + fabsf(ecf[0] * tf) +
-                                                            fabsf(ecf[1] * sf) + fabsf(ecf[2] * tf * tf) +
-                                                            fabsf(ecf[3] * tf * tf * tf)) + 1.0e-30f;
-                            if (!(rho_prev - rf > margin)) unstable = true;
-                        }
-                        rho_prev = rf;
+                        *Wk = make_double2(tn[0], tn[1]);
+                        // The column needs the convective adjustment iff two consecutive wet levels
+                        // are not strictly stably stratified: the test of co (goldstein.f90:2715-2716)
+                        // on the same FP64 densities (with ieos != 0 every column is adjusted).
+                        const double rk = eos_md(md, tn[0], tn[1]);
+                        if (k > k1c && !(rk < rho_prev)) unstable = true;
+                        rho_prev = rk;
                     }
                     // other tracers: FP32 transfers rounded once to int32, FP64 update
                     const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
                     const float As = AsX.hi, Bs = BsX.hi;
                     const float cC0 = C0X.hi, cC1 = C1X.hi, cW0 = W0X.hi, cE0 = E0X.hi, cS0 = S0X.hi, cN0 = N0X.hi;
                     const float cW1 = W1X.hi, cE1 = E1X.hi, cS1 = S1X.hi, cN1 = N1X.hi;
-                    const int q0 = ts_group ? 2 : 0;
+                    double2 told2 = make_double2(0.0, 0.0);
+                    double tlast = 0.0;
 #pragma unroll
                     for (int q = 0; q < kGroup; ++q) {
-                        if (q < q0 || q >= gl) continue;
-                        const double told = Rk[q];
+                        if (ts_group || q >= gl) continue;
+                        if ((q & 1) == 0) told2 = __ldg(Rk + q / 2);
+                        const double told = (q & 1) ? told2.y : told2.x;
                         const float Tc = pC[q], TE = pE[q], TW = pW[q], TN = pN[q], TS = pS[q];
                         const float ge = fmaf(Ae, TE, Be * Tc);
                         const float gw = fmaf(Aw, Tc, Bw * TW);
@@ -594,8 +606,11 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         const int sum = (qw - qe) + (qs - qn) + (carry[q] - qa);
                         carry[q] = qa;
                         const double tnew = fma(i2d_scaled(sum, scl[q]), rv, told);
-                        Wk[q] = tnew;
                         hmax = max(hmax, (unsigned)__double2hiint(tnew) & 0x7fffffffu);
+                        // 16-byte stores of pairs (the pad of an odd group is written as zero)
+                        if (q & 1) Wk[q / 2] = make_double2(tlast, tnew);
+                        else if (q + 1 >= gl) Wk[q / 2] = make_double2(tnew, 0.0);
+                        tlast = tnew;
                     }
                 }
                 bk = bk1;
@@ -604,8 +619,13 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             __syncthreads();
         }
 
-        // columns whose density profile may be unstable: exact convective adjustment next
-        if (item.z == 0 && interior) md.coflag[cl0] = unstable ? 1 : 0;
+        // columns that need the exact convective adjustment (every column with iconv = 1 or
+        // ieos != 0) join the step's list: (member, word offset of the column's record)
+        if (item.z == 0 && interior && (unstable || md.iconv == 1 || md.ieos != 0)) {
+            const int at = atomicAdd(&cocount[step & 1], 1);
+            if (at < cocap) colist[at] = make_int2(item.x, (int)(ticol - md.ptab) + kIcolWords * t);
+            else atomicOr(md.status, 4u);
+        }
         if (ISO && md.diso) {
             unsigned long long *dg = md.diag + 2 * (step & 1);
             unsigned long long db = __double_as_longlong(dmax_l);
@@ -648,62 +668,103 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
 }
 
 // Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step flagged
-// (all columns with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  An item is
-// (member, patch table offset): thread t takes the patch's interior column t.
+// (every column with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  An item is
+// (member, patch table offset); each warp takes interior columns of the patch in turn and
+// adjusts a column with one lane per tracer (co_warp), the column staged in shared memory
+// (kmax: the largest maxk of the batch).  coshuffle (iconv = 1) runs on one lane.
 __global__ void __launch_bounds__(kFp32Threads)
-k_co_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
-          const long long *__restrict__ step_ctr, int rel)
+k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
+          const long long *__restrict__ step_ctr, int rel, int kmax)
 {
+    extern __shared__ double cosm[];
     const long long step = *step_ctr + rel;
-    const int t = threadIdx.x;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int4 item = items[it];
-        const MemberDesc &md = mds[item.x];
-        if (step >= md.stop_step) continue;
-        const int32_t *tab = md.ptab + item.y;
-        const int ns = tab[0], ni = tab[1], maxk = md.maxk;
-        if (t >= ni) continue;
-        const int32_t *ticol = tab + ((kPatchHdr + 2 * (maxk + 2) + ns + 3) & ~3) + kIcolWords * t;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    double *tv = cosm + (size_t)warp * (kmax + 1) * 32;
+    CoWarpState *cs = reinterpret_cast<CoWarpState *>(cosm + (size_t)nwarp * (kmax + 1) * 32) + warp;
+    const int ncol = min(cocount[step & 1], cocap);
+    // the list of the next step starts empty (that step's kernel runs after this one)
+    if (blockIdx.x == 0 && threadIdx.x == 0) cocount[(step + 1) & 1] = 0;
+    for (int e = blockIdx.x * nwarp + warp; e < ncol; e += gridDim.x * nwarp) {
+        const int2 ent = colist[e];
+        const MemberDesc &md = mds[ent.x];
+        const int32_t *ticol = md.ptab + ent.y;
+        const int maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ, mkn = maxk + 2;
         const int k1c = (ticol[2] >> 16) & 0xffff, cl0 = ticol[3];
         const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
-        if (!(md.coflag[cl0] || md.iconv == 1 || md.ieos != 0)) continue;
         const int par = (int)((step + md.parity) & 1);
-        const int L = md.L, mkn = maxk + 2;
+        double *W = md.buf[par ^ 1];
         const double *mk = md.mk;
-        Fp32Col col;
-        col.w = md.buf[par ^ 1];
-        col.stat = md.ts_static;
-        col.L = L;
-        col.NI = md.NI;
-        col.NJ = md.NJ;
-        col.i = i;
-        col.j = j;
-        col.k1 = k1c;
+        const double *dz = mk, *rdz = mk + mkn, *zw = mk + 2 * mkn, *zro = mk + 3 * mkn;
         EosCoef ec;
         for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
         ec.ieos = md.ieos;
-        const double *dz = mk, *rdz = mk + mkn, *zw = mk + 2 * mkn, *zro = mk + 3 * mkn;
-        col.rho[0] = 0.0;
-        for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
-        int icos = 0;
-        if (md.iconv == 1) icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
-        const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
         if (md.iconv == 1) {
-            if (filled > icos) icos = filled;
-            md.icosd[cl0] = icos;
-            md.cost[cl0] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
-        } else if (filled > 0) {
+            if (lane == 0) {
+                Fp32Col col;
+                col.w = W;
+                col.stat = md.ts_static;
+                col.L = L;
+                col.NI = NI;
+                col.NJ = NJ;
+                col.nk = maxk + 2;
+                col.init_planes();
+                col.i = i;
+                col.j = j;
+                col.k1 = k1c;
+                col.rho[0] = 0.0;
+                for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
+                int icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
+                const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
+                if (filled > icos) icos = filled;
+                md.icosd[cl0] = icos;
+                md.cost[cl0] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
+            }
+            __syncwarp();
+            continue;
+        }
+        // the column's wet levels into shared memory, lane l holding tracer l
+        size_t wofs = 0;
+        int gpw = 2;
+        if (lane < L) {
+            int g0 = 0, gl = 2, gp = 2, pl = 0;
+            for (int h = 0; h < fp32_ngroups(L); ++h) {
+                fp32_plane(L, h, &g0, &gl, &gp, &pl);
+                if (lane < g0 + gl) break;
+            }
+            wofs = (size_t)pl * NI * NJ * (maxk + 2) + (lane - g0);
+            gpw = gp;
+        }
+        const size_t NIJ = (size_t)NI * NJ;
+        const double *wc = W + wofs + ((size_t)i + (size_t)NI * j) * gpw;
+        const size_t lstride = NIJ * gpw;
+        if (lane < L)
+            for (int lev = k1c; lev <= maxk; lev += 8) {
+                double v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (lev + u <= maxk) v[u] = wc[(size_t)(lev + u) * lstride];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
+            }
+        __syncwarp();
+        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane);
+        if (lane < L)
+            for (int lev = k1c; lev <= maxk; ++lev) const_cast<double *>(wc)[(size_t)lev * lstride] = tv[lev * 32 + lane];
+        if (lane == 0 && filled > 0) {
             double cst = md.cost[cl0];
             for (int f = 0; f < filled; ++f) cst = __dadd_rn(cst, 1.0);
             md.cost[cl0] = cst;
         }
+        __syncwarp();
     }
 }
 
 int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).total; }
 
-int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, const int4 *co_items, int nco,
-                int max_slots, const long long *step_ctr, int rel, int *work, bool iso, cudaStream_t s)
+int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int max_slots, int kmax,
+                const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap, bool iso,
+                cudaStream_t s)
 {
     static int nsm = 0;
     if (!nsm) {
@@ -720,8 +781,12 @@ int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, const in
     if (per_sm < 1) per_sm = 1;
     int grid = std::min(nitems, nsm * per_sm);
     if (grid < 1) grid = 1;
-    kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P);
-    k_co_fp32<<<std::max(1, std::min(nco, 4 * nsm)), kFp32Threads, 0, s>>>(descs, co_items, nco, step_ctr, rel);
+    kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P, colist, cocount, cocap);
+    const int co_smem = (kFp32Threads / 32) * ((kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
+    cudaFuncSetAttribute(k_co_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
+    int co_per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, k_co_fp32, kFp32Threads, co_smem);
+    k_co_fp32<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(descs, colist, cocount, cocap, step_ctr, rel, kmax);
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
@@ -885,7 +950,7 @@ int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, 
                 w[kPatchHdr + k] = a;
                 w[kPatchHdr + maxk + 2 + k] = r;
             }
-            for (int s = 0; s < ns; ++s) w[kPatchHdr + 2 * (maxk + 2) + s] = d.L * (sl[s].i + NI * sl[s].j);
+            for (int s = 0; s < ns; ++s) w[kPatchHdr + 2 * (maxk + 2) + s] = sl[s].i + NI * sl[s].j;
             while (w.size() & 3) w.push_back(0);
             auto nbslot = [&](int i, int j) -> int {
                 if (j < 0 || j > maxj + 1) return 0xffff;
@@ -933,7 +998,8 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     const double *dz = kb, *dza = kb + nk, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk,
                  *dt = kb + 5 * nk, *zw = kb + 6 * nk, *ssmax = kb + 7 * nk;
     const size_t ncell = (size_t)maxi * maxj * maxk;
-    out.coef.assign(12 * ncell, 0.0f);
+    out.coef.assign(8 * ncell, 0.0f);
+    out.coefl.assign(8 * ncell, 0.0f);
     out.rvol.assign((size_t)maxj * maxk, 0.0);
     out.cmax = 0.0;
     auto U = [&](int c, int i, int j, int k) -> double {
@@ -944,7 +1010,9 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
         for (int j = 1; j <= maxj; ++j) {
             out.rvol[(size_t)(j - 1) + (size_t)maxj * (k - 1)] = 1.0 / (p.dphi * ds[j] * dz[k]);
             for (int i = 1; i <= maxi; ++i) {
-                float *c = &out.coef[12 * ((size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1)))];
+                const size_t cell = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1));
+                float *c = &out.coef[8 * cell];
+                float *cl = &out.coefl[8 * cell];
                 double cd[6] = {0, 0, 0, 0, 0, 0};
                 const int k1c = K1(i, j);
                 const int ie = (i == maxi) ? 1 : i + 1;
@@ -969,10 +1037,10 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
                     cd[4] = g * (u3 * (1.0 - ups) * 0.5 - rdza[k] * p.diff2);
                     cd[5] = g * (u3 * (1.0 + ups) * 0.5 + rdza[k] * p.diff2);
                 }
-                // layout: Ae Be An Bn | Aa Ba, lo(Aa) lo(Ba) | lo(Ae) lo(Be) lo(An) lo(Bn)
+                // Ae Be An Bn Aa Ba 0 0 as FP32, and their FP64 remainders in the same order
                 for (int n = 0; n < 6; ++n) {
                     c[n] = (float)cd[n];
-                    c[n < 4 ? 8 + n : 2 + n] = (float)(cd[n] - (double)c[n]);
+                    cl[n] = (float)(cd[n] - (double)c[n]);
                 }
                 for (int f = 0; f < 3; ++f)
                     out.cmax = std::max(out.cmax, (double)std::fabs(c[2 * f]) + (double)std::fabs(c[2 * f + 1]));
@@ -1086,8 +1154,50 @@ __global__ void k_export_halo(const MemberDesc md, double *cur, double *rho)
     }
 }
 
-int fp32_export(const MemberDesc &md, const double *cur, double *rho, cudaStream_t s)
+// Fortran layout <-> group-planar layout, every cell of the arrays
+__global__ void k_to_planar(double *planar, double *fortran, Dims d, int to)
 {
+    const size_t ncell = (size_t)d.NI * d.NJ * (d.maxk + 2);
+    const size_t n = ncell * d.L;
+    const int ng = fp32_ngroups(d.L);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(e % d.L);
+        const size_t c = e / d.L;
+        int g0 = 0, gl = 2, gp = 2, pl = 0;
+        for (int h = 0; h < ng; ++h) {
+            fp32_plane(d.L, h, &g0, &gl, &gp, &pl);
+            if (l < g0 + gl) break;
+        }
+        const size_t pi = (size_t)pl * ncell + c * gp + (l - g0);
+        if (to) planar[pi] = fortran[e];
+        else fortran[e] = planar[pi];
+    }
+}
+
+static int planar_copy(double *planar, double *fortran, const Dims &d, int to, cudaStream_t s)
+{
+    const size_t n = (size_t)d.NI * d.NJ * (d.maxk + 2) * d.L;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 8192);
+    k_to_planar<<<std::max(1, blocks), 256, 0, s>>>(planar, fortran, d, to);
+    count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+}
+
+int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s)
+{
+    return planar_copy(planar, const_cast<double *>(fortran), d, 1, s);
+}
+
+int fp32_from_planar(double *fortran, const double *planar, const Dims &d, cudaStream_t s)
+{
+    return planar_copy(const_cast<double *>(planar), fortran, d, 0, s);
+}
+
+// The current state in Fortran layout (halo columns filled) and rho of it.
+int fp32_export(const MemberDesc &md, const double *planar, double *cur, double *rho, cudaStream_t s)
+{
+    Dims d{md.maxi, md.maxj, md.maxk, md.L, md.NI, md.NJ};
+    if (fp32_from_planar(cur, planar, d, s)) return GB_GO_ECUDA;
     const size_t ncell = (size_t)md.maxj * md.maxk * (md.maxi + 2);
     const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 4096);
     k_export_fp32<<<blocks, 256, 0, s>>>(md, const_cast<double *>(cur), rho);
@@ -1155,7 +1265,10 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     Fp32Data &D = h->data;
     D.max_slots = plan.max_slots;
     const size_t ncell = (size_t)d.maxi * d.maxj * d.maxk;
-    cudaError_t e = cudaMalloc(&D.coef, 12 * ncell * sizeof(float));
+    cudaError_t e = cudaMalloc(&D.coef, 8 * ncell * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&D.coefl, 8 * ncell * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&D.plan_buf[0], fp32_planar_size(d) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&D.plan_buf[1], fp32_planar_size(d) * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.rvol, (size_t)d.maxj * d.maxk * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.gtop, (size_t)(d.L + 2) * d.maxi * d.maxj * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.scale, (size_t)d.L * sizeof(int32_t));
@@ -1168,19 +1281,21 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMalloc(&D.step_ctr, sizeof(long long));
     const int ng = fp32_ngroups(d.L);
     D.nitems = (int)plan.offset.size() * ng;
-    D.nco = (int)plan.offset.size();
+    D.cocap = 0;
+    for (int j = 1; j <= d.maxj; ++j)
+        for (int i = 1; i <= d.maxi; ++i) D.cocap += k1_host[i + (size_t)d.NI * j] <= d.maxk;
     if (e == cudaSuccess) e = cudaMalloc(&D.work, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(D.work, 0, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&D.ptab, std::max<size_t>(1, plan.words.size()) * sizeof(int32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&D.coflag, (size_t)d.maxi * d.maxj);
-    if (e == cudaSuccess) e = cudaMemset(D.coflag, 0, (size_t)d.maxi * d.maxj);
-    if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems + D.nco) * sizeof(int4));
+    if (e == cudaSuccess) e = cudaMalloc(&D.colist, std::max(1, D.cocap) * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems) * sizeof(int4));
     if (e == cudaSuccess) {
-        // (patch, group) items, longest first (the group of T and S, then the others); then co items
+        // (patch, group) items, a patch's groups together
         std::vector<int4> it;
-        for (int g = 0; g < ng; ++g)
-            for (size_t n = 0; n < plan.offset.size(); ++n) it.push_back(make_int4(0, plan.offset[n], g, 0));
-        for (size_t n = 0; n < plan.offset.size(); ++n) it.push_back(make_int4(0, plan.offset[n], 0, 0));
+        for (size_t n = 0; n < plan.offset.size(); ++n)
+            for (int g = 0; g < ng; ++g) it.push_back(make_int4(0, plan.offset[n], g, 0));
         if (!plan.words.empty())
             e = cudaMemcpyAsync(D.ptab, plan.words.data(), plan.words.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !it.empty())
@@ -1205,9 +1320,9 @@ void fp32_member_free(Fp32Member *f)
     if (!f || !f->impl) return;
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
-    cudaFree(D.coef); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
+    cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
-    cudaFree(D.coflag);
+    cudaFree(D.colist); cudaFree(D.cocount);
     delete h;
     f->impl = nullptr;
     f->ready = false;
@@ -1224,9 +1339,11 @@ static int upload_scales(Fp32Host *h, cudaStream_t s)
            cuda_ok(cudaStreamSynchronize(s));
 }
 
-int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, cudaStream_t s)
+int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, const double *ts1_dev, cudaStream_t s)
 {
     Fp32Host *h = host_of(f);
+    if (fp32_to_planar(h->data.plan_buf[0], ts1_dev, h->d, s) || fp32_to_planar(h->data.plan_buf[1], ts1_dev, h->d, s))
+        return GB_GO_ECUDA;
     const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
     h->ts1_host.assign(ts1_host, ts1_host + nts);
     h->have_state = true;
@@ -1255,6 +1372,8 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s
     Fp32Data &D = h->data;
     D.cmax = st.cmax;
     cudaError_t e = cudaMemcpyAsync(D.coef, st.coef.data(), st.coef.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(D.coefl, st.coefl.data(), st.coefl.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.rvol, st.rvol.data(), st.rvol.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.mk, st.mk.data(), st.mk.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.mj, st.mj.data(), st.mj.size() * sizeof(double), cudaMemcpyHostToDevice, s);
@@ -1267,6 +1386,7 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s
 int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, const double *ts_static, double *cost,
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s)
 {
+    (void)ts_buf;   // the FP32-flux state lives in its own group-planar buffers
     (void)rho;
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
@@ -1281,13 +1401,12 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.dt = h->dt; md.dphi = h->p.dphi; md.rdphi = h->p.rdphi; md.diff1 = h->p.diff1;
         for (int n = 0; n < 5; ++n) md.ec[n] = h->p.ec[n];
         md.dsc = h->p.dsc;
-        md.buf[0] = ts_buf[0];
-        md.buf[1] = ts_buf[1];
+        md.buf[0] = D.plan_buf[0];
+        md.buf[1] = D.plan_buf[1];
         md.ts_static = ts_static;
-        md.coef = D.coef; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
+        md.coef = D.coef; md.coefl = D.coefl; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
         md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
         md.ptab = D.ptab;
-        md.coflag = D.coflag;
         md.status = D.status;
         md.diag = diag;
         if (cudaMemcpyAsync(D.dev, &md, sizeof(md), cudaMemcpyHostToDevice, s) != cudaSuccess) return GB_GO_ECUDA;
@@ -1302,8 +1421,8 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         const long long step = D.steps + n;
         if (cudaMemsetAsync(diag + 2 * (step & 1), 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
             return GB_GO_ECUDA;
-        int r = D.nitems ? fp32_launch(D.dev, D.items, D.nitems, D.items + D.nitems, D.nco, D.max_slots, D.step_ctr, n,
-                                       D.work, h->p.diso != 0, s)
+        int r = D.nitems ? fp32_launch(D.dev, D.items, D.nitems, D.max_slots, h->d.maxk, D.step_ctr, n, D.work, D.colist,
+                                       D.cocount, D.cocap, h->p.diso != 0, s)
                          : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;
@@ -1315,7 +1434,13 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
     return 0;
 }
 
-int fp32_member_export(Fp32Member *f, const double *ts_cur, double *rho, const double *ts_static, cudaStream_t s)
+int fp32_member_fortran(Fp32Member *f, double *dst, cudaStream_t s)
+{
+    Fp32Host *h = host_of(f);
+    return fp32_from_planar(dst, h->data.plan_buf[h->data.steps & 1], h->d, s);
+}
+
+int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s)
 {
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
@@ -1326,13 +1451,13 @@ int fp32_member_export(Fp32Member *f, const double *ts_cur, double *rho, const d
     md.ts_static = ts_static;
     md.mk = D.mk;
     md.k1 = h->k1_dev;
-    int r = fp32_export(md, ts_cur, rho, s);
+    int r = fp32_export(md, D.plan_buf[D.steps & 1], ts_cur, rho, s);
     if (r) return r;
     unsigned int st = 0;
     if (cudaMemcpyAsync(&st, D.status, sizeof(st), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GB_GO_ECUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return GB_GO_ECUDA;
     if (st & 1u) return GB_GO_ENONFINITE;
-    if (st & 2u) return GB_GO_ERANGE;
+    if (st & 6u) return GB_GO_ERANGE;
     return 0;
 }
 
