@@ -75,7 +75,9 @@ struct gb_ens {
     MemberDesc *descs = nullptr;        // device, capacity cap_desc
     int cap_desc = 0;
     int4 *items = nullptr;              // device, capacity cap_items
-    int cap_items = 0, nitems = 0;
+    int cap_items = 0, nitems = 0, n_ts = 0;
+    cudaStream_t s2 = nullptr;          // second stream: T-S items and the others side by side
+    cudaEvent_t fork = nullptr, join = nullptr;
     int max_slots = 1;
     bool any_iso = false;               // some member has the isoneutral branch
     int kmax = 1;                       // largest maxk of the members
@@ -142,8 +144,11 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
     }
     if (x == cudaSuccess) x = cudaMalloc(&e->step_ctr, sizeof(long long));
     if (x == cudaSuccess) x = cudaMemset(e->step_ctr, 0, sizeof(long long));
-    if (x == cudaSuccess) x = cudaMalloc(&e->work, 2 * sizeof(int));
-    if (x == cudaSuccess) x = cudaMemset(e->work, 0, 2 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMalloc(&e->work, 4 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMemset(e->work, 0, 4 * sizeof(int));
+    if (x == cudaSuccess) x = cudaStreamCreateWithFlags(&e->s2, cudaStreamNonBlocking);
+    if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+    if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
     if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 2 * sizeof(int));
     if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 2 * sizeof(int));
     if (x != cudaSuccess) {
@@ -174,6 +179,9 @@ extern "C" void gb_ens_destroy(gb_ens *e)
     if (e->graph) cudaGraphExecDestroy(e->graph);
     cudaFree(e->step_ctr);
     cudaFree(e->work);
+    if (e->s2) cudaStreamDestroy(e->s2);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->join) cudaEventDestroy(e->join);
     cudaFree(e->cocount);
     cudaFree(e->colist);
     cudaFree(e->descs);
@@ -391,8 +399,11 @@ static int rebuild(gb_ens *e)
     // column list holds at most every wet column of the batch.
     std::vector<int4> it;
     for (auto &o : order)
+        for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], 0, 0));
+    const int n_ts = (int)it.size();
+    for (auto &o : order)
         for (size_t n = 0; n < o.second->poff.size(); ++n)
-            for (int g = 0; g < fp32_group_count(o.second->d.L); ++g)
+            for (int g = 1; g < fp32_group_count(o.second->d.L); ++g)
                 it.push_back(make_int4(o.second->slot, o.second->poff[n], g, 0));
     int cocap = 0;
     for (auto &o : order) cocap += o.second->wet_cols;
@@ -406,6 +417,7 @@ static int rebuild(gb_ens *e)
     if (!it.empty()) ETRY(e, cudaMemcpyAsync(e->items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
     ETRY(e, cudaStreamSynchronize(s));
     e->nitems = (int)it.size();
+    e->n_ts = n_ts;
     if (cocap > e->cocap) {
         if (e->colist) cudaFreeAsync(e->colist, s);
         e->colist = nullptr;
@@ -423,17 +435,39 @@ static int rebuild(gb_ens *e)
     return GB_GO_OK;
 }
 
+static Fp32Batch batch_of(gb_ens *e)
+{
+    Fp32Batch b;
+    b.descs = e->descs;
+    b.items = e->items;
+    b.n_ts = e->n_ts;
+    b.n_bgc = e->nitems - e->n_ts;
+    b.max_slots = e->max_slots;
+    b.kmax = e->kmax;
+    b.work = e->work;
+    b.colist = e->colist;
+    b.cocount = e->cocount;
+    b.cocap = e->cocap;
+    b.iso = e->any_iso;
+    return b;
+}
+
+// kernels started by launch_steps(e, nsteps)
+static uint64_t launches_of(gb_ens *e, int nsteps)
+{
+    return (uint64_t)nsteps * (fp32_launches_per_step(batch_of(e)) + 1) + 1;
+}
+
 static int launch_steps(gb_ens *e, int nsteps)
 {
     cudaStream_t s = e->stream;
+    const Fp32Batch b = batch_of(e);
     for (int n = 0; n < nsteps; ++n) {
-        int r = fp32_launch(e->descs, e->items, e->nitems, e->max_slots, e->kmax, e->step_ctr, n, e->work, e->colist,
-                            e->cocount, e->cocap, e->any_iso, s);
+        int r = fp32_launch(b, e->step_ctr, n, s, e->s2, e->fork, e->join);
         if (!r) r = fp32_rescale(e->descs, (int)e->members.size(), s);
         if (r) return efail(e, r, "fp32 batched launch failed");
     }
     k_add_step<<<1, 1, 0, s>>>(e->step_ctr, nsteps);
-    count_launches(3 * (uint64_t)nsteps + 1);   // step, co, rescale per step; step counter
     return cudaGetLastError() == cudaSuccess ? GB_GO_OK : efail(e, GB_GO_ECUDA, "launch failed");
 }
 
@@ -469,11 +503,11 @@ extern "C" int gb_ens_step(gb_ens *e, int32_t nsteps)
             e->graph_steps = nsteps;
         }
         ETRY(e, cudaGraphLaunch(e->graph, e->stream));
-        count_launches(3 * (uint64_t)nsteps + 1);   // step, co, rescale per step; step counter
     } else {
         int r = launch_steps(e, nsteps);
         if (r) return r;
     }
+    count_launches(launches_of(e, nsteps));
     e->step += nsteps;
     return GB_GO_OK;
 }

@@ -116,6 +116,9 @@ struct Fp32Data {
     int2 *colist = nullptr;     // columns for the exact convective adjustment (capacity cocap)
     int *cocount = nullptr;     // their count, two by step parity
     int cocap = 0;
+    int n_ts = 0;               // items[0, n_ts): T-S groups
+    cudaStream_t s2 = nullptr;  // second stream and events: the two kinds of items side by side
+    cudaEvent_t fork = nullptr, join = nullptr;
     int32_t *ptab = nullptr;    // patch tables
     int *work = nullptr;        // work counters (two, by step parity)
     int max_slots = 1;
@@ -183,14 +186,28 @@ int fp32_group_count(int L);   // tracer groups (work items per patch): T and S,
 int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s);
 int fp32_from_planar(double *fortran, const double *planar, const Dims &d, cudaStream_t s);
 inline size_t fp32_planar_size(const Dims &d) { return (size_t)fp32_planar_width(d.L) * d.NI * d.NJ * (d.maxk + 2); }
-// One step of a batch: the transfer kernel over (member, patch, group) items, which lists the
-// columns that need the exact convective adjustment (colist, count in cocount[step & 1],
-// capacity cocap: the wet columns of the batch), then the adjustment of those columns.
-// kmax: the largest maxk of the batch; iso: some member has the isoneutral branch (selects
-// the kernel instance that has it).
-int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int max_slots, int kmax,
-                const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap, bool iso,
-                cudaStream_t s);
+// One step of a batch: the transfer kernels over (member, patch, group) items (items[0, n_ts)
+// are the T-S groups, items[n_ts, n_ts + n_bgc) the others), which list the columns that
+// need the exact convective adjustment (colist, count in cocount[step & 1], capacity cocap:
+// the wet columns of the batch), then the adjustment of those columns.  kmax: the largest
+// maxk of the batch; iso: some member has the isoneutral branch (selects the kernel
+// instances that have it); work: four counters.
+struct Fp32Batch {
+    const MemberDesc *descs = nullptr;
+    const int4 *items = nullptr;
+    int n_ts = 0, n_bgc = 0;
+    int max_slots = 1, kmax = 1;
+    int *work = nullptr;
+    int2 *colist = nullptr;
+    int *cocount = nullptr;
+    int cocap = 0;
+    bool iso = false;
+};
+// s2/fork/join: a second stream and two events to run the two item kinds side by side
+// (s2 null: one stream).
+int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStream_t s, cudaStream_t s2,
+                cudaEvent_t fork, cudaEvent_t join);
+int fp32_launches_per_step(const Fp32Batch &b);   // kernels fp32_launch starts
 int fp32_smem_bytes(int max_slots);
 // current state (group-planar) -> Fortran layout with halo columns, and rho
 int fp32_export(const MemberDesc &md, const double *planar, double *cur, double *rho, cudaStream_t s);

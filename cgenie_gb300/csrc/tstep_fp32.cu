@@ -211,9 +211,10 @@ __host__ __device__ inline Fp32Smem fp32_smem_layout(int P)
 __device__ __forceinline__ double ldg_d(const double *p) { return __ldg(p); }
 
 // ISO: the isoneutral branch is compiled in (members with diso); without it the kernel
-// needs fewer registers.  A work item is (member, patch table offset, tracer group).
-template <bool ISO>
-__global__ void __launch_bounds__(kFp32Threads, 4)
+// needs fewer registers.  TS: the instance for group 0 (T and S); the other instance takes
+// the other groups.  A work item is (member, patch table offset, tracer group).
+template <bool ISO, bool TS>
+__global__ void __launch_bounds__(kFp32Threads, TS ? 4 : 5)
 k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, int nitems,
             const long long *__restrict__ step_ctr, int rel, int *__restrict__ work, int P,
             int2 *__restrict__ colist, int *__restrict__ cocount, int cocap)
@@ -321,7 +322,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         {
             int g0, gl, gp, plane;
             fp32_plane(L, item.z, &g0, &gl, &gp, &plane);
-            const bool ts_group = (item.z == 0);
+            constexpr bool ts_group = TS;
             const long long NIJK = (long long)NI * NJ * (maxk + 2), NIJ = (long long)NI * NJ;
             const double *__restrict__ Rg = R + NIJK * plane;
             double *__restrict__ Wg = W + NIJK * plane;
@@ -762,9 +763,23 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
 
 int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).total; }
 
-int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int max_slots, int kmax,
-                const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap, bool iso,
-                cudaStream_t s)
+template <bool ISO, bool TS>
+static void launch_step_instance(const MemberDesc *descs, const int4 *items, int nitems, int P, int smem_bytes,
+                                 const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap,
+                                 int nsm, cudaStream_t s)
+{
+    if (nitems <= 0) return;
+    auto kern = k_step_fp32<ISO, TS>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
+    if (per_sm < 1) per_sm = 1;
+    const int grid = std::max(1, std::min(nitems, nsm * per_sm));
+    kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P, colist, cocount, cocap);
+}
+
+int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStream_t s, cudaStream_t s2,
+                cudaEvent_t fork, cudaEvent_t join)
 {
     static int nsm = 0;
     if (!nsm) {
@@ -772,23 +787,40 @@ int fp32_launch(const MemberDesc *descs, const int4 *items, int nitems, int max_
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
-    const int P = max_slots + 1;
+    const int P = b.max_slots + 1;
     const int smem_bytes = fp32_smem_layout(P).total;
-    auto kern = iso ? k_step_fp32<true> : k_step_fp32<false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
-    if (per_sm < 1) per_sm = 1;
-    int grid = std::min(nitems, nsm * per_sm);
-    if (grid < 1) grid = 1;
-    kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P, colist, cocount, cocap);
-    const int co_smem = (kFp32Threads / 32) * ((kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
+    // the T-S items and the other items run side by side (two streams), then the adjustment
+    const bool two = b.n_ts > 0 && b.n_bgc > 0 && s2 != nullptr;
+    if (two) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(s2, fork, 0);
+    }
+    cudaStream_t sb = two ? s2 : s;
+    if (b.iso) {
+        launch_step_instance<true, true>(b.descs, b.items, b.n_ts, P, smem_bytes, step_ctr, rel, b.work, b.colist,
+                                         b.cocount, b.cocap, nsm, s);
+        launch_step_instance<true, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, smem_bytes, step_ctr, rel, b.work + 2,
+                                          b.colist, b.cocount, b.cocap, nsm, sb);
+    } else {
+        launch_step_instance<false, true>(b.descs, b.items, b.n_ts, P, smem_bytes, step_ctr, rel, b.work, b.colist,
+                                          b.cocount, b.cocap, nsm, s);
+        launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, smem_bytes, step_ctr, rel,
+                                           b.work + 2, b.colist, b.cocount, b.cocap, nsm, sb);
+    }
+    if (two) {
+        cudaEventRecord(join, s2);
+        cudaStreamWaitEvent(s, join, 0);
+    }
+    const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
     cudaFuncSetAttribute(k_co_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
     int co_per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, k_co_fp32, kFp32Threads, co_smem);
-    k_co_fp32<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(descs, colist, cocount, cocap, step_ctr, rel, kmax);
+    k_co_fp32<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
+                                                                           step_ctr, rel, b.kmax);
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
+
+int fp32_launches_per_step(const Fp32Batch &b) { return (b.n_ts > 0) + (b.n_bgc > 0) + 1; }
 
 // ---------------------------------------------------------------------------
 // patch plan (host): rectangles of water columns, periodic in i, with the ring of
@@ -1284,18 +1316,23 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     D.cocap = 0;
     for (int j = 1; j <= d.maxj; ++j)
         for (int i = 1; i <= d.maxi; ++i) D.cocap += k1_host[i + (size_t)d.NI * j] <= d.maxk;
-    if (e == cudaSuccess) e = cudaMalloc(&D.work, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(D.work, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.work, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(D.work, 0, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&D.s2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&D.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&D.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&D.ptab, std::max<size_t>(1, plan.words.size()) * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc(&D.colist, std::max(1, D.cocap) * sizeof(int2));
     if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems) * sizeof(int4));
     if (e == cudaSuccess) {
-        // (patch, group) items, a patch's groups together
+        // the T-S items of the patches, then the other (patch, group) items
         std::vector<int4> it;
+        for (size_t n = 0; n < plan.offset.size(); ++n) it.push_back(make_int4(0, plan.offset[n], 0, 0));
         for (size_t n = 0; n < plan.offset.size(); ++n)
-            for (int g = 0; g < ng; ++g) it.push_back(make_int4(0, plan.offset[n], g, 0));
+            for (int g = 1; g < ng; ++g) it.push_back(make_int4(0, plan.offset[n], g, 0));
+        D.n_ts = (int)plan.offset.size();
         if (!plan.words.empty())
             e = cudaMemcpyAsync(D.ptab, plan.words.data(), plan.words.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !it.empty())
@@ -1323,6 +1360,9 @@ void fp32_member_free(Fp32Member *f)
     cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
     cudaFree(D.colist); cudaFree(D.cocount);
+    if (D.s2) cudaStreamDestroy(D.s2);
+    if (D.fork) cudaEventDestroy(D.fork);
+    if (D.join) cudaEventDestroy(D.join);
     delete h;
     f->impl = nullptr;
     f->ready = false;
@@ -1421,12 +1461,22 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         const long long step = D.steps + n;
         if (cudaMemsetAsync(diag + 2 * (step & 1), 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
             return GB_GO_ECUDA;
-        int r = D.nitems ? fp32_launch(D.dev, D.items, D.nitems, D.max_slots, h->d.maxk, D.step_ctr, n, D.work, D.colist,
-                                       D.cocount, D.cocap, h->p.diso != 0, s)
-                         : 0;
+        Fp32Batch bt;
+        bt.descs = D.dev;
+        bt.items = D.items;
+        bt.n_ts = D.n_ts;
+        bt.n_bgc = D.nitems - D.n_ts;
+        bt.max_slots = D.max_slots;
+        bt.kmax = h->d.maxk;
+        bt.work = D.work;
+        bt.colist = D.colist;
+        bt.cocount = D.cocount;
+        bt.cocap = D.cocap;
+        bt.iso = h->p.diso != 0;
+        int r = D.nitems ? fp32_launch(bt, D.step_ctr, n, s, D.s2, D.fork, D.join) : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;
-        count_launches(3);
+        count_launches((D.nitems ? fp32_launches_per_step(bt) : 0) + 1);
     }
     D.steps += nsteps;
     *cur = (int)(D.steps & 1);
