@@ -1,22 +1,30 @@
 """Benchmark of the GB300 GOLDSTEIN tracer step (one JSON line on rank 0).
 
 Workloads (seeded synthetic members with the reference's grid formulas):
+  c3  (default) batched ensemble: 256 members split evenly among 18x18x16,
+      36x36x16 and 36x36x32 grids, 2-24 tracers each, per-member diffusivities,
+      masks and velocities; FP32 transfers, FP64 state; every step one CUDA
+      graph replay (the transfer kernels, the exact convective adjustment and
+      the scale update)
   c2  single member 36x36x16, 17 tracers, isoneutral branch on, FP64 plain form
   c1  single member 36x36x16, 2 tracers, FP64 plain form
 
-A step is one tracer timestep (tstepo) of the member.  `value` is tracer
-cell-updates/s with the state resident in HBM; `e2e` is the same metric through
-the C-ABI with host buffers: every step uploads the surface forcing and the
-velocities from pinned host memory and reads rho back (the per-step exchange
-with the momentum solver, goldstein.f90:167-170,176-177,443-450 minus the state
-copies that residency removes).  The state (~3.5 MB) fits in L2, so L2 is
-flushed (a 256 MB write) before every timed step and the step is timed alone
-with CUDA events on the library's stream.
+A step is one tracer timestep (tstepo) of every member.  `value` is tracer
+cell-updates/s with the state resident in HBM (c3: the 256 states, 2 x 0.6 GB,
+are larger than L2, so L2 is not flushed; c1/c2: L2 flushed before every step).
+For c3 the line also gives the plain per-member GPU rate (the FP64 drop-in path
+stepping the members one at a time) and the largest per-tracer error of the
+batched result against that FP64 path (bit-identical to the FP64 oracle) on a
+sample of members.  `e2e` is the whole job through the C-ABI with host buffers:
+c3 admits the 256 members from host arrays (gb_ens_add), steps them and downloads
+every member (gb_ens_download); c1/c2 upload the forcing and velocities and read
+rho back every step.
 
 --impl reference times the reference algorithm on the host cores instead (the
-oracle's C restatement of goldstein.f90:2280-2842, serial like the reference).
-Multi-GPU (torchrun): every rank runs an independent replica (members are
-independent), weak scaling, time = max over ranks.
+oracle's C restatement of goldstein.f90:2280-2842 with the reference's dead
+copies, one member per process, all host cores).  Multi-GPU (torchrun): every
+rank runs an independent replica (members are independent), weak scaling, time
+= max over ranks.
 """
 from __future__ import annotations
 
@@ -35,6 +43,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "c1": dict(name="tstepo_fp64_36x36x16_L2", factory="config_c1"),
     "c2": dict(name="tstipo_diso_fp64_36x36x16_L17", factory="config_c2"),
+    "c3": dict(name="ensemble256_fp32flux_18x18x16_36x36x16_36x36x32_L2-24", members=256, seed=3),
 }
 
 
@@ -60,7 +69,7 @@ def profile_traffic(kernel: str, workload: str):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms during the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -75,7 +84,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -136,9 +145,61 @@ def cpu_baseline(m, target_s: float = 12.0):
             "sample": f"{n} steps of the same member, oracle C restatement with the reference's dead copies, -O2"}
 
 
-def run_reference(args, rank, world):
+def _ensemble_members(n: int, seed: int):
     from cgenie_gb300 import grid
+    return [grid.make_member(c) for c in grid.ensemble_configs(n, seed=seed)]
+
+
+def _oracle_worker(job):
+    """Step a share of the ensemble members with the oracle (one process); returns
+    (tracer cell-updates, seconds) of the timed steps."""
+    idx, n, seed, warmup, steps, faithful = job
+    sys.path.insert(0, ROOT)
+    from cgenie_gb300 import grid
+    from oracle import oracle_lib
+    cfgs = grid.ensemble_configs(n, seed=seed)
+    states = [oracle_lib.OracleState(grid.make_member(cfgs[i])) for i in idx]
+    for st in states:
+        st.step(warmup, faithful=faithful)
+    cu = sum(st.m.wet_cells * st.m.maxl for st in states) * steps
+    t0 = time.perf_counter()
+    for st in states:
+        st.step(steps, faithful=faithful)
+    return cu, time.perf_counter() - t0
+
+
+def oracle_pool_rate(n: int, seed: int, warmup: int, steps: int, faithful: bool = True):
+    """Ensemble throughput of the oracle on every host core (one process per core, the
+    members dealt round-robin); the slowest process sets the time."""
+    import multiprocessing as mp
+    procs = max(1, os.cpu_count() or 1)
+    jobs = [(list(range(p, n, procs)), n, seed, warmup, steps, faithful) for p in range(procs)]
+    jobs = [j for j in jobs if j[0]]
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        res = pool.map(_oracle_worker, jobs)
+    cu = sum(r[0] for r in res)
+    dt = max(r[1] for r in res)
+    return cu / dt, len(jobs), cu // max(1, steps)
+
+
+def run_reference(args, rank, world):
     w = WORKLOADS[args.workload]
+    if args.workload == "c3":
+        value, cores, cu_step = oracle_pool_rate(w["members"], w["seed"], args.warmup, args.steps, faithful=True)
+        line = {
+            "metric": "tracer cell-updates/s", "value": value, "unit": "tracer cell-updates/s", "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * cu_step / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "members": w["members"], "seed": w["seed"]},
+            "cpu_baseline": {"value": value, "unit": "tracer cell-updates/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} timed steps of all {w['members']} members, oracle C restatement "
+                                       f"with the reference's dead copies, one process per core"},
+            "e2e": {"value": value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+    from cgenie_gb300 import grid
     m = grid.make_member(getattr(grid, w["factory"])())
     from oracle import oracle_lib
     s = oracle_lib.OracleState(m)
@@ -162,13 +223,154 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def _tracer_err(m, a, b):
+    """Largest per-tracer error max|a - b| / max|b| over the wet interior cells."""
+    import numpy as np
+    kk = np.arange(m.maxk + 2)[:, None, None]
+    wet = (kk >= m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
+    wet[:, 0, :] = wet[:, -1, :] = False
+    wet[:, :, 0] = wet[:, :, -1] = False
+    err = 0.0
+    for l in range(m.maxl):
+        x, y = a[..., l][wet], b[..., l][wet]
+        err = max(err, float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300)))
+    return err
+
+
+def run_c3(args, rank, world, local, dist):
+    import numpy as np
+    import torch
+    from cgenie_gb300.ensemble import Ensemble
+    from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+
+    w = WORKLOADS["c3"]
+    mems = _ensemble_members(w["members"], w["seed"])
+    cu_step = sum(m.wet_cells * m.maxl for m in mems)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ens = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
+    ids = [ens.add(m) for m in mems]
+    for _ in range(args.warmup):
+        ens.step(1)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing: one graph replay (a full step of all members) per step
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    for k in range(args.steps):
+        starts[k].record(stream)
+        ens.step(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    launches = kernel_launch_count() - n0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = float(sum(ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * cu_step * args.steps / (total_ms * 1e-3)
+    done = args.warmup + args.steps
+
+    # ---- error against the FP64 path (bit-identical to the FP64 oracle), one member per grid shape
+    err = 0.0
+    for i in range(3):
+        out = ens.download(ids[i])
+        g = new_member_run(mems[i], device=local, stream=stream.cuda_stream)
+        g.tstepo(done)
+        ref = g.download()
+        g.close()
+        err = max(err, _tracer_err(mems[i], out["ts"], ref["ts"]))
+    ens.close()
+
+    # ---- the plain per-member GPU path (FP64 drop-in, one member at a time), two of each shape
+    plain_cu, plain_s = 0, 0.0
+    for i in range(6):
+        g = new_member_run(mems[i], device=local, stream=stream.cuda_stream)
+        g.tstepo(2)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        g.tstepo(20)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_s += a.elapsed_time(b) * 1e-3
+        plain_cu += mems[i].wet_cells * mems[i].maxl * 20
+        g.close()
+    plain_value = plain_cu / plain_s
+
+    # ---- end to end through the C-ABI: admit from host arrays, step, download every member
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
+    ids2 = [e2.add(m) for m in mems]
+    e2.step(args.steps)
+    outs = [e2.download(i) for i in ids2]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2.close()
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * cu_step * args.steps / e2e_s
+    h2d = sum(m.ts.nbytes + m.u.nbytes for m in mems) / args.steps
+    d2h = sum(o["ts"].nbytes + o["rho"].nbytes + o["cost"].nbytes for o in outs) / args.steps
+
+    peak, peak_kind = measured_peaks()
+    alg = sum(algorithmic_bytes(m) for m in mems)
+    achieved = alg / (total_ms * 1e-3 / args.steps) / 1e9
+    traffic = profile_traffic("k_step_fp32", w["name"])
+    if rank == 0:
+        line = {
+            "metric": "tracer cell-updates/s", "value": value, "unit": "tracer cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 transfers, f64 state",
+            "data": "synthetic (seeded members, reference grid formulas)",
+            "config": {"workload": w["name"], "members": w["members"], "seed": w["seed"],
+                       "cell_updates_per_step": cu_step, "precision": "fp32flux",
+                       "l2": "not flushed: the resident states (2 x 0.6 GB) exceed L2",
+                       "cuda_graph": True, "parallelism": f"replicas{world}",
+                       "plain_per_member_gpu": plain_value, "batched_over_plain": value / plain_value,
+                       "max_rel_err_vs_fp64": err, "err_after_steps": done, "err_members": 3},
+            "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "note": f"whole job through the C-ABI: admit {w['members']} members from host arrays, "
+                            f"{args.steps} steps, download every member"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
+                         "algorithmic_bytes_per_launch": alg,
+                         "note": "achieved = algorithmic bytes of a step (16 L + 24 per wet cell, k1) / step time"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            cpu, cores, _ = oracle_pool_rate(w["members"], w["seed"], 1, 12, faithful=True)
+            line["cpu_baseline"] = {"value": cpu, "unit": "tracer cell-updates/s", "cores": cores, "kind": "port",
+                                    "sample": f"12 steps of all {w['members']} members, oracle C restatement with "
+                                              "the reference's dead copies, one process per core"}
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -193,6 +395,11 @@ def main():
     from cgenie_gb300 import build, grid
     build.build()
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+    if args.workload == "c3":
+        run_c3(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     w = WORKLOADS[args.workload]
     m = grid.make_member(getattr(grid, w["factory"])())

@@ -835,6 +835,8 @@ namespace {
 struct PatchShape {
     std::vector<std::pair<int, int>> inner;   // (i, j) wet columns of the rectangle
     std::vector<std::pair<int, int>> ring;    // wet neighbours outside it
+    std::vector<int> seen;                    // scratch: stamp of the last patch that took a column
+    int stamp = 0;
 };
 }
 
@@ -850,15 +852,19 @@ static bool patch_shape(const Dims &d, const int32_t *k1, int i0, int i1, int j0
         for (int i = i0; i <= i1; ++i)
             if (wet(i, j)) ps.inner.push_back({i, j});
     if ((int)ps.inner.size() > kFp32Threads) return false;
-    std::vector<char> seen((size_t)NI * (maxj + 2), 0);
+    if (ps.seen.size() != (size_t)NI * (maxj + 2)) {
+        ps.seen.assign((size_t)NI * (maxj + 2), 0);
+        ps.stamp = 0;
+    }
+    const int stamp = ++ps.stamp;
     for (auto &c : ps.inner) {
         const int i = c.first, j = c.second;
         const int nb[4][2] = {{i == maxi ? 1 : i + 1, j}, {i == 1 ? maxi : i - 1, j}, {i, j + 1}, {i, j - 1}};
         for (auto &n : nb) {
             if (n[1] < 0 || n[1] > maxj + 1 || inside(n[0], n[1]) || !wet(n[0], n[1])) continue;
-            char &s = seen[n[0] + (size_t)NI * n[1]];
-            if (!s) {
-                s = 1;
+            int &s = ps.seen[n[0] + (size_t)NI * n[1]];
+            if (s != stamp) {
+                s = stamp;
                 ps.ring.push_back({n[0], n[1]});
             }
         }
