@@ -183,7 +183,9 @@ def oracle_pool_rate(n: int, seed: int, warmup: int, steps: int, faithful: bool 
 
 
 def run_reference(args, rank, world):
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.workload == "c3" and args.members:
+        w["members"] = args.members
     if args.workload == "c3":
         value, cores, cu_step = oracle_pool_rate(w["members"], w["seed"], args.warmup, args.steps, faithful=True)
         line = {
@@ -243,13 +245,18 @@ def run_c3(args, rank, world, local, dist):
     from cgenie_gb300.ensemble import Ensemble
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
 
-    w = WORKLOADS["c3"]
+    w = dict(WORKLOADS["c3"])
+    if args.members:
+        w["members"] = args.members
+        w["name"] = w["name"].replace("ensemble256", f"ensemble{args.members}")
     mems = _ensemble_members(w["members"], w["seed"])
     cu_step = sum(m.wet_cells * m.maxl for m in mems)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ens = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
     ids = [ens.add(m) for m in mems]
+    if args.steps_before:
+        ens.step(args.steps_before)
     for _ in range(args.warmup):
         ens.step(1)
     torch.cuda.synchronize()
@@ -279,7 +286,7 @@ def run_c3(args, rank, world, local, dist):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * cu_step * args.steps / (total_ms * 1e-3)
-    done = args.warmup + args.steps
+    done = args.steps_before + args.warmup + args.steps
 
     # ---- error against the FP64 path (bit-identical to the FP64 oracle), one member per grid shape
     err = 0.0
@@ -372,6 +379,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--members", type=int, default=0, help="c3: members of the ensemble (default 256)")
+    ap.add_argument("--steps-before", type=int, default=0,
+                    help="c3: steps taken before the warm-up (the members' convection develops over time)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -136,11 +136,46 @@ __device__ int co_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const
     return filled;
 }
 
-// Working arrays of co_warp (one per warp, shared memory).
+// a / b rounded to nearest even, from y ~ 1/b (b > 0 shared by many quotients).
+// Markstein's refinement (P. Markstein, IA-64 and Elementary Functions, 2000):
+// q = a*y, r = a - b*q (exact by FMA), q1 = q + r*y.  q1 is returned only when the exact
+// residual a - b*q1 proves |a/b - q1| < ulp(q1)/2 (q1 normal and not a power of two, so
+// the two neighbours are ulp(q1) away and q1 is the nearest double); otherwise the IEEE
+// division is taken.  The result is always the correctly rounded quotient.
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y)
+{
+    const double q = a * y;
+    const double r = fma(-b, q, a);
+    const double q1 = fma(r, y, q);
+    const double r1 = fma(-b, q1, a);   // a - b*q1, exact when q1 is within an ulp of a/b
+    const long long bits = __double_as_longlong(q1);
+    const int e = (int)((bits >> 52) & 0x7ff);
+    const long long bm = __double_as_longlong(b) & 0x7fffffffffffffffLL;
+    const int eb = (int)(bm >> 52);
+    // |b| * 2^(E-53), E the unbiased exponent of q1: b's exponent field moved by e - 1076
+    const int ebound = eb + e - 1076;
+    if (e > 54 && e < 2046 && (bits & 0xfffffffffffffLL) != 0 && eb > 0 && ebound > 0 && ebound < 2047) {
+        const long long bound = bm + ((long long)(e - 1076) << 52);
+        // non-negative doubles order as their bit patterns
+        if ((__double_as_longlong(r1) & 0x7fffffffffffffffLL) < bound) return q1;
+    }
+    return __ddiv_rn(a, b);
+}
+
+// Integer key that orders doubles as < does (no NaN; -0 and +0 both map to 0).
+__device__ __forceinline__ long long order_key(double x)
+{
+    const long long b = __double_as_longlong(x);
+    if ((b & 0x7fffffffffffffffLL) == 0) return 0;
+    return b < 0 ? (b ^ 0x7fffffffffffffffLL) : b;
+}
+
+// Working arrays of co_warp (one per warp, shared memory).  Densities are kept as
+// order_key values: every lane runs the same merge decisions, on the integer pipe.
 struct CoWarpState {
     int kk[kMaxK + 2];
     double dzm[kMaxK + 1];
-    double rho[kMaxK + 1];
+    long long rho[kMaxK + 1];
 };
 
 // co_rn with one warp per column: the tracers of the column are in shared memory,
@@ -148,27 +183,31 @@ struct CoWarpState {
 // to merge (kk, dzm, rho in cs) are kept by lane 0 (densities of the first pass one lane
 // per level); every value is the one co_rn computes.  Returns the number of filled levels
 // (in every lane).
+// rho0: the column's densities eos(T, S) of the wet levels (rho0[lev * rstride]) when
+// given (ieos = 0), else computed here.
 __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, int maxk, int L, int k1,
-                              const double *dz, const double *zro, const double *zw, int lane)
+                              const double *dz, const double *zro, const double *zw, int lane, const double *rho0,
+                              size_t rstride)
 {
     int *kk = cs->kk;
-    double *dzm = cs->dzm, *rho = cs->rho;
+    double *dzm = cs->dzm;
+    long long *rho = cs->rho;
     auto T = [&](int l, int lev) { return tv[lev * 32 + l]; };
     for (int lev = k1 + lane; lev <= maxk; lev += 32) {
-        rho[lev] = eos_rn(ec, T(0, lev), T(1, lev), zro[lev]);
+        rho[lev] = order_key(rho0 ? rho0[(size_t)lev * rstride] : eos_rn(ec, T(0, lev), T(1, lev), zro[lev]));
         kk[lev] = lev;
         dzm[lev] = dz[lev];
     }
     if (lane == 0) {
-        rho[0] = 0.0;
+        rho[0] = 0;
         kk[k1 - 1] = 0;
     }
     __syncwarp();
     auto refresh = [&](int x, int y) {
         if (ec.ieos != 0) {
             if (lane == 0) {
-                rho[kk[x]] = eos_rn(ec, T(0, kk[x]), T(1, kk[x]), zw[kk[y]]);
-                rho[kk[y]] = eos_rn(ec, T(0, kk[y]), T(1, kk[y]), zw[kk[y]]);
+                rho[kk[x]] = order_key(eos_rn(ec, T(0, kk[x]), T(1, kk[x]), zw[kk[y]]));
+                rho[kk[y]] = order_key(eos_rn(ec, T(0, kk[y]), T(1, kk[y]), zw[kk[y]]));
             }
             __syncwarp();
         }
@@ -191,19 +230,22 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             }
             const int km = kk[m];
             const double d0 = dzm[km];
-            double dtot = d0;
-            if (lane == 0)
+            double dtot = d0, y = 0.0;
+            if (lane == 0) {
                 for (int ni = 1; ni <= m - n; ++ni) dtot = __dadd_rn(dtot, dzm[kk[m - ni]]);
+                y = __drcp_rn(dtot);
+            }
             dtot = __shfl_sync(0xffffffffu, dtot, 0);
+            y = __shfl_sync(0xffffffffu, y, 0);
             if (lane < L) {
                 double s = __dmul_rn(T(lane, km), d0);
                 for (int ni = 1; ni <= m - n; ++ni) s = __dadd_rn(s, __dmul_rn(T(lane, kk[m - ni]), dzm[kk[m - ni]]));
-                tv[km * 32 + lane] = __ddiv_rn(s, dtot);
+                tv[km * 32 + lane] = div_rn_recip(s, dtot, y);
             }
             __syncwarp();
             if (lane == 0) {
                 dzm[km] = dtot;
-                rho[km] = eos_rn(ec, T(0, km), T(1, km), zw[kk[m - 1]]);
+                rho[km] = order_key(eos_rn(ec, T(0, km), T(1, km), zw[kk[m - 1]]));
                 int ni = m - 1;
                 while (kk[ni + 1] > 0) {
                     kk[ni] = kk[ni - m + n];
@@ -220,7 +262,7 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             const int src = kk[m + 1];
             if (lane < L) tv[n * 32 + lane] = T(lane, src);
             __syncwarp();
-            if (lane == 0) rho[n] = eos_rn(ec, T(0, n), T(1, n), zw[kk[n - 1]]);
+            if (lane == 0) rho[n] = order_key(eos_rn(ec, T(0, n), T(1, n), zw[kk[n - 1]]));
             __syncwarp();
             filled = filled + 1;
         } else {

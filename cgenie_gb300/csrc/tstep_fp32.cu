@@ -559,6 +559,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         const double rk = eos_md(md, tn[0], tn[1]);
                         if (k > k1c && !(rk < rho_prev)) unstable = true;
                         rho_prev = rk;
+                        md.rho[(size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k)] = rk;   // for the adjustment
                     }
                     // other tracers: FP32 transfers rounded once to int32, FP64 update
                     const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
@@ -749,7 +750,9 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
                     if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
             }
         __syncwarp();
-        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane);
+        // the step stored the FP64 densities of the column (ieos = 0)
+        const double *rho0 = md.ieos == 0 ? md.rho + (size_t)i + (size_t)NI * j : nullptr;
+        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane, rho0, NIJ);
         if (lane < L)
             for (int lev = k1c; lev <= maxk; ++lev) const_cast<double *>(wc)[(size_t)lev * lstride] = tv[lev * 32 + lane];
         if (lane == 0 && filled > 0) {
@@ -1433,7 +1436,6 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s)
 {
     (void)ts_buf;   // the FP32-flux state lives in its own group-planar buffers
-    (void)rho;
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
     if (!h->have_state || !h->have_vel) return GB_GO_ENOTREADY;
@@ -1450,6 +1452,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.buf[0] = D.plan_buf[0];
         md.buf[1] = D.plan_buf[1];
         md.ts_static = ts_static;
+        md.rho = rho;
         md.coef = D.coef; md.coefl = D.coefl; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
         md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
         md.ptab = D.ptab;
