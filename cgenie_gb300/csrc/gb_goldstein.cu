@@ -11,6 +11,8 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -43,6 +45,8 @@ struct gb_go_handle {
     double *stage = nullptr;
     double *inv_part = nullptr;
     int inv_blocks = 0;
+    double *inv_noalloc = nullptr;        // static scratch of gb_go_inventory_noalloc on this device
+    std::string inv_noalloc_err;
     Metrics m{};
     std::vector<int32_t> k1_host;
     bool state_ready = false, vel_ready = false;
@@ -295,6 +299,35 @@ static void free_handle(gb_go_handle *h)
     delete h;
 }
 
+// Scratch of gb_go_inventory_noalloc, a file-scope device array: for up to
+// kInvNoallocMaxL tracers, 64 (sum, compensation) pairs per tracer from the partial
+// kernel, then the per-tracer results.  Every entry is written before it is read, so
+// nothing has to start at zero.
+constexpr int kInvNoallocBlocks = 64;
+constexpr int kInvNoallocMaxL = 64;
+constexpr int kInvNoallocDoubles = 2 * kInvNoallocBlocks * kInvNoallocMaxL + kInvNoallocMaxL;
+static __device__ __align__(256) double g_inv_noalloc[kInvNoallocDoubles];
+
+// Device address of g_inv_noalloc, looked up once per device (at handle set-up; the first
+// lookup must happen outside stream capture).
+static cudaError_t inv_noalloc_scratch(int device, double **out)
+{
+    static std::mutex mu;
+    static std::map<int, double *> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(device);
+    if (it != cache.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    double *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void **)&p, g_inv_noalloc);
+    if (e != cudaSuccess) return e;
+    cache[device] = p;
+    *out = p;
+    return cudaSuccess;
+}
+
 extern "C" int gb_go_create(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid, int device,
                             gb_go_handle **out)
 {
@@ -328,6 +361,13 @@ extern "C" int gb_go_create(const gb_go_dims *dims, const gb_go_params *params, 
     std::vector<double> blob;
     build_metric_blob(dims, params, grid, blob);
     h->inv_blocks = 64;
+    {
+        const cudaError_t se = inv_noalloc_scratch(h->device, &h->inv_noalloc);
+        if (se != cudaSuccess) {
+            h->inv_noalloc = nullptr;
+            h->inv_noalloc_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(se);
+        }
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
         h->stream = h->own_stream;
@@ -555,6 +595,33 @@ extern "C" int gb_go_inventory(gb_go_handle *h, double *out)
     count_launches(2);
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpyAsync(out, h->stage, h->d.L * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_inventory_noalloc(gb_go_handle *h, double *out)
+{
+    if (!h || !out) return GB_GO_EINVAL;
+    if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "inventory before upload_state");
+    if (h->d.L > kInvNoallocMaxL)
+        return fail(h, GB_GO_ERANGE, "gb_go_inventory_noalloc takes at most 64 tracers (static scratch of 8256 doubles)");
+    if (!h->inv_noalloc) return fail(h, GB_GO_ECUDA, "gb_go_inventory_noalloc scratch unavailable: " + h->inv_noalloc_err);
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const double *src = h->ts_buf[h->cur];
+    if (h->steps_since_upload == 0) src = h->ts_static;
+    else if (h->precision == GB_GO_FP32FLUX) {
+        int r = fp32_member_fortran(&h->f32, h->ts_buf[h->cur], h->stream);
+        if (r) return fail(h, r, "fp32 export failed");
+    }
+    // the same kernels and partition as gb_go_inventory, on the static scratch
+    double *part = h->inv_noalloc;
+    double *res = part + 2 * (size_t)kInvNoallocBlocks * h->d.L;
+    dim3 grid(kInvNoallocBlocks, h->d.L);
+    k_inventory_partial<<<grid, 256, 0, h->stream>>>(src, h->d, h->m, part);
+    k_inventory_final<<<(h->d.L + 63) / 64, 64, 0, h->stream>>>(part, kInvNoallocBlocks, h->d.L, res);
+    count_launches(2);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(out, res, h->d.L * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
 }

@@ -94,6 +94,12 @@ MODULE gb_goldstein_c
        INTEGER(C_INT) :: gb_go_inventory
      END FUNCTION gb_go_inventory
 
+     FUNCTION gb_go_inventory_noalloc(handle, out) BIND(C, NAME='gb_go_inventory_noalloc')
+       IMPORT :: C_INT, C_PTR
+       TYPE(C_PTR), VALUE :: handle, out
+       INTEGER(C_INT) :: gb_go_inventory_noalloc
+     END FUNCTION gb_go_inventory_noalloc
+
      FUNCTION gb_go_errstr(code) BIND(C, NAME='gb_go_errstr')
        IMPORT :: C_INT, C_PTR
        INTEGER(C_INT), VALUE :: code

@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgb_goldstein.so")
 EXPORTED = [
     "gb_go_create", "gb_go_destroy", "gb_go_set_stream", "gb_go_upload_state", "gb_go_set_forcing",
     "gb_go_set_velocity", "gb_go_set_diag", "gb_go_tstepo", "gb_go_download", "gb_go_inventory",
+    "gb_go_inventory_noalloc",
     "gb_go_sync", "gb_go_errstr", "gb_go_last_error", "gb_go_kernel_launch_count",
     "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
     "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
@@ -68,6 +69,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_go_tstepo.argtypes = [vp, C.c_int32]
     L.gb_go_download.argtypes = [vp, dp, dp, dp, dp, ip, dp, ip]
     L.gb_go_inventory.argtypes = [vp, dp]
+    L.gb_go_inventory_noalloc.argtypes = [vp, dp]
     L.gb_go_sync.argtypes = [vp]
     L.gb_go_errstr.argtypes = [C.c_int]
     L.gb_go_errstr.restype = C.c_char_p
@@ -189,6 +191,12 @@ class Goldstein:
     def inventory(self) -> np.ndarray:
         out = np.zeros(self.m.maxl)
         self._check(self.lib.gb_go_inventory(self.h, dptr(out)), "gb_go_inventory")
+        return out
+
+    def inventory_noalloc(self) -> np.ndarray:
+        """The same inventory through gb_go_inventory_noalloc (static device scratch)."""
+        out = np.zeros(self.m.maxl)
+        self._check(self.lib.gb_go_inventory_noalloc(self.h, dptr(out)), "gb_go_inventory_noalloc")
         return out
 
 

@@ -156,6 +156,19 @@ int  gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *rho,
  * (Neumaier) summation.  `out` has maxl entries. */
 int  gb_go_inventory(gb_go_handle *h, double *out);
 
+/* gb_go_inventory without any device allocation: the same kernels and result, with their
+ * scratch in a static device array of the library (64 x 2 partial sums per tracer and the
+ * results, 8256 doubles).  No counterpart in the reference: it serves callers that must
+ * not allocate, e.g. inside a CUDA graph capture or under a fixed memory budget.
+ * - at most 64 tracers: a handle with more returns GB_GO_ERANGE;
+ * - the scratch address is looked up once per device when a handle is created
+ *   (cudaGetSymbolAddress), so create the first handle on a device before any stream
+ *   capture;
+ * - every scratch entry is written before it is read (nothing needs to start at zero);
+ * - the scratch is shared by all handles of a device: calls that overlap in time (other
+ *   threads, or handles on different streams) race and must be serialised by the caller. */
+int  gb_go_inventory_noalloc(gb_go_handle *h, double *out);
+
 /* Wait for all work queued on the handle's stream. */
 int  gb_go_sync(gb_go_handle *h);
 
