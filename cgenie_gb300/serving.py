@@ -120,6 +120,7 @@ class Server:
         total_cu = 0
         steps_run = 0
         busy_s = 0.0
+        max_active = 0
         while pending or waiting or active:
             now = (clock() - t0) * time_scale
             while pending and pending[0].arrival <= now:
@@ -139,6 +140,7 @@ class Server:
                 req.admitted = (clock() - t0) * time_scale
                 req.cell_updates = self._wet(m) * req.maxl * req.steps
                 active[mid] = req
+                max_active = max(max_active, len(active))
             if not active:
                 # idle until the next arrival
                 if pending:
@@ -169,9 +171,36 @@ class Server:
         wall = (clock() - t0) * time_scale
         lat = np.array([r.finished - r.arrival for r in done])
         return dict(
-            requests=len(done), wall_s=wall, busy_s=busy_s, batch_steps=steps_run,
+            requests=len(done), wall_s=wall, busy_s=busy_s, batch_steps=steps_run, max_active=max_active,
             cell_updates=total_cu, cell_updates_per_s=total_cu / wall if wall > 0 else 0.0,
             p50_latency_s=float(np.percentile(lat, 50)) if len(lat) else math.nan,
             p99_latency_s=float(np.percentile(lat, 99)) if len(lat) else math.nan,
             mean_latency_s=float(lat.mean()) if len(lat) else math.nan,
             done=done)
+
+
+def main(argv=None):
+    """Serve seeded Poisson arrivals and print one JSON line: p50/p99 run latency and
+    tracer cell-updates per second of wall time."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=50.0, help="arrivals per second")
+    ap.add_argument("--smin", type=int, default=200)
+    ap.add_argument("--smax", type=int, default=5000)
+    ap.add_argument("--chunk", type=int, default=25)
+    ap.add_argument("--budget-gb", type=float, default=0.0, help="HBM budget (0: 90%% of free memory)")
+    ap.add_argument("--seed", type=int, default=7)
+    a = ap.parse_args(argv)
+    reqs = poisson_requests(a.requests, rate=a.rate, seed=a.seed, smin=a.smin, smax=a.smax)
+    srv = Server(hbm_budget_bytes=int(a.budget_gb * 1e9), chunk=a.chunk)
+    st = srv.run(reqs)
+    srv.close()
+    st.pop("done")
+    st.update(dict(arrival_rate=a.rate, steps_range=[a.smin, a.smax], chunk=a.chunk))
+    print(json.dumps(st))
+
+
+if __name__ == "__main__":
+    main()
