@@ -8,6 +8,8 @@ Workloads (seeded synthetic members with the reference's grid formulas):
       the scale update)
   c2  single member 36x36x16, 17 tracers, isoneutral branch on, FP64 plain form
   c1  single member 36x36x16, 2 tracers, FP64 plain form
+  c5  single grid 360x180x32, 24 tracers (HBM stress test), FP64 plain form or, with
+      --precision fp32flux, the split-precision form
 
 A step is one tracer timestep (tstepo) of every member.  `value` is tracer
 cell-updates/s with the state resident in HBM (c3: the 256 states, 2 x 0.6 GB,
@@ -44,6 +46,7 @@ WORKLOADS = {
     "c1": dict(name="tstepo_fp64_36x36x16_L2", factory="config_c1"),
     "c2": dict(name="tstipo_diso_fp64_36x36x16_L17", factory="config_c2"),
     "c3": dict(name="ensemble256_fp32flux_18x18x16_36x36x16_36x36x32_L2-24", members=256, seed=3),
+    "c5": dict(name="stress_360x180x32_L24", factory="config_c5"),
 }
 
 
@@ -375,6 +378,7 @@ def main():
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--members", type=int, default=0, help="c3: members of the ensemble (default 256)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32flux"], help="single-grid workloads")
     ap.add_argument("--steps-before", type=int, default=0,
                     help="c3: steps taken before the warm-up (the members' convection develops over time)")
     args = ap.parse_args()
@@ -412,7 +416,9 @@ def main():
     # reads as "the handle's own stream"
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    g = new_member_run(m, device=local, stream=stream.cuda_stream)
+    from cgenie_gb300 import abi
+    prec = abi.GB_GO_FP32FLUX if args.precision == "fp32flux" else abi.GB_GO_FP64
+    g = new_member_run(m, device=local, stream=stream.cuda_stream, precision=prec)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     for _ in range(args.warmup):
@@ -483,24 +489,29 @@ def main():
     alg = algorithmic_bytes(m)
     avg_s = total_ms * 1e-3 / args.steps
     achieved = alg / avg_s / 1e9
-    traffic = profile_traffic("k_step_fp64", w["name"])
+    kname = "k_step_fp32" if args.precision == "fp32flux" else "k_step_fp64"
+    traffic = profile_traffic(kname, w["name"])
 
     if rank == 0:
         line = {
             "metric": "tracer cell-updates/s", "value": value, "unit": "tracer cell-updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 transfers, f64 state" if args.precision == "fp32flux" else "f64",
             "data": "synthetic (seeded member, reference grid formulas)",
             "config": {"workload": w["name"], "maxi": m.maxi, "maxj": m.maxj, "maxk": m.maxk, "maxl": m.maxl,
-                       "wet_cells": m.wet_cells, "diso": bool(m.cfg.diso), "precision": "fp64 plain",
-                       "l2": "flushed before every timed step (state 3.5 MB < L2)", "parallelism": f"replicas{world}"},
+                       "wet_cells": m.wet_cells, "diso": bool(m.cfg.diso),
+                       "precision": "fp32flux" if args.precision == "fp32flux" else "fp64 plain",
+                       "l2": "flushed before every timed step", "parallelism": f"replicas{world}"},
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "note": "per step: forcing + u H2D (pinned), step, rho D2H; L2 not flushed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_step_fp64", "algorithmic_bytes_per_launch": alg,
-                         "note": "plain FP64 form is FP64-issue bound on GB300, not HBM bound"},
+                         "kernel": kname, "algorithmic_bytes_per_launch": alg,
+                         "note": ("split-precision form on one grid: the batched kernels with one member"
+                                  if args.precision == "fp32flux" else
+                                  "the plain FP64 form is bound by the FP64 issue rate on GB300, not by HBM")},
             "gpu_launches": int(launches),
             "clocks": clocks,
         }

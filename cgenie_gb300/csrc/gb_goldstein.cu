@@ -476,7 +476,7 @@ extern "C" int gb_go_set_velocity(gb_go_handle *h, const double *u)
     const size_t nu = (size_t)3 * (h->d.maxi + 1) * (h->d.maxj + 1) * h->d.maxk;
     CUDA_TRY(h, cudaMemcpyAsync(h->u, u, nu * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (h->precision == GB_GO_FP32FLUX) {
-        int r = fp32_member_set_velocity(&h->f32, u, h->stream);
+        int r = fp32_member_set_velocity(&h->f32, u, h->u, h->m, h->stream);
         if (r) return fail(h, r, "fp32 set_velocity failed");
     }
     h->vel_ready = true;

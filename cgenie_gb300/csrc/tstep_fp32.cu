@@ -1105,6 +1105,64 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     }
 }
 
+// The transfer coefficients of fp32_build_static from device-resident velocities (the
+// velocity field of every ocean step in a coupled run): the same FP64 expressions in the
+// same order, with round-to-nearest intrinsics (no contraction), so the coefficients are
+// those the host builds.  One thread per interior cell.
+__global__ void k_build_coef(const double *__restrict__ u, Metrics m, Dims d, PhysParams p, float *coef, float *coefl)
+{
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
+    const size_t ncell = (size_t)maxi * maxj * maxk;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % maxi) + 1;
+        const int j = (int)((c / maxi) % maxj) + 1;
+        const int k = (int)(c / ((size_t)maxi * maxj)) + 1;
+        auto U = [&](int cc, int ii, int jj, int kk) {
+            return u[(size_t)cc + 3 * ((size_t)ii + (size_t)(maxi + 1) * ((size_t)jj + (size_t)(maxj + 1) * (size_t)(kk - 1)))];
+        };
+        auto K1 = [&](int ii, int jj) { return m.k1[ii + (size_t)NI * jj]; };
+        double cd[6] = {0, 0, 0, 0, 0, 0};
+        const int k1c = K1(i, j);
+        const int ie = (i == maxi) ? 1 : i + 1;
+        const int ke = K1(ie, j) > k1c ? K1(ie, j) : k1c;
+        if (k >= ke) {
+            const double u1 = U(0, i, j, k);
+            const double pec = __ddiv_rn(__dmul_rn(u1, p.dphi), p.diff1);
+            const double ups = __ddiv_rn(pec, __dadd_rn(2.0, fabs(pec)));
+            const double g = __dmul_rn(__dmul_rn(m.dt[k], m.ds[j]), m.dz[k]), a = __dmul_rn(u1, m.rc[j]);
+            const double dd = __dmul_rn(m.rc2[j], p.diff1);
+            cd[0] = __dmul_rn(g, __dsub_rn(__dmul_rn(__dmul_rn(a, __dsub_rn(1.0, ups)), 0.5), dd));
+            cd[1] = __dmul_rn(g, __dadd_rn(__dmul_rn(__dmul_rn(a, __dadd_rn(1.0, ups)), 0.5), dd));
+        }
+        const int kn = K1(i, j + 1) > k1c ? K1(i, j + 1) : k1c;
+        if (k >= kn) {
+            const double u2 = U(1, i, j, k);
+            const double pec = __ddiv_rn(__dmul_rn(u2, m.dsv[j < maxj - 1 ? j : maxj - 1]), p.diff1);
+            const double ups = __ddiv_rn(pec, __dadd_rn(2.0, fabs(pec)));
+            const double g = __dmul_rn(__dmul_rn(m.dt[k], p.dphi), m.dz[k]), a = __dmul_rn(m.cv[j], u2);
+            const double dd = __dmul_rn(m.cv2[j], p.diff1);
+            cd[2] = __dmul_rn(g, __dsub_rn(__dmul_rn(__dmul_rn(a, __dsub_rn(1.0, ups)), 0.5), dd));
+            cd[3] = __dmul_rn(g, __dadd_rn(__dmul_rn(__dmul_rn(a, __dadd_rn(1.0, ups)), 0.5), dd));
+        }
+        if (k >= k1c && k < maxk) {
+            const double u3 = U(2, i, j, k);
+            const double pec = __ddiv_rn(__dmul_rn(u3, m.dza[k]), p.diff2);
+            const double ups = __ddiv_rn(pec, __dadd_rn(2.0, fabs(pec)));
+            const double g = __dmul_rn(__dmul_rn(m.dt[k], p.dphi), m.ds[j]);
+            const double dd = __dmul_rn(m.rdza[k], p.diff2);
+            cd[4] = __dmul_rn(g, __dsub_rn(__dmul_rn(__dmul_rn(u3, __dsub_rn(1.0, ups)), 0.5), dd));
+            cd[5] = __dmul_rn(g, __dadd_rn(__dmul_rn(__dmul_rn(u3, __dadd_rn(1.0, ups)), 0.5), dd));
+        }
+        float *co = coef + 8 * c, *cl = coefl + 8 * c;
+        for (int n = 0; n < 6; ++n) {
+            const float h = __double2float_rn(cd[n]);
+            co[n] = h;
+            cl[n] = __double2float_rn(__dsub_rn(cd[n], (double)h));
+        }
+        co[6] = co[7] = cl[6] = cl[7] = 0.0f;
+    }
+}
+
 void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top,
                std::vector<float> &gtop)
 {
@@ -1413,9 +1471,20 @@ int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s)
     return cuda_ok(cudaStreamSynchronize(s));
 }
 
-int fp32_member_set_velocity(Fp32Member *f, const double *u_host, cudaStream_t s)
+int fp32_member_set_velocity(Fp32Member *f, const double *u_host, const double *u_dev, const Metrics &m,
+                              cudaStream_t s)
 {
     Fp32Host *h = host_of(f);
+    if (h->have_vel && u_dev) {
+        // later velocity fields: coefficients on the device; the fixed-point scales follow
+        // through the rescaling of the steps
+        Fp32Data &D = h->data;
+        const size_t ncell = (size_t)h->d.maxi * h->d.maxj * h->d.maxk;
+        const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 8192);
+        k_build_coef<<<std::max(1, blocks), 256, 0, s>>>(u_dev, m, h->d, h->p, D.coef, D.coefl);
+        count_launches(1);
+        return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    }
     Fp32Static st;
     fp32_build_static(h->d, h->p, h->blob, h->k1.data(), u_host, st);
     Fp32Data &D = h->data;

@@ -185,3 +185,34 @@ def test_ensemble_budget_and_removal(gpu_lib):
     ens.remove(b)
     ens.remove(c)
     ens.close()
+
+
+def test_fp32_velocity_updates_on_device(gpu_lib, oracle):
+    """A velocity field set after the first is turned into coefficients on the device:
+    the same field gives the run bit for bit, a new field stays within the bars against
+    the FP64 oracle run on that field."""
+    from cgenie_gb300.goldstein import new_member_run
+    m = grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=16, maxl=9, seed=91, tracer_kind="bgc"))
+    g1 = new_member_run(m, precision=abi.GB_GO_FP32FLUX)
+    g2 = new_member_run(m, precision=abi.GB_GO_FP32FLUX)
+    g2.set_velocity()                    # second field: device path, same values
+    g1.tstepo(20)
+    g2.tstepo(20)
+    a, b = g1.download(), g2.download()
+    assert np.array_equal(a["ts"], b["ts"])
+    u2 = m.u * 0.7
+    g2.set_velocity(u2)
+    g2.tstepo(30)
+    out = g2.download()
+    g1.close()
+    g2.close()
+    import dataclasses
+    m2 = dataclasses.replace(m)
+    m2.u = u2
+    ref = oracle.OracleState(m)
+    ref.step(20)
+    ref.u = np.ascontiguousarray(u2)
+    ref.step(30)
+    err = tracer_errors(m, out["ts"], ref.ts)
+    assert np.all(err[:2] <= 1e-9), err
+    assert np.all(err <= TOL_REL), err
