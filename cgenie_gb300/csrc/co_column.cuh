@@ -136,32 +136,6 @@ __device__ int co_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const
     return filled;
 }
 
-// a / b rounded to nearest even, from y ~ 1/b (b > 0 shared by many quotients).
-// Markstein's refinement (P. Markstein, IA-64 and Elementary Functions, 2000):
-// q = a*y, r = a - b*q (exact by FMA), q1 = q + r*y.  q1 is returned only when the exact
-// residual a - b*q1 proves |a/b - q1| < ulp(q1)/2 (q1 normal and not a power of two, so
-// the two neighbours are ulp(q1) away and q1 is the nearest double); otherwise the IEEE
-// division is taken.  The result is always the correctly rounded quotient.
-__device__ __forceinline__ double div_rn_recip(double a, double b, double y)
-{
-    const double q = a * y;
-    const double r = fma(-b, q, a);
-    const double q1 = fma(r, y, q);
-    const double r1 = fma(-b, q1, a);   // a - b*q1, exact when q1 is within an ulp of a/b
-    const long long bits = __double_as_longlong(q1);
-    const int e = (int)((bits >> 52) & 0x7ff);
-    const long long bm = __double_as_longlong(b) & 0x7fffffffffffffffLL;
-    const int eb = (int)(bm >> 52);
-    // |b| * 2^(E-53), E the unbiased exponent of q1: b's exponent field moved by e - 1076
-    const int ebound = eb + e - 1076;
-    if (e > 54 && e < 2046 && (bits & 0xfffffffffffffLL) != 0 && eb > 0 && ebound > 0 && ebound < 2047) {
-        const long long bound = bm + ((long long)(e - 1076) << 52);
-        // non-negative doubles order as their bit patterns
-        if ((__double_as_longlong(r1) & 0x7fffffffffffffffLL) < bound) return q1;
-    }
-    return __ddiv_rn(a, b);
-}
-
 // Integer key that orders doubles as < does (no NaN; -0 and +0 both map to 0).
 __device__ __forceinline__ long long order_key(double x)
 {
@@ -230,17 +204,14 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             }
             const int km = kk[m];
             const double d0 = dzm[km];
-            double dtot = d0, y = 0.0;
-            if (lane == 0) {
+            double dtot = d0;
+            if (lane == 0)
                 for (int ni = 1; ni <= m - n; ++ni) dtot = __dadd_rn(dtot, dzm[kk[m - ni]]);
-                y = __drcp_rn(dtot);
-            }
             dtot = __shfl_sync(0xffffffffu, dtot, 0);
-            y = __shfl_sync(0xffffffffu, y, 0);
             if (lane < L) {
                 double s = __dmul_rn(T(lane, km), d0);
                 for (int ni = 1; ni <= m - n; ++ni) s = __dadd_rn(s, __dmul_rn(T(lane, kk[m - ni]), dzm[kk[m - ni]]));
-                tv[km * 32 + lane] = div_rn_recip(s, dtot, y);
+                tv[km * 32 + lane] = __ddiv_rn(s, dtot);
             }
             __syncwarp();
             if (lane == 0) {
@@ -255,20 +226,20 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             __syncwarp();
         }
     }
+    // fill the merged levels (the densities of filled levels, which co also recomputes,
+    // are not read again: the step recomputes every density from the state)
     int filled = 0;
     m = maxk - 1;
     for (int n = maxk - 1; n >= k1; --n) {
         if (n > kk[m]) {
             const int src = kk[m + 1];
             if (lane < L) tv[n * 32 + lane] = T(lane, src);
-            __syncwarp();
-            if (lane == 0) rho[n] = order_key(eos_rn(ec, T(0, n), T(1, n), zw[kk[n - 1]]));
-            __syncwarp();
             filled = filled + 1;
         } else {
             m = m - 1;
         }
     }
+    __syncwarp();
     return filled;
 }
 
