@@ -320,7 +320,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.buf[0] = m->buf0; md.buf[1] = m->buf1;
     md.ts_static = m->ts_static; md.coef = m->coef; md.coefl = m->coefl; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
     md.scale = m->scale; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
-    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab; md.rho = m->rho;
+    md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission

@@ -93,8 +93,6 @@ struct MemberDesc {
     const double *mj;           // FP64 j metrics, 3 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), dt*dphi*ds(j)
     double *cost;
     int32_t *icosd;
-    double *rho;                // (maxi+2, maxj+2, maxk+1): the step writes the FP64 density of every
-                                // wet interior cell (read by the convective adjustment)
     unsigned long long *diag;   // two slots {dmax bits, limps}; step n uses slot n & 1 and clears
                                 // slot (n+1) & 1 for the next step
     unsigned int *status;       // bit0 non-finite, bit1 transfer range exceeded, bit2 column list full

@@ -123,14 +123,6 @@ __device__ __forceinline__ dflt df_split(double x)
     return {h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
 }
 
-// density of the equation of state with the ieos = 0 terms, the arithmetic of eos_rn
-template <class MD>
-__device__ __forceinline__ double eos_md(const MD &md, double t, double s)
-{
-    const double tt = __dmul_rn(t, t);
-    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(md.ec[0], t), __dmul_rn(md.ec[1], s)), __dmul_rn(md.ec[2], tt)),
-                     __dmul_rn(md.ec[3], __dmul_rn(tt, t)));
-}
 
 // column view used by the exact co: the group-planar FP64 state at and above k1,
 // the uploaded (Fortran-layout) state below
@@ -312,7 +304,9 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     }
         }
 
-        double rho_prev = 0.0;
+        float rho_prev = 0.0f, mag_prev = 0.0f;
+        float ecf[4];
+        for (int n = 0; n < 4; ++n) ecf[n] = (float)md.ec[n];
         bool unstable = false;
         float gmax = 0.0f;
         unsigned hmax = 0u;
@@ -556,10 +550,17 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         // The column needs the convective adjustment iff two consecutive wet levels
                         // are not strictly stably stratified: the test of co (goldstein.f90:2715-2716)
                         // on the same FP64 densities (with ieos != 0 every column is adjusted).
-                        const double rk = eos_md(md, tn[0], tn[1]);
-                        if (k > k1c && !(rk < rho_prev)) unstable = true;
-                        rho_prev = rk;
-                        md.rho[(size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k)] = rk;   // for the adjustment
+                        // FP32 density prescreen: a column joins the adjustment unless its densities
+                        // decrease upwards by clearly more than their FP32 error at every level
+                        // (the test of co, goldstein.f90:2715-2716, is then certainly passed); levels
+                        // that co mixed are equal and always join
+                        const float tf = d2f_scaled(tn[0], 0), sf = d2f_scaled(tn[1], 0);
+                        const float e0 = ecf[0] * tf, e1 = ecf[1] * sf, e2 = ecf[2] * (tf * tf), e3 = ecf[3] * (tf * tf * tf);
+                        const float rf = ((e0 + e1) + e2) + e3;
+                        const float mag = fabsf(e0) + fabsf(e1) + fabsf(e2) + fabsf(e3);
+                        if (k > k1c && !(rho_prev - rf > 2.0e-6f * (mag + mag_prev) + 1.0e-30f)) unstable = true;
+                        rho_prev = rf;
+                        mag_prev = mag;
                     }
                     // other tracers: FP32 transfers rounded once to int32, FP64 update
                     const float Ae = AeX.hi, Be = BeX.hi, An = AnX.hi, Bn = BnX.hi, Aw = AwX.hi, Bw = BwX.hi;
@@ -751,8 +752,7 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
             }
         __syncwarp();
         // the step stored the FP64 densities of the column (ieos = 0)
-        const double *rho0 = md.ieos == 0 ? md.rho + (size_t)i + (size_t)NI * j : nullptr;
-        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane, rho0, NIJ);
+        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane, nullptr, NIJ);
         if (lane < L)
             for (int lev = k1c; lev <= maxk; ++lev) const_cast<double *>(wc)[(size_t)lev * lstride] = tv[lev * 32 + lane];
         if (lane == 0 && filled > 0) {
@@ -1505,6 +1505,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s)
 {
     (void)ts_buf;   // the FP32-flux state lives in its own group-planar buffers
+    (void)rho;      // rho is computed on export
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
     if (!h->have_state || !h->have_vel) return GB_GO_ENOTREADY;
@@ -1521,7 +1522,6 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.buf[0] = D.plan_buf[0];
         md.buf[1] = D.plan_buf[1];
         md.ts_static = ts_static;
-        md.rho = rho;
         md.coef = D.coef; md.coefl = D.coefl; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
         md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
         md.ptab = D.ptab;
