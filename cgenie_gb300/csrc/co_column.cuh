@@ -136,6 +136,71 @@ __device__ int co_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const
     return filled;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float densities for the order decisions of the adjustment (ieos = 0).
+// An FP32 pair (hi, lo) carries ~47 bits, so the density difference of two levels is
+// known to ~1e-13 of the size of the terms; only closer pairs need the FP64 density.
+
+struct CoDf {
+    float hi, lo;
+};
+
+// x as an FP32 pair by integer operations: hi = x with its mantissa truncated to 24 bits,
+// lo = the remaining 29 bits rounded to FP32, so |x - hi - lo| <= 2^-47 |x|.  A nonzero |x|
+// outside [2^-74, 2^60] gives a NaN pair: every decision that uses it takes the FP64 path.
+__device__ __forceinline__ CoDf co_split(double x)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned a = hw & 0x7fffffffu, sgn = hw & 0x80000000u;
+    const int E = (int)(a >> 20);
+    if ((a | lw) == 0u) return {0.0f, 0.0f};
+    if (E < 949 || E > 1082) return {__int_as_float(0x7fc00000), 0.0f};
+    const float hi = __uint_as_float(sgn | ((unsigned)(E - 896) << 23) | ((a & 0xfffffu) << 3) | (lw >> 29));
+    const float lo = __fmul_rn(__uint2float_rn(lw & 0x1fffffffu), __uint_as_float((unsigned)(E - 948) << 23));
+    return {hi, __uint_as_float(__float_as_uint(lo) | sgn)};
+}
+
+// a + b, |a| >= |b| (or a = 0): exact pair
+__device__ __forceinline__ CoDf co_fast2sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// pair sum (Knuth's TwoSum of the hi parts, lo parts added): error <= ~3u^2 (|a| + |b|),
+// u = 2^-24
+__device__ __forceinline__ CoDf co_dfadd(CoDf a, CoDf b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    return co_fast2sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+// pair product (exact FMA product of the hi parts, cross terms; lo*lo dropped):
+// relative error <= ~7u^2
+__device__ __forceinline__ CoDf co_dfmul(CoDf a, CoDf b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return co_fast2sum(p, e);
+}
+
+// eos (goldstein.f90:3048-3061, ieos = 0) as a pair, and M = the sum of the magnitudes of
+// its four terms.  Split errors (2^-47 per input, three-fold in t^3), the products and the
+// three sums keep |result - eos_rn| below ~45u^2 M < 2^-42 M.
+__device__ __forceinline__ CoDf eos_df(const CoDf ecd[4], double t, double s, float &mag)
+{
+    const CoDf td = co_split(t), sd = co_split(s);
+    const CoDf tt = co_dfmul(td, td);
+    const CoDf ttt = co_dfmul(tt, td);
+    const CoDf p0 = co_dfmul(ecd[0], td), p1 = co_dfmul(ecd[1], sd);
+    const CoDf p2 = co_dfmul(ecd[2], tt), p3 = co_dfmul(ecd[3], ttt);
+    mag = __fadd_rn(__fadd_rn(fabsf(p0.hi), fabsf(p1.hi)), __fadd_rn(fabsf(p2.hi), fabsf(p3.hi)));
+    return co_dfadd(co_dfadd(co_dfadd(p0, p1), p2), p3);
+}
+
 // Integer key that orders doubles as < does (no NaN; -0 and +0 both map to 0).
 __device__ __forceinline__ long long order_key(double x)
 {
@@ -149,26 +214,46 @@ __device__ __forceinline__ long long order_key(double x)
 struct CoWarpState {
     int kk[kMaxK + 2];
     double dzm[kMaxK + 1];
-    long long rho[kMaxK + 1];
+    long long rho[kMaxK + 1];   // exact keys; with ieos = 0 computed when first needed (kNoKey before)
+    float2 rd[kMaxK + 1];       // ieos = 0: double-float density of the level
+    float rm[kMaxK + 1];        // ieos = 0: the magnitude M of its terms (error scale)
 };
+
+constexpr long long kNoKey = (long long)0x8000000000000000ULL;
 
 // co_rn with one warp per column: the tracers of the column are in shared memory,
 // tv[lev * 32 + l] for the wet levels, and lane l mixes and fills tracer l.  The levels
-// to merge (kk, dzm, rho in cs) are kept by lane 0 (densities of the first pass one lane
-// per level); every value is the one co_rn computes.  Returns the number of filled levels
-// (in every lane).
-// rho0: the column's densities eos(T, S) of the wet levels (rho0[lev * rstride]) when
-// given (ieos = 0), else computed here.
+// to merge (kk, dzm, densities in cs) are kept by lane 0; every lane runs the same
+// decisions from shared memory.  Every value and decision is the one co_rn makes.  Returns
+// the number of filled levels (in every lane).
+// With ieos = 0 a density depends on (T, S) only, and a decision rho(a) < rho(b) is taken
+// from the double-float densities when their difference exceeds 2^-40 (M_a + M_b) (more
+// than 4x their error bound); otherwise (and for bit-equal T and S, which give equal
+// densities) from the exact FP64 densities, computed once per level value.  With
+// ieos != 0 the FP64 densities are recomputed as co does.
 __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, int maxk, int L, int k1,
-                              const double *dz, const double *zro, const double *zw, int lane, const double *rho0,
-                              size_t rstride)
+                              const double *dz, const double *zro, const double *zw, int lane)
 {
     int *kk = cs->kk;
     double *dzm = cs->dzm;
     long long *rho = cs->rho;
+    float2 *rd = cs->rd;
+    float *rm = cs->rm;
+    const bool lazy = ec.ieos == 0;
     auto T = [&](int l, int lev) { return tv[lev * 32 + l]; };
+    CoDf ecd[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) ecd[n] = co_split(ec.ec[n]);
+    auto set_df = [&](int lev) {
+        float mg;
+        const CoDf r = eos_df(ecd, T(0, lev), T(1, lev), mg);
+        rd[lev] = make_float2(r.hi, r.lo);
+        rm[lev] = mg;
+        rho[lev] = kNoKey;
+    };
     for (int lev = k1 + lane; lev <= maxk; lev += 32) {
-        rho[lev] = order_key(rho0 ? rho0[(size_t)lev * rstride] : eos_rn(ec, T(0, lev), T(1, lev), zro[lev]));
+        if (lazy) set_df(lev);
+        else rho[lev] = order_key(eos_rn(ec, T(0, lev), T(1, lev), zro[lev]));
         kk[lev] = lev;
         dzm[lev] = dz[lev];
     }
@@ -178,7 +263,7 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
     }
     __syncwarp();
     auto refresh = [&](int x, int y) {
-        if (ec.ieos != 0) {
+        if (!lazy) {
             if (lane == 0) {
                 rho[kk[x]] = order_key(eos_rn(ec, T(0, kk[x]), T(1, kk[x]), zw[kk[y]]));
                 rho[kk[y]] = order_key(eos_rn(ec, T(0, kk[y]), T(1, kk[y]), zw[kk[y]]));
@@ -186,11 +271,30 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             __syncwarp();
         }
     };
+    // rho(a) < rho(b) for wet levels a, b (uniform over the warp)
+    auto lt = [&](int a, int b) -> bool {
+        if (lazy) {
+            const float2 ra = rd[a], rb = rd[b];
+            const float d = __fadd_rn(__fsub_rn(ra.x, rb.x), __fsub_rn(ra.y, rb.y));
+            const float tol = __fmul_rn(0x1p-40f, __fadd_rn(rm[a], rm[b]));
+            if (d < -tol) return true;
+            if (d > tol) return false;
+            if (__double_as_longlong(T(0, a)) == __double_as_longlong(T(0, b)) &&
+                __double_as_longlong(T(1, a)) == __double_as_longlong(T(1, b)))
+                return false;
+            if (lane == 0) {
+                if (rho[a] == kNoKey) rho[a] = order_key(eos_rn(ec, T(0, a), T(1, a), zro[a]));
+                if (rho[b] == kNoKey) rho[b] = order_key(eos_rn(ec, T(0, b), T(1, b), zro[b]));
+            }
+            __syncwarp();
+        }
+        return rho[a] < rho[b];
+    };
     // m, n, lastmix follow from the shared arrays, so they are the same in every lane
     int m = maxk, lastmix = 0;
     while (kk[m - 1] > 0 || (lastmix != 0 && kk[m] != maxk)) {
         refresh(m, m - 1);
-        if (rho[kk[m]] < rho[kk[m - 1]] || kk[m - 1] == 0) {
+        if (kk[m - 1] == 0 || lt(kk[m], kk[m - 1])) {
             if (lastmix == 0 || kk[m] == maxk) m = m - 1;
             else m = m + 1;
             lastmix = 0;
@@ -198,7 +302,7 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             lastmix = 1;
             int n = m - 1;
             refresh(n, n - 1);
-            while (kk[n - 1] > 0 && rho[kk[n]] >= rho[kk[n - 1]]) {
+            while (kk[n - 1] > 0 && !lt(kk[n], kk[n - 1])) {
                 n = n - 1;
                 refresh(n, n - 1);
             }
@@ -216,7 +320,8 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
             __syncwarp();
             if (lane == 0) {
                 dzm[km] = dtot;
-                rho[km] = order_key(eos_rn(ec, T(0, km), T(1, km), zw[kk[m - 1]]));
+                if (lazy) set_df(km);
+                else rho[km] = order_key(eos_rn(ec, T(0, km), T(1, km), zw[kk[m - 1]]));
                 int ni = m - 1;
                 while (kk[ni + 1] > 0) {
                     kk[ni] = kk[ni - m + n];
@@ -241,6 +346,187 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
     }
     __syncwarp();
     return filled;
+}
+
+
+// ---------------------------------------------------------------------------
+// Warp-parallel adjustment of one column with maxk <= 32 and ieos = 0.
+//
+// co's working list kk (position -> level, the sentinel 0 below the lowest active
+// position) is held one position per lane (position p = lane + 1), each position
+// carrying the record of its level: thickness dzm, T, S, double-float density and the
+// exact FP64 key once computed.  A round evaluates every pair (p, p-1) at once
+// (ballot), so co's walk down a stable stretch (goldstein.f90:2715-2719), and the scan
+// for the bottom of an unstable stretch (2727-2731), each take one round; a merge
+// (2732-2746) shifts the records below it with one shuffle.  Decisions, merge order and
+// arithmetic are co's; the fill (2748-2765) is computed from the final list.
+
+struct CoRec {
+    int kk;            // level at this position
+    double dzm, t, s;  // thickness, T and S of that level
+    float rdh, rdl, rm;
+    long long key;     // exact order key of its FP64 density, kNoKey until needed
+};
+
+__device__ __forceinline__ CoRec co_rec_up(const CoRec &r, int d)
+{
+    const unsigned F = 0xffffffffu;
+    CoRec o;
+    o.kk = __shfl_up_sync(F, r.kk, d);
+    o.dzm = __shfl_up_sync(F, r.dzm, d);
+    o.t = __shfl_up_sync(F, r.t, d);
+    o.s = __shfl_up_sync(F, r.s, d);
+    o.rdh = __shfl_up_sync(F, r.rdh, d);
+    o.rdl = __shfl_up_sync(F, r.rdl, d);
+    o.rm = __shfl_up_sync(F, r.rm, d);
+    o.key = __shfl_up_sync(F, r.key, d);
+    return o;
+}
+
+// bits of positions lo..hi (position p = bit p-1)
+__device__ __forceinline__ unsigned co_bits(int lo, int hi)
+{
+    if (hi < lo) return 0u;
+    const unsigned up = hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u);
+    return up & ~((1u << (lo - 1)) - 1u);
+}
+
+// tv: shared memory, tv[lev * 32 + l]; ts0: T of the column at level 0 (S follows), level
+// stride s0; wc (lanes < L): this lane's tracer at level 0, level stride lstride.  Loads
+// the column, adjusts it, writes back the levels that changed; returns the number of
+// filled levels.
+__device__ inline int co_warp32(double *tv, const EosCoef &ec, int maxk, int L, int k1, const double *dz,
+                                int lane, const double *ts0, size_t s0, double *wc, size_t lstride)
+{
+    const unsigned F = 0xffffffffu;
+    const int p = lane + 1;
+    CoDf ecd[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) ecd[n] = co_split(ec.ec[n]);
+    CoRec rec;
+    rec.kk = p;
+    rec.dzm = 0.0;
+    rec.t = 0.0;
+    rec.s = 0.0;
+    rec.rdh = rec.rdl = rec.rm = 0.0f;
+    rec.key = kNoKey;
+    if (p >= k1 && p <= maxk) {
+        const double2 v = *reinterpret_cast<const double2 *>(ts0 + (size_t)p * s0);
+        rec.t = v.x;
+        rec.s = v.y;
+        rec.dzm = dz[p];
+        float mg;
+        const CoDf r = eos_df(ecd, v.x, v.y, mg);
+        rec.rdh = r.hi;
+        rec.rdl = r.lo;
+        rec.rm = mg;
+    }
+    int sp = k1 - 1;   // sentinel position
+    // bit p-1 set iff rho(kk[p]) < rho(kk[p-1]) or p-1 is the sentinel, for p in [sp+2, lim];
+    // positions outside that range read as stable
+    auto stable_mask = [&](int lim) -> unsigned {
+        const float bh = __shfl_up_sync(F, rec.rdh, 1), bl = __shfl_up_sync(F, rec.rdl, 1);
+        const float bm = __shfl_up_sync(F, rec.rm, 1);
+        int st = 1;
+        if (p >= sp + 2 && p <= lim) {
+            const float d = __fadd_rn(__fsub_rn(rec.rdh, bh), __fsub_rn(rec.rdl, bl));
+            const float tol = __fmul_rn(0x1p-40f, __fadd_rn(rec.rm, bm));
+            st = d < -tol ? 1 : (d > tol ? 0 : 2);
+        }
+        if (__any_sync(F, st == 2)) {
+            const double bt = __shfl_up_sync(F, rec.t, 1), bs = __shfl_up_sync(F, rec.s, 1);
+            // equal T and S: equal densities, not stable
+            if (st == 2 && __double_as_longlong(rec.t) == __double_as_longlong(bt) &&
+                __double_as_longlong(rec.s) == __double_as_longlong(bs))
+                st = 0;
+            const int above = __shfl_down_sync(F, st, 1);
+            if ((st == 2 || (lane < 31 && above == 2)) && rec.key == kNoKey)
+                rec.key = order_key(eos_rn(ec, rec.t, rec.s, 0.0));
+            const long long bk = __shfl_up_sync(F, rec.key, 1);
+            if (st == 2) st = rec.key < bk ? 1 : 0;
+        }
+        return __ballot_sync(F, st == 1);
+    };
+    unsigned stab = stable_mask(maxk);
+    // no unstable pair: co changes nothing
+    if ((~stab & co_bits(k1 + 1, maxk)) == 0u) return 0;
+    if (lane < L)
+        for (int lev = k1; lev <= maxk; lev += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (lev + u <= maxk) v[u] = wc[(size_t)(lev + u) * lstride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
+        }
+    __syncwarp();
+    unsigned modified = 0u;
+    int m = maxk, lastmix = 0;
+    bool fresh = true;   // stab holds the pairs of the current list up to m
+    while (m > sp + 1 || (lastmix != 0 && m != maxk)) {
+        if (!fresh) stab = stable_mask(m);
+        fresh = false;
+        if (lastmix == 0) {
+            // walk down the stable pairs to the highest unstable one
+            const unsigned un = ~stab & co_bits(sp + 2, m);
+            if (un == 0u) break;
+            m = 32 - __clz(un);
+        } else if ((stab >> (m - 1)) & 1u) {
+            m = (m == maxk) ? m - 1 : m + 1;
+            lastmix = 0;
+            continue;
+        }
+        // merge positions n..m: n = the highest stable position below m (sp+1 always is)
+        const int n = 32 - __clz(stab & co_bits(sp + 1, m - 1));
+        const int d = m - n, lm = m - 1;
+        const int km = __shfl_sync(F, rec.kk, lm);
+        const double d0 = __shfl_sync(F, rec.dzm, lm);
+        double dtot = d0, acc = 0.0;
+        if (lane < L) acc = __dmul_rn(tv[km * 32 + lane], d0);
+        for (int ni = 1; ni <= d; ++ni) {
+            const int lv = __shfl_sync(F, rec.kk, lm - ni);
+            const double dzv = __shfl_sync(F, rec.dzm, lm - ni);
+            dtot = __dadd_rn(dtot, dzv);
+            if (lane < L) acc = __dadd_rn(acc, __dmul_rn(tv[lv * 32 + lane], dzv));
+        }
+        if (lane < L) tv[km * 32 + lane] = __ddiv_rn(acc, dtot);
+        __syncwarp();
+        modified |= 1u << (km - 1);
+        if (lane == lm) {
+            rec.dzm = dtot;
+            rec.t = tv[km * 32];
+            rec.s = tv[km * 32 + 1];
+            float mg;
+            const CoDf r = eos_df(ecd, rec.t, rec.s, mg);
+            rec.rdh = r.hi;
+            rec.rdl = r.lo;
+            rec.rm = mg;
+            rec.key = kNoKey;
+        }
+        // positions sp+d .. m-1 take the records d below (sp+d becomes the sentinel)
+        const CoRec sh = co_rec_up(rec, d);
+        if (p >= sp + d && p <= m - 1) rec = sh;
+        sp += d;
+        lastmix = 1;
+    }
+    // fill: every level of [k1, maxk-1] no longer in the list takes the values of the
+    // lowest listed level above it
+    const unsigned act = __reduce_or_sync(F, (p >= sp + 1 && p <= maxk) ? (1u << (rec.kk - 1)) : 0u);
+    const unsigned fillm = ~act & co_bits(k1, maxk - 1);
+    for (unsigned f = fillm; f; f &= f - 1u) {
+        const int lev = __ffs(f);
+        const int src = __ffs(act & ~((1u << lev) - 1u));
+        if (lane < L) tv[lev * 32 + lane] = tv[src * 32 + lane];
+    }
+    modified |= fillm;
+    __syncwarp();
+    if (lane < L)
+        for (unsigned f = modified; f; f &= f - 1u) {
+            const int lev = __ffs(f);
+            wc[(size_t)lev * lstride] = tv[lev * 32 + lane];
+        }
+    return __popc(fillm);
 }
 
 }  // namespace gbgo

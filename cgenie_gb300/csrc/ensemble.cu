@@ -80,6 +80,7 @@ struct gb_ens {
     cudaEvent_t fork = nullptr, join = nullptr;
     int max_slots = 1;
     bool any_iso = false;               // some member has the isoneutral branch
+    bool co_general = false;            // some member needs the serial adjustment
     int kmax = 1;                       // largest maxk of the members
     int2 *colist = nullptr;             // columns listed for the exact convective adjustment
     int *cocount = nullptr;             // two counters, by step parity
@@ -373,7 +374,7 @@ static int rebuild(gb_ens *e)
     // together so the ring columns one patch reads are in L2 from its neighbours
     std::vector<std::pair<double, Member *>> order;
     int max_slots = 1;
-    bool any_iso = false;
+    bool any_iso = false, co_general = false;
     int kmax = 1;
     int slot = 0;
     for (auto &kv : e->members) {
@@ -390,6 +391,7 @@ static int rebuild(gb_ens *e)
         order.push_back({c, m});
         max_slots = std::max(max_slots, m->max_slots);
         any_iso = any_iso || m->desc.diso;
+        co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->d.maxk);
         kmax = std::max(kmax, m->d.maxk);
         ++slot;
     }
@@ -426,6 +428,7 @@ static int rebuild(gb_ens *e)
     }
     e->max_slots = max_slots;
     e->any_iso = any_iso;
+    e->co_general = co_general;
     e->kmax = kmax;
     e->dirty = false;
     if (e->graph) {
@@ -449,6 +452,7 @@ static Fp32Batch batch_of(gb_ens *e)
     b.cocount = e->cocount;
     b.cocap = e->cocap;
     b.iso = e->any_iso;
+    b.co_general = e->co_general;
     return b;
 }
 

@@ -205,12 +205,15 @@ struct Fp32Batch {
     int *cocount = nullptr;
     int cocap = 0;
     bool iso = false;
+    bool co_general = false;   // some member has iconv = 1, ieos != 0 or maxk > 32
 };
 // s2/fork/join: a second stream and two events to run the two item kinds side by side
 // (s2 null: one stream).
 int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStream_t s, cudaStream_t s2,
                 cudaEvent_t fork, cudaEvent_t join);
 int fp32_launches_per_step(const Fp32Batch &b);   // kernels fp32_launch starts
+// columns the warp-parallel adjustment takes (the others run co's serial form)
+__host__ __device__ inline bool fp32_co_fast(int iconv, int ieos, int maxk) { return iconv == 0 && ieos == 0 && maxk <= 32; }
 int fp32_smem_bytes(int max_slots);
 // current state (group-planar) -> Fortran layout with halo columns, and rho
 int fp32_export(const MemberDesc &md, const double *planar, double *cur, double *rho, cudaStream_t s);

@@ -80,4 +80,21 @@ __host__ __device__ inline size_t rho_index(const Dims &d, int i, int j, int k)
 int launch_step_fp64(const StepArgs &a, void *stream);
 void step_fp64_tile(int maxk, int *tile_i, int *tile_j);
 
+#ifdef __CUDACC__
+// c + n computed as n additions of 1.0 in round-to-nearest (co adds 1 to cost(i,j) per
+// filled level, goldstein.f90:2759).  When c is integer-valued with |c| < 2^52 every partial
+// sum is exact, so one addition gives the same double; otherwise they run one by one.
+__device__ __forceinline__ double add_count_rn(double c, int n)
+{
+    if (n <= 0) return c;
+    const long long b = __double_as_longlong(c);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    const long long frac = b & 0xfffffffffffffLL;
+    const bool integral = ((unsigned long long)b << 1) == 0ull || (e >= 0 && e < 52 && (frac & ((1LL << (52 - e)) - 1)) == 0);
+    if (integral) return __dadd_rn(c, (double)n);
+    for (int f = 0; f < n; ++f) c = __dadd_rn(c, 1.0);
+    return c;
+}
+#endif
+
 }  // namespace gbgo

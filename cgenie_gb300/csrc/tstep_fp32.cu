@@ -675,6 +675,7 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
 // (member, patch table offset); each warp takes interior columns of the patch in turn and
 // adjusts a column with one lane per tracer (co_warp), the column staged in shared memory
 // (kmax: the largest maxk of the batch).  coshuffle (iconv = 1) runs on one lane.
+template <bool GENERAL>
 __global__ void __launch_bounds__(kFp32Threads)
 k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
           const long long *__restrict__ step_ctr, int rel, int kmax)
@@ -683,7 +684,7 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
     const long long step = *step_ctr + rel;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     double *tv = cosm + (size_t)warp * (kmax + 1) * 32;
-    CoWarpState *cs = reinterpret_cast<CoWarpState *>(cosm + (size_t)nwarp * (kmax + 1) * 32) + warp;
+    CoWarpState *cs = GENERAL ? reinterpret_cast<CoWarpState *>(cosm + (size_t)nwarp * (kmax + 1) * 32) + warp : nullptr;
     const int ncol = min(cocount[step & 1], cocap);
     // the list of the next step starts empty (that step's kernel runs after this one)
     if (blockIdx.x == 0 && threadIdx.x == 0) cocount[(step + 1) & 1] = 0;
@@ -692,6 +693,8 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         const MemberDesc &md = mds[ent.x];
         const int32_t *ticol = md.ptab + ent.y;
         const int maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ, mkn = maxk + 2;
+        // this instance takes either the warp-parallel columns or the others
+        if (fp32_co_fast(md.iconv, md.ieos, maxk) == GENERAL) continue;
         const int k1c = (ticol[2] >> 16) & 0xffff, cl0 = ticol[3];
         const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
         const int par = (int)((step + md.parity) & 1);
@@ -701,7 +704,7 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         EosCoef ec;
         for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
         ec.ieos = md.ieos;
-        if (md.iconv == 1) {
+        if (GENERAL && md.iconv == 1) {
             if (lane == 0) {
                 Fp32Col col;
                 col.w = W;
@@ -740,6 +743,14 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         const size_t NIJ = (size_t)NI * NJ;
         const double *wc = W + wofs + ((size_t)i + (size_t)NI * j) * gpw;
         const size_t lstride = NIJ * gpw;
+        if (!GENERAL) {
+            // T and S are plane 0, two values per cell
+            const int filled = co_warp32(tv, ec, maxk, L, k1c, dz, lane, W + 2 * ((size_t)i + (size_t)NI * j), 2 * NIJ,
+                                         const_cast<double *>(wc), lstride);
+            if (lane == 0 && filled > 0) md.cost[cl0] = add_count_rn(md.cost[cl0], filled);
+            __syncwarp();
+            continue;
+        }
         if (lane < L)
             for (int lev = k1c; lev <= maxk; lev += 8) {
                 double v[8];
@@ -752,14 +763,10 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
             }
         __syncwarp();
         // the step stored the FP64 densities of the column (ieos = 0)
-        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane, nullptr, NIJ);
+        const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane);
         if (lane < L)
             for (int lev = k1c; lev <= maxk; ++lev) const_cast<double *>(wc)[(size_t)lev * lstride] = tv[lev * 32 + lane];
-        if (lane == 0 && filled > 0) {
-            double cst = md.cost[cl0];
-            for (int f = 0; f < filled; ++f) cst = __dadd_rn(cst, 1.0);
-            md.cost[cl0] = cst;
-        }
+        if (lane == 0 && filled > 0) md.cost[cl0] = add_count_rn(md.cost[cl0], filled);
         __syncwarp();
     }
 }
@@ -814,16 +821,21 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         cudaEventRecord(join, s2);
         cudaStreamWaitEvent(s, join, 0);
     }
-    const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
-    cudaFuncSetAttribute(k_co_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
-    int co_per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, k_co_fp32, kFp32Threads, co_smem);
-    k_co_fp32<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
-                                                                           step_ctr, rel, b.kmax);
+    // the adjustment: warp-parallel columns, then (if the batch has any) the serial ones
+    for (int general = 0; general <= (b.co_general ? 1 : 0); ++general) {
+        auto kern = general ? k_co_fp32<true> : k_co_fp32<false>;
+        const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) +
+                                                   (general ? (int)sizeof(CoWarpState) : 0));
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
+        int co_per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, kern, kFp32Threads, co_smem);
+        kern<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
+                                                                         step_ctr, rel, b.kmax);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
-int fp32_launches_per_step(const Fp32Batch &b) { return (b.n_ts > 0) + (b.n_bgc > 0) + 1; }
+int fp32_launches_per_step(const Fp32Batch &b) { return (b.n_ts > 0) + (b.n_bgc > 0) + 1 + (b.co_general ? 1 : 0); }
 
 // ---------------------------------------------------------------------------
 // patch plan (host): rectangles of water columns, periodic in i, with the ring of
@@ -1551,6 +1563,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         bt.cocount = D.cocount;
         bt.cocap = D.cocap;
         bt.iso = h->p.diso != 0;
+        bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->d.maxk);
         int r = D.nitems ? fp32_launch(bt, D.step_ctr, n, s, D.s2, D.fork, D.join) : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;

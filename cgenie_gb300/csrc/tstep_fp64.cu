@@ -415,9 +415,7 @@ __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
             a.icosd[c2] = icos;
             a.cost[c2] = p.dsc * M.zw[maxk - 1 - icos];
         } else if (filled > 0) {
-            double c = a.cost[c2];
-            for (int f = 0; f < filled; ++f) c = c + 1.0;
-            a.cost[c2] = c;
+            a.cost[c2] = add_count_rn(a.cost[c2], filled);
         }
         if (p.ieos != 0) {
             for (int kk = 1; kk <= maxk; ++kk) {
