@@ -56,6 +56,7 @@ class GbParams(C.Structure):
         ("diso", C.c_int32),
         ("precision", C.c_int32),
         ("reserved", C.c_int32),
+        ("mldpebuoycoeff", C.c_double),
     ]
 
 
@@ -71,6 +72,7 @@ class GbGrid(C.Structure):
         ("diffmax", _dp),
         ("k1", _ip),
         ("dphi", C.c_double), ("rdphi", C.c_double),
+        ("mlddec", _dp), ("mlddecd", _dp), ("mldketau", _dp),
     ]
 
 
@@ -98,13 +100,16 @@ class GridRefs:
     """Owns contiguous copies of a member's metric arrays and the ctypes structs
     that point at them."""
 
-    def __init__(self, m, *, diso=None, ieos=None, iconv=None, iediff=None, precision=GB_GO_FP64):
+    def __init__(self, m, *, diso=None, ieos=None, iconv=None, iediff=None, imld=None, precision=GB_GO_FP64):
         cfg = m.cfg
         self.arrays = {}
         for name in ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza",
                      "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
             self.arrays[name] = np.ascontiguousarray(getattr(m, name), dtype=np.float64)
         self.arrays["k1"] = np.ascontiguousarray(m.k1, dtype=np.int32)
+        for name in ("mlddec", "mlddecd", "mldketau"):
+            v = getattr(m, name, None)
+            self.arrays[name] = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         self.dims = GbDims(m.maxi, m.maxj, m.maxk, m.maxl)
         p = GbParams()
         p.diff[0], p.diff[1] = float(m.diff[0]), float(m.diff[1])
@@ -117,7 +122,8 @@ class GridRefs:
         p.iediff = int(cfg.iediff if iediff is None else iediff)
         p.ediffpow2i = int(m.ediffpow2i)
         p.iconv = int(cfg.iconv if iconv is None else iconv)
-        p.imld = 0
+        p.imld = int(getattr(cfg, "imld", 0) if imld is None else imld)
+        p.mldpebuoycoeff = float(getattr(cfg, "mldpebuoycoeff", 0.15))
         p.diso = int(bool(cfg.diso if diso is None else diso))
         p.precision = int(precision)
         p.reserved = 0
@@ -127,6 +133,8 @@ class GridRefs:
                      "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
             setattr(g, name, dptr(self.arrays[name]))
         g.k1 = iptr(self.arrays["k1"])
+        for name in ("mlddec", "mlddecd", "mldketau"):
+            setattr(g, name, dptr(self.arrays[name]))
         g.dphi = float(m.dphi)
         g.rdphi = float(m.rdphi)
         self.grid = g

@@ -229,6 +229,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (rc) return efail(e, rc, msg);
     if (dims->maxl > kFp32MaxL) return efail(e, GB_GO_ERANGE, "ensemble members carry at most 32 tracers");
     if (params->iediff > 0 && params->iediff < 3) return efail(e, GB_GO_EUNSUPPORTED, "iediff 1/2 not provided in ensembles");
+    if (params->imld != 0) return efail(e, GB_GO_EUNSUPPORTED, "imld=1 not provided in ensembles");
     for (int k = 1; k < dims->maxk; ++k)
         if (grid->dt[k] != grid->dt[0]) return efail(e, GB_GO_EUNSUPPORTED, "ensemble members need one dt for all levels");
     const size_t bytes = member_bytes(dims);

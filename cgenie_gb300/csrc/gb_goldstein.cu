@@ -43,6 +43,8 @@ struct gb_go_handle {
     int32_t *k1 = nullptr;
     double *ediff1 = nullptr;
     double *stage = nullptr;
+    double *mldketau = nullptr, *mld = nullptr, *mldpe1 = nullptr;   // imld = 1, (maxi, maxj)
+    int32_t *mldk = nullptr;
     double *inv_part = nullptr;
     int inv_blocks = 0;
     double *inv_noalloc = nullptr;        // static scratch of gb_go_inventory_noalloc on this device
@@ -103,7 +105,11 @@ int validate_config(const gb_go_dims *dims, const gb_go_params *params, const gb
         return GB_GO_ERANGE;
     }
     if ((long long)dims->maxi * dims->maxj > (1LL << 28)) { msg = "grid too large"; return GB_GO_ERANGE; }
-    if (params->imld != 0) { msg = "imld=1 (Kraus-Turner mixed layer) is not provided"; return GB_GO_EUNSUPPORTED; }
+    if (params->imld != 0 && params->imld != 1) { msg = "imld must be 0 or 1"; return GB_GO_EINVAL; }
+    if (params->imld == 1 && (!grid->mlddec || !grid->mlddecd || !grid->mldketau)) {
+        msg = "imld=1 needs mlddec, mlddecd and mldketau";
+        return GB_GO_EINVAL;
+    }
     if (params->ieos != 0 && params->ieos != 1) { msg = "ieos must be 0 or 1"; return GB_GO_EINVAL; }
     if (params->iconv != 0 && params->iconv != 1) { msg = "iconv must be 0 or 1"; return GB_GO_EINVAL; }
     if (params->iediff < 0) { msg = "iediff must be >= 0"; return GB_GO_EINVAL; }
@@ -144,17 +150,20 @@ int validate_config(const gb_go_dims *dims, const gb_go_params *params, const gb
     return GB_GO_OK;
 }
 
-// Fortran-indexed metric blob: 8 j-arrays of maxj+2 entries then 9 k-arrays of maxk+2.
+// Fortran-indexed metric blob: 8 j-arrays of maxj+2 entries then 11 k-arrays of maxk+2.
 void build_metric_blob(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *g, std::vector<double> &blob)
 {
     const int nj = dims->maxj + 2, nk = dims->maxk + 2, maxj = dims->maxj, maxk = dims->maxk;
-    blob.assign((size_t)8 * nj + (size_t)9 * nk, 0.0);
+    blob.assign((size_t)8 * nj + (size_t)11 * nk, 0.0);
     double *b = blob.data();
     double *rc = b, *rc2 = b + nj, *cv = b + 2 * nj, *cv2 = b + 3 * nj, *dsv = b + 4 * nj, *rdsv = b + 5 * nj,
            *ds = b + 6 * nj, *rds = b + 7 * nj;
     double *kb = b + 8 * nj;
     double *dz = kb, *dza = kb + nk, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk, *dt = kb + 5 * nk,
            *zw = kb + 6 * nk, *ssmax = kb + 7 * nk, *diffmax = kb + 8 * nk;
+    double *mlddec = kb + 9 * nk, *mlddecd = kb + 10 * nk;
+    if (params->imld == 1)
+        for (int k = 1; k <= maxk; ++k) { mlddec[k] = g->mlddec[k - 1]; mlddecd[k] = g->mlddecd[k - 1]; }
     for (int j = 0; j <= maxj; ++j) { rc[j] = g->rc[j]; rc2[j] = g->rc2[j]; cv[j] = g->cv[j]; }
     for (int j = 1; j <= maxj - 1; ++j) { cv2[j] = g->cv2[j - 1]; dsv[j] = g->dsv[j - 1]; rdsv[j] = g->rdsv[j - 1]; }
     for (int j = 1; j <= maxj; ++j) { ds[j] = g->ds[j - 1]; rds[j] = g->rds[j - 1]; }
@@ -178,6 +187,7 @@ Metrics metrics_from_blob(const double *b, const int32_t *k1, const double *edif
     const double *kb = b + 8 * nj;
     m.dz = kb; m.dza = kb + nk; m.rdz = kb + 2 * nk; m.rdza = kb + 3 * nk; m.zro = kb + 4 * nk; m.dt = kb + 5 * nk;
     m.zw = kb + 6 * nk; m.ssmax = kb + 7 * nk; m.diffmax = kb + 8 * nk;
+    m.mlddec = kb + 9 * nk; m.mlddecd = kb + 10 * nk;
     m.ediff1 = ediff1;
     m.k1 = k1;
     return m;
@@ -199,6 +209,8 @@ PhysParams phys_from(const gb_go_params *pp, const gb_go_grid *g)
     p.ediffpow2i = pp->ediffpow2i;
     p.iconv = pp->iconv;
     p.diso = pp->diso ? 1 : 0;
+    p.imld = pp->imld;
+    p.mldpebuoycoeff = pp->mldpebuoycoeff;
     return p;
 }
 
@@ -293,6 +305,7 @@ static void free_handle(gb_go_handle *h)
     cudaFree(h->ts_static); cudaFree(h->ts1_static); cudaFree(h->top); cudaFree(h->rho); cudaFree(h->u);
     cudaFree(h->cost); cudaFree(h->icosd); cudaFree(h->diag); cudaFree(h->metrics); cudaFree(h->k1);
     cudaFree(h->ediff1); cudaFree(h->stage); cudaFree(h->inv_part);
+    cudaFree(h->mldketau); cudaFree(h->mld); cudaFree(h->mldpe1); cudaFree(h->mldk);
     fp32_member_free(&h->f32);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (prev >= 0) cudaSetDevice(prev);
@@ -389,6 +402,15 @@ extern "C" int gb_go_create(const gb_go_dims *dims, const gb_go_params *params, 
     const bool need_ediff = params->iediff > 0 && params->iediff < 3;
     const size_t ned = (size_t)h->d.maxi * h->d.maxj * (h->d.maxk - 1);
     if (e == cudaSuccess && need_ediff) e = cudaMalloc(&h->ediff1, ned * sizeof(double));
+    const bool need_mld = params->imld == 1;
+    if (e == cudaSuccess && need_mld) e = cudaMalloc(&h->mldketau, ncol * sizeof(double));
+    if (e == cudaSuccess && need_mld) e = cudaMalloc(&h->mld, ncol * sizeof(double));
+    if (e == cudaSuccess && need_mld) e = cudaMalloc(&h->mldpe1, ncol * sizeof(double));
+    if (e == cudaSuccess && need_mld) e = cudaMalloc(&h->mldk, ncol * sizeof(int32_t));
+    if (e == cudaSuccess && need_mld)
+        e = cudaMemcpyAsync(h->mldketau, grid->mldketau, ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && need_mld) e = cudaMemsetAsync(h->mld, 0, ncol * sizeof(double), h->stream);
+    if (e == cudaSuccess && need_mld) e = cudaMemsetAsync(h->mldk, 0, ncol * sizeof(int32_t), h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->metrics, blob.data(), blob.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->k1, grid->k1, (size_t)h->d.NI * h->d.NJ * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream);
@@ -518,9 +540,16 @@ extern "C" int gb_go_tstepo(gb_go_handle *h, int32_t nsteps)
     a.tile_i = h->tile_i;
     a.tile_j = h->tile_j;
     a.tiles_i = (h->d.maxi + h->tile_i - 1) / h->tile_i;
+    a.mldketau = h->mldketau;
+    a.mld = h->mld;
+    a.mldk = h->mldk;
+    a.mldpe1 = h->mldpe1;
     for (int s = 0; s < nsteps; ++s) {
         a.ts1 = h->ts_buf[h->cur];
         a.ts = h->ts_buf[1 - h->cur];
+        // ts at the start of the step: the uploaded ts before the first step, then the last
+        // step's result (equal to ts1 on wet cells)
+        a.ts_start = h->steps_since_upload == 0 ? h->ts_static : a.ts1;
         a.diag = h->diag + 2 * h->slot;
         a.diag_next = h->diag + 2 * (1 - h->slot);
         if (launch_step_fp64(a, h->stream)) return cuda_fail(h, cudaGetLastError(), "step_fp64 launch");
@@ -529,6 +558,29 @@ extern "C" int gb_go_tstepo(gb_go_handle *h, int32_t nsteps)
         h->slot = 1 - h->slot;
         ++h->steps_since_upload;
     }
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_set_mld_wind(gb_go_handle *h, const double *mldketau)
+{
+    if (!h || !mldketau) return fail(h, GB_GO_EINVAL, "set_mld_wind: NULL array");
+    if (h->p.imld != 1) return fail(h, GB_GO_EINVAL, "set_mld_wind: the handle was created with imld = 0");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t ncol = (size_t)h->d.maxi * h->d.maxj;
+    CUDA_TRY(h, cudaMemcpyAsync(h->mldketau, mldketau, ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_go_download_mld(gb_go_handle *h, double *mld, int32_t *mldk)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (h->p.imld != 1) return fail(h, GB_GO_EINVAL, "download_mld: the handle was created with imld = 0");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t ncol = (size_t)h->d.maxi * h->d.maxj;
+    if (mld) CUDA_TRY(h, cudaMemcpyAsync(mld, h->mld, ncol * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (mldk) CUDA_TRY(h, cudaMemcpyAsync(mldk, h->mldk, ncol * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
 }
 

@@ -28,6 +28,7 @@ constexpr int kMaxK = 64;
 struct Metrics {
     const double *rc, *rc2, *cv, *cv2, *dsv, *rdsv, *ds, *rds;      // [0 .. maxj+1]
     const double *dz, *dza, *rdz, *rdza, *zro, *dt, *zw, *ssmax, *diffmax;  // [0 .. maxk+1]
+    const double *mlddec, *mlddecd;                                 // [0 .. maxk+1] (imld = 1)
     const double *ediff1;                                           // (maxi, maxj, maxk-1)
     const int32_t *k1;                                              // (maxi+2, maxj+2)
 };
@@ -43,6 +44,8 @@ struct PhysParams {
     double ediff0, ediffpow2, dsc;
     double dphi, rdphi;
     int ieos, iediff, ediffpow2i, iconv, diso;
+    int imld;
+    double mldpebuoycoeff;
 };
 
 // Arguments of one FP64 step launch.
@@ -61,6 +64,13 @@ struct StepArgs {
     unsigned long long *diag;       // [0] dmax bits, [1] limps  (this step)
     unsigned long long *diag_next;  // zeroed by block 0 for the next step
     int tile_i, tile_j, tiles_i;
+    // imld = 1 (mixed layer): ts at the start of the step (its surface level), wind mixing
+    // energy, diagnostics mld/mldk and the per-column surface-layer energy (maxi, maxj)
+    const double *ts_start;
+    const double *mldketau;
+    double *mld;
+    int32_t *mldk;
+    double *mldpe1;
 };
 
 __host__ __device__ inline size_t ts_index(const Dims &d, int l, int i, int j, int k)

@@ -1346,6 +1346,10 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
         msg = "GB_GO_FP32FLUX supports at most 32 tracers per grid";
         return GB_GO_ERANGE;
     }
+    if (p.imld != 0) {
+        msg = "GB_GO_FP32FLUX does not provide imld=1 (use GB_GO_FP64)";
+        return GB_GO_EUNSUPPORTED;
+    }
     if (p.iediff != 0) {
         msg = "GB_GO_FP32FLUX does not provide iediff 1/2 (use GB_GO_FP64)";
         return GB_GO_EUNSUPPORTED;

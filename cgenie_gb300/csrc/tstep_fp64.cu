@@ -1,6 +1,6 @@
 // Plain (FP64) GOLDSTEIN tracer timestep for sm_103a: one launch per step.
 //
-// Restates src/goldstein/goldstein.f90:2280-2432 (tstepo, imld=0), :2436-2642
+// Restates src/goldstein/goldstein.f90:2280-2432 (tstepo, imld=0 and 1), :2436-2642
 // (tstepo_flux incl. the diso branch), :2657-2777 (co), :2781-2841 (coshuffle)
 // and :3048-3082 (eos/eosd).  Every expression keeps the reference's operation
 // order and this translation unit is compiled with -fmad=false, so each double
@@ -14,6 +14,7 @@
 // adjustment `co` of every column and the periodic halo columns are finished in
 // the same launch, after a barrier, by one thread per column.
 #include "gb_internal.h"
+#include "../../include/gb_goldstein.h"
 
 #include <cuda_runtime.h>
 
@@ -173,6 +174,109 @@ __device__ int co_column(const StepArgs &a, const ColumnView &cv)
         }
     }
     return filled;
+}
+
+// ---- Kraus-Turner mixed layer (imld = 1) ----
+// Level-pair depth grids of goldstein.f90:1013-1025: dzg(k,kk) = zw(k) - zw(kk-1),
+// z2dzg(k,kk) = -zw(k)^2 + zw(kk-1)^2, rdzg(k,kk) = 1/dzg(k,kk) (1e10 where k = kk-1).
+__device__ __forceinline__ double dzg_d(const Metrics &M, int k, int kk) { return M.zw[k] - M.zw[kk - 1]; }
+__device__ __forceinline__ double z2dzg_d(const Metrics &M, int k, int kk)
+{
+    return -M.zw[k] * M.zw[k] + M.zw[kk - 1] * M.zw[kk - 1];
+}
+__device__ __forceinline__ double rdzg_d(const Metrics &M, int k, int kk)
+{
+    return k != kk - 1 ? 1.0 / dzg_d(M, k, kk) : 1.0E10;
+}
+
+// krausturner, goldstein.f90:3337-3442, on one column (every level it touches is wet)
+__device__ void kraus_turner_column(const StepArgs &a, const ColumnView &cv, size_t c2, double pebuoy, double ketau)
+{
+    const Dims &d = a.d;
+    const PhysParams &p = a.p;
+    const Metrics &M = a.m;
+    const int maxk = d.maxk, L = d.L, tvkl = cv.k1;
+    double qmix[GB_GO_MAX_L + 1];
+    const int mldpk = maxk;   // the routine's first statement (goldstein.f90:3350)
+    int k = mldpk, partmix = 1;
+    double empe = pebuoy;
+    double emke = ketau * M.mlddec[k];
+    double em = empe + emke;
+    double eneed = 0.0;
+    double tmix = cv.get(0, k), smix = cv.get(1, k);
+    double rhou = 0.0, rhol = 0.0;
+    for (int l = 0; l < L; ++l) qmix[l] = cv.get(l, k);
+    double rhomix = eos_d(p, tmix, smix, M.zw[k]);
+    while (eneed < em && em > 0) {
+        if (k < mldpk) {
+            qmix[0] = tmix;
+            qmix[1] = smix;
+            for (int l = 2; l < L; ++l) qmix[l] = rdzg_d(M, maxk, k) * (qmix[l] * dzg_d(M, maxk, k + 1) + cv.get(l, k) * M.dz[k]);
+        }
+        if (k == tvkl) {
+            a.mldk[c2] = k;
+            a.mld[c2] = M.zw[k - 1];
+            partmix = 0;
+            em = -1.0E-8;
+            if (k < maxk)
+                for (int l = 0; l < L; ++l)
+                    for (int n = k; n <= maxk; ++n) cv.set(l, n, qmix[l]);
+        } else {
+            k = k - 1;
+            const double emr = (em - eneed) / em;
+            empe = empe * emr;
+            emke = emke * emr * M.mlddecd[k];
+            em = empe + emke;
+            rhou = p.ieos != 0 ? eos_d(p, tmix, smix, M.zw[k]) : rhomix;
+            tmix = rdzg_d(M, maxk, k) * (tmix * dzg_d(M, maxk, k + 1) + cv.get(0, k) * M.dz[k]);
+            smix = rdzg_d(M, maxk, k) * (smix * dzg_d(M, maxk, k + 1) + cv.get(1, k) * M.dz[k]);
+            rhol = eos_d(p, cv.get(0, k), cv.get(1, k), M.zw[k]);
+            rhomix = eos_d(p, tmix, smix, M.zw[k]);
+            eneed = z2dzg_d(M, maxk, k + 1) * rhou + z2dzg_d(M, k, k) * rhol - z2dzg_d(M, maxk, k) * rhomix;
+        }
+    }
+    if (partmix == 1 && em > 0) {
+        a.mldk[c2] = k;
+        const double mlda = dzg_d(M, maxk, k + 1) * rdzg_d(M, maxk, k) * em / eneed;
+        const double mldb = (dzg_d(M, maxk, k) * rdzg_d(M, maxk, k + 1) - 1) * mlda;
+        for (int l = 0; l < L; ++l) {
+            const double below = cv.get(l, k);
+            const double surf = (1 - mldb) * qmix[l] + mldb * below;
+            cv.set(l, maxk, surf);
+            for (int n = k + 1; n <= maxk - 1; ++n) cv.set(l, n, surf);
+            cv.set(l, k, mlda * qmix[l] + (1 - mlda) * below);
+        }
+        a.mld[c2] = k < maxk ? M.zw[k] + em / (M.zw[k] * (rhol - rhou)) : 0.0;
+    } else if (partmix == 1 && k < maxk) {
+        a.mldk[c2] = k + 1;
+        a.mld[c2] = M.zw[k];
+    }
+}
+
+// The mixed-layer part of tstepo after co, goldstein.f90:2336-2389, on one wet column:
+// potential energy released by co (rold: densities before co), wind energy, then
+// krausturner or the shallow-layer diagnostic.
+__device__ void mixed_layer_column(const StepArgs &a, const ColumnView &cv, size_t c2, const double *rold)
+{
+    const PhysParams &p = a.p;
+    const Metrics &M = a.m;
+    const int maxk = a.d.maxk;
+    double peconv = 0.0;
+    for (int k = maxk; k > 0; --k) {
+        const double rnew = eos_d(p, cv.get(0, k), cv.get(1, k), M.zro[k]);
+        peconv = peconv + (rnew - rold[k]) * z2dzg_d(M, k, k);
+    }
+    double pebuoy = peconv + a.mldpe1[c2];
+    if (pebuoy > 0.0) pebuoy = pebuoy * p.mldpebuoycoeff;
+    const double ketau = a.mldketau[c2];
+    const double emix = pebuoy + ketau * M.mlddec[maxk];
+    if (emix > 0.0) {
+        kraus_turner_column(a, cv, c2, pebuoy, ketau);
+    } else {
+        a.mldk[c2] = maxk;
+        const double pe1 = a.mldpe1[c2];
+        a.mld[c2] = pe1 < 0 ? M.zw[maxk - 1] * (1 - emix / pe1) : M.zw[maxk - 1];
+    }
 }
 
 __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
@@ -385,6 +489,16 @@ __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
             t0 = a.ts_static[ts_index(d, 0, i, j, k)];
             t1 = a.ts_static[ts_index(d, 1, i, j, k)];
         }
+        if (p.imld == 1 && k == maxk) {
+            // imld = 1: energy of mixing the surface forcing over the top layer, from ts at
+            // the start of the step and the previous step's rho (goldstein.f90:2294-2309)
+            const size_t o = (size_t)d.L * ((size_t)i + (size_t)d.NI * (size_t)j);
+            const double tt = a.ts_start[ts_index(d, 0, i, j, maxk)] - a.top[o];
+            const double st = a.ts_start[ts_index(d, 1, i, j, maxk)] - a.top[o + 1];
+            const double r = eos_d(p, tt, st, M.zro[maxk]);
+            a.mldpe1[(size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1)] =
+                (r - a.rho[rho_index(d, i, j, maxk)]) * z2dzg_d(M, maxk, maxk);
+        }
         a.rho[rho_index(d, i, j, k)] = eos_d(p, t0, t1, M.zro[k]);
     }
 
@@ -407,6 +521,10 @@ __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
     if (inside && kz == 0 && k1c <= maxk) {
         ColumnView cv{a.ts, a.ts_static, &a.d, i, j, k1c};
         const size_t c2 = (size_t)(i - 1) + (size_t)maxi * (size_t)(j - 1);
+        // imld = 1: densities before co (the flux step's, every level) for its energy release
+        double rold[GB_GO_MAX_K + 1];
+        if (p.imld == 1)
+            for (int kk = 1; kk <= maxk; ++kk) rold[kk] = a.rho[rho_index(d, i, j, kk)];
         int32_t icos = 0;
         if (p.iconv == 1) coshuffle_column(a, cv, icos);
         const int filled = co_column(a, cv);
@@ -417,6 +535,7 @@ __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
         } else if (filled > 0) {
             a.cost[c2] = add_count_rn(a.cost[c2], filled);
         }
+        if (p.imld == 1) mixed_layer_column(a, cv, c2, rold);
         if (p.ieos != 0) {
             for (int kk = 1; kk <= maxk; ++kk) {
                 const double t0 = kk >= k1c ? a.ts[ts_index(d, 0, i, j, kk)] : a.ts_static[ts_index(d, 0, i, j, kk)];

@@ -24,6 +24,7 @@ MODULE gb_goldstein_c
      REAL(C_DOUBLE) :: ec(5)
      REAL(C_DOUBLE) :: ediff0, ediffpow2, dsc
      INTEGER(C_INT32_T) :: ieos, iediff, ediffpow2i, iconv, imld, diso, precision, reserved
+     REAL(C_DOUBLE) :: mldpebuoycoeff
   END TYPE gb_go_params
 
   TYPE, BIND(C) :: gb_go_grid
@@ -31,6 +32,7 @@ MODULE gb_goldstein_c
      TYPE(C_PTR) :: dz, dza, rdz, rdza, zro, dt, zw, ssmax, ediff1, diffmax
      TYPE(C_PTR) :: k1
      REAL(C_DOUBLE) :: dphi, rdphi
+     TYPE(C_PTR) :: mlddec, mlddecd, mldketau
   END TYPE gb_go_grid
 
   INTEGER(C_INT32_T), PARAMETER :: GB_GO_FP64 = 0, GB_GO_FP32FLUX = 1
@@ -99,6 +101,18 @@ MODULE gb_goldstein_c
        TYPE(C_PTR), VALUE :: handle, out
        INTEGER(C_INT) :: gb_go_inventory_noalloc
      END FUNCTION gb_go_inventory_noalloc
+
+     FUNCTION gb_go_set_mld_wind(handle, mldketau) BIND(C, NAME='gb_go_set_mld_wind')
+       IMPORT :: C_INT, C_PTR
+       TYPE(C_PTR), VALUE :: handle, mldketau
+       INTEGER(C_INT) :: gb_go_set_mld_wind
+     END FUNCTION gb_go_set_mld_wind
+
+     FUNCTION gb_go_download_mld(handle, mld, mldk) BIND(C, NAME='gb_go_download_mld')
+       IMPORT :: C_INT, C_PTR
+       TYPE(C_PTR), VALUE :: handle, mld, mldk
+       INTEGER(C_INT) :: gb_go_download_mld
+     END FUNCTION gb_go_download_mld
 
      FUNCTION gb_go_errstr(code) BIND(C, NAME='gb_go_errstr')
        IMPORT :: C_INT, C_PTR

@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgb_goldstein.so")
 EXPORTED = [
     "gb_go_create", "gb_go_destroy", "gb_go_set_stream", "gb_go_upload_state", "gb_go_set_forcing",
     "gb_go_set_velocity", "gb_go_set_diag", "gb_go_tstepo", "gb_go_download", "gb_go_inventory",
-    "gb_go_inventory_noalloc",
+    "gb_go_inventory_noalloc", "gb_go_set_mld_wind", "gb_go_download_mld",
     "gb_go_sync", "gb_go_errstr", "gb_go_last_error", "gb_go_kernel_launch_count",
     "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
     "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
@@ -70,6 +70,8 @@ def load_library(path: str = LIB_PATH):
     L.gb_go_download.argtypes = [vp, dp, dp, dp, dp, ip, dp, ip]
     L.gb_go_inventory.argtypes = [vp, dp]
     L.gb_go_inventory_noalloc.argtypes = [vp, dp]
+    L.gb_go_set_mld_wind.argtypes = [vp, dp]
+    L.gb_go_download_mld.argtypes = [vp, dp, ip]
     L.gb_go_sync.argtypes = [vp]
     L.gb_go_errstr.argtypes = [C.c_int]
     L.gb_go_errstr.restype = C.c_char_p
@@ -114,10 +116,11 @@ class Goldstein:
     """
 
     def __init__(self, member, *, precision: int = abi.GB_GO_FP64, device: int = -1,
-                 diso=None, ieos=None, iconv=None, iediff=None, stream: Optional[int] = None):
+                 diso=None, ieos=None, iconv=None, iediff=None, imld=None, stream: Optional[int] = None):
         self.lib = load_library()
         self.m = member
-        self.refs = GridRefs(member, diso=diso, ieos=ieos, iconv=iconv, iediff=iediff, precision=precision)
+        self.refs = GridRefs(member, diso=diso, ieos=ieos, iconv=iconv, iediff=iediff, imld=imld,
+                             precision=precision)
         h = C.c_void_p()
         rc = self.lib.gb_go_create(C.byref(self.refs.dims), C.byref(self.refs.params), C.byref(self.refs.grid),
                                    int(device), C.byref(h))
@@ -187,6 +190,18 @@ class Goldstein:
         self._check(self.lib.gb_go_download(self.h, dptr(ts), dptr(ts1), dptr(rho), dptr(cost), iptr(icosd),
                                             C.byref(dmax), C.byref(limps)), "gb_go_download")
         return dict(ts=ts, ts1=ts1, rho=rho, cost=cost, icosd=icosd, dmax=dmax.value, limps=limps.value)
+
+    def set_mld_wind(self, mldketau):
+        """imld = 1: new wind mixing energy mldketau, (maxj, maxi) = Fortran (maxi, maxj)."""
+        a = np.ascontiguousarray(mldketau, dtype=np.float64)
+        self._check(self.lib.gb_go_set_mld_wind(self.h, dptr(a)), "gb_go_set_mld_wind")
+
+    def download_mld(self):
+        """imld = 1: (mld, mldk) of the last step, each (maxj, maxi)."""
+        mld = np.zeros((self.m.maxj, self.m.maxi))
+        mldk = np.zeros((self.m.maxj, self.m.maxi), dtype=np.int32)
+        self._check(self.lib.gb_go_download_mld(self.h, dptr(mld), iptr(mldk)), "gb_go_download_mld")
+        return mld, mldk
 
     def inventory(self) -> np.ndarray:
         out = np.zeros(self.m.maxl)

@@ -74,6 +74,10 @@ class MemberConfig:
     land_code: int = 0           # 0 -> maxk+1
     forcing: float = 0.0         # amplitude of a seeded surface forcing (0 = none)
     noise: float = 0.5           # degC of seeded T noise (drives convection)
+    imld: int = 0                # 1: Kraus-Turner mixed layer (goldstein.f90:2294-2390)
+    mldpebuoycoeff: float = 0.15     # namelist default (goldstein-defaults.nml)
+    mldwindkedec: float = 25.0       # m, wind-energy decay depth (namelist default)
+    mldketau_max: float = 2.0e-5     # seeded stand-in for the wind mixing energy, upper bound
 
 
 @dataclasses.dataclass
@@ -119,6 +123,12 @@ class Member:
     u: np.ndarray
     cost: np.ndarray
     icosd: np.ndarray
+    # mixed-layer scheme (read when cfg.imld = 1)
+    mlddec: np.ndarray = None        # [1:maxk]
+    mlddecd: np.ndarray = None       # [1:maxk]
+    mldketau: np.ndarray = None      # (maxj, maxi) = Fortran (1:maxi, 1:maxj)
+    mld: np.ndarray = None           # (maxj, maxi) diagnostics
+    mldk: np.ndarray = None
 
     @property
     def wet_cells(self) -> int:
@@ -424,7 +434,29 @@ def make_member(cfg: MemberConfig) -> Member:
         diffmax=diffmax, k1=k1, dphi=hg["dphi"], rdphi=hg["rdphi"],
         ts=ts, ts1=ts.copy(), rho=rho, u=u,
         cost=np.zeros((maxj, maxi)), icosd=np.zeros((maxj, maxi), dtype=np.int32),
+        **mld_fields(cfg, rng, maxi, maxj, vg["zro"]),
     )
+
+
+def mld_fields(cfg: MemberConfig, rng, maxi: int, maxj: int, zro: np.ndarray) -> dict:
+    """Inputs of the mixed-layer scheme: the wind-energy decay mlddec/mlddecd of
+    goldstein.f90:1676-1685 (from the namelist depth scale), and a seeded stand-in for the
+    wind mixing energy mldketau of goldstein.f90:120-140 (uniform in [0, mldketau_max],
+    zonally smooth).  Drawn after every other seeded field, so members without the
+    scheme are unchanged."""
+    maxk = len(zro)
+    dec = cfg.mldwindkedec / DSC
+    mlddec = np.exp(zro / dec)
+    mlddecd = np.empty(maxk)
+    mlddecd[:-1] = mlddec[:-1] / mlddec[1:]
+    mlddecd[-1] = mlddec[-1]
+    if cfg.imld:
+        lat = rng.uniform(0.0, 1.0, maxj)
+        mldketau = cfg.mldketau_max * lat[:, None] * rng.uniform(0.5, 1.0, (maxj, maxi))
+    else:
+        mldketau = np.zeros((maxj, maxi))
+    return dict(mlddec=mlddec, mlddecd=mlddecd, mldketau=mldketau, mld=np.zeros((maxj, maxi)),
+                mldk=np.zeros((maxj, maxi), dtype=np.int32))
 
 
 def config_c1(seed: int = 1) -> MemberConfig:

@@ -47,12 +47,12 @@
 extern "C" {
 #endif
 
-#define GB_GO_ABI_VERSION 1
+#define GB_GO_ABI_VERSION 2
 
 /* Error codes. */
 #define GB_GO_OK            0
 #define GB_GO_EINVAL       -1   /* bad argument (NULL pointer, size, flag value) */
-#define GB_GO_EUNSUPPORTED -2   /* option combination not implemented (e.g. imld=1) */
+#define GB_GO_EUNSUPPORTED -2   /* option combination not implemented (e.g. imld=1 with GB_GO_FP32FLUX) */
 #define GB_GO_ECUDA        -3   /* a CUDA runtime call failed */
 #define GB_GO_ENOMEM       -4   /* device allocation failed or over the memory budget */
 #define GB_GO_ENOTREADY    -5   /* state/velocity not uploaded yet */
@@ -90,10 +90,13 @@ typedef struct gb_go_params {
     int32_t iediff;       /* 0: uniform diff(2); 1 or 2: ediff1/diffmax profile */
     int32_t ediffpow2i;   /* 0, 1, 2 or any other value for the general power */
     int32_t iconv;        /* 0: co only; 1: coshuffle before co */
-    int32_t imld;         /* must be 0: the Kraus-Turner branch is not provided */
+    int32_t imld;         /* 0, or 1: Kraus-Turner mixed layer after co (goldstein.f90:2294-2390,
+                             3337-3442); GB_GO_FP64 single grids only */
     int32_t diso;         /* non-zero: isoneutral (Redi) branch on */
     int32_t precision;    /* GB_GO_FP64 or GB_GO_FP32FLUX */
     int32_t reserved;     /* must be 0 */
+    double  mldpebuoycoeff;  /* imld = 1: efficiency of convective energy release (ini_gold_nml,
+                                default 0.15, goldstein.f90:2354-2356) */
 } gb_go_params;
 
 /* Grid metrics (goldstein.f90:908-1076, 2057-2070).  Lower bounds in brackets. */
@@ -108,6 +111,9 @@ typedef struct gb_go_grid {
     const double  *diffmax;              /* [1:maxk], read when iediff is 1 or 2 */
     const int32_t *k1;                   /* (0:maxi+1, 0:maxj+1) */
     double dphi, rdphi;
+    const double  *mlddec, *mlddecd;     /* [1:maxk], read when imld = 1 (goldstein.f90:1678-1685) */
+    const double  *mldketau;             /* (1:maxi,1:maxj) wind mixing energy, read when imld = 1
+                                            (goldstein.f90:120-140); gb_go_set_mld_wind updates it */
 } gb_go_grid;
 
 typedef struct gb_go_handle gb_go_handle;
@@ -149,6 +155,15 @@ int  gb_go_tstepo(gb_go_handle *h, int32_t nsteps);
  * are the diagnostics of the last step (goldstein.f90:2459, 2598-2608). */
 int  gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *rho,
                     double *cost, int32_t *icosd, double *dmax, int32_t *limps);
+
+/* imld = 1: replace the wind mixing energy mldketau(1:maxi,1:maxj), which the reference
+ * recomputes from the wind stress at goldstein.f90:120-140. */
+int  gb_go_set_mld_wind(gb_go_handle *h, const double *mldketau);
+
+/* imld = 1: the mixed-layer diagnostics of the last step, mld(maxi,maxj) (depth, <= 0) and
+ * mldk(maxi,maxj) (index of the level holding it), written by tstepo for wet columns
+ * (goldstein.f90:2371-2386, 3337-3442); 0 where never written.  Either may be NULL. */
+int  gb_go_download_mld(gb_go_handle *h, double *mld, int32_t *mldk);
 
 /* Per-tracer inventory sum over wet cells of ts(l,i,j,k)*ds(j)*dz(k)
  * (the weighting of the reference's conservation diagnostic,

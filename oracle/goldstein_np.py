@@ -36,7 +36,7 @@ def eosd(ec, t1, t2, s1, s2, z, rdz, ieos):
 
 
 class Params:
-    def __init__(self, m, diso, ieos, iconv, iediff):
+    def __init__(self, m, diso, ieos, iconv, iediff, imld=0):
         self.diff = m.diff
         self.ec = m.ec
         self.diso = bool(diso)
@@ -46,6 +46,8 @@ class Params:
         self.ediff0 = m.ediff0
         self.ediffpow2 = m.ediffpow2
         self.ediffpow2i = m.ediffpow2i
+        self.imld = imld
+        self.mldpebuoycoeff = getattr(m.cfg, "mldpebuoycoeff", 0.15)
 
 
 def flux(m, p, ts, ts1, rho, u):
@@ -295,14 +297,134 @@ def co(m, p, ts, rho, cost, icosd):
                 cost[j - 1, i - 1] += float(filled)
 
 
-def tstepo(m, p, ts, ts1, rho, u, cost, icosd, nsteps=1):
-    """tstepo (goldstein.f90:2280-2432), imld = 0.  In place; returns (dmax, limps) of the last step."""
+
+def _level_pair_grids(zw):
+    """goldstein.f90:1013-1025 as functions of (k, kk): dzg = zw(k) - zw(kk-1),
+    z2dzg = -zw(k)^2 + zw(kk-1)^2, rdzg = 1/dzg (1e10 where k = kk-1)."""
+    def dzg(k, kk):
+        return zw[k] - zw[kk - 1]
+
+    def z2dzg(k, kk):
+        return -zw[k] * zw[k] + zw[kk - 1] * zw[kk - 1]
+
+    def rdzg(k, kk):
+        return 1.0 / dzg(k, kk) if k != kk - 1 else 1.0e10
+    return dzg, z2dzg, rdzg
+
+
+def _kraus_turner_col(m, p, tv, k1, pebuoy, ketau):
+    """krausturner (goldstein.f90:3337-3442) on one column; tv[k, l] is modified in place.
+    Returns (mld, mldk) or None where the routine leaves them untouched."""
+    maxk = m.maxk
+    ec, ieos, zw, dz = p.ec, p.ieos, m.zw, m.dz
+    dec, decd = m.mlddec, m.mlddecd          # [k-1] holds level k
+    dzg, z2dzg, rdzg = _level_pair_grids(zw)
+    top = maxk                               # mldpk, reset to maxk by the routine
+    k = top
+    empe = pebuoy
+    emke = ketau * dec[k - 1]
+    em = empe + emke
+    eneed = 0.0
+    tmix, smix = tv[k, 0], tv[k, 1]
+    q = tv[k, :].copy()
+    rhomix = eos(ec, tmix, smix, zw[k], ieos)
+    rhou = rhol = 0.0
+    out = None
+    partial = True
+    while eneed < em and em > 0:
+        if k < top:
+            q[0], q[1] = tmix, smix
+            q[2:] = rdzg(maxk, k) * (q[2:] * dzg(maxk, k + 1) + tv[k, 2:] * dz[k - 1])
+        if k == k1:
+            out = (zw[k - 1], k)
+            partial = False
+            em = -1.0e-8
+            if k < maxk:
+                tv[k:maxk + 1, :] = q[None, :]
+            continue
+        k -= 1
+        emr = (em - eneed) / em
+        empe = empe * emr
+        emke = emke * emr * decd[k - 1]
+        em = empe + emke
+        rhou = eos(ec, tmix, smix, zw[k], ieos) if ieos != 0 else rhomix
+        tmix = rdzg(maxk, k) * (tmix * dzg(maxk, k + 1) + tv[k, 0] * dz[k - 1])
+        smix = rdzg(maxk, k) * (smix * dzg(maxk, k + 1) + tv[k, 1] * dz[k - 1])
+        rhol = eos(ec, tv[k, 0], tv[k, 1], zw[k], ieos)
+        rhomix = eos(ec, tmix, smix, zw[k], ieos)
+        eneed = z2dzg(maxk, k + 1) * rhou + z2dzg(k, k) * rhol - z2dzg(maxk, k) * rhomix
+    if partial and em > 0:
+        a = dzg(maxk, k + 1) * rdzg(maxk, k) * em / eneed
+        b = (dzg(maxk, k) * rdzg(maxk, k + 1) - 1) * a
+        below = tv[k, :].copy()
+        surf = (1 - b) * q + b * below
+        tv[maxk, :] = surf
+        if k + 1 <= maxk - 1:
+            tv[k + 1:maxk, :] = surf[None, :]
+        tv[k, :] = a * q + (1 - a) * below
+        out = (zw[k] + em / (zw[k] * (rhol - rhou)) if k < maxk else 0.0, k)
+    elif partial and k < maxk:
+        out = (zw[k], k + 1)
+    return out
+
+
+def mixed_layer(m, p, ts, ts_before, pe1, mld, mldk):
+    """The imld = 1 part of tstepo after co (goldstein.f90:2336-2389): potential energy
+    released by co, wind energy, krausturner or the shallow-layer diagnostic."""
+    maxi, maxj, maxk = m.maxi, m.maxj, m.maxk
+    ec, ieos, zro, zw = p.ec, p.ieos, m.zro, m.zw
+    _, z2dzg, _ = _level_pair_grids(zw)
+    for i in range(1, maxi + 1):
+        for j in range(1, maxj + 1):
+            k1 = int(m.k1[j, i])
+            if k1 > maxk:
+                continue
+            pec = 0.0
+            for k in range(maxk, 0, -1):
+                ro = eos(ec, ts_before[k, j, i, 0], ts_before[k, j, i, 1], zro[k - 1], ieos)
+                rn = eos(ec, ts[k, j, i, 0], ts[k, j, i, 1], zro[k - 1], ieos)
+                pec = pec + (rn - ro) * z2dzg(k, k)
+            peb = pec + pe1[j - 1, i - 1]
+            if peb > 0.0:
+                peb = peb * p.mldpebuoycoeff
+            ketau = m.mldketau[j - 1, i - 1]
+            emix = peb + ketau * m.mlddec[maxk - 1]
+            if emix > 0.0:
+                r = _kraus_turner_col(m, p, ts[:, j, i, :], k1, peb, ketau)
+                if r is not None:
+                    mld[j - 1, i - 1], mldk[j - 1, i - 1] = r
+            else:
+                mldk[j - 1, i - 1] = maxk
+                p1 = pe1[j - 1, i - 1]
+                mld[j - 1, i - 1] = zw[maxk - 1] * (1 - emix / p1) if p1 < 0 else zw[maxk - 1]
+
+
+def surface_layer_energy(m, p, ts, rho):
+    """mldpelayer1 of goldstein.f90:2294-2309, before the flux step: (maxj, maxi)."""
+    maxi, maxj, maxk = m.maxi, m.maxj, m.maxk
+    _, z2dzg, _ = _level_pair_grids(m.zw)
+    t = ts[maxk, 1:maxj + 1, 1:maxi + 1, 0] - ts[maxk + 1, 1:maxj + 1, 1:maxi + 1, 0]
+    s = ts[maxk, 1:maxj + 1, 1:maxi + 1, 1] - ts[maxk + 1, 1:maxj + 1, 1:maxi + 1, 1]
+    r = eos(p.ec, t, s, m.zro[maxk - 1], p.ieos)
+    return (r - rho[maxk, 1:maxj + 1, 1:maxi + 1]) * z2dzg(maxk, maxk)
+
+
+def tstepo(m, p, ts, ts1, rho, u, cost, icosd, nsteps=1, mld=None, mldk=None):
+    """tstepo (goldstein.f90:2280-2432).  In place; returns (dmax, limps) of the last step.
+    With p.imld = 1 the mixed-layer diagnostics go to mld, mldk ((maxj, maxi))."""
     maxi, maxj, maxk = m.maxi, m.maxj, m.maxk
     dmax, limps = 0.0, 0
     k1 = m.k1
     for _ in range(nsteps):
+        if p.imld == 1:
+            pe1 = surface_layer_energy(m, p, ts, rho)
         dmax, limps = flux(m, p, ts, ts1, rho, u)
-        co(m, p, ts, rho, cost, icosd)
+        if p.imld == 1:
+            before = ts[..., :2].copy()
+            co(m, p, ts, rho, cost, icosd)
+            mixed_layer(m, p, ts, before, pe1, mld, mldk)
+        else:
+            co(m, p, ts, rho, cost, icosd)
         if p.ieos:
             wet = k1[1:maxj + 1, 1:maxi + 1] <= maxk
             t = ts[1:maxk + 1, 1:maxj + 1, 1:maxi + 1]

@@ -4,11 +4,12 @@
  * leg do, and only as the checker or the timed CPU reference.
  *
  * Line-for-line C restatement of the reference GOLDSTEIN tracer timestep:
- *   tstepo       src/goldstein/goldstein.f90:2280-2432   (imld = 0 path)
+ *   tstepo       src/goldstein/goldstein.f90:2280-2432   (imld = 0 and imld = 1)
  *   tstepo_flux  src/goldstein/goldstein.f90:2436-2642   (incl. diso branch :2561-2624)
  *   co           src/goldstein/goldstein.f90:2657-2777
  *   coshuffle    src/goldstein/goldstein.f90:2781-2841
  *   eos / eosd   src/goldstein/goldstein.f90:3048-3082
+ *   krausturner  src/goldstein/goldstein.f90:3337-3442   (imld = 1)
  * The module state of src/goldstein/goldstein_lib.f90:6-180 is passed in through
  * the structs of include/gb_goldstein.h.  The reference is Fortran compiled with
  * -fdefault-real-8 and no FMA-capable -march (platforms/LINUX), so every
@@ -37,6 +38,11 @@ typedef struct {
     double *cost;
     int32_t *icosd;
     int32_t *mldpk;        /* (2, maxi, maxj): local of tstepo, kept for fidelity */
+    /* imld = 1: diagnostics mld, mldk (maxi, maxj); scratch of tstepo: mldpelayer1 (maxi, maxj),
+     * T and S before co (2, maxi, maxj, maxk), qmix of krausturner (maxl + 1) */
+    double *mld;
+    int32_t *mldk;
+    double *pe1, *tsold, *qmix;
     double dmax;
     int32_t limps;
     /* scratch of tstepo_flux */
@@ -68,6 +74,13 @@ typedef struct {
 #define DT(k)   c->g->dt[(k) - 1]
 #define ZW(k)   c->g->zw[(k)]
 #define SSMAX(k) c->g->ssmax[(k) - 1]
+#define MLDDEC(k)  c->g->mlddec[(k) - 1]
+#define MLDDECD(k) c->g->mlddecd[(k) - 1]
+#define MLDKETAU(i, j) c->g->mldketau[((size_t)(i) - 1) + (size_t)c->maxi * ((size_t)(j) - 1)]
+#define MLD(i, j)  c->mld[((size_t)(i) - 1) + (size_t)c->maxi * ((size_t)(j) - 1)]
+#define MLDK(i, j) c->mldk[((size_t)(i) - 1) + (size_t)c->maxi * ((size_t)(j) - 1)]
+#define PE1(i, j)  c->pe1[((size_t)(i) - 1) + (size_t)c->maxi * ((size_t)(j) - 1)]
+#define TSOLD(l, i, j, k) c->tsold[((size_t)(l) - 1) + 2 * (((size_t)(i) - 1) + (size_t)c->maxi * (((size_t)(j) - 1) + (size_t)c->maxj * ((size_t)(k) - 1)))]
 #define DIFFMAX(k) c->g->diffmax[(k) - 1]
 #define EDIFF1(i, j, k) c->g->ediff1[((size_t)(i) - 1) + (size_t)c->maxi * (((size_t)(j) - 1) + (size_t)c->maxj * ((size_t)(k) - 1))]
 /* tstepo_flux scratch: fs(maxl,maxi), fb(maxl,maxi,maxj), dxts(maxl,4), dyts(maxl,4) */
@@ -414,6 +427,129 @@ static void co(ctx *c)
     }
 }
 
+/* Level-pair depth grids of the mixed-layer scheme, goldstein.f90:1013-1025:
+ * dzg(k,kk) = zw(k) - zw(kk-1), z2dzg(k,kk) = -zw(k)^2 + zw(kk-1)^2,
+ * rdzg(k,kk) = 1/dzg(k,kk), or 1e10 where k = kk-1. */
+static double dzg(const ctx *c, int k, int kk) { return ZW(k) - ZW(kk - 1); }
+static double z2dzg(const ctx *c, int k, int kk) { return -ZW(k) * ZW(k) + ZW(kk - 1) * ZW(kk - 1); }
+static double rdzg(const ctx *c, int k, int kk) { return k != kk - 1 ? 1.0 / dzg(c, k, kk) : 1.0E10; }
+
+/* Energy of mixing the surface forcing over the top layer, goldstein.f90:2294-2309
+ * (before the flux step: rho is still the previous step's). */
+static void mld_layer1(ctx *c)
+{
+    const int maxi = c->maxi, maxj = c->maxj, maxk = c->maxk;
+    const gb_go_params *p = c->p;
+    for (int j = 1; j <= maxj; ++j)
+        for (int i = 1; i <= maxi; ++i) {
+            const double t = TS(1, i, j, maxk) - TS(1, i, j, maxk + 1);
+            const double s = TS(2, i, j, maxk) - TS(2, i, j, maxk + 1);
+            const double r = eos(p->ec, t, s, ZRO(maxk), p->ieos);
+            PE1(i, j) = (r - RHO(i, j, maxk)) * z2dzg(c, maxk, maxk);
+        }
+}
+
+/* krausturner, goldstein.f90:3337-3442, on column (i, j) */
+static void krausturner(ctx *c, int i, int j, double pebuoy, double ketau)
+{
+    const int maxk = c->maxk, maxl = c->maxl, tvkl = K1(i, j);
+    const gb_go_params *p = c->p;
+    const double *ec = p->ec;
+    double *qmix = c->qmix;
+    const int mldpk = maxk;   /* the routine's first statement (goldstein.f90:3350) */
+    int k = mldpk, l, n, partmix = 1;
+    double empe = pebuoy;
+    double emke = ketau * MLDDEC(k);
+    double em = empe + emke;
+    double eneed = 0.0;
+    double tmix = TS(1, i, j, k), smix = TS(2, i, j, k);
+    double rhomix, rhou = 0.0, rhol = 0.0, emr;
+    for (l = 1; l <= maxl; ++l) qmix[l] = TS(l, i, j, k);
+    rhomix = eos(ec, tmix, smix, ZW(k), p->ieos);
+    while (eneed < em && em > 0) {
+        if (k < mldpk) {
+            qmix[1] = tmix;
+            qmix[2] = smix;
+            for (l = 3; l <= maxl; ++l)
+                qmix[l] = rdzg(c, maxk, k) * (qmix[l] * dzg(c, maxk, k + 1) + TS(l, i, j, k) * DZ(k));
+        }
+        if (k == tvkl) {
+            MLDK(i, j) = k;
+            MLD(i, j) = ZW(k - 1);
+            partmix = 0;
+            em = -1.0E-8;
+            if (k < maxk)
+                for (l = 1; l <= maxl; ++l)
+                    for (n = k; n <= maxk; ++n) TS(l, i, j, n) = qmix[l];
+        } else {
+            k = k - 1;
+            emr = (em - eneed) / em;
+            empe = empe * emr;
+            emke = emke * emr * MLDDECD(k);
+            em = empe + emke;
+            rhou = p->ieos != 0 ? eos(ec, tmix, smix, ZW(k), p->ieos) : rhomix;
+            tmix = rdzg(c, maxk, k) * (tmix * dzg(c, maxk, k + 1) + TS(1, i, j, k) * DZ(k));
+            smix = rdzg(c, maxk, k) * (smix * dzg(c, maxk, k + 1) + TS(2, i, j, k) * DZ(k));
+            rhol = eos(ec, TS(1, i, j, k), TS(2, i, j, k), ZW(k), p->ieos);
+            rhomix = eos(ec, tmix, smix, ZW(k), p->ieos);
+            eneed = z2dzg(c, maxk, k + 1) * rhou + z2dzg(c, k, k) * rhol - z2dzg(c, maxk, k) * rhomix;
+        }
+    }
+    if (partmix == 1 && em > 0) {
+        double mlda, mldb;
+        MLDK(i, j) = k;
+        mlda = dzg(c, maxk, k + 1) * rdzg(c, maxk, k) * em / eneed;
+        mldb = (dzg(c, maxk, k) * rdzg(c, maxk, k + 1) - 1) * mlda;
+        for (l = 1; l <= maxl; ++l) {
+            TS(l, i, j, maxk) = (1 - mldb) * qmix[l] + mldb * TS(l, i, j, k);
+            for (n = k + 1; n <= maxk - 1; ++n) TS(l, i, j, n) = TS(l, i, j, maxk);
+            TS(l, i, j, k) = mlda * qmix[l] + (1 - mlda) * TS(l, i, j, k);
+        }
+        if (k < maxk) MLD(i, j) = ZW(k) + em / (ZW(k) * (rhol - rhou));
+        else MLD(i, j) = 0.0;
+    } else if (partmix == 1 && k < maxk) {
+        MLDK(i, j) = k + 1;
+        MLD(i, j) = ZW(k);
+    }
+}
+
+/* co with the mixed-layer scheme around it, goldstein.f90:2318-2389 */
+static void co_mld(ctx *c)
+{
+    const int maxi = c->maxi, maxj = c->maxj, maxk = c->maxk;
+    const gb_go_params *p = c->p;
+    int i, j, k;
+    /* T and S before co, every level of the wet columns (the PE change uses only these two) */
+    for (i = 1; i <= maxi; ++i)
+        for (j = 1; j <= maxj; ++j)
+            if (K1(i, j) <= maxk)
+                for (k = 1; k <= maxk; ++k) {
+                    TSOLD(1, i, j, k) = TS(1, i, j, k);
+                    TSOLD(2, i, j, k) = TS(2, i, j, k);
+                }
+    co(c);
+    for (i = 1; i <= maxi; ++i)
+        for (j = 1; j <= maxj; ++j) {
+            if (K1(i, j) > maxk) continue;
+            double peconv = 0.0, pebuoy, emix;
+            for (k = maxk; k > 0; --k) {
+                const double rold = eos(p->ec, TSOLD(1, i, j, k), TSOLD(2, i, j, k), ZRO(k), p->ieos);
+                const double rnew = eos(p->ec, TS(1, i, j, k), TS(2, i, j, k), ZRO(k), p->ieos);
+                peconv = peconv + (rnew - rold) * z2dzg(c, k, k);
+            }
+            pebuoy = peconv + PE1(i, j);
+            if (pebuoy > 0.0) pebuoy = pebuoy * p->mldpebuoycoeff;
+            emix = pebuoy + MLDKETAU(i, j) * MLDDEC(maxk);
+            if (emix > 0.0) {
+                krausturner(c, i, j, pebuoy, MLDKETAU(i, j));
+            } else {
+                MLDK(i, j) = maxk;
+                if (PE1(i, j) < 0) MLD(i, j) = ZW(maxk - 1) * (1 - emix / PE1(i, j));
+                else MLD(i, j) = ZW(maxk - 1);
+            }
+        }
+}
+
 /* dead copies of tstepo (goldstein.f90:2311-2316): kept in faithful mode so the
  * timed CPU baseline moves the same bytes as the reference */
 typedef struct {
@@ -440,16 +576,18 @@ static void do_dead_copies(ctx *c, dead_copies *d)
             }
 }
 
-/* tstepo, goldstein.f90:2280-2432 with imld = 0 */
+/* tstepo, goldstein.f90:2280-2432 */
 static void tstepo(ctx *c, dead_copies *d)
 {
     const int maxi = c->maxi, maxj = c->maxj, maxk = c->maxk, maxl = c->maxl;
     const gb_go_params *p = c->p;
     int i, j, k, l;
 
+    if (p->imld == 1) mld_layer1(c);
     if (d) do_dead_copies(c, d);
     tstepo_flux(c);
-    co(c);
+    if (p->imld == 1) co_mld(c);
+    else co(c);
 
     if (p->ieos != 0) {
         for (i = 1; i <= maxi; ++i)
@@ -483,7 +621,8 @@ static int check_args(const gb_go_dims *dims, const gb_go_params *p, const gb_go
     if (!dims || !p || !g) return GB_GO_EINVAL;
     if (dims->maxi < 2 || dims->maxj < 3 || dims->maxk < 2 || dims->maxl < 2) return GB_GO_EINVAL;
     if (dims->maxk > GB_GO_MAX_K || dims->maxl > GB_GO_MAX_L) return GB_GO_ERANGE;
-    if (p->imld != 0) return GB_GO_EUNSUPPORTED;
+    if (p->imld != 0 && p->imld != 1) return GB_GO_EINVAL;
+    if (p->imld == 1 && (!g->mlddec || !g->mlddecd || !g->mldketau)) return GB_GO_EINVAL;
     if (p->ieos != 0 && p->ieos != 1) return GB_GO_EINVAL;
     if (p->iconv != 0 && p->iconv != 1) return GB_GO_EINVAL;
     if (!g->k1 || !g->rc || !g->rc2 || !g->cv || !g->cv2 || !g->dsv || !g->rdsv || !g->rds ||
@@ -513,6 +652,13 @@ static int ctx_init(ctx *c, const gb_go_dims *dims, const gb_go_params *p, const
     if (!c->fe || !c->fw || !c->fn || !c->fa || !c->fwsave || !c->dzts || !c->sum || !c->fs || !c->fb ||
         !c->dxts || !c->dyts || !c->mldpk)
         return GB_GO_ENOMEM;
+    if (p->imld == 1) {
+        const size_t ncol = (size_t)dims->maxi * dims->maxj;
+        c->pe1 = calloc(ncol, sizeof(double));
+        c->tsold = calloc(2 * ncol * (size_t)dims->maxk, sizeof(double));
+        c->qmix = calloc(L, sizeof(double));
+        if (!c->pe1 || !c->tsold || !c->qmix) return GB_GO_ENOMEM;
+    }
     return GB_GO_OK;
 }
 
@@ -520,18 +666,20 @@ static void ctx_free(ctx *c)
 {
     free(c->fe); free(c->fw); free(c->fn); free(c->fa); free(c->fwsave); free(c->dzts);
     free(c->sum); free(c->fs); free(c->fb); free(c->dxts); free(c->dyts); free(c->mldpk);
+    free(c->pe1); free(c->tsold); free(c->qmix);
 }
 
 /*
  * Advance `nsteps` tracer steps in place on Fortran-layout arrays (the index
- * maps of include/gb_goldstein.h).  cost/icosd may be NULL (then a zeroed
- * internal array is used).  faithful != 0 performs the reference's dead array
- * copies each step.  Returns 0 or a GB_GO_E* code.
+ * maps of include/gb_goldstein.h).  cost/icosd (and, for imld = 1, the mixed-layer
+ * diagnostics mld/mldk, (maxi, maxj)) may be NULL (then a zeroed internal array is
+ * used).  faithful != 0 performs the reference's dead array copies each step.
+ * Returns 0 or a GB_GO_E* code.
  */
-int gbo_tstepo(const gb_go_dims *dims, const gb_go_params *p, const gb_go_grid *g,
-               double *ts, double *ts1, double *rho, const double *u,
-               double *cost, int32_t *icosd, double *dmax, int32_t *limps,
-               int32_t nsteps, int32_t faithful)
+int gbo_tstepo_mld(const gb_go_dims *dims, const gb_go_params *p, const gb_go_grid *g,
+                   double *ts, double *ts1, double *rho, const double *u,
+                   double *cost, int32_t *icosd, double *dmax, int32_t *limps,
+                   int32_t nsteps, int32_t faithful, double *mld, int32_t *mldk)
 {
     int rc = check_args(dims, p, g);
     if (rc) return rc;
@@ -545,6 +693,10 @@ int gbo_tstepo(const gb_go_dims *dims, const gb_go_params *p, const gb_go_grid *
     size_t nts = (size_t)dims->maxl * ncol * dims->maxk;
     if (rc == GB_GO_OK && !cost) { own_cost = calloc(ncol, sizeof(double)); if (!own_cost) rc = GB_GO_ENOMEM; }
     if (rc == GB_GO_OK && !icosd) { own_icosd = calloc(ncol, sizeof(int32_t)); if (!own_icosd) rc = GB_GO_ENOMEM; }
+    double *own_mld = NULL;
+    int32_t *own_mldk = NULL;
+    if (rc == GB_GO_OK && !mld) { own_mld = calloc(ncol, sizeof(double)); if (!own_mld) rc = GB_GO_ENOMEM; }
+    if (rc == GB_GO_OK && !mldk) { own_mldk = calloc(ncol, sizeof(int32_t)); if (!own_mldk) rc = GB_GO_ENOMEM; }
     if (rc == GB_GO_OK && faithful) {
         d.ts_t1 = malloc(nts * sizeof(double)); d.ts1_t1 = malloc(nts * sizeof(double));
         d.ts_t2 = malloc(nts * sizeof(double)); d.ts1_t2 = malloc(nts * sizeof(double));
@@ -555,15 +707,25 @@ int gbo_tstepo(const gb_go_dims *dims, const gb_go_params *p, const gb_go_grid *
         c.ts = ts; c.ts1 = ts1; c.rho = rho; c.u = u;
         c.cost = cost ? cost : own_cost;
         c.icosd = icosd ? icosd : own_icosd;
+        c.mld = mld ? mld : own_mld;
+        c.mldk = mldk ? mldk : own_mldk;
         c.dmax = 0; c.limps = 0;
         for (int s = 0; s < nsteps; ++s) tstepo(&c, faithful ? &d : NULL);
         if (dmax) *dmax = c.dmax;
         if (limps) *limps = c.limps;
     }
-    free(own_cost); free(own_icosd);
+    free(own_cost); free(own_icosd); free(own_mld); free(own_mldk);
     free(d.ts_t1); free(d.ts1_t1); free(d.ts_t2); free(d.ts1_t2); free(d.rho_t1); free(d.rho_t2);
     ctx_free(&c);
     return rc;
+}
+
+int gbo_tstepo(const gb_go_dims *dims, const gb_go_params *p, const gb_go_grid *g,
+               double *ts, double *ts1, double *rho, const double *u,
+               double *cost, int32_t *icosd, double *dmax, int32_t *limps,
+               int32_t nsteps, int32_t faithful)
+{
+    return gbo_tstepo_mld(dims, p, g, ts, ts1, rho, u, cost, icosd, dmax, limps, nsteps, faithful, NULL, NULL);
 }
 
 /* The flux part alone (tstepo_flux), for unit tests of the pieces. */

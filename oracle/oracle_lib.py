@@ -38,6 +38,8 @@ def lib():
                                  P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_int32),
                                  P(C.c_double), P(C.c_int32), C.c_int32, C.c_int32]
         L.gbo_tstepo.restype = C.c_int
+        L.gbo_tstepo_mld.argtypes = L.gbo_tstepo.argtypes + [P(C.c_double), P(C.c_int32)]
+        L.gbo_tstepo_mld.restype = C.c_int
         L.gbo_tstepo_flux.argtypes = [P(GbDims), P(GbParams), P(GbGrid), P(C.c_double), P(C.c_double),
                                       P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_int32)]
         L.gbo_tstepo_flux.restype = C.c_int
@@ -69,13 +71,17 @@ class OracleState:
         self.icosd = m.icosd.copy()
         self.dmax = C.c_double(0.0)
         self.limps = C.c_int32(0)
+        mld = getattr(m, "mld", None)
+        self.mld = np.zeros((m.maxj, m.maxi)) if mld is None else mld.copy()
+        mldk = getattr(m, "mldk", None)
+        self.mldk = np.zeros((m.maxj, m.maxi), dtype=np.int32) if mldk is None else mldk.copy()
 
     def step(self, nsteps: int = 1, faithful: bool = False) -> None:
         r = self.refs
-        rc = lib().gbo_tstepo(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), dptr(self.ts),
-                              dptr(self.ts1), dptr(self.rho), dptr(self.u), dptr(self.cost),
-                              iptr(self.icosd), C.byref(self.dmax), C.byref(self.limps),
-                              int(nsteps), int(bool(faithful)))
+        rc = lib().gbo_tstepo_mld(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), dptr(self.ts),
+                                  dptr(self.ts1), dptr(self.rho), dptr(self.u), dptr(self.cost),
+                                  iptr(self.icosd), C.byref(self.dmax), C.byref(self.limps),
+                                  int(nsteps), int(bool(faithful)), dptr(self.mld), iptr(self.mldk))
         if rc != 0:
             raise RuntimeError(f"oracle gbo_tstepo failed: {rc}")
 

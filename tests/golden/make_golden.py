@@ -31,6 +31,11 @@ CASES = {
     "coshuffle_ieos_10x8x6_l2": (dict(maxi=10, maxj=8, maxk=6, maxl=2, seed=15, iconv=1, ieos=1, noise=2.0), 5),
     "ediff_10x8x6_l3": (dict(maxi=10, maxj=8, maxk=6, maxl=3, seed=16, iediff=1, ediffpow2=1.0, diso=True), 5),
     "forcing_land94_9x7x5_l2": (dict(maxi=9, maxj=7, maxk=5, maxl=2, seed=17, forcing=1.0, land_code=94), 5),
+    "mld_12x10x10_l3": (dict(maxi=12, maxj=10, maxk=10, maxl=3, seed=18, forcing=1.0, imld=1,
+                             mldketau_max=3e-3, mldwindkedec=500.0), 5),
+    "mld_ieos_coshuffle_12x10x10_l3": (dict(maxi=12, maxj=10, maxk=10, maxl=3, seed=19, forcing=1.0, imld=1,
+                                            ieos=1, iconv=1, noise=2.0, mldketau_max=1e-2,
+                                            mldwindkedec=2000.0), 5),
 }
 
 
@@ -39,18 +44,25 @@ def make(name, kw, steps):
     m = grid.make_member(cfg)
     s = oracle_lib.OracleState(m)
     s.step(steps)
-    p = gnp.Params(m, cfg.diso, cfg.ieos, cfg.iconv, cfg.iediff)
+    p = gnp.Params(m, cfg.diso, cfg.ieos, cfg.iconv, cfg.iediff, cfg.imld)
     ts, ts1, rho, cost, icosd = m.copy_state()
-    dmax, limps = gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, steps)
-    for a, b in [(s.ts, ts), (s.ts1, ts1), (s.rho, rho), (s.cost, cost), (s.icosd, icosd)]:
+    mld, mldk = m.mld.copy(), m.mldk.copy()
+    dmax, limps = gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, steps, mld, mldk)
+    for a, b in [(s.ts, ts), (s.ts1, ts1), (s.rho, rho), (s.cost, cost), (s.icosd, icosd), (s.mld, mld),
+                 (s.mldk, mldk)]:
         assert np.array_equal(a, b), name
     assert dmax == s.dmax.value and limps == s.limps.value, name
-    member_io.save(os.path.join(HERE, name + ".npz"), m, dict(
-        steps=steps, ts=s.ts, ts1=s.ts1, rho=s.rho, cost=s.cost, icosd=s.icosd, dmax=s.dmax.value,
-        limps=s.limps.value, inventory=s.inventory()))
+    outs = dict(steps=steps, ts=s.ts, ts1=s.ts1, rho=s.rho, cost=s.cost, icosd=s.icosd, dmax=s.dmax.value,
+                limps=s.limps.value, inventory=s.inventory())
+    if cfg.imld:
+        outs.update(mld=s.mld, mldk=s.mldk)
+    member_io.save(os.path.join(HERE, name + ".npz"), m, outs)
 
 
 if __name__ == "__main__":
+    only = sys.argv[1:]
     for name, (kw, steps) in CASES.items():
+        if only and name not in only:
+            continue
         make(name, kw, steps)
         print("wrote", name)

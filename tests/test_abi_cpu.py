@@ -30,9 +30,10 @@ def test_library_builds_and_exports_all_header_symbols():
 
 def test_struct_layouts():
     assert C.sizeof(abi.GbDims) == 16
-    # 2+5 doubles, 3 doubles, 8 int32
-    assert C.sizeof(abi.GbParams) == (7 + 3) * 8 + 8 * 4
-    assert C.sizeof(abi.GbGrid) == 19 * 8 + 2 * 8
+    # 2+5 doubles, 3 doubles, 8 int32, mldpebuoycoeff
+    assert C.sizeof(abi.GbParams) == (7 + 3) * 8 + 8 * 4 + 8
+    # 19 pointers, dphi and rdphi, 3 pointers of the mixed-layer scheme
+    assert C.sizeof(abi.GbGrid) == 19 * 8 + 2 * 8 + 3 * 8
     assert C.sizeof(abi.GbEnsTuning) == 16
 
 

@@ -24,6 +24,8 @@ def run_gpu(m, steps, chunks=None, **kw):
         g.tstepo(n)
     out = g.download()
     out["inventory"] = g.inventory()
+    if g.refs.params.imld == 1:
+        out["mld"], out["mldk"] = g.download_mld()
     g.close()
     return out
 
@@ -42,6 +44,8 @@ def test_golden_fixtures_bitexact(gpu_lib, path):
     m, ref = member_io.load(path)
     out = run_gpu(m, int(ref["steps"]))
     assert_same(out, ref)
+    if "mld" in ref:
+        assert_same(out, ref, ("mld", "mldk"))
     assert out["dmax"] == float(ref["dmax"])
     assert out["limps"] == int(ref["limps"])
     np.testing.assert_allclose(out["inventory"], ref["inventory"], rtol=1e-14)
@@ -147,11 +151,19 @@ def test_error_codes(gpu_lib):
     assert e.value.code == abi.GB_GO_EINVAL
     import ctypes as C
     from cgenie_gb300.abi import GridRefs
-    r = GridRefs(m)
-    r.params.imld = 1
     h = C.c_void_p()
+    # the mixed layer: FP64 single grids only; imld is 0 or 1; imld = 1 needs its inputs
+    r = GridRefs(m, imld=1, precision=abi.GB_GO_FP32FLUX)
     assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,
                                 C.byref(h)) == abi.GB_GO_EUNSUPPORTED
+    r = GridRefs(m)
+    r.params.imld = 2
+    assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,
+                                C.byref(h)) == abi.GB_GO_EINVAL
+    r = GridRefs(m, imld=1)
+    r.grid.mldketau = None
+    assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,
+                                C.byref(h)) == abi.GB_GO_EINVAL
     r = GridRefs(m)
     r.params.ieos = 3
     assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,

@@ -18,20 +18,28 @@ def test_c_oracle_reproduces_golden(oracle, path):
     m, out = member_io.load(path)
     s = oracle.OracleState(m)
     s.step(int(out["steps"]))
-    for name in ("ts", "ts1", "rho", "cost", "icosd"):
-        assert np.array_equal(getattr(s, name), out[name]), name
+    for name in ("ts", "ts1", "rho", "cost", "icosd", "mld", "mldk"):
+        if name in out:
+            assert np.array_equal(getattr(s, name), out[name]), name
     assert s.dmax.value == float(out["dmax"])
     assert s.limps.value == int(out["limps"])
 
 
-@pytest.mark.parametrize("path", GOLDEN[:4], ids=[os.path.basename(p)[:-4] for p in GOLDEN[:4]])
+GOLDEN_NP = GOLDEN[:4] + [p for p in GOLDEN if os.path.basename(p).startswith("mld_")]
+
+
+@pytest.mark.parametrize("path", GOLDEN_NP, ids=[os.path.basename(p)[:-4] for p in GOLDEN_NP])
 def test_numpy_oracle_reproduces_golden(path):
     m, out = member_io.load(path)
-    p = gnp.Params(m, m.cfg.diso, m.cfg.ieos, m.cfg.iconv, m.cfg.iediff)
+    p = gnp.Params(m, m.cfg.diso, m.cfg.ieos, m.cfg.iconv, m.cfg.iediff, m.cfg.imld)
     ts, ts1, rho, cost, icosd = m.copy_state()
-    dmax, limps = gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, int(out["steps"]))
-    for name, a in (("ts", ts), ("ts1", ts1), ("rho", rho), ("cost", cost), ("icosd", icosd)):
-        assert np.array_equal(a, out[name]), name
+    mld = None if m.mld is None else m.mld.copy()
+    mldk = None if m.mldk is None else m.mldk.copy()
+    dmax, limps = gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, int(out["steps"]), mld, mldk)
+    for name, a in (("ts", ts), ("ts1", ts1), ("rho", rho), ("cost", cost), ("icosd", icosd), ("mld", mld),
+                    ("mldk", mldk)):
+        if name in out:
+            assert np.array_equal(a, out[name]), name
     assert dmax == float(out["dmax"]) and limps == int(out["limps"])
 
 
@@ -39,18 +47,31 @@ def test_numpy_oracle_reproduces_golden(path):
     dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=101),
     dict(maxi=18, maxj=18, maxk=16, maxl=5, seed=102, diso=True, slope_max=1e-3),
     dict(maxi=15, maxj=9, maxk=7, maxl=3, seed=103, iconv=1, ieos=1, diso=True, noise=2.0),
-])
+    # Kraus-Turner mixed layer: partial mixing at many depths, mixing to the bottom,
+    # too little energy for the first layer (zero wind), thermobaricity and coshuffle
+    dict(maxi=18, maxj=14, maxk=12, maxl=3, seed=104, forcing=1.0, imld=1, mldketau_max=3e-3,
+         mldwindkedec=500.0),
+    dict(maxi=18, maxj=14, maxk=12, maxl=4, seed=105, forcing=1.0, imld=1, mldketau_max=1e-2,
+         mldwindkedec=2000.0, ieos=1, iconv=1, noise=2.0, diso=True),
+    dict(maxi=15, maxj=9, maxk=7, maxl=2, seed=106, forcing=1.0, imld=1, mldketau_max=0.0),
+], ids=["plain", "diso", "coshuffle_ieos", "mld", "mld_ieos_coshuffle_diso", "mld_nowind"])
 def test_restatements_agree_bitwise(oracle, kw):
     m = grid.make_member(grid.MemberConfig(**kw))
     s = oracle.OracleState(m)
     s.step(3)
-    p = gnp.Params(m, m.cfg.diso, m.cfg.ieos, m.cfg.iconv, m.cfg.iediff)
+    p = gnp.Params(m, m.cfg.diso, m.cfg.ieos, m.cfg.iconv, m.cfg.iediff, m.cfg.imld)
     ts, ts1, rho, cost, icosd = m.copy_state()
-    gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, 3)
+    mld, mldk = m.mld.copy(), m.mldk.copy()
+    gnp.tstepo(m, p, ts, ts1, rho, m.u, cost, icosd, 3, mld, mldk)
     assert np.array_equal(s.ts, ts)
     assert np.array_equal(s.ts1, ts1)
     assert np.array_equal(s.rho, rho)
     assert np.array_equal(s.cost, cost)
+    assert np.array_equal(s.mld, mld)
+    assert np.array_equal(s.mldk, mldk)
+    if m.cfg.imld:
+        wet = m.k1[1:-1, 1:-1] <= m.maxk
+        assert np.all(s.mldk[wet] >= 1)
 
 
 def test_conservation_zero_forcing(oracle):
@@ -137,7 +158,14 @@ def test_oracle_rejects_bad_options(oracle):
     from cgenie_gb300.abi import GridRefs, dptr, iptr
     m = grid.make_member(grid.MemberConfig(maxi=6, maxj=5, maxk=4, maxl=2, seed=1))
     r = GridRefs(m)
+    r.params.imld = 2
+    s = oracle.OracleState(m, refs=r)
+    with pytest.raises(RuntimeError):
+        s.step(1)
+    # imld = 1 needs the wind energy and its decay profile
+    r = GridRefs(m)
     r.params.imld = 1
+    r.grid.mldketau = None
     s = oracle.OracleState(m, refs=r)
     with pytest.raises(RuntimeError):
         s.step(1)
