@@ -71,7 +71,9 @@ def check_against_oracle(oracle, m, steps, tol_ts=TOL_TS, tol=TOL_REL):
     (grid.MemberConfig(maxi=36, maxj=36, maxk=16, maxl=9, seed=3, tracer_kind="bgc"), 100),
     (grid.MemberConfig(maxi=37, maxj=23, maxk=13, maxl=5, seed=51), 50),
     (grid.MemberConfig(maxi=18, maxj=18, maxk=32, maxl=24, seed=52, tracer_kind="bgc"), 50),
-], ids=["c1", "l9", "odd", "deep24"])
+    # more than 32 levels: the adjustment's serial form
+    (grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=57, noise=2.0), 30),
+], ids=["c1", "l9", "odd", "deep24", "levels40"])
 def test_fp32_matches_oracle(gpu_lib, oracle, cfg, steps):
     check_against_oracle(oracle, grid.make_member(cfg), steps)
 
@@ -163,6 +165,30 @@ def test_ensemble_matches_oracle_per_member(gpu_lib, oracle):
         assert np.array_equal(out["cost"], ref.cost)
         v1 = ens.inventory(i)
         assert np.all(np.abs(v1 - v0) <= TOL_CONS * np.abs(v0))
+        assert ens.status(i) == 0
+    ens.close()
+
+
+def test_ensemble_mixed_adjustment_forms(gpu_lib, oracle):
+    """One batch with members of both adjustment forms: warp-parallel (ieos = 0,
+    iconv = 0, maxk <= 32) and serial (ieos = 1 with coshuffle; 40 levels)."""
+    from cgenie_gb300.ensemble import Ensemble
+    mems = [grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=16, maxl=5, seed=61, noise=2.0,
+                                               tracer_kind="bgc")),
+            grid.make_member(grid.MemberConfig(maxi=15, maxj=12, maxk=10, maxl=3, seed=62, ieos=1, iconv=1,
+                                               noise=2.0)),
+            grid.make_member(grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=63, noise=2.0))]
+    ens = Ensemble(use_graph=True)
+    ids = [ens.add(m) for m in mems]
+    ens.step(25)
+    for m, i in zip(mems, ids):
+        ref = oracle.OracleState(m)
+        ref.step(25)
+        out = ens.download(i)
+        err = tracer_errors(m, out["ts"], ref.ts)
+        assert np.all(err[:2] <= TOL_TS), err
+        assert np.all(err <= TOL_REL), err
+        assert np.array_equal(out["cost"], ref.cost)
         assert ens.status(i) == 0
     ens.close()
 
