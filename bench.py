@@ -323,7 +323,7 @@ def run_c3(args, rank, world, local, dist):
         dist.barrier()
     t0 = time.perf_counter()
     e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
-    ids2 = [e2.add(m) for m in mems]
+    ids2 = e2.add_many(mems)
     e2.step(args.steps)
     outs = [e2.download(i) for i in ids2]
     torch.cuda.synchronize()

@@ -19,6 +19,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -64,6 +65,9 @@ struct Member {
 }  // namespace
 
 struct gb_ens {
+    // gb_ens_add may run in several host threads at once: the host preparation of a member
+    // runs unlocked, its allocation and registration under `mu`; `err_mu` guards last_error
+    std::mutex mu, err_mu;
     int device = 0;
     cudaStream_t stream = nullptr, own_stream = nullptr;
     cudaMemPool_t pool = nullptr;
@@ -95,7 +99,10 @@ struct gb_ens {
 
 static int efail(gb_ens *e, int code, const std::string &msg)
 {
-    if (e) e->last_error = msg;
+    if (e) {
+        std::lock_guard<std::mutex> lk(e->err_mu);
+        e->last_error = msg;
+    }
     return code;
 }
 
@@ -233,7 +240,6 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     for (int k = 1; k < dims->maxk; ++k)
         if (grid->dt[k] != grid->dt[0]) return efail(e, GB_GO_EUNSUPPORTED, "ensemble members need one dt for all levels");
     const size_t bytes = member_bytes(dims);
-    if (e->in_use + bytes > e->budget) return efail(e, GB_GO_ENOMEM, "member does not fit in the HBM budget");
     ETRY(e, cudaSetDevice(e->device));
 
     auto m = std::make_unique<Member>();
@@ -258,6 +264,9 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     std::vector<int32_t> scale;
     fp32_scales(m->d, grid->k1, ts, st.cmax, gtop.data(), scale);
 
+    // device allocation, copies and registration: one member at a time
+    std::lock_guard<std::mutex> lk(e->mu);
+    if (e->in_use + bytes > e->budget) return efail(e, GB_GO_ENOMEM, "member does not fit in the HBM budget");
     const size_t nts = ntop * (dims->maxk + 2);
     const size_t nrho = (size_t)m->d.NI * m->d.NJ * (dims->maxk + 1);
     const size_t ncol = (size_t)dims->maxi * dims->maxj;

@@ -939,16 +939,20 @@ int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, 
             best_ty = std::min(tile_j, maxj);
         }
     }
-    if (!best_tx) {
+    // Rectangles that split the rows and columns evenly (or nearly).  The first pass keeps
+    // to 48..256 cells: a patch holds at most 128 slots, so larger rectangles fit only on
+    // land-heavy grids, and below 48 cells the ring outweighs the interior.  A grid on
+    // which no such rectangle fits gets the full search.
+    for (int pass = 0; pass < 2 && !best_tx; ++pass) {
         double best = 1e300;
         for (int tx = maxi; tx >= 1; --tx) {
-            // widths that split the rows evenly (or nearly)
             const int nti = (maxi + tx - 1) / tx;
             if (tx != (maxi + nti - 1) / nti) continue;
             for (int ty = 1; ty <= maxj; ++ty) {
                 const int ntj = (maxj + ty - 1) / ty;
                 if (ty != (maxj + ntj - 1) / ntj) continue;
-                if (tx * ty > 4 * kFp32Threads) break;
+                if (tx * ty > (pass ? 4 : 2) * kFp32Threads) break;
+                if (pass == 0 && tx * ty < 48 && tx * ty < maxi * maxj) continue;
                 bool ok = false;
                 const double c = plan_cost(d, k1, tx, ty, cap, &ok);
                 if (ok && c < best) {

@@ -64,18 +64,45 @@ class Ensemble:
         r = GridRefs(member)
         return int(lib.gb_ens_member_bytes(C.byref(r.dims), C.byref(r.params)))
 
-    def add(self, member, steps: Optional[int] = None, **kw) -> int:
-        """Admit a member (its state ts is also the initial ts1); returns its id.
-        Raises GoldsteinError(GB_GO_ENOMEM) when it does not fit the HBM budget."""
-        r = GridRefs(member, precision=abi.GB_GO_FP32FLUX, **kw)
-        # tile shape: the one given at construction, else the autotuned one for this grid shape
+    def _tile_for(self, member):
+        """Tile shape: the one given at construction, else the autotuned one for this grid shape."""
         tile = self.tile
         if tile == (0, 0):
             from .autotune import lookup
             tile = lookup(self.table, member.maxi, member.maxj, member.maxk) or (0, 0)
+        return tile
+
+    def add(self, member, steps: Optional[int] = None, **kw) -> int:
+        """Admit a member (its state ts is also the initial ts1); returns its id.
+        Raises GoldsteinError(GB_GO_ENOMEM) when it does not fit the HBM budget."""
+        tile = self._tile_for(member)
         if tile != self._current_tile:
             self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
             self._current_tile = tile
+        return self._add_now(member, steps, **kw)
+
+    def add_many(self, members, threads: Optional[int] = None, **kw) -> list:
+        """Admit several members; their host-side preparation (patch plan, coefficients,
+        scales) runs in parallel threads, as gb_ens_add allows.  Returns the ids in order."""
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        members = list(members)
+        ids = [None] * len(members)
+        groups = {}
+        for n, m in enumerate(members):
+            groups.setdefault(self._tile_for(m), []).append(n)
+        workers = threads or min(16, os.cpu_count() or 1)
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            for tile, idx in groups.items():
+                if tile != self._current_tile:
+                    self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
+                    self._current_tile = tile
+                for n, mid in zip(idx, ex.map(lambda n: self._add_now(members[n], None, **kw), idx)):
+                    ids[n] = mid
+        return ids
+
+    def _add_now(self, member, steps, **kw) -> int:
+        r = GridRefs(member, precision=abi.GB_GO_FP32FLUX, **kw)
         ts = np.ascontiguousarray(member.ts, dtype=np.float64)
         u = np.ascontiguousarray(member.u, dtype=np.float64)
         mid = C.c_int32()

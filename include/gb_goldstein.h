@@ -218,7 +218,9 @@ size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params);
 
 /* Add a member: copies grid/params and the initial ts (full halo'd array,
  * also used as ts1), u and forcing slot; returns its id in *member_id.
- * GB_GO_ENOMEM when it does not fit in the budget. */
+ * GB_GO_ENOMEM when it does not fit in the budget.  Several host threads may call
+ * it at once (each member's host preparation runs in parallel, its device part one
+ * member at a time); no other gb_ens_* call on the ensemble may overlap them. */
 int  gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params,
                 const gb_go_grid *grid, const double *ts, const double *u,
                 int32_t *member_id);

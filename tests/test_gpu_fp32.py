@@ -242,3 +242,23 @@ def test_fp32_velocity_updates_on_device(gpu_lib, oracle):
     err = tracer_errors(m, out["ts"], ref.ts)
     assert np.all(err[:2] <= 1e-9), err
     assert np.all(err <= TOL_REL), err
+
+
+def test_ensemble_parallel_admission_equals_serial(gpu_lib):
+    """Members admitted from several host threads at once (add_many) step to the same
+    result, bit for bit, as members admitted one by one."""
+    from cgenie_gb300.ensemble import Ensemble
+    mems = [grid.make_member(c) for c in grid.ensemble_configs(n=12, seed=21)]
+    a = Ensemble(use_graph=True)
+    ids_a = [a.add(m) for m in mems]
+    b = Ensemble(use_graph=True)
+    ids_b = b.add_many(mems, threads=8)
+    assert len(set(ids_b)) == len(mems)
+    a.step(15)
+    b.step(15)
+    for ia, ib in zip(ids_a, ids_b):
+        oa, ob = a.download(ia), b.download(ib)
+        assert np.array_equal(oa["ts"], ob["ts"])
+        assert np.array_equal(oa["cost"], ob["cost"])
+    a.close()
+    b.close()
