@@ -364,7 +364,11 @@ extern "C" int gb_go_create(const gb_go_dims *dims, const gb_go_params *params, 
     h->d.NI = dims->maxi + 2; h->d.NJ = dims->maxj + 2;
     h->p = phys_from(params, grid);
     h->precision = params->precision;
-    step_fp64_tile(dims->maxk, &h->tile_i, &h->tile_j);
+    {
+        int nsm = 0;
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess || nsm < 1) nsm = 1;
+        step_fp64_tile(dims->maxi, dims->maxj, dims->maxk, nsm, &h->tile_i, &h->tile_j);
+    }
 
     const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
     const size_t ntop = (size_t)h->d.L * h->d.NI * h->d.NJ;

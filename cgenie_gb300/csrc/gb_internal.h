@@ -88,7 +88,8 @@ __host__ __device__ inline size_t rho_index(const Dims &d, int i, int j, int k)
 
 // Launchers (tstep_fp64.cu)
 int launch_step_fp64(const StepArgs &a, void *stream);
-void step_fp64_tile(int maxk, int *tile_i, int *tile_j);
+void step_fp64_tile(int maxi, int maxj, int maxk, int nsm, int *tile_i, int *tile_j);
+constexpr int kFp64TilesPerSm = 4;
 
 #ifdef __CUDACC__
 // c + n computed as n additions of 1.0 in round-to-nearest (co adds 1 to cost(i,j) per

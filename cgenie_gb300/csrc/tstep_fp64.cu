@@ -560,12 +560,23 @@ __global__ void __launch_bounds__(256) k_step_fp64(const StepArgs a)
     }
 }
 
-void step_fp64_tile(int maxk, int *tile_i, int *tile_j)
+void step_fp64_tile(int maxi, int maxj, int maxk, int nsm, int *tile_i, int *tile_j)
 {
-    if (maxk <= 8) { *tile_i = 8; *tile_j = 4; }
-    else if (maxk <= 16) { *tile_i = 4; *tile_j = 4; }
-    else if (maxk <= 32) { *tile_i = 4; *tile_j = 2; }
-    else { *tile_i = 2; *tile_j = 2; }
+    // Column tiles from large to small (one thread per cell, at most 256): the largest that
+    // still gives every SM kFp64TilesPerSm CTAs.  Larger tiles compute fewer edge faces
+    // twice; a small grid needs small tiles to occupy the GPU (one 36x36 grid of 4x4 tiles
+    // fills 81 of 152 SMs).
+    static const int cand[][2] = {{8, 4}, {4, 4}, {4, 2}, {2, 2}, {2, 1}, {1, 1}};
+    int bi = 1, bj = 1;
+    for (const auto &c : cand) {
+        if (c[0] * c[1] * maxk > 256) continue;
+        bi = c[0];
+        bj = c[1];
+        const long long tiles = (long long)((maxi + c[0] - 1) / c[0]) * ((maxj + c[1] - 1) / c[1]);
+        if (tiles >= (long long)kFp64TilesPerSm * nsm) break;
+    }
+    *tile_i = bi;
+    *tile_j = bj;
 }
 
 int launch_step_fp64(const StepArgs &a, void *stream)
