@@ -325,7 +325,7 @@ def run_c3(args, rank, world, local, dist):
     e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
     ids2 = e2.add_many(mems)
     e2.step(args.steps)
-    outs = [e2.download(i) for i in ids2]
+    outs = e2.download_many(ids2)
     torch.cuda.synchronize()
     e2e_s = job_time(time.perf_counter() - t0, dist, "cuda")
     e2.close()

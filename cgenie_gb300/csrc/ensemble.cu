@@ -578,14 +578,8 @@ __global__ void k_merge_member(double *out, const double *stat, const double *cu
     }
 }
 
-extern "C" int gb_ens_download(gb_ens *e, int32_t id, double *ts, double *rho, double *cost)
+static int download_on(gb_ens *e, Member *m, cudaStream_t s, double *ts, double *rho, double *cost)
 {
-    if (!e) return GB_GO_EINVAL;
-    auto it = e->members.find(id);
-    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
-    Member *m = it->second.get();
-    ETRY(e, cudaSetDevice(e->device));
-    cudaStream_t s = e->stream;
     double *cur = scratch_buffer(e, m);
     MemberDesc md = m->desc;
     int r = fp32_export(md, current_buffer(e, m), cur, m->rho, s);
@@ -601,6 +595,34 @@ extern "C" int gb_ens_download(gb_ens *e, int32_t id, double *ts, double *rho, d
     if (cost) ETRY(e, cudaMemcpyAsync(cost, m->cost, (size_t)m->d.maxi * m->d.maxj * 8, cudaMemcpyDeviceToHost, s));
     ETRY(e, cudaStreamSynchronize(s));
     return GB_GO_OK;
+}
+
+extern "C" int gb_ens_download(gb_ens *e, int32_t id, double *ts, double *rho, double *cost)
+{
+    if (!e) return GB_GO_EINVAL;
+    auto it = e->members.find(id);
+    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
+    ETRY(e, cudaSetDevice(e->device));
+    return download_on(e, it->second.get(), e->stream, ts, rho, cost);
+}
+
+extern "C" int gb_ens_download_stream(gb_ens *e, int32_t id, void *cuda_stream, double *ts, double *rho, double *cost)
+{
+    if (!e) return GB_GO_EINVAL;
+    auto it = e->members.find(id);
+    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
+    ETRY(e, cudaSetDevice(e->device));
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : e->stream;
+    if (s != e->stream) {
+        // after everything queued on the ensemble's stream (the steps)
+        cudaEvent_t ev;
+        ETRY(e, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t x = cudaEventRecord(ev, e->stream);
+        if (x == cudaSuccess) x = cudaStreamWaitEvent(s, ev, 0);
+        cudaEventDestroy(ev);
+        if (x != cudaSuccess) return efail(e, GB_GO_ECUDA, cudaGetErrorString(x));
+    }
+    return download_on(e, it->second.get(), s, ts, rho, cost);
 }
 
 __global__ void k_member_inventory(const double *ts, Dims d, const int32_t *k1, const double *mk, const double *rvol_unused,

@@ -28,6 +28,7 @@ class Ensemble:
         if rc != 0:
             raise GoldsteinError(rc, "gb_ens_create")
         self.e = e
+        self.device = int(device)
         self.members = {}
         self.tile = (int(tile_i), int(tile_j))
         self.use_graph = bool(use_graph)
@@ -135,6 +136,31 @@ class Ensemble:
         cost = np.empty_like(m.cost)
         self._check(self.lib.gb_ens_download(self.e, int(mid), dptr(ts), dptr(rho), dptr(cost)), "gb_ens_download")
         return dict(ts=ts, rho=rho, cost=cost)
+
+    def download_many(self, mids, threads: int = 8) -> list:
+        """download() of several members from host threads, each with its own CUDA stream
+        (gb_ens_download_stream), so that the device-to-host copies overlap."""
+        import queue
+        from concurrent.futures import ThreadPoolExecutor
+        import torch
+        mids = list(mids)
+        dev = torch.device("cuda", self.device if self.device >= 0 else torch.cuda.current_device())
+        free = queue.Queue()
+        for _ in range(threads):
+            free.put(torch.cuda.Stream(device=dev))
+
+        def one(mid):
+            m = self.members[mid]
+            ts, rho, cost = np.empty_like(m.ts), np.empty_like(m.rho), np.empty_like(m.cost)
+            st = free.get()
+            try:
+                self._check(self.lib.gb_ens_download_stream(self.e, int(mid), C.c_void_p(st.cuda_stream), dptr(ts),
+                                                            dptr(rho), dptr(cost)), "gb_ens_download_stream")
+            finally:
+                free.put(st)
+            return dict(ts=ts, rho=rho, cost=cost)
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            return list(ex.map(one, mids))
 
     def inventory(self, mid: int) -> np.ndarray:
         out = np.zeros(self.members[mid].maxl)

@@ -32,7 +32,7 @@ EXPORTED = [
     "gb_go_sync", "gb_go_errstr", "gb_go_last_error", "gb_go_kernel_launch_count",
     "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
     "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
-    "gb_ens_remaining", "gb_ens_download", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
+    "gb_ens_remaining", "gb_ens_download", "gb_ens_download_stream", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
     "gb_ens_count", "gb_ens_last_error",
 ]
 
@@ -93,6 +93,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_step_remaining.argtypes = [vp, C.c_int32]
     L.gb_ens_remaining.argtypes = [vp, C.c_int32, P(C.c_int64)]
     L.gb_ens_download.argtypes = [vp, C.c_int32, dp, dp, dp]
+    L.gb_ens_download_stream.argtypes = [vp, C.c_int32, vp, dp, dp, dp]
     L.gb_ens_inventory.argtypes = [vp, C.c_int32, dp]
     L.gb_ens_status.argtypes = [vp, C.c_int32, ip]
     L.gb_ens_sync.argtypes = [vp]

@@ -237,6 +237,12 @@ int  gb_ens_remaining(gb_ens *e, int32_t member_id, int64_t *steps);
 
 int  gb_ens_download(gb_ens *e, int32_t member_id, double *ts, double *rho,
                      double *cost);
+/* gb_ens_download on the CUDA stream `cuda_stream` (NULL = the ensemble's), ordered
+ * after the work queued on the ensemble's stream.  Several host threads may call it at
+ * once for different members, each with its own stream, so that the copies overlap; no
+ * other gb_ens_* call on the ensemble may overlap them. */
+int  gb_ens_download_stream(gb_ens *e, int32_t member_id, void *cuda_stream, double *ts,
+                            double *rho, double *cost);
 int  gb_ens_inventory(gb_ens *e, int32_t member_id, double *out);
 int  gb_ens_status(gb_ens *e, int32_t member_id, int32_t *status);
 int  gb_ens_sync(gb_ens *e);

@@ -262,3 +262,19 @@ def test_ensemble_parallel_admission_equals_serial(gpu_lib):
         assert np.array_equal(oa["cost"], ob["cost"])
     a.close()
     b.close()
+
+
+def test_ensemble_parallel_download_equals_serial(gpu_lib):
+    """download_many (host threads, one CUDA stream each, ordered after the steps) returns
+    the same arrays as download."""
+    from cgenie_gb300.ensemble import Ensemble
+    mems = [grid.make_member(c) for c in grid.ensemble_configs(n=9, seed=23)]
+    e = Ensemble(use_graph=True)
+    ids = e.add_many(mems)
+    e.step(12)
+    par = e.download_many(ids, threads=4)
+    for i, p in zip(ids, par):
+        s = e.download(i)
+        for k in ("ts", "rho", "cost"):
+            assert np.array_equal(s[k], p[k]), k
+    e.close()
