@@ -223,9 +223,9 @@ constexpr long long kNoKey = (long long)0x8000000000000000ULL;
 
 // co_rn with one warp per column: the tracers of the column are in shared memory,
 // tv[lev * 32 + l] for the wet levels, and lane l mixes and fills tracer l.  The levels
-// to merge (kk, dzm, densities in cs) are kept by lane 0; every lane runs the same
-// decisions from shared memory.  Every value and decision is the one co_rn makes.  Returns
-// the number of filled levels (in every lane).
+// to merge (kk, dzm, densities in cs) live in shared memory and are updated by lane 0;
+// every lane runs the same decisions from them.  Every value and decision is the one co_rn
+// makes.  Returns the number of filled levels (in every lane).
 // With ieos = 0 a density depends on (T, S) only, and a decision rho(a) < rho(b) is taken
 // from the double-float densities when their difference exceeds 2^-40 (M_a + M_b) (more
 // than 4x their error bound); otherwise (and for bit-equal T and S, which give equal

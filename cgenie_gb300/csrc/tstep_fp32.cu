@@ -547,13 +547,11 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             hmax = max(hmax, (unsigned)__double2hiint(tn[l]) & 0x7fffffffu);
                         }
                         *Wk = make_double2(tn[0], tn[1]);
-                        // The column needs the convective adjustment iff two consecutive wet levels
-                        // are not strictly stably stratified: the test of co (goldstein.f90:2715-2716)
-                        // on the same FP64 densities (with ieos != 0 every column is adjusted).
                         // FP32 density prescreen: a column joins the adjustment unless its densities
                         // decrease upwards by clearly more than their FP32 error at every level
                         // (the test of co, goldstein.f90:2715-2716, is then certainly passed); levels
-                        // that co mixed are equal and always join
+                        // that co mixed are equal and always join (with ieos != 0 or iconv = 1 every
+                        // column joins)
                         const float tf = d2f_scaled(tn[0], 0), sf = d2f_scaled(tn[1], 0);
                         const float e0 = ecf[0] * tf, e1 = ecf[1] * sf, e2 = ecf[2] * (tf * tf), e3 = ecf[3] * (tf * tf * tf);
                         const float rf = ((e0 + e1) + e2) + e3;
@@ -670,11 +668,13 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
-// Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step flagged
-// (every column with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  An item is
-// (member, patch table offset); each warp takes interior columns of the patch in turn and
-// adjusts a column with one lane per tracer (co_warp), the column staged in shared memory
-// (kmax: the largest maxk of the batch).  coshuffle (iconv = 1) runs on one lane.
+// Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step listed
+// (every column with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  A list
+// entry is (member, word offset of the column's record); warps take entries in turn.
+// GENERAL = false: columns of members with iconv = 0, ieos = 0, maxk <= 32, adjusted by
+// co_warp32 (one list position per lane); GENERAL = true: the others, by co_warp (the column
+// staged in shared memory, one lane per tracer; kmax: the largest maxk of the batch), with
+// coshuffle (iconv = 1) on one lane.
 template <bool GENERAL>
 __global__ void __launch_bounds__(kFp32Threads)
 k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
@@ -762,7 +762,6 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
                     if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
             }
         __syncwarp();
-        // the step stored the FP64 densities of the column (ieos = 0)
         const int filled = co_warp(tv, cs, ec, maxk, L, k1c, dz, zro, zw, lane);
         if (lane < L)
             for (int lev = k1c; lev <= maxk; ++lev) const_cast<double *>(wc)[(size_t)lev * lstride] = tv[lev * 32 + lane];
