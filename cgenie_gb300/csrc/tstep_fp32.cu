@@ -55,6 +55,19 @@ __device__ __forceinline__ float d2f_scaled(double x, int s)
     return __uint_as_float(f | (hi & 0x80000000u));
 }
 
+// d2f_scaled(x - f2d_scaled(d2f_scaled(x, s), s), s) by integer operations: the FP32
+// truncation of the 29 mantissa bits that d2f_scaled drops, scaled by 2^s (0 below the
+// FP32 normal range, like d2f_scaled).  No FP64 instruction.
+__device__ __forceinline__ float d2f_lo_scaled(double x, int s)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned r = lo & 0x1fffffffu;
+    const unsigned fb = __float_as_uint(__uint2float_rz(r));   // the top 24 bits of r, exactly
+    const int k = (int)((hi & 0x7fffffffu) >> 20) - 1075 + s;  // r counts units of 2^(E-1075)
+    const bool zero = r == 0u || (int)(fb >> 23) + k < 1;
+    return __uint_as_float(zero ? 0u : ((fb + ((unsigned)k << 23)) | (hi & 0x80000000u)));
+}
+
 // (double)f * 2^-s exactly (FP32 zero and subnormals give 0)
 __device__ __forceinline__ double f2d_scaled(float f, int s)
 {
@@ -120,7 +133,7 @@ __device__ __forceinline__ dflt df_dot2(dflt A, dflt X, dflt B, dflt Y)
 __device__ __forceinline__ dflt df_split(double x)
 {
     const float h = d2f_scaled(x, 0);
-    return {h, d2f_scaled(x - f2d_scaled(h, 0), 0)};
+    return {h, d2f_lo_scaled(x, 0)};
 }
 
 
@@ -347,7 +360,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         if (q >= gl) continue;
                         const float h = d2f_scaled(xr[q], scl[q]);
                         F[q] = h;
-                        if (ts_group && q < 2) slo[(buf * P + t) * 3 + q] = d2f_scaled(xr[q] - f2d_scaled(h, scl[q]), scl[q]);
+                        if (ts_group && q < 2) slo[(buf * P + t) * 3 + q] = d2f_lo_scaled(xr[q], scl[q]);
                     }
                 }
             };
