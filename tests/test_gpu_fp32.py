@@ -73,7 +73,9 @@ def check_against_oracle(oracle, m, steps, tol_ts=TOL_TS, tol=TOL_REL):
     (grid.MemberConfig(maxi=18, maxj=18, maxk=32, maxl=24, seed=52, tracer_kind="bgc"), 50),
     # more than 32 levels: the adjustment's serial form
     (grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=57, noise=2.0), 30),
-], ids=["c1", "l9", "odd", "deep24", "levels40"])
+    # the split-precision limits: 64 levels, 32 tracers
+    (grid.MemberConfig(maxi=10, maxj=8, maxk=64, maxl=32, seed=58, tracer_kind="bgc", noise=1.0), 10),
+], ids=["c1", "l9", "odd", "deep24", "levels40", "max_k64_l32"])
 def test_fp32_matches_oracle(gpu_lib, oracle, cfg, steps):
     check_against_oracle(oracle, grid.make_member(cfg), steps)
 
