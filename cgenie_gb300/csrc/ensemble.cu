@@ -50,6 +50,7 @@ struct Member {
     unsigned long long *diag = nullptr;   // two slots {dmax bits, limps}
     unsigned int *status = nullptr;
     int32_t *ptab = nullptr;              // patch tables
+    double *vel = nullptr, *ediff1 = nullptr, *mkd = nullptr;   // iediff: u, ediff1, dza and diffmax
     int wet_cols = 0;                     // wet columns (entries it may add to the co list)
     std::vector<int32_t> poff;            // per patch: word offset in ptab
     std::vector<double> pcost;            // per patch: cell-updates per step
@@ -114,8 +115,13 @@ static int efail(gb_ens *e, int code, const std::string &msg)
                          std::string(#call) + ": " + cudaGetErrorString(_x));                          \
     } while (0)
 
-static size_t member_bytes(const gb_go_dims *d)
+static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
 {
+    // iediff 1/2: velocities, ediff1, dza and diffmax stay on the device
+    const size_t ned = (p && p->iediff > 0 && p->iediff < 3)
+                           ? (size_t)3 * (d->maxi + 1) * (d->maxj + 1) * d->maxk + (size_t)d->maxi * d->maxj * d->maxk +
+                                 2 * ((size_t)d->maxk + 2)
+                           : 0;
     const size_t nts = (size_t)d->maxl * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     const size_t nrho = (size_t)(d->maxi + 2) * (d->maxj + 2) * (d->maxk + 1);
     const size_t ncell = (size_t)d->maxi * d->maxj * d->maxk;
@@ -124,10 +130,13 @@ static size_t member_bytes(const gb_go_dims *d)
     // and remainders), forcing, small arrays; patch tables: at most (31 + maxk) words per column
     const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
-           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + 4096;
+           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + 4096;
 }
 
-extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *) { return dims ? member_bytes(dims) : 0; }
+extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params)
+{
+    return dims ? member_bytes(dims, params) : 0;
+}
 
 extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
 {
@@ -172,7 +181,7 @@ static void free_member(gb_ens *e, Member *m)
     cudaStream_t s = e->stream;
     void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->coefl, m->gtop, m->mj,
                     m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax,
-                    m->ptab};
+                    m->ptab, m->vel, m->ediff1, m->mkd};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
 }
@@ -235,11 +244,10 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     int rc = validate_config(dims, params, grid, msg);
     if (rc) return efail(e, rc, msg);
     if (dims->maxl > kFp32MaxL) return efail(e, GB_GO_ERANGE, "ensemble members carry at most 32 tracers");
-    if (params->iediff > 0 && params->iediff < 3) return efail(e, GB_GO_EUNSUPPORTED, "iediff 1/2 not provided in ensembles");
     if (params->imld != 0) return efail(e, GB_GO_EUNSUPPORTED, "imld=1 not provided in ensembles");
     for (int k = 1; k < dims->maxk; ++k)
         if (grid->dt[k] != grid->dt[0]) return efail(e, GB_GO_EUNSUPPORTED, "ensemble members need one dt for all levels");
-    const size_t bytes = member_bytes(dims);
+    const size_t bytes = member_bytes(dims, params);
     ETRY(e, cudaSetDevice(e->device));
 
     auto m = std::make_unique<Member>();
@@ -315,6 +323,21 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = cudaMemsetAsync(m->icosd, 0, ncol * 4, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->k1, grid->k1, (size_t)m->d.NI * m->d.NJ * 4, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->scale, scale.data(), scale.size() * 4, cudaMemcpyHostToDevice, s);
+    const bool need_ediff = params->iediff > 0 && params->iediff < 3;
+    if (need_ediff) {
+        // the step rebuilds the top-face coefficients from u, ediff1, dza and diffmax
+        const size_t nu = (size_t)3 * (dims->maxi + 1) * (dims->maxj + 1) * dims->maxk;
+        const size_t ned = (size_t)dims->maxi * dims->maxj * (dims->maxk - 1);
+        const size_t nk = (size_t)dims->maxk + 2, nj = (size_t)dims->maxj + 2;
+        if (x == cudaSuccess) x = dalloc(e, &m->vel, nu);
+        if (x == cudaSuccess) x = dalloc(e, &m->ediff1, std::max<size_t>(1, ned));
+        if (x == cudaSuccess) x = dalloc(e, &m->mkd, 2 * nk);
+        if (x == cudaSuccess) x = cudaMemcpyAsync(m->vel, u, nu * 8, cudaMemcpyHostToDevice, s);
+        if (x == cudaSuccess && ned) x = cudaMemcpyAsync(m->ediff1, grid->ediff1, ned * 8, cudaMemcpyHostToDevice, s);
+        // Fortran-indexed dza, then diffmax, from the metric blob (8 j-arrays, then k-arrays)
+        if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd, blob.data() + 8 * nj + nk, nk * 8, cudaMemcpyHostToDevice, s);
+        if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd + nk, blob.data() + 8 * nj + 8 * nk, nk * 8, cudaMemcpyHostToDevice, s);
+    }
     // host staging vectors must outlive the copies
     if (x == cudaSuccess) x = cudaStreamSynchronize(s);
     if (x != cudaSuccess) {
@@ -325,6 +348,10 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     MemberDesc &md = m->desc;
     md.maxi = dims->maxi; md.maxj = dims->maxj; md.maxk = dims->maxk; md.L = dims->maxl;
     md.NI = m->d.NI; md.NJ = m->d.NJ; md.diso = m->p.diso; md.ieos = m->p.ieos; md.iconv = m->p.iconv;
+    md.iediff = m->p.iediff; md.ediffpow2i = m->p.ediffpow2i;
+    md.diff2 = m->p.diff2; md.ediff0 = m->p.ediff0; md.ediffpow2 = m->p.ediffpow2;
+    md.u = m->vel; md.ediff1 = m->ediff1;
+    md.dza = m->mkd; md.diffmax = m->mkd ? m->mkd + (dims->maxk + 2) : nullptr;
     md.dt = m->dt; md.dphi = m->p.dphi; md.rdphi = m->p.rdphi; md.diff1 = m->p.diff1;
     for (int n = 0; n < 5; ++n) md.ec[n] = m->p.ec[n];
     md.dsc = m->p.dsc;
@@ -400,7 +427,7 @@ static int rebuild(gb_ens *e)
         for (double v : m->pcost) c += v;
         order.push_back({c, m});
         max_slots = std::max(max_slots, m->max_slots);
-        any_iso = any_iso || m->desc.diso;
+        any_iso = any_iso || m->desc.diso || m->desc.iediff;
         co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->d.maxk);
         kmax = std::max(kmax, m->d.maxk);
         ++slot;

@@ -69,13 +69,20 @@ __host__ __device__ inline int fp32_planar_width(int L)
 struct MemberDesc {
     int maxi, maxj, maxk, L;
     int NI, NJ, diso, ieos;
-    int iconv, status_idx, parity, pad0;
+    int iconv, status_idx, parity, iediff;
     long long stop_step;        // the member advances while step < stop_step
     long long origin;           // step - origin = the member's own count of steps taken (while active);
                                 // its own steps 0, 4, 8, ... gather the transfer maxima for rescaling
     double dt, dphi, rdphi, diff1;
     double ec[5];
     double dsc;
+    // iediff 1/2 (local vertical diffusivity, goldstein.f90:2490-2516): the top-face
+    // coefficients of every cell are rebuilt each step from the FP64 T and S
+    double diff2, ediff0, ediffpow2;
+    int ediffpow2i, pad1;
+    const double *u;            // velocities u(3,0:maxi,0:maxj,1:maxk) (iediff)
+    const double *ediff1;       // (maxi, maxj, maxk-1) (iediff)
+    const double *dza, *diffmax;   // Fortran-indexed [0..maxk+1] (iediff)
     double *buf[2];             // state ping-pong, group-planar layout (fp32_plane)
     const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
     const float *coef;          // 8 floats per interior cell: Ae Be An Bn Aa Ba as FP32, 0, 0

@@ -426,6 +426,40 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         AeX.lo = l4.x; BeX.lo = l4.y; AnX.lo = l4.z; BnX.lo = l4.w;
                         AwX.lo = lw.x; BwX.lo = lw.y; AsX.lo = ls.x; BsX.lo = ls.y;
                     }
+                    if (ISO && md.iediff && !top) {
+                        // local vertical diffusivity (goldstein.f90:2490-2516, eosd :3064-3082): the
+                        // top-face coefficients of this cell from this step's FP64 T and S, in the
+                        // arithmetic of the static ones with diff(2) replaced by diffv
+                        auto ldv = [&](int kk, int l) {
+                            return ldg_d(R + 2 * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)kk)) + l);
+                        };
+                        const double t1 = ldv(k, 0), t2 = ldv(k + 1, 0), s1 = ldv(k, 1), s2 = ldv(k + 1, 1);
+                        const double tatw = 0.5 * (t1 + t2);
+                        double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
+                        if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
+                        const double rdza = mk[4 * mkn + k];
+                        const double dzrho = (md.ec[1] * (s2 - s1) - tec * (t2 - t1)) * rdza;
+                        const double rdzrho = dzrho < -1.0e-12 ? 1.0 / dzrho : -1.0e12;
+                        const double e1 = md.ediff1[(size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1))];
+                        double diffv;
+                        if (md.ediffpow2i == 0) diffv = md.ediff0 + e1;
+                        else if (md.ediffpow2i == 1) diffv = md.ediff0 + e1 * (-rdzrho);
+                        else if (md.ediffpow2i == 2) diffv = md.ediff0 + e1 * sqrt(-rdzrho);
+                        else diffv = md.ediff0 + e1 * pow(-rdzrho, md.ediffpow2);
+                        if (diffv > md.diffmax[k + 1]) diffv = md.diffmax[k + 1];
+                        const double u3 = md.u[2 + 3 * ((size_t)i + (size_t)(maxi + 1) * ((size_t)j + (size_t)(maxj + 1) * (size_t)(k - 1)))];
+                        const double pec = u3 * md.dza[k] / diffv, ups = pec / (2.0 + fabs(pec));
+                        const double g = mj[2 * mjn + j];   // dt*dphi*ds(j)
+                        const double c1 = g * (u3 * (1.0 - ups) * 0.5 - rdza * diffv);
+                        const double c0 = g * (u3 * (1.0 + ups) * 0.5 + rdza * diffv);
+                        if (ts_group) {
+                            C1X = df_split(c1);
+                            C0X = df_split(c0);
+                        } else {
+                            C1X = {d2f_scaled(c1, 0), 0.f};
+                            C0X = {d2f_scaled(c0, 0), 0.f};
+                        }
+                    }
                     if (ISO && md.diso && !top) {
                         // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
                         // state: the density differences scc*dS - tec*dT cancel strongly in weakly
@@ -1065,7 +1099,7 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
                  *ds = b + 6 * nj;
     const double *kb = b + 8 * nj;
     const double *dz = kb, *dza = kb + nk, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk,
-                 *dt = kb + 5 * nk, *zw = kb + 6 * nk, *ssmax = kb + 7 * nk;
+                 *dt = kb + 5 * nk, *zw = kb + 6 * nk, *ssmax = kb + 7 * nk, *diffmax = kb + 8 * nk;
     const size_t ncell = (size_t)maxi * maxj * maxk;
     out.coef.assign(8 * ncell, 0.0f);
     out.coefl.assign(8 * ncell, 0.0f);
@@ -1105,6 +1139,12 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
                     const double g = dt[k] * p.dphi * ds[j];
                     cd[4] = g * (u3 * (1.0 - ups) * 0.5 - rdza[k] * p.diff2);
                     cd[5] = g * (u3 * (1.0 + ups) * 0.5 + rdza[k] * p.diff2);
+                    if (p.iediff > 0 && p.iediff < 3) {
+                        // the step rebuilds these with diffv <= diffmax(k+1): bound the initial
+                        // fixed-point scales with the larger diffusivity
+                        const double dv = std::max(p.diff2, diffmax[k + 1]);
+                        out.cmax = std::max(out.cmax, g * (std::fabs(u3) + 2.0 * rdza[k] * dv));
+                    }
                 }
                 // Ae Be An Bn Aa Ba 0 0 as FP32, and their FP64 remainders in the same order
                 for (int n = 0; n < 6; ++n) {
@@ -1351,6 +1391,8 @@ struct Fp32Host {
     std::vector<int32_t> k1;
     std::vector<double> ts1_host;     // state used to pick the transfer scales
     const int32_t *k1_dev = nullptr;
+    Metrics m{};                      // the handle's device metrics (iediff reads dza, diffmax, ediff1)
+    const double *u_dev = nullptr;    // the handle's device velocities (iediff)
     bool have_state = false, have_vel = false;
     double dt = 0.0;
 };
@@ -1364,10 +1406,6 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     }
     if (p.imld != 0) {
         msg = "GB_GO_FP32FLUX does not provide imld=1 (use GB_GO_FP64)";
-        return GB_GO_EUNSUPPORTED;
-    }
-    if (p.iediff != 0) {
-        msg = "GB_GO_FP32FLUX does not provide iediff 1/2 (use GB_GO_FP64)";
         return GB_GO_EUNSUPPORTED;
     }
     const int nj = d.maxj + 2, nk = d.maxk + 2;
@@ -1392,6 +1430,7 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     h->blob = blob;
     h->k1.assign(k1_host, k1_host + (size_t)d.NI * d.NJ);
     h->k1_dev = m.k1;
+    h->m = m;
     h->dt = dtp[1];
     Fp32Data &D = h->data;
     D.max_slots = plan.max_slots;
@@ -1507,6 +1546,7 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, const double *
                               cudaStream_t s)
 {
     Fp32Host *h = host_of(f);
+    if (u_dev) h->u_dev = u_dev;
     if (h->have_vel && u_dev) {
         // later velocity fields: coefficients on the device; the fixed-point scales follow
         // through the rescaling of the steps
@@ -1545,6 +1585,9 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         MemberDesc &md = D.host;
         md.maxi = h->d.maxi; md.maxj = h->d.maxj; md.maxk = h->d.maxk; md.L = h->d.L; md.NI = h->d.NI; md.NJ = h->d.NJ;
         md.diso = h->p.diso; md.ieos = h->p.ieos; md.iconv = h->p.iconv;
+        md.iediff = h->p.iediff; md.ediffpow2i = h->p.ediffpow2i;
+        md.diff2 = h->p.diff2; md.ediff0 = h->p.ediff0; md.ediffpow2 = h->p.ediffpow2;
+        md.u = h->u_dev; md.ediff1 = h->m.ediff1; md.dza = h->m.dza; md.diffmax = h->m.diffmax;
         md.parity = 0;
         md.stop_step = (long long)1 << 62;
         md.origin = 0;
@@ -1582,7 +1625,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         bt.colist = D.colist;
         bt.cocount = D.cocount;
         bt.cocap = D.cocap;
-        bt.iso = h->p.diso != 0;
+        bt.iso = h->p.diso != 0 || h->p.iediff != 0;
         bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->d.maxk);
         int r = D.nitems ? fp32_launch(bt, D.step_ctr, n, s, D.s2, D.fork, D.join) : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);

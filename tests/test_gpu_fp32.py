@@ -88,6 +88,19 @@ def test_fp32_isoneutral_matches_oracle(gpu_lib, oracle, cfg, steps):
     check_against_oracle(oracle, grid.make_member(cfg), steps, tol_ts=1e-9)
 
 
+@pytest.mark.parametrize("cfg", [
+    grid.MemberConfig(maxi=18, maxj=18, maxk=16, maxl=4, seed=91, iediff=1, ediffpow2=1.0, tracer_kind="bgc"),
+    grid.MemberConfig(maxi=18, maxj=14, maxk=12, maxl=3, seed=92, iediff=2, ediffpow2=0.5, diso=True,
+                      slope_max=1e-3),
+    grid.MemberConfig(maxi=15, maxj=12, maxk=10, maxl=5, seed=93, iediff=1, ediffpow2=0.0, ieos=1, noise=1.0),
+    grid.MemberConfig(maxi=15, maxj=12, maxk=10, maxl=3, seed=94, iediff=1, ediffpow2=0.7),
+], ids=["pow1", "pow05_diso", "pow0_ieos", "pow07"])
+def test_fp32_local_vertical_diffusivity(gpu_lib, oracle, cfg):
+    """iediff 1/2 (goldstein.f90:2490-2516): the split-precision step rebuilds each cell's
+    top-face coefficients from the step's FP64 T and S; within the FP32-flux bars."""
+    check_against_oracle(oracle, grid.make_member(cfg), 40, tol_ts=1e-9)
+
+
 def test_fp32_config2_1000_steps(gpu_lib, oracle):
     """Config 2 (36x36x16, 17 tracers, isoneutral) for its full 1000 steps."""
     err = check_against_oracle(oracle, grid.make_member(grid.config_c2()), 1000, tol_ts=1e-9)
@@ -173,13 +186,16 @@ def test_ensemble_matches_oracle_per_member(gpu_lib, oracle):
 
 def test_ensemble_mixed_adjustment_forms(gpu_lib, oracle):
     """One batch with members of both adjustment forms: warp-parallel (ieos = 0,
-    iconv = 0, maxk <= 32) and serial (ieos = 1 with coshuffle; 40 levels)."""
+    iconv = 0, maxk <= 32) and serial (ieos = 1 with coshuffle; 40 levels), and a member
+    with the local vertical diffusivity (iediff = 1)."""
     from cgenie_gb300.ensemble import Ensemble
     mems = [grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=16, maxl=5, seed=61, noise=2.0,
                                                tracer_kind="bgc")),
             grid.make_member(grid.MemberConfig(maxi=15, maxj=12, maxk=10, maxl=3, seed=62, ieos=1, iconv=1,
                                                noise=2.0)),
-            grid.make_member(grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=63, noise=2.0))]
+            grid.make_member(grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=63, noise=2.0)),
+            grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=16, maxl=4, seed=64, iediff=1,
+                                               ediffpow2=1.0, tracer_kind="bgc"))]
     ens = Ensemble(use_graph=True)
     ids = [ens.add(m) for m in mems]
     ens.step(25)
