@@ -21,13 +21,16 @@ TABLE_PATH = os.path.join(HERE, "tuning.json")
 
 Shape = Tuple[int, int, int]
 
+# a tuned tile replaces the planner's only when it is faster by more than run-to-run noise
+NOISE = 1.02
+
 
 def candidates(maxi: int, maxj: int):
-    """Tile shapes worth timing: whole-row tiles, near-square tiles and the
-    default cost-model choice, all with 64..128 threads."""
+    """Tile shapes worth timing: the patch planner's own choice, written (0, 0), then
+    whole-row and near-square tiles of 64..128 columns."""
     out = set()
-    for tx in range(4, 65):
-        for ty in range(1, 33):
+    for tx in range(4, min(64, maxi) + 1):
+        for ty in range(1, min(32, maxj) + 1):
             n = tx * ty
             if n < 64 or n > 128:
                 continue
@@ -42,7 +45,7 @@ def candidates(maxi: int, maxj: int):
         tx, ty = t
         nti, ntj = -(-maxi // tx), -(-maxj // ty)
         return nti * ntj * (tx + 2) * (ty + 2) + 0.5 * (nti * ntj * tx * ty - maxi * maxj)
-    return sorted(out, key=cost)[:8]
+    return [(0, 0)] + sorted(out, key=cost)[:8]
 
 
 def load_table(path: str = TABLE_PATH) -> Dict[str, list]:
@@ -58,48 +61,60 @@ def lookup(table: Dict[str, list], maxi: int, maxj: int, maxk: int) -> Optional[
     return (int(v[0]), int(v[1])) if v else None
 
 
-def time_shape(shape: Shape, tile: Tuple[int, int], members: int = 48, steps: int = 10, seed: int = 5,
-               lmean: int = 13) -> float:
-    """Tracer cell-updates/s of the batched kernel for `members` copies of one shape."""
+def make_members(shape: Shape, members: int = 64, seed: int = 5):
+    """Seeded members of one grid shape with 2-24 tracers (the ensemble's mix)."""
     import numpy as np
-    import torch
     from . import grid
-    from .ensemble import Ensemble
     rng = np.random.default_rng(seed)
-    mems = []
-    for n in range(members):
-        cfg = grid.MemberConfig(maxi=shape[0], maxj=shape[1], maxk=shape[2], maxl=int(rng.integers(2, 25)),
-                                seed=int(rng.integers(0, 2**31 - 1)), tracer_kind="bgc")
-        mems.append(grid.make_member(cfg))
-    ens = Ensemble(tile_i=tile[0], tile_j=tile[1])
-    for m in mems:
-        ens.add(m)
-    ens.step(3)
+    return [grid.make_member(grid.MemberConfig(maxi=shape[0], maxj=shape[1], maxk=shape[2],
+                                               maxl=int(rng.integers(2, 25)), seed=int(rng.integers(0, 2**31 - 1)),
+                                               tracer_kind="bgc"))
+            for _ in range(members)]
+
+
+def time_shape(mems, tile: Tuple[int, int], steps: int = 30) -> float:
+    """Tracer cell-updates/s of the batched step (CUDA graph) on `mems` with one tile shape;
+    0 when the shape does not fit the kernel limits on some member."""
+    from .ensemble import Ensemble
+    ens = Ensemble(tile_i=tile[0], tile_j=tile[1], use_graph=True, use_table=False)
+    try:
+        ens.add_many(mems)
+    except Exception:
+        ens.close()
+        return 0.0
+    ens.step(steps)     # capture the graph, warm up
     ens.sync()
-    s = torch.cuda.Event(enable_timing=True)
-    e = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     ens.step(steps)
     ens.sync()
     dt = time.perf_counter() - t0
     cu = sum(m.wet_cells * m.maxl for m in mems) * steps
     ens.close()
-    del s, e
     return cu / dt
 
 
-def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), members: int = 48,
-         steps: int = 10, path: str = TABLE_PATH, verbose: bool = True) -> Dict[str, list]:
+def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), members: int = 64,
+         steps: int = 30, path: str = TABLE_PATH, verbose: bool = True) -> Dict[str, list]:
+    """Time every candidate tile of each shape (the planner's choice included) and store the
+    shapes whose best tile beats the planner's."""
     table = load_table(path)
     for shape in shapes:
+        mems = make_members(shape, members)
         best = None
+        rates = []
         for tile in candidates(shape[0], shape[1]):
-            rate = time_shape(shape, tile, members=members, steps=steps)
+            rate = time_shape(mems, tile, steps=steps)
+            rates.append((tile, rate))
             if verbose:
                 print(f"{shape} tile {tile}: {rate:.3e} cell-updates/s", flush=True)
             if best is None or rate > best[1]:
                 best = (tile, rate)
-        table[f"{shape[0]}x{shape[1]}x{shape[2]}"] = [best[0][0], best[0][1], best[1]]
+        key = f"{shape[0]}x{shape[1]}x{shape[2]}"
+        planner = next(r for t, r in rates if t == (0, 0))
+        if best[0] == (0, 0) or best[1] < NOISE * planner:
+            table.pop(key, None)     # the planner's choice is as good: no entry
+        else:
+            table[key] = [best[0][0], best[0][1], best[1]]
         if verbose:
             print(f"{shape}: best tile {best[0]} ({best[1]:.3e})", flush=True)
     with open(path, "w") as f:

@@ -21,7 +21,7 @@ from .goldstein import GoldsteinError, load_library
 
 class Ensemble:
     def __init__(self, device: int = -1, hbm_budget_bytes: int = 0, *, tile_i: int = 0, tile_j: int = 0,
-                 use_graph: bool = False, stream: Optional[int] = None):
+                 use_graph: bool = False, stream: Optional[int] = None, use_table: bool = True):
         self.lib = load_library()
         e = C.c_void_p()
         rc = self.lib.gb_ens_create(int(device), C.c_size_t(hbm_budget_bytes), C.byref(e))
@@ -34,7 +34,7 @@ class Ensemble:
         self.use_graph = bool(use_graph)
         self._current_tile = None
         from .autotune import load_table
-        self.table = load_table()
+        self.table = load_table() if use_table else {}
         self.set_tuning(tile_i=tile_i, tile_j=tile_j, use_graph=use_graph)
         if stream is not None:
             self._check(self.lib.gb_ens_set_stream(self.e, C.c_void_p(stream)), "gb_ens_set_stream")

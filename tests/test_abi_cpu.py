@@ -51,3 +51,13 @@ def test_oracle_header_cites_reference():
     assert "ORACLE -- test infrastructure only" in src
     assert "goldstein.f90:2436-2642" in src
     assert "parity unpinned" in src
+
+
+def test_autotune_candidates_start_with_planner_choice():
+    from cgenie_gb300 import autotune
+    for shape in [(18, 18), (36, 36), (37, 23)]:
+        c = autotune.candidates(*shape)
+        assert c[0] == (0, 0)
+        assert all(64 <= tx * ty <= 128 for tx, ty in c[1:])
+    assert autotune.lookup({"36x36x16": [12, 9, 1.0]}, 36, 36, 16) == (12, 9)
+    assert autotune.lookup({}, 36, 36, 16) is None
