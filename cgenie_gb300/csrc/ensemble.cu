@@ -51,6 +51,7 @@ struct Member {
     unsigned int *status = nullptr;
     int32_t *ptab = nullptr;              // patch tables
     double *vel = nullptr, *ediff1 = nullptr, *mkd = nullptr;   // iediff: u, ediff1, dza and diffmax
+    float *stencil = nullptr;             // diso or iediff: the per-step top-face stencil
     int wet_cols = 0;                     // wet columns (entries it may add to the co list)
     std::vector<int32_t> poff;            // per patch: word offset in ptab
     std::vector<double> pcost;            // per patch: cell-updates per step
@@ -86,6 +87,8 @@ struct gb_ens {
     int max_slots = 1;
     bool any_iso = false;               // some member has the isoneutral branch
     bool co_general = false;            // some member needs the serial adjustment
+    int *stencil_list = nullptr;        // device: descriptor slots of the members with a stencil
+    int cap_stencil = 0, n_stencil = 0, stencil_blocks = 1;
     int kmax = 1;                       // largest maxk of the members
     int2 *colist = nullptr;             // columns listed for the exact convective adjustment
     int *cocount = nullptr;             // two counters, by step parity
@@ -115,6 +118,8 @@ static int efail(gb_ens *e, int code, const std::string &msg)
                          std::string(#call) + ": " + cudaGetErrorString(_x));                          \
     } while (0)
 
+static bool has_stencil(const gb_go_params *p) { return p && (p->diso || (p->iediff > 0 && p->iediff < 3)); }
+
 static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
 {
     // iediff 1/2: velocities, ediff1, dza and diffmax stay on the device
@@ -122,6 +127,8 @@ static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
                            ? (size_t)3 * (d->maxi + 1) * (d->maxj + 1) * d->maxk + (size_t)d->maxi * d->maxj * d->maxk +
                                  2 * ((size_t)d->maxk + 2)
                            : 0;
+    // diso or iediff: the per-step top-face stencil
+    const size_t nst = has_stencil(p) ? (size_t)kStencilWords * d->maxi * d->maxj * d->maxk : 0;
     const size_t nts = (size_t)d->maxl * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     const size_t nrho = (size_t)(d->maxi + 2) * (d->maxj + 2) * (d->maxk + 1);
     const size_t ncell = (size_t)d->maxi * d->maxj * d->maxk;
@@ -130,7 +137,7 @@ static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
     // and remainders), forcing, small arrays; patch tables: at most (31 + maxk) words per column
     const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
-           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + 4096;
+           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + 4096;
 }
 
 extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params)
@@ -181,7 +188,7 @@ static void free_member(gb_ens *e, Member *m)
     cudaStream_t s = e->stream;
     void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->coefl, m->gtop, m->mj,
                     m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax,
-                    m->ptab, m->vel, m->ediff1, m->mkd};
+                    m->ptab, m->vel, m->ediff1, m->mkd, m->stencil};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
 }
@@ -201,6 +208,7 @@ extern "C" void gb_ens_destroy(gb_ens *e)
     if (e->join) cudaEventDestroy(e->join);
     cudaFree(e->cocount);
     cudaFree(e->colist);
+    cudaFree(e->stencil_list);
     cudaFree(e->descs);
     cudaFree(e->items);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
@@ -338,6 +346,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
         if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd, blob.data() + 8 * nj + nk, nk * 8, cudaMemcpyHostToDevice, s);
         if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd + nk, blob.data() + 8 * nj + 8 * nk, nk * 8, cudaMemcpyHostToDevice, s);
     }
+    if (x == cudaSuccess && has_stencil(params)) x = dalloc(e, &m->stencil, (size_t)kStencilWords * dims->maxi * dims->maxj * dims->maxk);
     // host staging vectors must outlive the copies
     if (x == cudaSuccess) x = cudaStreamSynchronize(s);
     if (x != cudaSuccess) {
@@ -352,6 +361,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.diff2 = m->p.diff2; md.ediff0 = m->p.ediff0; md.ediffpow2 = m->p.ediffpow2;
     md.u = m->vel; md.ediff1 = m->ediff1;
     md.dza = m->mkd; md.diffmax = m->mkd ? m->mkd + (dims->maxk + 2) : nullptr;
+    md.stencil = m->stencil;
     md.dt = m->dt; md.dphi = m->p.dphi; md.rdphi = m->p.rdphi; md.diff1 = m->p.diff1;
     for (int n = 0; n < 5; ++n) md.ec[n] = m->p.ec[n];
     md.dsc = m->p.dsc;
@@ -414,6 +424,8 @@ static int rebuild(gb_ens *e)
     bool any_iso = false, co_general = false;
     int kmax = 1;
     int slot = 0;
+    std::vector<int> slist;   // members with a stencil
+    int sblocks = 1;
     for (auto &kv : e->members) {
         Member *m = kv.second.get();
         // keep each member's status word and diag slots across rebuilds by
@@ -428,6 +440,10 @@ static int rebuild(gb_ens *e)
         order.push_back({c, m});
         max_slots = std::max(max_slots, m->max_slots);
         any_iso = any_iso || m->desc.diso || m->desc.iediff;
+        if (m->stencil) {
+            slist.push_back(slot);
+            sblocks = std::max(sblocks, fp32_stencil_blocks((size_t)m->d.maxi * m->d.maxj * m->d.maxk));
+        }
         co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->d.maxk);
         kmax = std::max(kmax, m->d.maxk);
         ++slot;
@@ -452,6 +468,15 @@ static int rebuild(gb_ens *e)
         ETRY(e, cudaMallocAsync(&e->items, (size_t)cap * sizeof(int4), s));
         e->cap_items = cap;
     }
+    if ((int)slist.size() > e->cap_stencil) {
+        int cap = std::max(64, (int)(2 * slist.size()));
+        if (e->stencil_list) cudaFreeAsync(e->stencil_list, s);
+        e->stencil_list = nullptr;
+        ETRY(e, cudaMallocAsync(&e->stencil_list, (size_t)cap * sizeof(int), s));
+        e->cap_stencil = cap;
+    }
+    if (!slist.empty())
+        ETRY(e, cudaMemcpyAsync(e->stencil_list, slist.data(), slist.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     if (!descs.empty()) ETRY(e, cudaMemcpyAsync(e->descs, descs.data(), descs.size() * sizeof(MemberDesc), cudaMemcpyHostToDevice, s));
     if (!it.empty()) ETRY(e, cudaMemcpyAsync(e->items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
     ETRY(e, cudaStreamSynchronize(s));
@@ -466,6 +491,8 @@ static int rebuild(gb_ens *e)
     e->max_slots = max_slots;
     e->any_iso = any_iso;
     e->co_general = co_general;
+    e->n_stencil = (int)slist.size();
+    e->stencil_blocks = sblocks;
     e->kmax = kmax;
     e->dirty = false;
     if (e->graph) {
@@ -490,6 +517,9 @@ static Fp32Batch batch_of(gb_ens *e)
     b.cocap = e->cocap;
     b.iso = e->any_iso;
     b.co_general = e->co_general;
+    b.stencil_list = e->stencil_list;
+    b.n_stencil = e->n_stencil;
+    b.stencil_blocks = e->stencil_blocks;
     return b;
 }
 

@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -65,6 +66,11 @@ __host__ __device__ inline int fp32_planar_width(int L)
     return pl + gp;
 }
 
+// Top-face stencil words per cell: the hi parts of C1 C0 W0 E0 S0 N0 W1 E1 S1 N1 (the weights of
+// T(k+1), T(k) and of T at the W, E, S, N neighbours of levels k and k+1), the isoneutral flag, 0,
+// then the lo parts in the same order, 0, 0.
+constexpr int kStencilWords = 24;
+
 // Per-member descriptor read by the batched kernel (device memory).
 struct MemberDesc {
     int maxi, maxj, maxk, L;
@@ -83,6 +89,8 @@ struct MemberDesc {
     const double *u;            // velocities u(3,0:maxi,0:maxj,1:maxk) (iediff)
     const double *ediff1;       // (maxi, maxj, maxk-1) (iediff)
     const double *dza, *diffmax;   // Fortran-indexed [0..maxk+1] (iediff)
+    float *stencil;             // diso or iediff: kStencilWords floats per interior cell (index as coef),
+                                // the top-face stencil rebuilt every step by k_stencil_fp32
     double *buf[2];             // state ping-pong, group-planar layout (fp32_plane)
     const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
     const float *coef;          // 8 floats per interior cell: Ae Be An Bn Aa Ba as FP32, 0, 0
@@ -118,6 +126,8 @@ struct Fp32Data {
     double *mk = nullptr, *mj = nullptr;
     unsigned int *status = nullptr;
     unsigned long long *diag = nullptr;
+    float *stencil = nullptr;   // diso or iediff: the per-step top-face stencil (kStencilWords per cell)
+    int *stencil_list = nullptr;   // {0}: the member's descriptor index for the prepass when stepped alone
     int4 *items = nullptr;      // work items when stepped alone: (0, patch, group)
     int nitems = 0;
     int2 *colist = nullptr;     // columns for the exact convective adjustment (capacity cocap)
@@ -192,6 +202,8 @@ struct PatchPlan {
 // tile_i/tile_j > 0 ask for that rectangle (if within the kernel limits), else the cheapest one
 int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, PatchPlan &plan);
 int fp32_group_count(int L);   // tracer groups (work items per patch): T and S, then groups of <= 8
+// blocks per member of the stencil prepass for a grid of `ncell` interior cells
+inline int fp32_stencil_blocks(size_t ncell) { return (int)std::min<size_t>(64, (ncell + 255) / 256); }
 // Fortran layout (L, NI, NJ, maxk+2) <-> group-planar layout of the FP32-flux state
 int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s);
 int fp32_from_planar(double *fortran, const double *planar, const Dims &d, cudaStream_t s);
@@ -213,6 +225,8 @@ struct Fp32Batch {
     int cocap = 0;
     bool iso = false;
     bool co_general = false;   // some member has iconv = 1, ieos != 0 or maxk > 32
+    const int *stencil_list = nullptr;   // descriptor indices of the members with a stencil
+    int n_stencil = 0, stencil_blocks = 1;   // their count; blocks per member of the prepass
 };
 // s2/fork/join: a second stream and two events to run the two item kinds side by side
 // (s2 null: one stream).

@@ -323,8 +323,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         bool unstable = false;
         float gmax = 0.0f;
         unsigned hmax = 0u;
-        double dmax_l = 0.0;
-        unsigned limps_l = 0;
 
         {
             int g0, gl, gp, plane;
@@ -414,9 +412,8 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     dflt W1X = {0.f, 0.f}, E1X = {0.f, 0.f}, S1X = {0.f, 0.f}, N1X = {0.f, 0.f};
                     dflt AeX = {a4.x, 0.f}, BeX = {a4.y, 0.f}, AnX = {a4.z, 0.f}, BnX = {a4.w, 0.f};
                     dflt AwX = {w2.x, 0.f}, BwX = {w2.y, 0.f}, AsX = {s2.x, 0.f}, BsX = {s2.y, 0.f};
-                    if (ts_group || (ISO && md.diso && !top)) {
-                        // lo parts of the coefficients (T and S use the FP32 pair; the isoneutral
-                        // stencil is built from the FP64 coefficient)
+                    if (ts_group) {
+                        // lo parts of the coefficients (T and S use the FP32 pairs)
                         const float4 l4 = __ldg(reinterpret_cast<const float4 *>(cfl));      // lo Ae Be An Bn
                         const float2 l2 = __ldg(reinterpret_cast<const float2 *>(cfl + 4));  // lo Aa Ba
                         const float2 lw = __ldg(reinterpret_cast<const float2 *>(md.coefl + cwi));
@@ -426,128 +423,20 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         AeX.lo = l4.x; BeX.lo = l4.y; AnX.lo = l4.z; BnX.lo = l4.w;
                         AwX.lo = lw.x; BwX.lo = lw.y; AsX.lo = ls.x; BsX.lo = ls.y;
                     }
-                    if (ISO && md.iediff && !top) {
-                        // local vertical diffusivity (goldstein.f90:2490-2516, eosd :3064-3082): the
-                        // top-face coefficients of this cell from this step's FP64 T and S, in the
-                        // arithmetic of the static ones with diff(2) replaced by diffv
-                        auto ldv = [&](int kk, int l) {
-                            return ldg_d(R + 2 * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (size_t)kk)) + l);
-                        };
-                        const double t1 = ldv(k, 0), t2 = ldv(k + 1, 0), s1 = ldv(k, 1), s2 = ldv(k + 1, 1);
-                        const double tatw = 0.5 * (t1 + t2);
-                        double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
-                        if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
-                        const double rdza = mk[4 * mkn + k];
-                        const double dzrho = (md.ec[1] * (s2 - s1) - tec * (t2 - t1)) * rdza;
-                        const double rdzrho = dzrho < -1.0e-12 ? 1.0 / dzrho : -1.0e12;
-                        const double e1 = md.ediff1[(size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1))];
-                        double diffv;
-                        if (md.ediffpow2i == 0) diffv = md.ediff0 + e1;
-                        else if (md.ediffpow2i == 1) diffv = md.ediff0 + e1 * (-rdzrho);
-                        else if (md.ediffpow2i == 2) diffv = md.ediff0 + e1 * sqrt(-rdzrho);
-                        else diffv = md.ediff0 + e1 * pow(-rdzrho, md.ediffpow2);
-                        if (diffv > md.diffmax[k + 1]) diffv = md.diffmax[k + 1];
-                        const double u3 = md.u[2 + 3 * ((size_t)i + (size_t)(maxi + 1) * ((size_t)j + (size_t)(maxj + 1) * (size_t)(k - 1)))];
-                        const double pec = u3 * md.dza[k] / diffv, ups = pec / (2.0 + fabs(pec));
-                        const double g = mj[2 * mjn + j];   // dt*dphi*ds(j)
-                        const double c1 = g * (u3 * (1.0 - ups) * 0.5 - rdza * diffv);
-                        const double c0 = g * (u3 * (1.0 + ups) * 0.5 + rdza * diffv);
+                    if (ISO && md.stencil && !top) {
+                        // the cell's top-face stencil from this step's prepass (k_stencil_fp32):
+                        // C1 C0 W0 E0 S0 N0 W1 E1 S1 N1 as FP32 pairs and the isoneutral flag
+                        const float4 *sp = reinterpret_cast<const float4 *>(md.stencil + (size_t)kStencilWords * cl);
+                        const float4 h0 = __ldg(sp), h1 = __ldg(sp + 1), h2 = __ldg(sp + 2);
+                        C1X = {h0.x, 0.f}; C0X = {h0.y, 0.f}; W0X = {h0.z, 0.f}; E0X = {h0.w, 0.f};
+                        S0X = {h1.x, 0.f}; N0X = {h1.y, 0.f}; W1X = {h1.z, 0.f}; E1X = {h1.w, 0.f};
+                        S1X = {h2.x, 0.f}; N1X = {h2.y, 0.f};
+                        iso = h2.z != 0.f;
                         if (ts_group) {
-                            C1X = df_split(c1);
-                            C0X = df_split(c0);
-                        } else {
-                            C1X = {d2f_scaled(c1, 0), 0.f};
-                            C0X = {d2f_scaled(c0, 0), 0.f};
-                        }
-                    }
-                    if (ISO && md.diso && !top) {
-                        // isoneutral coefficients (goldstein.f90:2561-2624) in FP64 from the FP64
-                        // state: the density differences scc*dS - tec*dT cancel strongly in weakly
-                        // stratified water; they are differences of D = ec(2)*S - tec*T with the
-                        // cell's tec (goldstein.f90:2587-2588)
-                        // T and S are plane 0 of the group-planar state, two values per cell
-                        auto ld = [&](int ii, int jj, int kk, int l) {
-                            return ldg_d(R + 2 * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
-                        };
-                        const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
-                        const double s1 = ld(i, j, k, 1), s2v = ld(i, j, k + 1, 1);
-                        const double tatw = 0.5 * (t1 + t2);
-                        double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
-                        if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
-                        const double scc = md.ec[1];
-                        const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2v - tec * t2;
-                        const double rdza = mk[4 * mkn + k];
-                        const double dzrho = (Dc1 - Dc0) * rdza;
-                        if (dzrho < -1.0e-12) {
-                            iso = true;
-                            const double rdzrho = 1.0 / dzrho;
-                            const double rcr = mj[j];                                 // rc(j)*rdphi
-                            const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
-                            const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
-                            const int k1E = k1nb & 0xff, k1W = (k1nb >> 8) & 0xff, k1N = (k1nb >> 16) & 0xff,
-                                      k1S = (k1nb >> 24) & 0xff;
-                            double dxr[4], dyr[4], mx[4], my[4];
-                            double tv1 = 0.0;
-#pragma unroll
-                            for (int knp = 0; knp <= 1; ++knp) {
-                                const double Dck = knp ? Dc1 : Dc0;
-#pragma unroll
-                                for (int nnp = 0; nnp <= 1; ++nnp) {
-                                    const int ina = nnp + 2 * knp;
-                                    const int kk = k + knp;
-                                    const bool okx = kk >= (nnp ? k1E : k1W);
-                                    const bool oky = kk >= (nnp ? k1N : k1S);
-                                    mx[ina] = okx ? rcr : 0.0;
-                                    my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
-                                    dxr[ina] = 0.0;
-                                    dyr[ina] = 0.0;
-                                    if (okx) {
-                                        const int ii = nnp ? ip : im;
-                                        const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
-                                        dxr[ina] = (nnp ? Dn - Dck : Dck - Dn) * rcr;
-                                    }
-                                    if (oky) {
-                                        const int jj = nnp ? j + 1 : j - 1;
-                                        const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
-                                        dyr[ina] = (nnp ? Dn - Dck : Dck - Dn) * my[ina];
-                                    }
-                                    tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
-                                }
-                            }
-                            const double sum2 = tv1;
-                            tv1 = 0.25 * tv1 * rdzrho * rdzrho;
-                            const double ss = mk[5 * mkn + k];
-                            double slim = 1.0;
-                            if (tv1 > ss) {
-                                slim = ss * ss / (tv1 * tv1);
-                                if (ts_group) limps_l += 1;
-                            }
-                            if (ts_group) dmax_l = fmax(dmax_l, tv1 * slim * md.diff1 * rdza * md.dt * rdza);
-                            // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
-                            const double c0 = mj[2 * mjn + j] * 0.25 * slim * md.diff1 * rdzrho * rdzrho;
-                            const double two_dz = 2.0 * dzrho * c0;
-                            double wx[4], wy[4];
-#pragma unroll
-                            for (int n = 0; n < 4; ++n) {
-                                wx[n] = two_dz * dxr[n] * mx[n];
-                                wy[n] = two_dz * dyr[n] * my[n];
-                            }
-                            const double wz = -c0 * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
-                            const double c0d = f2d_scaled(C0X.hi, 0) + f2d_scaled(C0X.lo, 0) + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
-                            const double c1d = f2d_scaled(C1X.hi, 0) + f2d_scaled(C1X.lo, 0) + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
-                            if (ts_group) {
-                                C0X = df_split(c0d);
-                                C1X = df_split(c1d);
-                                W0X = df_split(-wx[0]); E0X = df_split(wx[1]); W1X = df_split(-wx[2]); E1X = df_split(wx[3]);
-                                S0X = df_split(-wy[0]); N0X = df_split(wy[1]); S1X = df_split(-wy[2]); N1X = df_split(wy[3]);
-                            } else {
-                                // the other tracers use the FP32 part only (the FP32 part of the pair)
-                                C0X.hi = d2f_scaled(c0d, 0); C1X.hi = d2f_scaled(c1d, 0);
-                                W0X.hi = d2f_scaled(-wx[0], 0); E0X.hi = d2f_scaled(wx[1], 0);
-                                W1X.hi = d2f_scaled(-wx[2], 0); E1X.hi = d2f_scaled(wx[3], 0);
-                                S0X.hi = d2f_scaled(-wy[0], 0); N0X.hi = d2f_scaled(wy[1], 0);
-                                S1X.hi = d2f_scaled(-wy[2], 0); N1X.hi = d2f_scaled(wy[3], 0);
-                            }
+                            const float4 l0 = __ldg(sp + 3), l1 = __ldg(sp + 4), l2 = __ldg(sp + 5);
+                            C1X.lo = l0.x; C0X.lo = l0.y; W0X.lo = l0.z; E0X.lo = l0.w;
+                            S0X.lo = l1.x; N0X.lo = l1.y; W1X.lo = l1.z; E1X.lo = l1.w;
+                            S1X.lo = l2.x; N1X.lo = l2.y;
                         }
                     }
                     const float *pUE = Fu + sE * kGP, *pUW = Fu + sW * kGP, *pUN = Fu + sN * kGP, *pUS = Fu + sS * kGP;
@@ -674,12 +563,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             if (at < cocap) colist[at] = make_int2(item.x, (int)(ticol - md.ptab) + kIcolWords * t);
             else atomicOr(md.status, 4u);
         }
-        if (ISO && md.diso) {
-            unsigned long long *dg = md.diag + 2 * (step & 1);
-            unsigned long long db = __double_as_longlong(dmax_l);
-            if (db) atomicMax(&dg[0], db);
-            if (limps_l) atomicAdd(&dg[1], (unsigned long long)limps_l);
-        }
         // a scaled transfer above 3.5e8 could overflow the int32 sum of six faces
         const bool nonfinite = hmax >= 0x7ff00000u;
         if (nonfinite || gmax > 3.5e8f) atomicOr(md.status, (nonfinite ? 1u : 0u) | (gmax > 3.5e8f ? 2u : 0u));
@@ -704,6 +587,160 @@ __global__ void k_rescale(const MemberDesc *__restrict__ mds, int n)
             s = s < -120 ? -120 : (s > 120 ? 120 : s);
             md.scale[l] = s;
             md.gmax[l] = 0u;
+        }
+    }
+}
+
+// Top-face stencil of every wet cell below the surface, for the members with the isoneutral
+// branch or the local vertical diffusivity, built once per step (both transfer instances read
+// it) in FP64 from the step's T and S:
+//  * C1, C0: the weights of T(k+1) and T(k) -- the static coefficients, or with iediff 1/2
+//    those of the local diffusivity diffv (goldstein.f90:2490-2516, eosd :3064-3082);
+//  * with the isoneutral branch (goldstein.f90:2561-2624) the slope-tapered terms, which add
+//    to C1, C0 and give the weights of T at the W, E, S, N neighbours of levels k and k+1.
+// The density differences scc*dS - tec*dT cancel strongly in weakly stratified water, so they
+// are taken as differences of D = ec(2)*S - tec*T with the cell's tec (goldstein.f90:2587-2588).
+// One block row per listed member (blockIdx.y); also the diagnostics dmax and limps.
+__global__ void __launch_bounds__(256) k_stencil_fp32(const MemberDesc *__restrict__ mds, const int *__restrict__ list,
+                                                      const long long *__restrict__ step_ctr, int rel)
+{
+    const long long step = *step_ctr + rel;
+    const MemberDesc &md = mds[list[blockIdx.y]];
+    if (step >= md.stop_step) return;
+    const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, NI = md.NI, NJ = md.NJ;
+    const int mkn = maxk + 2, mjn = maxj + 2;
+    const double *mk = md.mk, *mj = md.mj;
+    const double *R = md.buf[(int)((step + md.parity) & 1)];
+    auto ld = [&](int ii, int jj, int kk, int l) {
+        return ldg_d(R + 2 * ((size_t)ii + (size_t)NI * ((size_t)jj + (size_t)NJ * (size_t)kk)) + l);
+    };
+    double dmax_l = 0.0;
+    unsigned limps_l = 0;
+    const size_t nij = (size_t)maxi * maxj, ncell = nij * (size_t)(maxk - 1);
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % maxi) + 1, j = (int)((c / maxi) % maxj) + 1, k = (int)(c / nij) + 1;
+        if (k < md.k1[i + NI * j]) continue;
+        double c1 = (double)__ldg(md.coef + 8 * c + 4) + (double)__ldg(md.coefl + 8 * c + 4);
+        double c0 = (double)__ldg(md.coef + 8 * c + 5) + (double)__ldg(md.coefl + 8 * c + 5);
+        double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // W0 E0 S0 N0 W1 E1 S1 N1
+        bool iso = false;
+        const double t1 = ld(i, j, k, 0), t2 = ld(i, j, k + 1, 0);
+        const double s1 = ld(i, j, k, 1), s2 = ld(i, j, k + 1, 1);
+        const double tatw = 0.5 * (t1 + t2);
+        double tec = -md.ec[0] - md.ec[2] * tatw * 2.0 - md.ec[3] * tatw * tatw * 3.0;
+        if (md.ieos) tec = tec - md.ec[4] * mk[2 * mkn + k];
+        const double rdza = mk[4 * mkn + k];
+        if (md.iediff) {
+            const double dzrho = (md.ec[1] * (s2 - s1) - tec * (t2 - t1)) * rdza;
+            const double rdzrho = dzrho < -1.0e-12 ? 1.0 / dzrho : -1.0e12;
+            const double e1 = md.ediff1[(size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1))];
+            double diffv;
+            if (md.ediffpow2i == 0) diffv = md.ediff0 + e1;
+            else if (md.ediffpow2i == 1) diffv = md.ediff0 + e1 * (-rdzrho);
+            else if (md.ediffpow2i == 2) diffv = md.ediff0 + e1 * sqrt(-rdzrho);
+            else diffv = md.ediff0 + e1 * pow(-rdzrho, md.ediffpow2);
+            if (diffv > md.diffmax[k + 1]) diffv = md.diffmax[k + 1];
+            const double u3 = md.u[2 + 3 * ((size_t)i + (size_t)(maxi + 1) * ((size_t)j + (size_t)(maxj + 1) * (size_t)(k - 1)))];
+            const double pec = u3 * md.dza[k] / diffv, ups = pec / (2.0 + fabs(pec));
+            const double g = mj[2 * mjn + j];   // dt*dphi*ds(j)
+            c1 = g * (u3 * (1.0 - ups) * 0.5 - rdza * diffv);
+            c0 = g * (u3 * (1.0 + ups) * 0.5 + rdza * diffv);
+        }
+        if (md.diso) {
+            const double scc = md.ec[1];
+            const double Dc0 = scc * s1 - tec * t1, Dc1 = scc * s2 - tec * t2;
+            const double dzrho = (Dc1 - Dc0) * rdza;
+            if (dzrho < -1.0e-12) {
+                iso = true;
+                const double rdzrho = 1.0 / dzrho;
+                const double rcr = mj[j];                                 // rc(j)*rdphi
+                const double cvs = mj[mjn + j - 1], cvn = mj[mjn + j];   // cv*rdsv at j-1, j
+                const int im = (i == 1) ? maxi : i - 1, ip = (i == maxi) ? 1 : i + 1;
+                const int k1E = md.k1[ip + NI * j], k1W = md.k1[im + NI * j];
+                const int k1N = md.k1[i + NI * (j + 1)], k1S = md.k1[i + NI * (j - 1)];
+                double dxr[4], dyr[4], mx[4], my[4];
+                double tv1 = 0.0;
+#pragma unroll
+                for (int knp = 0; knp <= 1; ++knp) {
+                    const double Dck = knp ? Dc1 : Dc0;
+#pragma unroll
+                    for (int nnp = 0; nnp <= 1; ++nnp) {
+                        const int ina = nnp + 2 * knp;
+                        const int kk = k + knp;
+                        const bool okx = kk >= (nnp ? k1E : k1W);
+                        const bool oky = kk >= (nnp ? k1N : k1S);
+                        mx[ina] = okx ? rcr : 0.0;
+                        my[ina] = oky ? (nnp ? cvn : cvs) : 0.0;
+                        dxr[ina] = 0.0;
+                        dyr[ina] = 0.0;
+                        if (okx) {
+                            const int ii = nnp ? ip : im;
+                            const double Dn = scc * ld(ii, j, kk, 1) - tec * ld(ii, j, kk, 0);
+                            dxr[ina] = (nnp ? Dn - Dck : Dck - Dn) * rcr;
+                        }
+                        if (oky) {
+                            const int jj = nnp ? j + 1 : j - 1;
+                            const double Dn = scc * ld(i, jj, kk, 1) - tec * ld(i, jj, kk, 0);
+                            dyr[ina] = (nnp ? Dn - Dck : Dck - Dn) * my[ina];
+                        }
+                        tv1 += dxr[ina] * dxr[ina] + dyr[ina] * dyr[ina];
+                    }
+                }
+                const double sum2 = tv1;
+                tv1 = 0.25 * tv1 * rdzrho * rdzrho;
+                const double ss = mk[5 * mkn + k];
+                double slim = 1.0;
+                if (tv1 > ss) {
+                    slim = ss * ss / (tv1 * tv1);
+                    limps_l += 1;
+                }
+                dmax_l = fmax(dmax_l, tv1 * slim * md.diff1 * rdza * md.dt * rdza);
+                // G_iso = dt*dphi*ds * 0.25*slim*diff1/dzrho^2 * sum_ina[...]
+                const double cc = mj[2 * mjn + j] * 0.25 * slim * md.diff1 * rdzrho * rdzrho;
+                const double two_dz = 2.0 * dzrho * cc;
+                double wx[4], wy[4];
+#pragma unroll
+                for (int n = 0; n < 4; ++n) {
+                    wx[n] = two_dz * dxr[n] * mx[n];
+                    wy[n] = two_dz * dyr[n] * my[n];
+                }
+                const double wz = -cc * sum2 * rdza;      // dzts = (T(k+1)-T(k))*rdza
+                c0 = c0 + ((wx[0] - wx[1]) + (wy[0] - wy[1]) - wz);
+                c1 = c1 + ((wx[2] - wx[3]) + (wy[2] - wy[3]) + wz);
+                w[0] = -wx[0]; w[1] = wx[1]; w[2] = -wy[0]; w[3] = wy[1];
+                w[4] = -wx[2]; w[5] = wx[3]; w[6] = -wy[2]; w[7] = wy[3];
+            }
+        }
+        const double v[10] = {c1, c0, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7]};
+        float hi[12], lo[12];
+#pragma unroll
+        for (int n = 0; n < 10; ++n) {
+            const dflt x = df_split(v[n]);
+            hi[n] = x.hi;
+            lo[n] = x.lo;
+        }
+        hi[10] = iso ? 1.f : 0.f;
+        hi[11] = lo[10] = lo[11] = 0.f;
+        float4 *dst = reinterpret_cast<float4 *>(md.stencil + (size_t)kStencilWords * c);
+        dst[0] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        dst[1] = make_float4(hi[4], hi[5], hi[6], hi[7]);
+        dst[2] = make_float4(hi[8], hi[9], hi[10], hi[11]);
+        dst[3] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        dst[4] = make_float4(lo[4], lo[5], lo[6], lo[7]);
+        dst[5] = make_float4(lo[8], lo[9], lo[10], lo[11]);
+    }
+    if (md.diso) {
+        // diagnostics dmax, limps of the step (goldstein.f90:2459, 2598-2608): one atomic per warp
+        unsigned long long db = __double_as_longlong(dmax_l);
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, db, o);
+            db = ob > db ? ob : db;
+            limps_l += __shfl_xor_sync(0xffffffffu, limps_l, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            unsigned long long *dg = md.diag + 2 * (step & 1);
+            if (db) atomicMax(&dg[0], db);
+            if (limps_l) atomicAdd(&dg[1], (unsigned long long)limps_l);
         }
     }
 }
@@ -845,6 +882,9 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
     }
     const int P = b.max_slots + 1;
     const int smem_bytes = fp32_smem_layout(P).total;
+    // the top-face stencils of the members that rebuild them every step
+    if (b.n_stencil > 0)
+        k_stencil_fp32<<<dim3(b.stencil_blocks, b.n_stencil), 256, 0, s>>>(b.descs, b.stencil_list, step_ctr, rel);
     // the T-S items and the other items run side by side (two streams), then the adjustment
     const bool two = b.n_ts > 0 && b.n_bgc > 0 && s2 != nullptr;
     if (two) {
@@ -881,7 +921,10 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
     return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
-int fp32_launches_per_step(const Fp32Batch &b) { return (b.n_ts > 0) + (b.n_bgc > 0) + 1 + (b.co_general ? 1 : 0); }
+int fp32_launches_per_step(const Fp32Batch &b)
+{
+    return (b.n_stencil > 0) + (b.n_ts > 0) + (b.n_bgc > 0) + 1 + (b.co_general ? 1 : 0);
+}
 
 // ---------------------------------------------------------------------------
 // patch plan (host): rectangles of water columns, periodic in i, with the ring of
@@ -1464,6 +1507,11 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems) * sizeof(int4));
+    if ((p.diso || p.iediff) && e == cudaSuccess) {
+        e = cudaMalloc(&D.stencil, (size_t)kStencilWords * ncell * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&D.stencil_list, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(D.stencil_list, 0, sizeof(int));
+    }
     if (e == cudaSuccess) {
         // the T-S items of the patches, then the other (patch, group) items
         std::vector<int4> it;
@@ -1497,7 +1545,7 @@ void fp32_member_free(Fp32Member *f)
     Fp32Data &D = h->data;
     cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
-    cudaFree(D.colist); cudaFree(D.cocount);
+    cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.stencil); cudaFree(D.stencil_list);
     if (D.s2) cudaStreamDestroy(D.s2);
     if (D.fork) cudaEventDestroy(D.fork);
     if (D.join) cudaEventDestroy(D.join);
@@ -1602,6 +1650,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.ptab = D.ptab;
         md.status = D.status;
         md.diag = diag;
+        md.stencil = D.stencil;
         if (cudaMemcpyAsync(D.dev, &md, sizeof(md), cudaMemcpyHostToDevice, s) != cudaSuccess) return GB_GO_ECUDA;
         if (cudaStreamSynchronize(s) != cudaSuccess) return GB_GO_ECUDA;
         D.desc_valid = true;
@@ -1625,8 +1674,13 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         bt.colist = D.colist;
         bt.cocount = D.cocount;
         bt.cocap = D.cocap;
-        bt.iso = h->p.diso != 0 || h->p.iediff != 0;
+        bt.iso = D.stencil != nullptr;
         bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->d.maxk);
+        if (D.stencil) {
+            bt.stencil_list = D.stencil_list;
+            bt.n_stencil = 1;
+            bt.stencil_blocks = fp32_stencil_blocks((size_t)h->d.maxi * h->d.maxj * h->d.maxk);
+        }
         int r = D.nitems ? fp32_launch(bt, D.step_ctr, n, s, D.s2, D.fork, D.join) : 0;
         if (!r) r = fp32_rescale(D.dev, 1, s);
         if (r) return r;
