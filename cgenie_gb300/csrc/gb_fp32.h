@@ -203,7 +203,7 @@ struct PatchPlan {
 int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, PatchPlan &plan);
 int fp32_group_count(int L);   // tracer groups (work items per patch): T and S, then groups of <= 8
 // blocks per member of the stencil prepass for a grid of `ncell` interior cells
-inline int fp32_stencil_blocks(size_t ncell) { return (int)std::min<size_t>(64, (ncell + 255) / 256); }
+inline int fp32_stencil_blocks(size_t ncell) { return (int)std::min<size_t>(16384, (ncell + 255) / 256); }
 // Fortran layout (L, NI, NJ, maxk+2) <-> group-planar layout of the FP32-flux state
 int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s);
 int fp32_from_planar(double *fortran, const double *planar, const Dims &d, cudaStream_t s);
