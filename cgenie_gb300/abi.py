@@ -76,6 +76,17 @@ class GbGrid(C.Structure):
     ]
 
 
+class GbBgDims(C.Structure):
+    """gb_bg_dims (include/gb_biogem.h)."""
+    _fields_ = [("n_i", C.c_int32), ("n_j", C.c_int32), ("n_k", C.c_int32), ("n_l_ocn", C.c_int32),
+                ("n_l_sed", C.c_int32), ("pad", C.c_int32)]
+
+
+class GbBgParams(C.Structure):
+    """gb_bg_params: tstoocn_offset(1:2) and ctrl_force_GOLDSTEInTS."""
+    _fields_ = [("ts_offset", C.c_double * 2), ("force_ts", C.c_int32), ("pad", C.c_int32)]
+
+
 class GbEnsTuning(C.Structure):
     _fields_ = [("tile_i", C.c_int32), ("tile_j", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("use_graph", C.c_int32)]

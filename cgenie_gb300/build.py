@@ -28,6 +28,7 @@ SOURCES = {
     "tstep_fp32.cu": [],
     "gb_goldstein.cu": ["-fmad=false"],
     "ensemble.cu": [],
+    "biogem_coupling.cu": ["-fmad=false"],
 }
 
 

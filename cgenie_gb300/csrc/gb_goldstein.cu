@@ -453,6 +453,37 @@ extern "C" int gb_go_set_stream(gb_go_handle *h, void *cuda_stream)
     return GB_GO_OK;
 }
 
+namespace gbgo {
+int ocean_state(gb_go_handle *h, OceanState *o)
+{
+    if (!h || !o) return GB_GO_EINVAL;
+    o->d = h->d;
+    o->precision = h->precision;
+    o->device = h->device;
+    o->stream = h->stream;
+    o->ts_static = h->ts_static;
+    o->ts1_static = h->ts1_static;
+    o->ts_buf[0] = h->ts_buf[0];
+    o->ts_buf[1] = h->ts_buf[1];
+    o->cur = h->cur;
+    o->steps_since_upload = h->steps_since_upload;
+    o->k1 = h->k1;
+    o->state_ready = h->state_ready;
+    return GB_GO_OK;
+}
+
+int ocean_state_reloaded(gb_go_handle *h)
+{
+    const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_buf[0], h->ts1_static, nts * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ts_buf[1], h->ts_static, nts * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    h->cur = 0;
+    h->slot = 0;
+    h->steps_since_upload = 0;
+    return GB_GO_OK;
+}
+}  // namespace gbgo
+
 extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const double *ts1, const double *rho)
 {
     if (!h || !ts || !ts1 || !rho) return fail(h, GB_GO_EINVAL, "upload_state: NULL array");

@@ -91,6 +91,30 @@ int launch_step_fp64(const StepArgs &a, void *stream);
 void step_fp64_tile(int maxi, int maxj, int maxk, int nsm, int *tile_i, int *tile_j);
 constexpr int kFp64TilesPerSm = 4;
 
+// The device tracer state of a single-grid handle, for the routines that act on it between
+// steps (the BIOGEM tracer coupling).  ts_static / ts1_static: the uploaded Fortran-layout
+// arrays; ts_buf: the step's ping-pong buffers; `cur`: the current one, valid on the wet cells
+// once steps_since_upload > 0 (before that the current ts is ts_static).
+struct OceanState {
+    Dims d;
+    int precision;
+    int device;
+    void *stream;   // cudaStream_t
+    double *ts_static, *ts1_static, *ts_buf[2];
+    int cur;
+    long long steps_since_upload;
+    const int32_t *k1;   // device, (maxi+2, maxj+2)
+    bool state_ready;
+};
+}  // namespace gbgo
+struct gb_go_handle;
+namespace gbgo {
+int ocean_state(gb_go_handle *h, OceanState *out);
+void count_launches(uint64_t n);   // kernels this library started (gb_go_kernel_launch_count)
+// after the state arrays were rewritten on the device: the handle continues as after an upload
+// (ts_buf[0] = ts1_static, ts_buf[1] = ts_static, step counters reset)
+int ocean_state_reloaded(gb_go_handle *h);
+
 #ifdef __CUDACC__
 // c + n computed as n additions of 1.0 in round-to-nearest (co adds 1 to cost(i,j) per
 // filled level, goldstein.f90:2759).  When c is integer-valued with |c| < 2^52 every partial

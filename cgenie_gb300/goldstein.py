@@ -34,6 +34,8 @@ EXPORTED = [
     "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
     "gb_ens_remaining", "gb_ens_download", "gb_ens_download_stream", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
     "gb_ens_count", "gb_ens_last_error",
+    "gb_bg_create", "gb_bg_destroy", "gb_bg_columns", "gb_bg_upload", "gb_bg_set_increments",
+    "gb_bg_tracercoupling", "gb_bg_download", "gb_bg_last_error",
 ]
 
 _lib = None
@@ -100,6 +102,17 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_count.argtypes = [vp, ip, P(C.c_size_t)]
     L.gb_ens_last_error.argtypes = [vp]
     L.gb_ens_last_error.restype = C.c_char_p
+    L.gb_bg_create.argtypes = [P(abi.GbBgDims), P(abi.GbBgParams), ip, C.c_int, P(vp)]
+    L.gb_bg_destroy.argtypes = [vp]
+    L.gb_bg_destroy.restype = None
+    L.gb_bg_columns.argtypes = [vp]
+    L.gb_bg_columns.restype = C.c_int32
+    L.gb_bg_upload.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.gb_bg_set_increments.argtypes = [vp, dp, dp]
+    L.gb_bg_tracercoupling.argtypes = [vp, vp]
+    L.gb_bg_download.argtypes = [vp, dp, dp, dp, dp]
+    L.gb_bg_last_error.argtypes = [vp]
+    L.gb_bg_last_error.restype = C.c_char_p
     _lib = L
     return L
 

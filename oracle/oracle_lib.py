@@ -12,7 +12,7 @@ import subprocess
 
 import numpy as np
 
-from cgenie_gb300.abi import GbDims, GbParams, GbGrid, GridRefs, dptr, iptr
+from cgenie_gb300.abi import GbBgDims, GbBgParams, GbDims, GbParams, GbGrid, GridRefs, dptr, iptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libgb_oracle.so")
@@ -22,8 +22,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle (make -C oracle)."""
-    src = os.path.join(HERE, "goldstein_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -53,6 +53,12 @@ def lib():
         L.gbo_eosd.restype = None
         L.gbo_inventory.argtypes = [P(GbDims), P(GbGrid), P(C.c_double), P(C.c_double)]
         L.gbo_inventory.restype = C.c_int
+        dp = P(C.c_double)
+        L.gbo_bg_tracercoupling.argtypes = [P(GbBgDims), P(GbBgParams), P(C.c_int32), dp, dp, dp, dp, dp, dp,
+                                            dp, dp, dp]
+        L.gbo_bg_tracercoupling.restype = C.c_int
+        L.gbo_bg_columns.argtypes = [P(GbBgDims), P(C.c_int32)]
+        L.gbo_bg_columns.restype = C.c_int
         _lib = L
     return _lib
 
@@ -98,3 +104,44 @@ def run(m, nsteps: int, **kw) -> OracleState:
     s = OracleState(m, **kw)
     s.step(nsteps)
     return s
+
+
+def go_ts_interior(ts: np.ndarray) -> np.ndarray:
+    """go_ts (n_l_ocn, n_i, n_j, n_k) from a halo'd ts array ([k, j, i, l] C order)."""
+    m_k = ts.shape[0] - 2
+    return np.ascontiguousarray(ts[1:m_k + 1, 1:-1, 1:-1, :])
+
+
+def bg_tracercoupling(m, st, go_ts: np.ndarray, *, force_ts: bool = False, ts_offset=(273.15, 34.9)):
+    """The C restatement of biogem_tracercoupling on go_ts ([k, j, i, l] C order, interior only)
+    and a BiogemState `st` (updated in place).  Returns (go_ts, go_ts1)."""
+    L, Ls = m.maxl, st.vbio_part.shape[-1]
+    d = GbBgDims(m.maxi, m.maxj, m.maxk, L, Ls, 0)
+    p = GbBgParams((C.c_double * 2)(*ts_offset), int(bool(force_ts)), 0)
+    k1 = np.ascontiguousarray(m.k1[1:m.maxj + 1, 1:m.maxi + 1], dtype=np.int32)
+    ts = np.ascontiguousarray(go_ts, dtype=np.float64).copy()
+    ts1 = np.zeros_like(ts)
+    for name in ("vocn", "mass", "volume", "rmass", "vbio_part", "vdocn", "vdbio_part"):
+        setattr(st, name, np.ascontiguousarray(getattr(st, name), dtype=np.float64))
+    nul = C.POINTER(C.c_double)()
+    rc = lib().gbo_bg_tracercoupling(C.byref(d), C.byref(p), iptr(k1), dptr(ts), dptr(ts1), dptr(st.vocn),
+                                     dptr(st.mass), dptr(st.volume), dptr(st.rmass), dptr(st.vdocn),
+                                     dptr(st.vbio_part) if Ls else nul, dptr(st.vdbio_part) if Ls else nul)
+    if rc != 0:
+        raise RuntimeError(f"oracle gbo_bg_tracercoupling failed: {rc}")
+    return ts, ts1
+
+
+def after_coupling(state: "OracleState", go_ts: np.ndarray, go_ts1: np.ndarray) -> None:
+    """step_goldstein's copy-in and boundary conditions after a coupling
+    (src/goldstein/goldstein.f90:176-187): ts and ts1 interiors from go_ts / go_ts1, then
+    ts1's periodic i-halo from ts."""
+    m = state.m
+    mk = m.maxk
+    state.ts[1:mk + 1, 1:-1, 1:-1, :] = go_ts
+    state.ts1[1:mk + 1, 1:-1, 1:-1, :] = go_ts1
+    for j in range(1, m.maxj + 1):
+        for k in range(int(m.k1[j, 0]), mk + 1):
+            state.ts1[k, j, 0, :] = state.ts[k, j, m.maxi, :]
+        for k in range(int(m.k1[j, m.maxi + 1]), mk + 1):
+            state.ts1[k, j, m.maxi + 1, :] = state.ts[k, j, 1, :]

@@ -12,9 +12,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def header_functions():
-    src = open(os.path.join(ROOT, "include", "gb_goldstein.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(gb_(?:go|ens)_[a-z0-9_]+)\s*\(", src)))
+    names = set()
+    for h in ("gb_goldstein.h", "gb_biogem.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(gb_(?:go|ens|bg)_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
 
 
 def test_library_builds_and_exports_all_header_symbols():
@@ -35,6 +38,8 @@ def test_struct_layouts():
     # 19 pointers, dphi and rdphi, 3 pointers of the mixed-layer scheme
     assert C.sizeof(abi.GbGrid) == 19 * 8 + 2 * 8 + 3 * 8
     assert C.sizeof(abi.GbEnsTuning) == 16
+    assert C.sizeof(abi.GbBgDims) == 24
+    assert C.sizeof(abi.GbBgParams) == 24
 
 
 def test_errstr_without_gpu():
