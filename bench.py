@@ -10,6 +10,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
   c1  single member 36x36x16, 2 tracers, FP64 plain form
   c5  single grid 360x180x32, 24 tracers (HBM stress test), FP64 plain form or, with
       --precision fp32flux, the split-precision form
+  bg5 the BIOGEM tracer coupling (biogem_tracercoupling) on the c5 grid with 8 particulate
+      tracers: a step is one coupling of the device-resident GOLDSTEIN and BIOGEM fields;
+      `value` is tracer cell-couplings/s (one tracer of one wet cell coupled)
 
 A step is one tracer timestep (tstepo) of every member.  `value` is tracer
 cell-updates/s with the state resident in HBM (c3: the 256 states, 2 x 0.6 GB,
@@ -47,6 +50,7 @@ WORKLOADS = {
     "c2": dict(name="tstipo_diso_fp64_36x36x16_L17", factory="config_c2"),
     "c3": dict(name="ensemble256_fp32flux_18x18x16_36x36x16_36x36x32_L2-24", members=256, seed=3),
     "c5": dict(name="stress_360x180x32_L24", factory="config_c5"),
+    "bg5": dict(name="biogem_tracercoupling_360x180x32_L24_sed8", factory="config_c5", n_l_sed=8),
 }
 
 
@@ -185,8 +189,166 @@ def oracle_pool_rate(n: int, seed: int, warmup: int, steps: int, faithful: bool 
     return cu / dt, len(jobs), cu // max(1, steps)
 
 
+def bg_algorithmic_bytes(wet_cells: int, L: int, Ls: int) -> int:
+    """Bytes one coupling must move: per wet cell read go_ts, vocn, vdocn (3L), mass, volume,
+    rmass (3), vbio_part, vdbio_part (2Ls); write vocn, ts, ts1 (3L), mass, rmass (2),
+    vbio_part (Ls) -- 8 * (6L + 3Ls + 5) bytes."""
+    return 8 * (6 * L + 3 * Ls + 5) * wet_cells
+
+
+def bg_cpu_rate(m, st, target_s: float = 12.0):
+    """The oracle's coupling (serial, 1 core) on the same fields: (cell-couplings/s, calls)."""
+    from oracle import oracle_lib
+    go = oracle_lib.go_ts_interior(m.ts)
+    a = st.copy()
+    t0 = time.perf_counter()
+    oracle_lib.bg_tracercoupling(m, a, go)
+    per = time.perf_counter() - t0
+    n = max(1, min(50, int(target_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        go, _ = oracle_lib.bg_tracercoupling(m, a, go)   # successive couplings of the evolving fields
+    dt = time.perf_counter() - t0
+    return m.wet_cells * m.maxl * n / dt, n
+
+
+def run_bg(args, rank, world, local, dist):
+    """The BIOGEM tracer coupling on the c5 grid: device-resident timing, end to end, roofline."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    from cgenie_gb300 import biogem, grid
+    from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+    w = WORKLOADS[args.workload]
+    m = grid.make_member(getattr(grid, w["factory"])())
+    Ls = w["n_l_sed"]
+    st = biogem.make_state(m, n_l_sed=Ls, seed=5)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = new_member_run(m, device=local, stream=stream.cuda_stream)
+    g.tstepo(1)
+    bg = biogem.BiogemCoupling(m, n_l_sed=Ls, device=local)
+    bg.upload(st)
+    bg.set_increments(st)
+    for _ in range(args.warmup):
+        bg.tracercoupling(g)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    for s in range(args.steps):
+        starts[s].record(stream)
+        bg.tracercoupling(g)
+        ends[s].record(stream)
+    torch.cuda.synchronize()
+    launches = kernel_launch_count() - n0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    total_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    units = m.wet_cells * m.maxl
+    value = world * units * args.steps / (total_ms * 1e-3)
+
+    # end to end through the C-ABI: the interval's increments from pinned host memory, the
+    # coupling, BIOGEM's ocean tracers and particulates back to pinned host memory
+    vd_h = torch.from_numpy(np.ascontiguousarray(st.vdocn)).pin_memory()
+    vdb_h = torch.from_numpy(np.ascontiguousarray(st.vdbio_part)).pin_memory()
+    vo_h = torch.empty(tuple(st.vocn.shape), dtype=torch.float64).pin_memory()
+    vb_h = torch.empty(tuple(st.vbio_part.shape), dtype=torch.float64).pin_memory()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(t.data_ptr(), dp)   # noqa: E731
+    lib = bg.lib
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        lib.gb_bg_set_increments(bg.h, ptr(vd_h), ptr(vdb_h))
+        lib.gb_bg_tracercoupling(bg.h, g.h)
+        lib.gb_bg_download(bg.h, ptr(vo_h), None, None, ptr(vb_h))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * units * args.steps / e2e_s
+
+    peak, peak_kind = measured_peaks()
+    alg = bg_algorithmic_bytes(m.wet_cells, m.maxl, Ls)
+    achieved = alg / (total_ms * 1e-3 / args.steps) / 1e9
+    if rank == 0:
+        line = {
+            "metric": "tracer cell-couplings/s", "value": value, "unit": "tracer cell-couplings/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded member and BIOGEM fields, reference grid formulas)",
+            "config": {"workload": w["name"], "maxi": m.maxi, "maxj": m.maxj, "maxk": m.maxk, "n_l_ocn": m.maxl,
+                       "n_l_sed": Ls, "wet_cells": m.wet_cells,
+                       "l2": "not flushed: the fields (2.4 GB) are larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": e2e_value, "unit": "tracer cell-couplings/s",
+                    "h2d_bytes_per_step": int(vd_h.numel() + vdb_h.numel()) * 8,
+                    "d2h_bytes_per_step": int(vo_h.numel() + vb_h.numel()) * 8,
+                    "note": "per coupling: vdocn + vdbio_part H2D (pinned), coupling, vocn + vbio_part D2H"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": profile_traffic("coupling", w["name"]),
+                         "peak_source": peak_kind, "kernel": "coupling: k_bg_partials x2, k_bg_seqsum x2, "
+                         "k_bg_apply, k_bg_zero, k_bg_halo, step-buffer reload copies",
+                         "algorithmic_bytes_per_launch": alg,
+                         "note": "algorithmic bytes 8*(6L + 3Ls + 5) per wet cell over the whole coupling"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, n = bg_cpu_rate(m, st)
+            line["cpu_baseline"] = {"value": v, "unit": "tracer cell-couplings/s", "cores": 1, "kind": "port",
+                                    "sample": f"{n} couplings of the same fields, oracle C restatement, -O2"}
+        print(json.dumps(line))
+    bg.close()
+    g.close()
+
+
 def run_reference(args, rank, world):
     w = dict(WORKLOADS[args.workload])
+    if args.workload == "bg5":
+        from cgenie_gb300 import biogem, grid
+        m = grid.make_member(getattr(grid, w["factory"])())
+        st = biogem.make_state(m, n_l_sed=w["n_l_sed"], seed=5)
+        from oracle import oracle_lib
+        go = oracle_lib.go_ts_interior(m.ts)
+        for _ in range(min(args.warmup, 1)):
+            go, _ = oracle_lib.bg_tracercoupling(m, st, go)
+        steps = max(1, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            go, _ = oracle_lib.bg_tracercoupling(m, st, go)   # successive couplings of the evolving fields
+        dt = time.perf_counter() - t0
+        value = m.wet_cells * m.maxl * steps / dt
+        line = {
+            "metric": "tracer cell-couplings/s", "value": value, "unit": "tracer cell-couplings/s",
+            "impl": "reference", "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "n_l_ocn": m.maxl, "n_l_sed": w["n_l_sed"], "wet_cells": m.wet_cells},
+            "cpu_baseline": {"value": value, "unit": "tracer cell-couplings/s", "cores": 1, "kind": "port",
+                             "sample": f"{steps} couplings (of {args.steps} asked), oracle C restatement, serial "
+                                       f"(the reference routine is serial)"},
+            "e2e": {"value": value, "unit": "tracer cell-couplings/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
     if args.workload == "c3" and args.members:
         w["members"] = args.members
     if args.workload == "c3":
@@ -406,6 +568,11 @@ def main():
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
     if args.workload == "c3":
         run_c3(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "bg5":
+        run_bg(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
         return

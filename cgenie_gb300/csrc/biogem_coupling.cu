@@ -11,7 +11,8 @@
 //                     then the old mean salinity and inventories
 //   k_bg_partials<1>  the same for vocn_new(S)*V and loc_vocn(l)*M (:1983-1996, :2016-2023)
 //   k_bg_seqsum<1>    the new mean salinity, the salinity ratio, the new inventories
-//   k_bg_zero         interior cells that are land or below k1: 0 in ts and ts1 (conv_vocnTOts)
+//   k_bg_zero         interior cells that are land or below k1: 0 in ts and ts1 (conv_vocnTOts);
+//                     once per upload of the ocean state, as nothing else writes those cells
 //   k_bg_apply        one thread per wet cell: T and S, the biogeochemical tracers, particulates,
 //                     masses, and the GOLDSTEIN tracers written back into ts and ts1 (:2000-2056)
 //   k_bg_halo         ts1's periodic i-halo from the new ts (goldstein.f90:180-186)
@@ -65,9 +66,9 @@ __device__ __forceinline__ size_t ts_index(const BgArgs &a, int l, int i, int j,
     return (size_t)l + (size_t)a.L * ((size_t)i + (size_t)a.NI * ((size_t)j + (size_t)a.NJ * (size_t)k));
 }
 
-// PHASE 0: q = 0: V (the volume total, at upload); q = 1: S*V; q >= 2: vocn(q)*M.
-// PHASE 1: q = 1: S_new*V with S_new = (vts(S) + offset) + vdocn(S); q >= 2: loc_vocn(q)*M with
-//          loc_vocn = vts(q)*S_old*rmean_s_old.
+// PHASE 0: q = 0: V (the volume total, at upload); q = 1: S*V times rtot_V; q >= 2: vocn(q)*M.
+// PHASE 1: q = 1: S_new*V times rtot_V with S_new = (vts(S) + offset) + vdocn(S); q >= 2:
+//          loc_vocn(q)*M with loc_vocn = vts(q)*S_old*rmean_s_old.
 template <int PHASE>
 __global__ void __launch_bounds__(256) k_bg_partials(BgArgs a)
 {
@@ -84,6 +85,7 @@ __global__ void __launch_bounds__(256) k_bg_partials(BgArgs a)
             for (int k = k1; k <= a.nk; ++k) s = s + V[k - 1];
         } else if (q == 1) {
             for (int k = k1; k <= a.nk; ++k) s = s + vo[1 + (size_t)a.L * (k - 1)] * V[k - 1];
+            s = s * a.sc->rtot_v;   // loc_partialtot(n) = SUM(...)*loc_ocn_rtot_V (biogem.f90:1951)
         } else {
             for (int k = k1; k <= a.nk; ++k) s = s + vo[q + (size_t)a.L * (k - 1)] * M[k - 1];
         }
@@ -95,6 +97,7 @@ __global__ void __launch_bounds__(256) k_bg_partials(BgArgs a)
                 const double snew = (a.tsrc[ts_index(a, 1, i, j, k)] + a.off1) + vd[1 + (size_t)a.L * (k - 1)];
                 s = s + snew * V[k - 1];
             }
+            s = s * a.sc->rtot_v;   // biogem.f90:2021
         } else {
             const double rm = a.sc->rmean_s_old;
             for (int k = k1; k <= a.nk; ++k) {
@@ -135,7 +138,6 @@ __global__ void __launch_bounds__(kSumThreads) k_bg_seqsum(BgArgs a, int tile)
         }
         cp_async_commit();
     };
-    const double scale = (MODE == 0) ? 1.0 : a.sc->rtot_v;
     double s = 0.0;
     int b = 0;
     if (a.nv > 0) load(0, 0);
@@ -146,12 +148,26 @@ __global__ void __launch_bounds__(kSumThreads) k_bg_seqsum(BgArgs a, int tile)
         if (t < nq) {
             const int cnt = min(tile, a.nv - n0);
             const double *row = buf[b] + (size_t)t * stride;
-            const bool scaled = (MODE != 0) && (q0 + t == 1);
-            if (scaled) {
-                for (int c = 0; c < cnt; ++c) s = s + row[c] * scale;
-            } else {
-                for (int c = 0; c < cnt; ++c) s = s + row[c];
+            // only the additions chain (an FP64 add takes ~63 cycles on GB300): the shared-memory
+            // loads of the next 8 columns are issued before the additions of these 8
+            int c = 0;
+            double nxt[8];
+            if (cnt >= 8) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) nxt[u] = row[u];
             }
+            for (; c + 8 <= cnt; c += 8) {
+                double cur[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
+                if (c + 16 <= cnt) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) nxt[u] = row[c + 8 + u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) s = s + cur[u];
+            }
+            for (; c < cnt; ++c) s = s + row[c];
         }
         __syncthreads();   // buffer b is reloaded two tiles later
         b ^= 1;
@@ -510,12 +526,17 @@ extern "C" int gb_bg_tracercoupling(gb_bg *h, gb_go_handle *ocean)
         count_launches(1);
         BG_TRY(h, cudaGetLastError());
     }
-    const long long ncell = (long long)maxi * maxj * a.nk;
-    const unsigned gz = (unsigned)std::min<long long>((ncell + 255) / 256, 8192);
-    k_bg_zero<<<gz, 256, 0, s>>>(a, maxi, maxj, o.k1);
+    if (!*o.dry_zeroed) {
+        // once per upload: nothing else writes the dry interior cells of ts_static / ts1_static
+        const long long ncell = (long long)maxi * maxj * a.nk;
+        const unsigned gz = (unsigned)std::min<long long>((ncell + 255) / 256, 8192);
+        k_bg_zero<<<gz, 256, 0, s>>>(a, maxi, maxj, o.k1);
+        count_launches(1);
+        *o.dry_zeroed = true;
+    }
     const long long nh = 2LL * maxj * a.nk * a.L;
     k_bg_halo<<<(unsigned)std::min<long long>((nh + 255) / 256, 4096), 256, 0, s>>>(a, maxi, maxj, o.k1);
-    count_launches(2);
+    count_launches(1);
     BG_TRY(h, cudaGetLastError());
     const int r = ocean_state_reloaded(ocean);
     if (r) return bfail(h, r, "tracercoupling: reloading the ocean step buffers failed");

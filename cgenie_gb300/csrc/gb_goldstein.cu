@@ -52,6 +52,7 @@ struct gb_go_handle {
     Metrics m{};
     std::vector<int32_t> k1_host;
     bool state_ready = false, vel_ready = false;
+    bool dry_zeroed = false;   // interior dry cells of ts_static/ts1_static are 0 (after a coupling)
     long long steps_since_upload = 0;
     std::string last_error;
     Fp32Member f32{};   // FP32-flux path data
@@ -469,6 +470,7 @@ int ocean_state(gb_go_handle *h, OceanState *o)
     o->steps_since_upload = h->steps_since_upload;
     o->k1 = h->k1;
     o->state_ready = h->state_ready;
+    o->dry_zeroed = &h->dry_zeroed;
     return GB_GO_OK;
 }
 
@@ -501,6 +503,7 @@ extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const doubl
     h->cur = 0;
     h->slot = 0;
     h->state_ready = true;
+    h->dry_zeroed = false;
     h->steps_since_upload = 0;
     if (h->precision == GB_GO_FP32FLUX) {
         int r = fp32_member_upload(&h->f32, ts1, ts, h->ts_buf[0], h->stream);

@@ -105,6 +105,8 @@ struct OceanState {
     long long steps_since_upload;
     const int32_t *k1;   // device, (maxi+2, maxj+2)
     bool state_ready;
+    bool *dry_zeroed;    // the interior cells that are land or below k1 hold 0 in ts_static and
+                         // ts1_static (set by the coupling, cleared by an upload)
 };
 }  // namespace gbgo
 struct gb_go_handle;

@@ -137,3 +137,36 @@ def test_errors(gpu_lib):
     for h in (g, g2, g3):
         h.close()
     bg.close()
+
+
+def test_reupload_between_couplings(gpu_lib):
+    """Dry interior cells are zeroed by the first coupling after each upload: upload a state
+    whose dry cells are not 0, couple, upload it again, couple again."""
+    from cgenie_gb300.goldstein import new_member_run
+    m = grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=8, maxl=4, seed=31))
+    kk = np.arange(m.maxk + 2)[:, None, None]
+    dry = (kk < m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
+    dry[:, 0, :] = dry[:, -1, :] = False
+    dry[:, :, 0] = dry[:, :, -1] = False
+    m.ts[dry] = 7.0
+    m.ts1[dry] = 5.0
+    st = biogem.make_state(m, n_l_sed=1, seed=13)
+    g = new_member_run(m)
+    bg = biogem.BiogemCoupling(m, n_l_sed=1)
+    bg.upload(st)
+    bg.set_increments(st)
+    bg.tracercoupling(g)
+    g.upload_state()
+    bg.tracercoupling(g)
+    out = g.download()
+    out["bg"] = bg.download()
+    bg.close()
+    g.close()
+    a = st.copy()
+    s = ol.OracleState(m)
+    go, go1 = ol.bg_tracercoupling(m, a, ol.go_ts_interior(s.ts))
+    s = ol.OracleState(m)
+    go, go1 = ol.bg_tracercoupling(m, a, ol.go_ts_interior(s.ts))
+    ol.after_coupling(s, go, go1)
+    assert_bitexact(out, s, a)
+    assert np.all(out["ts"][dry] == 0.0) and np.all(out["ts1"][dry] == 0.0)
