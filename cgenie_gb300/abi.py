@@ -87,6 +87,30 @@ class GbBgParams(C.Structure):
     _fields_ = [("ts_offset", C.c_double * 2), ("force_ts", C.c_int32), ("pad", C.c_int32)]
 
 
+GB_EA_EMBM = 0
+GB_EA_SEAICE = 1
+GB_EA_MAX_CELLS = 4096
+
+
+class GbEaDims(C.Structure):
+    """gb_ea_dims (include/gb_embm.h)."""
+    _fields_ = [("maxi", C.c_int32), ("maxj", C.c_int32)]
+
+
+class GbEaParams(C.Structure):
+    """gb_ea_params: the scalars of tstipa (EMBM) or tstipsic (sea ice)."""
+    _fields_ = [("kind", C.c_int32), ("maxk", C.c_int32), ("dt", C.c_double), ("dphi", C.c_double),
+                ("rdphi", C.c_double), ("betaz", C.c_double * 2), ("betam", C.c_double * 2),
+                ("diffmod0", C.c_double), ("ppmin", C.c_double), ("ppmax", C.c_double),
+                ("diffsic", C.c_double), ("tsc", C.c_double)]
+
+
+class GbEaGrid(C.Structure):
+    """gb_ea_grid: j metrics with their Fortran bounds, diffa (EMBM) or k1 (sea ice)."""
+    _fields_ = [("rc", _dp), ("cv", _dp), ("dsv", _dp), ("rdsv", _dp), ("rds", _dp), ("diffa", _dp),
+                ("k1", _ip)]
+
+
 class GbEnsTuning(C.Structure):
     _fields_ = [("tile_i", C.c_int32), ("tile_j", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("use_graph", C.c_int32)]

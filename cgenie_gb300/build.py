@@ -29,6 +29,7 @@ SOURCES = {
     "gb_goldstein.cu": ["-fmad=false"],
     "ensemble.cu": [],
     "biogem_coupling.cu": ["-fmad=false"],
+    "surface_step.cu": ["-fmad=false"],
 }
 
 

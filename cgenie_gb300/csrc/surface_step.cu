@@ -1,0 +1,401 @@
+// 2-D iterative implicit surface steppers on the device: the EMBM atmosphere step tstipa
+// (src/embm/embm.f90:2039-2138) and the sea-ice transport step tstipsic
+// (src/goldsteinseaice/gold_seaice.f90:937-1058), behind include/gb_embm.h.
+//
+// One thread block per tracer (the two tracers never interact): the block holds the tracer's
+// face coefficients cie/ciw/cin/cis and the Jacobi iterate tq2 of the whole grid in shared
+// memory, each thread keeps its cells' tq, tq1 and source in registers, and the four
+// iterations and the corrector are separated by block barriers instead of kernel launches.
+// A launch runs nsteps steps (the coefficients depend only on the forcing, fixed within a
+// launch).  Compiled with -fmad=false: every expression rounds as the reference's.
+#include "../../include/gb_embm.h"
+#include "gb_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+using namespace gbgo;
+
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kCellsPerThread = (GB_EA_MAX_CELLS + kThreads - 1) / kThreads;
+
+struct EaArgs {
+    int maxi, maxj, maxk, kind, nsteps;
+    double dt, dphi, rdphi, betaz[2], betam[2], diffmod0, ppmin, ppmax, diffsic, tsc;
+    const double *rc, *cv, *dsv, *rdsv, *rds, *diffa;
+    const int32_t *k1;
+    double *tq, *tq1;
+    const double *src, *vel, *pptn;
+};
+
+__device__ __forceinline__ double clamp01(double x)
+{
+    // MAX(0.0, MIN(1.0, x)) (embm.f90:2065-2066)
+    const double m = 1.0 < x ? 1.0 : x;
+    return 0.0 > m ? 0.0 : m;
+}
+
+__global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a)
+{
+    extern __shared__ double sm[];
+    const int maxi = a.maxi, maxj = a.maxj;
+    const int ncell = maxi * maxj;
+    const int l = blockIdx.x + 1;   // tracer, 1-based
+    const int NC = maxi + 1, NV = maxi + 2;
+    double *cie = sm, *ciw = cie + (size_t)NC * (maxj + 1), *cin = ciw + (size_t)NC * (maxj + 1);
+    double *cis = cin + (size_t)NC * (maxj + 1), *v2 = cis + (size_t)NC * (maxj + 1);
+    const int t = threadIdx.x;
+    const bool ice = a.kind == GB_EA_SEAICE;
+    const double cimp = 0.5, dt = a.dt;
+
+    // boundary rows of the local arrays (embm.f90:2054-2059, gold_seaice.f90:952-957)
+    for (int i = t; i <= maxi; i += blockDim.x) {
+        cin[i] = 0.0;
+        cis[i] = 0.0;
+        cin[i + (size_t)NC * maxj] = 0.0;
+        cis[i + (size_t)NC * maxj] = 0.0;
+    }
+    for (int i = t; i <= maxi + 1; i += blockDim.x) {
+        v2[i] = 0.0;
+        v2[i + (size_t)NV * (maxj + 1)] = 0.0;
+    }
+    __syncthreads();
+    // face coefficients of the thread's cells
+    for (int r = 0; r < kCellsPerThread; ++r) {
+        const int c = t + r * blockDim.x;
+        if (c >= ncell) break;
+        const int i = c % maxi + 1, j = c / maxi + 1;
+        const double u1 = a.vel[2 * (size_t)c], u2 = a.vel[2 * (size_t)c + 1];
+        const double rcj = a.rc[j], cvj = a.cv[j];
+        double e, w, n, s;
+        if (!ice) {
+            // embm.f90:2061-2088
+            const double clampp = clamp01((a.pptn[c] - a.ppmin) / (a.ppmax - a.ppmin));
+            const double bz = a.betaz[l - 1], bm = a.betam[l - 1];
+            const double fac = (double)(2 - l) * a.diffmod0;
+            e = bz * u1 * rcj * 0.5 * a.rdphi;
+            double diffpp = a.diffa[(l - 1) + 2 * (0 + 2 * (size_t)(j - 1))] + fac * clampp;
+            double tv = rcj * rcj * a.rdphi * diffpp * a.rdphi;
+            double pec = bz * u1 * a.dphi / diffpp;
+            double ups = pec / (2.0 + fabs(pec));
+            w = e * (1 + ups) + tv;
+            e = e * (1 - ups) - tv;
+            n = cvj * bm * u2 * 0.5;
+            const double da2 = a.diffa[(l - 1) + 2 * (1 + 2 * (size_t)(j - 1))];
+            diffpp = da2 + fac * clampp;
+            if (j < maxj) {
+                tv = cvj * cvj * a.rdsv[j - 1] * da2;
+                pec = bm * u2 * a.dsv[j - 1] / diffpp;
+                ups = pec / (2.0 + fabs(pec));
+            } else {
+                tv = 0.0;
+                ups = 0.0;
+            }
+            s = n * (1 + ups) + tv;
+            n = n * (1 - ups) - tv;
+        } else {
+            // gold_seaice.f90:966-992
+            const int NK = maxi + 2;
+            const int k1c = a.k1[i + (size_t)NK * j];
+            const int k1e = a.k1[i + 1 + (size_t)NK * j], k1n = a.k1[i + (size_t)NK * (j + 1)];
+            if (a.maxk < (k1c > k1e ? k1c : k1e)) {
+                e = 0;
+                w = 0;
+            } else {
+                e = u1 * rcj * 0.5 * a.rdphi;
+                const double tv = rcj * rcj * a.rdphi * a.diffsic * a.rdphi;
+                const double pec = u1 * a.dphi / a.diffsic;
+                const double ups = pec / (2.0 + fabs(pec));
+                w = e * (1 + ups) + tv;
+                e = e * (1 - ups) - tv;
+            }
+            if (a.maxk < (k1c > k1n ? k1c : k1n)) {
+                n = 0;
+                s = 0;
+            } else {
+                n = cvj * u2 * 0.5;
+                const double tv = cvj * cvj * a.rdsv[j - 1] * a.diffsic;
+                const double pec = u2 * a.dsv[j - 1] / a.diffsic;
+                const double ups = pec / (2.0 + fabs(pec));
+                s = n * (1 + ups) + tv;
+                n = n * (1 - ups) - tv;
+            }
+        }
+        const size_t f = (size_t)i + (size_t)NC * j;
+        cie[f] = e;
+        ciw[f] = w;
+        cin[f] = n;
+        cis[f] = s;
+    }
+    __syncthreads();
+    for (int j = 1 + t; j <= maxj; j += blockDim.x) {
+        cie[(size_t)NC * j] = cie[maxi + (size_t)NC * j];
+        ciw[(size_t)NC * j] = ciw[maxi + (size_t)NC * j];
+    }
+    __syncthreads();
+
+    // the thread's cells: state, source, and the iteration-invariant centre terms
+    double tq[kCellsPerThread], tq1[kCellsPerThread], src[kCellsPerThread], cen[kCellsPerThread];
+    bool upd[kCellsPerThread];
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r) {
+        const int c = t + r * blockDim.x;
+        upd[r] = false;
+        tq[r] = tq1[r] = src[r] = cen[r] = 0.0;
+        if (c >= ncell) continue;
+        const int i = c % maxi + 1, j = c / maxi + 1;
+        const size_t x = (size_t)(l - 1) + 2 * (size_t)c;
+        tq[r] = a.tq[x];
+        tq1[r] = a.tq1[x];
+        // tstipa: -tqa(l,i,j); tstipsic: -dtha(l,i,j) * tsc
+        src[r] = ice ? -a.src[x] * a.tsc : -a.src[x];
+        const size_t f = (size_t)i + (size_t)NC * j;
+        cen[r] = ciw[f] - cie[f - 1] + (cis[f] - cin[f - NC]) * a.rds[j - 1];
+        upd[r] = !ice || !(a.maxk < a.k1[i + (size_t)(maxi + 2) * j]);
+    }
+
+    for (int step = 0; step < a.nsteps; ++step) {
+        for (int it = 0; it < 5; ++it) {
+            const bool corr = it == 4;
+            // the Jacobi iterate tq2 = cimp*tq + (1-cimp)*tq1; the corrector's average with the last one
+#pragma unroll
+            for (int r = 0; r < kCellsPerThread; ++r) {
+                const int c = t + r * blockDim.x;
+                if (c >= ncell) continue;
+                const int i = c % maxi + 1, j = c / maxi + 1;
+                const size_t v = (size_t)i + (size_t)NV * j;
+                const double nv = corr ? 0.5 * (v2[v] + cimp * tq[r] + (1.0 - cimp) * tq1[r])
+                                       : cimp * tq[r] + (1.0 - cimp) * tq1[r];
+                v2[v] = nv;
+                if (i == maxi) v2[(size_t)NV * j] = nv;          // tq2(0,j) = tq2(maxi,j)
+                if (i == 1) v2[maxi + 1 + (size_t)NV * j] = nv;  // tq2(maxi+1,j) = tq2(1,j)
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kCellsPerThread; ++r) {
+                const int c = t + r * blockDim.x;
+                if (c >= ncell || !upd[r]) continue;
+                const int i = c % maxi + 1, j = c / maxi + 1;
+                const size_t v = (size_t)i + (size_t)NV * j, f = (size_t)i + (size_t)NC * j;
+                const double rdsj = a.rds[j - 1];
+                const double flux = src[r] + cie[f] * v2[v + 1] - ciw[f - 1] * v2[v - 1] +
+                                    (cin[f] * v2[v + NV] - cis[f - NC] * v2[v - NV]) * rdsj;
+                if (!corr) {
+                    const double centre = dt * cen[r];
+                    tq[r] = (tq1[r] * (1.0 - (1.0 - cimp) * centre) - dt * flux) / (1 + cimp * centre);
+                } else {
+                    tq[r] = tq1[r] - dt * flux - dt * v2[v] * cen[r];
+                }
+            }
+            __syncthreads();
+        }
+        if (!ice) {
+#pragma unroll
+            for (int r = 0; r < kCellsPerThread; ++r) tq1[r] = tq[r];   // tq1 = tq (embm.f90:2137)
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r) {
+        const int c = t + r * blockDim.x;
+        if (c >= ncell) continue;
+        const size_t x = (size_t)(l - 1) + 2 * (size_t)c;
+        a.tq[x] = tq[r];
+        a.tq1[x] = tq1[r];
+    }
+}
+
+size_t smem_bytes(int maxi, int maxj)
+{
+    return (4 * (size_t)(maxi + 1) * (maxj + 1) + (size_t)(maxi + 2) * (maxj + 2)) * sizeof(double);
+}
+
+}  // namespace
+
+struct gb_ea {
+    int device = 0;
+    gb_ea_dims d{};
+    gb_ea_params p{};
+    cudaStream_t stream = nullptr;
+    double *rc = nullptr, *cv = nullptr, *dsv = nullptr, *rdsv = nullptr, *rds = nullptr, *diffa = nullptr;
+    int32_t *k1 = nullptr;
+    double *tq = nullptr, *tq1 = nullptr, *src = nullptr, *vel = nullptr, *pptn = nullptr;
+    bool have_state = false, have_forcing = false;
+    std::string last_error;
+};
+
+static int efail(gb_ea *h, int code, const std::string &msg)
+{
+    if (h) h->last_error = msg;
+    return code;
+}
+
+#define EA_TRY(h, call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t _e = (call);                                                                          \
+        if (_e != cudaSuccess)                                                                            \
+            return efail(h, _e == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA,                 \
+                         std::string(#call) + ": " + cudaGetErrorString(_e));                             \
+    } while (0)
+
+extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, const gb_ea_grid *grid, int device,
+                            gb_ea **out)
+{
+    if (!out) return GB_GO_EINVAL;
+    *out = nullptr;
+    if (!dims || !params || !grid) return GB_GO_EINVAL;
+    const int maxi = dims->maxi, maxj = dims->maxj;
+    if (maxi < 1 || maxj < 2) return GB_GO_EINVAL;
+    if ((long long)maxi * maxj > GB_EA_MAX_CELLS) return GB_GO_ERANGE;
+    const gb_ea_params p = *params;
+    if (p.kind != GB_EA_EMBM && p.kind != GB_EA_SEAICE) return GB_GO_EINVAL;
+    if (!grid->rc || !grid->cv || !grid->dsv || !grid->rdsv || !grid->rds) return GB_GO_EINVAL;
+    if (p.kind == GB_EA_EMBM && !grid->diffa) return GB_GO_EINVAL;
+    if (p.kind == GB_EA_SEAICE && (!grid->k1 || p.maxk < 1)) return GB_GO_EINVAL;
+    if (device < 0) cudaGetDevice(&device);
+    int smem_max = 0;
+    if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
+        return GB_GO_ECUDA;
+    if (smem_bytes(maxi, maxj) > (size_t)smem_max) return GB_GO_ERANGE;   // the grid must fit one block
+    gb_ea *h = new gb_ea();
+    h->d = *dims;
+    h->p = p;
+    h->device = device;
+    const size_t n2 = 2 * (size_t)maxi * maxj;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    auto up = [&](double **dst, const double *srcp, size_t n) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(dst, std::max<size_t>(1, n) * sizeof(double));
+        if (e == cudaSuccess && srcp && n) e = cudaMemcpy(*dst, srcp, n * sizeof(double), cudaMemcpyHostToDevice);
+    };
+    up(&h->rc, grid->rc, (size_t)maxj + 1);
+    up(&h->cv, grid->cv, (size_t)maxj + 1);
+    up(&h->dsv, grid->dsv, (size_t)maxj - 1);
+    up(&h->rdsv, grid->rdsv, (size_t)maxj - 1);
+    up(&h->rds, grid->rds, (size_t)maxj);
+    up(&h->diffa, p.kind == GB_EA_EMBM ? grid->diffa : nullptr, p.kind == GB_EA_EMBM ? 4 * (size_t)maxj : 1);
+    up(&h->tq, nullptr, n2);
+    up(&h->tq1, nullptr, n2);
+    up(&h->src, nullptr, n2);
+    up(&h->vel, nullptr, n2);
+    up(&h->pptn, nullptr, (size_t)maxi * maxj);
+    const size_t nk = (size_t)(maxi + 2) * (maxj + 2);
+    if (e == cudaSuccess) e = cudaMalloc(&h->k1, nk * sizeof(int32_t));
+    if (e == cudaSuccess && p.kind == GB_EA_SEAICE)
+        e = cudaMemcpy(h->k1, grid->k1, nk * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && p.kind == GB_EA_EMBM) e = cudaMemset(h->k1, 0, nk * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemset(h->pptn, 0, (size_t)maxi * maxj * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_surface_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(maxi, maxj));
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
+        gb_ea_destroy(h);
+        return code;
+    }
+    *out = h;
+    return GB_GO_OK;
+}
+
+extern "C" void gb_ea_destroy(gb_ea *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" const char *gb_ea_last_error(const gb_ea *h) { return h ? h->last_error.c_str() : ""; }
+
+extern "C" int gb_ea_upload_state(gb_ea *h, const double *tq, const double *tq1)
+{
+    if (!h || !tq || !tq1) return efail(h, GB_GO_EINVAL, "upload_state: NULL array");
+    EA_TRY(h, cudaSetDevice(h->device));
+    const size_t n2 = 2 * (size_t)h->d.maxi * h->d.maxj;
+    EA_TRY(h, cudaMemcpyAsync(h->tq, tq, n2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    EA_TRY(h, cudaMemcpyAsync(h->tq1, tq1, n2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->have_state = true;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_set_forcing(gb_ea *h, const double *source, const double *vel, const double *pptn)
+{
+    if (!h || !source || !vel) return efail(h, GB_GO_EINVAL, "set_forcing: NULL array");
+    if (h->p.kind == GB_EA_EMBM && !pptn) return efail(h, GB_GO_EINVAL, "set_forcing: EMBM needs pptn");
+    EA_TRY(h, cudaSetDevice(h->device));
+    const size_t n1 = (size_t)h->d.maxi * h->d.maxj, n2 = 2 * n1;
+    EA_TRY(h, cudaMemcpyAsync(h->src, source, n2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    EA_TRY(h, cudaMemcpyAsync(h->vel, vel, n2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (pptn) EA_TRY(h, cudaMemcpyAsync(h->pptn, pptn, n1 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->have_forcing = true;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (nsteps < 0) return efail(h, GB_GO_EINVAL, "step: nsteps < 0");
+    if (h->p.kind == GB_EA_SEAICE && nsteps > 1)
+        return efail(h, GB_GO_EINVAL, "step: sea ice takes one step per call (step_seaice post-processes between steps)");
+    if (!h->have_state || !h->have_forcing) return efail(h, GB_GO_ENOTREADY, "step before upload_state/set_forcing");
+    if (nsteps == 0) return GB_GO_OK;
+    EA_TRY(h, cudaSetDevice(h->device));
+    EaArgs a{};
+    a.maxi = h->d.maxi;
+    a.maxj = h->d.maxj;
+    a.maxk = h->p.maxk;
+    a.kind = h->p.kind;
+    a.nsteps = nsteps;
+    a.dt = h->p.dt;
+    a.dphi = h->p.dphi;
+    a.rdphi = h->p.rdphi;
+    for (int l = 0; l < 2; ++l) {
+        a.betaz[l] = h->p.betaz[l];
+        a.betam[l] = h->p.betam[l];
+    }
+    a.diffmod0 = h->p.diffmod0;
+    a.ppmin = h->p.ppmin;
+    a.ppmax = h->p.ppmax;
+    a.diffsic = h->p.diffsic;
+    a.tsc = h->p.tsc;
+    a.rc = h->rc;
+    a.cv = h->cv;
+    a.dsv = h->dsv;
+    a.rdsv = h->rdsv;
+    a.rds = h->rds;
+    a.diffa = h->diffa;
+    a.k1 = h->k1;
+    a.tq = h->tq;
+    a.tq1 = h->tq1;
+    a.src = h->src;
+    a.vel = h->vel;
+    a.pptn = h->pptn;
+    const int ncell = h->d.maxi * h->d.maxj;
+    const int threads = std::min(kThreads, (ncell + 31) / 32 * 32);
+    k_surface_step<<<2, threads, smem_bytes(h->d.maxi, h->d.maxj), h->stream>>>(a);
+    count_launches(1);
+    EA_TRY(h, cudaGetLastError());
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_download(gb_ea *h, double *tq, double *tq1)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (!h->have_state) return efail(h, GB_GO_ENOTREADY, "download before upload_state");
+    EA_TRY(h, cudaSetDevice(h->device));
+    const size_t n2 = 2 * (size_t)h->d.maxi * h->d.maxj;
+    if (tq) EA_TRY(h, cudaMemcpyAsync(tq, h->tq, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (tq1) EA_TRY(h, cudaMemcpyAsync(tq1, h->tq1, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}

@@ -36,6 +36,8 @@ EXPORTED = [
     "gb_ens_count", "gb_ens_last_error",
     "gb_bg_create", "gb_bg_destroy", "gb_bg_columns", "gb_bg_upload", "gb_bg_set_increments",
     "gb_bg_tracercoupling", "gb_bg_download", "gb_bg_last_error",
+    "gb_ea_create", "gb_ea_destroy", "gb_ea_upload_state", "gb_ea_set_forcing", "gb_ea_step", "gb_ea_download",
+    "gb_ea_last_error",
 ]
 
 _lib = None
@@ -113,6 +115,15 @@ def load_library(path: str = LIB_PATH):
     L.gb_bg_download.argtypes = [vp, dp, dp, dp, dp]
     L.gb_bg_last_error.argtypes = [vp]
     L.gb_bg_last_error.restype = C.c_char_p
+    L.gb_ea_create.argtypes = [P(abi.GbEaDims), P(abi.GbEaParams), P(abi.GbEaGrid), C.c_int, P(vp)]
+    L.gb_ea_destroy.argtypes = [vp]
+    L.gb_ea_destroy.restype = None
+    L.gb_ea_upload_state.argtypes = [vp, dp, dp]
+    L.gb_ea_set_forcing.argtypes = [vp, dp, dp, dp]
+    L.gb_ea_step.argtypes = [vp, C.c_int32]
+    L.gb_ea_download.argtypes = [vp, dp, dp]
+    L.gb_ea_last_error.argtypes = [vp]
+    L.gb_ea_last_error.restype = C.c_char_p
     _lib = L
     return L
 

@@ -1,0 +1,82 @@
+/*
+ * gb_embm.h -- C-ABI of the device-resident 2-D iterative implicit steppers: the EMBM
+ * atmosphere step tstipa (src/embm/embm.f90:2039-2138) and the sea-ice transport step
+ * tstipsic (src/goldsteinseaice/gold_seaice.f90:937-1058).
+ *
+ * Both advance two tracers on the (maxi, maxj) surface grid (air temperature and humidity;
+ * ice height and area) by four Jacobi iterations of a Crank-Nicolson (cimp = 0.5) upwind
+ * advection-diffusion step and an explicit conservative corrector, periodic in i.  Here the
+ * tracers stay on the device between steps; a step is one kernel launch.  The arithmetic is
+ * the reference's, operation for operation (no FMA contraction): results are bit-identical.
+ *
+ * Layouts are the reference's, column-major: tq(2, maxi, maxj) (tq(l,i,j) at
+ * (l-1) + 2*((i-1) + maxi*(j-1))), uatm(2, maxi, maxj), pptn(maxi, maxj); the j-metric arrays
+ * keep their Fortran bounds (rc(0:maxj) has maxj+1 entries starting at j = 0, dsv and rdsv
+ * (1:maxj-1), rds(1:maxj)); diffa(2, 2, maxj).
+ *
+ * Return codes are those of gb_goldstein.h.  A handle is not thread-safe; every call returns
+ * after its work has finished.
+ */
+#ifndef GB_EMBM_H
+#define GB_EMBM_H
+
+#include "gb_goldstein.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_ea gb_ea;
+
+/* grids up to GB_EA_MAX_CELLS surface cells (one thread block holds a tracer's grid) */
+#define GB_EA_MAX_CELLS 4096
+
+typedef struct {
+    int32_t maxi, maxj;
+} gb_ea_dims;
+
+/* kind = GB_EA_EMBM: tstipa.  dt = dtatm, betaz/betam (embm_lib.f90:98), diffmod0, ppmin,
+   ppmax (embm_lib.f90:83, 112).
+   kind = GB_EA_SEAICE: tstipsic.  dt = dtsic, diffsic, tsc (the source term is
+   dtha(l,i,j)*tsc); betaz, betam, diffmod0, ppmin, ppmax unused. */
+#define GB_EA_EMBM 0
+#define GB_EA_SEAICE 1
+typedef struct {
+    int32_t kind;
+    int32_t maxk;        /* sea ice: land iff k1(i,j) > maxk */
+    double dt, dphi, rdphi;
+    double betaz[2], betam[2];
+    double diffmod0, ppmin, ppmax;
+    double diffsic, tsc;
+} gb_ea_params;
+
+typedef struct {
+    const double *rc;    /* rc(0:maxj) */
+    const double *cv;    /* cv(0:maxj) */
+    const double *dsv;   /* dsv(1:maxj-1) */
+    const double *rdsv;  /* rdsv(1:maxj-1) */
+    const double *rds;   /* rds(1:maxj) */
+    const double *diffa; /* EMBM: diffa(2, 2, maxj); NULL for sea ice */
+    const int32_t *k1;   /* sea ice: k1(0:maxi+1, 0:maxj+1) of the ocean; NULL for EMBM */
+} gb_ea_grid;
+
+int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, const gb_ea_grid *grid, int device, gb_ea **out);
+void gb_ea_destroy(gb_ea *h);
+/* tq (the new iterate's starting value) and tq1 (the previous step), (2, maxi, maxj) each */
+int gb_ea_upload_state(gb_ea *h, const double *tq, const double *tq1);
+/* EMBM: tqa (2, maxi, maxj), uatm (2, maxi, maxj), pptn (maxi, maxj).
+   Sea ice: dtha (2, maxi, maxj) as `source`, the surface ocean velocities u(1:2, i, j) as
+   `vel` (2, maxi, maxj) -- u(1,i,j) on the east face, u(2,i,j) on the north face; pptn NULL. */
+int gb_ea_set_forcing(gb_ea *h, const double *source, const double *vel, const double *pptn);
+/* EMBM: nsteps tstipa steps with the same forcing, each ending with tq1 = tq
+   (embm.f90:2137).  Sea ice: nsteps = 1, one tstipsic; tq1 is left as it was (step_seaice
+   post-processes the ice and copies it, gold_seaice.f90:604-619). */
+int gb_ea_step(gb_ea *h, int32_t nsteps);
+int gb_ea_download(gb_ea *h, double *tq, double *tq1);
+const char *gb_ea_last_error(const gb_ea *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

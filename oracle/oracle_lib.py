@@ -12,7 +12,8 @@ import subprocess
 
 import numpy as np
 
-from cgenie_gb300.abi import GbBgDims, GbBgParams, GbDims, GbParams, GbGrid, GridRefs, dptr, iptr
+from cgenie_gb300.abi import (GbBgDims, GbBgParams, GbDims, GbEaDims, GbEaGrid, GbEaParams, GbGrid, GbParams,
+                              GridRefs, dptr, iptr)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libgb_oracle.so")
@@ -22,7 +23,7 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle (make -C oracle)."""
-    srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c", "surface_oracle.c")]
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
@@ -59,6 +60,8 @@ def lib():
         L.gbo_bg_tracercoupling.restype = C.c_int
         L.gbo_bg_columns.argtypes = [P(GbBgDims), P(C.c_int32)]
         L.gbo_bg_columns.restype = C.c_int
+        L.gbo_ea_step.argtypes = [P(GbEaDims), P(GbEaParams), P(GbEaGrid), dp, dp, dp, dp, dp, C.c_int]
+        L.gbo_ea_step.restype = C.c_int
         _lib = L
     return _lib
 
@@ -145,3 +148,20 @@ def after_coupling(state: "OracleState", go_ts: np.ndarray, go_ts1: np.ndarray) 
             state.ts1[k, j, 0, :] = state.ts[k, j, m.maxi, :]
         for k in range(int(m.k1[j, m.maxi + 1]), mk + 1):
             state.ts1[k, j, m.maxi + 1, :] = state.ts[k, j, 1, :]
+
+
+def surface_step(case, nsteps: int = 1):
+    """The C restatement of tstipa / tstipsic on a cgenie_gb300.surface.SurfaceCase (its tq,
+    tq1 are updated in place)."""
+    d = GbEaDims(case.maxi, case.maxj)
+    p = case.params()
+    g = case.grid()
+    case.tq = np.ascontiguousarray(case.tq, dtype=np.float64)
+    case.tq1 = np.ascontiguousarray(case.tq1, dtype=np.float64)
+    src = np.ascontiguousarray(case.source, dtype=np.float64)
+    vel = np.ascontiguousarray(case.vel, dtype=np.float64)
+    pp = None if case.pptn is None else np.ascontiguousarray(case.pptn, dtype=np.float64)
+    rc = lib().gbo_ea_step(C.byref(d), C.byref(p), C.byref(g), dptr(case.tq), dptr(case.tq1), dptr(src), dptr(vel),
+                           dptr(pp), int(nsteps))
+    if rc != 0:
+        raise RuntimeError(f"oracle gbo_ea_step failed: {rc}")

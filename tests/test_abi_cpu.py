@@ -13,10 +13,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     names = set()
-    for h in ("gb_goldstein.h", "gb_biogem.h"):
+    for h in ("gb_goldstein.h", "gb_biogem.h", "gb_embm.h"):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"\b(gb_(?:go|ens|bg)_[a-z0-9_]+)\s*\(", src))
+        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea)_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 
@@ -40,6 +40,9 @@ def test_struct_layouts():
     assert C.sizeof(abi.GbEnsTuning) == 16
     assert C.sizeof(abi.GbBgDims) == 24
     assert C.sizeof(abi.GbBgParams) == 24
+    assert C.sizeof(abi.GbEaDims) == 8
+    assert C.sizeof(abi.GbEaParams) == 8 + 12 * 8
+    assert C.sizeof(abi.GbEaGrid) == 7 * 8
 
 
 def test_errstr_without_gpu():

@@ -1,0 +1,64 @@
+"""GPU parity of the 2-D surface steppers (tstipa, src/embm/embm.f90:2039-2138; tstipsic,
+src/goldsteinseaice/gold_seaice.f90:937-1058) against the C oracle, through the C-ABI
+(include/gb_embm.h).  The device keeps the reference's operation order without FMA
+contraction: every comparison is bit-exact."""
+import numpy as np
+import pytest
+
+from cgenie_gb300 import abi, grid, surface
+from oracle import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+
+def run(c, nsteps, calls=1):
+    s = surface.SurfaceStepper(c)
+    s.upload_state()
+    s.set_forcing()
+    for _ in range(calls):
+        s.step(nsteps)
+    out = s.download()
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("cfg,kind,nsteps,calls,dm", [
+    (dict(maxi=12, maxj=10, maxk=8, maxl=2, seed=11), "embm", 1, 1, 0.0),
+    (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=12), "embm", 5, 2, 0.0),     # 10 steps, two launches
+    (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=13), "embm", 3, 1, 0.7),     # pptn-dependent diffusion
+    (dict(maxi=37, maxj=23, maxk=8, maxl=2, seed=14), "embm", 2, 1, 0.0),      # odd shape
+    (dict(maxi=64, maxj=64, maxk=8, maxl=2, seed=15), "embm", 2, 1, 0.0),      # largest grid (4096 cells)
+    (dict(maxi=1, maxj=2, maxk=4, maxl=2, seed=16, land_frac=0.0), "embm", 2, 1, 0.0),   # smallest grid
+    (dict(maxi=12, maxj=10, maxk=8, maxl=2, seed=17), "seaice", 1, 1, 0.0),
+    (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=18, land_frac=0.5), "seaice", 1, 3, 0.0),
+], ids=["embm_small", "embm_10steps", "embm_diffmod", "embm_odd", "embm_64x64", "embm_1x2", "ice_small",
+        "ice_land_3calls"])
+def test_bitexact_vs_oracle(gpu_lib, cfg, kind, nsteps, calls, dm):
+    m = grid.make_member(grid.MemberConfig(**cfg))
+    c = surface.embm_case(m, seed=3, diffmod0=dm) if kind == "embm" else surface.seaice_case(m, seed=3)
+    tq, tq1 = run(c.copy(), nsteps, calls)
+    ref = c.copy()
+    for _ in range(calls):
+        ol.surface_step(ref, nsteps)
+    assert np.array_equal(tq, ref.tq), np.abs(tq - ref.tq).max()
+    assert np.array_equal(tq1, ref.tq1)
+
+
+def test_errors(gpu_lib):
+    from cgenie_gb300.goldstein import GoldsteinError
+    m = grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=8, maxl=2, seed=19))
+    c = surface.seaice_case(m, seed=4)
+    s = surface.SurfaceStepper(c)
+    with pytest.raises(GoldsteinError) as e:
+        s.step(1)
+    assert e.value.code == abi.GB_GO_ENOTREADY
+    s.upload_state()
+    s.set_forcing()
+    with pytest.raises(GoldsteinError) as e:
+        s.step(2)                 # sea ice: one step per call
+    assert e.value.code == abi.GB_GO_EINVAL
+    s.close()
+    big = grid.make_member(grid.MemberConfig(maxi=72, maxj=64, maxk=8, maxl=2, seed=20))
+    with pytest.raises(GoldsteinError) as e:
+        surface.SurfaceStepper(surface.embm_case(big, seed=5))
+    assert e.value.code == abi.GB_GO_ERANGE
