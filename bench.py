@@ -13,6 +13,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
   bg5 the BIOGEM tracer coupling (biogem_tracercoupling) on the c5 grid with 8 particulate
       tracers: a step is one coupling of the device-resident GOLDSTEIN and BIOGEM fields;
       `value` is tracer cell-couplings/s (one tracer of one wet cell coupled)
+  ea64 the EMBM atmosphere step (tstipa) on a 64x64 surface grid, one launch per step as
+      the model calls it; `value` is air cell-updates/s
+      (two tracers of one surface cell advanced one step)
 
 A step is one tracer timestep (tstepo) of every member.  `value` is tracer
 cell-updates/s with the state resident in HBM (c3: the 256 states, 2 x 0.6 GB,
@@ -51,6 +54,7 @@ WORKLOADS = {
     "c3": dict(name="ensemble256_fp32flux_18x18x16_36x36x16_36x36x32_L2-24", members=256, seed=3),
     "c5": dict(name="stress_360x180x32_L24", factory="config_c5"),
     "bg5": dict(name="biogem_tracercoupling_360x180x32_L24_sed8", factory="config_c5", n_l_sed=8),
+    "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
 }
 
 
@@ -319,8 +323,118 @@ def run_bg(args, rank, world, local, dist):
     g.close()
 
 
+def _ea_case(w):
+    from cgenie_gb300 import grid, surface
+    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=8, maxl=2, seed=21))
+    return surface.embm_case(m, seed=22)
+
+
+def ea_cpu_rate(case, target_s: float = 10.0):
+    """The oracle's tstipa (serial, 1 core): (cell-updates/s, steps)."""
+    from oracle import oracle_lib
+    c = case.copy()
+    t0 = time.perf_counter()
+    oracle_lib.surface_step(c, 10)
+    per = (time.perf_counter() - t0) / 10
+    n = max(10, min(100000, int(target_s / max(per, 1e-9))))
+    t0 = time.perf_counter()
+    oracle_lib.surface_step(c, n)
+    dt = time.perf_counter() - t0
+    return case.maxi * case.maxj * 2 * n / dt, n
+
+
+def run_ea(args, rank, world, local, dist):
+    """tstipa on one device-resident surface grid: one launch per step."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    from cgenie_gb300 import surface
+    from cgenie_gb300.goldstein import kernel_launch_count
+    w = WORKLOADS[args.workload]
+    case = _ea_case(w)
+    s = surface.SurfaceStepper(case.copy(), device=local)
+    s.upload_state()
+    s.set_forcing()
+    for _ in range(args.warmup):
+        s.step(1)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step(1)
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t0
+    launches = kernel_launch_count() - n0
+    clocks = sampler.stop()
+    units = case.maxi * case.maxj * 2
+    value = world * units * args.steps / dev_s
+    # end to end: the step's forcing (tqa, uatm, pptn) from pinned host memory, the step, tq back
+    src_h = torch.from_numpy(np.ascontiguousarray(case.source)).pin_memory()
+    vel_h = torch.from_numpy(np.ascontiguousarray(case.vel)).pin_memory()
+    pp_h = torch.from_numpy(np.ascontiguousarray(case.pptn)).pin_memory()
+    tq_h = torch.empty(tuple(case.tq.shape), dtype=torch.float64).pin_memory()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(t.data_ptr(), dp)   # noqa: E731
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.lib.gb_ea_set_forcing(s.h, ptr(src_h), ptr(vel_h), ptr(pp_h))
+        s.lib.gb_ea_step(s.h, 1)
+        s.lib.gb_ea_download(s.h, ptr(tq_h), None)
+    e2e_s = time.perf_counter() - t0
+    peak, peak_kind = measured_peaks()
+    alg = 13 * 8 * case.maxi * case.maxj   # read tq, tq1, tqa, uatm (2 each), pptn; write tq, tq1
+    achieved = alg / (dev_s / args.steps) / 1e9
+    if rank == 0:
+        line = {
+            "metric": "air cell-updates/s", "value": value, "unit": "air cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded fields on the reference's sin-latitude grid)",
+            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2,
+                       "timing": "host clock around the synchronous C-ABI step calls (one launch each)",
+                       "l2": "not flushed: the grid (0.3 MB) lives in L2, as in the model",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * units * args.steps / e2e_s, "unit": "air cell-updates/s",
+                    "h2d_bytes_per_step": int(src_h.numel() + vel_h.numel() + pp_h.numel()) * 8,
+                    "d2h_bytes_per_step": int(tq_h.numel()) * 8,
+                    "note": "per step: tqa + uatm + pptn H2D (pinned), step, tq D2H"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind, "kernel": "k_surface_step",
+                         "algorithmic_bytes_per_launch": alg,
+                         "note": "latency-bound: one cluster of 8 blocks per tracer, 5 cluster-barrier-separated "
+                                 "sweeps per step; the HBM roofline does not bind a 0.3 MB grid"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, n = ea_cpu_rate(case)
+            line["cpu_baseline"] = {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
+                                    "sample": f"{n} steps of the same grid, oracle C restatement, -O2"}
+        print(json.dumps(line))
+    s.close()
+
+
 def run_reference(args, rank, world):
     w = dict(WORKLOADS[args.workload])
+    if args.workload == "ea64":
+        case = _ea_case(w)
+        v, n = ea_cpu_rate(case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
+        line = {
+            "metric": "air cell-updates/s", "value": v, "unit": "air cell-updates/s", "impl": "reference",
+            "n_gpus": world, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * case.maxi * case.maxj * 2 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2},
+            "cpu_baseline": {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} steps, oracle C restatement, serial (the reference routine is serial)"},
+            "e2e": {"value": v, "unit": "air cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
     if args.workload == "bg5":
         from cgenie_gb300 import biogem, grid
         m = grid.make_member(getattr(grid, w["factory"])())
@@ -568,6 +682,11 @@ def main():
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
     if args.workload == "c3":
         run_c3(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "ea64":
+        run_ea(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
         return

@@ -89,7 +89,7 @@ class GbBgParams(C.Structure):
 
 GB_EA_EMBM = 0
 GB_EA_SEAICE = 1
-GB_EA_MAX_CELLS = 4096
+GB_EA_MAX_CELLS = 32768
 
 
 class GbEaDims(C.Structure):

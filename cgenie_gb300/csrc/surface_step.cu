@@ -2,15 +2,18 @@
 // (src/embm/embm.f90:2039-2138) and the sea-ice transport step tstipsic
 // (src/goldsteinseaice/gold_seaice.f90:937-1058), behind include/gb_embm.h.
 //
-// One thread block per tracer (the two tracers never interact): the block holds the tracer's
-// face coefficients cie/ciw/cin/cis and the Jacobi iterate tq2 of the whole grid in shared
-// memory, each thread keeps its cells' tq, tq1 and source in registers, and the four
-// iterations and the corrector are separated by block barriers instead of kernel launches.
-// A launch runs nsteps steps (the coefficients depend only on the forcing, fixed within a
-// launch).  Compiled with -fmad=false: every expression rounds as the reference's.
+// One thread-block cluster per tracer (the two tracers never interact), its blocks splitting the
+// rows: GB300's FP64 pipe is ~2 lanes per clock per SM, so the grid's FP64 work is spread over
+// up to 8 SMs per tracer.  Each block keeps its rows' face coefficients and Jacobi iterate in
+// shared memory and its cells' tq, tq1 and source in registers; the four iterations and the
+// corrector are separated by cluster barriers, with the halo rows of the iterate read from the
+// neighbouring blocks' shared memory, instead of kernel launches.  A launch runs nsteps steps
+// (the coefficients depend only on the forcing, fixed within a launch).  Compiled with
+// -fmad=false: every expression rounds as the reference's.
 #include "../../include/gb_embm.h"
 #include "gb_internal.h"
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,7 +24,8 @@ using namespace gbgo;
 namespace {
 
 constexpr int kThreads = 1024;
-constexpr int kCellsPerThread = (GB_EA_MAX_CELLS + kThreads - 1) / kThreads;
+constexpr int kClusterMax = 16;        // blocks per tracer (GB300 runs clusters of 16 when opted in)
+constexpr int kCellsPerThread = 4;     // cells of one block: at most kThreads * kCellsPerThread
 
 struct EaArgs {
     int maxi, maxj, maxk, kind, nsteps;
@@ -39,102 +43,119 @@ __device__ __forceinline__ double clamp01(double x)
     return 0.0 > m ? 0.0 : m;
 }
 
-__global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a)
+// Face coefficients of cell (i, j) for tracer l: east (cie, ciw) and north (cin, cis) faces.
+__device__ __forceinline__ void face_coefs(const EaArgs &a, int l, int i, int j, double *e_, double *w_, double *n_,
+                                           double *s_)
 {
+    const int maxi = a.maxi, maxj = a.maxj;
+    const size_t c = (size_t)(i - 1) + (size_t)maxi * (j - 1);
+    const double u1 = a.vel[2 * c], u2 = a.vel[2 * c + 1];
+    const double rcj = a.rc[j], cvj = a.cv[j];
+    double e, w, n, s;
+    if (a.kind == GB_EA_EMBM) {
+        // embm.f90:2061-2088
+        const double clampp = clamp01((a.pptn[c] - a.ppmin) / (a.ppmax - a.ppmin));
+        const double bz = a.betaz[l - 1], bm = a.betam[l - 1];
+        const double fac = (double)(2 - l) * a.diffmod0;
+        e = bz * u1 * rcj * 0.5 * a.rdphi;
+        double diffpp = a.diffa[(l - 1) + 2 * (0 + 2 * (size_t)(j - 1))] + fac * clampp;
+        double tv = rcj * rcj * a.rdphi * diffpp * a.rdphi;
+        double pec = bz * u1 * a.dphi / diffpp;
+        double ups = pec / (2.0 + fabs(pec));
+        w = e * (1 + ups) + tv;
+        e = e * (1 - ups) - tv;
+        n = cvj * bm * u2 * 0.5;
+        const double da2 = a.diffa[(l - 1) + 2 * (1 + 2 * (size_t)(j - 1))];
+        diffpp = da2 + fac * clampp;
+        if (j < maxj) {
+            tv = cvj * cvj * a.rdsv[j - 1] * da2;
+            pec = bm * u2 * a.dsv[j - 1] / diffpp;
+            ups = pec / (2.0 + fabs(pec));
+        } else {
+            tv = 0.0;
+            ups = 0.0;
+        }
+        s = n * (1 + ups) + tv;
+        n = n * (1 - ups) - tv;
+    } else {
+        // gold_seaice.f90:966-992
+        const int NK = maxi + 2;
+        const int k1c = a.k1[i + (size_t)NK * j];
+        const int k1e = a.k1[i + 1 + (size_t)NK * j], k1n = a.k1[i + (size_t)NK * (j + 1)];
+        if (a.maxk < (k1c > k1e ? k1c : k1e)) {
+            e = 0;
+            w = 0;
+        } else {
+            e = u1 * rcj * 0.5 * a.rdphi;
+            const double tv = rcj * rcj * a.rdphi * a.diffsic * a.rdphi;
+            const double pec = u1 * a.dphi / a.diffsic;
+            const double ups = pec / (2.0 + fabs(pec));
+            w = e * (1 + ups) + tv;
+            e = e * (1 - ups) - tv;
+        }
+        if (a.maxk < (k1c > k1n ? k1c : k1n)) {
+            n = 0;
+            s = 0;
+        } else {
+            n = cvj * u2 * 0.5;
+            const double tv = cvj * cvj * a.rdsv[j - 1] * a.diffsic;
+            const double pec = u2 * a.dsv[j - 1] / a.diffsic;
+            const double ups = pec / (2.0 + fabs(pec));
+            s = n * (1 + ups) + tv;
+            n = n * (1 - ups) - tv;
+        }
+    }
+    *e_ = e;
+    *w_ = w;
+    *n_ = n;
+    *s_ = s;
+}
+
+// One cluster per tracer; cluster rank r holds rows [1 + r*R, min(maxj, (r+1)*R)] (R = rows_per)
+// with the face coefficients of those rows (and the north faces of the row below, recomputed
+// locally), and the iterate tq2 of those rows plus one halo row on each side, which it copies
+// from its neighbours' shared memory (distributed shared memory) after every iterate update.
+// Shared-memory layout of every block: cie, ciw (maxi+1) x R; cin, cis (maxi+1) x (R+1) from
+// row j0-1; v2 (maxi+2) x (R+2) from row j0-1.
+__global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a, int R)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ double sm[];
     const int maxi = a.maxi, maxj = a.maxj;
-    const int ncell = maxi * maxj;
-    const int l = blockIdx.x + 1;   // tracer, 1-based
+    const int C = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+    const int l = (int)(blockIdx.x / C) + 1;   // tracer, 1-based
+    const int j0 = 1 + rank * R, j1 = min(maxj + 1, j0 + R), nrow = j1 - j0;
     const int NC = maxi + 1, NV = maxi + 2;
-    double *cie = sm, *ciw = cie + (size_t)NC * (maxj + 1), *cin = ciw + (size_t)NC * (maxj + 1);
-    double *cis = cin + (size_t)NC * (maxj + 1), *v2 = cis + (size_t)NC * (maxj + 1);
+    double *cie = sm, *ciw = cie + (size_t)NC * R, *cin = ciw + (size_t)NC * R;
+    double *cis = cin + (size_t)NC * (R + 1), *v2 = cis + (size_t)NC * (R + 1);
     const int t = threadIdx.x;
+    const int ncell = maxi * nrow;
     const bool ice = a.kind == GB_EA_SEAICE;
     const double cimp = 0.5, dt = a.dt;
 
-    // boundary rows of the local arrays (embm.f90:2054-2059, gold_seaice.f90:952-957)
-    for (int i = t; i <= maxi; i += blockDim.x) {
-        cin[i] = 0.0;
-        cis[i] = 0.0;
-        cin[i + (size_t)NC * maxj] = 0.0;
-        cis[i + (size_t)NC * maxj] = 0.0;
-    }
-    for (int i = t; i <= maxi + 1; i += blockDim.x) {
-        v2[i] = 0.0;
-        v2[i + (size_t)NV * (maxj + 1)] = 0.0;
-    }
-    __syncthreads();
-    // face coefficients of the thread's cells
-    for (int r = 0; r < kCellsPerThread; ++r) {
-        const int c = t + r * blockDim.x;
-        if (c >= ncell) break;
-        const int i = c % maxi + 1, j = c / maxi + 1;
-        const double u1 = a.vel[2 * (size_t)c], u2 = a.vel[2 * (size_t)c + 1];
-        const double rcj = a.rc[j], cvj = a.cv[j];
+    // coefficients of the block's rows; north faces of the row below (0 below j = 1: the
+    // boundary rows of embm.f90:2054-2059, gold_seaice.f90:952-957)
+    for (int c = t; c < ncell; c += blockDim.x) {
+        const int i = c % maxi + 1, j = j0 + c / maxi;
         double e, w, n, s;
-        if (!ice) {
-            // embm.f90:2061-2088
-            const double clampp = clamp01((a.pptn[c] - a.ppmin) / (a.ppmax - a.ppmin));
-            const double bz = a.betaz[l - 1], bm = a.betam[l - 1];
-            const double fac = (double)(2 - l) * a.diffmod0;
-            e = bz * u1 * rcj * 0.5 * a.rdphi;
-            double diffpp = a.diffa[(l - 1) + 2 * (0 + 2 * (size_t)(j - 1))] + fac * clampp;
-            double tv = rcj * rcj * a.rdphi * diffpp * a.rdphi;
-            double pec = bz * u1 * a.dphi / diffpp;
-            double ups = pec / (2.0 + fabs(pec));
-            w = e * (1 + ups) + tv;
-            e = e * (1 - ups) - tv;
-            n = cvj * bm * u2 * 0.5;
-            const double da2 = a.diffa[(l - 1) + 2 * (1 + 2 * (size_t)(j - 1))];
-            diffpp = da2 + fac * clampp;
-            if (j < maxj) {
-                tv = cvj * cvj * a.rdsv[j - 1] * da2;
-                pec = bm * u2 * a.dsv[j - 1] / diffpp;
-                ups = pec / (2.0 + fabs(pec));
-            } else {
-                tv = 0.0;
-                ups = 0.0;
-            }
-            s = n * (1 + ups) + tv;
-            n = n * (1 - ups) - tv;
-        } else {
-            // gold_seaice.f90:966-992
-            const int NK = maxi + 2;
-            const int k1c = a.k1[i + (size_t)NK * j];
-            const int k1e = a.k1[i + 1 + (size_t)NK * j], k1n = a.k1[i + (size_t)NK * (j + 1)];
-            if (a.maxk < (k1c > k1e ? k1c : k1e)) {
-                e = 0;
-                w = 0;
-            } else {
-                e = u1 * rcj * 0.5 * a.rdphi;
-                const double tv = rcj * rcj * a.rdphi * a.diffsic * a.rdphi;
-                const double pec = u1 * a.dphi / a.diffsic;
-                const double ups = pec / (2.0 + fabs(pec));
-                w = e * (1 + ups) + tv;
-                e = e * (1 - ups) - tv;
-            }
-            if (a.maxk < (k1c > k1n ? k1c : k1n)) {
-                n = 0;
-                s = 0;
-            } else {
-                n = cvj * u2 * 0.5;
-                const double tv = cvj * cvj * a.rdsv[j - 1] * a.diffsic;
-                const double pec = u2 * a.dsv[j - 1] / a.diffsic;
-                const double ups = pec / (2.0 + fabs(pec));
-                s = n * (1 + ups) + tv;
-                n = n * (1 - ups) - tv;
-            }
-        }
-        const size_t f = (size_t)i + (size_t)NC * j;
-        cie[f] = e;
-        ciw[f] = w;
-        cin[f] = n;
-        cis[f] = s;
+        face_coefs(a, l, i, j, &e, &w, &n, &s);
+        const int lr = j - j0;
+        cie[i + (size_t)NC * lr] = e;
+        ciw[i + (size_t)NC * lr] = w;
+        cin[i + (size_t)NC * (lr + 1)] = n;
+        cis[i + (size_t)NC * (lr + 1)] = s;
+    }
+    for (int i = 1 + t; i <= maxi; i += blockDim.x) {
+        double e, w, n = 0.0, s = 0.0;
+        if (j0 > 1) face_coefs(a, l, i, j0 - 1, &e, &w, &n, &s);
+        cin[i] = n;
+        cis[i] = s;
     }
     __syncthreads();
-    for (int j = 1 + t; j <= maxj; j += blockDim.x) {
-        cie[(size_t)NC * j] = cie[maxi + (size_t)NC * j];
-        ciw[(size_t)NC * j] = ciw[maxi + (size_t)NC * j];
+    for (int lr = t; lr < nrow; lr += blockDim.x) {   // periodic in i: cie(0,j) = cie(maxi,j)
+        cie[(size_t)NC * lr] = cie[maxi + (size_t)NC * lr];
+        ciw[(size_t)NC * lr] = ciw[maxi + (size_t)NC * lr];
     }
     __syncthreads();
 
@@ -147,43 +168,52 @@ __global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a)
         upd[r] = false;
         tq[r] = tq1[r] = src[r] = cen[r] = 0.0;
         if (c >= ncell) continue;
-        const int i = c % maxi + 1, j = c / maxi + 1;
-        const size_t x = (size_t)(l - 1) + 2 * (size_t)c;
+        const int i = c % maxi + 1, j = j0 + c / maxi, lr = j - j0;
+        const size_t x = (size_t)(l - 1) + 2 * ((size_t)(i - 1) + (size_t)maxi * (j - 1));
         tq[r] = a.tq[x];
         tq1[r] = a.tq1[x];
         // tstipa: -tqa(l,i,j); tstipsic: -dtha(l,i,j) * tsc
         src[r] = ice ? -a.src[x] * a.tsc : -a.src[x];
-        const size_t f = (size_t)i + (size_t)NC * j;
-        cen[r] = ciw[f] - cie[f - 1] + (cis[f] - cin[f - NC]) * a.rds[j - 1];
+        cen[r] = ciw[i + (size_t)NC * lr] - cie[i - 1 + (size_t)NC * lr] +
+                 (cis[i + (size_t)NC * (lr + 1)] - cin[i + (size_t)NC * lr]) * a.rds[j - 1];
         upd[r] = !ice || !(a.maxk < a.k1[i + (size_t)(maxi + 2) * j]);
     }
+    const double *v2_lo = rank > 0 ? cluster.map_shared_rank(v2, rank - 1) : nullptr;
+    const double *v2_hi = j1 <= maxj ? cluster.map_shared_rank(v2, rank + 1) : nullptr;
 
     for (int step = 0; step < a.nsteps; ++step) {
         for (int it = 0; it < 5; ++it) {
             const bool corr = it == 4;
-            // the Jacobi iterate tq2 = cimp*tq + (1-cimp)*tq1; the corrector's average with the last one
+            // own rows of the iterate: tq2 = cimp*tq + (1-cimp)*tq1; the corrector's average with the last one
 #pragma unroll
             for (int r = 0; r < kCellsPerThread; ++r) {
                 const int c = t + r * blockDim.x;
                 if (c >= ncell) continue;
-                const int i = c % maxi + 1, j = c / maxi + 1;
-                const size_t v = (size_t)i + (size_t)NV * j;
+                const int i = c % maxi + 1, lr = c / maxi + 1;
+                const size_t v = (size_t)i + (size_t)NV * lr;
                 const double nv = corr ? 0.5 * (v2[v] + cimp * tq[r] + (1.0 - cimp) * tq1[r])
                                        : cimp * tq[r] + (1.0 - cimp) * tq1[r];
                 v2[v] = nv;
-                if (i == maxi) v2[(size_t)NV * j] = nv;          // tq2(0,j) = tq2(maxi,j)
-                if (i == 1) v2[maxi + 1 + (size_t)NV * j] = nv;  // tq2(maxi+1,j) = tq2(1,j)
+                if (i == maxi) v2[(size_t)NV * lr] = nv;          // tq2(0,j) = tq2(maxi,j)
+                if (i == 1) v2[maxi + 1 + (size_t)NV * lr] = nv;  // tq2(maxi+1,j) = tq2(1,j)
             }
-            __syncthreads();
+            cluster.sync();
+            // halo rows j0-1 and j1 from the neighbours (0 outside the grid)
+            for (int i = t; i <= maxi + 1; i += blockDim.x) {
+                v2[i] = v2_lo ? v2_lo[i + (size_t)NV * R] : 0.0;
+                v2[i + (size_t)NV * (nrow + 1)] = v2_hi ? v2_hi[i + (size_t)NV * 1] : 0.0;
+            }
+            cluster.sync();   // the neighbours have their copies: own rows may change again
 #pragma unroll
             for (int r = 0; r < kCellsPerThread; ++r) {
                 const int c = t + r * blockDim.x;
                 if (c >= ncell || !upd[r]) continue;
-                const int i = c % maxi + 1, j = c / maxi + 1;
-                const size_t v = (size_t)i + (size_t)NV * j, f = (size_t)i + (size_t)NC * j;
+                const int i = c % maxi + 1, lr = c / maxi, j = j0 + lr;
+                const size_t v = (size_t)i + (size_t)NV * (lr + 1);
+                const size_t fe = (size_t)i + (size_t)NC * lr, fn = (size_t)i + (size_t)NC * (lr + 1);
                 const double rdsj = a.rds[j - 1];
-                const double flux = src[r] + cie[f] * v2[v + 1] - ciw[f - 1] * v2[v - 1] +
-                                    (cin[f] * v2[v + NV] - cis[f - NC] * v2[v - NV]) * rdsj;
+                const double flux = src[r] + cie[fe] * v2[v + 1] - ciw[fe - 1] * v2[v - 1] +
+                                    (cin[fn] * v2[v + NV] - cis[fn - NC] * v2[v - NV]) * rdsj;
                 if (!corr) {
                     const double centre = dt * cen[r];
                     tq[r] = (tq1[r] * (1.0 - (1.0 - cimp) * centre) - dt * flux) / (1 + cimp * centre);
@@ -202,15 +232,23 @@ __global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a)
     for (int r = 0; r < kCellsPerThread; ++r) {
         const int c = t + r * blockDim.x;
         if (c >= ncell) continue;
-        const size_t x = (size_t)(l - 1) + 2 * (size_t)c;
+        const int i = c % maxi + 1, j = j0 + c / maxi;
+        const size_t x = (size_t)(l - 1) + 2 * ((size_t)(i - 1) + (size_t)maxi * (j - 1));
         a.tq[x] = tq[r];
         a.tq1[x] = tq1[r];
     }
 }
 
-size_t smem_bytes(int maxi, int maxj)
+// rows per block and blocks per tracer (the cluster size, at most kClusterMax)
+void split_rows(int maxj, int *R, int *C, int cmax = kClusterMax)
 {
-    return (4 * (size_t)(maxi + 1) * (maxj + 1) + (size_t)(maxi + 2) * (maxj + 2)) * sizeof(double);
+    *R = (maxj + cmax - 1) / cmax;
+    *C = (maxj + *R - 1) / *R;
+}
+
+size_t smem_bytes(int maxi, int R)
+{
+    return (2 * (size_t)(maxi + 1) * R + 2 * (size_t)(maxi + 1) * (R + 1) + (size_t)(maxi + 2) * (R + 2)) * sizeof(double);
 }
 
 }  // namespace
@@ -224,6 +262,7 @@ struct gb_ea {
     int32_t *k1 = nullptr;
     double *tq = nullptr, *tq1 = nullptr, *src = nullptr, *vel = nullptr, *pptn = nullptr;
     bool have_state = false, have_forcing = false;
+    int cluster_max = 8;   // 16 where the device schedules clusters of 16 (gb_ea_create)
     std::string last_error;
 };
 
@@ -250,6 +289,10 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     const int maxi = dims->maxi, maxj = dims->maxj;
     if (maxi < 1 || maxj < 2) return GB_GO_EINVAL;
     if ((long long)maxi * maxj > GB_EA_MAX_CELLS) return GB_GO_ERANGE;
+    // limits for the portable cluster size (the larger rows per block)
+    int R = 0, C = 0;
+    split_rows(maxj, &R, &C, 8);
+    if ((long long)maxi * R > (long long)kThreads * kCellsPerThread) return GB_GO_ERANGE;   // one block's cells
     const gb_ea_params p = *params;
     if (p.kind != GB_EA_EMBM && p.kind != GB_EA_SEAICE) return GB_GO_EINVAL;
     if (!grid->rc || !grid->cv || !grid->dsv || !grid->rdsv || !grid->rds) return GB_GO_EINVAL;
@@ -259,7 +302,7 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     int smem_max = 0;
     if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
         return GB_GO_ECUDA;
-    if (smem_bytes(maxi, maxj) > (size_t)smem_max) return GB_GO_ERANGE;   // the grid must fit one block
+    if (smem_bytes(maxi, R) > (size_t)smem_max) return GB_GO_ERANGE;   // a block's rows must fit its shared memory
     gb_ea *h = new gb_ea();
     h->d = *dims;
     h->p = p;
@@ -290,7 +333,29 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     if (e == cudaSuccess && p.kind == GB_EA_EMBM) e = cudaMemset(h->k1, 0, nk * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemset(h->pptn, 0, (size_t)maxi * maxj * sizeof(double));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_surface_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(maxi, maxj));
+        e = cudaFuncSetAttribute(k_surface_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(maxi, R));
+    // clusters of up to 16 blocks where the device schedules them, else the portable 8
+    h->cluster_max = 8;
+    int R16 = 0, C16 = 0;
+    split_rows(maxj, &R16, &C16, 16);
+    if (e == cudaSuccess && C16 > 8 &&
+        cudaFuncSetAttribute(k_surface_step, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * C16);
+        cfg.blockDim = dim3(std::min(kThreads, (maxi * R16 + 31) / 32 * 32));
+        cfg.dynamicSmemBytes = smem_bytes(maxi, R16);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = C16;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_surface_step, &cfg) == cudaSuccess && nclusters >= 1)
+            h->cluster_max = 16;
+    }
+    cudaGetLastError();   // a refused query leaves no sticky error: clear the last one
     if (e != cudaSuccess) {
         const int code = e == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
         gb_ea_destroy(h);
@@ -379,9 +444,22 @@ extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
     a.src = h->src;
     a.vel = h->vel;
     a.pptn = h->pptn;
-    const int ncell = h->d.maxi * h->d.maxj;
-    const int threads = std::min(kThreads, (ncell + 31) / 32 * 32);
-    k_surface_step<<<2, threads, smem_bytes(h->d.maxi, h->d.maxj), h->stream>>>(a);
+    int R = 0, C = 0;
+    split_rows(h->d.maxj, &R, &C, h->cluster_max);
+    const int cells = h->d.maxi * R;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * C);
+    cfg.blockDim = dim3(std::min(kThreads, (cells + 31) / 32 * 32));
+    cfg.dynamicSmemBytes = smem_bytes(h->d.maxi, R);
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    EA_TRY(h, cudaLaunchKernelEx(&cfg, k_surface_step, a, R));
     count_launches(1);
     EA_TRY(h, cudaGetLastError());
     EA_TRY(h, cudaStreamSynchronize(h->stream));

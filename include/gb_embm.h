@@ -28,8 +28,9 @@ extern "C" {
 
 typedef struct gb_ea gb_ea;
 
-/* grids up to GB_EA_MAX_CELLS surface cells (one thread block holds a tracer's grid) */
-#define GB_EA_MAX_CELLS 4096
+/* grids up to GB_EA_MAX_CELLS surface cells (a cluster of up to 8 thread blocks holds a
+   tracer's grid; each block at most 4096 cells of ceil(maxj/8) rows, in shared memory) */
+#define GB_EA_MAX_CELLS 32768
 
 typedef struct {
     int32_t maxi, maxj;

@@ -27,12 +27,14 @@ def run(c, nsteps, calls=1):
     (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=12), "embm", 5, 2, 0.0),     # 10 steps, two launches
     (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=13), "embm", 3, 1, 0.7),     # pptn-dependent diffusion
     (dict(maxi=37, maxj=23, maxk=8, maxl=2, seed=14), "embm", 2, 1, 0.0),      # odd shape
-    (dict(maxi=64, maxj=64, maxk=8, maxl=2, seed=15), "embm", 2, 1, 0.0),      # largest grid (4096 cells)
+    (dict(maxi=64, maxj=64, maxk=8, maxl=2, seed=15), "embm", 2, 1, 0.0),      # 8 blocks of 8 rows per tracer
+    (dict(maxi=128, maxj=61, maxk=8, maxl=2, seed=21), "embm", 2, 1, 0.0),     # ragged last block (5 rows)
+    (dict(maxi=180, maxj=90, maxk=8, maxl=2, seed=22, land_frac=0.4), "seaice", 1, 1, 0.0),   # 16,200 cells
     (dict(maxi=1, maxj=2, maxk=4, maxl=2, seed=16, land_frac=0.0), "embm", 2, 1, 0.0),   # smallest grid
     (dict(maxi=12, maxj=10, maxk=8, maxl=2, seed=17), "seaice", 1, 1, 0.0),
     (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=18, land_frac=0.5), "seaice", 1, 3, 0.0),
-], ids=["embm_small", "embm_10steps", "embm_diffmod", "embm_odd", "embm_64x64", "embm_1x2", "ice_small",
-        "ice_land_3calls"])
+], ids=["embm_small", "embm_10steps", "embm_diffmod", "embm_odd", "embm_64x64", "embm_128x61", "ice_180x90",
+        "embm_1x2", "ice_small", "ice_land_3calls"])
 def test_bitexact_vs_oracle(gpu_lib, cfg, kind, nsteps, calls, dm):
     m = grid.make_member(grid.MemberConfig(**cfg))
     c = surface.embm_case(m, seed=3, diffmod0=dm) if kind == "embm" else surface.seaice_case(m, seed=3)
@@ -58,7 +60,7 @@ def test_errors(gpu_lib):
         s.step(2)                 # sea ice: one step per call
     assert e.value.code == abi.GB_GO_EINVAL
     s.close()
-    big = grid.make_member(grid.MemberConfig(maxi=72, maxj=64, maxk=8, maxl=2, seed=20))
+    big = grid.make_member(grid.MemberConfig(maxi=200, maxj=200, maxk=8, maxl=2, seed=20))   # 40,000 cells
     with pytest.raises(GoldsteinError) as e:
         surface.SurfaceStepper(surface.embm_case(big, seed=5))
     assert e.value.code == abi.GB_GO_ERANGE
