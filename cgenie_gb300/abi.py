@@ -89,6 +89,7 @@ class GbBgParams(C.Structure):
 
 GB_EA_EMBM = 0
 GB_EA_SEAICE = 1
+GB_EA_SEAICE_EXPLICIT = 2
 GB_EA_MAX_CELLS = 32768
 
 
@@ -102,7 +103,8 @@ class GbEaParams(C.Structure):
     _fields_ = [("kind", C.c_int32), ("maxk", C.c_int32), ("dt", C.c_double), ("dphi", C.c_double),
                 ("rdphi", C.c_double), ("betaz", C.c_double * 2), ("betam", C.c_double * 2),
                 ("diffmod0", C.c_double), ("ppmin", C.c_double), ("ppmax", C.c_double),
-                ("diffsic", C.c_double), ("tsc", C.c_double)]
+                ("diffsic", C.c_double), ("tsc", C.c_double), ("sica_thresh", C.c_double),
+                ("sich_thresh", C.c_double)]
 
 
 class GbEaGrid(C.Structure):

@@ -1,6 +1,7 @@
-// 2-D iterative implicit surface steppers on the device: the EMBM atmosphere step tstipa
-// (src/embm/embm.f90:2039-2138) and the sea-ice transport step tstipsic
-// (src/goldsteinseaice/gold_seaice.f90:937-1058), behind include/gb_embm.h.
+// 2-D surface steppers on the device: the EMBM atmosphere step tstipa
+// (src/embm/embm.f90:2039-2138) and the sea-ice transport steps tstipsic
+// (src/goldsteinseaice/gold_seaice.f90:937-1058, iterative implicit) and tstepsic (:844-929,
+// explicit), behind include/gb_embm.h.
 //
 // One thread-block cluster per tracer (the two tracers never interact), its blocks splitting the
 // rows: GB300's FP64 pipe is ~2 lanes per clock per SM, so the grid's FP64 work is spread over
@@ -30,6 +31,7 @@ constexpr int kCellsPerThread = 4;     // cells of one block: at most kThreads *
 struct EaArgs {
     int maxi, maxj, maxk, kind, nsteps;
     double dt, dphi, rdphi, betaz[2], betam[2], diffmod0, ppmin, ppmax, diffsic, tsc;
+    double sica, sich;
     const double *rc, *cv, *dsv, *rdsv, *rds, *diffa;
     const int32_t *k1;
     double *tq, *tq1;
@@ -239,6 +241,59 @@ __global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a, int R)
     }
 }
 
+// tstepsic (gold_seaice.f90:844-929): the ice flux through the east face of (i, j) for tracer
+// l (the west "doorway" flux of cell 1 is the east flux of cell maxi), and through the north
+// face.  Advection stops when the receiving cell already holds more ice than the thresholds.
+__device__ __forceinline__ double ice_east(const EaArgs &a, int l, int i, int j)
+{
+    const int maxi = a.maxi, NK = maxi + 2;
+    const int ip = i == maxi ? 1 : i + 1;
+    const int k1c = a.k1[i + (size_t)NK * j], k1e = a.k1[ip + (size_t)NK * j];
+    if (a.maxk < (k1c > k1e ? k1c : k1e)) return 0;
+    auto v = [&](int ll, int ii) { return a.tq1[(size_t)(ll - 1) + 2 * ((size_t)(ii - 1) + (size_t)maxi * (j - 1))]; };
+    const double u1 = a.vel[2 * ((size_t)(i - 1) + (size_t)maxi * (j - 1))];
+    const double rcj = a.rc[j];
+    double f = u1 * rcj * (v(l, ip) + v(l, i)) * 0.5;
+    const int down = u1 >= 0.0 ? ip : i;
+    if (v(2, down) > a.sica) f = 0;
+    if (v(1, down) > a.sich) f = 0;
+    return f - (v(l, ip) - v(l, i)) * rcj * rcj * a.rdphi * a.diffsic;
+}
+
+__device__ __forceinline__ double ice_north(const EaArgs &a, int l, int i, int j)
+{
+    const int maxi = a.maxi, NK = maxi + 2;
+    const int k1c = a.k1[i + (size_t)NK * j], k1n = a.k1[i + (size_t)NK * (j + 1)];
+    if (a.maxk < (k1c > k1n ? k1c : k1n)) return 0;   // always for j = maxj: row maxj+1 is land
+    auto v = [&](int ll, int jj) { return a.tq1[(size_t)(ll - 1) + 2 * ((size_t)(i - 1) + (size_t)maxi * (jj - 1))]; };
+    const double u2 = a.vel[2 * ((size_t)(i - 1) + (size_t)maxi * (j - 1)) + 1];
+    const double cvj = a.cv[j];
+    double f = cvj * u2 * (v(l, j + 1) + v(l, j)) * 0.5;
+    const int down = u2 >= 0.0 ? j + 1 : j;
+    if (v(2, down) > a.sica) f = 0;
+    if (v(1, down) > a.sich) f = 0;
+    return f - cvj * cvj * (v(l, j + 1) - v(l, j)) * a.rdsv[j - 1] * a.diffsic;
+}
+
+// One thread per cell: the reference's west and south carries are the east and north fluxes of
+// the neighbours, recomputed here with the same expressions.
+__global__ void __launch_bounds__(256) k_seaice_explicit(EaArgs a)
+{
+    const int maxi = a.maxi, maxj = a.maxj;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= maxi * maxj) return;
+    const int i = c % maxi + 1, j = c / maxi + 1;
+    if (a.maxk < a.k1[i + (size_t)(maxi + 2) * j]) return;
+    for (int l = 1; l <= 2; ++l) {
+        const double fe = ice_east(a, l, i, j);
+        const double fw = ice_east(a, l, i == 1 ? maxi : i - 1, j);
+        const double fn = ice_north(a, l, i, j);
+        const double fs = j > 1 ? ice_north(a, l, i, j - 1) : 0.0;
+        const size_t x = (size_t)(l - 1) + 2 * (size_t)c;
+        a.tq[x] = a.tq1[x] - a.dt * ((fe - fw) * a.rdphi + (fn - fs) * a.rds[j - 1]) + a.tsc * a.dt * a.src[x];
+    }
+}
+
 // rows per block and blocks per tracer (the cluster size, at most kClusterMax)
 void split_rows(int maxj, int *R, int *C, int cmax = kClusterMax)
 {
@@ -294,10 +349,16 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     split_rows(maxj, &R, &C, 8);
     if ((long long)maxi * R > (long long)kThreads * kCellsPerThread) return GB_GO_ERANGE;   // one block's cells
     const gb_ea_params p = *params;
-    if (p.kind != GB_EA_EMBM && p.kind != GB_EA_SEAICE) return GB_GO_EINVAL;
+    if (p.kind != GB_EA_EMBM && p.kind != GB_EA_SEAICE && p.kind != GB_EA_SEAICE_EXPLICIT) return GB_GO_EINVAL;
     if (!grid->rc || !grid->cv || !grid->dsv || !grid->rdsv || !grid->rds) return GB_GO_EINVAL;
     if (p.kind == GB_EA_EMBM && !grid->diffa) return GB_GO_EINVAL;
-    if (p.kind == GB_EA_SEAICE && (!grid->k1 || p.maxk < 1)) return GB_GO_EINVAL;
+    if (p.kind != GB_EA_EMBM) {
+        if (!grid->k1 || p.maxk < 1) return GB_GO_EINVAL;
+        // rows 0 and maxj+1 are land (the reference's grid convention): no north face of row maxj
+        // is wet, so nothing reads beyond row maxj
+        for (int i = 0; i <= maxi + 1; ++i)
+            if (grid->k1[i] <= p.maxk || grid->k1[i + (size_t)(maxi + 2) * (maxj + 1)] <= p.maxk) return GB_GO_EINVAL;
+    }
     if (device < 0) cudaGetDevice(&device);
     int smem_max = 0;
     if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
@@ -328,7 +389,7 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     up(&h->pptn, nullptr, (size_t)maxi * maxj);
     const size_t nk = (size_t)(maxi + 2) * (maxj + 2);
     if (e == cudaSuccess) e = cudaMalloc(&h->k1, nk * sizeof(int32_t));
-    if (e == cudaSuccess && p.kind == GB_EA_SEAICE)
+    if (e == cudaSuccess && p.kind != GB_EA_EMBM)
         e = cudaMemcpy(h->k1, grid->k1, nk * sizeof(int32_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && p.kind == GB_EA_EMBM) e = cudaMemset(h->k1, 0, nk * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemset(h->pptn, 0, (size_t)maxi * maxj * sizeof(double));
@@ -409,7 +470,7 @@ extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
 {
     if (!h) return GB_GO_EINVAL;
     if (nsteps < 0) return efail(h, GB_GO_EINVAL, "step: nsteps < 0");
-    if (h->p.kind == GB_EA_SEAICE && nsteps > 1)
+    if (h->p.kind != GB_EA_EMBM && nsteps > 1)
         return efail(h, GB_GO_EINVAL, "step: sea ice takes one step per call (step_seaice post-processes between steps)");
     if (!h->have_state || !h->have_forcing) return efail(h, GB_GO_ENOTREADY, "step before upload_state/set_forcing");
     if (nsteps == 0) return GB_GO_OK;
@@ -432,6 +493,8 @@ extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
     a.ppmax = h->p.ppmax;
     a.diffsic = h->p.diffsic;
     a.tsc = h->p.tsc;
+    a.sica = h->p.sica_thresh;
+    a.sich = h->p.sich_thresh;
     a.rc = h->rc;
     a.cv = h->cv;
     a.dsv = h->dsv;
@@ -444,6 +507,14 @@ extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
     a.src = h->src;
     a.vel = h->vel;
     a.pptn = h->pptn;
+    if (h->p.kind == GB_EA_SEAICE_EXPLICIT) {
+        const int ncell = h->d.maxi * h->d.maxj;
+        k_seaice_explicit<<<(ncell + 255) / 256, 256, 0, h->stream>>>(a);
+        count_launches(1);
+        EA_TRY(h, cudaGetLastError());
+        EA_TRY(h, cudaStreamSynchronize(h->stream));
+        return GB_GO_OK;
+    }
     int R = 0, C = 0;
     split_rows(h->d.maxj, &R, &C, h->cluster_max);
     const int cells = h->d.maxi * R;

@@ -9,8 +9,8 @@
 !     in place of the routine; go_ts/go_ts1 stay on the device in the gb_go handle.
 !   - tstipa (src/embm/embm.f90:2039-2138): gb_ea_set_forcing(tqa, uatm, pptn) then
 !     gb_ea_step(eah, 1) in place of CALL tstipa.
-!   - tstipsic (src/goldsteinseaice/gold_seaice.f90:937-1058): gb_ea_set_forcing(dtha, u, NULL)
-!     then gb_ea_step(sih, 1).
+!   - tstipsic (src/goldsteinseaice/gold_seaice.f90:937-1058) or tstepsic (:844-929):
+!     gb_ea_set_forcing(dtha, u, NULL) then gb_ea_step(sih, 1).
 !
 ! Not compiled in this repository (no Fortran compiler on the build machines); the same
 ! entry points are exercised from C via ctypes in tests/.
@@ -32,11 +32,12 @@ MODULE gb_surface_biogem_c
   END TYPE gb_ea_dims
 
   TYPE, BIND(C) :: gb_ea_params
-     INTEGER(C_INT32_T) :: kind, maxk        ! 0: tstipa, 1: tstipsic
+     INTEGER(C_INT32_T) :: kind, maxk        ! 0: tstipa, 1: tstipsic, 2: tstepsic
      REAL(C_DOUBLE) :: dt, dphi, rdphi
      REAL(C_DOUBLE) :: betaz(2), betam(2)
      REAL(C_DOUBLE) :: diffmod0, ppmin, ppmax
      REAL(C_DOUBLE) :: diffsic, tsc
+     REAL(C_DOUBLE) :: sica_thresh, sich_thresh   ! par_sica_thresh, par_sich_thresh (tstepsic)
   END TYPE gb_ea_params
 
   TYPE, BIND(C) :: gb_ea_grid

@@ -48,12 +48,15 @@ class SurfaceCase:
     ppmax: float = 1.0
     diffsic: float = 0.0
     tsc: float = 0.0
+    sica_thresh: float = 0.0
+    sich_thresh: float = 0.0
     keep: list = field(default_factory=list)
 
     def params(self) -> abi.GbEaParams:
         return abi.GbEaParams(self.kind, self.maxk, self.dt, self.dphi, self.rdphi,
                               (C.c_double * 2)(*self.betaz), (C.c_double * 2)(*self.betam),
-                              self.diffmod0, self.ppmin, self.ppmax, self.diffsic, self.tsc)
+                              self.diffmod0, self.ppmin, self.ppmax, self.diffsic, self.tsc, self.sica_thresh,
+                              self.sich_thresh)
 
     def grid(self) -> abi.GbEaGrid:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (self.rc, self.cv, self.dsv, self.rdsv, self.rds)]
@@ -98,9 +101,10 @@ def embm_case(member, seed: int = 0, diffmod0: float = 0.0) -> SurfaceCase:
                        betaz=(0.1, 0.9), betam=(0.0, 0.4), diffmod0=diffmod0, ppmin=1e-8, ppmax=2e-8)
 
 
-def seaice_case(member, seed: int = 0) -> SurfaceCase:
+def seaice_case(member, seed: int = 0, explicit: bool = False) -> SurfaceCase:
     """A sea-ice step on a member's grid and mask: ice height (m) and area fraction where the
-    seeded surface is cold, the member's surface ocean velocities, seeded thermodynamic rates."""
+    seeded surface is cold, the member's surface ocean velocities, seeded thermodynamic rates.
+    explicit: the tstepsic form, with area/height thresholds (0.9, 2.5 m) that some cells pass."""
     rng = np.random.default_rng(seed)
     m = member
     mi, mj = m.maxi, m.maxj
@@ -117,9 +121,10 @@ def seaice_case(member, seed: int = 0) -> SurfaceCase:
     usc, rsc = 0.05, 6.37e6
     tsc = rsc / usc
     source = np.where(wet[..., None], 1e-9 * rng.standard_normal((mj, mi, 2)), 0.0)
-    return SurfaceCase(kind=abi.GB_EA_SEAICE, maxi=mi, maxj=mj, maxk=m.maxk, dt=float(m.dt[0]),
-                       dphi=m.dphi, rdphi=m.rdphi, rc=m.rc, cv=m.cv, dsv=m.dsv, rdsv=m.rdsv, rds=m.rds,
-                       tq=tq, tq1=tq1, source=source, vel=vel, k1=k1, diffsic=2000.0 / (rsc * usc), tsc=tsc)
+    return SurfaceCase(kind=abi.GB_EA_SEAICE_EXPLICIT if explicit else abi.GB_EA_SEAICE, maxi=mi, maxj=mj,
+                       maxk=m.maxk, dt=float(m.dt[0]), dphi=m.dphi, rdphi=m.rdphi, rc=m.rc, cv=m.cv, dsv=m.dsv,
+                       rdsv=m.rdsv, rds=m.rds, tq=tq, tq1=tq1, source=source, vel=vel, k1=k1,
+                       diffsic=2000.0 / (rsc * usc), tsc=tsc, sica_thresh=0.9, sich_thresh=2.5)
 
 
 class SurfaceStepper:

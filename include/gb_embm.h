@@ -36,12 +36,15 @@ typedef struct {
     int32_t maxi, maxj;
 } gb_ea_dims;
 
-/* kind = GB_EA_EMBM: tstipa.  dt = dtatm, betaz/betam (embm_lib.f90:98), diffmod0, ppmin,
+/* kind = GB_EA_SEAICE_EXPLICIT: tstepsic: as GB_EA_SEAICE, plus the area and height thresholds
+   above which advection into a cell stops.
+   kind = GB_EA_EMBM: tstipa.  dt = dtatm, betaz/betam (embm_lib.f90:98), diffmod0, ppmin,
    ppmax (embm_lib.f90:83, 112).
    kind = GB_EA_SEAICE: tstipsic.  dt = dtsic, diffsic, tsc (the source term is
    dtha(l,i,j)*tsc); betaz, betam, diffmod0, ppmin, ppmax unused. */
 #define GB_EA_EMBM 0
 #define GB_EA_SEAICE 1
+#define GB_EA_SEAICE_EXPLICIT 2   /* tstepsic (gold_seaice.f90:844-929), the impsic = .FALSE. step */
 typedef struct {
     int32_t kind;
     int32_t maxk;        /* sea ice: land iff k1(i,j) > maxk */
@@ -49,6 +52,7 @@ typedef struct {
     double betaz[2], betam[2];
     double diffmod0, ppmin, ppmax;
     double diffsic, tsc;
+    double sica_thresh, sich_thresh;   /* tstepsic: par_sica_thresh, par_sich_thresh */
 } gb_ea_params;
 
 typedef struct {

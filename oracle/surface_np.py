@@ -1,9 +1,11 @@
 """ORACLE -- test infrastructure only (tests and bench.py's CPU leg use it, the product never does).
 
-Independent NumPy restatement of the 2-D iterative implicit surface steppers, written from
-the Fortran separately from oracle/surface_oracle.c:
+Independent NumPy restatement of the 2-D surface steppers, written from the Fortran
+separately from oracle/surface_oracle.c:
   tstipa    src/embm/embm.f90:2039-2138
   tstipsic  src/goldsteinseaice/gold_seaice.f90:937-1058 (without the diagnostics of :1047-1055)
+  tstepsic  src/goldsteinseaice/gold_seaice.f90:844-929 (as whole-array face fluxes: the
+            reference's west/south carries are the east/north fluxes of the neighbours)
 Arrays are [j, i] views (C order) of the Fortran (i, j) fields; tq is [j, i, l].  Every cell's
 arithmetic is elementwise, so whole-array NumPy expressions evaluate the same IEEE operations
 in the same order as the Fortran loops.
@@ -88,3 +90,35 @@ def step(kind, maxk, dt, dphi, rdphi, betaz, betam, diffmod0, ppmin, ppmax, diff
             tq[..., l] = t
         if kind == 0:
             tq1[...] = tq
+
+
+def tstepsic(maxk, dt, rdphi, diffsic, tsc, sica, sich, rc, cv, rdsv, rds, k1, tq, tq1, dtha, vel):
+    """The explicit sea-ice step; tq, tq1, dtha, vel [j, i, l]; updates tq on wet cells."""
+    maxj, maxi = tq.shape[:2]
+    rcj, cvj, rdsj = rc[1:maxj + 1][:, None], cv[1:maxj + 1][:, None], rds[:, None]
+    rdsv_j = np.concatenate([rdsv, [0.0]])[:, None]
+    k1c = k1[1:maxj + 1, 1:maxi + 1]
+    k1e = k1[1:maxj + 1, 2:maxi + 2]
+    k1n = k1[2:maxj + 2, 1:maxi + 1]
+    u1, u2 = vel[..., 0], vel[..., 1]
+    ve = np.roll(tq1, -1, axis=1)                                   # cell i+1 (periodic)
+    vn = np.concatenate([tq1[1:], np.zeros((1, maxi, 2))], axis=0)  # cell j+1 (row maxj+1 unused: land)
+    # east faces: the receiving cell's ice stops advection
+    stop_e = np.where(u1 >= 0.0, (ve[..., 1] > sica) | (ve[..., 0] > sich),
+                      (tq1[..., 1] > sica) | (tq1[..., 0] > sich))
+    stop_n = np.where(u2 >= 0.0, (vn[..., 1] > sica) | (vn[..., 0] > sich),
+                      (tq1[..., 1] > sica) | (tq1[..., 0] > sich))
+    fe = np.zeros_like(tq1)
+    fn = np.zeros_like(tq1)
+    for l in range(2):
+        adv = np.where(stop_e, 0.0, u1 * rcj * (ve[..., l] + tq1[..., l]) * 0.5)
+        fe[..., l] = np.where(maxk < np.maximum(k1c, k1e), 0.0,
+                              adv - (ve[..., l] - tq1[..., l]) * rcj * rcj * rdphi * diffsic)
+        adv = np.where(stop_n, 0.0, cvj * u2 * (vn[..., l] + tq1[..., l]) * 0.5)
+        fn[..., l] = np.where(maxk < np.maximum(k1c, k1n), 0.0,
+                              adv - cvj * cvj * (vn[..., l] - tq1[..., l]) * rdsv_j * diffsic)
+    fw = np.roll(fe, 1, axis=1)
+    fs = np.concatenate([np.zeros((1, maxi, 2)), fn[:-1]], axis=0)
+    new = tq1 - dt * ((fe - fw) * rdphi + (fn - fs) * rdsj[..., None]) + tsc * dt * dtha
+    wet = (k1c <= maxk)[..., None]
+    tq[...] = np.where(wet, new, tq)

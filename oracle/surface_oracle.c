@@ -7,6 +7,7 @@
  *   tstipa    src/embm/embm.f90:2039-2138                   (EMBM air temperature, humidity)
  *   tstipsic  src/goldsteinseaice/gold_seaice.f90:937-1058  (sea-ice height, area; the
  *             diagnostic variceth/varicedy of :1047-1055 are not restated)
+ *   tstepsic  src/goldsteinseaice/gold_seaice.f90:844-929   (the explicit sea-ice step)
  * Arrays as in include/gb_embm.h.  Every expression keeps gfortran's left-to-right
  * evaluation in IEEE double; compile with -ffp-contract=off.
  *
@@ -95,11 +96,88 @@ static void coefficients(const gb_ea_dims *d, const gb_ea_params *p, const gb_ea
     }
 }
 
+/* tstepsic, with the reference's west/south flux carries (gold_seaice.f90:844-929);
+   tq = varice (written on wet cells), tq1 = varice1 */
+static int tstepsic(const gb_ea_dims *d, const gb_ea_params *p, const gb_ea_grid *g, double *tq, const double *tq1,
+                    const double *dtha, const double *u)
+{
+    const int maxi = d->maxi, maxj = d->maxj, maxk = p->maxk;
+    double fe[2], fw[2], fn[2], fwsave[2];
+    double *fs = calloc(2 * (size_t)maxi, sizeof(double));   /* fs(2, maxi) = 0 */
+    if (!fs) return -2;
+#define FS(l, i) fs[((l) - 1) + 2 * ((size_t)(i) - 1)]
+    for (int j = 1; j <= maxj; ++j) {
+        for (int l = 1; l <= 2; ++l) {
+            const int kk = K1(maxi, j) > K1(1, j) ? K1(maxi, j) : K1(1, j);
+            if (maxk >= kk) {
+                fw[l - 1] = TQ(u, 1, maxi, j) * g->rc[j] * (TQ(tq1, l, 1, j) + TQ(tq1, l, maxi, j)) * 0.5;
+                if (TQ(u, 1, maxi, j) >= 0.0) {
+                    if (TQ(tq1, 2, 1, j) > p->sica_thresh) fw[l - 1] = 0;
+                    if (TQ(tq1, 1, 1, j) > p->sich_thresh) fw[l - 1] = 0;
+                } else {
+                    if (TQ(tq1, 2, maxi, j) > p->sica_thresh) fw[l - 1] = 0;
+                    if (TQ(tq1, 1, maxi, j) > p->sich_thresh) fw[l - 1] = 0;
+                }
+                fw[l - 1] = fw[l - 1] - (TQ(tq1, l, 1, j) - TQ(tq1, l, maxi, j)) * g->rc[j] * g->rc[j] * p->rdphi * p->diffsic;
+            } else {
+                fw[l - 1] = 0;
+            }
+            fwsave[l - 1] = fw[l - 1];
+        }
+        for (int i = 1; i <= maxi; ++i)
+            for (int l = 1; l <= 2; ++l) {
+                const int ke = K1(i, j) > K1(i + 1, j) ? K1(i, j) : K1(i + 1, j);
+                if (i == maxi) {
+                    fe[l - 1] = fwsave[l - 1];
+                } else if (maxk < ke) {
+                    fe[l - 1] = 0;
+                } else {
+                    fe[l - 1] = TQ(u, 1, i, j) * g->rc[j] * (TQ(tq1, l, i + 1, j) + TQ(tq1, l, i, j)) * 0.5;
+                    if (TQ(u, 1, i, j) >= 0.0) {
+                        if (TQ(tq1, 2, i + 1, j) > p->sica_thresh) fe[l - 1] = 0;
+                        if (TQ(tq1, 1, i + 1, j) > p->sich_thresh) fe[l - 1] = 0;
+                    } else {
+                        if (TQ(tq1, 2, i, j) > p->sica_thresh) fe[l - 1] = 0;
+                        if (TQ(tq1, 1, i, j) > p->sich_thresh) fe[l - 1] = 0;
+                    }
+                    fe[l - 1] = fe[l - 1] - (TQ(tq1, l, i + 1, j) - TQ(tq1, l, i, j)) * g->rc[j] * g->rc[j] * p->rdphi * p->diffsic;
+                }
+                const int kn = K1(i, j) > K1(i, j + 1) ? K1(i, j) : K1(i, j + 1);
+                if (maxk < kn) {
+                    fn[l - 1] = 0;
+                } else {
+                    /* j + 1 <= maxj here: row maxj + 1 is land */
+                    fn[l - 1] = g->cv[j] * TQ(u, 2, i, j) * (TQ(tq1, l, i, j + 1) + TQ(tq1, l, i, j)) * 0.5;
+                    if (TQ(u, 2, i, j) >= 0.0) {
+                        if (TQ(tq1, 2, i, j + 1) > p->sica_thresh) fn[l - 1] = 0;
+                        if (TQ(tq1, 1, i, j + 1) > p->sich_thresh) fn[l - 1] = 0;
+                    } else {
+                        if (TQ(tq1, 2, i, j) > p->sica_thresh) fn[l - 1] = 0;
+                        if (TQ(tq1, 1, i, j) > p->sich_thresh) fn[l - 1] = 0;
+                    }
+                    fn[l - 1] = fn[l - 1] - g->cv[j] * g->cv[j] * (TQ(tq1, l, i, j + 1) - TQ(tq1, l, i, j)) * g->rdsv[j - 1] * p->diffsic;
+                }
+                if (maxk >= K1(i, j))
+                    TQ(tq, l, i, j) = TQ(tq1, l, i, j) - p->dt * ((fe[l - 1] - fw[l - 1]) * p->rdphi + (fn[l - 1] - FS(l, i)) * g->rds[j - 1]) +
+                                      p->tsc * p->dt * TQ(dtha, l, i, j);
+                fw[l - 1] = fe[l - 1];
+                FS(l, i) = fn[l - 1];
+            }
+    }
+#undef FS
+    free(fs);
+    return 0;
+}
+
 int gbo_ea_step(const gb_ea_dims *d, const gb_ea_params *p, const gb_ea_grid *g, double *tq, double *tq1,
                 const double *source, const double *vel, const double *pptn, int nsteps)
 {
     const int maxi = d->maxi, maxj = d->maxj;
     if (maxi < 1 || maxj < 2 || nsteps < 0) return -1;
+    if (p->kind == GB_EA_SEAICE_EXPLICIT) {
+        if (nsteps > 1) return -1;
+        return nsteps ? tstepsic(d, p, g, tq, tq1, source, vel) : 0;
+    }
     if (p->kind == GB_EA_SEAICE && nsteps > 1) return -1;
     const size_t nc = (size_t)(maxi + 1) * (maxj + 1), nv = (size_t)(maxi + 2) * (maxj + 2);
     double *cie = calloc(nc, sizeof(double)), *ciw = calloc(nc, sizeof(double));

@@ -41,7 +41,7 @@ def test_struct_layouts():
     assert C.sizeof(abi.GbBgDims) == 24
     assert C.sizeof(abi.GbBgParams) == 24
     assert C.sizeof(abi.GbEaDims) == 8
-    assert C.sizeof(abi.GbEaParams) == 8 + 12 * 8
+    assert C.sizeof(abi.GbEaParams) == 8 + 14 * 8
     assert C.sizeof(abi.GbEaGrid) == 7 * 8
 
 

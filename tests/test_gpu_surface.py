@@ -33,11 +33,16 @@ def run(c, nsteps, calls=1):
     (dict(maxi=1, maxj=2, maxk=4, maxl=2, seed=16, land_frac=0.0), "embm", 2, 1, 0.0),   # smallest grid
     (dict(maxi=12, maxj=10, maxk=8, maxl=2, seed=17), "seaice", 1, 1, 0.0),
     (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=18, land_frac=0.5), "seaice", 1, 3, 0.0),
+    (dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=23, land_frac=0.5), "ice_explicit", 1, 2, 0.0),
+    (dict(maxi=37, maxj=23, maxk=8, maxl=2, seed=24, land_frac=0.0), "ice_explicit", 1, 1, 0.0),
 ], ids=["embm_small", "embm_10steps", "embm_diffmod", "embm_odd", "embm_64x64", "embm_128x61", "ice_180x90",
-        "embm_1x2", "ice_small", "ice_land_3calls"])
+        "embm_1x2", "ice_small", "ice_land_3calls", "ice_explicit_land", "ice_explicit_odd"])
 def test_bitexact_vs_oracle(gpu_lib, cfg, kind, nsteps, calls, dm):
     m = grid.make_member(grid.MemberConfig(**cfg))
-    c = surface.embm_case(m, seed=3, diffmod0=dm) if kind == "embm" else surface.seaice_case(m, seed=3)
+    if kind == "embm":
+        c = surface.embm_case(m, seed=3, diffmod0=dm)
+    else:
+        c = surface.seaice_case(m, seed=3, explicit=kind == "ice_explicit")
     tq, tq1 = run(c.copy(), nsteps, calls)
     ref = c.copy()
     for _ in range(calls):
@@ -64,3 +69,10 @@ def test_errors(gpu_lib):
     with pytest.raises(GoldsteinError) as e:
         surface.SurfaceStepper(surface.embm_case(big, seed=5))
     assert e.value.code == abi.GB_GO_ERANGE
+    # sea ice needs land in rows 0 and maxj+1 (nothing may read beyond row maxj)
+    c = surface.seaice_case(m, seed=6)
+    c.k1 = c.k1.copy()
+    c.k1[-1, 3] = 1
+    with pytest.raises(GoldsteinError) as e:
+        surface.SurfaceStepper(c)
+    assert e.value.code == abi.GB_GO_EINVAL

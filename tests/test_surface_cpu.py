@@ -62,3 +62,19 @@ def test_oracle_header_cites_reference():
     assert "ORACLE -- test infrastructure only" in src
     assert "embm.f90:2039-2138" in src and "gold_seaice.f90:937-1058" in src
     assert "parity unpinned" in src
+
+
+@pytest.mark.parametrize("cfg", [dict(maxi=12, maxj=10, maxk=8, maxl=2, seed=9),
+                                 dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=10, land_frac=0.5)])
+def test_explicit_seaice_restatements_agree(cfg):
+    """tstepsic: the C oracle keeps the reference's west/south flux carries, the NumPy one
+    computes whole-array face fluxes; the area/height thresholds stop advection in some cells."""
+    m = grid.make_member(grid.MemberConfig(**cfg))
+    c = surface.seaice_case(m, seed=11, explicit=True)
+    assert (c.tq1[..., 1] > c.sica_thresh).any() and (c.tq1[..., 0] > c.sich_thresh).any()
+    a, b = c.copy(), c.copy()
+    ol.surface_step(a, 1)
+    snp.tstepsic(b.maxk, b.dt, b.rdphi, b.diffsic, b.tsc, b.sica_thresh, b.sich_thresh, b.rc, b.cv, b.rdsv, b.rds,
+                 b.k1, b.tq, b.tq1, b.source, b.vel)
+    assert np.array_equal(a.tq, b.tq)
+    assert not np.array_equal(a.tq, c.tq)
