@@ -30,6 +30,7 @@ SOURCES = {
     "ensemble.cu": [],
     "biogem_coupling.cu": ["-fmad=false"],
     "surface_step.cu": ["-fmad=false"],
+    "momentum.cu": ["-fmad=false"],
 }
 
 

@@ -471,6 +471,9 @@ int ocean_state(gb_go_handle *h, OceanState *o)
     o->k1 = h->k1;
     o->state_ready = h->state_ready;
     o->dry_zeroed = &h->dry_zeroed;
+    o->rho = h->rho;
+    o->u = h->u;
+    o->vel_ready = &h->vel_ready;
     return GB_GO_OK;
 }
 

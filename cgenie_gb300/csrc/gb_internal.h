@@ -107,6 +107,9 @@ struct OceanState {
     bool state_ready;
     bool *dry_zeroed;    // the interior cells that are land or below k1 hold 0 in ts_static and
                          // ts1_static (set by the coupling, cleared by an upload)
+    const double *rho;   // (0:maxi+1, 0:maxj+1, 0:maxk), the last step's density
+    double *u;           // (3, 0:maxi, 0:maxj, 1:maxk), the velocities the next step reads
+    bool *vel_ready;
 };
 }  // namespace gbgo
 struct gb_go_handle;

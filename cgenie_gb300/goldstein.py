@@ -38,6 +38,8 @@ EXPORTED = [
     "gb_bg_tracercoupling", "gb_bg_download", "gb_bg_last_error",
     "gb_ea_create", "gb_ea_destroy", "gb_ea_upload_state", "gb_ea_set_forcing", "gb_ea_step", "gb_ea_download",
     "gb_ea_last_error",
+    "gb_mo_create", "gb_mo_destroy", "gb_mo_set_wind", "gb_mo_upload_velocity", "gb_mo_step", "gb_mo_download",
+    "gb_mo_last_error",
 ]
 
 _lib = None
@@ -124,6 +126,15 @@ def load_library(path: str = LIB_PATH):
     L.gb_ea_download.argtypes = [vp, dp, dp]
     L.gb_ea_last_error.argtypes = [vp]
     L.gb_ea_last_error.restype = C.c_char_p
+    L.gb_mo_create.argtypes = [vp, vp, vp, C.c_int, P(vp)]
+    L.gb_mo_destroy.argtypes = [vp]
+    L.gb_mo_destroy.restype = None
+    L.gb_mo_set_wind.argtypes = [vp, dp, dp, dp]
+    L.gb_mo_upload_velocity.argtypes = [vp, dp, dp]
+    L.gb_mo_step.argtypes = [vp, vp]
+    L.gb_mo_download.argtypes = [vp, dp, dp, dp, dp]
+    L.gb_mo_last_error.argtypes = [vp]
+    L.gb_mo_last_error.restype = C.c_char_p
     _lib = L
     return L
 

@@ -78,6 +78,10 @@ class MemberConfig:
     mldpebuoycoeff: float = 0.15     # namelist default (goldstein-defaults.nml)
     mldwindkedec: float = 25.0       # m, wind-energy decay depth (namelist default)
     mldketau_max: float = 2.0e-5     # seeded stand-in for the wind mixing energy, upper bound
+    mask: str = "noise"          # "noise": seeded land fraction; "basin" / "basin_island": one
+                                 # continent joined to the north boundary, an open channel in
+                                 # rows 1-2 (the southern boundary is an island) and, for
+                                 # "basin_island", one rectangular island (momentum tests)
 
 
 @dataclasses.dataclass
@@ -276,6 +280,41 @@ def make_k1(rng, maxi, maxj, maxk, land_frac, land_code):
     return k1
 
 
+def basin_island_cells(maxi, maxj):
+    """(continent i-range, continent first row, island i-range, island j-range), 1-based
+    inclusive, of make_k1_basin's layout."""
+    w = max(2, maxi // 6)
+    ic0 = max(1, maxi // 6)
+    jc = max(4, maxj // 3)
+    ii0 = ic0 + w + 3
+    jj0 = max(4, maxj // 3)
+    return (ic0, ic0 + w - 1), jc, (ii0, ii0 + 1), (jj0, jj0 + 1)
+
+
+def make_k1_basin(rng, maxi, maxj, maxk, land_code, island):
+    """Seeded bathymetry on a basin: a continent of columns from row maxj//3 to the north
+    boundary, every other cell wet (rows 1-2 always), optionally a 2x2 island with two wet
+    cells around it; the reference's halo rules (goldstein.f90:1111-1118)."""
+    if maxi < 12 or maxj < 10:
+        raise ValueError("basin masks need maxi >= 12 and maxj >= 10")
+    land = land_code if land_code > maxk else maxk + 1
+    passes = max(2, int(round(min(maxi, maxj) / 9)))
+    bathy = _smooth_periodic(rng, maxi, maxj, passes)
+    nlev = np.clip(np.round(1 + (maxk - 1) * (0.15 + 0.85 * bathy) ** 0.7), 1, maxk).astype(np.int32)
+    k1i = (maxk - nlev + 1).astype(np.int32)
+    (a0, a1), jc, (b0, b1), (c0, c1) = basin_island_cells(maxi, maxj)
+    k1i[jc - 1:, a0 - 1:a1] = land
+    if island:
+        k1i[c0 - 1:c1, b0 - 1:b1] = land
+    k1 = np.full((maxj + 2, maxi + 2), land, dtype=np.int32)
+    k1[1:maxj + 1, 1:maxi + 1] = k1i
+    k1[:, 0] = k1[:, maxi]
+    k1[:, maxi + 1] = k1[:, 1]
+    k1[0, :] = land
+    k1[maxj + 1, :] = land
+    return k1
+
+
 def make_velocity(rng, maxi, maxj, maxk, k1, hg, vg, umax):
     """Seeded velocity field u(3,0:maxi,0:maxj,1:maxk), nondimensional.
 
@@ -394,7 +433,10 @@ def make_member(cfg: MemberConfig) -> Member:
     maxi, maxj, maxk, maxl = cfg.maxi, cfg.maxj, cfg.maxk, cfg.maxl
     hg = horizontal_grid(maxi, maxj)
     vg = vertical_grid(maxk)
-    k1 = make_k1(rng, maxi, maxj, maxk, cfg.land_frac, cfg.land_code)
+    if cfg.mask == "noise":
+        k1 = make_k1(rng, maxi, maxj, maxk, cfg.land_frac, cfg.land_code)
+    else:
+        k1 = make_k1_basin(rng, maxi, maxj, maxk, cfg.land_code, island=cfg.mask == "basin_island")
     u = make_velocity(rng, maxi, maxj, maxk, k1, hg, vg, cfg.umax)
     ts = make_tracers(rng, cfg, maxi, maxj, maxk, maxl, k1, vg, hg)
     ec = eos_coefficients(cfg.ieos)

@@ -23,7 +23,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle (make -C oracle)."""
-    srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c", "surface_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c", "surface_oracle.c",
+                                             "momentum_oracle.c")]
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
@@ -62,6 +63,20 @@ def lib():
         L.gbo_bg_columns.restype = C.c_int
         L.gbo_ea_step.argtypes = [P(GbEaDims), P(GbEaParams), P(GbEaGrid), dp, dp, dp, dp, dp, C.c_int]
         L.gbo_ea_step.restype = C.c_int
+        L.gbo_mo_init.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbo_mo_init.restype = C.c_void_p
+        L.gbo_mo_step.argtypes = [C.c_void_p, dp, dp, dp, dp]
+        L.gbo_mo_step.restype = C.c_int
+        L.gbo_mo_get.argtypes = [C.c_void_p, dp, dp, dp, dp, dp, dp]
+        L.gbo_mo_get.restype = None
+        L.gbo_mo_matrix.argtypes = [C.c_void_p, dp]
+        L.gbo_mo_matrix.restype = None
+        L.gbo_mo_get_islands.argtypes = [C.c_void_p, dp, dp, dp]
+        L.gbo_mo_get_islands.restype = None
+        L.gbo_mo_set_velocity.argtypes = [C.c_void_p, dp, dp]
+        L.gbo_mo_set_velocity.restype = None
+        L.gbo_mo_free.argtypes = [C.c_void_p]
+        L.gbo_mo_free.restype = None
         _lib = L
     return _lib
 
@@ -165,3 +180,53 @@ def surface_step(case, nsteps: int = 1):
                            dptr(pp), int(nsteps))
     if rc != 0:
         raise RuntimeError(f"oracle gbo_ea_step failed: {rc}")
+
+
+class OracleMomentum:
+    """The C restatement of the momentum step (oracle/momentum_oracle.c) on a
+    cgenie_gb300.momentum.MomentumCase."""
+
+    def __init__(self, case):
+        self.case = case
+        self._d, self._p, self._g = case.dims(), case.params(), case.grid()
+        self.s = lib().gbo_mo_init(C.byref(self._d), C.byref(self._p), C.byref(self._g))
+        if not self.s:
+            raise RuntimeError("oracle gbo_mo_init failed")
+
+    def close(self):
+        if self.s:
+            lib().gbo_mo_free(self.s)
+            self.s = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, rho, tau=None, dztau=None, dztav=None):
+        c = self.case
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in
+                (c.tau if tau is None else tau, c.dztau if dztau is None else dztau,
+                 c.dztav if dztav is None else dztav, rho)]
+        lib().gbo_mo_step(self.s, *[dptr(a) for a in arrs])
+
+    def state(self):
+        c = self.case
+        nu = (c.maxk, c.maxj + 1, c.maxi + 1, 3)
+        u, u1 = np.zeros(nu), np.zeros(nu)
+        ub = np.zeros((c.maxj + 1, c.maxi + 2, 2))
+        psi = np.zeros((c.maxj + 1, c.maxi + 1))
+        lib().gbo_mo_get(self.s, dptr(u), dptr(u1), dptr(ub), dptr(psi), None, None)
+        return dict(u=u, u1=u1, ub=ub, psi=psi)
+
+    def matrix(self):
+        nm = self.case.maxi * (self.case.maxj + 1)
+        A = np.zeros((nm, nm))
+        lib().gbo_mo_matrix(self.s, dptr(A))
+        return A
+
+    def islands(self):
+        c = self.case
+        psisl = np.zeros((c.isles, c.maxj + 1, c.maxi + 1))
+        ubisl = np.zeros((c.isles, c.maxj + 1, c.maxi + 2, 2))
+        erisl = np.zeros((c.isles + 1, c.isles))
+        lib().gbo_mo_get_islands(self.s, dptr(psisl), dptr(ubisl), dptr(erisl))
+        return psisl, ubisl, erisl
