@@ -15,6 +15,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
       `value` is tracer cell-couplings/s (one tracer of one wet cell coupled)
   ea64 the EMBM atmosphere step (tstipa) on a 64x64 surface grid, one launch per step as
       the model calls it; `value` is air cell-updates/s
+  mo36 the momentum step (wind, jbar, streamfunction, islands, velc) of a 36x36x16 basin
+      with two islands, on the density of an FP64 handle; `value` is wet-cell momentum
+      updates/s (each wet cell's u, v, w advanced one step)
       (two tracers of one surface cell advanced one step)
 
 A step is one tracer timestep (tstepo) of every member.  `value` is tracer
@@ -55,6 +58,7 @@ WORKLOADS = {
     "c5": dict(name="stress_360x180x32_L24", factory="config_c5"),
     "bg5": dict(name="biogem_tracercoupling_360x180x32_L24_sed8", factory="config_c5", n_l_sed=8),
     "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
+    "mo36": dict(name="momentum_36x36x16_2islands", maxi=36, maxj=36, maxk=16),
 }
 
 
@@ -419,8 +423,130 @@ def run_ea(args, rank, world, local, dist):
     s.close()
 
 
+def _mo_member(w):
+    from cgenie_gb300 import grid, momentum
+    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=w["maxk"], maxl=2, seed=31,
+                                           mask="basin_island"))
+    return m, momentum.make_case(m, seed=32)
+
+
+def mo_cpu_rate(m, case, target_s: float = 10.0):
+    """The oracle's momentum step (serial, 1 core): (wet-cell updates/s, steps)."""
+    from oracle import oracle_lib
+    o = oracle_lib.OracleMomentum(case)
+    t0 = time.perf_counter()
+    o.step(m.rho)
+    per = time.perf_counter() - t0
+    n = max(3, min(20000, int(target_s / max(per, 1e-9))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        o.step(m.rho)
+    dt = time.perf_counter() - t0
+    o.close()
+    return m.wet_cells * n / dt, n
+
+
+def run_mo(args, rank, world, local, dist):
+    """The momentum step on one basin: device-resident timing (CUDA events on the ocean
+    handle's stream), end to end with the wind uploaded and u read back."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    from cgenie_gb300 import momentum
+    from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+    w = WORKLOADS[args.workload]
+    m, case = _mo_member(w)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = new_member_run(m, device=local, stream=stream.cuda_stream)
+    mo = momentum.Momentum(case, device=local)
+    mo.set_wind()
+    for _ in range(args.warmup):
+        mo.step(g)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    for s_ in range(args.steps):
+        starts[s_].record(stream)
+        mo.step(g)
+        ends[s_].record(stream)
+    torch.cuda.synchronize()
+    launches = kernel_launch_count() - n0
+    clocks = sampler.stop()
+    total_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
+    units = m.wet_cells
+    value = world * units * args.steps / (total_ms * 1e-3)
+    tau_h = torch.from_numpy(np.ascontiguousarray(case.tau)).pin_memory()
+    dzt_h = torch.from_numpy(np.ascontiguousarray(case.dztau)).pin_memory()
+    dzv_h = torch.from_numpy(np.ascontiguousarray(case.dztav)).pin_memory()
+    u_h = torch.empty((case.maxk, case.maxj + 1, case.maxi + 1, 3), dtype=torch.float64).pin_memory()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(t.data_ptr(), dp)   # noqa: E731
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mo.lib.gb_mo_set_wind(mo.h, ptr(tau_h), ptr(dzt_h), ptr(dzv_h))
+        mo.lib.gb_mo_step(mo.h, g.h)
+        mo.lib.gb_mo_download(mo.h, ptr(u_h), None, None, None)
+    e2e_s = time.perf_counter() - t0
+    peak, peak_kind = measured_peaks()
+    nm = case.maxi * (case.maxj + 1)
+    alg = 8 * nm * nm   # the streamfunction product reads the inverse once
+    achieved = alg / (total_ms * 1e-3 / args.steps) / 1e9
+    if rank == 0:
+        line = {
+            "metric": "wet-cell momentum updates/s", "value": value, "unit": "wet-cell momentum updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded basin with two islands, reference grid formulas)",
+            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "maxk": case.maxk,
+                       "isles": case.isles, "wet_cells": m.wet_cells,
+                       "l2": "not flushed: the 14 MB inverse and the fields stay in L2, as between model steps",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * units * args.steps / e2e_s, "unit": "wet-cell momentum updates/s",
+                    "h2d_bytes_per_step": int(tau_h.numel() + dzt_h.numel() + dzv_h.numel()) * 8,
+                    "d2h_bytes_per_step": int(u_h.numel()) * 8,
+                    "note": "per step: the wind stress H2D (pinned), momentum step, u D2H"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind, "kernel": "momentum step (8 kernels)",
+                         "algorithmic_bytes_per_launch": alg,
+                         "note": "latency-bound chain of 8 small kernels; the inverse (8*nm^2 bytes) is the "
+                                 "largest read"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, n = mo_cpu_rate(m, case)
+            line["cpu_baseline"] = {"value": v, "unit": "wet-cell momentum updates/s", "cores": 1, "kind": "port",
+                                    "sample": f"{n} steps of the same basin, oracle C restatement (banded LU), -O2"}
+        print(json.dumps(line))
+    mo.close()
+    g.close()
+
+
 def run_reference(args, rank, world):
     w = dict(WORKLOADS[args.workload])
+    if args.workload == "mo36":
+        m, case = _mo_member(w)
+        v, n = mo_cpu_rate(m, case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
+        line = {
+            "metric": "wet-cell momentum updates/s", "value": v, "unit": "wet-cell momentum updates/s",
+            "impl": "reference", "n_gpus": world, "steps": n, "warmup": args.warmup,
+            "ms_per_step": 1e3 * m.wet_cells / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "maxk": case.maxk, "isles": case.isles},
+            "cpu_baseline": {"value": v, "unit": "wet-cell momentum updates/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} steps, oracle C restatement, serial (the reference routine is serial)"},
+            "e2e": {"value": v, "unit": "wet-cell momentum updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
     if args.workload == "ea64":
         case = _ea_case(w)
         v, n = ea_cpu_rate(case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
@@ -682,6 +808,11 @@ def main():
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
     if args.workload == "c3":
         run_c3(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "mo36":
+        run_mo(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
         return

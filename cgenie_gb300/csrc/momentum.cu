@@ -13,9 +13,11 @@
 //   k_psi      one warp per psi point: the streamfunction, inverse x right-hand side (the
 //              reference's back substitution is a serial chain of dependent FP64 adds)
 //   k_ub       one thread per velocity point: ub from psi (ubarsolv :3530-3564)
-//   k_island   one block: the island path integrals, matmult, psibc (:203-215, island)
+//   k_island   one block: the island path integrals (a thread per path point, summed in path
+//              order per island), matmult, psibc (:203-215, island)
 //   k_corr     ub and psi island corrections (:217-229)
-//   k_velc     one thread per column: the baroclinic velocities, relaxation (velc :3574-3655)
+//   k_dzu      one thread per cell: the thermal-wind shear dzu (velc :3580-3640)
+//   k_velc     one thread per column: the vertical integration, relaxation (velc :3641-3662)
 //   k_w        one thread per column: w from continuity (velc :3666-3678)
 #include "../../include/gb_momentum.h"
 #include "gb_internal.h"
@@ -40,7 +42,7 @@ struct MoDev {
     const int32_t *npi, *lpisl, *ipisl, *jpisl;
     const double *tau, *dztau, *dztav;
     const double *minv, *ubisl, *psisl, *erisl;   // erisl: (isles, isles+1) after matinv_gold
-    double *psibc, *gb, *gbold, *bp, *sbp, *ub, *psi, *praw, *u, *u1;
+    double *psibc, *gb, *gbold, *bp, *sbp, *ub, *psi, *scr, *dzu, *u, *u1;
     const double *rho;
 };
 
@@ -82,7 +84,7 @@ __device__ __forceinline__ int imax2(int x, int y) { return x > y ? x : y; }
 __device__ __forceinline__ int imax4(int w, int x, int y, int z) { return imax2(imax2(w, x), imax2(y, z)); }
 
 // jbar :3226-3262: bp, sbp, and the periodic copies at i = maxi+1 (by the i = 1 thread)
-__global__ void __launch_bounds__(128) k_bp(MoDev a)
+__global__ void __launch_bounds__(32) k_bp(MoDev a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.maxi * a.maxj) return;
@@ -112,7 +114,7 @@ __device__ double ksum(const MoDev &a, int i, int j, int ka, int kb)
 }
 
 // wind :3696-3712 and the J term of jbar :3266-3314, one psi point each
-__global__ void __launch_bounds__(128) k_rhs(MoDev a)
+__global__ void __launch_bounds__(32) k_rhs(MoDev a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.nm) return;
@@ -181,38 +183,48 @@ __global__ void __launch_bounds__(128) k_ub(MoDev a)
     a.ub[UBi(a, 2, ib, j)] = v2;
 }
 
-// island path integral (goldstein_lib.f90:186-241, indj = 1), then matmult and psibc (:203-215)
-__global__ void __launch_bounds__(32) k_island(MoDev a)
+// island path integral (goldstein_lib.f90:186-241, indj = 1), then matmult and psibc (:203-215).
+// Each path point's two contributions (the velocity and wind term, the J term) are computed by
+// its own thread; one thread per island then adds them in path order, as the reference does.
+__global__ void __launch_bounds__(256) k_island(MoDev a, double *scr)
 {
     __shared__ double rhs[33];
+    const int npt = a.isles * a.mpi;
+    for (int q = threadIdx.x; q < npt; q += blockDim.x) {
+        const int isl = q / a.mpi + 1, p = q % a.mpi + 1;
+        if (p > a.npi[isl - 1]) continue;
+        const int lpi = a.lpisl[q], ipi = a.ipisl[q], jpi = a.jpisl[q];
+        const int al = lpi < 0 ? -lpi : lpi;
+        const double sg = lpi >= 0 ? 1.0 : -1.0;
+        double cor;
+        if (al == 1)
+            cor = -a.s[jpi] * 0.25 * (a.ub[UBi(a, 2, ipi, jpi)] + a.ub[UBi(a, 2, ipi + 1, jpi)] + a.ub[UBi(a, 2, ipi, jpi - 1)] +
+                                      a.ub[UBi(a, 2, ipi + 1, jpi - 1)]);
+        else
+            cor = a.sv[jpi] * 0.25 * (a.ub[UBi(a, 1, ipi - 1, jpi)] + a.ub[UBi(a, 1, ipi, jpi)] + a.ub[UBi(a, 1, ipi - 1, jpi + 1)] +
+                                      a.ub[UBi(a, 1, ipi, jpi + 1)]);
+        scr[2 * q] = sg * (DRAG(a, al, ipi, jpi) * a.ub[UBi(a, al, ipi, jpi)] + cor - 1.0 * TAU(a.tau, a, al, ipi, jpi) * RH(a, al, ipi, jpi)) *
+                     (a.c[jpi] * a.dphi * (2.0 - al) + a.rcv[jpi - 1] * a.dsv[jpi - 1] * (al - 1.0));
+        if (al == 1) {
+            double tv1 = 0.0;
+            for (int k = KU(a, 1, ipi, jpi); k <= MK(a, ipi + 1, jpi); ++k) tv1 = tv1 + a.bp[BPi(a, ipi + 1, jpi, k)] * a.dz[k - 1];
+            for (int k = KU(a, 1, ipi, jpi); k <= MK(a, ipi, jpi); ++k) tv1 = tv1 - a.bp[BPi(a, ipi, jpi, k)] * a.dz[k - 1];
+            scr[2 * q + 1] = (a.sbp[SBPi(a, ipi + 1, jpi)] - a.sbp[SBPi(a, ipi, jpi)] + tv1) * sg * RH(a, 1, ipi, jpi);
+        } else {
+            double tv2 = 0.0;
+            for (int k = KU(a, 2, ipi, jpi); k <= MK(a, ipi, jpi + 1); ++k) tv2 = tv2 + a.bp[BPi(a, ipi, jpi + 1, k)] * a.dz[k - 1];
+            for (int k = KU(a, 2, ipi, jpi); k <= MK(a, ipi, jpi); ++k) tv2 = tv2 - a.bp[BPi(a, ipi, jpi, k)] * a.dz[k - 1];
+            scr[2 * q + 1] = (a.sbp[SBPi(a, ipi, jpi + 1)] - a.sbp[SBPi(a, ipi, jpi)] + tv2) * sg * RH(a, 2, ipi, jpi);
+        }
+    }
+    __syncthreads();
     const int isl = threadIdx.x + 1;
     if (isl <= a.isles) {
         double e = 0.0;
-        for (int p = 1; p <= a.npi[isl - 1]; ++p) {
-            const size_t q = (size_t)(p - 1) + (size_t)a.mpi * (isl - 1);
-            const int lpi = a.lpisl[q], ipi = a.ipisl[q], jpi = a.jpisl[q];
-            const int al = lpi < 0 ? -lpi : lpi;
-            const double sg = lpi >= 0 ? 1.0 : -1.0;
-            double cor;
-            if (al == 1)
-                cor = -a.s[jpi] * 0.25 * (a.ub[UBi(a, 2, ipi, jpi)] + a.ub[UBi(a, 2, ipi + 1, jpi)] + a.ub[UBi(a, 2, ipi, jpi - 1)] +
-                                          a.ub[UBi(a, 2, ipi + 1, jpi - 1)]);
-            else
-                cor = a.sv[jpi] * 0.25 * (a.ub[UBi(a, 1, ipi - 1, jpi)] + a.ub[UBi(a, 1, ipi, jpi)] + a.ub[UBi(a, 1, ipi - 1, jpi + 1)] +
-                                          a.ub[UBi(a, 1, ipi, jpi + 1)]);
-            e = e + sg * (DRAG(a, al, ipi, jpi) * a.ub[UBi(a, al, ipi, jpi)] + cor - 1.0 * TAU(a.tau, a, al, ipi, jpi) * RH(a, al, ipi, jpi)) *
-                        (a.c[jpi] * a.dphi * (2.0 - al) + a.rcv[jpi - 1] * a.dsv[jpi - 1] * (al - 1.0));
-            if (al == 1) {
-                double tv1 = 0.0;
-                for (int k = KU(a, 1, ipi, jpi); k <= MK(a, ipi + 1, jpi); ++k) tv1 = tv1 + a.bp[BPi(a, ipi + 1, jpi, k)] * a.dz[k - 1];
-                for (int k = KU(a, 1, ipi, jpi); k <= MK(a, ipi, jpi); ++k) tv1 = tv1 - a.bp[BPi(a, ipi, jpi, k)] * a.dz[k - 1];
-                e = e + (a.sbp[SBPi(a, ipi + 1, jpi)] - a.sbp[SBPi(a, ipi, jpi)] + tv1) * sg * RH(a, 1, ipi, jpi);
-            } else {
-                double tv2 = 0.0;
-                for (int k = KU(a, 2, ipi, jpi); k <= MK(a, ipi, jpi + 1); ++k) tv2 = tv2 + a.bp[BPi(a, ipi, jpi + 1, k)] * a.dz[k - 1];
-                for (int k = KU(a, 2, ipi, jpi); k <= MK(a, ipi, jpi); ++k) tv2 = tv2 - a.bp[BPi(a, ipi, jpi, k)] * a.dz[k - 1];
-                e = e + (a.sbp[SBPi(a, ipi, jpi + 1)] - a.sbp[SBPi(a, ipi, jpi)] + tv2) * sg * RH(a, 2, ipi, jpi);
-            }
+        for (int p = 0; p < a.npi[isl - 1]; ++p) {
+            const size_t q = (size_t)p + (size_t)a.mpi * (isl - 1);
+            e = e + scr[2 * q];
+            e = e + scr[2 * q + 1];
         }
         rhs[isl] = e;
     }
@@ -255,74 +267,91 @@ __global__ void __launch_bounds__(128) k_corr(MoDev a)
     }
 }
 
-// velc :3574-3661, one column each; the i = maxi thread also makes u(1,0,j,:) (:3658-3662)
-__global__ void __launch_bounds__(128) k_velc(MoDev a)
+// velc :3580-3640: dzu(1:2,k) of every wet cell at once (they depend on the density of level k
+// only), one thread per (column, level)
+__global__ void __launch_bounds__(128) k_dzu(MoDev a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.maxi * a.maxj) return;
+    const int ncol = a.maxi * a.maxj;
+    if (t >= ncol * a.maxk) return;
+    const int col = t % ncol, k = t / ncol + 1;
+    const int i = col % a.maxi + 1, j = col / a.maxi + 1;
+    if (k < K1(a, i, j)) return;
+    const double rdphi = a.rdphi;
+    double tv1, tv2, tv4, tv5;
+    if (K1(a, i + 1, j) > k) {
+        tv1 = 0;
+        tv2 = 0;
+    } else {
+        tv2 = -(RHO(a, i + 1, j, k) - RHO(a, i, j, k)) * rdphi * a.rc[j];
+        if (imax4(K1(a, i, j - 1), K1(a, i, j + 1), K1(a, i + 1, j - 1), K1(a, i + 1, j + 1)) <= k)
+            tv1 = -a.c[j] * (RHO(a, i + 1, j + 1, k) - RHO(a, i + 1, j - 1, k) + RHO(a, i, j + 1, k) - RHO(a, i, j - 1, k)) *
+                  a.rds2[j - 2] * 0.25;
+        else if (imax2(K1(a, i, j - 1), K1(a, i + 1, j - 1)) <= k)
+            tv1 = -a.c[j] * (RHO(a, i + 1, j, k) - RHO(a, i + 1, j - 1, k) + RHO(a, i, j, k) - RHO(a, i, j - 1, k)) *
+                  a.rdsv[j - 2] * 0.5;
+        else if (imax2(K1(a, i, j + 1), K1(a, i + 1, j + 1)) <= k)
+            tv1 = -a.c[j] * (RHO(a, i + 1, j + 1, k) - RHO(a, i + 1, j, k) + RHO(a, i, j + 1, k) - RHO(a, i, j, k)) *
+                  a.rdsv[j - 1] * 0.5;
+        else
+            tv1 = 0;
+    }
+    if (K1(a, i, j + 1) > k) {
+        tv4 = 0;
+        tv5 = 0;
+    } else {
+        tv4 = -a.cv[j] * (RHO(a, i, j + 1, k) - RHO(a, i, j, k)) * a.rdsv[j - 1];
+        if (imax4(K1(a, i - 1, j), K1(a, i - 1, j + 1), K1(a, i + 1, j), K1(a, i + 1, j + 1)) <= k)
+            tv5 = -(RHO(a, i + 1, j + 1, k) - RHO(a, i - 1, j + 1, k) + RHO(a, i + 1, j, k) - RHO(a, i - 1, j, k)) * rdphi * 0.25 *
+                  a.rcv[j - 1];
+        else if (imax2(K1(a, i - 1, j), K1(a, i - 1, j + 1)) <= k)
+            tv5 = -(RHO(a, i, j + 1, k) - RHO(a, i - 1, j + 1, k) + RHO(a, i, j, k) - RHO(a, i - 1, j, k)) * rdphi * 0.5 * a.rcv[j - 1];
+        else if (imax2(K1(a, i + 1, j), K1(a, i + 1, j + 1)) <= k)
+            tv5 = -(RHO(a, i + 1, j + 1, k) - RHO(a, i, j + 1, k) + RHO(a, i + 1, j, k) - RHO(a, i, j, k)) * rdphi * 0.5 * a.rcv[j - 1];
+        else
+            tv5 = 0;
+    }
+    if (k == a.maxk) {
+        if (K1(a, i + 1, j) <= k) {
+            tv1 = tv1 - TAU(a.dztau, a, 2, i, j);
+            tv2 = tv2 - TAU(a.dztau, a, 1, i, j);
+        }
+        if (K1(a, i, j + 1) <= k) {
+            tv4 = tv4 - TAU(a.dztav, a, 2, i, j);
+            tv5 = tv5 - TAU(a.dztav, a, 1, i, j);
+        }
+    }
+    const size_t ij = (size_t)(i - 1) + (size_t)a.maxi * (j - 1);
+    a.dzu[(size_t)t] = -(a.s[j] * tv1 + DRAG(a, 1, i, j) * tv2) * a.rtv[ij];
+    a.dzu[(size_t)t + (size_t)ncol * a.maxk] = -(DRAG(a, 2, i, j) * tv4 - a.sv[j] * tv5) * a.rtv3[ij];
+}
+
+// velc :3641-3662: the vertical integration of dzu, the barotropic part and the relaxation,
+// one column each; the i = maxi thread also makes u(1,0,j,:)
+__global__ void __launch_bounds__(32) k_velc(MoDev a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncol = a.maxi * a.maxj;
+    if (t >= ncol) return;
     const int i = t % a.maxi + 1, j = t / a.maxi + 1;
     const int maxk = a.maxk;
-    const double rdphi = a.rdphi, rel = a.rel;
+    const double rel = a.rel;
     const int k1 = K1(a, i, j);
+    const double *dzu1 = a.dzu + t, *dzu2 = a.dzu + t + (size_t)ncol * maxk;
     double sum[2] = {0.0, 0.0};
-    double dprev[2] = {0.0, 0.0};
-    for (int k = k1; k <= maxk; ++k) {
-        double tv1, tv2, tv4, tv5;
-        if (K1(a, i + 1, j) > k) {
-            tv1 = 0;
-            tv2 = 0;
-        } else {
-            tv2 = -(RHO(a, i + 1, j, k) - RHO(a, i, j, k)) * rdphi * a.rc[j];
-            if (imax4(K1(a, i, j - 1), K1(a, i, j + 1), K1(a, i + 1, j - 1), K1(a, i + 1, j + 1)) <= k)
-                tv1 = -a.c[j] * (RHO(a, i + 1, j + 1, k) - RHO(a, i + 1, j - 1, k) + RHO(a, i, j + 1, k) - RHO(a, i, j - 1, k)) *
-                      a.rds2[j - 2] * 0.25;
-            else if (imax2(K1(a, i, j - 1), K1(a, i + 1, j - 1)) <= k)
-                tv1 = -a.c[j] * (RHO(a, i + 1, j, k) - RHO(a, i + 1, j - 1, k) + RHO(a, i, j, k) - RHO(a, i, j - 1, k)) *
-                      a.rdsv[j - 2] * 0.5;
-            else if (imax2(K1(a, i, j + 1), K1(a, i + 1, j + 1)) <= k)
-                tv1 = -a.c[j] * (RHO(a, i + 1, j + 1, k) - RHO(a, i + 1, j, k) + RHO(a, i, j + 1, k) - RHO(a, i, j, k)) *
-                      a.rdsv[j - 1] * 0.5;
-            else
-                tv1 = 0;
-        }
-        if (K1(a, i, j + 1) > k) {
-            tv4 = 0;
-            tv5 = 0;
-        } else {
-            tv4 = -a.cv[j] * (RHO(a, i, j + 1, k) - RHO(a, i, j, k)) * a.rdsv[j - 1];
-            if (imax4(K1(a, i - 1, j), K1(a, i - 1, j + 1), K1(a, i + 1, j), K1(a, i + 1, j + 1)) <= k)
-                tv5 = -(RHO(a, i + 1, j + 1, k) - RHO(a, i - 1, j + 1, k) + RHO(a, i + 1, j, k) - RHO(a, i - 1, j, k)) * rdphi * 0.25 *
-                      a.rcv[j - 1];
-            else if (imax2(K1(a, i - 1, j), K1(a, i - 1, j + 1)) <= k)
-                tv5 = -(RHO(a, i, j + 1, k) - RHO(a, i - 1, j + 1, k) + RHO(a, i, j, k) - RHO(a, i - 1, j, k)) * rdphi * 0.5 * a.rcv[j - 1];
-            else if (imax2(K1(a, i + 1, j), K1(a, i + 1, j + 1)) <= k)
-                tv5 = -(RHO(a, i + 1, j + 1, k) - RHO(a, i, j + 1, k) + RHO(a, i + 1, j, k) - RHO(a, i, j, k)) * rdphi * 0.5 * a.rcv[j - 1];
-            else
-                tv5 = 0;
-        }
-        if (k == maxk) {
-            if (K1(a, i + 1, j) <= k) {
-                tv1 = tv1 - TAU(a.dztau, a, 2, i, j);
-                tv2 = tv2 - TAU(a.dztau, a, 1, i, j);
-            }
-            if (K1(a, i, j + 1) <= k) {
-                tv4 = tv4 - TAU(a.dztav, a, 2, i, j);
-                tv5 = tv5 - TAU(a.dztav, a, 1, i, j);
-            }
-        }
-        const size_t ij = (size_t)(i - 1) + (size_t)a.maxi * (j - 1);
-        double dzu[2];
-        dzu[0] = -(a.s[j] * tv1 + DRAG(a, 1, i, j) * tv2) * a.rtv[ij];
-        dzu[1] = -(DRAG(a, 2, i, j) * tv4 - a.sv[j] * tv5) * a.rtv3[ij];
-        for (int l = 1; l <= 2; ++l) {
+    for (int l = 1; l <= 2; ++l) {
+        const double *dz_l = l == 1 ? dzu1 : dzu2;
+        double prev = 0.0, uprev = 0.0;
+        for (int k = k1; k <= maxk; ++k) {
+            const double d = dz_l[(size_t)ncol * (k - 1)];
             if (k == k1) {
-                a.u[Ui(a, l, i, j, k)] = 0;
+                uprev = 0;
             } else {
-                const double v = a.u[Ui(a, l, i, j, k - 1)] + a.dza[k - 2] * (dzu[l - 1] + dprev[l - 1]) * 0.5;
-                a.u[Ui(a, l, i, j, k)] = v;
-                sum[l - 1] = sum[l - 1] + a.dz[k - 1] * v;
+                uprev = uprev + a.dza[k - 2] * (d + prev) * 0.5;
+                sum[l - 1] = sum[l - 1] + a.dz[k - 1] * uprev;
             }
-            dprev[l - 1] = dzu[l - 1];
+            a.u[Ui(a, l, i, j, k)] = uprev;
+            prev = d;
         }
     }
     for (int k = k1; k <= maxk; ++k) {
@@ -344,7 +373,7 @@ __global__ void __launch_bounds__(128) k_velc(MoDev a)
 }
 
 // w from continuity (velc :3666-3678)
-__global__ void __launch_bounds__(128) k_w(MoDev a)
+__global__ void __launch_bounds__(32) k_w(MoDev a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.maxi * a.maxj) return;
@@ -497,6 +526,12 @@ struct gb_mo {
     int device = 0;
     cudaStream_t stream = nullptr;
     MoDev dev{};
+    // the step's launches as a CUDA graph, captured for one ocean handle's density, velocity
+    // buffer and stream (re-captured when those change)
+    cudaGraphExec_t graph = nullptr;
+    const double *graph_rho = nullptr;
+    double *graph_u = nullptr;
+    cudaStream_t graph_stream = nullptr;
     std::vector<void *> allocs;
     bool have_wind = false;
     std::string last_error;
@@ -661,7 +696,8 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     if (e == cudaSuccess) e = dev_zero(h, &a.sbp, (size_t)(maxi + 1) * maxj);
     if (e == cudaSuccess) e = dev_zero(h, &a.ub, nub);
     if (e == cudaSuccess) e = dev_zero(h, &a.psi, npsi);
-    if (e == cudaSuccess) e = dev_zero(h, &a.praw, (size_t)nm);
+    if (e == cudaSuccess) e = dev_zero(h, &a.scr, 2 * (size_t)d.isles * d.mpi);   // island path terms
+    if (e == cudaSuccess) e = dev_zero(h, &a.dzu, 2 * (size_t)maxi * maxj * maxk);
     if (e == cudaSuccess) e = dev_zero(h, &a.u, nu);
     if (e == cudaSuccess) e = dev_zero(h, &a.u1, nu);
     if (e != cudaSuccess) {
@@ -679,6 +715,7 @@ extern "C" void gb_mo_destroy(gb_mo *h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (void *p : h->allocs) cudaFree(p);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -709,6 +746,8 @@ extern "C" int gb_mo_upload_velocity(gb_mo *h, const double *u, const double *u1
     return GB_GO_OK;
 }
 
+static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u);
+
 extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
 {
     if (!h || !ocean) return mfail(h, GB_GO_EINVAL, "step: NULL handle");
@@ -724,24 +763,56 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
     MO_TRY(h, cudaSetDevice(h->device));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     a.rho = o.rho;
-    const int ncol = a.maxi * a.maxj;
-    const size_t nub = 2 * (size_t)(a.maxi + 2) * (a.maxj + 1), npsi = (size_t)(a.maxi + 1) * (a.maxj + 1);
-    k_bp<<<(ncol + 127) / 128, 128, 0, s>>>(a);
-    k_rhs<<<(a.nm + 127) / 128, 128, 0, s>>>(a);
-    k_psi<<<(a.nm * 32 + 255) / 256, 256, 0, s>>>(a);
-    k_ub<<<((a.maxi + 2) * (a.maxj + 1) + 127) / 128, 128, 0, s>>>(a);
-    k_island<<<1, 32, 0, s>>>(a);
-    k_corr<<<(unsigned)((nub + npsi + 127) / 128), 128, 0, s>>>(a);
-    k_velc<<<(ncol + 127) / 128, 128, 0, s>>>(a);
-    k_w<<<(ncol + 127) / 128, 128, 0, s>>>(a);
-    count_launches(8);
-    MO_TRY(h, cudaGetLastError());
-    // the new velocities are the ocean handle's for its next tstepo
-    const size_t nu = 3 * (size_t)(a.maxi + 1) * (a.maxj + 1) * a.maxk;
-    MO_TRY(h, cudaMemcpyAsync(o.u, a.u, nu * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (h->graph && (h->graph_rho != o.rho || h->graph_u != o.u || h->graph_stream != s)) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    if (!h->graph) {
+        cudaGraph_t gr = nullptr;
+        MO_TRY(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int r = launch_step(a, s, o.u);
+        cudaError_t e = cudaStreamEndCapture(s, &gr);
+        if (r || e != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return mfail(h, GB_GO_ECUDA, std::string("step: graph capture failed: ") + cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&h->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) {
+            h->graph = nullptr;
+            return mfail(h, GB_GO_ECUDA, std::string("step: graph instantiation failed: ") + cudaGetErrorString(e));
+        }
+        h->graph_rho = o.rho;
+        h->graph_u = o.u;
+        h->graph_stream = s;
+    }
+    MO_TRY(h, cudaGraphLaunch(h->graph, s));
+    count_launches(9);
     MO_TRY(h, cudaStreamSynchronize(s));
     *o.vel_ready = true;
     return GB_GO_OK;
+}
+
+// the step's kernels and the copy of the new velocities into the ocean handle's buffer
+static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u)
+{
+    const int ncol = a.maxi * a.maxj;
+    const size_t nub = 2 * (size_t)(a.maxi + 2) * (a.maxj + 1), npsi = (size_t)(a.maxi + 1) * (a.maxj + 1);
+    // blocks of one warp for the per-column kernels: their FP64 chains then spread over many
+    // SMs (GB300's FP64 pipe is ~2 lanes per clock per SM)
+    k_bp<<<(ncol + 31) / 32, 32, 0, s>>>(a);
+    k_rhs<<<(a.nm + 31) / 32, 32, 0, s>>>(a);
+    k_psi<<<(a.nm * 32 + 255) / 256, 256, 0, s>>>(a);
+    k_ub<<<((a.maxi + 2) * (a.maxj + 1) + 127) / 128, 128, 0, s>>>(a);
+    k_island<<<1, 256, 0, s>>>(a, a.scr);
+    k_corr<<<(unsigned)((nub + npsi + 127) / 128), 128, 0, s>>>(a);
+    k_dzu<<<(unsigned)(((size_t)ncol * a.maxk + 127) / 128), 128, 0, s>>>(a);
+    k_velc<<<(ncol + 31) / 32, 32, 0, s>>>(a);
+    k_w<<<(ncol + 31) / 32, 32, 0, s>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return GB_GO_ECUDA;
+    // the new velocities are the ocean handle's for its next tstepo
+    const size_t nu = 3 * (size_t)(a.maxi + 1) * (a.maxj + 1) * a.maxk;
+    return cudaMemcpyAsync(ocean_u, a.u, nu * sizeof(double), cudaMemcpyDeviceToDevice, s) == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
 extern "C" int gb_mo_download(gb_mo *h, double *u, double *u1, double *ub, double *psi)
