@@ -15,6 +15,8 @@ Workloads (seeded synthetic members with the reference's grid formulas):
       `value` is tracer cell-couplings/s (one tracer of one wet cell coupled)
   ea64 the EMBM atmosphere step (tstipa) on a 64x64 surface grid, one launch per step as
       the model calls it; `value` is air cell-updates/s
+  ea36e the EMBM step of a 256-member ensemble of 36x36 surface grids, one launch per step
+      for all members (gb_ea_step_many)
   mo36 the momentum step (wind, jbar, streamfunction, islands, velc) of a 36x36x16 basin
       with two islands, on the density of an FP64 handle; `value` is wet-cell momentum
       updates/s (each wet cell's u, v, w advanced one step)
@@ -58,6 +60,7 @@ WORKLOADS = {
     "c5": dict(name="stress_360x180x32_L24", factory="config_c5"),
     "bg5": dict(name="biogem_tracercoupling_360x180x32_L24_sed8", factory="config_c5", n_l_sed=8),
     "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
+    "ea36e": dict(name="embm_tstipa_ensemble256_36x36", maxi=36, maxj=36, members=256),
     "mo36": dict(name="momentum_36x36x16_2islands", maxi=36, maxj=36, maxk=16),
 }
 
@@ -327,10 +330,10 @@ def run_bg(args, rank, world, local, dist):
     g.close()
 
 
-def _ea_case(w):
+def _ea_case(w, member: int = 0):
     from cgenie_gb300 import grid, surface
-    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=8, maxl=2, seed=21))
-    return surface.embm_case(m, seed=22)
+    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=8, maxl=2, seed=21 + 7919 * member))
+    return surface.embm_case(m, seed=22 + 7919 * member)
 
 
 def ea_cpu_rate(case, target_s: float = 10.0):
@@ -356,12 +359,17 @@ def run_ea(args, rank, world, local, dist):
     from cgenie_gb300 import surface
     from cgenie_gb300.goldstein import kernel_launch_count
     w = WORKLOADS[args.workload]
-    case = _ea_case(w)
-    s = surface.SurfaceStepper(case.copy(), device=local)
-    s.upload_state()
-    s.set_forcing()
+    nmem = w.get("members", 1)
+    cases = [_ea_case(w, n) for n in range(nmem)]
+    case = cases[0]
+    steppers = [surface.SurfaceStepper(c.copy(), device=local) for c in cases]
+    for st in steppers:
+        st.upload_state()
+        st.set_forcing()
+    s = steppers[0]
+    step = (lambda: s.step(1)) if nmem == 1 else (lambda: surface.step_many(steppers, 1))
     for _ in range(args.warmup):
-        s.step(1)
+        step()
     sampler = ClockSampler(local)
     sampler.start()
     if dist:
@@ -370,12 +378,12 @@ def run_ea(args, rank, world, local, dist):
     n0 = kernel_launch_count()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s.step(1)
+        step()
     torch.cuda.synchronize()
     dev_s = time.perf_counter() - t0
     launches = kernel_launch_count() - n0
     clocks = sampler.stop()
-    units = case.maxi * case.maxj * 2
+    units = case.maxi * case.maxj * 2 * nmem
     value = world * units * args.steps / dev_s
     # end to end: the step's forcing (tqa, uatm, pptn) from pinned host memory, the step, tq back
     src_h = torch.from_numpy(np.ascontiguousarray(case.source)).pin_memory()
@@ -384,14 +392,17 @@ def run_ea(args, rank, world, local, dist):
     tq_h = torch.empty(tuple(case.tq.shape), dtype=torch.float64).pin_memory()
     dp = C.POINTER(C.c_double)
     ptr = lambda t: C.cast(t.data_ptr(), dp)   # noqa: E731
+    e2e_steps = args.steps if nmem == 1 else max(1, args.steps // 10)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.lib.gb_ea_set_forcing(s.h, ptr(src_h), ptr(vel_h), ptr(pp_h))
-        s.lib.gb_ea_step(s.h, 1)
-        s.lib.gb_ea_download(s.h, ptr(tq_h), None)
+    for _ in range(e2e_steps):
+        for st in steppers:
+            st.lib.gb_ea_set_forcing(st.h, ptr(src_h), ptr(vel_h), ptr(pp_h))
+        step()
+        for st in steppers:
+            st.lib.gb_ea_download(st.h, ptr(tq_h), None)
     e2e_s = time.perf_counter() - t0
     peak, peak_kind = measured_peaks()
-    alg = 13 * 8 * case.maxi * case.maxj   # read tq, tq1, tqa, uatm (2 each), pptn; write tq, tq1
+    alg = 13 * 8 * case.maxi * case.maxj * nmem   # read tq, tq1, tqa, uatm (2 each), pptn; write tq, tq1
     achieved = alg / (dev_s / args.steps) / 1e9
     if rank == 0:
         line = {
@@ -399,14 +410,14 @@ def run_ea(args, rank, world, local, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fields on the reference's sin-latitude grid)",
-            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2,
+            "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2, "grids": nmem,
                        "timing": "host clock around the synchronous C-ABI step calls (one launch each)",
                        "l2": "not flushed: the grid (0.3 MB) lives in L2, as in the model",
                        "parallelism": f"replicas{world}"},
-            "e2e": {"value": world * units * args.steps / e2e_s, "unit": "air cell-updates/s",
-                    "h2d_bytes_per_step": int(src_h.numel() + vel_h.numel() + pp_h.numel()) * 8,
-                    "d2h_bytes_per_step": int(tq_h.numel()) * 8,
-                    "note": "per step: tqa + uatm + pptn H2D (pinned), step, tq D2H"},
+            "e2e": {"value": world * units * e2e_steps / e2e_s, "unit": "air cell-updates/s",
+                    "h2d_bytes_per_step": int(src_h.numel() + vel_h.numel() + pp_h.numel()) * 8 * nmem,
+                    "d2h_bytes_per_step": int(tq_h.numel()) * 8 * nmem,
+                    "note": "per step and grid: tqa + uatm + pptn H2D (pinned), step, tq D2H"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind, "kernel": "k_surface_step",
                          "algorithmic_bytes_per_launch": alg,
@@ -420,7 +431,8 @@ def run_ea(args, rank, world, local, dist):
             line["cpu_baseline"] = {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
                                     "sample": f"{n} steps of the same grid, oracle C restatement, -O2"}
         print(json.dumps(line))
-    s.close()
+    for st in steppers:
+        st.close()
 
 
 def _mo_member(w):
@@ -547,7 +559,7 @@ def run_reference(args, rank, world):
         }
         print(json.dumps(line))
         return
-    if args.workload == "ea64":
+    if args.workload in ("ea64", "ea36e"):
         case = _ea_case(w)
         v, n = ea_cpu_rate(case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
         line = {
@@ -816,7 +828,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    if args.workload == "ea64":
+    if args.workload in ("ea64", "ea36e"):
         run_ea(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <string>
+#include <vector>
 
 using namespace gbgo;
 
@@ -119,8 +120,9 @@ __device__ __forceinline__ void face_coefs(const EaArgs &a, int l, int i, int j,
 // from its neighbours' shared memory (distributed shared memory) after every iterate update.
 // Shared-memory layout of every block: cie, ciw (maxi+1) x R; cin, cis (maxi+1) x (R+1) from
 // row j0-1; v2 (maxi+2) x (R+2) from row j0-1.
-__global__ void __launch_bounds__(kThreads) k_surface_step(EaArgs a, int R)
+__global__ void __launch_bounds__(kThreads) k_surface_step(const EaArgs *__restrict__ args, int R)
 {
+    const EaArgs a = args[blockIdx.y];   // one grid per blockIdx.y (gb_ea_step_many)
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ double sm[];
@@ -277,8 +279,9 @@ __device__ __forceinline__ double ice_north(const EaArgs &a, int l, int i, int j
 
 // One thread per cell: the reference's west and south carries are the east and north fluxes of
 // the neighbours, recomputed here with the same expressions.
-__global__ void __launch_bounds__(256) k_seaice_explicit(EaArgs a)
+__global__ void __launch_bounds__(256) k_seaice_explicit(const EaArgs *__restrict__ args)
 {
+    const EaArgs a = args[blockIdx.y];
     const int maxi = a.maxi, maxj = a.maxj;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= maxi * maxj) return;
@@ -318,6 +321,8 @@ struct gb_ea {
     double *tq = nullptr, *tq1 = nullptr, *src = nullptr, *vel = nullptr, *pptn = nullptr;
     bool have_state = false, have_forcing = false;
     int cluster_max = 8;   // 16 where the device schedules clusters of 16 (gb_ea_create)
+    EaArgs *dargs = nullptr;   // kernel arguments in device memory (capacity cap_args grids)
+    int cap_args = 0;
     std::string last_error;
 };
 
@@ -431,7 +436,7 @@ extern "C" void gb_ea_destroy(gb_ea *h)
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn};
+    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn, h->dargs};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -466,15 +471,8 @@ extern "C" int gb_ea_set_forcing(gb_ea *h, const double *source, const double *v
     return GB_GO_OK;
 }
 
-extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
+static EaArgs args_of(const gb_ea *h, int nsteps)
 {
-    if (!h) return GB_GO_EINVAL;
-    if (nsteps < 0) return efail(h, GB_GO_EINVAL, "step: nsteps < 0");
-    if (h->p.kind != GB_EA_EMBM && nsteps > 1)
-        return efail(h, GB_GO_EINVAL, "step: sea ice takes one step per call (step_seaice post-processes between steps)");
-    if (!h->have_state || !h->have_forcing) return efail(h, GB_GO_ENOTREADY, "step before upload_state/set_forcing");
-    if (nsteps == 0) return GB_GO_OK;
-    EA_TRY(h, cudaSetDevice(h->device));
     EaArgs a{};
     a.maxi = h->d.maxi;
     a.maxj = h->d.maxj;
@@ -507,34 +505,73 @@ extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
     a.src = h->src;
     a.vel = h->vel;
     a.pptn = h->pptn;
+    return a;
+}
+
+// nsteps steps of n grids of the same kind and shape, one launch (blockIdx.y = grid)
+static int step_grids(gb_ea *const *hs, int n, int nsteps)
+{
+    gb_ea *h = hs[0];
+    if (nsteps < 0) return efail(h, GB_GO_EINVAL, "step: nsteps < 0");
+    for (int m = 0; m < n; ++m) {
+        const gb_ea *g = hs[m];
+        if (!g) return efail(h, GB_GO_EINVAL, "step: NULL handle");
+        if (g->device != h->device || g->p.kind != h->p.kind || g->d.maxi != h->d.maxi || g->d.maxj != h->d.maxj ||
+            g->cluster_max != h->cluster_max)
+            return efail(h, GB_GO_EINVAL, "step_many: grids differ in device, kind or shape");
+        if (!g->have_state || !g->have_forcing) return efail(h, GB_GO_ENOTREADY, "step before upload_state/set_forcing");
+    }
+    if (h->p.kind != GB_EA_EMBM && nsteps > 1)
+        return efail(h, GB_GO_EINVAL, "step: sea ice takes one step per call (step_seaice post-processes between steps)");
+    if (nsteps == 0 || n == 0) return GB_GO_OK;
+    EA_TRY(h, cudaSetDevice(h->device));
+    if (n > h->cap_args) {
+        if (h->dargs) cudaFree(h->dargs);
+        h->dargs = nullptr;
+        h->cap_args = 0;
+        EA_TRY(h, cudaMalloc(&h->dargs, (size_t)n * sizeof(EaArgs)));
+        h->cap_args = n;
+    }
+    std::vector<EaArgs> args((size_t)n);
+    for (int m = 0; m < n; ++m) args[m] = args_of(hs[m], nsteps);
+    EA_TRY(h, cudaMemcpyAsync(h->dargs, args.data(), (size_t)n * sizeof(EaArgs), cudaMemcpyHostToDevice, h->stream));
     if (h->p.kind == GB_EA_SEAICE_EXPLICIT) {
         const int ncell = h->d.maxi * h->d.maxj;
-        k_seaice_explicit<<<(ncell + 255) / 256, 256, 0, h->stream>>>(a);
-        count_launches(1);
-        EA_TRY(h, cudaGetLastError());
-        EA_TRY(h, cudaStreamSynchronize(h->stream));
-        return GB_GO_OK;
+        k_seaice_explicit<<<dim3((ncell + 255) / 256, n), 256, 0, h->stream>>>(h->dargs);
+    } else {
+        int R = 0, C = 0;
+        split_rows(h->d.maxj, &R, &C, h->cluster_max);
+        const int cells = h->d.maxi * R;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * C, n);
+        cfg.blockDim = dim3(std::min(kThreads, (cells + 31) / 32 * 32));
+        cfg.dynamicSmemBytes = smem_bytes(h->d.maxi, R);
+        cfg.stream = h->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        EA_TRY(h, cudaLaunchKernelEx(&cfg, k_surface_step, (const EaArgs *)h->dargs, R));
     }
-    int R = 0, C = 0;
-    split_rows(h->d.maxj, &R, &C, h->cluster_max);
-    const int cells = h->d.maxi * R;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * C);
-    cfg.blockDim = dim3(std::min(kThreads, (cells + 31) / 32 * 32));
-    cfg.dynamicSmemBytes = smem_bytes(h->d.maxi, R);
-    cfg.stream = h->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    EA_TRY(h, cudaLaunchKernelEx(&cfg, k_surface_step, a, R));
     count_launches(1);
     EA_TRY(h, cudaGetLastError());
     EA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
+}
+
+extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
+{
+    if (!h) return GB_GO_EINVAL;
+    return step_grids(&h, 1, nsteps);
+}
+
+extern "C" int gb_ea_step_many(gb_ea *const *handles, int32_t n, int32_t nsteps)
+{
+    if (!handles || n < 1 || !handles[0]) return GB_GO_EINVAL;
+    return step_grids(handles, n, nsteps);
 }
 
 extern "C" int gb_ea_download(gb_ea *h, double *tq, double *tq1)

@@ -182,3 +182,14 @@ class SurfaceStepper:
         tq1 = np.zeros((c.maxj, c.maxi, 2))
         self._check(self.lib.gb_ea_download(self.h, dptr(tq), dptr(tq1)), "gb_ea_download")
         return tq, tq1
+
+
+def step_many(steppers, nsteps: int = 1):
+    """One launch advancing every stepper (same kind and shape, one device) by nsteps."""
+    if not steppers:
+        return
+    lib = steppers[0].lib
+    arr = (C.c_void_p * len(steppers))(*[s.h for s in steppers])
+    rc = lib.gb_ea_step_many(arr, len(steppers), int(nsteps))
+    if rc != 0:
+        steppers[0]._check(rc, "gb_ea_step_many")

@@ -77,6 +77,9 @@ int gb_ea_set_forcing(gb_ea *h, const double *source, const double *vel, const d
    (embm.f90:2137).  Sea ice: nsteps = 1, one tstipsic; tq1 is left as it was (step_seaice
    post-processes the ice and copies it, gold_seaice.f90:604-619). */
 int gb_ea_step(gb_ea *h, int32_t nsteps);
+/* The same for n grids of one kind and shape on one device (an ensemble), in one launch:
+   errors are reported on handles[0]. */
+int gb_ea_step_many(gb_ea *const *handles, int32_t n, int32_t nsteps);
 int gb_ea_download(gb_ea *h, double *tq, double *tq1);
 const char *gb_ea_last_error(const gb_ea *h);
 

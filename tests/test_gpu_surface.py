@@ -76,3 +76,41 @@ def test_errors(gpu_lib):
     with pytest.raises(GoldsteinError) as e:
         surface.SurfaceStepper(c)
     assert e.value.code == abi.GB_GO_EINVAL
+
+
+@pytest.mark.parametrize("kind", ["embm", "ice_explicit", "ice"])
+def test_step_many_bitexact(gpu_lib, kind):
+    """Several grids of one shape (distinct masks, states and forcing) in one launch."""
+    cases = []
+    for n in range(5):
+        m = grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=8, maxl=2, seed=60 + n, land_frac=0.3))
+        if kind == "embm":
+            cases.append(surface.embm_case(m, seed=70 + n))
+        else:
+            cases.append(surface.seaice_case(m, seed=70 + n, explicit=kind == "ice_explicit"))
+    steppers = [surface.SurfaceStepper(c.copy()) for c in cases]
+    for s in steppers:
+        s.upload_state()
+        s.set_forcing()
+    nsteps = 3 if kind == "embm" else 1
+    surface.step_many(steppers, nsteps)
+    for s, c in zip(steppers, cases):
+        tq, tq1 = s.download()
+        ref = c.copy()
+        ol.surface_step(ref, nsteps)
+        assert np.array_equal(tq, ref.tq) and np.array_equal(tq1, ref.tq1)
+        s.close()
+
+
+def test_step_many_rejects_mixed_shapes(gpu_lib):
+    from cgenie_gb300.goldstein import GoldsteinError
+    a = surface.SurfaceStepper(surface.embm_case(grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=4, maxl=2, seed=1)), seed=1))
+    b = surface.SurfaceStepper(surface.embm_case(grid.make_member(grid.MemberConfig(maxi=14, maxj=10, maxk=4, maxl=2, seed=2)), seed=2))
+    for s in (a, b):
+        s.upload_state()
+        s.set_forcing()
+    with pytest.raises(GoldsteinError) as e:
+        surface.step_many([a, b], 1)
+    assert e.value.code == abi.GB_GO_EINVAL
+    a.close()
+    b.close()
