@@ -327,49 +327,64 @@ __global__ void __launch_bounds__(128) k_dzu(MoDev a)
 }
 
 // velc :3641-3662: the vertical integration of dzu, the barotropic part and the relaxation,
-// one column each; the i = maxi thread also makes u(1,0,j,:)
+// one column per thread, 32 columns per block; the i = maxi thread also makes u(1,0,j,:).
+// The column's dzu and u1 are first loaded into shared memory for every level at once, so
+// that only the FP64 additions remain on the per-level chain.
 __global__ void __launch_bounds__(32) k_velc(MoDev a)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ncol = a.maxi * a.maxj;
-    if (t >= ncol) return;
-    const int i = t % a.maxi + 1, j = t / a.maxi + 1;
-    const int maxk = a.maxk;
+    extern __shared__ double vsm[];   // [6][maxk][32]: dzu(1), dzu(2), u1(1), u1(2), u(1), u(2)
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + lane;
+    const int ncol = a.maxi * a.maxj, maxk = a.maxk;
+    const bool on = t < ncol;
+    const int i = on ? t % a.maxi + 1 : 1, j = on ? t / a.maxi + 1 : 1;
+    const int k1 = on ? K1(a, i, j) : maxk + 1;
+    auto S = [&](int q, int k) -> double & { return vsm[((size_t)q * maxk + (k - 1)) * 32 + lane]; };
+    for (int k = k1; k <= maxk; ++k) {
+        S(0, k) = a.dzu[(size_t)t + (size_t)ncol * (k - 1)];
+        S(1, k) = a.dzu[(size_t)t + (size_t)ncol * (k - 1) + (size_t)ncol * maxk];
+        S(2, k) = a.u1[Ui(a, 1, i, j, k)];
+        S(3, k) = a.u1[Ui(a, 2, i, j, k)];
+    }
+    if (!on) return;
     const double rel = a.rel;
-    const int k1 = K1(a, i, j);
-    const double *dzu1 = a.dzu + t, *dzu2 = a.dzu + t + (size_t)ncol * maxk;
     double sum[2] = {0.0, 0.0};
-    for (int l = 1; l <= 2; ++l) {
-        const double *dz_l = l == 1 ? dzu1 : dzu2;
+    for (int l = 0; l < 2; ++l) {
         double prev = 0.0, uprev = 0.0;
         for (int k = k1; k <= maxk; ++k) {
-            const double d = dz_l[(size_t)ncol * (k - 1)];
+            const double d = S(l, k);
             if (k == k1) {
                 uprev = 0;
             } else {
                 uprev = uprev + a.dza[k - 2] * (d + prev) * 0.5;
-                sum[l - 1] = sum[l - 1] + a.dz[k - 1] * uprev;
+                sum[l] = sum[l] + a.dz[k - 1] * uprev;
             }
-            a.u[Ui(a, l, i, j, k)] = uprev;
+            S(4 + l, k) = uprev;
             prev = d;
         }
     }
+    const int k1e = K1(a, i + 1, j), k1n = K1(a, i, j + 1);
+    const double rh1 = RH(a, 1, i, j), rh2 = RH(a, 2, i, j);
+    const double ub1 = a.ub[UBi(a, 1, i, j)], ub2 = a.ub[UBi(a, 2, i, j)];
     for (int k = k1; k <= maxk; ++k) {
-        if (K1(a, i + 1, j) <= k) {
-            double v = a.u[Ui(a, 1, i, j, k)] - sum[0] * RH(a, 1, i, j) + a.ub[UBi(a, 1, i, j)];
-            v = rel * a.u1[Ui(a, 1, i, j, k)] + (1.0 - rel) * v;
-            a.u[Ui(a, 1, i, j, k)] = v;
-            a.u1[Ui(a, 1, i, j, k)] = v;
+        double v1 = S(4, k), v2 = S(5, k);
+        if (k1e <= k) {
+            v1 = v1 - sum[0] * rh1 + ub1;
+            v1 = rel * S(2, k) + (1.0 - rel) * v1;
+            a.u1[Ui(a, 1, i, j, k)] = v1;
         }
-        if (K1(a, i, j + 1) <= k) {
-            double v = a.u[Ui(a, 2, i, j, k)] - sum[1] * RH(a, 2, i, j) + a.ub[UBi(a, 2, i, j)];
-            v = rel * a.u1[Ui(a, 2, i, j, k)] + (1.0 - rel) * v;
-            a.u[Ui(a, 2, i, j, k)] = v;
-            a.u1[Ui(a, 2, i, j, k)] = v;
+        if (k1n <= k) {
+            v2 = v2 - sum[1] * rh2 + ub2;
+            v2 = rel * S(3, k) + (1.0 - rel) * v2;
+            a.u1[Ui(a, 2, i, j, k)] = v2;
         }
+        a.u[Ui(a, 1, i, j, k)] = v1;
+        a.u[Ui(a, 2, i, j, k)] = v2;
     }
-    if (i == a.maxi)
-        for (int k = K1(a, 1, j); k <= maxk; ++k) a.u[Ui(a, 1, 0, j, k)] = a.u[Ui(a, 1, a.maxi, j, k)];
+    if (i == a.maxi) {
+        const int k1w = K1(a, 1, j);
+        for (int k = k1w; k <= maxk; ++k) a.u[Ui(a, 1, 0, j, k)] = a.u[Ui(a, 1, a.maxi, j, k)];
+    }
 }
 
 // w from continuity (velc :3666-3678)
@@ -698,6 +713,8 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     if (e == cudaSuccess) e = dev_zero(h, &a.psi, npsi);
     if (e == cudaSuccess) e = dev_zero(h, &a.scr, 2 * (size_t)d.isles * d.mpi);   // island path terms
     if (e == cudaSuccess) e = dev_zero(h, &a.dzu, 2 * (size_t)maxi * maxj * maxk);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_velc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(6 * (size_t)maxk * 32 * sizeof(double)));
     if (e == cudaSuccess) e = dev_zero(h, &a.u, nu);
     if (e == cudaSuccess) e = dev_zero(h, &a.u1, nu);
     if (e != cudaSuccess) {
@@ -807,7 +824,7 @@ static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u)
     k_island<<<1, 256, 0, s>>>(a, a.scr);
     k_corr<<<(unsigned)((nub + npsi + 127) / 128), 128, 0, s>>>(a);
     k_dzu<<<(unsigned)(((size_t)ncol * a.maxk + 127) / 128), 128, 0, s>>>(a);
-    k_velc<<<(ncol + 31) / 32, 32, 0, s>>>(a);
+    k_velc<<<(ncol + 31) / 32, 32, 6 * (size_t)a.maxk * 32 * sizeof(double), s>>>(a);
     k_w<<<(ncol + 31) / 32, 32, 0, s>>>(a);
     if (cudaGetLastError() != cudaSuccess) return GB_GO_ECUDA;
     // the new velocities are the ocean handle's for its next tstepo
