@@ -14,11 +14,10 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import Optional
 
 import numpy as np
 
-from . import abi, grid
+from . import grid
 from .abi import dptr
 from .goldstein import GoldsteinError, load_library
 
