@@ -477,6 +477,24 @@ int ocean_state(gb_go_handle *h, OceanState *o)
     return GB_GO_OK;
 }
 
+int ocean_refresh_rho(gb_go_handle *h)
+{
+    if (h->precision != GB_GO_FP32FLUX || h->steps_since_upload == 0) return GB_GO_OK;
+    const int r = fp32_member_export(&h->f32, h->ts_buf[h->cur], h->rho, h->ts_static, h->stream);
+    return r ? fail(h, r, "fp32 export failed") : GB_GO_OK;
+}
+
+int ocean_velocity_changed(gb_go_handle *h)
+{
+    if (h->precision != GB_GO_FP32FLUX) {
+        h->vel_ready = true;
+        return GB_GO_OK;
+    }
+    if (!h->vel_ready) return fail(h, GB_GO_ENOTREADY, "split-precision form: the first velocity field comes from gb_go_set_velocity");
+    const int r = fp32_member_set_velocity(&h->f32, nullptr, h->u, h->m, h->stream);
+    return r ? fail(h, r, "fp32 set_velocity (device) failed") : GB_GO_OK;
+}
+
 int ocean_state_reloaded(gb_go_handle *h)
 {
     const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);

@@ -115,6 +115,12 @@ struct OceanState {
 struct gb_go_handle;
 namespace gbgo {
 int ocean_state(gb_go_handle *h, OceanState *out);
+// the split-precision form keeps its state group-planar and forms rho on export: bring rho up to
+// date with the current state (a no-op for the FP64 form)
+int ocean_refresh_rho(gb_go_handle *h);
+// velocities written on the device: the split-precision form rebuilds its transfer
+// coefficients from them (on the device; the first velocity field must come from the host)
+int ocean_velocity_changed(gb_go_handle *h);
 void count_launches(uint64_t n);   // kernels this library started (gb_go_kernel_launch_count)
 // after the state arrays were rewritten on the device: the handle continues as after an upload
 // (ts_buf[0] = ts1_static, ts_buf[1] = ts_static, step counters reset)

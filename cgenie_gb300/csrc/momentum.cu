@@ -775,9 +775,10 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
     MoDev a = h->dev;
     if (o.d.maxi != a.maxi || o.d.maxj != a.maxj || o.d.maxk != a.maxk)
         return mfail(h, GB_GO_EINVAL, "step: ocean grid differs from the momentum grid");
-    if (o.precision != GB_GO_FP64) return mfail(h, GB_GO_EUNSUPPORTED, "step: FP64-form ocean handles only");
     if (o.device != h->device) return mfail(h, GB_GO_EINVAL, "step: handles on different devices");
     MO_TRY(h, cudaSetDevice(h->device));
+    // the split-precision form's density is formed from its current state first
+    if (ocean_refresh_rho(ocean) != GB_GO_OK) return mfail(h, GB_GO_ECUDA, std::string("step: ") + gb_go_last_error(ocean));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     a.rho = o.rho;
     if (h->graph && (h->graph_rho != o.rho || h->graph_u != o.u || h->graph_stream != s)) {
@@ -805,8 +806,10 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
     }
     MO_TRY(h, cudaGraphLaunch(h->graph, s));
     count_launches(9);
+    // the split-precision form rebuilds its transfer coefficients from the new velocities
+    const int r = ocean_velocity_changed(ocean);
+    if (r != GB_GO_OK) return mfail(h, r, std::string("step: ") + gb_go_last_error(ocean));
     MO_TRY(h, cudaStreamSynchronize(s));
-    *o.vel_ready = true;
     return GB_GO_OK;
 }
 

@@ -4,9 +4,11 @@
  * Replaces the momentum part of step_goldstein (src/goldstein/goldstein.f90:198-233): wind
  * (:3685-3714), jbar (:3217-3315), ubarsolv (:3500-3565), the island path integrals
  * (goldstein_lib.f90:186-241) with matmult (:3470-3492) and the island corrections of ub and
- * psi (:209-229), and velc (:3568-3679).  It reads the density of an FP64-form gb_go handle
- * and writes that handle's velocities, so the ocean step (momentum, then tstepo) runs without
- * host copies of rho or u.
+ * psi (:209-229), and velc (:3568-3679).  It reads the density of a gb_go handle and writes
+ * that handle's velocities, so the ocean step (momentum, then tstepo) runs without host copies
+ * of rho or u.  With the split-precision form the density is first formed from the current
+ * state, and the transfer coefficients are rebuilt on the device from the new velocities (the
+ * handle's first velocity field must come from gb_go_set_velocity).
  *
  * The initialisation of the reference (invert :3138-3204, the unit-source solves and island
  * integrals and matinv_gold of :1788-1814) runs on the host at gb_mo_create.  The banded
@@ -71,7 +73,7 @@ void gb_mo_destroy(gb_mo *h);
 int gb_mo_set_wind(gb_mo *h, const double *tau, const double *dztau, const double *dztav);
 /* u and u1 (3, 0:maxi, 0:maxj, maxk), e.g. from a restart; both start at 0 otherwise */
 int gb_mo_upload_velocity(gb_mo *h, const double *u, const double *u1);
-/* One momentum step on `ocean`'s density (an FP64-form gb_go handle of the same grid); the new
+/* One momentum step on `ocean`'s density (a gb_go handle of the same grid, either form); the new
    velocities become `ocean`'s velocities for its next gb_go_tstepo. */
 int gb_mo_step(gb_mo *h, gb_go_handle *ocean);
 /* u, u1 (3, 0:maxi, 0:maxj, maxk), ub (2, 0:maxi+1, 0:maxj), psi (0:maxi, 0:maxj); any may be NULL */
