@@ -498,9 +498,10 @@ extern "C" int gb_bg_tracercoupling(gb_bg *h, gb_go_handle *ocean)
     if (!o.state_ready) return bfail(h, GB_GO_ENOTREADY, "tracercoupling: ocean state not uploaded");
     if (o.d.maxi != h->d.n_i || o.d.maxj != h->d.n_j || o.d.maxk != h->d.n_k || o.d.L != h->d.n_l_ocn)
         return bfail(h, GB_GO_EINVAL, "tracercoupling: ocean grid differs from the BIOGEM grid");
-    if (o.precision != GB_GO_FP64) return bfail(h, GB_GO_EUNSUPPORTED, "tracercoupling: FP64-form ocean handles only");
     if (o.device != h->device) return bfail(h, GB_GO_EINVAL, "tracercoupling: handles on different devices");
     BG_TRY(h, cudaSetDevice(h->device));
+    // the split-precision form: its current state in Fortran layout first (into ts_buf[cur])
+    if (ocean_refresh_rho(ocean) != GB_GO_OK) return bfail(h, GB_GO_ECUDA, std::string("tracercoupling: ") + gb_go_last_error(ocean));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     BgArgs a = args_of(h);
     // go_ts: the wet cells of the current step buffer once the handle has stepped

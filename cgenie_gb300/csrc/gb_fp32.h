@@ -160,6 +160,8 @@ void fp32_member_free(Fp32Member *f);
 // uploaded ts1 on the device (Fortran layout), converted to the group-planar state
 int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_host, const double *ts1_dev, cudaStream_t s);
 int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s);
+// both step buffers from a Fortran-layout ts1 on the device (state rewritten between steps)
+int fp32_member_reload(Fp32Member *f, const double *ts1_dev, cudaStream_t s);
 // The first velocity field is taken from the host (coefficients and fixed-point scales);
 // later ones from u_dev (device copy, coefficients rebuilt on the device).
 int fp32_member_set_velocity(Fp32Member *f, const double *u_host, const double *u_dev, const Metrics &m,

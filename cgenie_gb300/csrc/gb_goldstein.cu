@@ -503,6 +503,10 @@ int ocean_state_reloaded(gb_go_handle *h)
     h->cur = 0;
     h->slot = 0;
     h->steps_since_upload = 0;
+    if (h->precision == GB_GO_FP32FLUX) {
+        const int r = fp32_member_reload(&h->f32, h->ts1_static, h->stream);
+        if (r) return fail(h, r, "fp32 reload failed");
+    }
     return GB_GO_OK;
 }
 }  // namespace gbgo

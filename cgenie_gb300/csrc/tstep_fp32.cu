@@ -1580,6 +1580,18 @@ int fp32_member_upload(Fp32Member *f, const double *ts1_host, const double *ts_h
     return upload_scales(h, s);
 }
 
+int fp32_member_reload(Fp32Member *f, const double *ts1_dev, cudaStream_t s)
+{
+    // the state rewritten on the device (the BIOGEM coupling): both step buffers from ts1, the
+    // step parity restarts; the forcing transfers and the fixed-point scales are kept (the
+    // scales follow the state through the rescaling of the steps)
+    Fp32Host *h = host_of(f);
+    if (fp32_to_planar(h->data.plan_buf[0], ts1_dev, h->d, s) || fp32_to_planar(h->data.plan_buf[1], ts1_dev, h->d, s))
+        return GB_GO_ECUDA;
+    h->data.steps = 0;
+    return cuda_ok(cudaStreamSynchronize(s));
+}
+
 int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s)
 {
     Fp32Host *h = host_of(f);

@@ -63,8 +63,10 @@ int gb_bg_upload(gb_bg *h, const double *vocn, const double *mass, const double 
 /* The increments of the interval: vdocn (n_l_ocn, n_k, n_vocn) and vdbio_part
    (n_l_sed, n_k, n_vocn; NULL when n_l_sed = 0). */
 int gb_bg_set_increments(gb_bg *h, const double *vdocn, const double *vdbio_part);
-/* biogem_tracercoupling(go_ts, go_ts1) on the current state of `ocean` (an FP64-form
-   gb_go handle of the same n_i, n_j, n_k and maxl = n_l_ocn, with its state uploaded).
+/* biogem_tracercoupling(go_ts, go_ts1) on the current state of `ocean` (a gb_go handle of the
+   same n_i, n_j, n_k and maxl = n_l_ocn, with its state uploaded).  The split-precision form's
+   state is exported to Fortran layout first and re-imported afterwards (its fixed-point scales
+   are kept and follow the state through the steps' rescaling).
    Afterwards the handle's ts and ts1 hold the coupled tracers on every interior cell (0 on
    land and below k1) and ts1 its periodic i-halo, as step_goldstein's copy-in and boundary
    conditions (src/goldstein/goldstein.f90:176-187) leave them before the next tstepo. */

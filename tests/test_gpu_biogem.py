@@ -130,13 +130,38 @@ def test_errors(gpu_lib):
     with pytest.raises(GoldsteinError) as e:
         bg.tracercoupling(g2)
     assert e.value.code == abi.GB_GO_EINVAL
-    g3 = new_member_run(m, precision=abi.GB_GO_FP32FLUX)
-    with pytest.raises(GoldsteinError) as e:
-        bg.tracercoupling(g3)
-    assert e.value.code == abi.GB_GO_EUNSUPPORTED
-    for h in (g, g2, g3):
+    for h in (g, g2):
         h.close()
     bg.close()
+
+
+def test_split_precision_handle(gpu_lib):
+    """The coupling on a split-precision handle: its state is exported, coupled in FP64 and
+    re-imported; steps before and after stay within the form's bars of the oracle (T and S
+    1e-11, the other tracers 1e-6), BIOGEM's fields within 1e-10."""
+    from cgenie_gb300.goldstein import new_member_run
+    m = grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=12, maxl=6, seed=32, tracer_kind="bgc"))
+    st = biogem.make_state(m, n_l_sed=2, seed=14)
+    g = new_member_run(m, precision=abi.GB_GO_FP32FLUX)
+    bg = biogem.BiogemCoupling(m, n_l_sed=2)
+    bg.upload(st)
+    bg.set_increments(st)
+    g.tstepo(4)
+    bg.tracercoupling(g)
+    g.tstepo(3)
+    out = g.download()
+    vocn = bg.download()[0]
+    s, a = oracle_run(m, st, steps_before=4, steps_after=3)
+    kk = np.arange(m.maxk + 2)[:, None, None]
+    wet = (kk >= m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
+    wet[:, :, 0] = wet[:, :, -1] = False
+    for l in range(m.maxl):
+        x, y = out["ts"][..., l][wet], s.ts[..., l][wet]
+        err = np.abs(x - y).max() / np.abs(y).max()
+        assert err <= (1e-11 if l < 2 else 1e-6), (l, err)
+    np.testing.assert_allclose(vocn, a.vocn, rtol=1e-10, atol=1e-12 * np.abs(a.vocn).max())
+    bg.close()
+    g.close()
 
 
 def test_reupload_between_couplings(gpu_lib):
