@@ -17,6 +17,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
       the model calls it; `value` is air cell-updates/s
   ea36e the EMBM step of a 256-member ensemble of 36x36 surface grids, one launch per step
       for all members (gb_ea_step_many)
+  ocean36 the device-resident ocean step of a 36x36x16 basin with 8 tracers: momentum, then
+      tstepo (split-precision form), and the BIOGEM tracer coupling every 5th step; `value` is
+      tracer cell-updates/s of the whole step
   mo36 the momentum step (wind, jbar, streamfunction, islands, velc) of a 36x36x16 basin
       with two islands, on the density of an FP64 handle; `value` is wet-cell momentum
       updates/s (each wet cell's u, v, w advanced one step)
@@ -62,6 +65,8 @@ WORKLOADS = {
     "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
     "ea36e": dict(name="embm_tstipa_ensemble256_36x36", maxi=36, maxj=36, members=256),
     "mo36": dict(name="momentum_36x36x16_2islands", maxi=36, maxj=36, maxk=16),
+    "ocean36": dict(name="ocean_step_36x36x16_L8_momentum_tracers_biogem", maxi=36, maxj=36, maxk=16, maxl=8,
+                    couple_every=5),
 }
 
 
@@ -542,8 +547,120 @@ def run_mo(args, rank, world, local, dist):
     g.close()
 
 
+def run_ocean(args, rank, world, local, dist):
+    """Momentum + tracer step + BIOGEM coupling on one basin, all on the device."""
+    import torch
+    from cgenie_gb300 import abi, biogem, grid, momentum
+    from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+    w = WORKLOADS[args.workload]
+    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=w["maxk"], maxl=w["maxl"], seed=41,
+                                           mask="basin_island", tracer_kind="bgc"))
+    case = momentum.make_case(m, seed=42)
+    st = biogem.make_state(m, n_l_sed=4, seed=43)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = new_member_run(m, device=local, stream=stream.cuda_stream, precision=abi.GB_GO_FP32FLUX)
+    mo = momentum.Momentum(case, device=local)
+    mo.set_wind()
+    bg = biogem.BiogemCoupling(m, n_l_sed=4, device=local)
+    bg.upload(st)
+    bg.set_increments(st)
+    every = w["couple_every"]
+
+    def ocean_step(n):
+        mo.step(g)
+        g.tstepo(1)
+        if (n + 1) % every == 0:
+            bg.tracercoupling(g)
+
+    for n in range(args.warmup):
+        ocean_step(n)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    n0 = kernel_launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for n in range(args.steps):
+        ocean_step(n)
+    end.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = kernel_launch_count() - n0
+    total_ms = start.elapsed_time(end)
+    units = m.wet_cells * m.maxl
+    value = world * units * args.steps / (total_ms * 1e-3)
+    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(m)
+    if rank == 0:
+        line = {
+            "metric": "tracer cell-updates/s", "value": value, "unit": "tracer cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 transfers, f64 state",
+            "data": "synthetic (seeded basin with two islands, BIOGEM fields, reference grid formulas)",
+            "config": {"workload": w["name"], "maxi": m.maxi, "maxj": m.maxj, "maxk": m.maxk, "maxl": m.maxl,
+                       "wet_cells": m.wet_cells, "couple_every": every, "precision": "fp32flux",
+                       "l2": "not flushed: the whole model state stays on the device, as in a run",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "the ocean step moves nothing across the host boundary: rho, u, ts stay on the device"},
+            "roofline": {"bound": "hbm", "achieved": alg / (total_ms * 1e-3 / args.steps) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg / (total_ms * 1e-3 / args.steps) / 1e9 / peak, "traffic": None,
+                         "peak_source": peak_kind, "kernel": "ocean step (momentum graph, tracer step, coupling)",
+                         "algorithmic_bytes_per_launch": alg, "note": "tracer-step algorithmic bytes per ocean step"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, n, _ = ocean_cpu_rate(w, 20)
+            line["cpu_baseline"] = {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
+                                    "sample": f"{n} ocean steps (momentum, tracer step, coupling), oracle C "
+                                              f"restatements, serial"}
+        print(json.dumps(line))
+    bg.close()
+    mo.close()
+    g.close()
+
+
+def ocean_cpu_rate(w, steps):
+    """The oracles' ocean step (momentum, tracer step, coupling every few steps), serial."""
+    import numpy as np
+    from cgenie_gb300 import biogem, grid, momentum
+    from oracle import oracle_lib
+    m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=w["maxk"], maxl=w["maxl"], seed=41,
+                                           mask="basin_island", tracer_kind="bgc"))
+    case = momentum.make_case(m, seed=42)
+    st = biogem.make_state(m, n_l_sed=4, seed=43)
+    om = oracle_lib.OracleMomentum(case)
+    s = oracle_lib.OracleState(m)
+    t0 = time.perf_counter()
+    for n in range(steps):
+        om.step(s.rho)
+        s.u = np.ascontiguousarray(om.state()["u"])
+        s.step(1)
+        if (n + 1) % w["couple_every"] == 0:
+            go, go1 = oracle_lib.bg_tracercoupling(m, st, oracle_lib.go_ts_interior(s.ts))
+            oracle_lib.after_coupling(s, go, go1)
+    dt = time.perf_counter() - t0
+    om.close()
+    return m.wet_cells * m.maxl * steps / dt, steps, dt
+
+
 def run_reference(args, rank, world):
     w = dict(WORKLOADS[args.workload])
+    if args.workload == "ocean36":
+        v, n, dt = ocean_cpu_rate(w, max(5, min(args.steps, 50)))
+        line = {
+            "metric": "tracer cell-updates/s", "value": v, "unit": "tracer cell-updates/s", "impl": "reference",
+            "n_gpus": world, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "couple_every": w["couple_every"]},
+            "cpu_baseline": {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} ocean steps (momentum, tracer step, coupling), oracle C restatements, serial"},
+            "e2e": {"value": v, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
     if args.workload == "mo36":
         m, case = _mo_member(w)
         v, n = mo_cpu_rate(m, case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
@@ -820,6 +937,11 @@ def main():
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
     if args.workload == "c3":
         run_c3(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload == "ocean36":
+        run_ocean(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
         return
