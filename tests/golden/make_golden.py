@@ -5,6 +5,8 @@ these fixtures pin the oracle's results: every case was produced by the C
 restatement (oracle/goldstein_oracle.c) and checked bit-identical against the
 independent NumPy restatement (oracle/goldstein_np.py) before being written.
 Run from the repository root:  python tests/golden/make_golden.py
+(The fixtures of the BIOGEM coupling, the surface steppers and the momentum step are in
+rows/, made by rows/make_golden_rows.py.)
 """
 import os
 import sys
