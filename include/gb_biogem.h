@@ -8,7 +8,7 @@
  * tracer field, adds BIOGEM's increments (vdocn, vdbio_part), rescales the biogeochemical
  * inventories and the cell masses with the change of mean salinity, and writes the result back
  * into go_ts and go_ts1.  Here the GOLDSTEIN tracers are the device state of a gb_go handle
- * (FP64 form) and BIOGEM's vector fields stay on the same device, so no tracer array crosses
+ * (either form) and BIOGEM's vector fields stay on the same device, so no tracer array crosses
  * the host boundary at a coupling.
  *
  * Vector form (src/biogem/biogem_lib.f90:1056-1081, 1335-1410): the wet columns of
