@@ -65,6 +65,8 @@ WORKLOADS = {
     "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
     "ea36e": dict(name="embm_tstipa_ensemble256_36x36", maxi=36, maxj=36, members=256),
     "mo36": dict(name="momentum_36x36x16_2islands", maxi=36, maxj=36, maxk=16),
+    "rs5": dict(name="goldstein_restart_write_360x180x32_L24", factory="config_c5"),
+    "rs5s": dict(name="goldstein_restart_write_360x180x32_L2", factory="config_c5", maxl=2),
     "ocean36": dict(name="ocean_step_36x36x16_L8_momentum_tracers_biogem", maxi=36, maxj=36, maxk=16, maxl=8,
                     couple_every=5),
 }
@@ -547,6 +549,131 @@ def run_mo(args, rank, world, local, dist):
     g.close()
 
 
+def _rs_coords(m):
+    import numpy as np
+    return (np.linspace(0.0, 360.0, m.maxi, endpoint=False) + 0.5, np.linspace(-89.5, 89.5, m.maxj),
+            np.cumsum(np.linspace(10.0, 400.0, m.maxk)))
+
+
+def rs_cpu_rate(m, target_s: float):
+    """The reference's restart path restated on the host: outm_netcdf's field forming (NumPy
+    restatement of the oracle) and a netCDF classic write (scipy's writer standing in for the
+    netCDF library), repeated for about target_s seconds."""
+    import tempfile
+
+    import numpy as np
+    from scipy.io import netcdf_file
+    from oracle import restart_np
+    lon, lat, ncdepth = _rs_coords(m)
+    n, t0 = 0, time.perf_counter()
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "goldstein_restart.nc")
+        while True:
+            f = restart_np.restart_fields(m.ts, m.u, m.k1, m.maxi, m.maxj, m.maxk)
+            with netcdf_file(path, "w", version=1) as nc:
+                for d, ln in (("nrecs", 1), ("longitude", m.maxi), ("latitude", m.maxj), ("depth", m.maxk)):
+                    nc.createDimension(d, ln)
+                for v, a, d in (("longitude", lon, "longitude"), ("latitude", lat, "latitude")):
+                    nc.createVariable(v, "f", (d,))[:] = a
+                nc.createVariable("depth", "f", ("depth",))[:] = restart_np.depths1(ncdepth)
+                for v in ("ioffset", "iyear", "imonth", "iday"):
+                    nc.createVariable(v, "i", ("nrecs",))[:] = 1
+                for v, a in zip(("temp", "salinity", "uvel", "vvel"), f):
+                    nc.createVariable(v, "d", ("depth", "latitude", "longitude"))[:] = a
+                for v in ("evap", "late", "sens"):
+                    nc.createVariable(v, "d", ("latitude", "longitude"))[:] = np.zeros((m.maxj, m.maxi))
+            n += 1
+            dt = time.perf_counter() - t0
+            if dt >= target_s or n >= 200:
+                break
+    return n * m.maxi * m.maxj * m.maxk / dt, n
+
+
+def run_rs(args, rank, world, local, dist):
+    """Restart writes of a device-resident ocean (outm_netcdf): the fields formed on the device
+    in the file's byte order and one D2H copy.  value: ocean cells per second of that device
+    part (gb_rs_pack_goldstein + the copy into pinned memory, CUDA events), the state resident;
+    e2e: the public call gb_rs_write_goldstein, file written, timed on the host clock."""
+    import tempfile
+
+    import torch
+    from cgenie_gb300 import grid, restart
+    from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
+    import dataclasses
+    w = WORKLOADS[args.workload]
+    m = grid.make_member(dataclasses.replace(getattr(grid, w["factory"])(), **({"maxl": w["maxl"]} if "maxl" in w else {})))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = new_member_run(m, device=local, stream=stream.cuda_stream)
+    g.tstepo(1)
+    lon, lat, ncdepth = _rs_coords(m)
+    cal = restart.Calendar(iyear=2000, imonth=1, day=1.0)
+    td = tempfile.mkdtemp(prefix="gb_rs_")
+    path = os.path.join(td, f"goldstein_restart_r{rank}.nc")
+    cells = m.maxi * m.maxj * m.maxk
+    dev = torch.empty(4 * cells, dtype=torch.float64, device=f"cuda:{local}")
+    host = torch.empty(4 * cells, dtype=torch.float64).pin_memory()
+    for _ in range(args.warmup):
+        restart.pack_goldstein(g, dev.data_ptr())
+        host.copy_(dev, non_blocking=True)
+        restart.write_goldstein(g, path, cal, lon, lat, ncdepth)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=f"cuda:{local}")   # 256 MB > L2
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = kernel_launch_count()
+    for s_ in range(args.steps):
+        flush.zero_()
+        ev[s_][0].record(stream)
+        restart.pack_goldstein(g, dev.data_ptr())
+        ev[s_][1].record(stream)
+        host.copy_(dev, non_blocking=True)
+        ev[s_][2].record(stream)
+    torch.cuda.synchronize()
+    launches = kernel_launch_count() - n0
+    clocks = sampler.stop()
+    kern_ms = float(sum(e[0].elapsed_time(e[1]) for e in ev)) / args.steps
+    dev_ms = float(sum(e[0].elapsed_time(e[2]) for e in ev)) / args.steps
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        restart.write_goldstein(g, path, cal, lon, lat, ncdepth)
+    e2e_s = time.perf_counter() - t1
+    size = os.path.getsize(path)
+    os.remove(path)
+    os.rmdir(td)
+    cells = m.maxi * m.maxj * m.maxk
+    peak, peak_kind = measured_peaks()
+    alg = 64 * cells   # per cell: T, S and u, v read (32 B), the four fields written (32 B)
+    if rank == 0:
+        line = {
+            "metric": "ocean cells written/s", "value": world * cells / (dev_ms * 1e-3), "unit": "ocean cells written/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": f"synthetic (seeded 360x180x32 ocean, {m.maxl} tracers, one step taken)",
+            "config": {"workload": w["name"], "maxi": m.maxi, "maxj": m.maxj, "maxk": m.maxk, "maxl": m.maxl,
+                       "file_bytes": size, "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * cells * args.steps / e2e_s, "unit": "ocean cells written/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 32 * cells,
+                    "note": "per step: gb_rs_write_goldstein, the public call: device fields, one D2H into the "
+                            "pinned file image, the file written (page cache)"},
+            "roofline": {"bound": "hbm", "achieved": alg / (kern_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (kern_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "k_rs_pack (stream events around gb_rs_pack_goldstein)", "kernel_us": 1e3 * kern_ms,
+                         "algorithmic_bytes_per_launch": alg},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, n = rs_cpu_rate(m, target_s=10.0)
+            line["cpu_baseline"] = {"value": v, "unit": "ocean cells written/s", "cores": 1, "kind": "port",
+                                    "sample": f"{n} restarts of the same ocean: NumPy field forming + scipy netCDF write"}
+        print(json.dumps(line))
+    g.close()
+
+
 def run_ocean(args, rank, world, local, dist):
     """Momentum + tracer step + BIOGEM coupling on one basin, all on the device."""
     import torch
@@ -658,6 +785,22 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
                              "sample": f"{n} ocean steps (momentum, tracer step, coupling), oracle C restatements, serial"},
             "e2e": {"value": v, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+    if args.workload in ("rs5", "rs5s"):
+        import dataclasses
+        from cgenie_gb300 import grid
+        m = grid.make_member(dataclasses.replace(getattr(grid, w["factory"])(), **({"maxl": w["maxl"]} if "maxl" in w else {})))
+        v, n = rs_cpu_rate(m, target_s=min(20.0, 2.0 * max(args.steps, 1)))
+        line = {
+            "metric": "ocean cells written/s", "value": v, "unit": "ocean cells written/s", "impl": "reference",
+            "n_gpus": world, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * m.maxi * m.maxj * m.maxk / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "maxi": m.maxi, "maxj": m.maxj, "maxk": m.maxk, "maxl": m.maxl},
+            "cpu_baseline": {"value": v, "unit": "ocean cells written/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} restarts: NumPy restatement of outm_netcdf's fields + scipy netCDF write"},
+            "e2e": {"value": v, "unit": "ocean cells written/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
         return
@@ -942,6 +1085,11 @@ def main():
         return
     if args.workload == "ocean36":
         run_ocean(args, rank, world, local, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in ("rs5", "rs5s"):
+        run_rs(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
         return

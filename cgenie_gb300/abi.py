@@ -87,6 +87,12 @@ class GbBgParams(C.Structure):
     _fields_ = [("ts_offset", C.c_double * 2), ("force_ts", C.c_int32), ("pad", C.c_int32)]
 
 
+class GbRsCalendar(C.Structure):
+    """gb_rs_calendar: iyear_rest, imonth_rest, ioffset_rest, istep_ocn and day_rest."""
+    _fields_ = [("iyear", C.c_int32), ("imonth", C.c_int32), ("ioffset", C.c_int32), ("istep", C.c_int32),
+                ("day", C.c_double)]
+
+
 GB_EA_EMBM = 0
 GB_EA_SEAICE = 1
 GB_EA_SEAICE_EXPLICIT = 2

@@ -31,6 +31,7 @@ SOURCES = {
     "biogem_coupling.cu": ["-fmad=false"],
     "surface_step.cu": ["-fmad=false"],
     "momentum.cu": ["-fmad=false"],
+    "restart.cu": ["-fmad=false"],
 }
 
 

@@ -41,6 +41,8 @@ EXPORTED = [
     "gb_ea_last_error",
     "gb_mo_create", "gb_mo_destroy", "gb_mo_set_wind", "gb_mo_upload_velocity", "gb_mo_step", "gb_mo_download",
     "gb_mo_last_error",
+    "gb_rs_write_goldstein", "gb_rs_pack_goldstein", "gb_rs_write_fields", "gb_rs_read_goldstein", "gb_rs_goldstein_name",
+    "gb_rs_calendar_step", "gb_rs_calendar_after_read", "gb_rs_last_error",
 ]
 
 _lib = None
@@ -137,6 +139,19 @@ def load_library(path: str = LIB_PATH):
     L.gb_mo_download.argtypes = [vp, dp, dp, dp, dp]
     L.gb_mo_last_error.argtypes = [vp]
     L.gb_mo_last_error.restype = C.c_char_p
+    L.gb_rs_write_goldstein.argtypes = [vp, C.c_char_p, vp, C.c_int32, dp, dp, dp, dp, dp, dp]
+    L.gb_rs_pack_goldstein.argtypes = [vp, vp]
+    L.gb_rs_write_fields.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32,
+                                     dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+    L.gb_rs_read_goldstein.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp,
+                                       dp, dp, dp, dp, dp, dp, dp]
+    L.gb_rs_goldstein_name.argtypes = [C.c_char_p, vp, C.c_char_p, C.c_int32]
+    L.gb_rs_calendar_step.argtypes = [vp, C.c_double, C.c_int32]
+    L.gb_rs_calendar_step.restype = None
+    L.gb_rs_calendar_after_read.argtypes = [vp, C.c_double, C.c_int32]
+    L.gb_rs_calendar_after_read.restype = None
+    L.gb_rs_last_error.argtypes = []
+    L.gb_rs_last_error.restype = C.c_char_p
     _lib = L
     return L
 

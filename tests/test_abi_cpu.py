@@ -13,10 +13,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     names = set()
-    for h in ("gb_goldstein.h", "gb_biogem.h", "gb_embm.h", "gb_momentum.h"):
+    for h in ("gb_goldstein.h", "gb_biogem.h", "gb_embm.h", "gb_momentum.h", "gb_restart.h"):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo)_[a-z0-9_]+)\s*\(", src))
+        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo|rs)_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 
@@ -43,6 +43,7 @@ def test_struct_layouts():
     assert C.sizeof(abi.GbEaDims) == 8
     assert C.sizeof(abi.GbEaParams) == 8 + 14 * 8
     assert C.sizeof(abi.GbEaGrid) == 7 * 8
+    assert C.sizeof(abi.GbRsCalendar) == 4 * 4 + 8
     from cgenie_gb300 import momentum
     assert C.sizeof(momentum.GbMoDims) == 24
     assert C.sizeof(momentum.GbMoParams) == 24
