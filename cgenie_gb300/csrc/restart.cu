@@ -180,7 +180,8 @@ int fill_image(uint8_t *img, const NcLayout &L, int maxi, int maxj, int maxk, co
                const double *lon, const double *lat, const double *depths1, const double *evap, const double *late,
                const double *sens)
 {
-    std::memset(img, 0, L.total_bytes);
+    // every byte after the header belongs to a variable and is written below (all types are
+    // 4 or 8 bytes wide, so no variable has padding)
     const std::vector<uint8_t> h = L.header();
     std::memcpy(img, h.data(), h.size());
     const double *axes[3] = {lon, lat, depths1};
