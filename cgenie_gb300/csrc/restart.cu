@@ -11,11 +11,7 @@
 // one at begin + vsize, which the writer does as well.
 #include <cuda_runtime.h>
 
-#include <fcntl.h>
-#include <unistd.h>
-
 #include <algorithm>
-#include <cerrno>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -23,7 +19,6 @@
 #include <map>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "gb_internal.h"
@@ -217,37 +212,13 @@ int fill_image(uint8_t *img, const NcLayout &L, int maxi, int maxj, int maxk, co
     return GB_GO_OK;
 }
 
-// The file image written with positioned writes from a few threads: one thread moves a few GB/s
-// through the page cache, so a restart of a large grid splits its image in chunks of >= 16 MB.
 int write_file(const char *path, const uint8_t *img, size_t n)
 {
-    const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
-    if (fd < 0) return rs_fail(GB_GO_EINVAL, std::string("cannot create ") + path);
-    const size_t chunk_min = (size_t)16 << 20;
-    const int nthreads = (int)std::max<size_t>(1, std::min<size_t>(8, n / chunk_min));
-    const size_t chunk = (n + nthreads - 1) / nthreads;
-    std::vector<int> ok(nthreads, 1);
-    auto put = [&](int t) {
-        size_t off = (size_t)t * chunk;
-        const size_t end = std::min(n, off + chunk);
-        while (off < end) {
-            const ssize_t w = ::pwrite(fd, img + off, end - off, (off_t)off);
-            if (w <= 0) {
-                if (w < 0 && errno == EINTR) continue;
-                ok[t] = 0;
-                return;
-            }
-            off += (size_t)w;
-        }
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nthreads; ++t) pool.emplace_back(put, t);
-    put(0);
-    for (auto &th : pool) th.join();
-    const int c = ::close(fd);
-    for (int t = 0; t < nthreads; ++t)
-        if (!ok[t]) return rs_fail(GB_GO_EINVAL, std::string("write failed: ") + path);
-    if (c != 0) return rs_fail(GB_GO_EINVAL, std::string("close failed: ") + path);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return rs_fail(GB_GO_EINVAL, std::string("cannot create ") + path);
+    const size_t w = std::fwrite(img, 1, n, f);
+    const int c = std::fclose(f);
+    if (w != n || c != 0) return rs_fail(GB_GO_EINVAL, std::string("write failed: ") + path);
     return GB_GO_OK;
 }
 
