@@ -237,24 +237,53 @@ __device__ __forceinline__ unsigned long long bswap64(unsigned long long v)
     return ((unsigned long long)lo << 32) | hi;
 }
 
-// temp, salinity, uvel, vvel of outm_netcdf (goldstein_data.f90:200-213), one thread per cell,
-// written big-endian one field after another: the data sections of the four variables.
-__global__ void k_rs_pack(unsigned long long *out, const double *ts_static, const double *cur, int use_cur,
-                          const double *u, const int32_t *k1, Dims d)
+// temp, salinity, uvel, vvel of outm_netcdf (goldstein_data.f90:200-213) of one cell c.
+struct PackedCell {
+    double t, s, u, v;
+};
+
+__device__ __forceinline__ PackedCell pack_load(size_t c, const double *__restrict__ ts_static,
+                                                const double *__restrict__ cur, int use_cur,
+                                                const double *__restrict__ u, const int32_t *__restrict__ k1,
+                                                const Dims &d)
+{
+    const int i = (int)(c % d.maxi) + 1;
+    const int j = (int)((c / d.maxi) % d.maxj) + 1;
+    const int k = (int)(c / ((size_t)d.maxi * d.maxj)) + 1;
+    const int kk = k1[i + d.NI * j];
+    const double landmask = kk <= d.maxk ? 1.0 : 0.0;   // the whole column of a wet column
+    const double *src = (use_cur && k >= kk) ? cur : ts_static;
+    const size_t t = ts_index(d, 0, i, j, k);
+    const size_t q = u_index(d, 0, i, j, k);
+    return PackedCell{src[t] * landmask, src[t + 1] * landmask, u[q], u[q + 1]};
+}
+
+__device__ __forceinline__ void pack_store(unsigned long long *__restrict__ out, size_t n, size_t c, const PackedCell &p)
+{
+    out[c] = bswap64((unsigned long long)__double_as_longlong(p.t));
+    out[n + c] = bswap64((unsigned long long)__double_as_longlong(p.s));
+    out[2 * n + c] = bswap64((unsigned long long)__double_as_longlong(p.u));
+    out[3 * n + c] = bswap64((unsigned long long)__double_as_longlong(p.v));
+}
+
+// One thread per pair of cells a grid-stride apart (both cells' loads are issued before the
+// stores), written big-endian one field after another: the data sections of the four variables.
+__global__ void k_rs_pack(unsigned long long *__restrict__ out, const double *__restrict__ ts_static,
+                          const double *__restrict__ cur, int use_cur, const double *__restrict__ u,
+                          const int32_t *__restrict__ k1, Dims d)
 {
     const size_t n = (size_t)d.maxi * d.maxj * d.maxk;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(c % d.maxi) + 1;
-        const int j = (int)((c / d.maxi) % d.maxj) + 1;
-        const int k = (int)(c / ((size_t)d.maxi * d.maxj)) + 1;
-        const int kk = k1[i + d.NI * j];
-        const double landmask = kk <= d.maxk ? 1.0 : 0.0;   // the whole column of a wet column
-        const double *src = (use_cur && k >= kk) ? cur : ts_static;
-        const size_t t = ts_index(d, 0, i, j, k);
-        out[c] = bswap64((unsigned long long)__double_as_longlong(src[t] * landmask));
-        out[n + c] = bswap64((unsigned long long)__double_as_longlong(src[t + 1] * landmask));
-        out[2 * n + c] = bswap64((unsigned long long)__double_as_longlong(u[u_index(d, 0, i, j, k)]));
-        out[3 * n + c] = bswap64((unsigned long long)__double_as_longlong(u[u_index(d, 1, i, j, k)]));
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t c0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c0 < n; c0 += 2 * stride) {
+        const size_t c1 = c0 + stride;
+        const PackedCell p0 = pack_load(c0, ts_static, cur, use_cur, u, k1, d);
+        if (c1 < n) {
+            const PackedCell p1 = pack_load(c1, ts_static, cur, use_cur, u, k1, d);
+            pack_store(out, n, c0, p0);
+            pack_store(out, n, c1, p1);
+        } else {
+            pack_store(out, n, c0, p0);
+        }
     }
 }
 
@@ -535,7 +564,8 @@ int pack_fields(gb_go_handle *ocean, unsigned long long *dev, OceanState &o, boo
         return rs_fail(GB_GO_ECUDA, std::string("restart: state export failed: ") + gb_go_last_error(ocean));
     if (!dev) return GB_GO_OK;
     const size_t n = (size_t)o.d.maxi * o.d.maxj * o.d.maxk;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    // two cells per thread; at most one wave of 8 resident 256-thread blocks on each of 152 SMs
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 511) / 512, 152 * 8));
     k_rs_pack<<<blocks, 256, 0, (cudaStream_t)o.stream>>>(dev, o.ts_static, o.ts_buf[o.cur], o.steps_since_upload > 0 ? 1 : 0,
                                                          o.u, o.k1, o.d);
     count_launches(1);
