@@ -3,7 +3,7 @@
 ! (src/goldstein/goldstein.f90:2280-2432), written in the binding style the
 ! reference already uses for its ITT shim (src/utils/itt_fortran.f90:1-44).
 !
-! Usage in goldstein.f90 (sketch, see INTEGRATION.md):
+! Usage in goldstein.f90 (sketch):
 !   - at the end of initialise_goldstein: CALL gb_tstepo_init()
 !   - replace the body of tstepo with:     CALL gb_tstepo_step()
 !   - at coupling intervals (before go_ts is exported):  CALL gb_tstepo_sync_out()

@@ -1,7 +1,7 @@
 ! ISO_C_BINDING interfaces to the GOLDSTEIN restart files (include/gb_restart.h) of
 ! libgb_goldstein.so, in the binding style of gb_goldstein_mod.f90.
 !
-! Drop-in use (sketch, see INTEGRATION.md):
+! Drop-in use (sketch):
 !   - outm_netcdf(istep) (src/goldstein/goldstein_data.f90:153-354): when MOD(istep, iwstp) == 0
 !     (or a GUI restart is due) form the name with gb_rs_goldstein_name(dirnetout, cal, ...) and
 !     CALL gb_rs_write_goldstein(goh, name, cal, gui, nclon1, nclat1, ncdepth, evap_save2,

@@ -2,7 +2,7 @@
 ! 2-D surface steppers (include/gb_embm.h) of libgb_goldstein.so, in the binding style of
 ! gb_goldstein_mod.f90.
 !
-! Drop-in use (sketch, see INTEGRATION.md):
+! Drop-in use (sketch):
 !   - biogem_tracercoupling (src/biogem/biogem.f90:1885-2077): pack vocn(n)%mk, the masses,
 !     volumes, reciprocal masses and vbio_part once (gb_bg_upload), the interval's vdocn and
 !     vdbio_part every call (gb_bg_set_increments), then CALL gb_bg_tracercoupling(bgh, goh)
