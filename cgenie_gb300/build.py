@@ -42,7 +42,7 @@ def nvcc() -> str:
 
 def _deps() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(INCLUDE, "gb_goldstein.h"))
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     return files
 
 

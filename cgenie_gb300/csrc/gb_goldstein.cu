@@ -322,8 +322,9 @@ constexpr int kInvNoallocMaxL = 64;
 constexpr int kInvNoallocDoubles = 2 * kInvNoallocBlocks * kInvNoallocMaxL + kInvNoallocMaxL;
 static __device__ __align__(256) double g_inv_noalloc[kInvNoallocDoubles];
 
-// Device address of g_inv_noalloc, looked up once per device (at handle set-up; the first
-// lookup must happen outside stream capture).
+// Device address of g_inv_noalloc, looked up once per device at handle set-up, with that
+// device current.  In host code the name g_inv_noalloc is a host-side stand-in, not a
+// device address: kernels get this pointer.
 static cudaError_t inv_noalloc_scratch(int device, double **out)
 {
     static std::mutex mu;

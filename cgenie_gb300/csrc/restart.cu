@@ -222,10 +222,17 @@ int write_file(const char *path, const uint8_t *img, size_t n)
     return GB_GO_OK;
 }
 
+// The classic format gives a variable's size in 32 bits; only the last fixed-size variable
+// may exceed 4 GiB - 4 bytes (its size field then reads 0xFFFFFFFF).  temp, salinity, uvel and
+// vvel (8 bytes per cell) are followed by the surface fluxes, so like the netCDF library
+// (NC_EVARSIZE) grids of more than 536,870,911 cells are refused.
 int check_dims(int maxi, int maxj, int maxk)
 {
-    if (maxi < 1 || maxj < 1 || maxk < 1 || (long long)maxi * maxj * maxk > (1LL << 31))
+    if (maxi < 1 || maxj < 1 || maxk < 1)
         return rs_fail(GB_GO_EINVAL, "grid size out of range");
+    if ((long long)maxi * maxj * maxk > 536870911LL)
+        return rs_fail(GB_GO_EINVAL, "grid too large for the netCDF classic format: a 3-D variable other than the "
+                                     "last would exceed 4 GiB - 4 bytes");
     return GB_GO_OK;
 }
 

@@ -173,12 +173,16 @@ int  gb_go_inventory(gb_go_handle *h, double *out);
 
 /* gb_go_inventory without any device allocation: the same kernels and result, with their
  * scratch in a static device array of the library (64 x 2 partial sums per tracer and the
- * results, 8256 doubles).  No counterpart in the reference: it serves callers that must
- * not allocate, e.g. inside a CUDA graph capture or under a fixed memory budget.
+ * results, 8256 doubles, held by every device that loads the library until the process
+ * exits).  No counterpart in the reference.  It serves callers that cannot allocate device
+ * memory at this point of their time loop: a host model whose device memory is reserved
+ * up front by a pool it does not control, or one that runs other work on other streams
+ * and cannot afford cudaMalloc/cudaFree, which may synchronise the whole device.
  * - at most 64 tracers: a handle with more returns GB_GO_ERANGE;
  * - the scratch address is looked up once per device when a handle is created
- *   (cudaGetSymbolAddress), so create the first handle on a device before any stream
- *   capture;
+ *   (cudaGetSymbolAddress);
+ * - the call is synchronous: it copies the sums into `out` and waits for the handle's
+ *   stream before it returns;
  * - every scratch entry is written before it is read (nothing needs to start at zero);
  * - the scratch is shared by all handles of a device: calls that overlap in time (other
  *   threads, or handles on different streams) race and must be serialised by the caller. */

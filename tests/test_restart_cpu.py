@@ -192,6 +192,21 @@ def test_reader_errors(rs, tmp_path):
     assert e.value.code == abi.GB_GO_EUNSUPPORTED
 
 
+def test_grid_beyond_classic_format_refused(rs, tmp_path):
+    """A 3-D variable that is not the file's last may not exceed 4 GiB - 4 bytes in the
+    classic format (the netCDF library's NC_EVARSIZE): 536,870,912 cells are refused before
+    any field is touched, 536,870,911 pass the size check."""
+    from cgenie_gb300.goldstein import GoldsteinError
+    p = str(tmp_path / "none.nc")
+    with pytest.raises(GoldsteinError, match="classic format") as e:
+        rs.read_goldstein(p, 1024, 1024, 512 + 1, fields=())
+    assert e.value.code == abi.GB_GO_EINVAL
+    with pytest.raises(GoldsteinError, match="classic format"):
+        rs.read_goldstein(p, 7, 76695845, 1, fields=())   # 536,870,915 cells
+    with pytest.raises(GoldsteinError, match="missing file"):
+        rs.read_goldstein(p, 1, 536870911, 1, fields=())
+
+
 def test_file_name_matches_oracle(rs):
     for y, m, d in [(0, 1, 1.0), (2000, 12, 30.5), (-5, 3, 2.49), (12345, 100, 14.6), (7, 7, 99.4), (7, 7, 99.6),
                     (-2147483647, 1, 1.0)]:
