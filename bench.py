@@ -902,18 +902,18 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def _tracer_err(m, a, b):
-    """Largest per-tracer error max|a - b| / max|b| over the wet interior cells."""
+def _tracer_errs(m, a, b):
+    """Per-tracer error max|a - b| / max|b| over the wet interior cells."""
     import numpy as np
     kk = np.arange(m.maxk + 2)[:, None, None]
     wet = (kk >= m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
     wet[:, 0, :] = wet[:, -1, :] = False
     wet[:, :, 0] = wet[:, :, -1] = False
-    err = 0.0
+    out = []
     for l in range(m.maxl):
         x, y = a[..., l][wet], b[..., l][wet]
-        err = max(err, float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300)))
-    return err
+        out.append(float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300)))
+    return out
 
 
 def run_c3(args, rank, world, local, dist):
@@ -921,14 +921,17 @@ def run_c3(args, rank, world, local, dist):
     import torch
     from cgenie_gb300.ensemble import Ensemble
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
-    from cgenie_gb300.replicas import job_time, job_units, rank_seed
+    from cgenie_gb300.replicas import job_time, job_units, partition
 
     w = dict(WORKLOADS["c3"])
     if args.members:
         w["members"] = args.members
         w["name"] = w["name"].replace("ensemble256", f"ensemble{args.members}")
-    # every rank advances its own members (weak scaling); rank 0 has the workload's seed
-    mems = _ensemble_members(w["members"], rank_seed(w["seed"], rank))
+    # one ensemble of members x ranks, partitioned: rank r advances members r::world (weak
+    # scaling, no collective on the data path); at one rank it is the workload's ensemble
+    from cgenie_gb300 import grid as _g
+    cfgs_all = _g.ensemble_configs(w["members"] * world, seed=w["seed"])
+    mems = [_g.make_member(cfgs_all[i]) for i in partition(len(cfgs_all), rank, world)]
     cu_step = sum(m.wet_cells * m.maxl for m in mems)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -964,15 +967,24 @@ def run_c3(args, rank, world, local, dist):
     value = all_cu_step * args.steps / (total_ms * 1e-3)
     done = args.steps_before + args.warmup + args.steps
 
-    # ---- error against the FP64 path (bit-identical to the FP64 oracle), one member per grid shape
-    err = 0.0
-    for i in range(3):
+    # ---- error against the FP64 path (bit-identical to the FP64 oracle) after at least the
+    # configuration's 1000 steps, per tracer, on a sample of the members (per grid shape the
+    # fewest, the most and a middle tracer count)
+    from cgenie_gb300 import grid as _grid
+    err_steps = max(done, args.err_steps) if args.err_steps > 0 else done
+    if err_steps > done:
+        ens.step(err_steps - done)
+    sample = _grid.error_sample([m.cfg for m in mems]) if args.err_steps > 0 else []
+    per_tracer = [0.0] * max(m.maxl for m in mems)
+    for i in sample:
         out = ens.download(ids[i])
         g = new_member_run(mems[i], device=local, stream=stream.cuda_stream)
-        g.tstepo(done)
+        g.tstepo(err_steps)
         ref = g.download()
         g.close()
-        err = max(err, _tracer_err(mems[i], out["ts"], ref["ts"]))
+        for l, e in enumerate(_tracer_errs(mems[i], out["ts"], ref["ts"])):
+            per_tracer[l] = max(per_tracer[l], e)
+    err = max(per_tracer) if sample else None
     ens.close()
 
     # ---- the plain per-member GPU path (FP64 drop-in, one member at a time), two of each shape
@@ -991,17 +1003,32 @@ def run_c3(args, rank, world, local, dist):
         g.close()
     plain_value = plain_cu / plain_s
 
-    # ---- end to end through the C-ABI: admit from host arrays, step, download every member
+    # ---- end to end through the C-ABI: admit from pinned host arrays, step, download every
+    # member into pinned host arrays (the host buffers exist before the timed region)
+    import dataclasses
+
+    def pinned(a):
+        p = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        p[...] = a
+        return p
+    hmems = [dataclasses.replace(m, ts=pinned(m.ts), u=pinned(m.u)) for m in mems]
+    houts = [dict(ts=pinned(np.zeros_like(m.ts)), rho=pinned(np.zeros_like(m.rho)), cost=pinned(np.zeros_like(m.cost)))
+             for m in mems]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
-    ids2 = e2.add_many(mems)
+    ids2 = e2.add_many(hmems)
+    t1 = time.perf_counter()
     e2.step(args.steps)
-    outs = e2.download_many(ids2)
+    e2.sync()
+    t2 = time.perf_counter()
+    outs = e2.download_many(ids2, out=houts)
     torch.cuda.synchronize()
-    e2e_s = job_time(time.perf_counter() - t0, dist, "cuda")
+    t3 = time.perf_counter()
+    e2e_s = job_time(t3 - t0, dist, "cuda")
+    e2e_parts = {"admit_s": round(t1 - t0, 5), "steps_s": round(t2 - t1, 5), "download_s": round(t3 - t2, 5)}
     e2.close()
     e2e_value = all_cu_step * args.steps / e2e_s
     h2d = sum(m.ts.nbytes + m.u.nbytes for m in mems) / args.steps
@@ -1020,13 +1047,17 @@ def run_c3(args, rank, world, local, dist):
             "config": {"workload": w["name"], "members": w["members"], "seed": w["seed"],
                        "cell_updates_per_step": all_cu_step, "precision": "fp32flux",
                        "l2": "not flushed: the resident states (2 x 0.6 GB) exceed L2",
-                       "cuda_graph": True, "parallelism": f"members sharded over {world} rank(s), no collective",
+                       "cuda_graph": True, "parallelism": f"one ensemble of {w['members'] * world} members partitioned over {world} rank(s) "
+                                      "(members r::N), no collective on the data path",
                        "plain_per_member_gpu": plain_value, "batched_over_plain": value / plain_value,
-                       "max_rel_err_vs_fp64": err, "err_after_steps": done, "err_members": 3},
+                       "max_rel_err_vs_fp64": err, "err_after_steps": err_steps, "err_members": len(sample),
+                       "per_tracer_err": [float(f"{e:.3e}") for e in per_tracer],
+                       "err_note": "per tracer index: max over the sampled members of max|x - x_fp64| / max|x_fp64| "
+                                   "over wet cells, against each member's FP64 run (the reference arithmetic)"},
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
-                    "note": f"whole job through the C-ABI: admit {w['members']} members from host arrays, "
-                            f"{args.steps} steps, download every member"},
+                    "d2h_bytes_per_step": d2h, "parts": e2e_parts,
+                    "note": f"whole job through the C-ABI: admit {w['members']} members from pinned host arrays, "
+                            f"{args.steps} steps, download every member into pinned host arrays"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
@@ -1051,6 +1082,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--err-steps", type=int, default=1000,
+                    help="c3: steps after which the per-tracer error against the FP64 path is taken (0: no error leg)")
     ap.add_argument("--members", type=int, default=0, help="c3: members of the ensemble (default 256)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32flux"], help="single-grid workloads")
     ap.add_argument("--steps-before", type=int, default=0,
@@ -1203,7 +1236,7 @@ def main():
                        "precision": "fp32flux" if args.precision == "fp32flux" else "fp64 plain",
                        "l2": "flushed before every timed step", "parallelism": f"replicas{world}"},
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
+                    "d2h_bytes_per_step": d2h, "parts": e2e_parts,
                     "note": "per step: forcing + u H2D (pinned), step, rho D2H; L2 not flushed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,

@@ -46,6 +46,7 @@ struct Member {
     float *coef = nullptr, *coefl = nullptr, *gtop = nullptr;
     double *rvol = nullptr, *mk = nullptr, *mj = nullptr, *cost = nullptr, *dsj = nullptr;
     int32_t *k1 = nullptr, *scale = nullptr, *icosd = nullptr;
+    float *tref = nullptr;                // per tracer offset of the FP32 transfers
     unsigned int *gmax = nullptr;         // per tracer, scale re-targeting
     unsigned long long *diag = nullptr;   // two slots {dmax bits, limps}
     unsigned int *status = nullptr;
@@ -137,7 +138,7 @@ static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
     // and remainders), forcing, small arrays; patch tables: at most (31 + maxk) words per column
     const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
-           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + 4096;
+           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + (size_t)d->maxl * 4 + 4096;
 }
 
 extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params)
@@ -187,7 +188,7 @@ static void free_member(gb_ens *e, Member *m)
 {
     cudaStream_t s = e->stream;
     void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->coefl, m->gtop, m->mj,
-                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->icosd, m->dsj, m->diag, m->status, m->gmax,
+                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->tref, m->icosd, m->dsj, m->diag, m->status, m->gmax,
                     m->ptab, m->vel, m->ediff1, m->mkd, m->stencil};
     for (void *p : ptrs)
         if (p) cudaFreeAsync(p, s);
@@ -278,7 +279,8 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     const size_t ntop = (size_t)dims->maxl * m->d.NI * m->d.NJ;
     fp32_gtop(m->d, m->p, blob, ts + ntop * (dims->maxk + 1), gtop);
     std::vector<int32_t> scale;
-    fp32_scales(m->d, grid->k1, ts, st.cmax, gtop.data(), scale);
+    std::vector<float> tref;
+    fp32_scales(m->d, grid->k1, ts, st.cmax, st.dmax, gtop.data(), scale, tref);
 
     // device allocation, copies and registration: one member at a time
     std::lock_guard<std::mutex> lk(e->mu);
@@ -303,6 +305,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = dalloc(e, &m->icosd, ncol);
     if (x == cudaSuccess) x = dalloc(e, &m->k1, (size_t)m->d.NI * m->d.NJ);
     if (x == cudaSuccess) x = dalloc(e, &m->scale, scale.size());
+    if (x == cudaSuccess) x = dalloc(e, &m->tref, tref.size());
     if (x == cudaSuccess) x = dalloc(e, &m->dsj, (size_t)dims->maxj + 2);
     if (x == cudaSuccess) x = dalloc(e, &m->gmax, (size_t)dims->maxl);
     if (x == cudaSuccess) x = cudaMemsetAsync(m->gmax, 0, (size_t)dims->maxl * sizeof(unsigned int), s);
@@ -331,6 +334,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     if (x == cudaSuccess) x = cudaMemsetAsync(m->icosd, 0, ncol * 4, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->k1, grid->k1, (size_t)m->d.NI * m->d.NJ * 4, cudaMemcpyHostToDevice, s);
     if (x == cudaSuccess) x = cudaMemcpyAsync(m->scale, scale.data(), scale.size() * 4, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->tref, tref.data(), tref.size() * 4, cudaMemcpyHostToDevice, s);
     const bool need_ediff = params->iediff > 0 && params->iediff < 3;
     if (need_ediff) {
         // the step rebuilds the top-face coefficients from u, ediff1, dza and diffmax
@@ -367,7 +371,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.dsc = m->p.dsc;
     md.buf[0] = m->buf0; md.buf[1] = m->buf1;
     md.ts_static = m->ts_static; md.coef = m->coef; md.coefl = m->coefl; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
-    md.scale = m->scale; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
+    md.scale = m->scale; md.tref = m->tref; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
     md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;

@@ -93,7 +93,9 @@ struct MemberDesc {
                                 // the top-face stencil rebuilt every step by k_stencil_fp32
     double *buf[2];             // state ping-pong, group-planar layout (fp32_plane)
     const double *ts_static;    // uploaded ts (values below k1 for co with ieos=1)
-    const float *coef;          // 8 floats per interior cell: Ae Be An Bn Aa Ba as FP32, 0, 0
+    const float *coef;          // 8 floats per interior cell: Ae Be An Bn Aa Ba as FP32, then Dh Dl: the
+                                // cell's sum of signed face transfer sums (A + B) as an FP32 pair, 0 where
+                                // it is at the rounding level of FP64 (a divergence-free velocity field)
     const float *coefl;         // 8 floats per interior cell: the FP64 remainders of the same (hi+lo
                                 // carries the FP64 coefficient; read by the T-S group only)
     const double *rvol;         // 1/(dphi*ds(j)*dz(k)), index (j-1) + maxj*(k-1)
@@ -103,6 +105,8 @@ struct MemberDesc {
     const int32_t *ptab;        // patch tables (fp32_plan_patches); a work item gives a word offset
     int32_t *scale;             // per tracer power-of-two exponent of the fixed-point transfers; re-targeted
                                 // between steps from gmax so the largest transfer sits near 2^26
+    const float *tref;          // per tracer offset (FP32, 8 significant bits, 0 = none): the FP32 transfers
+                                // carry T - tref, the offset's share enters through Dh Dl
     unsigned int *gmax;         // per tracer: largest |scaled transfer| of the step (FP32 bits)
     const double *mk;           // FP64 k metrics, Fortran-indexed, 6 arrays of maxk+2: dz, rdz, zw, zro, rdza, ssmax
     const double *mj;           // FP64 j metrics, 3 arrays of maxj+2: rc*rdphi, cv(j)*rdsv(j), dt*dphi*ds(j)
@@ -122,6 +126,7 @@ struct Fp32Data {
     double *rvol = nullptr;
     float *gtop = nullptr;
     int32_t *scale = nullptr;
+    float *tref = nullptr;
     unsigned int *gmax = nullptr;
     double *mk = nullptr, *mj = nullptr;
     unsigned int *status = nullptr;
@@ -141,8 +146,10 @@ struct Fp32Data {
     int max_slots = 1;
     long long *step_ctr = nullptr;
     std::vector<int32_t> scale_host;
+    std::vector<float> tref_host;
     std::vector<float> gtop_host_unscaled;
     double cmax = 0.0;          // max over faces of |A|+|B|
+    double dmax = 0.0;          // max over cells of |D| (the divergence pair)
     long long steps = 0;
     long long step_host = 0;
     bool desc_valid = false;
@@ -180,11 +187,15 @@ struct Fp32Static {
     std::vector<double> rvol;
     std::vector<double> mk, mj;
     double cmax = 0.0;
+    double dmax = 0.0;             // max over cells of |D| (coefficient words 6, 7)
 };
 void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const int32_t *k1,
                        const double *u_host, Fp32Static &out);
-void fp32_scales(const Dims &d, const int32_t *k1, const double *ts_host, double cmax, const float *gtop_unscaled,
-                 std::vector<int32_t> &scale);
+// Per tracer: the offset tref (tracers whose wet values lie within a factor of two of each
+// other: DIC, alkalinity; 0 for the others and for T and S) and the fixed-point scale from
+// the largest transfer: 2 cmax max |T - tref|, the forcing, and |tref| dmax.
+void fp32_scales(const Dims &d, const int32_t *k1, const double *ts_host, double cmax, double dmax,
+                 const float *gtop_unscaled, std::vector<int32_t> &scale, std::vector<float> &tref);
 void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top_host,
                std::vector<float> &gtop);
 // Patch plan of one member: the kernel's work items.  Word layout of one patch table:

@@ -129,6 +129,17 @@ __device__ __forceinline__ dflt df_dot2(dflt A, dflt X, dflt B, dflt Y)
     return df_fast(s.hi, ((e1 + e2) + t) + s.lo);
 }
 
+// rint(tr * (dh + dl)) for an FP32 offset tr and an FP32 pair (dh, dl): the product's hi part
+// and its exact remainder (FMA), rounded to an integer in two parts, within 1 of the exact value
+__device__ __forceinline__ int offset_transfer(float tr, float dh, float dl)
+{
+    const float p = __fmul_rn(tr, dh);
+    const float e = __fmaf_rn(tr, dh, -p);
+    const int qi = __float2int_rn(p);
+    const float r = __fadd_rn(__fsub_rn(p, __int2float_rn(qi)), __fadd_rn(e, __fmul_rn(tr, dl)));
+    return qi + __float2int_rn(r);
+}
+
 // FP64 value as a double-float (hi truncated, lo the rest)
 __device__ __forceinline__ dflt df_split(double x)
 {
@@ -227,6 +238,7 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_nki[kMaxK + 2], s_nkr[kMaxK + 2];
     __shared__ int s_scale[kFp32MaxL];
+    __shared__ float s_trs[kFp32MaxL];      // tref * 2^scale per tracer (0: no offset)
     __shared__ unsigned int s_gmax[kFp32MaxL];
     __shared__ int s_it;
     const int t = threadIdx.x;
@@ -275,7 +287,9 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
         const double *mj = md.mj;
         const int mkn = maxk + 2, mjn = maxj + 2;
         for (int l = t; l < L; l += blockDim.x) {
-            s_scale[l] = md.scale[l];
+            const int sc = md.scale[l];
+            s_scale[l] = sc;
+            s_trs[l] = md.tref ? md.tref[l] * __int_as_float((127 + sc) << 23) : 0.0f;
             s_gmax[l] = 0u;
         }
         for (int e = t; e < maxk + 2; e += blockDim.x) {
@@ -356,7 +370,12 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
 #pragma unroll
                     for (int q = 0; q < kGroup; ++q) {
                         if (q >= gl) continue;
-                        const float h = d2f_scaled(xr[q], scl[q]);
+                        float h = d2f_scaled(xr[q], scl[q]);
+                        if (!ts_group) {
+                            // offset tracers: T - tref to FP32 from the leading 24 and the next 24 bits
+                            const float tr = s_trs[g0 + q];
+                            if (tr != 0.0f) h = __fadd_rn(__fsub_rn(h, tr), d2f_lo_scaled(xr[q], scl[q]));
+                        }
                         F[q] = h;
                         if (ts_group && q < 2) slo[(buf * P + t) * 3 + q] = d2f_lo_scaled(xr[q], scl[q]);
                     }
@@ -381,22 +400,35 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     convert_level(k + 1, bk1);
                     if (k + 2 <= maxk) load_level(k + 2);
                 }
+                const bool act = interior && k >= k1c;
+                // coefficients of level k, loaded before the barrier (used after it)
+                const size_t cl = (size_t)cl0 + nij * (size_t)(k - 1);
+                const float *cf = md.coef + 8 * cl;
+                const float *cfl = md.coefl + 8 * cl;
+                const size_t cwi = 8 * ((size_t)cw0 + nij * (size_t)(k - 1));
+                float4 a4 = make_float4(0.f, 0.f, 0.f, 0.f), l4 = a4, a2 = a4;
+                float2 w2 = make_float2(0.f, 0.f), s2 = w2, l2 = w2, lw = w2, ls = w2;
+                double rv = 0.0;
+                auto load_coef = [&]() {
+                    a4 = __ldg(reinterpret_cast<const float4 *>(cf));        // Ae Be An Bn
+                    a2 = __ldg(reinterpret_cast<const float4 *>(cf + 4));    // Aa Ba Dh Dl
+                    w2 = __ldg(reinterpret_cast<const float2 *>(md.coef + cwi));   // Ae Be of the west cell
+                    if (j > 1) s2 = __ldg(reinterpret_cast<const float2 *>(cf - 8 * (size_t)maxi + 2));  // An Bn south
+                    rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
+                    if (ts_group) {
+                        // lo parts of the coefficients (T and S use the FP32 pairs)
+                        l4 = __ldg(reinterpret_cast<const float4 *>(cfl));      // lo Ae Be An Bn
+                        l2 = __ldg(reinterpret_cast<const float2 *>(cfl + 4));  // lo Aa Ba
+                        lw = __ldg(reinterpret_cast<const float2 *>(md.coefl + cwi));
+                        if (j > 1) ls = __ldg(reinterpret_cast<const float2 *>(cfl - 8 * (size_t)maxi + 2));
+                    }
+                };
+                if (act) load_coef();
                 __syncthreads();
                 // ---- interior column wet at k: transfers of level k and the FP64 update
-                if (interior && k >= k1c) {
+                if (act) {
                     const double2 *Rk = reinterpret_cast<const double2 *>(Rg + ((long long)goffs + NIJ * k) * gp);
                     double2 *Wk = reinterpret_cast<double2 *>(Wg + ((long long)goffs + NIJ * k) * gp);
-                    const size_t cl = (size_t)cl0 + nij * (size_t)(k - 1);
-                    const float *cf = md.coef + 8 * cl;
-                    const float *cfl = md.coefl + 8 * cl;
-                    const float4 a4 = __ldg(reinterpret_cast<const float4 *>(cf));        // Ae Be An Bn
-                    const float2 a2 = __ldg(reinterpret_cast<const float2 *>(cf + 4));    // Aa Ba
-                    const size_t cwi = 8 * ((size_t)cw0 + nij * (size_t)(k - 1));
-                    const float *cw = md.coef + cwi;
-                    const float2 w2 = __ldg(reinterpret_cast<const float2 *>(cw));        // Ae Be of the west cell
-                    float2 s2 = make_float2(0.f, 0.f);
-                    if (j > 1) s2 = __ldg(reinterpret_cast<const float2 *>(cf - 8 * (size_t)maxi + 2));  // An Bn south
-                    const double rv = __ldg(md.rvol + (size_t)(j - 1) + (size_t)maxj * (size_t)(k - 1));
                     const bool top = (k == maxk);
                     const float *gt = md.gtop + (size_t)(L + 2) * (size_t)cl0;
                     const float *Fk = slab + bk * P * kGP;
@@ -413,12 +445,6 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                     dflt AeX = {a4.x, 0.f}, BeX = {a4.y, 0.f}, AnX = {a4.z, 0.f}, BnX = {a4.w, 0.f};
                     dflt AwX = {w2.x, 0.f}, BwX = {w2.y, 0.f}, AsX = {s2.x, 0.f}, BsX = {s2.y, 0.f};
                     if (ts_group) {
-                        // lo parts of the coefficients (T and S use the FP32 pairs)
-                        const float4 l4 = __ldg(reinterpret_cast<const float4 *>(cfl));      // lo Ae Be An Bn
-                        const float2 l2 = __ldg(reinterpret_cast<const float2 *>(cfl + 4));  // lo Aa Ba
-                        const float2 lw = __ldg(reinterpret_cast<const float2 *>(md.coefl + cwi));
-                        float2 ls = make_float2(0.f, 0.f);
-                        if (j > 1) ls = __ldg(reinterpret_cast<const float2 *>(cfl - 8 * (size_t)maxi + 2));
                         C1X.lo = l2.x; C0X.lo = l2.y;
                         AeX.lo = l4.x; BeX.lo = l4.y; AnX.lo = l4.z; BnX.lo = l4.w;
                         AwX.lo = lw.x; BwX.lo = lw.y; AsX.lo = ls.x; BsX.lo = ls.y;
@@ -530,9 +556,11 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                             }
                         }
                         if (track) {
-                            // per-tracer maximum for the scale of later steps: one shared atomic
-                            // per warp; also the int32 range check
-                            const float gm = fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga)));
+                            // per-tracer maximum for the scale of later steps (the faces and the
+                            // offset's share tref * D): one shared atomic per warp; also the int32
+                            // range check
+                            const float gm = fmaxf(fmaxf(fmaxf(fabsf(ge), fabsf(gw)), fmaxf(fmaxf(fabsf(gn), fabsf(gs)), fabsf(ga))),
+                                                   a2.z != 0.0f ? fabsf(__fmul_rn(s_trs[g0 + q], a2.z)) : 0.0f);
                             gmax = fmaxf(gmax, gm);
                             const unsigned wmax = __reduce_max_sync(amask, __float_as_uint(gm));
                             if (lane == __ffs(amask) - 1) atomicMax(&s_gmax[g0 + q], wmax);
@@ -540,7 +568,12 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
                         const int qe = __float2int_rn(ge), qw = __float2int_rn(gw);
                         const int qn = __float2int_rn(gn), qs = __float2int_rn(gs);
                         const int qa = __float2int_rn(ga);
-                        const int sum = (qw - qe) + (qs - qn) + (carry[q] - qa);
+                        int sum = (qw - qe) + (qs - qn) + (carry[q] - qa);
+                        if (a2.z != 0.0f) {
+                            // the offset's share tref * D of a cell whose faces do not cancel
+                            const float tr = s_trs[g0 + q];
+                            if (tr != 0.0f) sum += offset_transfer(tr, a2.z, a2.w);
+                        }
                         carry[q] = qa;
                         const double tnew = fma(i2d_scaled(sum, scl[q]), rv, told);
                         hmax = max(hmax, (unsigned)__double2hiint(tnew) & 0x7fffffffu);
@@ -857,11 +890,12 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
 int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).total; }
 
 template <bool ISO, bool TS>
-static void launch_step_instance(const MemberDesc *descs, const int4 *items, int nitems, int P, int smem_bytes,
+static void launch_step_instance(const MemberDesc *descs, const int4 *items, int nitems, int P,
                                  const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap,
                                  int nsm, cudaStream_t s)
 {
     if (nitems <= 0) return;
+    const int smem_bytes = fp32_smem_layout(P).total;
     auto kern = k_step_fp32<ISO, TS>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int per_sm = 0;
@@ -881,7 +915,6 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     }
     const int P = b.max_slots + 1;
-    const int smem_bytes = fp32_smem_layout(P).total;
     // the top-face stencils of the members that rebuild them every step
     if (b.n_stencil > 0)
         k_stencil_fp32<<<dim3(b.stencil_blocks, b.n_stencil), 256, 0, s>>>(b.descs, b.stencil_list, step_ctr, rel);
@@ -893,14 +926,14 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
     }
     cudaStream_t sb = two ? s2 : s;
     if (b.iso) {
-        launch_step_instance<true, true>(b.descs, b.items, b.n_ts, P, smem_bytes, step_ctr, rel, b.work, b.colist,
+        launch_step_instance<true, true>(b.descs, b.items, b.n_ts, P, step_ctr, rel, b.work, b.colist,
                                          b.cocount, b.cocap, nsm, s);
-        launch_step_instance<true, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, smem_bytes, step_ctr, rel, b.work + 2,
+        launch_step_instance<true, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel, b.work + 2,
                                           b.colist, b.cocount, b.cocap, nsm, sb);
     } else {
-        launch_step_instance<false, true>(b.descs, b.items, b.n_ts, P, smem_bytes, step_ctr, rel, b.work, b.colist,
+        launch_step_instance<false, true>(b.descs, b.items, b.n_ts, P, step_ctr, rel, b.work, b.colist,
                                           b.cocount, b.cocap, nsm, s);
-        launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, smem_bytes, step_ctr, rel,
+        launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel,
                                            b.work + 2, b.colist, b.cocount, b.cocap, nsm, sb);
     }
     if (two) {
@@ -1132,6 +1165,34 @@ int fp32_plan_patches(const Dims &d, const int32_t *k1, int tile_i, int tile_j, 
 // ---------------------------------------------------------------------------
 // host-side static data
 
+// The cell's sum of signed face transfer sums D = (Cw - Ce) + (Cs - Cn) + (Cb - Ca), C = A + B of a
+// face, in FP64 from the FP32 pairs (coefficient + remainder) of the cell and of its west, south
+// and lower neighbours, as an FP32 pair (dh, dl); zero where |D| is within 2^-40 of the faces'
+// magnitudes (a divergence-free velocity field leaves only FP64 rounding there).  A uniform
+// offset tref then gains tref * D per step, the share of the offset the transfers of T - tref
+// leave out.  Host and device evaluate the same expressions (additions only).
+__host__ __device__ inline void fp32_div_pair(const float *ch, const float *cl, int maxi, size_t nij, size_t c,
+                                              size_t cw, bool south, bool below, float *dh, float *dl)
+{
+    auto C = [&](size_t cell, int f) {
+        return ((double)ch[8 * cell + 2 * f] + (double)cl[8 * cell + 2 * f]) +
+               ((double)ch[8 * cell + 2 * f + 1] + (double)cl[8 * cell + 2 * f + 1]);
+    };
+    const double ce = C(c, 0), cn = C(c, 1), ca = C(c, 2), cwe = C(cw, 0);
+    const double cs = south ? C(c - (size_t)maxi, 1) : 0.0;
+    const double cb = below ? C(c - nij, 2) : 0.0;
+    const double D = ((cwe - ce) + (cs - cn)) + (cb - ca);
+    const double S = ((fabs(cwe) + fabs(ce)) + (fabs(cs) + fabs(cn))) + (fabs(cb) + fabs(ca));
+    if (!(fabs(D) > 0x1p-40 * S)) {
+        *dh = 0.0f;
+        *dl = 0.0f;
+        return;
+    }
+    const float h = (float)D;
+    *dh = h;
+    *dl = (float)(D - (double)h);
+}
+
 void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const int32_t *k1,
                        const double *u, Fp32Static &out)
 {
@@ -1148,6 +1209,7 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     out.coefl.assign(8 * ncell, 0.0f);
     out.rvol.assign((size_t)maxj * maxk, 0.0);
     out.cmax = 0.0;
+    out.dmax = 0.0;
     auto U = [&](int c, int i, int j, int k) -> double {
         return u[(size_t)c + 3 * ((size_t)i + (size_t)(maxi + 1) * ((size_t)j + (size_t)(maxj + 1) * (size_t)(k - 1)))];
     };
@@ -1199,6 +1261,18 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
             }
         }
     }
+    // words 6, 7: the cell's divergence pair (fp32_div_pair)
+    const size_t nij = (size_t)maxi * maxj;
+    for (int k = 1; k <= maxk; ++k)
+        for (int j = 1; j <= maxj; ++j)
+            for (int i = 1; i <= maxi; ++i) {
+                const size_t c = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1));
+                const int iw = i == 1 ? maxi : i - 1;
+                const size_t cw = (size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1));
+                fp32_div_pair(out.coef.data(), out.coefl.data(), maxi, nij, c, cw, j > 1, k > 1, &out.coef[8 * c + 6],
+                              &out.coef[8 * c + 7]);
+                out.dmax = std::max(out.dmax, std::fabs((double)out.coef[8 * c + 6]) + std::fabs((double)out.coef[8 * c + 7]));
+            }
     out.mk.assign(6 * (size_t)nk, 0.0);
     for (int k = 0; k <= maxk + 1; ++k) {
         out.mk[k] = dz[k];
@@ -1274,6 +1348,24 @@ __global__ void k_build_coef(const double *__restrict__ u, Metrics m, Dims d, Ph
     }
 }
 
+// Words 6, 7 of the coefficients (the divergence pair) after k_build_coef, as the host builds them.
+__global__ void k_build_div(Dims d, float *coef, const float *coefl)
+{
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk;
+    const size_t nij = (size_t)maxi * maxj, ncell = nij * maxk;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % maxi) + 1;
+        const int j = (int)((c / maxi) % maxj) + 1;
+        const int k = (int)(c / nij) + 1;
+        const int iw = i == 1 ? maxi : i - 1;
+        const size_t cw = (size_t)(iw - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1));
+        float dh, dl;
+        fp32_div_pair(coef, coefl, maxi, nij, c, cw, j > 1, k > 1, &dh, &dl);
+        coef[8 * c + 6] = dh;
+        coef[8 * c + 7] = dl;
+    }
+}
+
 void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top,
                std::vector<float> &gtop)
 {
@@ -1295,18 +1387,39 @@ void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &bl
         }
 }
 
-void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax, const float *gtop,
-                 std::vector<int32_t> &scale)
+void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax, double dmax, const float *gtop,
+                 std::vector<int32_t> &scale, std::vector<float> &tref)
 {
     const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, L = d.L, NI = d.NI, NJ = d.NJ;
-    std::vector<double> tmax(L, 0.0), gmax(L, 0.0);
-    for (int k = 1; k <= maxk; ++k)
-        for (int j = 1; j <= maxj; ++j)
-            for (int i = 1; i <= maxi; ++i) {
-                if (k < k1[i + (size_t)NI * j]) continue;
-                const double *p = ts + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k));
-                for (int l = 0; l < L; ++l) tmax[l] = std::max(tmax[l], std::fabs(p[l]));
-            }
+    std::vector<double> tmax(L, 0.0), gmax(L, 0.0), vlo(L, HUGE_VAL), vhi(L, -HUGE_VAL);
+    auto each_wet = [&](auto &&fn) {
+        for (int k = 1; k <= maxk; ++k)
+            for (int j = 1; j <= maxj; ++j)
+                for (int i = 1; i <= maxi; ++i) {
+                    if (k < k1[i + (size_t)NI * j]) continue;
+                    fn(ts + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k)));
+                }
+    };
+    each_wet([&](const double *p) {
+        for (int l = 0; l < L; ++l) {
+            vlo[l] = std::min(vlo[l], p[l]);
+            vhi[l] = std::max(vhi[l], p[l]);
+        }
+    });
+    // offset: the mid-range, rounded to 8 significant bits, for tracers (other than T and S)
+    // whose wet values stay within a factor of two of each other; the transfers then carry
+    // T - tref, whose FP32 rounding is smaller than T's by about max|T| / max|T - tref|
+    tref.assign(L, 0.0f);
+    for (int l = 2; l < L; ++l) {
+        const double lo = vlo[l], hi = vhi[l];
+        if (!((lo > 0.0 && lo > 0.5 * hi) || (hi < 0.0 && hi < 0.5 * lo))) continue;
+        int ex = 0;
+        const double f = std::frexp(0.5 * (lo + hi), &ex);
+        tref[l] = (float)std::ldexp(std::nearbyint(f * 256.0), ex - 8);
+    }
+    each_wet([&](const double *p) {
+        for (int l = 0; l < L; ++l) tmax[l] = std::max(tmax[l], std::fabs(p[l] - (double)tref[l]));
+    });
     if (gtop)
         for (size_t n = 0; n < (size_t)maxi * maxj; ++n)
             for (int l = 0; l < L; ++l) gmax[l] = std::max(gmax[l], (double)std::fabs(gtop[n * (L + 2) + l]));
@@ -1316,7 +1429,7 @@ void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax
         // isoneutral stencil and growth of max|T| are covered by 2^4 headroom
         // below the int32 range (2^26 target); a transfer above 3e8 (the sum of six
         // stays inside int32) sets the member's range flag
-        const double g = std::max(2.0 * cmax * tmax[l], gmax[l]);
+        const double g = std::max(std::max(2.0 * cmax * tmax[l], gmax[l]), std::fabs((double)tref[l]) * dmax);
         int s = 0;
         if (g > 0.0 && std::isfinite(g)) s = (int)std::floor(std::log2(67108864.0 / g));
         scale[l] = std::max(-120, std::min(120, s));
@@ -1485,6 +1598,8 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMalloc(&D.rvol, (size_t)d.maxj * d.maxk * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.gtop, (size_t)(d.L + 2) * d.maxi * d.maxj * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.scale, (size_t)d.L * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&D.tref, (size_t)d.L * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(D.tref, 0, (size_t)d.L * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&D.gmax, (size_t)d.L * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(D.gmax, 0, (size_t)d.L * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&D.mk, 6 * (size_t)nk * sizeof(double));
@@ -1543,7 +1658,7 @@ void fp32_member_free(Fp32Member *f)
     if (!f || !f->impl) return;
     Fp32Host *h = host_of(f);
     Fp32Data &D = h->data;
-    cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
+    cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.tref); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
     cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.stencil); cudaFree(D.stencil_list);
     if (D.s2) cudaStreamDestroy(D.s2);
@@ -1558,9 +1673,14 @@ static int upload_scales(Fp32Host *h, cudaStream_t s)
 {
     if (!h->have_state || !h->have_vel) return 0;
     std::vector<int32_t> sc;
-    fp32_scales(h->d, h->k1.data(), h->ts1_host.data(), h->data.cmax, h->data.gtop_host_unscaled.data(), sc);
+    std::vector<float> tr;
+    fp32_scales(h->d, h->k1.data(), h->ts1_host.data(), h->data.cmax, h->data.dmax, h->data.gtop_host_unscaled.data(),
+                sc, tr);
     h->data.scale_host = sc;
+    h->data.tref_host = tr;
     return cuda_ok(cudaMemcpyAsync(h->data.scale, h->data.scale_host.data(), sc.size() * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, s)) ||
+           cuda_ok(cudaMemcpyAsync(h->data.tref, h->data.tref_host.data(), tr.size() * sizeof(float),
                                    cudaMemcpyHostToDevice, s)) ||
            cuda_ok(cudaStreamSynchronize(s));
 }
@@ -1614,13 +1734,15 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, const double *
         const size_t ncell = (size_t)h->d.maxi * h->d.maxj * h->d.maxk;
         const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 8192);
         k_build_coef<<<std::max(1, blocks), 256, 0, s>>>(u_dev, m, h->d, h->p, D.coef, D.coefl);
-        count_launches(1);
+        k_build_div<<<std::max(1, blocks), 256, 0, s>>>(h->d, D.coef, D.coefl);
+        count_launches(2);
         return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
     }
     Fp32Static st;
     fp32_build_static(h->d, h->p, h->blob, h->k1.data(), u_host, st);
     Fp32Data &D = h->data;
     D.cmax = st.cmax;
+    D.dmax = st.dmax;
     cudaError_t e = cudaMemcpyAsync(D.coef, st.coef.data(), st.coef.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(D.coefl, st.coefl.data(), st.coefl.size() * sizeof(float), cudaMemcpyHostToDevice, s);
@@ -1657,7 +1779,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.buf[0] = D.plan_buf[0];
         md.buf[1] = D.plan_buf[1];
         md.ts_static = ts_static;
-        md.coef = D.coef; md.coefl = D.coefl; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.gmax = D.gmax;
+        md.coef = D.coef; md.coefl = D.coefl; md.rvol = D.rvol; md.gtop = D.gtop; md.k1 = h->k1_dev; md.scale = D.scale; md.tref = D.tref; md.gmax = D.gmax;
         md.mk = D.mk; md.mj = D.mj; md.cost = cost; md.icosd = icosd;
         md.ptab = D.ptab;
         md.status = D.status;

@@ -137,9 +137,11 @@ class Ensemble:
         self._check(self.lib.gb_ens_download(self.e, int(mid), dptr(ts), dptr(rho), dptr(cost)), "gb_ens_download")
         return dict(ts=ts, rho=rho, cost=cost)
 
-    def download_many(self, mids, threads: int = 8) -> list:
+    def download_many(self, mids, threads: int = 8, out=None) -> list:
         """download() of several members from host threads, each with its own CUDA stream
-        (gb_ens_download_stream), so that the device-to-host copies overlap."""
+        (gb_ens_download_stream), so that the device-to-host copies overlap.  `out`: one dict
+        of ts, rho and cost arrays per member to write into (e.g. pinned host memory, which
+        the copies reach without staging); new arrays otherwise."""
         import queue
         from concurrent.futures import ThreadPoolExecutor
         import torch
@@ -148,10 +150,17 @@ class Ensemble:
         free = queue.Queue()
         for _ in range(threads):
             free.put(torch.cuda.Stream(device=dev))
+        dst = dict(zip(mids, out)) if out is not None else {}
 
         def one(mid):
             m = self.members[mid]
-            ts, rho, cost = np.empty_like(m.ts), np.empty_like(m.rho), np.empty_like(m.cost)
+            if mid in dst:
+                ts, rho, cost = dst[mid]["ts"], dst[mid]["rho"], dst[mid]["cost"]
+                for a, ref in ((ts, m.ts), (rho, m.rho), (cost, m.cost)):
+                    if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                        raise ValueError("download_many: output arrays must match the member's shapes (float64, C order)")
+            else:
+                ts, rho, cost = np.empty_like(m.ts), np.empty_like(m.rho), np.empty_like(m.cost)
             st = free.get()
             try:
                 self._check(self.lib.gb_ens_download_stream(self.e, int(mid), C.c_void_p(st.cuda_stream), dptr(ts),

@@ -81,7 +81,9 @@ class MemberConfig:
     mask: str = "noise"          # "noise": seeded land fraction; "basin" / "basin_island": one
                                  # continent joined to the north boundary, an open channel in
                                  # rows 1-2 (the southern boundary is an island) and, for
-                                 # "basin_island", one rectangular island (momentum tests)
+                                 # "basin_island", one rectangular island (momentum tests);
+                                 # "file": the .k1 bathymetry at mask_file (read_k1)
+    mask_file: str = ""          # mask = "file": path without extension of .k1 (.psiles, .paths)
 
 
 @dataclasses.dataclass
@@ -280,6 +282,57 @@ def make_k1(rng, maxi, maxj, maxk, land_frac, land_code):
     return k1
 
 
+def read_k1(path: str, maxi: int, maxj: int) -> np.ndarray:
+    """A .k1 bathymetry file as initialise_goldstein reads it (goldstein.f90:1107-1123):
+    rows j = maxj+1 .. 0 of k1(0:maxi+1, j), list-directed; then k1(0,j) = k1(maxi,j) and
+    k1(maxi+1,j) = k1(1,j).  Returns k1[j, i], (maxj+2, maxi+2), int32."""
+    vals = np.array(open(path).read().split(), dtype=np.int64)
+    n = (maxj + 2) * (maxi + 2)
+    if vals.size < n:
+        raise ValueError(f"{path}: {vals.size} values, {n} expected")
+    k1 = np.zeros((maxj + 2, maxi + 2), np.int32)
+    for r, j in enumerate(range(maxj + 1, -1, -1)):
+        k1[j, :] = vals[r * (maxi + 2):(r + 1) * (maxi + 2)]
+        k1[j, 0] = k1[j, maxi]
+        k1[j, maxi + 1] = k1[j, 1]
+    return k1
+
+
+def read_psiles(path: str, maxi: int, maxj: int) -> np.ndarray:
+    """A .psiles file (goldstein.f90:1502-1518): rows j = maxj .. 0 of the psi-point landmass
+    labels, i = 1..maxi; returned as the reference's gbold(i + j*maxi), flat index
+    (i - 1) + j*maxi, float64.  isles = its maximum - 1."""
+    vals = np.array(open(path).read().split(), dtype=np.float64)
+    n = (maxj + 1) * maxi
+    if vals.size < n:
+        raise ValueError(f"{path}: {vals.size} values, {n} expected")
+    out = np.zeros(n)
+    for r, j in enumerate(range(maxj, -1, -1)):
+        out[j * maxi:(j + 1) * maxi] = vals[r * maxi:(r + 1) * maxi]
+    return out
+
+
+def read_paths(path: str, isles: int):
+    """A .paths file (goldstein.f90:1541-1573): npi(1:isles), then per island one skipped
+    record and npi(i) records (lpisl, ipisl, jpisl).  Returns (npi, [[(l, i, j), ...], ...])."""
+    lines = open(path).read().split("\n")
+    tok, r = [], 0
+    while len(tok) < isles:
+        tok += lines[r].split()
+        r += 1
+    npi = [int(x) for x in tok[:isles]]
+    paths = []
+    for n in npi:
+        r += 1                       # the record each island's path starts after
+        p = []
+        for _ in range(n):
+            a = lines[r].split()
+            p.append((int(a[0]), int(a[1]), int(a[2])))
+            r += 1
+        paths.append(p)
+    return np.array(npi, np.int32), paths
+
+
 def basin_island_cells(maxi, maxj):
     """(continent i-range, continent first row, island i-range, island j-range), 1-based
     inclusive, of make_k1_basin's layout."""
@@ -435,6 +488,8 @@ def make_member(cfg: MemberConfig) -> Member:
     vg = vertical_grid(maxk)
     if cfg.mask == "noise":
         k1 = make_k1(rng, maxi, maxj, maxk, cfg.land_frac, cfg.land_code)
+    elif cfg.mask == "file":
+        k1 = read_k1(cfg.mask_file + ".k1", maxi, maxj)
     else:
         k1 = make_k1_basin(rng, maxi, maxj, maxk, cfg.land_code, island=cfg.mask == "basin_island")
     u = make_velocity(rng, maxi, maxj, maxk, k1, hg, vg, cfg.umax)
@@ -534,3 +589,21 @@ def ensemble_configs(n: int = 256, seed: int = 3, lmin: int = 2, lmax: int = 24)
             diff_v=float(math.exp(rng.uniform(math.log(1e-6), math.log(1e-4)))),
             diso=False, tracer_kind="bgc"))
     return out
+
+
+def error_sample(cfgs, per_shape: int = 3):
+    """Indices of members that a long error check runs: for every grid shape of the list,
+    the members with the fewest and the most tracers and one in between (tracer counts
+    of the mixed ensemble span 2-24, so the sample holds both ends)."""
+    by_shape = {}
+    for n, c in enumerate(cfgs):
+        by_shape.setdefault((c.maxi, c.maxj, c.maxk), []).append(n)
+    out = []
+    for shape in sorted(by_shape):
+        idx = sorted(by_shape[shape], key=lambda n: (cfgs[n].maxl, n))
+        pick = [idx[0], idx[-1], idx[len(idx) // 2]][:per_shape]
+        for n in pick:
+            if n not in out:
+                out.append(n)
+    return out
+

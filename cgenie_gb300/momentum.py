@@ -112,8 +112,9 @@ def _labels(dry, maxi, maxj):
 
 def make_case(member, seed: int = 0, rel: float = 0.9, adrag_days: float = 2.5) -> MomentumCase:
     m = member
-    if m.cfg.mask not in ("basin", "basin_island"):
-        raise ValueError("momentum cases need a basin mask (MemberConfig(mask='basin' or 'basin_island'))")
+    if m.cfg.mask not in ("basin", "basin_island", "file"):
+        raise ValueError("momentum cases need a basin mask (MemberConfig(mask='basin' or 'basin_island')) "
+                         "or a mask file with its .psiles and .paths")
     rng = np.random.default_rng(seed)
     maxi, maxj, maxk = m.maxi, m.maxj, m.maxk
     hg = grid.horizontal_grid(maxi, maxj)
@@ -186,6 +187,15 @@ def make_case(member, seed: int = 0, rel: float = 0.9, adrag_days: float = 2.5) 
         for i in range(1, maxi + 1):
             getj[i, j] = int(max(k1[i, j], k1[i + 1, j], k1[i, j + 1], k1[i + 1, j + 1]) <= maxk and
                              (k1[i, j] != k1[i, j + 1] or k1[i, j] != k1[i + 1, j] or k1[i, j] != k1[i + 1, j + 1]))
+    if m.cfg.mask == "file":
+        psiles = grid.read_psiles(m.cfg.mask_file + ".psiles", maxi, maxj)
+        isles = int(psiles.max()) - 1
+        npi, paths = grid.read_paths(m.cfg.mask_file + ".paths", isles) if isles > 0 else (np.zeros(0, np.int32), [])
+        for p in paths:
+            for (l_, i_, j_) in p:
+                if abs(l_) not in (1, 2) or not (0 <= i_ <= maxi) or not (0 <= j_ <= maxj) or k1[i_, j_] > maxk:
+                    raise ValueError(f"bad path point {(l_, i_, j_)}")
+        return _case_from(m, rng, hg, dz, k1, ku, mk, getj, rh, drag, rtv, rtv3, psiles, isles, paths, rel)
     # psi-point landmasses (a .psiles file) and the island paths (a .paths file)
     dry = np.zeros((maxj + 1, maxi), bool)
     for j in range(maxj + 1):
@@ -197,7 +207,6 @@ def make_case(member, seed: int = 0, rel: float = 0.9, adrag_days: float = 2.5) 
     if isles != expect:
         raise ValueError(f"unexpected landmasses: {isles + 1}")
     psiles = lab.astype(np.float64).reshape(-1)   # index i + j*maxi - 1
-    mpi = 2 * (maxi + maxj)
     paths = [[(1, i, 1) for i in range(1, maxi + 1)]]   # the southern boundary: eastward along row 1
     if isles == 2:
         (_, _), _, (b0, b1), (c0, c1) = grid.basin_island_cells(maxi, maxj)
@@ -205,6 +214,12 @@ def make_case(member, seed: int = 0, rel: float = 0.9, adrag_days: float = 2.5) 
         p = [(1, i, cc) for i in range(a, b)] + [(2, b, j) for j in range(cc, d)]
         p += [(-1, i, d) for i in range(b - 1, a - 1, -1)] + [(-2, a, j) for j in range(d - 1, cc - 1, -1)]
         paths.append(p)
+    return _case_from(m, rng, hg, dz, k1, ku, mk, getj, rh, drag, rtv, rtv3, psiles, isles, paths, rel)
+
+
+def _case_from(m, rng, hg, dz, k1, ku, mk, getj, rh, drag, rtv, rtv3, psiles, isles, paths, rel):
+    maxi, maxj, maxk = m.maxi, m.maxj, m.maxk
+    mpi = max([2 * (maxi + maxj)] + [len(p) for p in paths])
     npi = np.array([len(p) for p in paths], np.int32)
     lp = np.zeros((isles, mpi), np.int32)
     ip = np.zeros((isles, mpi), np.int32)

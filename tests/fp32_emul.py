@@ -7,6 +7,10 @@ It follows the arithmetic of k_step_fp32 without the isoneutral branch:
 - other tracers are truncated to FP32 after scaling by 2^s_l, each face
   transfer is evaluated as an FMA of the FP32 coefficients and rounded to int32
   (half to even), and the FP64 state gets T += sum(q) * 2^-s_l / V;
+- a tracer whose wet values stay within a factor of two of each other carries an
+  offset tref (the mid-range to 8 significant bits): its FP32 value is
+  (trunc(T 2^s) - tref 2^s) + trunc(the next 24 bits), and a cell whose signed face
+  sums (A + B) do not cancel (D, an FP32 pair) gains rint(tref 2^s * D);
 - after every 4th step (steps 0, 4, 8, ... since upload) s_l moves so that
   that step's largest |scaled transfer| of a wet cell would have landed in
   [2^25, 2^26);
@@ -80,21 +84,71 @@ def coefficients(m):
     return c32, lo, cmax
 
 
-def scales(m, ts, cmax):
-    k1 = m.k1
+def wet_cells(m):
     kk = np.arange(m.maxk + 2)[:, None, None]
-    wet = (kk >= k1[None]) & (kk >= 1) & (kk <= m.maxk)
+    wet = (kk >= m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
     wet[:, 0] = False
     wet[:, -1] = False
     wet[:, :, 0] = False
     wet[:, :, -1] = False
+    return wet
+
+
+def offsets(m, ts):
+    """Per tracer offset tref (float32): the mid-range to 8 significant bits for tracers
+    (other than T and S) whose wet values stay within a factor of two of each other."""
+    wet = wet_cells(m)
+    tref = np.zeros(m.maxl, dtype=np.float32)
+    for l in range(2, m.maxl):
+        v = ts[..., l][wet]
+        lo, hi = float(v.min()), float(v.max())
+        if (lo > 0.0 and lo > 0.5 * hi) or (hi < 0.0 and hi < 0.5 * lo):
+            f, ex = np.frexp(0.5 * (lo + hi))
+            tref[l] = np.float32(np.ldexp(np.rint(f * 256.0), int(ex) - 8))
+    return tref
+
+
+def scales(m, ts, cmax, tref=None, dmax=0.0):
+    wet = wet_cells(m)
     out = []
     for l in range(m.maxl):
-        tmax = np.max(np.abs(ts[..., l][wet])) if wet.any() else 0.0
-        g = 2.0 * cmax * tmax
+        off = 0.0 if tref is None else float(tref[l])
+        tmax = np.max(np.abs(ts[..., l][wet] - off)) if wet.any() else 0.0
+        g = max(2.0 * cmax * tmax, abs(off) * dmax)
         s = int(math.floor(math.log2(67108864.0 / g))) if g > 0 else 0
         out.append(max(-120, min(120, s)))
     return out
+
+
+def divergence_pair(m, c32, lo):
+    """Per interior cell the FP32 pair (dh, dl) of D = (Cw - Ce) + (Cs - Cn) + (Cb - Ca),
+    C = A + B of a face from the coefficient pairs; zero where |D| <= 2^-40 * sum |C|."""
+    maxi = m.maxi
+    h = c32.astype(np.float64)
+    r = lo.astype(np.float64)
+    C = [(h[..., 2 * f] + r[..., 2 * f]) + (h[..., 2 * f + 1] + r[..., 2 * f + 1]) for f in range(3)]
+    im = np.r_[maxi, np.arange(1, maxi)] - 1
+    cwe = C[0][:, :, im]
+    cs = np.zeros_like(C[1])
+    cs[:, 1:] = C[1][:, :-1]
+    cb = np.zeros_like(C[2])
+    cb[1:] = C[2][:-1]
+    D = ((cwe - C[0]) + (cs - C[1])) + (cb - C[2])
+    S = ((np.abs(cwe) + np.abs(C[0])) + (np.abs(cs) + np.abs(C[1]))) + (np.abs(cb) + np.abs(C[2]))
+    keep = np.abs(D) > 2.0 ** -40 * S
+    dh = np.where(keep, D, 0.0).astype(np.float32)
+    dl = np.where(keep, D - dh.astype(np.float64), 0.0).astype(np.float32)
+    return dh, dl
+
+
+def offset_transfer(tr, dh, dl):
+    """rint(tr * (dh + dl)) as the kernel forms it (float32 arrays)."""
+    f32 = np.float32
+    p = (tr * dh).astype(f32)
+    e = (tr.astype(np.float64) * dh.astype(np.float64) - p.astype(np.float64)).astype(f32)
+    qi = np.rint(p.astype(np.float64))
+    r = ((p - qi.astype(f32)).astype(f32) + (e + (tr * dl).astype(f32)).astype(f32)).astype(f32)
+    return (qi + np.rint(r.astype(np.float64))).astype(np.int64)
 
 
 class Fp32Emulator:
@@ -106,7 +160,10 @@ class Fp32Emulator:
         self.icosd = np.zeros_like(m.icosd)
         self.c, self.clo, self.cmax = coefficients(m)
         self.cd = self.c.astype(np.float64) + self.clo.astype(np.float64)
-        self.s = scales(m, m.ts, self.cmax)
+        self.tref = offsets(m, m.ts)
+        self.dh, self.dl = divergence_pair(m, self.c, self.clo)
+        dmax = float(np.max(np.abs(self.dh.astype(np.float64)) + np.abs(self.dl.astype(np.float64))))
+        self.s = scales(m, m.ts, self.cmax, self.tref, dmax)
         self.oracle = oracle_mod
         self.refs = GridRefs(m)
         rv = np.zeros((m.maxk, m.maxj))
@@ -152,7 +209,12 @@ class Fp32Emulator:
                         upd = Tc + sm * self.rv[k - 1][:, None]
                         new[k, 1:-1, 1:-1, l] = np.where(wet, upd, Tc)
                     continue
-                T = trunc32(self.ts[..., l] * sc)          # (maxk+2, maxj+2, maxi+2)
+                xs = self.ts[..., l] * sc
+                T = trunc32(xs)                            # (maxk+2, maxj+2, maxi+2)
+                trs = np.float32(float(self.tref[l]) * sc)
+                if trs != 0:
+                    lo = trunc32(xs - T.astype(np.float64))
+                    T = ((T - trs).astype(np.float32) + lo).astype(np.float32)
                 qa_prev = np.zeros((maxj, maxi), dtype=np.int64)
                 gmax = np.float32(0.0)
                 for k in range(1, maxk + 1):
@@ -179,6 +241,12 @@ class Fp32Emulator:
                     sm = (q[1] - q[0]) + (q[3] - q[2]) + (qa_prev - q[4])
                     qa_prev = q[4]
                     wet = k >= m.k1[1:-1, 1:-1]
+                    dh, dl = self.dh[k - 1], self.dl[k - 1]
+                    if trs != 0 and np.any(dh != 0):
+                        qd = offset_transfer(np.full(dh.shape, trs, dtype=np.float32), dh, dl)
+                        sm = sm + np.where(dh != 0, qd, 0)
+                        if wet.any():
+                            gmax = max(gmax, np.abs((trs * dh).astype(np.float32))[wet].max())
                     if wet.any():
                         gm = np.max([np.abs(g)[wet].max() for g in (ge, gw, gn, gs, ga)])
                         gmax = max(gmax, gm)
