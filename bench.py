@@ -328,6 +328,8 @@ def run_bg(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = bg_cpu_rate(m, st)
             line["cpu_baseline"] = {"value": v, "unit": "tracer cell-couplings/s", "cores": 1, "kind": "port",
@@ -433,6 +435,8 @@ def run_ea(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = ea_cpu_rate(case)
             line["cpu_baseline"] = {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
@@ -540,6 +544,8 @@ def run_mo(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = mo_cpu_rate(m, case)
             line["cpu_baseline"] = {"value": v, "unit": "wet-cell momentum updates/s", "cores": 1, "kind": "port",
@@ -666,6 +672,8 @@ def run_rs(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = rs_cpu_rate(m, target_s=10.0)
             line["cpu_baseline"] = {"value": v, "unit": "ocean cells written/s", "cores": 1, "kind": "port",
@@ -738,6 +746,8 @@ def run_ocean(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n, _ = ocean_cpu_rate(w, 20)
             line["cpu_baseline"] = {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
@@ -1034,6 +1044,24 @@ def run_c3(args, rank, world, local, dist):
     h2d = sum(m.ts.nbytes + m.u.nbytes for m in mems) / args.steps
     d2h = sum(o["ts"].nbytes + o["rho"].nbytes + o["cost"].nbytes for o in outs) / args.steps
 
+    # ---- serving (the serving configuration at a bounded request count): Poisson arrivals at
+    # 50 runs/s of 200-5000-step members of the three grids, admitted by free HBM, continuously
+    # batched; p50/p99 run latency and tracer cell-updates per second of wall time
+    serving = None
+    if args.serving_requests > 0 and rank == 0:
+        from cgenie_gb300.serving import Server, poisson_requests
+        reqs = poisson_requests(args.serving_requests, rate=50.0, seed=7)
+        srv = Server(chunk=25, device=local)
+        st = srv.run(reqs)
+        srv.close()
+        serving = {"requests": st["requests"], "arrival_rate_per_s": 50.0, "steps_range": [200, 5000],
+                   "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
+                   "cell_updates_per_s": st["cell_updates_per_s"], "wall_s": st["wall_s"],
+                   "gpu_busy_over_wall": st["busy_s"] / st["wall_s"] if st["wall_s"] > 0 else None,
+                   "max_active": st["max_active"],
+                   "note": "wall time is set by the arrivals (the last arrives at ~requests/rate s); "
+                           "busy = time in the batched steps"}
+
     peak, peak_kind = measured_peaks()
     alg = sum(algorithmic_bytes(m) for m in mems)
     achieved = alg / (total_ms * 1e-3 / args.steps) / 1e9
@@ -1066,6 +1094,8 @@ def run_c3(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             cpu, cores, _ = oracle_pool_rate(w["members"], w["seed"], 1, 12, faithful=True)
             line["cpu_baseline"] = {"value": cpu, "unit": "tracer cell-updates/s", "cores": cores, "kind": "port",
@@ -1082,6 +1112,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=1000,
+                    help="c3: requests of the serving leg (Poisson, 50/s; 0: no serving leg)")
     ap.add_argument("--err-steps", type=int, default=1000,
                     help="c3: steps after which the per-tracer error against the FP64 path is taken (0: no error leg)")
     ap.add_argument("--members", type=int, default=0, help="c3: members of the ensemble (default 256)")
@@ -1247,6 +1279,8 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if serving is not None:
+            line["serving"] = serving
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(m)
         print(json.dumps(line))

@@ -10,6 +10,7 @@
 // holds (member, column tile) items ordered by decreasing cost (longest
 // processing time first); persistent CTAs take items round-robin.
 #include "gb_fp32.h"
+#include "co_column.cuh"
 #include "gb_internal.h"
 #include "../../include/gb_goldstein.h"
 
@@ -22,11 +23,15 @@
 #include <mutex>
 #include <string>
 #include <vector>
+#include <thread>
+#include <atomic>
+#include <unordered_map>
 
 namespace gbgo {
 int validate_config(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid, std::string &msg);
 void build_metric_blob(const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *g, std::vector<double> &blob);
 PhysParams phys_from(const gb_go_params *pp, const gb_go_grid *g);
+Metrics metrics_from_blob(const double *b, const int32_t *k1, const double *ediff1, int maxj, int maxk);
 }  // namespace gbgo
 
 using namespace gbgo;
@@ -53,11 +58,14 @@ struct Member {
     int32_t *ptab = nullptr;              // patch tables
     double *vel = nullptr, *ediff1 = nullptr, *mkd = nullptr;   // iediff: u, ediff1, dza and diffmax
     float *stencil = nullptr;             // diso or iediff: the per-step top-face stencil
+    char *block = nullptr;                // the one device allocation every array above lies in
+    double *blob = nullptr;               // metrics (build_metric_blob layout) on the device
+    double *tmaxd = nullptr, *gmaxd = nullptr;   // per tracer max |T - tref| and largest forcing transfer
+    unsigned long long *cd = nullptr;     // coefficient maxima (k_setup_stats_many)
     int wet_cols = 0;                     // wet columns (entries it may add to the co list)
     std::vector<int32_t> poff;            // per patch: word offset in ptab
     std::vector<double> pcost;            // per patch: cell-updates per step
     int max_slots = 1;
-    std::vector<double> ds_host;          // ds(0:maxj+1), for the inventory
     MemberDesc desc{};
     long long start_step = 0;    // step index at admission (state in buf0)
     long long stop_step = 0;
@@ -100,6 +108,10 @@ struct gb_ens {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     std::string last_error;
+    // patch plans by (dims, tracers, tile, k1): members admitted again with a mask the ensemble
+    // has seen (a serving loop's request types) skip the planner; bounded, cleared when full
+    std::mutex plan_mu;
+    std::unordered_map<std::string, std::shared_ptr<const PatchPlan>> plans;
 };
 
 static int efail(gb_ens *e, int code, const std::string &msg)
@@ -186,12 +198,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
 
 static void free_member(gb_ens *e, Member *m)
 {
-    cudaStream_t s = e->stream;
-    void *ptrs[] = {m->buf0, m->buf1, m->ts_static, m->rho, m->stage, m->coef, m->coefl, m->gtop, m->mj,
-                    m->rvol, m->mk, m->cost, m->k1, m->scale, m->tref, m->icosd, m->dsj, m->diag, m->status, m->gmax,
-                    m->ptab, m->vel, m->ediff1, m->mkd, m->stencil};
-    for (void *p : ptrs)
-        if (p) cudaFreeAsync(p, s);
+    if (m->block) cudaFreeAsync(m->block, e->stream);
+    m->block = nullptr;
 }
 
 extern "C" void gb_ens_destroy(gb_ens *e)
@@ -239,132 +247,263 @@ extern "C" int gb_ens_set_stream(gb_ens *e, void *s)
     return GB_GO_OK;
 }
 
-template <class T>
-static cudaError_t dalloc(gb_ens *e, T **p, size_t n)
+
+namespace {
+// Host part of a member's admission (no CUDA call): checks, patch plan, metrics, forcing
+// transfers, per-tracer offsets and maxima, and the block of small arrays copied to the device
+// in one piece.  Several host threads may prepare members at once.
+struct Prepared {
+    const gb_go_dims *dims = nullptr;
+    const gb_go_params *params = nullptr;
+    const gb_go_grid *grid = nullptr;
+    const double *ts = nullptr, *u = nullptr;
+    Dims d{};
+    PhysParams p{};
+    double dt = 0.0;
+    size_t bytes = 0;              // budget charge (member_bytes)
+    PatchPlan plan;
+    std::vector<double> blob;
+    Fp32Static small;              // rvol, mk, mj
+    std::vector<float> gtop, tref;
+    std::vector<double> tmax, gmax;
+    long long wet = 0;
+    int wet_cols = 0;
+    // device block layout (byte offsets): the copied segment [0, copied), the zeroed segment
+    // [copied, zeroed), then the arrays the device fills
+    size_t o_blob, o_mj, o_rvol, o_mk, o_dsj, o_tmax, o_gmax, o_k1, o_tref, o_gtop, o_ptab, o_ediff1, copied;
+    size_t o_rho, o_cost, o_icosd, o_gmaxu, o_diag, o_status, o_cd, o_scale, zeroed;
+    size_t o_buf0, o_buf1, o_static, o_stage, o_vel, o_coef, o_coefl, o_stencil, total;
+    std::vector<char> host;        // the copied segment
+    int rc = GB_GO_OK;
+    std::string msg;
+};
+
+// The patch plan of a member from the ensemble's cache, or the planner's (then cached).
+int cached_plan(gb_ens *e, const Dims &d, const int32_t *k1, const gb_ens_tuning &tuning, PatchPlan &out)
 {
-    return cudaMallocFromPoolAsync((void **)p, n * sizeof(T), e->pool, e->stream);
+    std::string key(sizeof(int) * 6 + sizeof(int32_t) * (size_t)d.NI * d.NJ, '\0');
+    const int hdr[6] = {d.maxi, d.maxj, d.maxk, d.L, tuning.tile_i, tuning.tile_j};
+    std::memcpy(&key[0], hdr, sizeof(hdr));
+    std::memcpy(&key[sizeof(hdr)], k1, sizeof(int32_t) * (size_t)d.NI * d.NJ);
+    {
+        std::lock_guard<std::mutex> lk(e->plan_mu);
+        auto it = e->plans.find(key);
+        if (it != e->plans.end()) {
+            out = *it->second;
+            return GB_GO_OK;
+        }
+    }
+    int rc = fp32_plan_patches(d, k1, tuning.tile_i, tuning.tile_j, out);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(e->plan_mu);
+    if (e->plans.size() >= 1024) e->plans.clear();
+    e->plans.emplace(std::move(key), std::make_shared<const PatchPlan>(out));
+    return GB_GO_OK;
 }
 
-extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid,
-                          const double *ts, const double *u, int32_t *member_id)
+int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dims, const gb_go_params *params,
+                   const gb_go_grid *grid, const double *ts, const double *u, Prepared &pm)
 {
-    if (!e || !ts || !u || !member_id) return GB_GO_EINVAL;
-    std::string msg;
-    int rc = validate_config(dims, params, grid, msg);
-    if (rc) return efail(e, rc, msg);
-    if (dims->maxl > kFp32MaxL) return efail(e, GB_GO_ERANGE, "ensemble members carry at most 32 tracers");
-    if (params->imld != 0) return efail(e, GB_GO_EUNSUPPORTED, "imld=1 not provided in ensembles");
+    pm.dims = dims;
+    pm.params = params;
+    pm.grid = grid;
+    pm.ts = ts;
+    pm.u = u;
+    if (!dims || !params || !grid || !ts || !u) {
+        pm.msg = "NULL argument";
+        return pm.rc = GB_GO_EINVAL;
+    }
+    int rc = validate_config(dims, params, grid, pm.msg);
+    if (rc) return pm.rc = rc;
+    if (dims->maxl > kFp32MaxL) {
+        pm.msg = "ensemble members carry at most 32 tracers";
+        return pm.rc = GB_GO_ERANGE;
+    }
+    if (params->imld != 0) {
+        pm.msg = "imld=1 not provided in ensembles";
+        return pm.rc = GB_GO_EUNSUPPORTED;
+    }
     for (int k = 1; k < dims->maxk; ++k)
-        if (grid->dt[k] != grid->dt[0]) return efail(e, GB_GO_EUNSUPPORTED, "ensemble members need one dt for all levels");
-    const size_t bytes = member_bytes(dims, params);
-    ETRY(e, cudaSetDevice(e->device));
+        if (grid->dt[k] != grid->dt[0]) {
+            pm.msg = "ensemble members need one dt for all levels";
+            return pm.rc = GB_GO_EUNSUPPORTED;
+        }
+    if (dims->maxk > kMaxK) {
+        pm.msg = "ensemble members have at most 64 levels";
+        return pm.rc = GB_GO_ERANGE;
+    }
+    pm.d = Dims{dims->maxi, dims->maxj, dims->maxk, dims->maxl, dims->maxi + 2, dims->maxj + 2};
+    pm.p = phys_from(params, grid);
+    pm.dt = grid->dt[0];
+    pm.bytes = member_bytes(dims, params);
+    if (cached_plan(e, pm.d, grid->k1, tuning, pm.plan) != GB_GO_OK) {
+        pm.msg = "no patch shape fits the FP32-flux kernel limits";
+        return pm.rc = GB_GO_ERANGE;
+    }
+    build_metric_blob(dims, params, grid, pm.blob);
+    fp32_build_small(pm.d, pm.p, pm.blob, pm.small);
+    const int L = dims->maxl, NI = pm.d.NI, NJ = pm.d.NJ, maxi = dims->maxi, maxj = dims->maxj, maxk = dims->maxk;
+    const size_t ntop = (size_t)L * NI * NJ;
+    fp32_gtop(pm.d, pm.p, pm.blob, ts + ntop * (maxk + 1), pm.gtop);
+    fp32_tracer_maxima(pm.d, grid->k1, ts, pm.gtop.data(), pm.tref, pm.tmax, pm.gmax);
+    for (int j = 1; j <= maxj; ++j)
+        for (int i = 1; i <= maxi; ++i) {
+            const int k1 = grid->k1[i + (size_t)NI * j];
+            if (k1 <= maxk) {
+                pm.wet += maxk - k1 + 1;
+                pm.wet_cols += 1;
+            }
+        }
+    // layout of the member's device block (256-byte aligned arrays)
+    const bool ediff = params->iediff > 0 && params->iediff < 3;
+    const size_t nts = ntop * (maxk + 2), nrho = (size_t)NI * NJ * (maxk + 1), ncol = (size_t)maxi * maxj;
+    const size_t ncell = ncol * maxk, nplan = fp32_planar_size(pm.d);
+    const size_t nu = (size_t)3 * (maxi + 1) * (maxj + 1) * maxk;
+    const size_t ned = ediff ? (size_t)maxi * maxj * (maxk - 1) : 0;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = (off + bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    pm.o_blob = take(pm.blob.size() * 8);
+    pm.o_mj = take(pm.small.mj.size() * 8);
+    pm.o_rvol = take(pm.small.rvol.size() * 8);
+    pm.o_mk = take(pm.small.mk.size() * 8);
+    pm.o_dsj = take((size_t)(maxj + 2) * 8);
+    pm.o_tmax = take((size_t)L * 8);
+    pm.o_gmax = take((size_t)L * 8);
+    pm.o_k1 = take((size_t)NI * NJ * 4);
+    pm.o_tref = take((size_t)L * 4);
+    pm.o_gtop = take(pm.gtop.size() * 4);
+    pm.o_ptab = take(std::max<size_t>(4, pm.plan.words.size()) * 4);
+    pm.o_ediff1 = take(std::max<size_t>(1, ned) * 8);
+    pm.copied = off;
+    pm.o_rho = take(nrho * 8);
+    pm.o_cost = take(ncol * 8);
+    pm.o_icosd = take(ncol * 4);
+    pm.o_gmaxu = take((size_t)L * 4);
+    pm.o_diag = take(4 * 8);
+    pm.o_status = take(4);
+    pm.o_cd = take(2 * 8);
+    pm.o_scale = take((size_t)L * 4);
+    pm.zeroed = off;
+    pm.o_buf0 = take(nplan * 8);
+    pm.o_buf1 = take(nplan * 8);
+    pm.o_static = take(nts * 8);
+    pm.o_stage = take(nts * 8);
+    pm.o_vel = take(nu * 8);
+    pm.o_coef = take(8 * ncell * 4);
+    pm.o_coefl = take(8 * ncell * 4);
+    pm.o_stencil = take(has_stencil(params) ? (size_t)kStencilWords * ncell * 4 : 0);
+    pm.total = off;
+    pm.host.assign(pm.copied, 0);
+    char *h = pm.host.data();
+    auto put = [&](size_t o, const void *src, size_t bytes) {
+        if (bytes) std::memcpy(h + o, src, bytes);
+    };
+    put(pm.o_blob, pm.blob.data(), pm.blob.size() * 8);
+    put(pm.o_mj, pm.small.mj.data(), pm.small.mj.size() * 8);
+    put(pm.o_rvol, pm.small.rvol.data(), pm.small.rvol.size() * 8);
+    put(pm.o_mk, pm.small.mk.data(), pm.small.mk.size() * 8);
+    put(pm.o_dsj, pm.blob.data() + 6 * (maxj + 2), (size_t)(maxj + 2) * 8);   // ds(0:maxj+1)
+    put(pm.o_tmax, pm.tmax.data(), (size_t)L * 8);
+    put(pm.o_gmax, pm.gmax.data(), (size_t)L * 8);
+    put(pm.o_k1, grid->k1, (size_t)NI * NJ * 4);
+    put(pm.o_tref, pm.tref.data(), (size_t)L * 4);
+    put(pm.o_gtop, pm.gtop.data(), pm.gtop.size() * 4);
+    put(pm.o_ptab, pm.plan.words.data(), pm.plan.words.size() * 4);
+    if (ned) put(pm.o_ediff1, grid->ediff1, ned * 8);
+    return GB_GO_OK;
+}
+}  // namespace
 
-    auto m = std::make_unique<Member>();
-    m->d = Dims{dims->maxi, dims->maxj, dims->maxk, dims->maxl, dims->maxi + 2, dims->maxj + 2};
-    m->p = phys_from(params, grid);
-    m->dt = grid->dt[0];
-    m->bytes = bytes;
-    if (dims->maxk > kMaxK) return efail(e, GB_GO_ERANGE, "ensemble members have at most 64 levels");
-    PatchPlan plan;
-    if (fp32_plan_patches(m->d, grid->k1, e->tuning.tile_i, e->tuning.tile_j, plan) != GB_GO_OK)
-        return efail(e, GB_GO_ERANGE, "no patch shape fits the FP32-flux kernel limits");
-    m->poff = plan.offset;
-    m->pcost = plan.cost;
-    m->max_slots = plan.max_slots;
-    std::vector<double> blob;
-    build_metric_blob(dims, params, grid, blob);
-    Fp32Static st;
-    fp32_build_static(m->d, m->p, blob, grid->k1, u, st);
-    std::vector<float> gtop;
-    const size_t ntop = (size_t)dims->maxl * m->d.NI * m->d.NJ;
-    fp32_gtop(m->d, m->p, blob, ts + ntop * (dims->maxk + 1), gtop);
-    std::vector<int32_t> scale;
-    std::vector<float> tref;
-    fp32_scales(m->d, grid->k1, ts, st.cmax, st.dmax, gtop.data(), scale, tref);
-
-    // device allocation, copies and registration: one member at a time
-    std::lock_guard<std::mutex> lk(e->mu);
-    if (e->in_use + bytes > e->budget) return efail(e, GB_GO_ENOMEM, "member does not fit in the HBM budget");
-    const size_t nts = ntop * (dims->maxk + 2);
-    const size_t nrho = (size_t)m->d.NI * m->d.NJ * (dims->maxk + 1);
-    const size_t ncol = (size_t)dims->maxi * dims->maxj;
+// Device part of a member's admission (caller holds e->mu): one pool allocation, the copied
+// segment, the zeroed segment, ts and u from the caller's arrays; the member's item of the
+// batched device set-up; then its descriptor and registration.  Queued on the ensemble's
+// stream: the caller synchronises before the caller's arrays or pm.host may go.
+static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem *item)
+{
+    if (e->in_use + pm.bytes > e->budget) return efail(e, GB_GO_ENOMEM, "member does not fit in the HBM budget");
     cudaStream_t s = e->stream;
-    const size_t nplan = fp32_planar_size(m->d);
-    cudaError_t x = dalloc(e, &m->buf0, nplan);
-    if (x == cudaSuccess) x = dalloc(e, &m->buf1, nplan);
-    if (x == cudaSuccess) x = dalloc(e, &m->ts_static, nts);
-    if (x == cudaSuccess) x = dalloc(e, &m->stage, nts);
-    if (x == cudaSuccess) x = dalloc(e, &m->rho, nrho);
-    if (x == cudaSuccess) x = dalloc(e, &m->coef, st.coef.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->coefl, st.coefl.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->gtop, gtop.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->mj, st.mj.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->rvol, st.rvol.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->mk, st.mk.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->cost, ncol);
-    if (x == cudaSuccess) x = dalloc(e, &m->icosd, ncol);
-    if (x == cudaSuccess) x = dalloc(e, &m->k1, (size_t)m->d.NI * m->d.NJ);
-    if (x == cudaSuccess) x = dalloc(e, &m->scale, scale.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->tref, tref.size());
-    if (x == cudaSuccess) x = dalloc(e, &m->dsj, (size_t)dims->maxj + 2);
-    if (x == cudaSuccess) x = dalloc(e, &m->gmax, (size_t)dims->maxl);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->gmax, 0, (size_t)dims->maxl * sizeof(unsigned int), s);
-    if (x == cudaSuccess) x = dalloc(e, &m->diag, 4);
-    if (x == cudaSuccess) x = dalloc(e, &m->status, 1);
-    if (x == cudaSuccess) x = dalloc(e, &m->ptab, std::max<size_t>(4, plan.words.size()));
-    if (x == cudaSuccess && !plan.words.empty())
-        x = cudaMemcpyAsync(m->ptab, plan.words.data(), plan.words.size() * 4, cudaMemcpyHostToDevice, s);
-    m->ds_host.assign(blob.begin() + 6 * (dims->maxj + 2), blob.begin() + 7 * (dims->maxj + 2));
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->dsj, m->ds_host.data(), m->ds_host.size() * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->diag, 0, 4 * sizeof(unsigned long long), s);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->status, 0, sizeof(unsigned int), s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, ts, nts * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess && (fp32_to_planar(m->buf0, m->ts_static, m->d, s) || fp32_to_planar(m->buf1, m->ts_static, m->d, s))) {
-        const cudaError_t le = cudaGetLastError();
-        x = le != cudaSuccess ? le : cudaErrorLaunchFailure;
-    }
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->rho, 0, nrho * 8, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->coef, st.coef.data(), st.coef.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->coefl, st.coefl.data(), st.coefl.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->gtop, gtop.data(), gtop.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->mj, st.mj.data(), st.mj.size() * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->rvol, st.rvol.data(), st.rvol.size() * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->mk, st.mk.data(), st.mk.size() * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->cost, 0, ncol * 8, s);
-    if (x == cudaSuccess) x = cudaMemsetAsync(m->icosd, 0, ncol * 4, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->k1, grid->k1, (size_t)m->d.NI * m->d.NJ * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->scale, scale.data(), scale.size() * 4, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->tref, tref.data(), tref.size() * 4, cudaMemcpyHostToDevice, s);
-    const bool need_ediff = params->iediff > 0 && params->iediff < 3;
-    if (need_ediff) {
-        // the step rebuilds the top-face coefficients from u, ediff1, dza and diffmax
-        const size_t nu = (size_t)3 * (dims->maxi + 1) * (dims->maxj + 1) * dims->maxk;
-        const size_t ned = (size_t)dims->maxi * dims->maxj * (dims->maxk - 1);
-        const size_t nk = (size_t)dims->maxk + 2, nj = (size_t)dims->maxj + 2;
-        if (x == cudaSuccess) x = dalloc(e, &m->vel, nu);
-        if (x == cudaSuccess) x = dalloc(e, &m->ediff1, std::max<size_t>(1, ned));
-        if (x == cudaSuccess) x = dalloc(e, &m->mkd, 2 * nk);
-        if (x == cudaSuccess) x = cudaMemcpyAsync(m->vel, u, nu * 8, cudaMemcpyHostToDevice, s);
-        if (x == cudaSuccess && ned) x = cudaMemcpyAsync(m->ediff1, grid->ediff1, ned * 8, cudaMemcpyHostToDevice, s);
-        // Fortran-indexed dza, then diffmax, from the metric blob (8 j-arrays, then k-arrays)
-        if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd, blob.data() + 8 * nj + nk, nk * 8, cudaMemcpyHostToDevice, s);
-        if (x == cudaSuccess) x = cudaMemcpyAsync(m->mkd + nk, blob.data() + 8 * nj + 8 * nk, nk * 8, cudaMemcpyHostToDevice, s);
-    }
-    if (x == cudaSuccess && has_stencil(params)) x = dalloc(e, &m->stencil, (size_t)kStencilWords * dims->maxi * dims->maxj * dims->maxk);
-    // host staging vectors must outlive the copies
-    if (x == cudaSuccess) x = cudaStreamSynchronize(s);
+    const gb_go_dims *dims = pm.dims;
+    const gb_go_params *params = pm.params;
+    const int L = dims->maxl, maxk = dims->maxk;
+    const size_t nts = (size_t)L * pm.d.NI * pm.d.NJ * (maxk + 2);
+    const size_t nu = (size_t)3 * (dims->maxi + 1) * (dims->maxj + 1) * maxk;
+    auto m = std::make_unique<Member>();
+    m->d = pm.d;
+    m->p = pm.p;
+    m->dt = pm.dt;
+    m->bytes = pm.bytes;
+    m->poff = pm.plan.offset;
+    m->pcost = pm.plan.cost;
+    m->max_slots = pm.plan.max_slots;
+    m->wet_cols = pm.wet_cols;
+    cudaError_t x = cudaMallocFromPoolAsync((void **)&m->block, pm.total, e->pool, s);
+    if (x != cudaSuccess) return efail(e, x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA, cudaGetErrorString(x));
+    char *b = m->block;
+    m->blob = (double *)(b + pm.o_blob);
+    m->mj = (double *)(b + pm.o_mj);
+    m->rvol = (double *)(b + pm.o_rvol);
+    m->mk = (double *)(b + pm.o_mk);
+    m->dsj = (double *)(b + pm.o_dsj);
+    m->tmaxd = (double *)(b + pm.o_tmax);
+    m->gmaxd = (double *)(b + pm.o_gmax);
+    m->k1 = (int32_t *)(b + pm.o_k1);
+    m->tref = (float *)(b + pm.o_tref);
+    m->gtop = (float *)(b + pm.o_gtop);
+    m->ptab = (int32_t *)(b + pm.o_ptab);
+    const bool ediff = params->iediff > 0 && params->iediff < 3;
+    m->ediff1 = ediff ? (double *)(b + pm.o_ediff1) : nullptr;
+    m->rho = (double *)(b + pm.o_rho);
+    m->cost = (double *)(b + pm.o_cost);
+    m->icosd = (int32_t *)(b + pm.o_icosd);
+    m->gmax = (unsigned int *)(b + pm.o_gmaxu);
+    m->diag = (unsigned long long *)(b + pm.o_diag);
+    m->status = (unsigned int *)(b + pm.o_status);
+    m->cd = (unsigned long long *)(b + pm.o_cd);
+    m->scale = (int32_t *)(b + pm.o_scale);
+    m->buf0 = (double *)(b + pm.o_buf0);
+    m->buf1 = (double *)(b + pm.o_buf1);
+    m->ts_static = (double *)(b + pm.o_static);
+    m->stage = (double *)(b + pm.o_stage);
+    m->vel = (double *)(b + pm.o_vel);
+    m->coef = (float *)(b + pm.o_coef);
+    m->coefl = (float *)(b + pm.o_coefl);
+    m->stencil = has_stencil(params) ? (float *)(b + pm.o_stencil) : nullptr;
+    const int nj = dims->maxj + 2, nk = maxk + 2;
+    m->mkd = ediff ? m->blob + 8 * nj + nk : nullptr;   // dza, then (7 k-arrays on) diffmax
+    x = cudaMemcpyAsync(b, pm.host.data(), pm.copied, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess) x = cudaMemsetAsync(b + pm.copied, 0, pm.zeroed - pm.copied, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, pm.ts, nts * 8, cudaMemcpyHostToDevice, s);
+    if (x == cudaSuccess) x = cudaMemcpyAsync(m->vel, pm.u, nu * 8, cudaMemcpyHostToDevice, s);
     if (x != cudaSuccess) {
         free_member(e, m.get());
-        cudaStreamSynchronize(s);
         return efail(e, x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA, cudaGetErrorString(x));
     }
+    // the device set-up (state buffers, coefficients, scales) runs batched after the copies
+    item->d = m->d;
+    item->p = m->p;
+    item->m = metrics_from_blob(m->blob, m->k1, m->ediff1, dims->maxj, maxk);
+    item->u = m->vel;
+    item->ts_static = m->ts_static;
+    item->buf0 = m->buf0;
+    item->buf1 = m->buf1;
+    item->coef = m->coef;
+    item->coefl = m->coefl;
+    item->cd = m->cd;
+    item->tmax = m->tmaxd;
+    item->gmax = m->gmaxd;
+    item->tref = m->tref;
+    item->scale = m->scale;
     MemberDesc &md = m->desc;
-    md.maxi = dims->maxi; md.maxj = dims->maxj; md.maxk = dims->maxk; md.L = dims->maxl;
+    md.maxi = dims->maxi; md.maxj = dims->maxj; md.maxk = maxk; md.L = L;
     md.NI = m->d.NI; md.NJ = m->d.NJ; md.diso = m->p.diso; md.ieos = m->p.ieos; md.iconv = m->p.iconv;
     md.iediff = m->p.iediff; md.ediffpow2i = m->p.ediffpow2i;
     md.diff2 = m->p.diff2; md.ediff0 = m->p.ediff0; md.ediffpow2 = m->p.ediffpow2;
     md.u = m->vel; md.ediff1 = m->ediff1;
-    md.dza = m->mkd; md.diffmax = m->mkd ? m->mkd + (dims->maxk + 2) : nullptr;
+    md.dza = m->mkd; md.diffmax = m->mkd ? m->blob + 8 * nj + 8 * nk : nullptr;
     md.stencil = m->stencil;
     md.dt = m->dt; md.dphi = m->p.dphi; md.rdphi = m->p.rdphi; md.diff1 = m->p.diff1;
     for (int n = 0; n < 5; ++n) md.ec[n] = m->p.ec[n];
@@ -378,21 +517,78 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission
     md.stop_step = m->stop_step;
     md.origin = e->step;
-    long long wet = 0;
-    for (int j = 1; j <= dims->maxj; ++j)
-        for (int i = 1; i <= dims->maxi; ++i) {
-            const int k1 = grid->k1[i + (size_t)m->d.NI * j];
-            if (k1 <= dims->maxk) {
-                wet += dims->maxk - k1 + 1;
-                m->wet_cols += 1;
-            }
-        }
-    m->cost_est = (double)wet * (dims->maxl + 4) * (params->diso ? 2.0 : 1.0);
+    m->cost_est = (double)pm.wet * (L + 4) * (params->diso ? 2.0 : 1.0);
     m->id = e->next_id++;
     *member_id = m->id;
-    e->in_use += bytes;
+    e->in_use += pm.bytes;
     e->members[m->id] = std::move(m);
     e->dirty = true;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params, const gb_go_grid *grid,
+                          const double *ts, const double *u, int32_t *member_id)
+{
+    if (!e || !ts || !u || !member_id) return GB_GO_EINVAL;
+    return gb_ens_add_many(e, 1, dims, params, grid, &ts, &u, member_id);
+}
+
+extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, const gb_go_params *params,
+                               const gb_go_grid *grids, const double *const *ts, const double *const *u, int32_t *ids)
+{
+    if (!e || n < 0 || (n > 0 && (!dims || !params || !grids || !ts || !u || !ids))) return GB_GO_EINVAL;
+    if (n == 0) return GB_GO_OK;
+    ETRY(e, cudaSetDevice(e->device));
+    // host preparation on up to 16 threads
+    std::vector<Prepared> pm(n);
+    const gb_ens_tuning tuning = e->tuning;
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (int q = next++; q < n; q = next++) prepare_member(e, tuning, dims + q, params + q, grids + q, ts[q], u[q], pm[q]);
+    };
+    const int nt = std::max(1, std::min<int>(std::min<int>(n, 16), (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+    for (int q = 0; q < n; ++q)
+        if (pm[q].rc) return efail(e, pm[q].rc, pm[q].msg);
+    // the device part, one member at a time, the batched set-up, then one synchronisation
+    std::lock_guard<std::mutex> lk(e->mu);
+    int q = 0, rc = GB_GO_OK;
+    std::vector<SetupItem> items(n);
+    size_t max_elems = 1, max_cells = 1;
+    for (; q < n; ++q) {
+        if ((rc = commit_member(e, pm[q], ids + q, &items[q]))) break;
+        const Dims &d = items[q].d;
+        max_elems = std::max(max_elems, (size_t)d.NI * d.NJ * (d.maxk + 2) * d.L);
+        max_cells = std::max(max_cells, (size_t)d.maxi * d.maxj * d.maxk);
+    }
+    if (!rc) {
+        SetupItem *dit = nullptr;
+        cudaError_t x = cudaMallocAsync((void **)&dit, sizeof(SetupItem) * n, e->stream);
+        if (x == cudaSuccess) x = cudaMemcpyAsync(dit, items.data(), sizeof(SetupItem) * n, cudaMemcpyHostToDevice, e->stream);
+        if (x == cudaSuccess && fp32_setup_many(dit, n, max_elems, max_cells, e->stream)) x = cudaErrorLaunchFailure;
+        if (dit) cudaFreeAsync(dit, e->stream);
+        if (x != cudaSuccess) {
+            rc = efail(e, x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA, cudaGetErrorString(x));
+            q = n;
+        }
+    }
+    if (rc) {
+        // all or nothing: the members of this call that were committed leave again
+        for (int r = 0; r < q; ++r) {
+            auto it = e->members.find(ids[r]);
+            if (it == e->members.end()) continue;
+            free_member(e, it->second.get());
+            e->in_use -= it->second->bytes;
+            e->members.erase(it);
+        }
+        const std::string msg = e->last_error;
+        cudaStreamSynchronize(e->stream);
+        return efail(e, rc, msg);
+    }
+    ETRY(e, cudaStreamSynchronize(e->stream));
     return GB_GO_OK;
 }
 
@@ -658,13 +854,119 @@ static int download_on(gb_ens *e, Member *m, cudaStream_t s, double *ts, double 
     return GB_GO_OK;
 }
 
+// One member's download in one kernel: the Fortran-layout ts (the current group-planar state on
+// wet interior cells, the uploaded values elsewhere -- halo columns included, which the steps
+// leave as uploaded) into `stage`, and rho (eos of that state on interior cells at zro(k), the
+// periodic copies on wet halo cells; other entries keep their value, zero from admission).
+// The same values as fp32_export followed by k_merge_member, without the intermediate Fortran
+// copy.  A grid-stride range over the cells of the (NI, NJ, maxk+2) box.
+struct DownloadItem {
+    MemberDesc md;
+    const double *planar;
+    double *stage, *rho;
+};
+
+__device__ __forceinline__ void member_download_cells(const MemberDesc &md, const double *planar, double *stage, double *rho,
+                                                      size_t c0, size_t cs)
+{
+    const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
+    const size_t NIJ = (size_t)NI * NJ, ncell = NIJ * (maxk + 2), NIJK = ncell;
+    const double *zro = md.mk + 3 * (maxk + 2);
+    EosCoef ec;
+    for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
+    ec.ieos = md.ieos;
+    const int ng = fp32_ngroups(L);
+    for (size_t c = c0; c < ncell; c += cs) {
+        const int i = (int)(c % NI);
+        const int j = (int)((c / NI) % NJ);
+        const int k = (int)(c / NIJ);
+        const bool inner = k >= 1 && k <= maxk && j >= 1 && j <= maxj;
+        const bool wet = inner && i >= 1 && i <= maxi && k >= md.k1[i + NI * j];
+        double t = 0.0, sv = 0.0;
+        for (int g = 0, l = 0; g < ng; ++g) {
+            int g0, gl, gp, pl;
+            fp32_plane(L, g, &g0, &gl, &gp, &pl);
+            for (int q = 0; q < gl; ++q, ++l) {
+                const double v = wet ? planar[(size_t)pl * NIJK + c * gp + q] : md.ts_static[c * L + l];
+                stage[c * L + l] = v;
+                if (l == 0) t = v;
+                if (l == 1) sv = v;
+            }
+        }
+        if (!inner) continue;
+        if (i >= 1 && i <= maxi) {
+            rho[i + NI * (j + NJ * (size_t)k)] = eos_rn(ec, t, sv, zro[k]);
+        } else {
+            // wet halo cells: the density of the periodic source column (k1 is periodic, so the
+            // source is wet there too)
+            if (k < md.k1[i + NI * j]) continue;
+            const int src = i == 0 ? maxi : 1;
+            const size_t cs2 = (size_t)src + NI * (j + NJ * (size_t)k);
+            rho[i + NI * (j + NJ * (size_t)k)] = eos_rn(ec, planar[cs2 * 2], planar[cs2 * 2 + 1], zro[k]);
+        }
+    }
+}
+
+// The downloads of several members in one launch (blockIdx.y: the member's item).
+__global__ void k_member_download_many(const DownloadItem *it)
+{
+    const DownloadItem &I = it[blockIdx.y];
+    member_download_cells(I.md, I.planar, I.stage, I.rho, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                          (size_t)gridDim.x * blockDim.x);
+}
+
+extern "C" int gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, double *const *ts, double *const *rho,
+                                    double *const *cost)
+{
+    if (!e || n < 0 || (n > 0 && !ids)) return GB_GO_EINVAL;
+    std::vector<Member *> ms;
+    for (int32_t q = 0; q < n; ++q) {
+        auto it = e->members.find(ids[q]);
+        if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
+        ms.push_back(it->second.get());
+    }
+    ETRY(e, cudaSetDevice(e->device));
+    if (n == 0) return GB_GO_OK;
+    // one kernel forms every member's Fortran-layout ts and rho, then the copies
+    std::vector<DownloadItem> items(n);
+    size_t max_cells = 1;
+    for (int32_t q = 0; q < n; ++q) {
+        items[q].md = ms[q]->desc;
+        items[q].planar = current_buffer(e, ms[q]);
+        items[q].stage = ms[q]->stage;
+        items[q].rho = ms[q]->rho;
+        max_cells = std::max(max_cells, (size_t)ms[q]->d.NI * ms[q]->d.NJ * (ms[q]->d.maxk + 2));
+    }
+    cudaStream_t s = e->stream;
+    for (int32_t q0 = 0; q0 < n; q0 += 65535) {
+        const int nq = std::min<int>(n - q0, 65535);
+        DownloadItem *dit = nullptr;
+        ETRY(e, cudaMallocAsync((void **)&dit, sizeof(DownloadItem) * nq, s));
+        cudaError_t x = cudaMemcpyAsync(dit, items.data() + q0, sizeof(DownloadItem) * nq, cudaMemcpyHostToDevice, s);
+        if (x == cudaSuccess) {
+            const int bx = (int)std::max<size_t>(1, std::min<size_t>((max_cells + 255) / 256, 128));
+            k_member_download_many<<<dim3(bx, nq), 256, 0, s>>>(dit);
+            count_launches(1);
+            x = cudaGetLastError();
+        }
+        cudaFreeAsync(dit, s);
+        if (x != cudaSuccess) return efail(e, GB_GO_ECUDA, cudaGetErrorString(x));
+    }
+    for (int32_t q = 0; q < n; ++q) {
+        Member *m = ms[q];
+        const size_t nts = (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 2) * m->d.L;
+        if (ts && ts[q]) ETRY(e, cudaMemcpyAsync(ts[q], m->stage, nts * 8, cudaMemcpyDeviceToHost, s));
+        if (rho && rho[q])
+            ETRY(e, cudaMemcpyAsync(rho[q], m->rho, (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 1) * 8, cudaMemcpyDeviceToHost, s));
+        if (cost && cost[q]) ETRY(e, cudaMemcpyAsync(cost[q], m->cost, (size_t)m->d.maxi * m->d.maxj * 8, cudaMemcpyDeviceToHost, s));
+    }
+    ETRY(e, cudaStreamSynchronize(s));
+    return GB_GO_OK;
+}
+
 extern "C" int gb_ens_download(gb_ens *e, int32_t id, double *ts, double *rho, double *cost)
 {
-    if (!e) return GB_GO_EINVAL;
-    auto it = e->members.find(id);
-    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
-    ETRY(e, cudaSetDevice(e->device));
-    return download_on(e, it->second.get(), e->stream, ts, rho, cost);
+    return gb_ens_download_many(e, 1, &id, ts ? &ts : nullptr, rho ? &rho : nullptr, cost ? &cost : nullptr);
 }
 
 extern "C" int gb_ens_download_stream(gb_ens *e, int32_t id, void *cuda_stream, double *ts, double *rho, double *cost)

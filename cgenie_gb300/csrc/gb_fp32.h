@@ -191,11 +191,54 @@ struct Fp32Static {
 };
 void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const int32_t *k1,
                        const double *u_host, Fp32Static &out);
+// rvol, mk, mj of fp32_build_static only (no coefficients)
+void fp32_build_small(const Dims &d, const PhysParams &p, const std::vector<double> &blob, Fp32Static &out);
+
+// Exponent s of the fixed-point transfers of a tracer whose largest transfer is g: the largest
+// s with g * 2^s <= 2^26, i.e. floor(log2(2^26 / g)), from the exact binary exponent of g;
+// clamped to [-120, 120]; 0 for g = 0 or non-finite g.  Host and device give the same value.
+__host__ __device__ inline int fp32_scale_of(double g)
+{
+    if (!(g > 0.0) || !(g <= 1.7976931348623157e308)) return 0;
+    int e = 0;
+    const double f = frexp(g, &e);   // g = f 2^e, f in [0.5, 1)
+    const int s = 26 - e + (f == 0.5 ? 1 : 0);
+    return s < -120 ? -120 : (s > 120 ? 120 : s);
+}
 // Per tracer: the offset tref (tracers whose wet values lie within a factor of two of each
 // other: DIC, alkalinity; 0 for the others and for T and S) and the fixed-point scale from
 // the largest transfer: 2 cmax max |T - tref|, the forcing, and |tref| dmax.
 void fp32_scales(const Dims &d, const int32_t *k1, const double *ts_host, double cmax, double dmax,
                  const float *gtop_unscaled, std::vector<int32_t> &scale, std::vector<float> &tref);
+// The per-tracer inputs of fp32_scales that come from the state: tref, max |T - tref| over wet
+// cells, and the largest forcing transfer.
+void fp32_tracer_maxima(const Dims &d, const int32_t *k1, const double *ts, const float *gtop, std::vector<float> &tref,
+                        std::vector<double> &tmax, std::vector<double> &gmax);
+// the largest transfer bound whose exponent fp32_scale_of gives (host; k_member_scales on the device)
+double fp32_transfer_bound(double cmax, double dmax, double tmax, double gmax, float tref);
+
+// One member of a batched device set-up (device pointers; Metrics into the member's uploaded
+// metric blob).
+struct SetupItem {
+    Dims d;
+    PhysParams p;
+    Metrics m;
+    const double *u, *ts_static;
+    double *buf0, *buf1;
+    float *coef, *coefl;
+    unsigned long long *cd;
+    const double *tmax, *gmax;
+    const float *tref;
+    int32_t *scale;
+};
+// Device part of the set-up of n ensemble members (items in device memory; stream order, no
+// synchronisation), five launches in all: both state buffers from the uploaded ts; the transfer
+// coefficients from u as fp32_build_static builds them (words 0-5, then the divergence pair);
+// their largest face sums and divergence into cd[0], cd[1] (double bits, cd zeroed beforehand);
+// the fixed-point scales from cd and the per-tracer maxima (fp32_transfer_bound,
+// fp32_scale_of).  max_elems / max_cells: the largest state (L x cells) and interior cell count
+// of the items.
+int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t max_cells, cudaStream_t s);
 void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &blob, const double *top_host,
                std::vector<float> &gtop);
 // Patch plan of one member: the kernel's work items.  Word layout of one patch table:

@@ -1207,7 +1207,6 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     const size_t ncell = (size_t)maxi * maxj * maxk;
     out.coef.assign(8 * ncell, 0.0f);
     out.coefl.assign(8 * ncell, 0.0f);
-    out.rvol.assign((size_t)maxj * maxk, 0.0);
     out.cmax = 0.0;
     out.dmax = 0.0;
     auto U = [&](int c, int i, int j, int k) -> double {
@@ -1216,7 +1215,6 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
     auto K1 = [&](int i, int j) { return k1[i + (size_t)NI * j]; };
     for (int k = 1; k <= maxk; ++k) {
         for (int j = 1; j <= maxj; ++j) {
-            out.rvol[(size_t)(j - 1) + (size_t)maxj * (k - 1)] = 1.0 / (p.dphi * ds[j] * dz[k]);
             for (int i = 1; i <= maxi; ++i) {
                 const size_t cell = (size_t)(i - 1) + (size_t)maxi * ((size_t)(j - 1) + (size_t)maxj * (k - 1));
                 float *c = &out.coef[8 * cell];
@@ -1273,6 +1271,21 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
                               &out.coef[8 * c + 7]);
                 out.dmax = std::max(out.dmax, std::fabs((double)out.coef[8 * c + 6]) + std::fabs((double)out.coef[8 * c + 7]));
             }
+    fp32_build_small(d, p, blob, out);
+}
+
+void fp32_build_small(const Dims &d, const PhysParams &p, const std::vector<double> &blob, Fp32Static &out)
+{
+    const int maxj = d.maxj, maxk = d.maxk;
+    const int nj = maxj + 2, nk = maxk + 2;
+    const double *b = blob.data();
+    const double *rc = b, *cv = b + 2 * nj, *rdsv = b + 5 * nj, *ds = b + 6 * nj;
+    const double *kb = b + 8 * nj;
+    const double *dz = kb, *rdz = kb + 2 * nk, *rdza = kb + 3 * nk, *zro = kb + 4 * nk, *dt = kb + 5 * nk,
+                 *zw = kb + 6 * nk, *ssmax = kb + 7 * nk;
+    out.rvol.assign((size_t)maxj * maxk, 0.0);
+    for (int k = 1; k <= maxk; ++k)
+        for (int j = 1; j <= maxj; ++j) out.rvol[(size_t)(j - 1) + (size_t)maxj * (k - 1)] = 1.0 / (p.dphi * ds[j] * dz[k]);
     out.mk.assign(6 * (size_t)nk, 0.0);
     for (int k = 0; k <= maxk + 1; ++k) {
         out.mk[k] = dz[k];
@@ -1294,11 +1307,12 @@ void fp32_build_static(const Dims &d, const PhysParams &p, const std::vector<dou
 // velocity field of every ocean step in a coupled run): the same FP64 expressions in the
 // same order, with round-to-nearest intrinsics (no contraction), so the coefficients are
 // those the host builds.  One thread per interior cell.
-__global__ void k_build_coef(const double *__restrict__ u, Metrics m, Dims d, PhysParams p, float *coef, float *coefl)
+__device__ __forceinline__ void build_coef_cells(const double *__restrict__ u, const Metrics &m, const Dims &d,
+                                                 const PhysParams &p, float *coef, float *coefl, size_t c0, size_t cs)
 {
     const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
     const size_t ncell = (size_t)maxi * maxj * maxk;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+    for (size_t c = c0; c < ncell; c += cs) {
         const int i = (int)(c % maxi) + 1;
         const int j = (int)((c / maxi) % maxj) + 1;
         const int k = (int)(c / ((size_t)maxi * maxj)) + 1;
@@ -1348,12 +1362,17 @@ __global__ void k_build_coef(const double *__restrict__ u, Metrics m, Dims d, Ph
     }
 }
 
+__global__ void k_build_coef(const double *__restrict__ u, Metrics m, Dims d, PhysParams p, float *coef, float *coefl)
+{
+    build_coef_cells(u, m, d, p, coef, coefl, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
 // Words 6, 7 of the coefficients (the divergence pair) after k_build_coef, as the host builds them.
-__global__ void k_build_div(Dims d, float *coef, const float *coefl)
+__device__ __forceinline__ void build_div_cells(const Dims &d, float *coef, const float *coefl, size_t c0, size_t cs)
 {
     const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk;
     const size_t nij = (size_t)maxi * maxj, ncell = nij * maxk;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+    for (size_t c = c0; c < ncell; c += cs) {
         const int i = (int)(c % maxi) + 1;
         const int j = (int)((c / maxi) % maxj) + 1;
         const int k = (int)(c / nij) + 1;
@@ -1363,6 +1382,59 @@ __global__ void k_build_div(Dims d, float *coef, const float *coefl)
         fp32_div_pair(coef, coefl, maxi, nij, c, cw, j > 1, k > 1, &dh, &dl);
         coef[8 * c + 6] = dh;
         coef[8 * c + 7] = dl;
+    }
+}
+
+__global__ void k_build_div(Dims d, float *coef, const float *coefl)
+{
+    build_div_cells(d, coef, coefl, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
+// The coefficient maxima fp32_build_static keeps, from the coefficients on the device: cd[0]
+// = max over faces of |A| + |B| (and, with iediff 1/2, the bound of the rebuilt top faces),
+// cd[1] = max over cells of |Dh| + |Dl|; as double bits (non-negative doubles order as their
+// bits).  Same expressions and order as the host, round-to-nearest intrinsics.
+__device__ __forceinline__ void coef_stats_cells(const Dims &d, const PhysParams &p, const Metrics &m,
+                                                 const double *__restrict__ u, const float *__restrict__ coef,
+                                                 unsigned long long *cd, size_t c0, size_t cs)
+{
+    const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, NI = d.NI;
+    const size_t nij = (size_t)maxi * maxj, ncell = nij * maxk;
+    double cm = 0.0, dm = 0.0;
+    for (size_t c = c0; c < ncell; c += cs) {
+        const float *cf = coef + 8 * c;
+        for (int f = 0; f < 3; ++f) cm = fmax(cm, __dadd_rn((double)fabsf(cf[2 * f]), (double)fabsf(cf[2 * f + 1])));
+        dm = fmax(dm, __dadd_rn((double)fabsf(cf[6]), (double)fabsf(cf[7])));
+        if (p.iediff > 0 && p.iediff < 3) {
+            const int i = (int)(c % maxi) + 1, j = (int)((c / maxi) % maxj) + 1, k = (int)(c / nij) + 1;
+            if (k >= m.k1[i + (size_t)NI * j] && k < maxk) {
+                const double u3 = u[2 + 3 * ((size_t)i + (size_t)(maxi + 1) * ((size_t)j + (size_t)(maxj + 1) * (size_t)(k - 1)))];
+                const double g = __dmul_rn(__dmul_rn(m.dt[k], p.dphi), m.ds[j]);
+                const double dv = fmax(p.diff2, m.diffmax[k + 1]);
+                cm = fmax(cm, __dmul_rn(g, __dadd_rn(fabs(u3), __dmul_rn(__dmul_rn(2.0, m.rdza[k]), dv))));
+            }
+        }
+    }
+    unsigned long long a = (unsigned long long)__double_as_longlong(cm), b = (unsigned long long)__double_as_longlong(dm);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, a, o), y = __shfl_xor_sync(0xffffffffu, b, o);
+        a = x > a ? x : a;
+        b = y > b ? y : b;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(cd, a);
+        atomicMax(cd + 1, b);
+    }
+}
+
+// Per-tracer fixed-point scales from the device coefficient maxima (fp32_transfer_bound, fp32_scale_of).
+__device__ __forceinline__ void member_scales(const unsigned long long *cd, const double *tmax, const double *gmax,
+                                              const float *tref, int L, int32_t *scale)
+{
+    const double cmax = __longlong_as_double((long long)cd[0]), dmax = __longlong_as_double((long long)cd[1]);
+    for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        const double g = fmax(fmax(__dmul_rn(__dmul_rn(2.0, cmax), tmax[l]), gmax[l]), __dmul_rn(fabs((double)tref[l]), dmax));
+        scale[l] = fp32_scale_of(g);
     }
 }
 
@@ -1387,25 +1459,21 @@ void fp32_gtop(const Dims &d, const PhysParams &p, const std::vector<double> &bl
         }
 }
 
-void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax, double dmax, const float *gtop,
-                 std::vector<int32_t> &scale, std::vector<float> &tref)
+void fp32_tracer_maxima(const Dims &d, const int32_t *k1, const double *ts, const float *gtop, std::vector<float> &tref,
+                        std::vector<double> &tmax, std::vector<double> &gmax)
 {
     const int maxi = d.maxi, maxj = d.maxj, maxk = d.maxk, L = d.L, NI = d.NI, NJ = d.NJ;
-    std::vector<double> tmax(L, 0.0), gmax(L, 0.0), vlo(L, HUGE_VAL), vhi(L, -HUGE_VAL);
-    auto each_wet = [&](auto &&fn) {
-        for (int k = 1; k <= maxk; ++k)
-            for (int j = 1; j <= maxj; ++j)
-                for (int i = 1; i <= maxi; ++i) {
-                    if (k < k1[i + (size_t)NI * j]) continue;
-                    fn(ts + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k)));
+    std::vector<double> vlo(L, HUGE_VAL), vhi(L, -HUGE_VAL);
+    for (int k = 1; k <= maxk; ++k)
+        for (int j = 1; j <= maxj; ++j)
+            for (int i = 1; i <= maxi; ++i) {
+                if (k < k1[i + (size_t)NI * j]) continue;
+                const double *p = ts + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k));
+                for (int l = 0; l < L; ++l) {
+                    vlo[l] = std::min(vlo[l], p[l]);
+                    vhi[l] = std::max(vhi[l], p[l]);
                 }
-    };
-    each_wet([&](const double *p) {
-        for (int l = 0; l < L; ++l) {
-            vlo[l] = std::min(vlo[l], p[l]);
-            vhi[l] = std::max(vhi[l], p[l]);
-        }
-    });
+            }
     // offset: the mid-range, rounded to 8 significant bits, for tracers (other than T and S)
     // whose wet values stay within a factor of two of each other; the transfers then carry
     // T - tref, whose FP32 rounding is smaller than T's by about max|T| / max|T - tref|
@@ -1417,23 +1485,33 @@ void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax
         const double f = std::frexp(0.5 * (lo + hi), &ex);
         tref[l] = (float)std::ldexp(std::nearbyint(f * 256.0), ex - 8);
     }
-    each_wet([&](const double *p) {
-        for (int l = 0; l < L; ++l) tmax[l] = std::max(tmax[l], std::fabs(p[l] - (double)tref[l]));
-    });
+    // max over wet cells of |T - tref|: T - tref rounds monotonically, so the extremes decide
+    tmax.assign(L, 0.0);
+    for (int l = 0; l < L; ++l)
+        if (vlo[l] <= vhi[l])
+            tmax[l] = std::max(std::fabs(vlo[l] - (double)tref[l]), std::fabs(vhi[l] - (double)tref[l]));
+    gmax.assign(L, 0.0);
     if (gtop)
         for (size_t n = 0; n < (size_t)maxi * maxj; ++n)
             for (int l = 0; l < L; ++l) gmax[l] = std::max(gmax[l], (double)std::fabs(gtop[n * (L + 2) + l]));
-    scale.assign(L, 0);
-    for (int l = 0; l < L; ++l) {
-        // largest transfer the step can produce: (|A|+|B|)*max|T| per face; the
-        // isoneutral stencil and growth of max|T| are covered by 2^4 headroom
-        // below the int32 range (2^26 target); a transfer above 3e8 (the sum of six
-        // stays inside int32) sets the member's range flag
-        const double g = std::max(std::max(2.0 * cmax * tmax[l], gmax[l]), std::fabs((double)tref[l]) * dmax);
-        int s = 0;
-        if (g > 0.0 && std::isfinite(g)) s = (int)std::floor(std::log2(67108864.0 / g));
-        scale[l] = std::max(-120, std::min(120, s));
-    }
+}
+
+double fp32_transfer_bound(double cmax, double dmax, double tmax, double gmax, float tref)
+{
+    // largest transfer the step can produce: (|A|+|B|)*max|T - tref| per face, the forcing, the
+    // offset's share; the isoneutral stencil and growth of max|T| are covered by 2^4 headroom
+    // below the int32 range (2^26 target); a transfer above 3.5e8 (the sum of six stays inside
+    // int32) sets the member's range flag
+    return std::max(std::max(2.0 * cmax * tmax, gmax), std::fabs((double)tref) * dmax);
+}
+
+void fp32_scales(const Dims &d, const int32_t *k1, const double *ts, double cmax, double dmax, const float *gtop,
+                 std::vector<int32_t> &scale, std::vector<float> &tref)
+{
+    std::vector<double> tmax, gmax;
+    fp32_tracer_maxima(d, k1, ts, gtop, tref, tmax, gmax);
+    scale.assign(d.L, 0);
+    for (int l = 0; l < d.L; ++l) scale[l] = fp32_scale_of(fp32_transfer_bound(cmax, dmax, tmax[l], gmax[l], tref[l]));
 }
 
 // ---------------------------------------------------------------------------
@@ -1478,12 +1556,13 @@ __global__ void k_export_halo(const MemberDesc md, double *cur, double *rho)
 }
 
 // Fortran layout <-> group-planar layout, every cell of the arrays
-__global__ void k_to_planar(double *planar, double *fortran, Dims d, int to)
+__device__ __forceinline__ void to_planar_range(double *planar, double *fortran, const Dims &d, int to, double *planar2,
+                                                size_t e0, size_t es)
 {
     const size_t ncell = (size_t)d.NI * d.NJ * (d.maxk + 2);
     const size_t n = ncell * d.L;
     const int ng = fp32_ngroups(d.L);
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    for (size_t e = e0; e < n; e += es) {
         const int l = (int)(e % d.L);
         const size_t c = e / d.L;
         int g0 = 0, gl = 2, gp = 2, pl = 0;
@@ -1492,9 +1571,67 @@ __global__ void k_to_planar(double *planar, double *fortran, Dims d, int to)
             if (l < g0 + gl) break;
         }
         const size_t pi = (size_t)pl * ncell + c * gp + (l - g0);
-        if (to) planar[pi] = fortran[e];
-        else fortran[e] = planar[pi];
+        if (to) {
+            const double v = fortran[e];
+            planar[pi] = v;
+            if (planar2) planar2[pi] = v;
+        } else {
+            fortran[e] = planar[pi];
+        }
     }
+}
+
+__global__ void k_to_planar(double *planar, double *fortran, Dims d, int to)
+{
+    to_planar_range(planar, fortran, d, to, nullptr, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                    (size_t)gridDim.x * blockDim.x);
+}
+
+// Batched device set-up of ensemble members (blockIdx.y: the member's item).
+__global__ void k_setup_planar_many(const SetupItem *it)
+{
+    const SetupItem &I = it[blockIdx.y];
+    to_planar_range(I.buf0, const_cast<double *>(I.ts_static), I.d, 1, I.buf1, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                    (size_t)gridDim.x * blockDim.x);
+}
+__global__ void k_setup_coef_many(const SetupItem *it)
+{
+    const SetupItem &I = it[blockIdx.y];
+    build_coef_cells(I.u, I.m, I.d, I.p, I.coef, I.coefl, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                     (size_t)gridDim.x * blockDim.x);
+}
+__global__ void k_setup_div_many(const SetupItem *it)
+{
+    const SetupItem &I = it[blockIdx.y];
+    build_div_cells(I.d, I.coef, I.coefl, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+__global__ void k_setup_stats_many(const SetupItem *it)
+{
+    const SetupItem &I = it[blockIdx.y];
+    coef_stats_cells(I.d, I.p, I.m, I.u, I.coef, I.cd, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                     (size_t)gridDim.x * blockDim.x);
+}
+__global__ void k_setup_scales_many(const SetupItem *it)
+{
+    const SetupItem &I = it[blockIdx.x];
+    member_scales(I.cd, I.tmax, I.gmax, I.tref, I.d.L, I.scale);
+}
+
+int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t max_cells, cudaStream_t s)
+{
+    for (int q0 = 0; q0 < n; q0 += 65535) {
+        const int nq = std::min(n - q0, 65535);
+        const SetupItem *it = items_dev + q0;
+        const int pb = (int)std::max<size_t>(1, std::min<size_t>((max_elems + 255) / 256, 128));
+        const int cb = (int)std::max<size_t>(1, std::min<size_t>((max_cells + 255) / 256, 64));
+        k_setup_planar_many<<<dim3(pb, nq), 256, 0, s>>>(it);
+        k_setup_coef_many<<<dim3(cb, nq), 256, 0, s>>>(it);
+        k_setup_div_many<<<dim3(cb, nq), 256, 0, s>>>(it);
+        k_setup_stats_many<<<dim3(cb, nq), 256, 0, s>>>(it);
+        k_setup_scales_many<<<nq, 64, 0, s>>>(it);
+        count_launches(5);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
 }
 
 static int planar_copy(double *planar, double *fortran, const Dims &d, int to, cudaStream_t s)

@@ -82,24 +82,34 @@ class Ensemble:
             self._current_tile = tile
         return self._add_now(member, steps, **kw)
 
-    def add_many(self, members, threads: Optional[int] = None, **kw) -> list:
-        """Admit several members; their host-side preparation (patch plan, coefficients,
-        scales) runs in parallel threads, as gb_ens_add allows.  Returns the ids in order."""
-        import os
-        from concurrent.futures import ThreadPoolExecutor
+    def add_many(self, members, **kw) -> list:
+        """Admit several members in one call per tile shape (gb_ens_add_many: host preparation
+        on up to 16 threads inside the library, one synchronisation).  All or nothing per call.
+        Returns the ids in order."""
+        from .abi import GbDims, GbGrid, GbParams
         members = list(members)
         ids = [None] * len(members)
         groups = {}
         for n, m in enumerate(members):
             groups.setdefault(self._tile_for(m), []).append(n)
-        workers = threads or min(16, os.cpu_count() or 1)
-        with ThreadPoolExecutor(max_workers=workers) as ex:
-            for tile, idx in groups.items():
-                if tile != self._current_tile:
-                    self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
-                    self._current_tile = tile
-                for n, mid in zip(idx, ex.map(lambda n: self._add_now(members[n], None, **kw), idx)):
-                    ids[n] = mid
+        dp = C.POINTER(C.c_double)
+        for tile, idx in groups.items():
+            if tile != self._current_tile:
+                self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
+                self._current_tile = tile
+            k = len(idx)
+            refs = [GridRefs(members[n], precision=abi.GB_GO_FP32FLUX, **kw) for n in idx]
+            tss = [np.ascontiguousarray(members[n].ts, dtype=np.float64) for n in idx]
+            us = [np.ascontiguousarray(members[n].u, dtype=np.float64) for n in idx]
+            dims = (GbDims * k)(*[r.dims for r in refs])
+            params = (GbParams * k)(*[r.params for r in refs])
+            grids = (GbGrid * k)(*[r.grid for r in refs])
+            out = (C.c_int32 * k)()
+            self._check(self.lib.gb_ens_add_many(self.e, k, dims, params, grids, (dp * k)(*[dptr(a) for a in tss]),
+                                                 (dp * k)(*[dptr(a) for a in us]), out), "gb_ens_add_many")
+            for n, mid in zip(idx, out):
+                ids[n] = int(mid)
+                self.members[int(mid)] = members[n]
         return ids
 
     def _add_now(self, member, steps, **kw) -> int:
@@ -137,39 +147,33 @@ class Ensemble:
         self._check(self.lib.gb_ens_download(self.e, int(mid), dptr(ts), dptr(rho), dptr(cost)), "gb_ens_download")
         return dict(ts=ts, rho=rho, cost=cost)
 
-    def download_many(self, mids, threads: int = 8, out=None) -> list:
-        """download() of several members from host threads, each with its own CUDA stream
-        (gb_ens_download_stream), so that the device-to-host copies overlap.  `out`: one dict
-        of ts, rho and cost arrays per member to write into (e.g. pinned host memory, which
-        the copies reach without staging); new arrays otherwise."""
-        import queue
-        from concurrent.futures import ThreadPoolExecutor
-        import torch
+    def download_many(self, mids, out=None) -> list:
+        """download() of several members in one call (gb_ens_download_many: one kernel for all,
+        copies queued behind the steps, one synchronisation).  `out`: one dict of ts, rho and
+        cost arrays per member to write into (e.g. pinned host memory, which the copies reach
+        without staging); new arrays otherwise."""
         mids = list(mids)
-        dev = torch.device("cuda", self.device if self.device >= 0 else torch.cuda.current_device())
-        free = queue.Queue()
-        for _ in range(threads):
-            free.put(torch.cuda.Stream(device=dev))
-        dst = dict(zip(mids, out)) if out is not None else {}
-
-        def one(mid):
+        outs = []
+        for n, mid in enumerate(mids):
             m = self.members[mid]
-            if mid in dst:
-                ts, rho, cost = dst[mid]["ts"], dst[mid]["rho"], dst[mid]["cost"]
-                for a, ref in ((ts, m.ts), (rho, m.rho), (cost, m.cost)):
+            if out is not None:
+                o = out[n]
+                for key, ref in (("ts", m.ts), ("rho", m.rho), ("cost", m.cost)):
+                    a = o[key]
                     if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
                         raise ValueError("download_many: output arrays must match the member's shapes (float64, C order)")
+                outs.append(o)
             else:
-                ts, rho, cost = np.empty_like(m.ts), np.empty_like(m.rho), np.empty_like(m.cost)
-            st = free.get()
-            try:
-                self._check(self.lib.gb_ens_download_stream(self.e, int(mid), C.c_void_p(st.cuda_stream), dptr(ts),
-                                                            dptr(rho), dptr(cost)), "gb_ens_download_stream")
-            finally:
-                free.put(st)
-            return dict(ts=ts, rho=rho, cost=cost)
-        with ThreadPoolExecutor(max_workers=threads) as ex:
-            return list(ex.map(one, mids))
+                outs.append(dict(ts=np.empty_like(m.ts), rho=np.empty_like(m.rho), cost=np.empty_like(m.cost)))
+        n = len(mids)
+        if n == 0:
+            return outs
+        dp = C.POINTER(C.c_double)
+        ids = (C.c_int32 * n)(*mids)
+        arr = {key: (dp * n)(*[dptr(o[key]) for o in outs]) for key in ("ts", "rho", "cost")}
+        self._check(self.lib.gb_ens_download_many(self.e, n, ids, arr["ts"], arr["rho"], arr["cost"]),
+                    "gb_ens_download_many")
+        return outs
 
     def inventory(self, mid: int) -> np.ndarray:
         out = np.zeros(self.members[mid].maxl)

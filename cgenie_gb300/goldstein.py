@@ -31,8 +31,8 @@ EXPORTED = [
     "gb_go_inventory_noalloc", "gb_go_set_mld_wind", "gb_go_download_mld",
     "gb_go_sync", "gb_go_errstr", "gb_go_last_error", "gb_go_kernel_launch_count",
     "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
-    "gb_ens_add", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
-    "gb_ens_remaining", "gb_ens_download", "gb_ens_download_stream", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
+    "gb_ens_add", "gb_ens_add_many", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
+    "gb_ens_remaining", "gb_ens_download", "gb_ens_download_many", "gb_ens_download_stream", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
     "gb_ens_count", "gb_ens_last_error",
     "gb_bg_create", "gb_bg_destroy", "gb_bg_columns", "gb_bg_upload", "gb_bg_set_increments",
     "gb_bg_tracercoupling", "gb_bg_download", "gb_bg_last_error",
@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_member_bytes.argtypes = [P(GbDims), P(GbParams)]
     L.gb_ens_member_bytes.restype = C.c_size_t
     L.gb_ens_add.argtypes = [vp, P(GbDims), P(GbParams), P(GbGrid), dp, dp, ip]
+    L.gb_ens_add_many.argtypes = [vp, C.c_int32, P(GbDims), P(GbParams), P(GbGrid), P(dp), P(dp), ip]
     L.gb_ens_remove.argtypes = [vp, C.c_int32]
     L.gb_ens_step.argtypes = [vp, C.c_int32]
     L.gb_ens_set_remaining.argtypes = [vp, C.c_int32, C.c_int64]
@@ -103,6 +104,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_remaining.argtypes = [vp, C.c_int32, P(C.c_int64)]
     L.gb_ens_download.argtypes = [vp, C.c_int32, dp, dp, dp]
     L.gb_ens_download_stream.argtypes = [vp, C.c_int32, vp, dp, dp, dp]
+    L.gb_ens_download_many.argtypes = [vp, C.c_int32, ip, P(dp), P(dp), P(dp)]
     L.gb_ens_inventory.argtypes = [vp, C.c_int32, dp]
     L.gb_ens_status.argtypes = [vp, C.c_int32, ip]
     L.gb_ens_sync.argtypes = [vp]

@@ -228,6 +228,15 @@ size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params);
 int  gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params,
                 const gb_go_grid *grid, const double *ts, const double *u,
                 int32_t *member_id);
+/* gb_ens_add for n members in one call: dims[q], params[q], grids[q], ts[q], u[q] describe
+ * member q, whose id goes to ids[q].  The host preparation of the members runs on up to 16
+ * threads, their device set-up (one allocation each, the coefficients and fixed-point scales
+ * built on the device) is queued on the ensemble's stream, and the call returns after one
+ * synchronisation (the caller's arrays are then no longer needed; pinned ts and u are copied
+ * without staging).  All or nothing: on an error no member of the call is admitted. */
+int  gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, const gb_go_params *params,
+                     const gb_go_grid *grids, const double *const *ts, const double *const *u,
+                     int32_t *ids);
 int  gb_ens_remove(gb_ens *e, int32_t member_id);
 
 /* Advance every active member by `nsteps` steps. */
@@ -247,6 +256,12 @@ int  gb_ens_download(gb_ens *e, int32_t member_id, double *ts, double *rho,
  * other gb_ens_* call on the ensemble may overlap them. */
 int  gb_ens_download_stream(gb_ens *e, int32_t member_id, void *cuda_stream, double *ts,
                             double *rho, double *cost);
+/* gb_ens_download for n members at once: one kernel forms every member's arrays, their copies
+ * are queued on the ensemble's stream behind the steps, and the call returns after one
+ * synchronisation.  ts[q], rho[q], cost[q] receive member ids[q] (any of the three pointer
+ * arrays, or entries of them, may be NULL; pinned host buffers are copied to without staging). */
+int  gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, double *const *ts, double *const *rho,
+                          double *const *cost);
 int  gb_ens_inventory(gb_ens *e, int32_t member_id, double *out);
 int  gb_ens_status(gb_ens *e, int32_t member_id, int32_t *status);
 int  gb_ens_sync(gb_ens *e);

@@ -84,6 +84,14 @@ def coefficients(m):
     return c32, lo, cmax
 
 
+def scale_of(g):
+    """floor(log2(2^26 / g)) from the exact binary exponent of g, clamped to [-120, 120]."""
+    if not (g > 0.0) or not math.isfinite(g):
+        return 0
+    f, e = math.frexp(g)
+    return max(-120, min(120, 26 - e + (1 if f == 0.5 else 0)))
+
+
 def wet_cells(m):
     kk = np.arange(m.maxk + 2)[:, None, None]
     wet = (kk >= m.k1[None]) & (kk >= 1) & (kk <= m.maxk)
@@ -115,8 +123,7 @@ def scales(m, ts, cmax, tref=None, dmax=0.0):
         off = 0.0 if tref is None else float(tref[l])
         tmax = np.max(np.abs(ts[..., l][wet] - off)) if wet.any() else 0.0
         g = max(2.0 * cmax * tmax, abs(off) * dmax)
-        s = int(math.floor(math.log2(67108864.0 / g))) if g > 0 else 0
-        out.append(max(-120, min(120, s)))
+        out.append(scale_of(g))
     return out
 
 

@@ -295,14 +295,15 @@ def test_fp32_velocity_updates_on_device(gpu_lib, oracle):
 
 
 def test_ensemble_parallel_admission_equals_serial(gpu_lib):
-    """Members admitted from several host threads at once (add_many) step to the same
-    result, bit for bit, as members admitted one by one."""
+    """Members admitted in one batched call (add_many: host preparation on several threads,
+    device set-up batched) step to the same result, bit for bit, as members admitted one by
+    one."""
     from cgenie_gb300.ensemble import Ensemble
     mems = [grid.make_member(c) for c in grid.ensemble_configs(n=12, seed=21)]
     a = Ensemble(use_graph=True)
     ids_a = [a.add(m) for m in mems]
     b = Ensemble(use_graph=True)
-    ids_b = b.add_many(mems, threads=8)
+    ids_b = b.add_many(mems)
     assert len(set(ids_b)) == len(mems)
     a.step(15)
     b.step(15)
@@ -314,17 +315,27 @@ def test_ensemble_parallel_admission_equals_serial(gpu_lib):
     b.close()
 
 
-def test_ensemble_parallel_download_equals_serial(gpu_lib):
-    """download_many (host threads, one CUDA stream each, ordered after the steps) returns
-    the same arrays as download."""
+def test_ensemble_batched_download_equals_export_path(gpu_lib):
+    """download_many (gb_ens_download_many: one kernel for all members, copies queued behind the
+    steps, one synchronisation; into new or caller-given arrays) returns what the
+    export-then-merge path of gb_ens_download_stream returns, bit for bit, for ts, rho and
+    cost."""
+    from cgenie_gb300.abi import dptr
     from cgenie_gb300.ensemble import Ensemble
     mems = [grid.make_member(c) for c in grid.ensemble_configs(n=9, seed=23)]
+    mems.append(grid.make_member(grid.MemberConfig(maxi=15, maxj=12, maxk=10, maxl=3, seed=62, ieos=1, iconv=1,
+                                                   noise=2.0)))
     e = Ensemble(use_graph=True)
     ids = e.add_many(mems)
     e.step(12)
-    par = e.download_many(ids, threads=4)
-    for i, p in zip(ids, par):
-        s = e.download(i)
+    par = e.download_many(ids)
+    given = [dict(ts=np.zeros_like(m.ts), rho=np.zeros_like(m.rho), cost=np.zeros_like(m.cost)) for m in mems]
+    e.download_many(ids, out=given)
+    for i, m, p, g in zip(ids, mems, par, given):
+        s = dict(ts=np.empty_like(m.ts), rho=np.empty_like(m.rho), cost=np.empty_like(m.cost))
+        rc = e.lib.gb_ens_download_stream(e.e, int(i), None, dptr(s["ts"]), dptr(s["rho"]), dptr(s["cost"]))
+        assert rc == 0
         for k in ("ts", "rho", "cost"):
             assert np.array_equal(s[k], p[k]), k
+            assert np.array_equal(s[k], g[k]), k
     e.close()
