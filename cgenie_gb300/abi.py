@@ -60,19 +60,22 @@ class GbParams(C.Structure):
     ]
 
 
+_vp = C.c_void_p   # array addresses (const double * / const int32_t * in C); set from numpy addresses
+
+
 class GbGrid(C.Structure):
     _fields_ = [
-        ("rc", _dp), ("rc2", _dp), ("cv", _dp),
-        ("cv2", _dp), ("dsv", _dp), ("rdsv", _dp),
-        ("ds", _dp), ("rds", _dp),
-        ("dz", _dp), ("dza", _dp), ("rdz", _dp), ("rdza", _dp), ("zro", _dp), ("dt", _dp),
-        ("zw", _dp),
-        ("ssmax", _dp),
-        ("ediff1", _dp),
-        ("diffmax", _dp),
-        ("k1", _ip),
+        ("rc", _vp), ("rc2", _vp), ("cv", _vp),
+        ("cv2", _vp), ("dsv", _vp), ("rdsv", _vp),
+        ("ds", _vp), ("rds", _vp),
+        ("dz", _vp), ("dza", _vp), ("rdz", _vp), ("rdza", _vp), ("zro", _vp), ("dt", _vp),
+        ("zw", _vp),
+        ("ssmax", _vp),
+        ("ediff1", _vp),
+        ("diffmax", _vp),
+        ("k1", _vp),
         ("dphi", C.c_double), ("rdphi", C.c_double),
-        ("mlddec", _dp), ("mlddecd", _dp), ("mldketau", _dp),
+        ("mlddec", _vp), ("mlddecd", _vp), ("mldketau", _vp),
     ]
 
 
@@ -172,12 +175,8 @@ class GridRefs:
         p.reserved = 0
         self.params = p
         g = GbGrid()
-        for name in ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza",
-                     "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
-            setattr(g, name, dptr(self.arrays[name]))
-        g.k1 = iptr(self.arrays["k1"])
-        for name in ("mlddec", "mlddecd", "mldketau"):
-            setattr(g, name, dptr(self.arrays[name]))
+        for name, a in self.arrays.items():     # contiguous float64 (k1: int32) or None
+            setattr(g, name, None if a is None else a.__array_interface__["data"][0])
         g.dphi = float(m.dphi)
         g.rdphi = float(m.rdphi)
         self.grid = g

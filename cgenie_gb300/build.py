@@ -32,6 +32,7 @@ SOURCES = {
     "surface_step.cu": ["-fmad=false"],
     "momentum.cu": ["-fmad=false"],
     "restart.cu": ["-fmad=false"],
+    "timeseries.cu": ["-fmad=false"],
 }
 
 

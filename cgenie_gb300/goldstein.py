@@ -43,6 +43,7 @@ EXPORTED = [
     "gb_mo_last_error",
     "gb_rs_write_goldstein", "gb_rs_pack_goldstein", "gb_rs_write_fields", "gb_rs_read_goldstein", "gb_rs_goldstein_name",
     "gb_rs_calendar_step", "gb_rs_calendar_after_read", "gb_rs_last_error",
+    "gb_ts_create", "gb_ts_destroy", "gb_ts_diagnose", "gb_ts_format", "gb_ts_last_error",
 ]
 
 _lib = None
@@ -95,6 +96,14 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_set_stream.argtypes = [vp, vp]
     L.gb_ens_member_bytes.argtypes = [P(GbDims), P(GbParams)]
     L.gb_ens_member_bytes.restype = C.c_size_t
+    L.gb_ts_create.argtypes = [P(GbDims), P(GbGrid), vp, C.c_int, P(vp)]
+    L.gb_ts_destroy.argtypes = [vp]
+    L.gb_ts_destroy.restype = None
+    L.gb_ts_diagnose.argtypes = [vp, vp, dp, dp, dp, dp, ip, dp, dp, dp]
+    L.gb_ts_format.argtypes = [C.c_double, C.c_int32, dp, C.c_double, C.c_double, dp, ip, C.c_double,
+                               C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]
+    L.gb_ts_last_error.argtypes = [vp]
+    L.gb_ts_last_error.restype = C.c_char_p
     L.gb_ens_add.argtypes = [vp, P(GbDims), P(GbParams), P(GbGrid), dp, dp, ip]
     L.gb_ens_add_many.argtypes = [vp, C.c_int32, P(GbDims), P(GbParams), P(GbGrid), P(dp), P(dp), ip]
     L.gb_ens_remove.argtypes = [vp, C.c_int32]

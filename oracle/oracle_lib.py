@@ -24,7 +24,7 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the oracle (make -C oracle)."""
     srcs = [os.path.join(HERE, f) for f in ("goldstein_oracle.c", "biogem_oracle.c", "surface_oracle.c",
-                                             "momentum_oracle.c")]
+                                             "momentum_oracle.c", "timeseries_oracle.c")]
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
@@ -77,6 +77,11 @@ def lib():
         L.gbo_mo_set_velocity.restype = None
         L.gbo_mo_free.argtypes = [C.c_void_p]
         L.gbo_mo_free.restype = None
+        from cgenie_gb300.timeseries import GbTsBasins
+        L.gbo_diag2.argtypes = [P(GbDims), P(GbGrid), P(GbTsBasins), dp, dp, dp, dp, dp, dp]
+        L.gbo_diag2.restype = C.c_int
+        L.gbo_diagopsi.argtypes = [P(GbDims), P(GbGrid), P(GbTsBasins), dp, dp, dp, dp, dp, P(C.c_int32)]
+        L.gbo_diagopsi.restype = C.c_int
         _lib = L
     return _lib
 
@@ -230,3 +235,22 @@ class OracleMomentum:
         erisl = np.zeros((c.isles + 1, c.isles))
         lib().gbo_mo_get_islands(self.s, dptr(psisl), dptr(ubisl), dptr(erisl))
         return psisl, ubisl, erisl
+
+
+def timeseries(m, ts, rho, u, basins):
+    """diag2 and diagopsi of the oracle (oracle/timeseries_oracle.c) on Fortran-layout arrays."""
+    r = GridRefs(m)
+    cb = basins.c()
+    sums = np.zeros(8 * m.maxl)
+    avn, avs = C.c_double(), C.c_double()
+    shape = (m.maxk + 1, m.maxj + 1)
+    ops = [np.zeros(shape) for _ in range(3)]
+    ext = np.zeros(4)
+    iposa = np.zeros(2, np.int32)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (ts, rho, u)]
+    lib().gbo_diag2(C.byref(r.dims), C.byref(r.grid), C.byref(cb), dptr(a[0]), dptr(a[1]), dptr(a[2]), dptr(sums),
+                    C.byref(avn), C.byref(avs))
+    lib().gbo_diagopsi(C.byref(r.dims), C.byref(r.grid), C.byref(cb), dptr(a[2]), *[dptr(o) for o in ops], dptr(ext),
+                       iptr(iposa))
+    return dict(sums=sums, avn=avn.value, avs=avs.value, ext=ext, iposa=iposa, opsi=ops[0], opsip=ops[1], opsia=ops[2])
+

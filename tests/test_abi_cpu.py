@@ -13,10 +13,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     names = set()
-    for h in ("gb_goldstein.h", "gb_biogem.h", "gb_embm.h", "gb_momentum.h", "gb_restart.h"):
+    for h in sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo|rs)_[a-z0-9_]+)\s*\(", src))
+        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo|rs|ts)_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 
