@@ -20,6 +20,8 @@ Workloads (seeded synthetic members with the reference's grid formulas):
   ocean36 the device-resident ocean step of a 36x36x16 basin with 8 tracers: momentum, then
       tstepo (split-precision form), and the BIOGEM tracer coupling every 5th step; `value` is
       tracer cell-updates/s of the whole step
+  ocean5 the same ocean step at the stress-test size, 360x180x32 with 24 tracers (65,160
+      streamfunction points: the block-tridiagonal streamfunction solve)
   mo36 the momentum step (wind, jbar, streamfunction, islands, velc) of a 36x36x16 basin
       with two islands, on the density of an FP64 handle; `value` is wet-cell momentum
       updates/s (each wet cell's u, v, w advanced one step)
@@ -69,6 +71,8 @@ WORKLOADS = {
     "rs5s": dict(name="goldstein_restart_write_360x180x32_L2", factory="config_c5", maxl=2),
     "ocean36": dict(name="ocean_step_36x36x16_L8_momentum_tracers_biogem", maxi=36, maxj=36, maxk=16, maxl=8,
                     couple_every=5),
+    "ocean5": dict(name="ocean_step_360x180x32_L24_momentum_tracers_biogem", maxi=360, maxj=180, maxk=32, maxl=24,
+                   couple_every=5, cpu_steps=3),
 }
 
 
@@ -749,7 +753,7 @@ def run_ocean(args, rank, world, local, dist):
         if serving is not None:
             line["serving"] = serving
         if not args.no_cpu_baseline:
-            v, n, _ = ocean_cpu_rate(w, 20)
+            v, n, _ = ocean_cpu_rate(w, w.get("cpu_steps", 20))
             line["cpu_baseline"] = {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
                                     "sample": f"{n} ocean steps (momentum, tracer step, coupling), oracle C "
                                               f"restatements, serial"}
@@ -785,8 +789,8 @@ def ocean_cpu_rate(w, steps):
 
 def run_reference(args, rank, world):
     w = dict(WORKLOADS[args.workload])
-    if args.workload == "ocean36":
-        v, n, dt = ocean_cpu_rate(w, max(5, min(args.steps, 50)))
+    if args.workload in ("ocean36", "ocean5"):
+        v, n, dt = ocean_cpu_rate(w, w.get("cpu_steps", max(5, min(args.steps, 50))))
         line = {
             "metric": "tracer cell-updates/s", "value": v, "unit": "tracer cell-updates/s", "impl": "reference",
             "n_gpus": world, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True,
@@ -1013,17 +1017,13 @@ def run_c3(args, rank, world, local, dist):
         g.close()
     plain_value = plain_cu / plain_s
 
-    # ---- end to end through the C-ABI: admit from pinned host arrays, step, download every
-    # member into pinned host arrays (the host buffers exist before the timed region)
+    # ---- end to end through the C-ABI: admit from mapped pinned host arrays (gb_ens_host_alloc),
+    # step, download every member into such arrays (the host buffers exist before the timed region)
     import dataclasses
-
-    def pinned(a):
-        p = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
-        p[...] = a
-        return p
-    hmems = [dataclasses.replace(m, ts=pinned(m.ts), u=pinned(m.u)) for m in mems]
-    houts = [dict(ts=pinned(np.zeros_like(m.ts)), rho=pinned(np.zeros_like(m.rho)), cost=pinned(np.zeros_like(m.cost)))
-             for m in mems]
+    from cgenie_gb300.ensemble import host_copy
+    hmems = [dataclasses.replace(m, ts=host_copy(m.ts), u=host_copy(m.u)) for m in mems]
+    houts = [dict(ts=host_copy(np.zeros_like(m.ts)), rho=host_copy(np.zeros_like(m.rho)),
+                  cost=host_copy(np.zeros_like(m.cost))) for m in mems]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -1084,8 +1084,8 @@ def run_c3(args, rank, world, local, dist):
                                    "over wet cells, against each member's FP64 run (the reference arithmetic)"},
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "parts": e2e_parts,
-                    "note": f"whole job through the C-ABI: admit {w['members']} members from pinned host arrays, "
-                            f"{args.steps} steps, download every member into pinned host arrays"},
+                    "note": f"whole job through the C-ABI: admit {w['members']} members from mapped pinned host arrays, "
+                            f"{args.steps} steps, download every member into mapped pinned host arrays"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
@@ -1148,7 +1148,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    if args.workload == "ocean36":
+    if args.workload in ("ocean36", "ocean5"):
         run_ocean(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()

@@ -127,6 +127,15 @@ class GbEnsTuning(C.Structure):
                 ("use_graph", C.c_int32)]
 
 
+def addr(a: np.ndarray) -> int:
+    """Address of a contiguous array's first element (ctypes' buffer view for writable arrays,
+    a third of the cost of __array_interface__)."""
+    try:
+        return C.addressof(C.c_char.from_buffer(a))
+    except (TypeError, ValueError):
+        return a.__array_interface__["data"][0]
+
+
 def dptr(a: np.ndarray):
     """Pointer to a contiguous float64 numpy array (None -> NULL)."""
     if a is None:
@@ -146,37 +155,30 @@ class GridRefs:
     """Owns contiguous copies of a member's metric arrays and the ctypes structs
     that point at them."""
 
+    _F64 = ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza", "zro", "dt", "zw",
+            "ssmax", "ediff1", "diffmax")
+    _MLD = ("mlddec", "mlddecd", "mldketau")
+
     def __init__(self, m, *, diso=None, ieos=None, iconv=None, iediff=None, imld=None, precision=GB_GO_FP64):
         cfg = m.cfg
-        self.arrays = {}
-        for name in ("rc", "rc2", "cv", "cv2", "dsv", "rdsv", "ds", "rds", "dz", "dza", "rdz", "rdza",
-                     "zro", "dt", "zw", "ssmax", "ediff1", "diffmax"):
-            self.arrays[name] = np.ascontiguousarray(getattr(m, name), dtype=np.float64)
-        self.arrays["k1"] = np.ascontiguousarray(m.k1, dtype=np.int32)
-        for name in ("mlddec", "mlddecd", "mldketau"):
+        f64 = np.float64
+        asc = np.ascontiguousarray
+        arrays = {name: asc(getattr(m, name), dtype=f64) for name in self._F64}
+        arrays["k1"] = asc(m.k1, dtype=np.int32)
+        for name in self._MLD:
             v = getattr(m, name, None)
-            self.arrays[name] = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+            arrays[name] = None if v is None else asc(v, dtype=f64)
+        self.arrays = arrays
         self.dims = GbDims(m.maxi, m.maxj, m.maxk, m.maxl)
-        p = GbParams()
-        p.diff[0], p.diff[1] = float(m.diff[0]), float(m.diff[1])
-        for n in range(5):
-            p.ec[n] = float(m.ec[n])
-        p.ediff0 = float(m.ediff0)
-        p.ediffpow2 = float(m.ediffpow2)
-        p.dsc = 5.0e3
-        p.ieos = int(cfg.ieos if ieos is None else ieos)
-        p.iediff = int(cfg.iediff if iediff is None else iediff)
-        p.ediffpow2i = int(m.ediffpow2i)
-        p.iconv = int(cfg.iconv if iconv is None else iconv)
-        p.imld = int(getattr(cfg, "imld", 0) if imld is None else imld)
-        p.mldpebuoycoeff = float(getattr(cfg, "mldpebuoycoeff", 0.15))
-        p.diso = int(bool(cfg.diso if diso is None else diso))
-        p.precision = int(precision)
-        p.reserved = 0
-        self.params = p
-        g = GbGrid()
-        for name, a in self.arrays.items():     # contiguous float64 (k1: int32) or None
-            setattr(g, name, None if a is None else a.__array_interface__["data"][0])
-        g.dphi = float(m.dphi)
-        g.rdphi = float(m.rdphi)
-        self.grid = g
+        diff, ec = m.diff, m.ec
+        self.params = GbParams(
+            diff=(C.c_double * 2)(float(diff[0]), float(diff[1])), ec=(C.c_double * 5)(*[float(x) for x in ec[:5]]),
+            ediff0=float(m.ediff0), ediffpow2=float(m.ediffpow2), dsc=5.0e3,
+            ieos=int(cfg.ieos if ieos is None else ieos), iediff=int(cfg.iediff if iediff is None else iediff),
+            ediffpow2i=int(m.ediffpow2i), iconv=int(cfg.iconv if iconv is None else iconv),
+            imld=int(getattr(cfg, "imld", 0) if imld is None else imld),
+            diso=int(bool(cfg.diso if diso is None else diso)), precision=int(precision), reserved=0,
+            mldpebuoycoeff=float(getattr(cfg, "mldpebuoycoeff", 0.15)))
+        ptr = {name: (None if a is None else addr(a)) for name, a in arrays.items()}   # contiguous, or None
+        self.grid = GbGrid(*[ptr[name] for name in self._F64], ptr["k1"], float(m.dphi), float(m.rdphi),
+                           *[ptr[name] for name in self._MLD])

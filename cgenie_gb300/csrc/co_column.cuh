@@ -10,6 +10,7 @@
 //                  double &R(int lev);   (rho of this column, levels 0..maxk)
 #pragma once
 
+#include "gb_fp32.h"
 #include "gb_internal.h"
 
 namespace gbgo {
@@ -527,6 +528,133 @@ __device__ inline int co_warp32(double *tv, const EosCoef &ec, int maxk, int L, 
             wc[(size_t)lev * lstride] = tv[lev * 32 + lane];
         }
     return __popc(fillm);
+}
+
+// ---------------------------------------------------------------------------
+// Kraus-Turner mixed layer (imld = 1) of one wet column, with explicit round-to-nearest
+// intrinsics like co above, so that the FP32-flux form applies the reference's arithmetic
+// (and the same operation order as the FP64 drop-in kernel) to its FP64 state.
+//   energy of the surface forcing    goldstein.f90:2294-2309
+//   energy released by co, decision  goldstein.f90:2336-2389
+//   krausturner                      goldstein.f90:3337-3442
+// Level-pair depth grids of goldstein.f90:1013-1025: dzg(k,kk) = zw(k) - zw(kk-1),
+// z2dzg(k,kk) = -zw(k)^2 + zw(kk-1)^2, rdzg(k,kk) = 1/dzg(k,kk) (1e10 where k = kk-1).
+
+struct MixedLayerArgs {
+    const double *zw, *zro, *dz;        // Fortran-indexed k metrics
+    const double *mlddec, *mlddecd;     // [1..maxk]
+    double mldpebuoycoeff;
+    double ketau;                       // the column's wind mixing energy
+    double pe1;                         // the column's mldpe1 (forcing energy over the top layer)
+};
+
+__device__ __forceinline__ double ml_dzg(const double *zw, int k, int kk) { return __dadd_rn(zw[k], -zw[kk - 1]); }
+__device__ __forceinline__ double ml_z2dzg(const double *zw, int k, int kk)
+{
+    return __dadd_rn(__dmul_rn(-zw[k], zw[k]), __dmul_rn(zw[kk - 1], zw[kk - 1]));
+}
+__device__ __forceinline__ double ml_rdzg(const double *zw, int k, int kk)
+{
+    return k != kk - 1 ? __ddiv_rn(1.0, ml_dzg(zw, k, kk)) : 1.0E10;
+}
+
+// mldpe1 of goldstein.f90:2294-2309: the density change of the top layer when the step's
+// surface forcing is taken out of its start-of-step T and S (tt, st), against the density
+// the previous step left there (rho_prev), times z2dzg(maxk, maxk)
+__device__ __forceinline__ double ml_pe1(const EosCoef &ec, double tt, double st, double rho_prev, const double *zw,
+                                         const double *zro, int maxk)
+{
+    const double r = eos_rn(ec, tt, st, zro[maxk]);
+    return __dmul_rn(__dadd_rn(r, -rho_prev), ml_z2dzg(zw, maxk, maxk));
+}
+
+// krausturner on one column (tvkl = k1, every level it touches is wet)
+template <class Col>
+__device__ void kraus_turner_rn(Col &col, const EosCoef &ec, int maxk, int L, int tvkl, const MixedLayerArgs &a,
+                                double pebuoy, double *mld, int32_t *mldk)
+{
+    const double *zw = a.zw, *dz = a.dz;
+    double qmix[kFp32MaxL];
+    const int mldpk = maxk;   // the routine's first statement (goldstein.f90:3350)
+    int k = mldpk, partmix = 1;
+    double empe = pebuoy;
+    double emke = __dmul_rn(a.ketau, a.mlddec[k]);
+    double em = __dadd_rn(empe, emke);
+    double eneed = 0.0;
+    double tmix = col.T(0, k), smix = col.T(1, k);
+    double rhou = 0.0, rhol = 0.0;
+    for (int l = 0; l < L; ++l) qmix[l] = col.T(l, k);
+    double rhomix = eos_rn(ec, tmix, smix, zw[k]);
+    while (eneed < em && em > 0) {
+        if (k < mldpk) {
+            qmix[0] = tmix;
+            qmix[1] = smix;
+            const double r = ml_rdzg(zw, maxk, k), g = ml_dzg(zw, maxk, k + 1);
+            for (int l = 2; l < L; ++l) qmix[l] = __dmul_rn(r, __dadd_rn(__dmul_rn(qmix[l], g), __dmul_rn(col.T(l, k), dz[k])));
+        }
+        if (k == tvkl) {
+            *mldk = k;
+            *mld = zw[k - 1];
+            partmix = 0;
+            em = -1.0E-8;
+            if (k < maxk)
+                for (int l = 0; l < L; ++l)
+                    for (int n = k; n <= maxk; ++n) col.setT(l, n, qmix[l]);
+        } else {
+            k = k - 1;
+            const double emr = __ddiv_rn(__dadd_rn(em, -eneed), em);
+            empe = __dmul_rn(empe, emr);
+            emke = __dmul_rn(__dmul_rn(emke, emr), a.mlddecd[k]);
+            em = __dadd_rn(empe, emke);
+            rhou = ec.ieos != 0 ? eos_rn(ec, tmix, smix, zw[k]) : rhomix;
+            const double r = ml_rdzg(zw, maxk, k), g = ml_dzg(zw, maxk, k + 1);
+            tmix = __dmul_rn(r, __dadd_rn(__dmul_rn(tmix, g), __dmul_rn(col.T(0, k), dz[k])));
+            smix = __dmul_rn(r, __dadd_rn(__dmul_rn(smix, g), __dmul_rn(col.T(1, k), dz[k])));
+            rhol = eos_rn(ec, col.T(0, k), col.T(1, k), zw[k]);
+            rhomix = eos_rn(ec, tmix, smix, zw[k]);
+            eneed = __dadd_rn(__dadd_rn(__dmul_rn(ml_z2dzg(zw, maxk, k + 1), rhou), __dmul_rn(ml_z2dzg(zw, k, k), rhol)),
+                              -__dmul_rn(ml_z2dzg(zw, maxk, k), rhomix));
+        }
+    }
+    if (partmix == 1 && em > 0) {
+        *mldk = k;
+        const double mlda = __ddiv_rn(__dmul_rn(__dmul_rn(ml_dzg(zw, maxk, k + 1), ml_rdzg(zw, maxk, k)), em), eneed);
+        const double mldb = __dmul_rn(__dadd_rn(__dmul_rn(ml_dzg(zw, maxk, k), ml_rdzg(zw, maxk, k + 1)), -1.0), mlda);
+        for (int l = 0; l < L; ++l) {
+            const double below = col.T(l, k);
+            const double surf = __dadd_rn(__dmul_rn(__dadd_rn(1.0, -mldb), qmix[l]), __dmul_rn(mldb, below));
+            col.setT(l, maxk, surf);
+            for (int n = k + 1; n <= maxk - 1; ++n) col.setT(l, n, surf);
+            col.setT(l, k, __dadd_rn(__dmul_rn(mlda, qmix[l]), __dmul_rn(__dadd_rn(1.0, -mlda), below)));
+        }
+        *mld = k < maxk ? __dadd_rn(zw[k], __ddiv_rn(em, __dmul_rn(zw[k], __dadd_rn(rhol, -rhou)))) : 0.0;
+    } else if (partmix == 1 && k < maxk) {
+        *mldk = k + 1;
+        *mld = zw[k];
+    }
+}
+
+// The mixed-layer part of tstepo after co (goldstein.f90:2336-2389) on one wet column: the
+// potential energy co released (rold: the densities before co, levels 1..maxk), the wind
+// energy, then krausturner or the shallow-layer diagnostic.
+template <class Col>
+__device__ void mixed_layer_rn(Col &col, const EosCoef &ec, int maxk, int L, int k1, const MixedLayerArgs &a,
+                               const double *rold, double *mld, int32_t *mldk)
+{
+    double peconv = 0.0;
+    for (int k = maxk; k > 0; --k) {
+        const double rnew = eos_rn(ec, col.T(0, k), col.T(1, k), a.zro[k]);
+        peconv = __dadd_rn(peconv, __dmul_rn(__dadd_rn(rnew, -rold[k]), ml_z2dzg(a.zw, k, k)));
+    }
+    double pebuoy = __dadd_rn(peconv, a.pe1);
+    if (pebuoy > 0.0) pebuoy = __dmul_rn(pebuoy, a.mldpebuoycoeff);
+    const double emix = __dadd_rn(pebuoy, __dmul_rn(a.ketau, a.mlddec[maxk]));
+    if (emix > 0.0) {
+        kraus_turner_rn(col, ec, maxk, L, k1, a, pebuoy, mld, mldk);
+    } else {
+        *mldk = maxk;
+        *mld = a.pe1 < 0 ? __dmul_rn(a.zw[maxk - 1], __dadd_rn(1.0, -__ddiv_rn(emix, a.pe1))) : a.zw[maxk - 1];
+    }
 }
 
 }  // namespace gbgo

@@ -40,6 +40,134 @@ namespace {
 
 __global__ void k_add_step(long long *ctr, long long n) { *ctr += n; }
 
+// ---------------------------------------------------------------------------
+// mapped host memory
+//
+// gb_ens_host_alloc's allocations (page-locked, mapped) are registered by address range, so a
+// call can tell whether a caller's array lies inside one and then let its batched kernel read or
+// write it through the device address (over NVLink-C2C on Grace) instead of issuing one copy
+// call per array.  The staging arena of admission is such an allocation too: the members' host
+// segments are gathered there and the scatter kernel copies them into the member blocks.
+
+struct HostRange {
+    size_t bytes;
+    uintptr_t dev;
+};
+
+std::mutex &host_mu()
+{
+    static std::mutex m;
+    return m;
+}
+
+std::map<uintptr_t, HostRange> &host_ranges()
+{
+    static std::map<uintptr_t, HostRange> r;
+    return r;
+}
+
+// The device address of [p, p + bytes) when the range lies inside one registered allocation.
+void *host_mapped(const void *p, size_t bytes)
+{
+    if (!p) return nullptr;
+    std::lock_guard<std::mutex> lk(host_mu());
+    auto &r = host_ranges();
+    auto it = r.upper_bound((uintptr_t)p);
+    if (it == r.begin()) return nullptr;
+    --it;
+    const uintptr_t a = (uintptr_t)p;
+    if (a < it->first || a + bytes > it->first + it->second.bytes) return nullptr;
+    return (void *)(it->second.dev + (a - it->first));
+}
+
+int host_alloc(size_t bytes, void **out, void **dev)
+{
+    void *p = nullptr, *d = nullptr;
+    cudaError_t x = cudaHostAlloc(&p, bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (x != cudaSuccess) return x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
+    x = cudaHostGetDevicePointer(&d, p, 0);
+    if (x != cudaSuccess) {
+        cudaFreeHost(p);
+        return GB_GO_ECUDA;
+    }
+    {
+        std::lock_guard<std::mutex> lk(host_mu());
+        host_ranges()[(uintptr_t)p] = HostRange{bytes, (uintptr_t)d};
+    }
+    *out = p;
+    if (dev) *dev = d;
+    return GB_GO_OK;
+}
+
+int host_free(void *p)
+{
+    {
+        std::lock_guard<std::mutex> lk(host_mu());
+        auto it = host_ranges().find((uintptr_t)p);
+        if (it == host_ranges().end()) return GB_GO_EINVAL;
+        host_ranges().erase(it);
+    }
+    return cudaFreeHost(p) == cudaSuccess ? GB_GO_OK : GB_GO_ECUDA;
+}
+
+// The process's admission staging arena (grown on demand, kept): one admission call at a time
+// holds `mu` from the gathering of its segments until its synchronisation.
+struct StagingArena {
+    std::mutex mu;
+    char *host = nullptr;
+    char *dev = nullptr;
+    size_t bytes = 0;
+};
+
+StagingArena &staging_arena()
+{
+    static StagingArena a;
+    return a;
+}
+
+// At least `bytes` of arena (caller holds its mutex); false when page-locked memory is short.
+bool arena_reserve(StagingArena &a, size_t bytes)
+{
+    if (a.bytes >= bytes) return true;
+    if (a.host) host_free(a.host);
+    a.host = a.dev = nullptr;
+    a.bytes = 0;
+    const size_t want = std::max(bytes, (size_t)1 << 24);
+    void *h = nullptr, *d = nullptr;
+    if (host_alloc(want, &h, &d) != GB_GO_OK) return false;
+    a.host = (char *)h;
+    a.dev = (char *)d;
+    a.bytes = want;
+    return true;
+}
+
+// One copy of the batched admission: `bytes` from src (device or mapped host address) to dst;
+// src NULL: zero fill.
+struct CopySeg {
+    const void *src;
+    void *dst;
+    unsigned long long bytes;
+};
+
+// Segment blockIdx.y, grid-stride over 16-byte words when the addresses and size allow,
+// else over 8-byte words (the segments are arrays of doubles or 256-byte aligned blocks).
+__global__ void __launch_bounds__(256) k_scatter(const CopySeg *segs)
+{
+    const CopySeg g = segs[blockIdx.y];
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, ts = (size_t)gridDim.x * blockDim.x;
+    if ((((uintptr_t)g.src | (uintptr_t)g.dst | g.bytes) & 15) == 0) {
+        const size_t n = g.bytes / 16;
+        const uint4 *s = (const uint4 *)g.src;
+        uint4 *d = (uint4 *)g.dst;
+        for (size_t w = t0; w < n; w += ts) d[w] = s ? s[w] : make_uint4(0u, 0u, 0u, 0u);
+    } else {
+        const size_t n = g.bytes / 8;
+        const unsigned long long *s = (const unsigned long long *)g.src;
+        unsigned long long *d = (unsigned long long *)g.dst;
+        for (size_t w = t0; w < n; w += ts) d[w] = s ? s[w] : 0ull;
+    }
+}
+
 struct Member {
     int id = -1;
     Dims d{};
@@ -58,6 +186,9 @@ struct Member {
     int32_t *ptab = nullptr;              // patch tables
     double *vel = nullptr, *ediff1 = nullptr, *mkd = nullptr;   // iediff: u, ediff1, dza and diffmax
     float *stencil = nullptr;             // diso or iediff: the per-step top-face stencil
+    double *mld = nullptr;                // imld = 1: mixed-layer depth and level per column
+    int32_t *mldk = nullptr;
+    double *mldketau = nullptr;           // imld = 1: wind mixing energy per column
     char *block = nullptr;                // the one device allocation every array above lies in
     double *blob = nullptr;               // metrics (build_metric_blob layout) on the device
     double *tmaxd = nullptr, *gmaxd = nullptr;   // per tracer max |T - tref| and largest forcing transfer
@@ -150,7 +281,8 @@ static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
     // and remainders), forcing, small arrays; patch tables: at most (31 + maxk) words per column
     const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
-           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + (size_t)d->maxl * 4 + 4096;
+           ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + (size_t)d->maxl * 4 +
+           (p && p->imld == 1 ? ncol * 28 + ((size_t)d->maxk + 1) * 16 + 1024 : 0) + 4096;
 }
 
 extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params)
@@ -270,13 +402,24 @@ struct Prepared {
     int wet_cols = 0;
     // device block layout (byte offsets): the copied segment [0, copied), the zeroed segment
     // [copied, zeroed), then the arrays the device fills
-    size_t o_blob, o_mj, o_rvol, o_mk, o_dsj, o_tmax, o_gmax, o_k1, o_tref, o_gtop, o_ptab, o_ediff1, copied;
-    size_t o_rho, o_cost, o_icosd, o_gmaxu, o_diag, o_status, o_cd, o_scale, zeroed;
+    size_t o_blob, o_mj, o_rvol, o_mk, o_dsj, o_tmax, o_gmax, o_k1, o_tref, o_gtop, o_ptab, o_ediff1;
+    size_t o_mlddec, o_mldketau, o_rhos, copied;
+    size_t o_rho, o_cost, o_icosd, o_gmaxu, o_diag, o_status, o_cd, o_scale, o_mld, o_mldk, zeroed;
     size_t o_buf0, o_buf1, o_static, o_stage, o_vel, o_coef, o_coefl, o_stencil, total;
     std::vector<char> host;        // the copied segment
     int rc = GB_GO_OK;
     std::string msg;
 };
+
+// eos (goldstein.f90:3048-3061) in the operation order of the device's eos_rn (the host code is
+// compiled without contraction)
+static double eos_host(const PhysParams &p, double t, double s, double z)
+{
+    const double tt = t * t;
+    double r = ((p.ec[0] * t + p.ec[1] * s) + p.ec[2] * tt) + p.ec[3] * (tt * t);
+    if (p.ieos != 0) r = r + (p.ec[4] * t) * z;
+    return r;
+}
 
 // The patch plan of a member from the ensemble's cache, or the planner's (then cached).
 int cached_plan(gb_ens *e, const Dims &d, const int32_t *k1, const gb_ens_tuning &tuning, PatchPlan &out)
@@ -318,10 +461,6 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     if (dims->maxl > kFp32MaxL) {
         pm.msg = "ensemble members carry at most 32 tracers";
         return pm.rc = GB_GO_ERANGE;
-    }
-    if (params->imld != 0) {
-        pm.msg = "imld=1 not provided in ensembles";
-        return pm.rc = GB_GO_EUNSUPPORTED;
     }
     for (int k = 1; k < dims->maxk; ++k)
         if (grid->dt[k] != grid->dt[0]) {
@@ -378,6 +517,10 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     pm.o_gtop = take(pm.gtop.size() * 4);
     pm.o_ptab = take(std::max<size_t>(4, pm.plan.words.size()) * 4);
     pm.o_ediff1 = take(std::max<size_t>(1, ned) * 8);
+    const bool mldon = params->imld == 1;
+    pm.o_mlddec = take(mldon ? (size_t)2 * (maxk + 1) * 8 : 0);
+    pm.o_mldketau = take(mldon ? ncol * 8 : 0);
+    pm.o_rhos = take(mldon ? ncol * 8 : 0);
     pm.copied = off;
     pm.o_rho = take(nrho * 8);
     pm.o_cost = take(ncol * 8);
@@ -387,6 +530,8 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     pm.o_status = take(4);
     pm.o_cd = take(2 * 8);
     pm.o_scale = take((size_t)L * 4);
+    pm.o_mld = take(mldon ? ncol * 8 : 0);
+    pm.o_mldk = take(mldon ? ncol * 4 : 0);
     pm.zeroed = off;
     pm.o_buf0 = take(nplan * 8);
     pm.o_buf1 = take(nplan * 8);
@@ -414,6 +559,23 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     put(pm.o_gtop, pm.gtop.data(), pm.gtop.size() * 4);
     put(pm.o_ptab, pm.plan.words.data(), pm.plan.words.size() * 4);
     if (ned) put(pm.o_ediff1, grid->ediff1, ned * 8);
+    if (mldon) {
+        // mlddec, mlddecd Fortran-indexed [1..maxk]; the wind energy; rho(maxk) of the initial state
+        double *dec = reinterpret_cast<double *>(h + pm.o_mlddec);
+        for (int k = 1; k <= maxk; ++k) {
+            dec[k] = grid->mlddec[k - 1];
+            dec[maxk + 1 + k] = grid->mlddecd[k - 1];
+        }
+        put(pm.o_mldketau, grid->mldketau, ncol * 8);
+        double *rhos = reinterpret_cast<double *>(h + pm.o_rhos);
+        const double zro = pm.small.mk[3 * (size_t)(maxk + 2) + maxk];
+        for (int j = 1; j <= maxj; ++j)
+            for (int i = 1; i <= maxi; ++i) {
+                const size_t c = (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * maxk));
+                rhos[(i - 1) + (size_t)maxi * (j - 1)] =
+                    grid->k1[i + (size_t)NI * j] <= maxk ? eos_host(pm.p, ts[c], ts[c + 1], zro) : 0.0;
+            }
+    }
     return GB_GO_OK;
 }
 }  // namespace
@@ -421,8 +583,12 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
 // Device part of a member's admission (caller holds e->mu): one pool allocation, the copied
 // segment, the zeroed segment, ts and u from the caller's arrays; the member's item of the
 // batched device set-up; then its descriptor and registration.  Queued on the ensemble's
-// stream: the caller synchronises before the caller's arrays or pm.host may go.
-static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem *item)
+// stream: the caller synchronises before the caller's arrays or pm.host may go.  With `staged`
+// (the device address of the member's copied segment in the staging arena) the segment copy,
+// the zero fill and the copies of mapped ts and u become entries of `segs` for the batched
+// scatter kernel; the rest are copy calls.
+static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem *item, const char *staged,
+                         const char *ts_dev, const char *u_dev, std::vector<CopySeg> &segs)
 {
     if (e->in_use + pm.bytes > e->budget) return efail(e, GB_GO_ENOMEM, "member does not fit in the HBM budget");
     cudaStream_t s = e->stream;
@@ -472,12 +638,30 @@ static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem 
     m->coef = (float *)(b + pm.o_coef);
     m->coefl = (float *)(b + pm.o_coefl);
     m->stencil = has_stencil(params) ? (float *)(b + pm.o_stencil) : nullptr;
+    const bool mldon = params->imld == 1;
+    m->mld = mldon ? (double *)(b + pm.o_mld) : nullptr;
+    m->mldk = mldon ? (int32_t *)(b + pm.o_mldk) : nullptr;
+    m->mldketau = mldon ? (double *)(b + pm.o_mldketau) : nullptr;
     const int nj = dims->maxj + 2, nk = maxk + 2;
     m->mkd = ediff ? m->blob + 8 * nj + nk : nullptr;   // dza, then (7 k-arrays on) diffmax
-    x = cudaMemcpyAsync(b, pm.host.data(), pm.copied, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemsetAsync(b + pm.copied, 0, pm.zeroed - pm.copied, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, pm.ts, nts * 8, cudaMemcpyHostToDevice, s);
-    if (x == cudaSuccess) x = cudaMemcpyAsync(m->vel, pm.u, nu * 8, cudaMemcpyHostToDevice, s);
+    if (staged) {
+        segs.push_back(CopySeg{staged, b, pm.copied});
+        segs.push_back(CopySeg{nullptr, b + pm.copied, pm.zeroed - pm.copied});
+    } else {
+        x = cudaMemcpyAsync(b, pm.host.data(), pm.copied, cudaMemcpyHostToDevice, s);
+        if (x == cudaSuccess) x = cudaMemsetAsync(b + pm.copied, 0, pm.zeroed - pm.copied, s);
+    }
+    // ts and u already on the device (ts_dev, u_dev: staged at the start of the call) or in
+    // mapped host memory (8-byte aligned) are copied by the scatter kernel
+    // (the segment list lives in the staging arena: without it, copy calls)
+    const void *tsd = !staged ? nullptr : ts_dev ? (const void *)ts_dev
+                                                 : (((uintptr_t)pm.ts & 7) == 0 ? host_mapped(pm.ts, nts * 8) : nullptr);
+    const void *ud = !staged ? nullptr : u_dev ? (const void *)u_dev
+                                               : (((uintptr_t)pm.u & 7) == 0 ? host_mapped(pm.u, nu * 8) : nullptr);
+    if (tsd) segs.push_back(CopySeg{tsd, m->ts_static, nts * 8});
+    else if (x == cudaSuccess) x = cudaMemcpyAsync(m->ts_static, pm.ts, nts * 8, cudaMemcpyHostToDevice, s);
+    if (ud) segs.push_back(CopySeg{ud, m->vel, nu * 8});
+    else if (x == cudaSuccess) x = cudaMemcpyAsync(m->vel, pm.u, nu * 8, cudaMemcpyHostToDevice, s);
     if (x != cudaSuccess) {
         free_member(e, m.get());
         return efail(e, x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA, cudaGetErrorString(x));
@@ -512,6 +696,14 @@ static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem 
     md.ts_static = m->ts_static; md.coef = m->coef; md.coefl = m->coefl; md.rvol = m->rvol; md.gtop = m->gtop; md.k1 = m->k1;
     md.scale = m->scale; md.tref = m->tref; md.mk = m->mk; md.mj = m->mj; md.cost = m->cost; md.icosd = m->icosd;
     md.diag = m->diag; md.status = m->status; md.gmax = m->gmax; md.ptab = m->ptab;
+    md.imld = mldon ? 1 : 0;
+    md.mldpebuoycoeff = m->p.mldpebuoycoeff;
+    md.mlddec = mldon ? (const double *)(b + pm.o_mlddec) : nullptr;
+    md.mlddecd = mldon ? (const double *)(b + pm.o_mlddec) + (maxk + 1) : nullptr;
+    md.mldketau = m->mldketau;
+    md.mld = m->mld;
+    md.mldk = m->mldk;
+    md.rhos = mldon ? (double *)(b + pm.o_rhos) : nullptr;
     m->start_step = e->step;
     m->stop_step = (long long)1 << 62;
     md.parity = (int)(e->step & 1);     // (step + parity) & 1 == 0 at admission
@@ -539,6 +731,67 @@ extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, con
     if (!e || n < 0 || (n > 0 && (!dims || !params || !grids || !ts || !u || !ids))) return GB_GO_EINVAL;
     if (n == 0) return GB_GO_OK;
     ETRY(e, cudaSetDevice(e->device));
+    // ts and u in mapped host memory start their transfer now, into one device staging block,
+    // so that it overlaps the host preparation; the members then take them with device copies
+    std::vector<const char *> ts_pre(n, nullptr), u_pre(n, nullptr);
+    char *dstage = nullptr;
+    {
+        std::vector<CopySeg> pre;
+        std::vector<size_t> tso(n, SIZE_MAX), uo(n, SIZE_MAX);
+        size_t db = 0;
+        for (int q = 0; q < n; ++q) {
+            const gb_go_dims &d = dims[q];
+            // sizes of plausible dimensions only (the preparation validates them)
+            if (d.maxi < 1 || d.maxj < 1 || d.maxk < 1 || d.maxl < 1 || d.maxi > 65536 || d.maxj > 65536 ||
+                d.maxk > GB_GO_MAX_K || d.maxl > GB_GO_MAX_L)
+                continue;
+            const size_t nts = (size_t)d.maxl * (d.maxi + 2) * (d.maxj + 2) * (d.maxk + 2);
+            const size_t nu = (size_t)3 * (d.maxi + 1) * (d.maxj + 1) * d.maxk;
+            const void *th = ((uintptr_t)ts[q] & 7) == 0 ? host_mapped(ts[q], nts * 8) : nullptr;
+            const void *uh = ((uintptr_t)u[q] & 7) == 0 ? host_mapped(u[q], nu * 8) : nullptr;
+            if (th) {
+                tso[q] = db;
+                pre.push_back(CopySeg{th, (void *)(uintptr_t)db, nts * 8});
+                db += (nts * 8 + 255) & ~(size_t)255;
+            }
+            if (uh) {
+                uo[q] = db;
+                pre.push_back(CopySeg{uh, (void *)(uintptr_t)db, nu * 8});
+                db += (nu * 8 + 255) & ~(size_t)255;
+            }
+        }
+        CopySeg *dl = nullptr;
+        if (!pre.empty() && cudaMallocFromPoolAsync((void **)&dstage, db, e->pool, e->stream) == cudaSuccess &&
+            cudaMallocAsync((void **)&dl, sizeof(CopySeg) * pre.size(), e->stream) == cudaSuccess) {
+            size_t longest = 16;
+            for (CopySeg &g : pre) {
+                g.dst = dstage + (uintptr_t)g.dst;
+                longest = std::max<size_t>(longest, g.bytes);
+            }
+            cudaError_t x = cudaMemcpyAsync(dl, pre.data(), sizeof(CopySeg) * pre.size(), cudaMemcpyHostToDevice, e->stream);
+            const int bx = (int)std::min<size_t>((longest / 16 + 255) / 256, 64);
+            for (size_t g0 = 0; x == cudaSuccess && g0 < pre.size(); g0 += 65535) {
+                const int ng = (int)std::min<size_t>(pre.size() - g0, 65535);
+                k_scatter<<<dim3(bx, ng), 256, 0, e->stream>>>(dl + g0);
+                count_launches(1);
+                x = cudaGetLastError();
+            }
+            if (x == cudaSuccess)
+                for (int q = 0; q < n; ++q) {
+                    if (tso[q] != SIZE_MAX) ts_pre[q] = dstage + tso[q];
+                    if (uo[q] != SIZE_MAX) u_pre[q] = dstage + uo[q];
+                }
+        }
+        if (dl) cudaFreeAsync(dl, e->stream);
+        cudaGetLastError();
+    }
+    // the staging block goes after the member copies; an early return waits for the transfer
+    // (it reads the caller's arrays)
+    auto drop_stage = [&](bool wait) {
+        if (dstage) cudaFreeAsync(dstage, e->stream);
+        dstage = nullptr;
+        if (wait) cudaStreamSynchronize(e->stream);
+    };
     // host preparation on up to 16 threads
     std::vector<Prepared> pm(n);
     const gb_ens_tuning tuning = e->tuning;
@@ -552,17 +805,64 @@ extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, con
     work();
     for (auto &t : th) t.join();
     for (int q = 0; q < n; ++q)
-        if (pm[q].rc) return efail(e, pm[q].rc, pm[q].msg);
+        if (pm[q].rc) {
+            drop_stage(true);
+            return efail(e, pm[q].rc, pm[q].msg);
+        }
+    // the members' copied segments gathered in the staging arena (threads), then one scatter
+    // kernel; without arena memory, one copy call per segment
+    std::vector<size_t> soff(n);
+    size_t sbytes = 0;
+    for (int q = 0; q < n; ++q) {
+        soff[q] = sbytes;
+        sbytes += (pm[q].copied + 255) & ~(size_t)255;
+    }
+    const size_t seg_at = sbytes;
+    sbytes += sizeof(CopySeg) * 4 * (size_t)n;
+    StagingArena &arena = staging_arena();
+    std::unique_lock<std::mutex> alk(arena.mu);
+    const bool staged = arena_reserve(arena, sbytes);
+    if (staged) {
+        next = 0;
+        auto gather = [&]() {
+            for (int q = next++; q < n; q = next++) std::memcpy(arena.host + soff[q], pm[q].host.data(), pm[q].copied);
+        };
+        th.clear();
+        for (int t = 1; t < nt; ++t) th.emplace_back(gather);
+        gather();
+        for (auto &t : th) t.join();
+    }
     // the device part, one member at a time, the batched set-up, then one synchronisation
     std::lock_guard<std::mutex> lk(e->mu);
     int q = 0, rc = GB_GO_OK;
     std::vector<SetupItem> items(n);
+    std::vector<CopySeg> segs;
     size_t max_elems = 1, max_cells = 1;
     for (; q < n; ++q) {
-        if ((rc = commit_member(e, pm[q], ids + q, &items[q]))) break;
+        if ((rc = commit_member(e, pm[q], ids + q, &items[q], staged ? arena.dev + soff[q] : nullptr, ts_pre[q], u_pre[q],
+                                segs)))
+            break;
         const Dims &d = items[q].d;
         max_elems = std::max(max_elems, (size_t)d.NI * d.NJ * (d.maxk + 2) * d.L);
         max_cells = std::max(max_cells, (size_t)d.maxi * d.maxj * d.maxk);
+    }
+    if (!rc && !segs.empty()) {
+        // the segment list in the arena, read by the kernel through its device address
+        std::memcpy(arena.host + seg_at, segs.data(), segs.size() * sizeof(CopySeg));
+        size_t longest = 16;
+        for (const CopySeg &g : segs) longest = std::max<size_t>(longest, g.bytes);
+        const int bx = (int)std::min<size_t>((longest / 16 + 255) / 256, 64);
+        const CopySeg *dsegs = (const CopySeg *)(arena.dev + seg_at);
+        for (size_t g0 = 0; g0 < segs.size(); g0 += 65535) {
+            const int ng = (int)std::min<size_t>(segs.size() - g0, 65535);
+            k_scatter<<<dim3(bx, ng), 256, 0, e->stream>>>(dsegs + g0);
+            count_launches(1);
+        }
+        const cudaError_t x = cudaGetLastError();
+        if (x != cudaSuccess) {
+            rc = efail(e, GB_GO_ECUDA, cudaGetErrorString(x));
+            q = n;
+        }
     }
     if (!rc) {
         SetupItem *dit = nullptr;
@@ -575,6 +875,7 @@ extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, con
             q = n;
         }
     }
+    drop_stage(false);
     if (rc) {
         // all or nothing: the members of this call that were committed leave again
         for (int r = 0; r < q; ++r) {
@@ -590,6 +891,19 @@ extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, con
     }
     ETRY(e, cudaStreamSynchronize(e->stream));
     return GB_GO_OK;
+}
+
+extern "C" int gb_ens_host_alloc(size_t bytes, void **out)
+{
+    if (!out || bytes == 0) return GB_GO_EINVAL;
+    *out = nullptr;
+    return host_alloc(bytes, out, nullptr);
+}
+
+extern "C" int gb_ens_host_free(void *p)
+{
+    if (!p) return GB_GO_EINVAL;
+    return host_free(p);
 }
 
 extern "C" int gb_ens_remove(gb_ens *e, int32_t id)
@@ -644,7 +958,7 @@ static int rebuild(gb_ens *e)
             slist.push_back(slot);
             sblocks = std::max(sblocks, fp32_stencil_blocks((size_t)m->d.maxi * m->d.maxj * m->d.maxk));
         }
-        co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->d.maxk);
+        co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->desc.imld, m->d.maxk);
         kmax = std::max(kmax, m->d.maxk);
         ++slot;
     }
@@ -927,15 +1241,37 @@ extern "C" int gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, do
     }
     ETRY(e, cudaSetDevice(e->device));
     if (n == 0) return GB_GO_OK;
-    // one kernel forms every member's Fortran-layout ts and rho, then the copies
+    // one kernel forms every member's Fortran-layout ts and rho on the device; destinations in
+    // mapped host memory (8-byte aligned) then take their arrays in one scatter kernel with
+    // coalesced 16-byte stores, the others in one copy call each
     std::vector<DownloadItem> items(n);
+    std::vector<CopySeg> segs;
+    std::vector<unsigned char> direct(n, 0);   // bit 0 ts, bit 1 rho, bit 2 cost by the scatter kernel
     size_t max_cells = 1;
+    auto mapped = [](double *p, size_t count) -> void * {
+        return p && ((uintptr_t)p & 7) == 0 ? host_mapped(p, count * 8) : nullptr;
+    };
     for (int32_t q = 0; q < n; ++q) {
-        items[q].md = ms[q]->desc;
-        items[q].planar = current_buffer(e, ms[q]);
-        items[q].stage = ms[q]->stage;
-        items[q].rho = ms[q]->rho;
-        max_cells = std::max(max_cells, (size_t)ms[q]->d.NI * ms[q]->d.NJ * (ms[q]->d.maxk + 2));
+        Member *m = ms[q];
+        const size_t ncell = (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 2);
+        const size_t nrho = (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 1), ncol = (size_t)m->d.maxi * m->d.maxj;
+        items[q].md = m->desc;
+        items[q].planar = current_buffer(e, m);
+        items[q].stage = m->stage;
+        items[q].rho = m->rho;
+        if (void *d = mapped(ts ? ts[q] : nullptr, ncell * m->d.L)) {
+            segs.push_back(CopySeg{m->stage, d, ncell * m->d.L * 8});
+            direct[q] |= 1;
+        }
+        if (void *d = mapped(rho ? rho[q] : nullptr, nrho)) {
+            segs.push_back(CopySeg{m->rho, d, nrho * 8});
+            direct[q] |= 2;
+        }
+        if (void *d = mapped(cost ? cost[q] : nullptr, ncol)) {
+            segs.push_back(CopySeg{m->cost, d, ncol * 8});
+            direct[q] |= 4;
+        }
+        max_cells = std::max(max_cells, ncell);
     }
     cudaStream_t s = e->stream;
     for (int32_t q0 = 0; q0 < n; q0 += 65535) {
@@ -952,13 +1288,30 @@ extern "C" int gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, do
         cudaFreeAsync(dit, s);
         if (x != cudaSuccess) return efail(e, GB_GO_ECUDA, cudaGetErrorString(x));
     }
+    if (!segs.empty()) {
+        CopySeg *dsg = nullptr;
+        ETRY(e, cudaMallocAsync((void **)&dsg, sizeof(CopySeg) * segs.size(), s));
+        cudaError_t x = cudaMemcpyAsync(dsg, segs.data(), sizeof(CopySeg) * segs.size(), cudaMemcpyHostToDevice, s);
+        size_t longest = 16;
+        for (const CopySeg &g : segs) longest = std::max<size_t>(longest, g.bytes);
+        const int bx = (int)std::min<size_t>((longest / 16 + 255) / 256, 64);
+        for (size_t g0 = 0; x == cudaSuccess && g0 < segs.size(); g0 += 65535) {
+            const int ng = (int)std::min<size_t>(segs.size() - g0, 65535);
+            k_scatter<<<dim3(bx, ng), 256, 0, s>>>(dsg + g0);
+            count_launches(1);
+            x = cudaGetLastError();
+        }
+        cudaFreeAsync(dsg, s);
+        if (x != cudaSuccess) return efail(e, GB_GO_ECUDA, cudaGetErrorString(x));
+    }
     for (int32_t q = 0; q < n; ++q) {
         Member *m = ms[q];
         const size_t nts = (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 2) * m->d.L;
-        if (ts && ts[q]) ETRY(e, cudaMemcpyAsync(ts[q], m->stage, nts * 8, cudaMemcpyDeviceToHost, s));
-        if (rho && rho[q])
+        if (ts && ts[q] && !(direct[q] & 1)) ETRY(e, cudaMemcpyAsync(ts[q], m->stage, nts * 8, cudaMemcpyDeviceToHost, s));
+        if (rho && rho[q] && !(direct[q] & 2))
             ETRY(e, cudaMemcpyAsync(rho[q], m->rho, (size_t)m->d.NI * m->d.NJ * (m->d.maxk + 1) * 8, cudaMemcpyDeviceToHost, s));
-        if (cost && cost[q]) ETRY(e, cudaMemcpyAsync(cost[q], m->cost, (size_t)m->d.maxi * m->d.maxj * 8, cudaMemcpyDeviceToHost, s));
+        if (cost && cost[q] && !(direct[q] & 4))
+            ETRY(e, cudaMemcpyAsync(cost[q], m->cost, (size_t)m->d.maxi * m->d.maxj * 8, cudaMemcpyDeviceToHost, s));
     }
     ETRY(e, cudaStreamSynchronize(s));
     return GB_GO_OK;
@@ -1039,6 +1392,35 @@ extern "C" int gb_ens_inventory(gb_ens *e, int32_t id, double *out)
     ETRY(e, cudaMemcpyAsync(out, dout, m->d.L * sizeof(double), cudaMemcpyDeviceToHost, s));
     cudaFreeAsync(dout, s);
     ETRY(e, cudaStreamSynchronize(s));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ens_set_mld_wind(gb_ens *e, int32_t id, const double *mldketau)
+{
+    if (!e || !mldketau) return GB_GO_EINVAL;
+    auto it = e->members.find(id);
+    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
+    Member *m = it->second.get();
+    if (!m->mldketau) return efail(e, GB_GO_EINVAL, "set_mld_wind: the member has imld = 0");
+    ETRY(e, cudaSetDevice(e->device));
+    // queued behind the steps already launched: it applies from the next step on
+    ETRY(e, cudaMemcpyAsync(m->mldketau, mldketau, (size_t)m->d.maxi * m->d.maxj * 8, cudaMemcpyHostToDevice, e->stream));
+    ETRY(e, cudaStreamSynchronize(e->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ens_download_mld(gb_ens *e, int32_t id, double *mld, int32_t *mldk)
+{
+    if (!e) return GB_GO_EINVAL;
+    auto it = e->members.find(id);
+    if (it == e->members.end()) return efail(e, GB_GO_EINVAL, "no such member");
+    Member *m = it->second.get();
+    if (!m->mld) return efail(e, GB_GO_EINVAL, "download_mld: the member has imld = 0");
+    ETRY(e, cudaSetDevice(e->device));
+    const size_t ncol = (size_t)m->d.maxi * m->d.maxj;
+    if (mld) ETRY(e, cudaMemcpyAsync(mld, m->mld, ncol * 8, cudaMemcpyDeviceToHost, e->stream));
+    if (mldk) ETRY(e, cudaMemcpyAsync(mldk, m->mldk, ncol * 4, cudaMemcpyDeviceToHost, e->stream));
+    ETRY(e, cudaStreamSynchronize(e->stream));
     return GB_GO_OK;
 }
 

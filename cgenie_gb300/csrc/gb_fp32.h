@@ -115,6 +115,15 @@ struct MemberDesc {
     unsigned long long *diag;   // two slots {dmax bits, limps}; step n uses slot n & 1 and clears
                                 // slot (n+1) & 1 for the next step
     unsigned int *status;       // bit0 non-finite, bit1 transfer range exceeded, bit2 column list full
+    // imld = 1, the Kraus-Turner mixed layer (goldstein.f90:2294-2390): every wet column joins the
+    // column pass, which runs co and then the mixed layer in FP64 on the FP64 state
+    int imld, pad2;
+    double mldpebuoycoeff;
+    const double *mlddec, *mlddecd;   // Fortran-indexed [1..maxk] (entry 0 unused)
+    const double *mldketau;           // per column (i-1)+maxi*(j-1): wind mixing energy
+    double *mld;                      // per column: mixed-layer depth
+    int32_t *mldk;                    // per column: the level the mixed layer reaches
+    double *rhos;                     // per column: rho(i,j,maxk) as the previous step left it
 };
 
 // Host-side owner of one member's FP32-path device data.
@@ -280,7 +289,7 @@ struct Fp32Batch {
     int *cocount = nullptr;
     int cocap = 0;
     bool iso = false;
-    bool co_general = false;   // some member has iconv = 1, ieos != 0 or maxk > 32
+    bool co_general = false;   // some member has iconv = 1, ieos != 0, imld = 1 or maxk > 32
     const int *stencil_list = nullptr;   // descriptor indices of the members with a stencil
     int n_stencil = 0, stencil_blocks = 1;   // their count; blocks per member of the prepass
 };
@@ -290,7 +299,10 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
                 cudaEvent_t fork, cudaEvent_t join);
 int fp32_launches_per_step(const Fp32Batch &b);   // kernels fp32_launch starts
 // columns the warp-parallel adjustment takes (the others run co's serial form)
-__host__ __device__ inline bool fp32_co_fast(int iconv, int ieos, int maxk) { return iconv == 0 && ieos == 0 && maxk <= 32; }
+__host__ __device__ inline bool fp32_co_fast(int iconv, int ieos, int imld, int maxk)
+{
+    return iconv == 0 && ieos == 0 && imld == 0 && maxk <= 32;
+}
 int fp32_smem_bytes(int max_slots);
 // current state (group-planar) -> Fortran layout with halo columns, and rho
 int fp32_export(const MemberDesc &md, const double *planar, double *cur, double *rho, cudaStream_t s);

@@ -482,7 +482,7 @@ int ocean_refresh_rho(gb_go_handle *h)
 {
     if (h->precision != GB_GO_FP32FLUX || h->steps_since_upload == 0) return GB_GO_OK;
     const int r = fp32_member_export(&h->f32, h->ts_buf[h->cur], h->rho, h->ts_static, h->stream);
-    return r ? fail(h, r, "fp32 export failed") : GB_GO_OK;
+    return r ? fail(h, r, std::string("fp32 export failed: ") + cudaGetErrorString(cudaPeekAtLastError())) : GB_GO_OK;
 }
 
 int ocean_velocity_changed(gb_go_handle *h)

@@ -42,6 +42,12 @@ struct MoDev {
     const int32_t *npi, *lpisl, *ipisl, *jpisl;
     const double *tau, *dztau, *dztav;
     const double *minv, *ubisl, *psisl, *erisl;   // erisl: (isles, isles+1) after matinv_gold
+    // grids above GB_MO_MAX_PSI points: the block-tridiagonal form of the same matrix, one block
+    // per row j of psi points (n = maxi unknowns): the inverse Schur complements T_j (row-major,
+    // n*n each), the couplings l_j (to row j-1) and u_j (to row j+1), and the forward vectors z
+    const double *btT, *btl, *btu;
+    double *btz;
+    int bt;
     double *psibc, *gb, *gbold, *bp, *sbp, *ub, *psi, *scr, *dzu, *u, *u1;
     const double *rho;
 };
@@ -163,6 +169,57 @@ __global__ void __launch_bounds__(256) k_psi(MoDev a)
         a.psi[PSIi(a, i, j)] = s;
         if (i == a.maxi) a.psi[PSIi(a, 0, j)] = s;   // psi(0,j) = psi(maxi,j)
     }
+}
+
+// Block-tridiagonal streamfunction solve (grids above GB_MO_MAX_PSI points).  The matrix of
+// invert couples psi point (i, j) to (i+-1, j) (periodic in i) and to (i, j+-1), so with one
+// block per row j it is block tridiagonal with diagonal off-diagonal blocks: block LU with the
+// Schur complements S_0 = D_0, S_j = D_j - diag(l_j) S_{j-1}^-1 diag(u_{j-1}), factored once on
+// the host; per step
+//   forward   z_j = T_j (g_j - l_j o z_{j-1})       (T_j = S_j^-1, z_{-1} = 0)
+//   backward  x_J = z_J,  x_j = z_j - T_j (u_j o x_{j+1})
+// one launch per block row, one warp per row of T_j (contiguous), x overwriting z in place.
+__global__ void __launch_bounds__(256) k_bt_forward(MoDev a, int j)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int n = a.maxi;
+    if (w >= n) return;
+    const double *row = a.btT + ((size_t)j * n + w) * n;
+    const double *g = a.gb + (size_t)j * n;
+    const double *l = a.btl + (size_t)j * n;
+    const double *zp = a.btz + (size_t)(j > 0 ? j - 1 : 0) * n;
+    double s = 0.0;
+    for (int c = lane; c < n; c += 32) {
+        const double y = j > 0 ? g[c] - l[c] * zp[c] : g[c];
+        s = s + row[c] * y;
+    }
+    for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) a.btz[(size_t)j * n + w] = s;
+}
+
+__global__ void __launch_bounds__(256) k_bt_backward(MoDev a, int j)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int n = a.maxi;
+    if (w >= n) return;
+    const double *row = a.btT + ((size_t)j * n + w) * n;
+    const double *u = a.btu + (size_t)j * n;
+    const double *xn = a.btz + (size_t)(j + 1) * n;
+    double s = 0.0;
+    for (int c = lane; c < n; c += 32) s = s + row[c] * (u[c] * xn[c]);
+    for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) a.btz[(size_t)j * n + w] = a.btz[(size_t)j * n + w] - s;
+}
+
+// psi from the solution (psi(i, j) = x(i + j*maxi), psi(0, j) = psi(maxi, j))
+__global__ void __launch_bounds__(128) k_bt_psi(MoDev a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.nm) return;
+    const int i = t % a.maxi + 1, j = t / a.maxi;
+    const double v = a.btz[t];
+    a.psi[PSIi(a, i, j)] = v;
+    if (i == a.maxi) a.psi[PSIi(a, 0, j)] = v;
 }
 
 // ub from psi (ubarsolv :3538-3564); the periodic columns i = 0, maxi+1 evaluate the formula
@@ -418,8 +475,8 @@ struct HostInit {
     std::vector<double> ubisl, psisl, erisl;
 };
 
-// band matrix and its elimination (invert, goldstein.f90:3138-3204)
-void host_invert(const HostGrid &G, HostInit &I)
+// band matrix of invert (goldstein.f90:3138-3188), before the elimination
+void host_band(const HostGrid &G, HostInit &I)
 {
     const int maxi = G.d.maxi, maxj = G.d.maxj, maxk = G.d.maxk, n = maxi, nm = I.nm;
     const double dphi = G.p.dphi, rdphi = G.p.rdphi;
@@ -428,7 +485,6 @@ void host_invert(const HostGrid &G, HostInit &I)
     auto DRAG = [&](int l, int i, int j) { return G.drag[(l - 1) + 2 * ((size_t)(i - 1) + (size_t)(maxi + 1) * (j - 1))]; };
     auto GAP = [&](int r, int cc) -> double & { return I.gap[(size_t)(r - 1) + (size_t)nm * (cc - 1)]; };
     I.gap.assign((size_t)nm * (2 * n + 3), 0.0);
-    I.ratm.assign((size_t)nm * (n + 1), 0.0);
     for (int i = 1; i <= maxi; ++i)
         for (int j = 0; j <= maxj; ++j) {
             const int k = i + j * n;
@@ -448,6 +504,14 @@ void host_invert(const HostGrid &G, HostInit &I)
                 GAP(k, n + 2) = 1;
             }
         }
+}
+
+// the elimination of invert (goldstein.f90:3189-3204) on the band matrix
+void host_eliminate(HostInit &I)
+{
+    const int n = I.n, nm = I.nm;
+    auto GAP = [&](int r, int cc) -> double & { return I.gap[(size_t)(r - 1) + (size_t)nm * (cc - 1)]; };
+    I.ratm.assign((size_t)nm * (n + 1), 0.0);
     for (int i = 1; i <= nm - 1; ++i) {
         const int im = std::min(i + n + 1, nm);
         for (int j = i + 1; j <= im; ++j) {
@@ -474,6 +538,121 @@ void host_solve(const HostInit &I, double *gb)
         for (int k = 1; k <= km; ++k) gb[i - 1] = gb[i - 1] - GAP(i, n + 2 + k) * gb[i + k - 1];
         gb[i - 1] = gb[i - 1] / GAP(i, n + 2);
     }
+}
+
+// Block-tridiagonal factors of the band matrix (before elimination): blocks of n = maxi rows,
+// block j = psi row j.  T_j = S_j^-1 (row-major) with S_j = D_j - diag(l_j) T_{j-1} diag(u_{j-1}),
+// each S_j factored by LU without pivoting (the reference's band elimination pivots on the
+// diagonal too, so the leading minors it divides by are those of the S_j) and inverted column
+// by column on host threads.
+struct HostBT {
+    int n = 0, J = 0;
+    std::vector<double> T, l, u;   // (J+1)*n*n, (J+1)*n, (J+1)*n
+};
+
+int host_bt_factor(const HostInit &I, HostBT &B)
+{
+    const int n = I.n, nm = I.nm, J = nm / n - 1;
+    auto GAP = [&](int r, int cc) { return I.gap[(size_t)(r - 1) + (size_t)nm * (cc - 1)]; };
+    B.n = n;
+    B.J = J;
+    B.T.assign((size_t)(J + 1) * n * n, 0.0);
+    B.l.assign((size_t)(J + 1) * n, 0.0);
+    B.u.assign((size_t)(J + 1) * n, 0.0);
+    std::vector<double> S((size_t)n * n);
+    const int nt = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+    for (int j = 0; j <= J; ++j) {
+        // D_j and the couplings from the band rows of block j
+        std::fill(S.begin(), S.end(), 0.0);
+        for (int a = 0; a < n; ++a) {
+            const int k = a + 1 + j * n;
+            for (int c = 1; c <= 2 * n + 3; ++c) {
+                const double v = GAP(k, c);
+                if (v == 0.0) continue;
+                const int kk = k + c - (n + 2);
+                if (kk < 1 || kk > nm) return GB_GO_EINVAL;
+                const int jj = (kk - 1) / n, b = (kk - 1) % n;
+                if (jj == j) S[(size_t)a * n + b] += v;
+                else if (jj == j - 1 && b == a) B.l[(size_t)j * n + a] = v;
+                else if (jj == j + 1 && b == a) B.u[(size_t)j * n + a] = v;
+                else return GB_GO_EINVAL;
+            }
+        }
+        if (j > 0) {
+            const double *Tp = B.T.data() + (size_t)(j - 1) * n * n;
+            const double *l = B.l.data() + (size_t)j * n, *up = B.u.data() + (size_t)(j - 1) * n;
+            for (int a = 0; a < n; ++a)
+                if (l[a] != 0.0)
+                    for (int b = 0; b < n; ++b) S[(size_t)a * n + b] -= l[a] * Tp[(size_t)a * n + b] * up[b];
+        }
+        // LU without pivoting, in place (unit lower L below the diagonal)
+        for (int p = 0; p < n; ++p) {
+            const double d = S[(size_t)p * n + p];
+            if (d == 0.0 || !std::isfinite(d)) return GB_GO_ERANGE;
+            for (int r = p + 1; r < n; ++r) {
+                const double f = S[(size_t)r * n + p] / d;
+                S[(size_t)r * n + p] = f;
+                if (f != 0.0) {
+                    double *Sr = S.data() + (size_t)r * n;
+                    const double *Sp = S.data() + (size_t)p * n;
+                    for (int c = p + 1; c < n; ++c) Sr[c] -= f * Sp[c];
+                }
+            }
+        }
+        // T_j = S_j^-1, column c from L U x = e_c (threads over columns)
+        double *T = B.T.data() + (size_t)j * n * n;
+        std::vector<std::thread> th;
+        for (int w = 0; w < nt; ++w)
+            th.emplace_back([&, w]() {
+                std::vector<double> x((size_t)n);
+                for (int c = w; c < n; c += nt) {
+                    std::fill(x.begin(), x.end(), 0.0);
+                    x[c] = 1.0;
+                    for (int r = c + 1; r < n; ++r) {
+                        double v = x[r];
+                        const double *Lr = S.data() + (size_t)r * n;
+                        for (int p = c; p < r; ++p) v -= Lr[p] * x[p];
+                        x[r] = v;
+                    }
+                    for (int r = n - 1; r >= 0; --r) {
+                        double v = x[r];
+                        const double *Ur = S.data() + (size_t)r * n;
+                        for (int p = r + 1; p < n; ++p) v -= Ur[p] * x[p];
+                        x[r] = v / Ur[r];
+                    }
+                    for (int r = 0; r < n; ++r) T[(size_t)r * n + c] = x[r];
+                }
+            });
+        for (auto &t : th) t.join();
+    }
+    return GB_GO_OK;
+}
+
+// The block-tridiagonal solve on the host (unit-source solves of the initialisation)
+void host_bt_solve(const HostBT &B, double *gb)
+{
+    const int n = B.n, J = B.J;
+    std::vector<double> z((size_t)(J + 1) * n), y((size_t)n);
+    for (int j = 0; j <= J; ++j) {
+        for (int b = 0; b < n; ++b) y[b] = j > 0 ? gb[(size_t)j * n + b] - B.l[(size_t)j * n + b] * z[(size_t)(j - 1) * n + b]
+                                                 : gb[b];
+        const double *T = B.T.data() + (size_t)j * n * n;
+        for (int a = 0; a < n; ++a) {
+            double s = 0.0;
+            for (int b = 0; b < n; ++b) s += T[(size_t)a * n + b] * y[b];
+            z[(size_t)j * n + a] = s;
+        }
+    }
+    for (int j = J - 1; j >= 0; --j) {
+        const double *T = B.T.data() + (size_t)j * n * n;
+        for (int b = 0; b < n; ++b) y[b] = B.u[(size_t)j * n + b] * z[(size_t)(j + 1) * n + b];
+        for (int a = 0; a < n; ++a) {
+            double s = 0.0;
+            for (int b = 0; b < n; ++b) s += T[(size_t)a * n + b] * y[b];
+            z[(size_t)j * n + a] -= s;
+        }
+    }
+    std::copy(z.begin(), z.end(), gb);
 }
 
 // ubarsolv's psi and ub from a solved gb (:3527-3564), into zero-initialised psi, ub
@@ -598,7 +777,9 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     if (d.maxi < 3 || d.maxj < 3 || d.maxk < 1 || d.maxk > GB_GO_MAX_K || d.isles < 1 || d.isles > 32 || d.mpi < 1)
         return GB_GO_EINVAL;
     const long long nm = (long long)d.maxi * (d.maxj + 1);
-    if (nm > GB_MO_MAX_PSI) return GB_GO_ERANGE;
+    if (d.maxi > GB_MO_MAX_ROW || nm > GB_MO_MAX_PSI_BT) return GB_GO_ERANGE;
+    if (d.solver != 0 && d.solver != 1) return GB_GO_EINVAL;
+    const bool bt = nm > GB_MO_MAX_PSI || d.solver == 1;   // the block-tridiagonal solve instead of the inverse
     const gb_mo_grid &g = *grid;
     const void *need[] = {g.s, g.c, g.sv, g.cv, g.rc, g.rcv, g.dsv, g.rdsv, g.ds, g.rds, g.rds2, g.dz, g.dza, g.k1, g.ku,
                           g.mk, g.getj, g.rh, g.drag, g.rtv, g.rtv3, g.psiles, g.npi, g.lpisl, g.ipisl, g.jpisl};
@@ -642,7 +823,14 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     HostInit I;
     I.n = maxi;
     I.nm = (int)nm;
-    host_invert(G, I);
+    host_band(G, I);
+    HostBT B;
+    if (bt) {
+        const int r = host_bt_factor(I, B);
+        if (r) return r;
+    } else {
+        host_eliminate(I);
+    }
     const size_t nub = 2 * (size_t)(maxi + 2) * (maxj + 1), npsi = (size_t)(maxi + 1) * (maxj + 1);
     I.ubisl.assign(nub * d.isles, 0.0);
     I.psisl.assign(npsi * d.isles, 0.0);
@@ -650,7 +838,8 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     std::vector<double> gbv((size_t)nm);
     for (int isol = 1; isol <= d.isles; ++isol) {
         for (long long k = 0; k < nm; ++k) gbv[k] = ((int)G.psiles[k] == isol + 1) ? 1.0 : 0.0;
-        host_solve(I, gbv.data());
+        if (bt) host_bt_solve(B, gbv.data());
+        else host_solve(I, gbv.data());
         host_psi_ub(G, gbv.data(), I.psisl.data() + npsi * (isol - 1), I.ubisl.data() + nub * (isol - 1));
         for (int isl = 1; isl <= d.isles; ++isl)
             I.erisl[(size_t)(isl - 1) + (size_t)d.isles * (isol - 1)] = host_island0(G, I.ubisl.data() + nub * (isol - 1), isl);
@@ -664,8 +853,8 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     }
     // the explicit inverse, row-major (row r of the inverse is the response of psi(r) to every
     // right-hand side entry): column c = the solve of unit vector c
-    std::vector<double> minv((size_t)nm * nm);
-    {
+    std::vector<double> minv(bt ? 0 : (size_t)nm * nm);
+    if (!bt) {
         const int nt = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
         std::vector<std::thread> th;
         for (int w = 0; w < nt; ++w)
@@ -694,7 +883,12 @@ extern "C" int gb_mo_create(const gb_mo_dims *dims, const gb_mo_params *params, 
     UP(rds, rds); UP(rds2, rds2); UP(dz, dz); UP(dza, dza); UP(k1, k1); UP(ku, ku); UP(mk, mk); UP(getj, getj); UP(rh, rh);
     UP(drag, drag); UP(rtv, rtv); UP(rtv3, rtv3); UP(npi, npi); UP(lpisl, lpisl); UP(ipisl, ipisl); UP(jpisl, jpisl);
 #undef UP
-    if (e == cudaSuccess) e = dev_copy(h, &a.minv, minv);
+    a.bt = bt ? 1 : 0;
+    if (e == cudaSuccess && !bt) e = dev_copy(h, &a.minv, minv);
+    if (e == cudaSuccess && bt) e = dev_copy(h, &a.btT, B.T);
+    if (e == cudaSuccess && bt) e = dev_copy(h, &a.btl, B.l);
+    if (e == cudaSuccess && bt) e = dev_copy(h, &a.btu, B.u);
+    if (e == cudaSuccess && bt) e = dev_zero(h, &a.btz, (size_t)nm);
     if (e == cudaSuccess) e = dev_copy(h, &a.ubisl, I.ubisl);
     if (e == cudaSuccess) e = dev_copy(h, &a.psisl, I.psisl);
     if (e == cudaSuccess) e = dev_copy(h, &a.erisl, I.erisl);
@@ -805,7 +999,7 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
         h->graph_stream = s;
     }
     MO_TRY(h, cudaGraphLaunch(h->graph, s));
-    count_launches(9);
+    count_launches(a.bt ? 8 + 2 * (a.nm / a.maxi) : 9);
     // the split-precision form rebuilds its transfer coefficients from the new velocities
     const int r = ocean_velocity_changed(ocean);
     if (r != GB_GO_OK) return mfail(h, r, std::string("step: ") + gb_go_last_error(ocean));
@@ -822,7 +1016,14 @@ static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u)
     // SMs (GB300's FP64 pipe is ~2 lanes per clock per SM)
     k_bp<<<(ncol + 31) / 32, 32, 0, s>>>(a);
     k_rhs<<<(a.nm + 31) / 32, 32, 0, s>>>(a);
-    k_psi<<<(a.nm * 32 + 255) / 256, 256, 0, s>>>(a);
+    if (a.bt) {
+        const int nb = (a.maxi * 32 + 255) / 256, J = a.nm / a.maxi - 1;
+        for (int j = 0; j <= J; ++j) k_bt_forward<<<nb, 256, 0, s>>>(a, j);
+        for (int j = J - 1; j >= 0; --j) k_bt_backward<<<nb, 256, 0, s>>>(a, j);
+        k_bt_psi<<<(a.nm + 127) / 128, 128, 0, s>>>(a);
+    } else {
+        k_psi<<<(a.nm * 32 + 255) / 256, 256, 0, s>>>(a);
+    }
     k_ub<<<((a.maxi + 2) * (a.maxj + 1) + 127) / 128, 128, 0, s>>>(a);
     k_island<<<1, 256, 0, s>>>(a, a.scr);
     k_corr<<<(unsigned)((nub + npsi + 127) / 128), 128, 0, s>>>(a);

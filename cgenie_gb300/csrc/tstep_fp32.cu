@@ -589,9 +589,9 @@ k_step_fp32(const MemberDesc *__restrict__ mds, const int4 *__restrict__ items, 
             __syncthreads();
         }
 
-        // columns that need the exact convective adjustment (every column with iconv = 1 or
-        // ieos != 0) join the step's list: (member, word offset of the column's record)
-        if (item.z == 0 && interior && (unstable || md.iconv == 1 || md.ieos != 0)) {
+        // columns that need the exact convective adjustment (every column with iconv = 1,
+        // ieos != 0 or imld = 1) join the step's list: (member, word offset of the column's record)
+        if (item.z == 0 && interior && (unstable || md.iconv == 1 || md.ieos != 0 || md.imld != 0)) {
             const int at = atomicAdd(&cocount[step & 1], 1);
             if (at < cocap) colist[at] = make_int2(item.x, (int)(ticol - md.ptab) + kIcolWords * t);
             else atomicOr(md.status, 4u);
@@ -811,7 +811,7 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         const int32_t *ticol = md.ptab + ent.y;
         const int maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ, mkn = maxk + 2;
         // this instance takes either the warp-parallel columns or the others
-        if (fp32_co_fast(md.iconv, md.ieos, maxk) == GENERAL) continue;
+        if (fp32_co_fast(md.iconv, md.ieos, md.imld, maxk) == GENERAL) continue;
         const int k1c = (ticol[2] >> 16) & 0xffff, cl0 = ticol[3];
         const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
         const int par = (int)((step + md.parity) & 1);
@@ -821,7 +821,9 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         EosCoef ec;
         for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
         ec.ieos = md.ieos;
-        if (GENERAL && md.iconv == 1) {
+        if (GENERAL && (md.iconv == 1 || md.imld != 0)) {
+            // coshuffle (iconv = 1), co and the mixed layer (imld = 1) on one lane, in the
+            // order of tstepo (goldstein.f90:2311-2389)
             if (lane == 0) {
                 Fp32Col col;
                 col.w = W;
@@ -836,11 +838,41 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
                 col.k1 = k1c;
                 col.rho[0] = 0.0;
                 for (int kk = 1; kk <= maxk; ++kk) col.rho[kk] = eos_rn(ec, col.T(0, kk), col.T(1, kk), zro[kk]);
-                int icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
-                const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
-                if (filled > icos) icos = filled;
-                md.icosd[cl0] = icos;
-                md.cost[cl0] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
+                double rold[kMaxK + 1];
+                MixedLayerArgs ml{};
+                if (md.imld != 0) {
+                    // the densities before co, and mldpe1 from the start-of-step T and S of the top
+                    // layer (the other buffer) less the forcing slot ts(:,i,j,maxk+1)
+                    for (int kk = 1; kk <= maxk; ++kk) rold[kk] = col.rho[kk];
+                    Fp32Col c0 = col;
+                    c0.w = md.buf[par];
+                    const double *top = md.ts_static + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (maxk + 1)));
+                    ml.zw = zw;
+                    ml.zro = zro;
+                    ml.dz = dz;
+                    ml.mlddec = md.mlddec;
+                    ml.mlddecd = md.mlddecd;
+                    ml.mldpebuoycoeff = md.mldpebuoycoeff;
+                    ml.ketau = md.mldketau[cl0];
+                    ml.pe1 = ml_pe1(ec, __dadd_rn(c0.T(0, maxk), -top[0]), __dadd_rn(c0.T(1, maxk), -top[1]), md.rhos[cl0],
+                                    zw, zro, maxk);
+                }
+                if (md.iconv == 1) {
+                    int icos = coshuffle_rn(col, ec, maxk, L, k1c, dz, rdz, zw);
+                    const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
+                    if (filled > icos) icos = filled;
+                    md.icosd[cl0] = icos;
+                    md.cost[cl0] = __dmul_rn(md.dsc, zw[maxk - 1 - icos]);
+                } else {
+                    const int filled = co_rn(col, ec, maxk, L, k1c, dz, zw);
+                    if (filled > 0) md.cost[cl0] = add_count_rn(md.cost[cl0], filled);
+                }
+                if (md.imld != 0) {
+                    mixed_layer_rn(col, ec, maxk, L, k1c, ml, rold, &md.mld[cl0], &md.mldk[cl0]);
+                    // rho(maxk) for the next step's mldpe1: co's value, or with ieos != 0 the
+                    // density of the final state (goldstein.f90:2391-2398)
+                    md.rhos[cl0] = ec.ieos != 0 ? eos_rn(ec, col.T(0, maxk), col.T(1, maxk), zro[maxk]) : col.rho[maxk];
+                }
             }
             __syncwarp();
             continue;
@@ -1946,7 +1978,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         bt.cocount = D.cocount;
         bt.cocap = D.cocap;
         bt.iso = D.stencil != nullptr;
-        bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->d.maxk);
+        bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->p.imld, h->d.maxk);
         if (D.stencil) {
             bt.stencil_list = D.stencil_list;
             bt.n_stencil = 1;

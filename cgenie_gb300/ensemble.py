@@ -19,6 +19,32 @@ from .abi import GbEnsTuning, GridRefs, dptr
 from .goldstein import GoldsteinError, load_library
 
 
+def host_empty(shape, dtype=np.float64) -> np.ndarray:
+    """An uninitialised array in mapped page-locked host memory (gb_ens_host_alloc), freed with
+    the array.  Ensemble.add_many reads ts and u that lie in such memory, and download_many
+    writes ts, rho and cost there, through the device address inside the call's batched kernel
+    (no copy call per array)."""
+    import weakref
+    lib = load_library()
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    p = C.c_void_p()
+    rc = lib.gb_ens_host_alloc(C.c_size_t(max(n, 1)), C.byref(p))
+    if rc != 0:
+        raise GoldsteinError(rc, "gb_ens_host_alloc")
+    buf = (C.c_char * max(n, 1)).from_address(p.value)
+    arr = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+    weakref.finalize(buf, lib.gb_ens_host_free, C.c_void_p(p.value))
+    return arr
+
+
+def host_copy(a) -> np.ndarray:
+    """host_empty filled with a copy of `a`."""
+    out = host_empty(np.shape(a), np.asarray(a).dtype)
+    out[...] = a
+    return out
+
+
 class Ensemble:
     def __init__(self, device: int = -1, hbm_budget_bytes: int = 0, *, tile_i: int = 0, tile_j: int = 0,
                  use_graph: bool = False, stream: Optional[int] = None, use_table: bool = True):
@@ -82,34 +108,46 @@ class Ensemble:
             self._current_tile = tile
         return self._add_now(member, steps, **kw)
 
-    def add_many(self, members, **kw) -> list:
+    def add_many(self, members, steps=None, **kw) -> list:
         """Admit several members in one call per tile shape (gb_ens_add_many: host preparation
-        on up to 16 threads inside the library, one synchronisation).  All or nothing per call.
-        Returns the ids in order."""
+        on up to 16 threads inside the library, one synchronisation).  All or nothing: when a
+        call fails, the members this method admitted before it leave again.  `steps`: per
+        member, its remaining-step count (set_remaining), or None.  Returns the ids in order."""
         from .abi import GbDims, GbGrid, GbParams
         members = list(members)
         ids = [None] * len(members)
         groups = {}
         for n, m in enumerate(members):
             groups.setdefault(self._tile_for(m), []).append(n)
-        dp = C.POINTER(C.c_double)
-        for tile, idx in groups.items():
-            if tile != self._current_tile:
-                self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
-                self._current_tile = tile
-            k = len(idx)
-            refs = [GridRefs(members[n], precision=abi.GB_GO_FP32FLUX, **kw) for n in idx]
-            tss = [np.ascontiguousarray(members[n].ts, dtype=np.float64) for n in idx]
-            us = [np.ascontiguousarray(members[n].u, dtype=np.float64) for n in idx]
-            dims = (GbDims * k)(*[r.dims for r in refs])
-            params = (GbParams * k)(*[r.params for r in refs])
-            grids = (GbGrid * k)(*[r.grid for r in refs])
-            out = (C.c_int32 * k)()
-            self._check(self.lib.gb_ens_add_many(self.e, k, dims, params, grids, (dp * k)(*[dptr(a) for a in tss]),
-                                                 (dp * k)(*[dptr(a) for a in us]), out), "gb_ens_add_many")
-            for n, mid in zip(idx, out):
-                ids[n] = int(mid)
-                self.members[int(mid)] = members[n]
+        try:
+            for tile, idx in groups.items():
+                if tile != self._current_tile:
+                    self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
+                    self._current_tile = tile
+                k = len(idx)
+                refs = [GridRefs(members[n], precision=abi.GB_GO_FP32FLUX, **kw) for n in idx]
+                tss = [np.ascontiguousarray(members[n].ts, dtype=np.float64) for n in idx]
+                us = [np.ascontiguousarray(members[n].u, dtype=np.float64) for n in idx]
+                dims = (GbDims * k)(*[r.dims for r in refs])
+                params = (GbParams * k)(*[r.params for r in refs])
+                grids = (GbGrid * k)(*[r.grid for r in refs])
+                out = (C.c_int32 * k)()
+                vp = C.c_void_p
+                self._check(self.lib.gb_ens_add_many(self.e, k, dims, params, grids,
+                                                     (vp * k)(*[abi.addr(a) for a in tss]),
+                                                     (vp * k)(*[abi.addr(a) for a in us]), out), "gb_ens_add_many")
+                for n, mid in zip(idx, out):
+                    ids[n] = int(mid)
+                    self.members[int(mid)] = members[n]
+        except BaseException:
+            for mid in ids:
+                if mid is not None:
+                    self.remove(mid)
+            raise
+        if steps is not None:
+            for mid, st in zip(ids, steps):
+                if st is not None:
+                    self.set_remaining(mid, int(st))
         return ids
 
     def _add_now(self, member, steps, **kw) -> int:
@@ -174,6 +212,21 @@ class Ensemble:
         self._check(self.lib.gb_ens_download_many(self.e, n, ids, arr["ts"], arr["rho"], arr["cost"]),
                     "gb_ens_download_many")
         return outs
+
+    def set_mld_wind(self, mid: int, mldketau):
+        """imld = 1 members: the wind mixing energy per column ((maxj, maxi) array) from the next
+        step on (gb_ens_set_mld_wind)."""
+        a = np.ascontiguousarray(mldketau, dtype=np.float64)
+        self._check(self.lib.gb_ens_set_mld_wind(self.e, int(mid), dptr(a)), "gb_ens_set_mld_wind")
+
+    def download_mld(self, mid: int):
+        """imld = 1 members: (mld, mldk), the mixed-layer depth and level of every column as
+        (maxj, maxi) arrays (gb_ens_download_mld)."""
+        m = self.members[mid]
+        mld = np.zeros((m.maxj, m.maxi))
+        mldk = np.zeros((m.maxj, m.maxi), dtype=np.int32)
+        self._check(self.lib.gb_ens_download_mld(self.e, int(mid), dptr(mld), abi.iptr(mldk)), "gb_ens_download_mld")
+        return mld, mldk
 
     def inventory(self, mid: int) -> np.ndarray:
         out = np.zeros(self.members[mid].maxl)

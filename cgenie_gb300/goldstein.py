@@ -33,7 +33,8 @@ EXPORTED = [
     "gb_ens_create", "gb_ens_destroy", "gb_ens_set_tuning", "gb_ens_set_stream", "gb_ens_member_bytes",
     "gb_ens_add", "gb_ens_add_many", "gb_ens_remove", "gb_ens_step", "gb_ens_set_remaining", "gb_ens_step_remaining",
     "gb_ens_remaining", "gb_ens_download", "gb_ens_download_many", "gb_ens_download_stream", "gb_ens_inventory", "gb_ens_status", "gb_ens_sync",
-    "gb_ens_count", "gb_ens_last_error",
+    "gb_ens_count", "gb_ens_last_error", "gb_ens_host_alloc", "gb_ens_host_free", "gb_ens_set_mld_wind",
+    "gb_ens_download_mld",
     "gb_bg_create", "gb_bg_destroy", "gb_bg_columns", "gb_bg_upload", "gb_bg_set_increments",
     "gb_bg_tracercoupling", "gb_bg_download", "gb_bg_last_error",
     "gb_ea_create", "gb_ea_destroy", "gb_ea_upload_state", "gb_ea_set_forcing", "gb_ea_step", "gb_ea_step_many",
@@ -105,7 +106,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_ts_last_error.argtypes = [vp]
     L.gb_ts_last_error.restype = C.c_char_p
     L.gb_ens_add.argtypes = [vp, P(GbDims), P(GbParams), P(GbGrid), dp, dp, ip]
-    L.gb_ens_add_many.argtypes = [vp, C.c_int32, P(GbDims), P(GbParams), P(GbGrid), P(dp), P(dp), ip]
+    L.gb_ens_add_many.argtypes = [vp, C.c_int32, P(GbDims), P(GbParams), P(GbGrid), P(vp), P(vp), ip]
     L.gb_ens_remove.argtypes = [vp, C.c_int32]
     L.gb_ens_step.argtypes = [vp, C.c_int32]
     L.gb_ens_set_remaining.argtypes = [vp, C.c_int32, C.c_int64]
@@ -120,6 +121,10 @@ def load_library(path: str = LIB_PATH):
     L.gb_ens_count.argtypes = [vp, ip, P(C.c_size_t)]
     L.gb_ens_last_error.argtypes = [vp]
     L.gb_ens_last_error.restype = C.c_char_p
+    L.gb_ens_host_alloc.argtypes = [C.c_size_t, P(vp)]
+    L.gb_ens_set_mld_wind.argtypes = [vp, C.c_int32, dp]
+    L.gb_ens_download_mld.argtypes = [vp, C.c_int32, dp, ip]
+    L.gb_ens_host_free.argtypes = [vp]
     L.gb_bg_create.argtypes = [P(abi.GbBgDims), P(abi.GbBgParams), ip, C.c_int, P(vp)]
     L.gb_bg_destroy.argtypes = [vp]
     L.gb_bg_destroy.restype = None

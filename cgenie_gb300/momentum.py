@@ -26,7 +26,7 @@ FSC = 2 * 7.2921e-5    # Coriolis scale (goldstein_lib.f90:49-52)
 
 class GbMoDims(C.Structure):
     _fields_ = [("maxi", C.c_int32), ("maxj", C.c_int32), ("maxk", C.c_int32), ("isles", C.c_int32),
-                ("mpi", C.c_int32), ("pad", C.c_int32)]
+                ("mpi", C.c_int32), ("solver", C.c_int32)]
 
 
 class GbMoParams(C.Structure):
@@ -255,10 +255,13 @@ def _case_from(m, rng, hg, dz, k1, ku, mk, getj, rh, drag, rtv, rtv3, psiles, is
 class Momentum:
     """A device-resident momentum step (gb_mo handle) for a Goldstein handle of the same grid."""
 
-    def __init__(self, case: MomentumCase, device: int = -1):
+    def __init__(self, case: MomentumCase, device: int = -1, solver: int = 0):
+        """solver: 0 = by grid size (the explicit inverse up to GB_MO_MAX_PSI streamfunction
+        points, else the block-tridiagonal solve), 1 = block-tridiagonal at any size."""
         self.lib = load_library()
         self.case = case
         self._dims, self._params, self._grid = case.dims(), case.params(), case.grid()
+        self._dims.solver = int(solver)
         h = C.c_void_p()
         rc = self.lib.gb_mo_create(C.addressof(self._dims), C.addressof(self._params), C.addressof(self._grid),
                                    int(device), C.byref(h))

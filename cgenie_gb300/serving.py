@@ -92,9 +92,19 @@ def poisson_requests(n: int, rate: float = 50.0, seed: int = 7, smin: int = 200,
 
 
 class Server:
+    """The serving loop over one Ensemble on its own CUDA stream.  Each round launches the next
+    chunk of batched steps (asynchronously), admits the requests that arrived meanwhile while the
+    chunk runs (their host preparation overlaps the GPU work; their device set-up is queued
+    behind the chunk, so they join at the next step boundary), synchronises, and retires the
+    members whose step count is reached.  GPU busy time is the chunks' CUDA-event time."""
+
     def __init__(self, hbm_budget_bytes: int = 0, chunk: int = 25, device: int = -1, keep_results: bool = False,
                  use_graph: bool = False, factory: Optional[MemberFactory] = None):
-        self.ens = Ensemble(device=device, hbm_budget_bytes=hbm_budget_bytes, use_graph=use_graph)
+        import torch
+        dev = torch.device("cuda", device if device >= 0 else torch.cuda.current_device())
+        self.stream = torch.cuda.Stream(device=dev)
+        self.ens = Ensemble(device=device, hbm_budget_bytes=hbm_budget_bytes, use_graph=use_graph,
+                            stream=self.stream.cuda_stream)
         self.chunk = chunk
         self.keep = keep_results
         self.factory = factory or MemberFactory()
@@ -109,54 +119,78 @@ class Server:
             self.wet[key] = m.wet_cells
         return self.wet[key]
 
+    def _admit(self, waiting, active, stamp):
+        """Admit waiting requests in arrival order while the HBM budget allows: all of them in
+        one batched call, else (the budget is short) one at a time until one does not fit."""
+        if not waiting:
+            return
+        reqs = list(waiting)
+        ms = [self.factory.member(r) for r in reqs]
+        try:
+            ids = self.ens.add_many(ms, steps=[r.steps for r in reqs])
+        except GoldsteinError as e:
+            if e.code != abi.GB_GO_ENOMEM:
+                raise
+            ids = []
+            for r, m in zip(reqs, ms):
+                try:
+                    ids.append(self.ens.add(m, steps=r.steps))
+                except GoldsteinError as e2:
+                    if e2.code == abi.GB_GO_ENOMEM:
+                        break
+                    raise
+        now = stamp()
+        for req, m, mid in zip(reqs, ms, ids):
+            waiting.popleft()
+            req.member_id = mid
+            req.admitted = now
+            req.cell_updates = self._wet(m) * req.maxl * req.steps
+            active[mid] = req
+
     def run(self, requests, clock: Callable[[], float] = time.perf_counter, time_scale: float = 1.0):
         """Serve `requests` (arrival times in seconds from the start).  Returns stats."""
+        import torch
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         waiting = collections.deque()
         active = {}
         done = []
         ens = self.ens
         t0 = clock()
+        stamp = lambda: (clock() - t0) * time_scale   # noqa: E731
         total_cu = 0
         steps_run = 0
-        busy_s = 0.0
+        events = []
         max_active = 0
         while pending or waiting or active:
-            now = (clock() - t0) * time_scale
+            now = stamp()
             while pending and pending[0].arrival <= now:
                 waiting.append(pending.popleft())
-            # admission by free HBM
-            while waiting:
-                req = waiting[0]
-                m = self.factory.member(req)
-                try:
-                    mid = ens.add(m, steps=req.steps)
-                except GoldsteinError as e:
-                    if e.code == abi.GB_GO_ENOMEM:
-                        break
-                    raise
-                waiting.popleft()
-                req.member_id = mid
-                req.admitted = (clock() - t0) * time_scale
-                req.cell_updates = self._wet(m) * req.maxl * req.steps
-                active[mid] = req
-                max_active = max(max_active, len(active))
             if not active:
-                # idle until the next arrival
-                if pending:
-                    wait = pending[0].arrival - (clock() - t0) * time_scale
-                    if wait > 0:
-                        time.sleep(min(wait / time_scale, 0.01))
-                continue
-            # advance the batch up to the next completion (at most `chunk` steps)
+                self._admit(waiting, active, stamp)
+                max_active = max(max_active, len(active))
+                if not active:
+                    # idle until the next arrival
+                    if pending:
+                        wait = pending[0].arrival - stamp()
+                        if wait > 0:
+                            time.sleep(min(wait / time_scale, 0.01))
+                    continue
+            # launch the batch up to the next completion (at most `chunk` steps) ...
             nxt = min(ens.remaining(mid) for mid in active)
             n = max(1, min(self.chunk, nxt))
-            tb = clock()
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record(self.stream)
             ens.step(n)
-            ens.sync()
-            busy_s += clock() - tb
+            ev[1].record(self.stream)
+            events.append(ev)
             steps_run += n
-            now = (clock() - t0) * time_scale
+            # ... and while it runs, admit the arrivals (they join at the next step boundary)
+            now = stamp()
+            while pending and pending[0].arrival <= now:
+                waiting.append(pending.popleft())
+            self._admit(waiting, active, stamp)
+            max_active = max(max_active, len(active))
+            ens.sync()
             for mid in [mid for mid in active if ens.remaining(mid) == 0]:
                 req = active.pop(mid)
                 if self.keep:
@@ -165,10 +199,12 @@ class Server:
                 if st != 0:
                     raise RuntimeError(f"member {mid} (request {req.rid}) reported status {st}")
                 ens.remove(mid)
-                req.finished = (clock() - t0) * time_scale
+                req.finished = stamp()
                 total_cu += req.cell_updates
                 done.append(req)
-        wall = (clock() - t0) * time_scale
+        wall = stamp()
+        torch.cuda.synchronize()
+        busy_s = sum(a.elapsed_time(b) for a, b in events) * 1e-3 * time_scale
         lat = np.array([r.finished - r.arrival for r in done])
         return dict(
             requests=len(done), wall_s=wall, busy_s=busy_s, batch_steps=steps_run, max_active=max_active,

@@ -232,12 +232,24 @@ int  gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params *params,
  * member q, whose id goes to ids[q].  The host preparation of the members runs on up to 16
  * threads, their device set-up (one allocation each, the coefficients and fixed-point scales
  * built on the device) is queued on the ensemble's stream, and the call returns after one
- * synchronisation (the caller's arrays are then no longer needed; pinned ts and u are copied
- * without staging).  All or nothing: on an error no member of the call is admitted. */
+ * synchronisation (the caller's arrays are then no longer needed).  ts and u in memory from
+ * gb_ens_host_alloc are read by the device directly, from the start of the call (the transfer
+ * overlaps the host preparation); other arrays take one copy call each.  All or nothing: on
+ * an error no member of the call is admitted. */
 int  gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, const gb_go_params *params,
                      const gb_go_grid *grids, const double *const *ts, const double *const *u,
                      int32_t *ids);
 int  gb_ens_remove(gb_ens *e, int32_t member_id);
+
+/* Host memory for the arrays of the ensemble calls: page-locked and mapped into the devices'
+ * address space (cudaHostAlloc, mapped and portable).  Arrays that lie inside one such
+ * allocation are read (ts and u of gb_ens_add_many) and written (ts, rho and cost of
+ * gb_ens_download_many) by the device directly, in one batched kernel per call, instead of
+ * one copy call per array.  Other host memory is copied as before.  gb_ens_host_free takes
+ * the pointer gb_ens_host_alloc returned (GB_GO_EINVAL otherwise); the caller frees only
+ * memory that no call in progress uses. */
+int  gb_ens_host_alloc(size_t bytes, void **out);
+int  gb_ens_host_free(void *p);
 
 /* Advance every active member by `nsteps` steps. */
 int  gb_ens_step(gb_ens *e, int32_t nsteps);
@@ -259,9 +271,16 @@ int  gb_ens_download_stream(gb_ens *e, int32_t member_id, void *cuda_stream, dou
 /* gb_ens_download for n members at once: one kernel forms every member's arrays, their copies
  * are queued on the ensemble's stream behind the steps, and the call returns after one
  * synchronisation.  ts[q], rho[q], cost[q] receive member ids[q] (any of the three pointer
- * arrays, or entries of them, may be NULL; pinned host buffers are copied to without staging). */
+ * arrays, or entries of them, may be NULL).  Destinations in memory from gb_ens_host_alloc are
+ * written by one scatter kernel for the whole call; other destinations take one copy call each. */
 int  gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, double *const *ts, double *const *rho,
                           double *const *cost);
+/* Members with imld = 1 (the Kraus-Turner mixed layer, run in FP64 after the convective
+ * adjustment of every wet column): the wind mixing energy mldketau (maxi*maxj, Fortran
+ * (1:maxi, 1:maxj)) used from the next step on, as gb_go_set_mld_wind; and the mixed-layer depth
+ * and level of every column, as gb_go_download_mld.  GB_GO_EINVAL for a member with imld = 0. */
+int  gb_ens_set_mld_wind(gb_ens *e, int32_t member_id, const double *mldketau);
+int  gb_ens_download_mld(gb_ens *e, int32_t member_id, double *mld, int32_t *mldk);
 int  gb_ens_inventory(gb_ens *e, int32_t member_id, double *out);
 int  gb_ens_status(gb_ens *e, int32_t member_id, int32_t *status);
 int  gb_ens_sync(gb_ens *e);

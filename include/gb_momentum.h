@@ -18,7 +18,12 @@
  * reference's LU factors, one unit column at a time) and the right-hand side.  psi, ub and u
  * then agree with the reference's to a relative 1e-9 (the tests' tolerance), not bit for bit;
  * everything else follows the reference's operation order.  Grids up to GB_MO_MAX_PSI
- * streamfunction points (maxi*(maxj+1)); the inverse takes 8*(maxi*(maxj+1))^2 bytes.
+ * streamfunction points (maxi*(maxj+1)) use the inverse (8*(maxi*(maxj+1))^2 bytes).  Larger
+ * grids (up to GB_MO_MAX_PSI_BT points, rows of at most GB_MO_MAX_ROW) solve the same matrix in
+ * its block-tridiagonal form -- one block per row j of psi points, coupled to rows j-1 and j+1
+ * through diagonal blocks -- with the inverse Schur complements of its block LU factored at
+ * create (8*maxi^2*(maxj+1) bytes on the device, e.g. 188 MB for 360x180) and, per step, one
+ * matrix-vector product per block row forward and one backward; the same 1e-9 tolerance.
  *
  * Layouts are the reference's, column-major, with their Fortran lower bounds: e.g.
  * rh(3, 0:maxi+1, 0:maxj+1) at (l-1) + 3*(i + (maxi+2)*j); u(3, 0:maxi, 0:maxj, 1:maxk);
@@ -37,10 +42,14 @@ extern "C" {
 typedef struct gb_mo gb_mo;
 
 #define GB_MO_MAX_PSI 8192
+#define GB_MO_MAX_PSI_BT 1048576
+#define GB_MO_MAX_ROW 2048
 
-/* isles: islands (landmasses - 1, goldstein.f90:1505-1518), mpi: path array length (2*(maxi+maxj)) */
+/* isles: islands (landmasses - 1, goldstein.f90:1505-1518), mpi: path array length (2*(maxi+maxj));
+ * solver: 0 = by size (the inverse up to GB_MO_MAX_PSI points, else block-tridiagonal),
+ * 1 = block-tridiagonal at any size */
 typedef struct {
-    int32_t maxi, maxj, maxk, isles, mpi, pad;
+    int32_t maxi, maxj, maxk, isles, mpi, solver;
 } gb_mo_dims;
 
 typedef struct {

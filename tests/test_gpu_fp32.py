@@ -339,3 +339,39 @@ def test_ensemble_batched_download_equals_export_path(gpu_lib):
             assert np.array_equal(s[k], p[k]), k
             assert np.array_equal(s[k], g[k]), k
     e.close()
+
+
+def test_ensemble_mapped_host_arrays(gpu_lib):
+    """Arrays in mapped page-locked host memory (gb_ens_host_alloc): add_many reads ts and u
+    through the device address in its scatter kernel and download_many writes ts, rho and cost
+    there from its kernel.  Results equal those of ordinary host arrays bit for bit, every
+    element of the outputs is written, and gb_ens_host_free refuses a pointer it did not
+    allocate."""
+    import ctypes as C
+    import dataclasses
+    from cgenie_gb300.ensemble import Ensemble, host_copy, host_empty
+    mems = [grid.make_member(c) for c in grid.ensemble_configs(n=9, seed=27)]
+    mems.append(grid.make_member(grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=63, noise=2.0)))
+    hmems = [dataclasses.replace(m, ts=host_copy(m.ts), u=host_copy(m.u)) for m in mems]
+    a = Ensemble(use_graph=True)
+    ids_a = a.add_many(mems)
+    b = Ensemble(use_graph=True)
+    ids_b = b.add_many(hmems)
+    a.step(11)
+    b.step(11)
+    ref = a.download_many(ids_a)
+    outs = []
+    for m in mems:
+        o = dict(ts=host_empty(m.ts.shape), rho=host_empty(m.rho.shape), cost=host_empty(m.cost.shape))
+        for v in o.values():
+            v[...] = np.nan
+        outs.append(o)
+    b.download_many(ids_b, out=outs)
+    for r, o in zip(ref, outs):
+        for k in ("ts", "rho", "cost"):
+            assert not np.isnan(o[k]).any(), k
+            assert np.array_equal(r[k], o[k]), k
+    junk = np.zeros(4)
+    assert a.lib.gb_ens_host_free(C.c_void_p(junk.ctypes.data)) != 0
+    a.close()
+    b.close()

@@ -70,6 +70,58 @@ def test_mixed_layer_bitexact(gpu_lib, oracle, name):
     g.close()
 
 
+def test_mixed_layer_in_ensembles_within_fp32_bars(gpu_lib):
+    """imld = 1 members in the batched split-precision form, in a batch with imld = 0 members:
+    the column pass runs co and then the mixed layer in FP64 on the FP64 state, with the
+    previous step's rho(maxk) kept per column.  Against each member's FP64 run (bit-exact to
+    the oracle above): T and S within 1e-11, every tracer within 1e-6 (per tracer, relative to
+    its largest magnitude), convection counts and mixed-layer levels equal, depths within 1e-9;
+    also after a change of the wind mixing energy.  The imld = 0 batch-mates equal their runs
+    in a batch of their own, bit for bit."""
+    from cgenie_gb300.ensemble import Ensemble
+    from cgenie_gb300.goldstein import new_member_run
+    from test_gpu_long import per_tracer_errors
+    mld_mems = [grid.make_member(grid.MemberConfig(**c)) for c in CASES.values()]
+    plain = [grid.make_member(c) for c in grid.ensemble_configs(n=4, seed=31)]
+    ens = Ensemble(use_graph=True)
+    ids = ens.add_many(mld_mems + plain)
+    alone = Ensemble(use_graph=True)
+    ids_alone = alone.add_many(plain)
+    runs = [new_member_run(m, precision=abi.GB_GO_FP64) for m in mld_mems]
+    rng = np.random.default_rng(11)
+    winds = [np.ascontiguousarray(m.mldketau * rng.uniform(0.0, 3.0, m.mldketau.shape)) for m in mld_mems]
+    for phase in range(2):
+        ens.step(15)
+        alone.step(15)
+        for n, (m, g) in enumerate(zip(mld_mems, runs)):
+            g.tstepo(15)
+            out = ens.download(ids[n])
+            ref = g.download()
+            err = per_tracer_errors(m, out["ts"], ref["ts"])
+            assert np.all(err[:2] <= 1e-11), (n, phase, err)
+            assert np.all(err <= 1e-6), (n, phase, err)
+            assert np.array_equal(out["cost"], ref["cost"]), (n, phase)
+            mld, mldk = ens.download_mld(ids[n])
+            rmld, rmldk = g.download_mld()
+            assert np.array_equal(mldk, rmldk), (n, phase)
+            assert np.max(np.abs(mld - rmld)) <= 1e-9 * max(np.max(np.abs(rmld)), 1e-30), (n, phase)
+            assert ens.status(ids[n]) == 0
+            if phase == 0:
+                ens.set_mld_wind(ids[n], winds[n])
+                g.set_mld_wind(winds[n])
+        for mid, mida in zip(ids[len(mld_mems):], ids_alone):
+            a, b = ens.download(mid), alone.download(mida)
+            assert np.array_equal(a["ts"], b["ts"]) and np.array_equal(a["cost"], b["cost"])
+    wet = mld_mems[0].k1[1:-1, 1:-1] <= mld_mems[0].maxk
+    assert np.any(ens.download_mld(ids[0])[1][wet] < mld_mems[0].maxk - 1)
+    with pytest.raises(Exception):
+        ens.download_mld(ids[len(mld_mems)])
+    for g in runs:
+        g.close()
+    ens.close()
+    alone.close()
+
+
 def test_mixed_layer_rejections(gpu_lib):
     from cgenie_gb300.goldstein import Goldstein, GoldsteinError
     m = grid.make_member(grid.MemberConfig(**CASES["nowind"]))
