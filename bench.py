@@ -20,8 +20,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
   ocean36 the device-resident ocean step of a 36x36x16 basin with 8 tracers: momentum, then
       tstepo (split-precision form), and the BIOGEM tracer coupling every 5th step; `value` is
       tracer cell-updates/s of the whole step
-  ocean5 the same ocean step at the stress-test size, 360x180x32 with 24 tracers (65,160
-      streamfunction points: the block-tridiagonal streamfunction solve)
+  ocean5 the same ocean step at the stress-test size, 360x180x32 with 24 tracers and the
+      stress test's stable time step (1/2400 yr; 65,160 streamfunction points: the
+      block-tridiagonal streamfunction solve)
   mo36 the momentum step (wind, jbar, streamfunction, islands, velc) of a 36x36x16 basin
       with two islands, on the density of an FP64 handle; `value` is wet-cell momentum
       updates/s (each wet cell's u, v, w advanced one step)
@@ -72,7 +73,7 @@ WORKLOADS = {
     "ocean36": dict(name="ocean_step_36x36x16_L8_momentum_tracers_biogem", maxi=36, maxj=36, maxk=16, maxl=8,
                     couple_every=5),
     "ocean5": dict(name="ocean_step_360x180x32_L24_momentum_tracers_biogem", maxi=360, maxj=180, maxk=32, maxl=24,
-                   couple_every=5, cpu_steps=3),
+                   couple_every=5, cpu_steps=3, member_kw=dict(nyear=2400, diff_h=1000.0)),
 }
 
 
@@ -332,8 +333,6 @@ def run_bg(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = bg_cpu_rate(m, st)
             line["cpu_baseline"] = {"value": v, "unit": "tracer cell-couplings/s", "cores": 1, "kind": "port",
@@ -439,8 +438,6 @@ def run_ea(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = ea_cpu_rate(case)
             line["cpu_baseline"] = {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
@@ -548,8 +545,6 @@ def run_mo(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = mo_cpu_rate(m, case)
             line["cpu_baseline"] = {"value": v, "unit": "wet-cell momentum updates/s", "cores": 1, "kind": "port",
@@ -676,8 +671,6 @@ def run_rs(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n = rs_cpu_rate(m, target_s=10.0)
             line["cpu_baseline"] = {"value": v, "unit": "ocean cells written/s", "cores": 1, "kind": "port",
@@ -693,7 +686,7 @@ def run_ocean(args, rank, world, local, dist):
     from cgenie_gb300.goldstein import kernel_launch_count, new_member_run
     w = WORKLOADS[args.workload]
     m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=w["maxk"], maxl=w["maxl"], seed=41,
-                                           mask="basin_island", tracer_kind="bgc"))
+                                           mask="basin_island", tracer_kind="bgc", **w.get("member_kw", {})))
     case = momentum.make_case(m, seed=42)
     st = biogem.make_state(m, n_l_sed=4, seed=43)
     stream = torch.cuda.Stream()
@@ -750,8 +743,6 @@ def run_ocean(args, rank, world, local, dist):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             v, n, _ = ocean_cpu_rate(w, w.get("cpu_steps", 20))
             line["cpu_baseline"] = {"value": v, "unit": "tracer cell-updates/s", "cores": 1, "kind": "port",
@@ -769,7 +760,7 @@ def ocean_cpu_rate(w, steps):
     from cgenie_gb300 import biogem, grid, momentum
     from oracle import oracle_lib
     m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=w["maxk"], maxl=w["maxl"], seed=41,
-                                           mask="basin_island", tracer_kind="bgc"))
+                                           mask="basin_island", tracer_kind="bgc", **w.get("member_kw", {})))
     case = momentum.make_case(m, seed=42)
     st = biogem.make_state(m, n_l_sed=4, seed=43)
     om = oracle_lib.OracleMomentum(case)
@@ -1024,22 +1015,29 @@ def run_c3(args, rank, world, local, dist):
     hmems = [dataclasses.replace(m, ts=host_copy(m.ts), u=host_copy(m.u)) for m in mems]
     houts = [dict(ts=host_copy(np.zeros_like(m.ts)), rho=host_copy(np.zeros_like(m.rho)),
                   cost=host_copy(np.zeros_like(m.cost))) for m in mems]
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
-    ids2 = e2.add_many(hmems)
-    t1 = time.perf_counter()
-    e2.step(args.steps)
-    e2.sync()
-    t2 = time.perf_counter()
-    outs = e2.download_many(ids2, out=houts)
-    torch.cuda.synchronize()
-    t3 = time.perf_counter()
+    def e2e_job():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        e2 = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
+        ids2 = e2.add_many(hmems)
+        t1 = time.perf_counter()
+        e2.step(args.steps)
+        e2.sync()
+        t2 = time.perf_counter()
+        outs = e2.download_many(ids2, out=houts)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        e2.close()
+        return t0, t1, t2, t3, outs
+
+    # one untimed job first (first-use costs of the mapped buffers and the memory pool), then
+    # the timed job: the whole sequence again from a new ensemble
+    e2e_job()
+    t0, t1, t2, t3, outs = e2e_job()
     e2e_s = job_time(t3 - t0, dist, "cuda")
     e2e_parts = {"admit_s": round(t1 - t0, 5), "steps_s": round(t2 - t1, 5), "download_s": round(t3 - t2, 5)}
-    e2.close()
     e2e_value = all_cu_step * args.steps / e2e_s
     h2d = sum(m.ts.nbytes + m.u.nbytes for m in mems) / args.steps
     d2h = sum(o["ts"].nbytes + o["rho"].nbytes + o["cost"].nbytes for o in outs) / args.steps
@@ -1085,7 +1083,8 @@ def run_c3(args, rank, world, local, dist):
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "parts": e2e_parts,
                     "note": f"whole job through the C-ABI: admit {w['members']} members from mapped pinned host arrays, "
-                            f"{args.steps} steps, download every member into mapped pinned host arrays"},
+                            f"{args.steps} steps, download every member into mapped pinned host arrays; the "
+                            f"second of two identical jobs (the first absorbs first-use costs)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
@@ -1268,7 +1267,7 @@ def main():
                        "precision": "fp32flux" if args.precision == "fp32flux" else "fp64 plain",
                        "l2": "flushed before every timed step", "parallelism": f"replicas{world}"},
             "e2e": {"value": e2e_value, "unit": "tracer cell-updates/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "parts": e2e_parts,
+                    "d2h_bytes_per_step": d2h,
                     "note": "per step: forcing + u H2D (pinned), step, rho D2H; L2 not flushed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
@@ -1279,8 +1278,6 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        if serving is not None:
-            line["serving"] = serving
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(m)
         print(json.dumps(line))

@@ -501,7 +501,8 @@ extern "C" int gb_bg_tracercoupling(gb_bg *h, gb_go_handle *ocean)
     if (o.device != h->device) return bfail(h, GB_GO_EINVAL, "tracercoupling: handles on different devices");
     BG_TRY(h, cudaSetDevice(h->device));
     // the split-precision form: its current state in Fortran layout first (into ts_buf[cur])
-    if (ocean_refresh_rho(ocean) != GB_GO_OK) return bfail(h, GB_GO_ECUDA, std::string("tracercoupling: ") + gb_go_last_error(ocean));
+    if (const int rr = ocean_refresh_rho(ocean))
+        return bfail(h, rr, std::string("tracercoupling: ") + gb_go_last_error(ocean));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     BgArgs a = args_of(h);
     // go_ts: the wet cells of the current step buffer once the handle has stepped

@@ -141,6 +141,7 @@ struct Fp32Data {
     unsigned int *status = nullptr;
     unsigned long long *diag = nullptr;
     float *stencil = nullptr;   // diso or iediff: the per-step top-face stencil (kStencilWords per cell)
+    double *rhos = nullptr;     // imld = 1: rho(maxk) per column as the previous step left it
     int *stencil_list = nullptr;   // {0}: the member's descriptor index for the prepass when stepped alone
     int4 *items = nullptr;      // work items when stepped alone: (0, patch, group)
     int nitems = 0;
@@ -186,6 +187,12 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s);
 // current state -> ts_cur (Fortran layout, halo columns) and rho
 int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s);
+// the last CUDA error the FP32-path checks saw in this thread
+const char *fp32_cuda_error_string();
+// imld = 1: the handle's mixed-layer arrays (wind energy, outputs; mlddec, mlddecd Fortran-indexed
+// [1..maxk]) and rho(maxk) of the uploaded density rho (NI, NJ, maxk+1) as the previous step's
+int fp32_member_set_mixed_layer(Fp32Member *f, const double *mldketau, double *mld, int32_t *mldk, const double *mlddec,
+                                const double *mlddecd, const double *rho, cudaStream_t s);
 // current state -> dst (Fortran layout)
 int fp32_member_fortran(Fp32Member *f, double *dst, cudaStream_t s);
 

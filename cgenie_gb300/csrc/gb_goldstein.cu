@@ -482,7 +482,7 @@ int ocean_refresh_rho(gb_go_handle *h)
 {
     if (h->precision != GB_GO_FP32FLUX || h->steps_since_upload == 0) return GB_GO_OK;
     const int r = fp32_member_export(&h->f32, h->ts_buf[h->cur], h->rho, h->ts_static, h->stream);
-    return r ? fail(h, r, std::string("fp32 export failed: ") + cudaGetErrorString(cudaPeekAtLastError())) : GB_GO_OK;
+    return r ? fail(h, r, std::string("fp32 export failed: ") + fp32_cuda_error_string()) : GB_GO_OK;
 }
 
 int ocean_velocity_changed(gb_go_handle *h)
@@ -534,6 +534,12 @@ extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const doubl
     if (h->precision == GB_GO_FP32FLUX) {
         int r = fp32_member_upload(&h->f32, ts1, ts, h->ts_buf[0], h->stream);
         if (r) return fail(h, r, "fp32 upload failed");
+        if (h->p.imld == 1) {
+            // the mixed layer's arrays, and rho(maxk) of the uploaded rho as the previous step's
+            r = fp32_member_set_mixed_layer(&h->f32, h->mldketau, h->mld, h->mldk, h->m.mlddec, h->m.mlddecd, h->rho,
+                                            h->stream);
+            if (r) return fail(h, r, "fp32 mixed-layer set-up failed");
+        }
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;

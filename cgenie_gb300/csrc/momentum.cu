@@ -972,7 +972,7 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
     if (o.device != h->device) return mfail(h, GB_GO_EINVAL, "step: handles on different devices");
     MO_TRY(h, cudaSetDevice(h->device));
     // the split-precision form's density is formed from its current state first
-    if (ocean_refresh_rho(ocean) != GB_GO_OK) return mfail(h, GB_GO_ECUDA, std::string("step: ") + gb_go_last_error(ocean));
+    if (const int rr = ocean_refresh_rho(ocean)) return mfail(h, rr, std::string("step: ") + gb_go_last_error(ocean));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     a.rho = o.rho;
     if (h->graph && (h->graph_rho != o.rho || h->graph_u != o.u || h->graph_stream != s)) {

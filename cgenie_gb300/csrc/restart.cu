@@ -567,8 +567,8 @@ int pack_fields(gb_go_handle *ocean, unsigned long long *dev, OceanState &o, boo
     if (int r = check_dims(o.d.maxi, o.d.maxj, o.d.maxk)) return r;
     cudaError_t e = cudaSetDevice(o.device);
     if (e != cudaSuccess) return rs_fail(GB_GO_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
-    if (export_state && ocean_refresh_rho(ocean) != GB_GO_OK)   // the split-precision form exports its state
-        return rs_fail(GB_GO_ECUDA, std::string("restart: state export failed: ") + gb_go_last_error(ocean));
+    if (const int rr = export_state ? ocean_refresh_rho(ocean) : GB_GO_OK)   // the split-precision form exports its state
+        return rs_fail(rr, std::string("restart: state export failed: ") + gb_go_last_error(ocean));
     if (!dev) return GB_GO_OK;
     const size_t n = (size_t)o.d.maxi * o.d.maxj * o.d.maxk;
     // two cells per thread; at most one wave of 8 resident 256-thread blocks on each of 152 SMs

@@ -341,8 +341,8 @@ extern "C" int gb_ts_diagnose(gb_ts_handle *h, gb_go_handle *ocean, double *sums
     if (!o.state_ready) return tsfail(h, GB_GO_ENOTREADY, "ocean state not uploaded");
     TS_TRY(h, cudaSetDevice(h->device));
     // the split-precision form exports its state (Fortran layout) and rho first
-    if (ocean_refresh_rho(ocean) != GB_GO_OK)
-        return tsfail(h, GB_GO_ECUDA, std::string("state export failed: ") + gb_go_last_error(ocean));
+    if (const int rr = ocean_refresh_rho(ocean))
+        return tsfail(h, rr, std::string("state export failed: ") + gb_go_last_error(ocean));
     cudaStream_t s = (cudaStream_t)o.stream;
     const double *ts = o.steps_since_upload > 0 ? o.ts_buf[o.cur] : o.ts_static;
     const int L = d.maxl;

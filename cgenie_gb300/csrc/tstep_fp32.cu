@@ -42,6 +42,18 @@
 
 namespace gbgo {
 
+// The last CUDA error this file's checks saw in this thread (for the callers' messages).
+static thread_local cudaError_t tl_cuda_error = cudaSuccess;
+
+static int launch_status()
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) tl_cuda_error = e;
+    return e == cudaSuccess ? 0 : GB_GO_ECUDA;
+}
+
+const char *fp32_cuda_error_string() { return cudaGetErrorString(tl_cuda_error); }
+
 // ---------------------------------------------------------------------------
 // bit-level conversions (exact, integer pipe)
 
@@ -782,7 +794,7 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
 {
     if (n <= 0) return 0;
     k_rescale<<<std::min(n, 1024), 32, 0, s>>>(descs, n);
-    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    return launch_status();
 }
 
 // Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step listed
@@ -846,6 +858,9 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
                     for (int kk = 1; kk <= maxk; ++kk) rold[kk] = col.rho[kk];
                     Fp32Col c0 = col;
                     c0.w = md.buf[par];
+                    // the first step after an upload reads the uploaded ts (the step itself starts
+                    // from ts1), as the reference's first tstepo does
+                    if (step == md.origin) c0.k1 = maxk + 1;
                     const double *top = md.ts_static + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * (maxk + 1)));
                     ml.zw = zw;
                     ml.zro = zro;
@@ -983,7 +998,7 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         kern<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
                                                                          step_ctr, rel, b.kmax);
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    return launch_status();
 }
 
 int fp32_launches_per_step(const Fp32Batch &b)
@@ -1663,7 +1678,7 @@ int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t 
         k_setup_scales_many<<<nq, 64, 0, s>>>(it);
         count_launches(5);
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    return launch_status();
 }
 
 static int planar_copy(double *planar, double *fortran, const Dims &d, int to, cudaStream_t s)
@@ -1672,7 +1687,7 @@ static int planar_copy(double *planar, double *fortran, const Dims &d, int to, c
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 8192);
     k_to_planar<<<std::max(1, blocks), 256, 0, s>>>(planar, fortran, d, to);
     count_launches(1);
-    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    return launch_status();
 }
 
 int fp32_to_planar(double *planar, const double *fortran, const Dims &d, cudaStream_t s)
@@ -1696,7 +1711,7 @@ int fp32_export(const MemberDesc &md, const double *planar, double *cur, double 
     k_export_halo<<<std::max(1, (int)std::min<size_t>((2 * (size_t)md.maxj * md.maxk + 255) / 256, 1024)), 256, 0, s>>>(
         md, const_cast<double *>(cur), rho);
     count_launches(2);
-    return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+    return launch_status();
 }
 
 }  // namespace gbgo
@@ -1728,10 +1743,6 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (d.L > kFp32MaxL) {
         msg = "GB_GO_FP32FLUX supports at most 32 tracers per grid";
         return GB_GO_ERANGE;
-    }
-    if (p.imld != 0) {
-        msg = "GB_GO_FP32FLUX does not provide imld=1 (use GB_GO_FP64)";
-        return GB_GO_EUNSUPPORTED;
     }
     const int nj = d.maxj + 2, nk = d.maxk + 2;
     const double *dtp = blob.data() + 8 * nj + 5 * nk;
@@ -1773,6 +1784,8 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaMemset(D.gmax, 0, (size_t)d.L * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&D.mk, 6 * (size_t)nk * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.mj, 3 * (size_t)nj * sizeof(double));
+    if (e == cudaSuccess && p.imld == 1) e = cudaMalloc(&D.rhos, (size_t)d.maxi * d.maxj * sizeof(double));
+    if (e == cudaSuccess && p.imld == 1) e = cudaMemset(D.rhos, 0, (size_t)d.maxi * d.maxj * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&D.status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&D.dev, sizeof(MemberDesc));
     if (e == cudaSuccess) e = cudaMalloc(&D.step_ctr, sizeof(long long));
@@ -1829,7 +1842,7 @@ void fp32_member_free(Fp32Member *f)
     Fp32Data &D = h->data;
     cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.tref); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
-    cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.stencil); cudaFree(D.stencil_list);
+    cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.stencil); cudaFree(D.stencil_list); cudaFree(D.rhos);
     if (D.s2) cudaStreamDestroy(D.s2);
     if (D.fork) cudaEventDestroy(D.fork);
     if (D.join) cudaEventDestroy(D.join);
@@ -1881,6 +1894,37 @@ int fp32_member_reload(Fp32Member *f, const double *ts1_dev, cudaStream_t s)
     return cuda_ok(cudaStreamSynchronize(s));
 }
 
+__global__ void k_surface_rho(const double *rho, double *rhos, int maxi, int maxj, int maxk, int NI, int NJ)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= maxi * maxj) return;
+    const int i = c % maxi + 1, j = c / maxi + 1;
+    rhos[c] = rho[(size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * maxk)];
+}
+
+int fp32_member_set_mixed_layer(Fp32Member *f, const double *mldketau, double *mld, int32_t *mldk, const double *mlddec,
+                                const double *mlddecd, const double *rho, cudaStream_t s)
+{
+    Fp32Host *h = host_of(f);
+    Fp32Data &D = h->data;
+    if (h->p.imld != 1 || !D.rhos) return GB_GO_EINVAL;
+    MemberDesc &md = D.host;
+    md.imld = 1;
+    md.mldpebuoycoeff = h->p.mldpebuoycoeff;
+    md.mlddec = mlddec;
+    md.mlddecd = mlddecd;
+    md.mldketau = mldketau;
+    md.mld = mld;
+    md.mldk = mldk;
+    md.rhos = D.rhos;
+    D.desc_valid = false;
+    const int ncol = h->d.maxi * h->d.maxj;
+    k_surface_rho<<<(ncol + 127) / 128, 128, 0, s>>>(rho, D.rhos, h->d.maxi, h->d.maxj, h->d.maxk, h->d.NI, h->d.NJ);
+    count_launches(1);
+    if (launch_status()) return GB_GO_ECUDA;
+    return cuda_ok(cudaStreamSynchronize(s));
+}
+
 int fp32_member_set_top(Fp32Member *f, const double *top_host, cudaStream_t s)
 {
     Fp32Host *h = host_of(f);
@@ -1905,7 +1949,7 @@ int fp32_member_set_velocity(Fp32Member *f, const double *u_host, const double *
         k_build_coef<<<std::max(1, blocks), 256, 0, s>>>(u_dev, m, h->d, h->p, D.coef, D.coefl);
         k_build_div<<<std::max(1, blocks), 256, 0, s>>>(h->d, D.coef, D.coefl);
         count_launches(2);
-        return cudaGetLastError() == cudaSuccess ? 0 : GB_GO_ECUDA;
+        return launch_status();
     }
     Fp32Static st;
     fp32_build_static(h->d, h->p, h->blob, h->k1.data(), u_host, st);
@@ -1954,6 +1998,7 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         md.status = D.status;
         md.diag = diag;
         md.stencil = D.stencil;
+        if (h->p.imld == 1 && !md.rhos) return GB_GO_ENOTREADY;   // fp32_member_set_mixed_layer first
         if (cudaMemcpyAsync(D.dev, &md, sizeof(md), cudaMemcpyHostToDevice, s) != cudaSuccess) return GB_GO_ECUDA;
         if (cudaStreamSynchronize(s) != cudaSuccess) return GB_GO_ECUDA;
         D.desc_valid = true;
@@ -2015,8 +2060,12 @@ int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double 
     int r = fp32_export(md, D.plan_buf[D.steps & 1], ts_cur, rho, s);
     if (r) return r;
     unsigned int st = 0;
-    if (cudaMemcpyAsync(&st, D.status, sizeof(st), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GB_GO_ECUDA;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return GB_GO_ECUDA;
+    cudaError_t e = cudaMemcpyAsync(&st, D.status, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        tl_cuda_error = e;
+        return GB_GO_ECUDA;
+    }
     if (st & 1u) return GB_GO_ENONFINITE;
     if (st & 6u) return GB_GO_ERANGE;
     return 0;

@@ -52,7 +52,7 @@ extern "C" {
 /* Error codes. */
 #define GB_GO_OK            0
 #define GB_GO_EINVAL       -1   /* bad argument (NULL pointer, size, flag value) */
-#define GB_GO_EUNSUPPORTED -2   /* option combination not implemented (e.g. imld=1 with GB_GO_FP32FLUX) */
+#define GB_GO_EUNSUPPORTED -2   /* option combination not implemented (e.g. GB_GO_FP32FLUX with per-level dt) */
 #define GB_GO_ECUDA        -3   /* a CUDA runtime call failed */
 #define GB_GO_ENOMEM       -4   /* device allocation failed or over the memory budget */
 #define GB_GO_ENOTREADY    -5   /* state/velocity not uploaded yet */
@@ -91,7 +91,7 @@ typedef struct gb_go_params {
     int32_t ediffpow2i;   /* 0, 1, 2 or any other value for the general power */
     int32_t iconv;        /* 0: co only; 1: coshuffle before co */
     int32_t imld;         /* 0, or 1: Kraus-Turner mixed layer after co (goldstein.f90:2294-2390,
-                             3337-3442); GB_GO_FP64 single grids only */
+                             3337-3442); both precision forms, single grids and ensembles */
     int32_t diso;         /* non-zero: isoneutral (Redi) branch on */
     int32_t precision;    /* GB_GO_FP64 or GB_GO_FP32FLUX */
     int32_t reserved;     /* must be 0 */

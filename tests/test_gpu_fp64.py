@@ -152,10 +152,7 @@ def test_error_codes(gpu_lib):
     import ctypes as C
     from cgenie_gb300.abi import GridRefs
     h = C.c_void_p()
-    # the mixed layer: FP64 single grids only; imld is 0 or 1; imld = 1 needs its inputs
-    r = GridRefs(m, imld=1, precision=abi.GB_GO_FP32FLUX)
-    assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,
-                                C.byref(h)) == abi.GB_GO_EUNSUPPORTED
+    # the mixed layer: imld is 0 or 1; imld = 1 needs its inputs
     r = GridRefs(m)
     r.params.imld = 2
     assert gpu_lib.gb_go_create(C.byref(r.dims), C.byref(r.params), C.byref(r.grid), -1,

@@ -122,6 +122,40 @@ def test_mixed_layer_in_ensembles_within_fp32_bars(gpu_lib):
     alone.close()
 
 
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_layer_split_precision_handle(gpu_lib, name):
+    """imld = 1 on a single grid in the split-precision form, against the same grid in the FP64
+    form (bit-exact to the oracle above), including a first step whose uploaded ts differs from
+    ts1 at the surface and a change of the wind energy: T and S within 1e-11, every tracer
+    within 1e-6, convection counts and mixed-layer levels equal, depths within 1e-9."""
+    from cgenie_gb300.goldstein import new_member_run
+    from test_gpu_long import per_tracer_errors
+    m = grid.make_member(grid.MemberConfig(**CASES[name]))
+    kk = np.arange(m.maxk + 2)[:, None, None]
+    wet_top = (kk == m.maxk) & (m.k1[None] <= m.maxk)
+    m.ts[..., 0] = np.where(wet_top, m.ts[..., 0] + 0.25, m.ts[..., 0])
+    f = new_member_run(m, precision=abi.GB_GO_FP32FLUX)
+    g = new_member_run(m, precision=abi.GB_GO_FP64)
+    rng = np.random.default_rng(13)
+    wind = np.ascontiguousarray(m.mldketau * rng.uniform(0.0, 3.0, m.mldketau.shape))
+    for phase in range(2):
+        f.tstepo(9)
+        g.tstepo(9)
+        a, b = f.download(), g.download()
+        err = per_tracer_errors(m, a["ts"], b["ts"])
+        assert np.all(err[:2] <= 1e-11), (phase, err)
+        assert np.all(err <= 1e-6), (phase, err)
+        assert np.array_equal(a["cost"], b["cost"]), phase
+        mld, mldk = f.download_mld()
+        rmld, rmldk = g.download_mld()
+        assert np.array_equal(mldk, rmldk), phase
+        assert np.max(np.abs(mld - rmld)) <= 1e-9 * max(np.max(np.abs(rmld)), 1e-30), phase
+        f.set_mld_wind(wind)
+        g.set_mld_wind(wind)
+    f.close()
+    g.close()
+
+
 def test_mixed_layer_rejections(gpu_lib):
     from cgenie_gb300.goldstein import Goldstein, GoldsteinError
     m = grid.make_member(grid.MemberConfig(**CASES["nowind"]))
@@ -133,6 +167,3 @@ def test_mixed_layer_rejections(gpu_lib):
         g.set_mld_wind(m.mldketau)
     assert e.value.code == abi.GB_GO_EINVAL
     g.close()
-    with pytest.raises(GoldsteinError) as e:
-        Goldstein(m, precision=abi.GB_GO_FP32FLUX)
-    assert e.value.code == abi.GB_GO_EUNSUPPORTED
