@@ -941,7 +941,7 @@ def run_c3(args, rank, world, local, dist):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ens = Ensemble(device=local, use_graph=True, stream=stream.cuda_stream)
-    ids = [ens.add(m) for m in mems]
+    ids = ens.add_many(mems)
     if args.steps_before:
         ens.step(args.steps_before)
     for _ in range(args.warmup):
