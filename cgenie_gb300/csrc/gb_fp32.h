@@ -187,6 +187,8 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
                      int32_t *icosd, unsigned long long *diag, int *slot, int nsteps, cudaStream_t s);
 // current state -> ts_cur (Fortran layout, halo columns) and rho
 int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s);
+// rho of the current state only (no Fortran-layout export of the tracers)
+int fp32_member_rho(Fp32Member *f, double *rho, const double *ts_static, cudaStream_t s);
 // the last CUDA error the FP32-path checks saw in this thread
 const char *fp32_cuda_error_string();
 // imld = 1: the handle's mixed-layer arrays (wind energy, outputs; mlddec, mlddecd Fortran-indexed

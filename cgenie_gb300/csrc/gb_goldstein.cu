@@ -485,6 +485,13 @@ int ocean_refresh_rho(gb_go_handle *h)
     return r ? fail(h, r, std::string("fp32 export failed: ") + fp32_cuda_error_string()) : GB_GO_OK;
 }
 
+int ocean_refresh_rho_only(gb_go_handle *h)
+{
+    if (h->precision != GB_GO_FP32FLUX || h->steps_since_upload == 0) return GB_GO_OK;
+    const int r = fp32_member_rho(&h->f32, h->rho, h->ts_static, h->stream);
+    return r ? fail(h, r, std::string("fp32 density failed: ") + fp32_cuda_error_string()) : GB_GO_OK;
+}
+
 int ocean_velocity_changed(gb_go_handle *h)
 {
     if (h->precision != GB_GO_FP32FLUX) {

@@ -118,6 +118,8 @@ int ocean_state(gb_go_handle *h, OceanState *out);
 // the split-precision form keeps its state group-planar and forms rho on export: bring rho up to
 // date with the current state (a no-op for the FP64 form)
 int ocean_refresh_rho(gb_go_handle *h);
+// the split-precision form's rho only (callers that read rho and not the tracers)
+int ocean_refresh_rho_only(gb_go_handle *h);
 // velocities written on the device: the split-precision form rebuilds its transfer
 // coefficients from them (on the device; the first velocity field must come from the host)
 int ocean_velocity_changed(gb_go_handle *h);

@@ -179,36 +179,53 @@ __global__ void __launch_bounds__(256) k_psi(MoDev a)
 //   forward   z_j = T_j (g_j - l_j o z_{j-1})       (T_j = S_j^-1, z_{-1} = 0)
 //   backward  x_J = z_J,  x_j = z_j - T_j (u_j o x_{j+1})
 // one launch per block row, one warp per row of T_j (contiguous), x overwriting z in place.
-__global__ void __launch_bounds__(256) k_bt_forward(MoDev a, int j)
+// One row of T_j per 64 threads (two warps: each thread's products issued together, then a
+// shuffle sum per warp and one shared add), four rows per 256-thread block.
+constexpr int kBtRowThreads = 64, kBtRowsPerBlock = 4;
+
+__device__ __forceinline__ double bt_row_sum(double s, double *part)
 {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int n = a.maxi;
-    if (w >= n) return;
-    const double *row = a.btT + ((size_t)j * n + w) * n;
-    const double *g = a.gb + (size_t)j * n;
-    const double *l = a.btl + (size_t)j * n;
-    const double *zp = a.btz + (size_t)(j > 0 ? j - 1 : 0) * n;
-    double s = 0.0;
-    for (int c = lane; c < n; c += 32) {
-        const double y = j > 0 ? g[c] - l[c] * zp[c] : g[c];
-        s = s + row[c] * y;
-    }
     for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) a.btz[(size_t)j * n + w] = s;
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) part[w] = s;
+    __syncthreads();
+    return part[w & ~1] + part[w | 1];   // the row's two warps, in one order
 }
 
-__global__ void __launch_bounds__(256) k_bt_backward(MoDev a, int j)
+__global__ void __launch_bounds__(kBtRowThreads * kBtRowsPerBlock) k_bt_forward(MoDev a, int j)
 {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    __shared__ double part[kBtRowsPerBlock * 2];
     const int n = a.maxi;
-    if (w >= n) return;
-    const double *row = a.btT + ((size_t)j * n + w) * n;
-    const double *u = a.btu + (size_t)j * n;
-    const double *xn = a.btz + (size_t)(j + 1) * n;
+    const int r = blockIdx.x * kBtRowsPerBlock + threadIdx.x / kBtRowThreads, c0 = threadIdx.x % kBtRowThreads;
     double s = 0.0;
-    for (int c = lane; c < n; c += 32) s = s + row[c] * (u[c] * xn[c]);
-    for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) a.btz[(size_t)j * n + w] = a.btz[(size_t)j * n + w] - s;
+    if (r < n) {
+        const double *row = a.btT + ((size_t)j * n + r) * n;
+        const double *g = a.gb + (size_t)j * n;
+        const double *l = a.btl + (size_t)j * n;
+        const double *zp = a.btz + (size_t)(j > 0 ? j - 1 : 0) * n;
+        for (int c = c0; c < n; c += kBtRowThreads) {
+            const double y = j > 0 ? g[c] - l[c] * zp[c] : g[c];
+            s = s + row[c] * y;
+        }
+    }
+    s = bt_row_sum(s, part);
+    if (r < n && c0 == 0) a.btz[(size_t)j * n + r] = s;
+}
+
+__global__ void __launch_bounds__(kBtRowThreads * kBtRowsPerBlock) k_bt_backward(MoDev a, int j)
+{
+    __shared__ double part[kBtRowsPerBlock * 2];
+    const int n = a.maxi;
+    const int r = blockIdx.x * kBtRowsPerBlock + threadIdx.x / kBtRowThreads, c0 = threadIdx.x % kBtRowThreads;
+    double s = 0.0;
+    if (r < n) {
+        const double *row = a.btT + ((size_t)j * n + r) * n;
+        const double *u = a.btu + (size_t)j * n;
+        const double *xn = a.btz + (size_t)(j + 1) * n;
+        for (int c = c0; c < n; c += kBtRowThreads) s = s + row[c] * (u[c] * xn[c]);
+    }
+    s = bt_row_sum(s, part);
+    if (r < n && c0 == 0) a.btz[(size_t)j * n + r] = a.btz[(size_t)j * n + r] - s;
 }
 
 // psi from the solution (psi(i, j) = x(i + j*maxi), psi(0, j) = psi(maxi, j))
@@ -972,7 +989,7 @@ extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
     if (o.device != h->device) return mfail(h, GB_GO_EINVAL, "step: handles on different devices");
     MO_TRY(h, cudaSetDevice(h->device));
     // the split-precision form's density is formed from its current state first
-    if (const int rr = ocean_refresh_rho(ocean)) return mfail(h, rr, std::string("step: ") + gb_go_last_error(ocean));
+    if (const int rr = ocean_refresh_rho_only(ocean)) return mfail(h, rr, std::string("step: ") + gb_go_last_error(ocean));
     cudaStream_t s = static_cast<cudaStream_t>(o.stream);
     a.rho = o.rho;
     if (h->graph && (h->graph_rho != o.rho || h->graph_u != o.u || h->graph_stream != s)) {
@@ -1017,9 +1034,10 @@ static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u)
     k_bp<<<(ncol + 31) / 32, 32, 0, s>>>(a);
     k_rhs<<<(a.nm + 31) / 32, 32, 0, s>>>(a);
     if (a.bt) {
-        const int nb = (a.maxi * 32 + 255) / 256, J = a.nm / a.maxi - 1;
-        for (int j = 0; j <= J; ++j) k_bt_forward<<<nb, 256, 0, s>>>(a, j);
-        for (int j = J - 1; j >= 0; --j) k_bt_backward<<<nb, 256, 0, s>>>(a, j);
+        const int nb = (a.maxi + kBtRowsPerBlock - 1) / kBtRowsPerBlock, J = a.nm / a.maxi - 1;
+        const int nt = kBtRowThreads * kBtRowsPerBlock;
+        for (int j = 0; j <= J; ++j) k_bt_forward<<<nb, nt, 0, s>>>(a, j);
+        for (int j = J - 1; j >= 0; --j) k_bt_backward<<<nb, nt, 0, s>>>(a, j);
         k_bt_psi<<<(a.nm + 127) / 128, 128, 0, s>>>(a);
     } else {
         k_psi<<<(a.nm * 32 + 255) / 256, 256, 0, s>>>(a);

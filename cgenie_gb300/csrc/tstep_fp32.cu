@@ -2046,19 +2046,48 @@ int fp32_member_fortran(Fp32Member *f, double *dst, cudaStream_t s)
     return fp32_from_planar(dst, h->data.plan_buf[h->data.steps & 1], h->d, s);
 }
 
-int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s)
+// rho of the current state without the Fortran-layout export of the tracers: interior cells
+// from T and S of the group-planar state (wet) or of the uploaded state (dry), wet halo cells
+// from their periodic source column -- the values k_export_fp32 and k_export_halo give
+__global__ void k_rho_fp32(const MemberDesc md, const double *planar, double *rho)
 {
-    Fp32Host *h = host_of(f);
-    Fp32Data &D = h->data;
+    const int maxi = md.maxi, maxj = md.maxj, maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ;
+    const size_t ncell = (size_t)maxj * maxk * (maxi + 2);
+    const double *zro = md.mk + 3 * (maxk + 2);
+    EosCoef ec;
+    for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
+    ec.ieos = md.ieos;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % (maxi + 2));
+        const int j = (int)((c / (maxi + 2)) % maxj) + 1;
+        const int k = (int)(c / ((size_t)(maxi + 2) * maxj)) + 1;
+        const size_t o = (size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k);
+        const int kk = md.k1[i + NI * j];
+        if (i >= 1 && i <= maxi) {
+            if (k >= kk) rho[o] = eos_rn(ec, planar[o * 2], planar[o * 2 + 1], zro[k]);
+            else rho[o] = eos_rn(ec, md.ts_static[o * L], md.ts_static[o * L + 1], zro[k]);
+        } else if (k >= kk) {
+            const int src = i == 0 ? maxi : 1;
+            const size_t os = (size_t)src + (size_t)NI * ((size_t)j + (size_t)NJ * k);
+            rho[o] = eos_rn(ec, planar[os * 2], planar[os * 2 + 1], zro[k]);
+        }
+    }
+}
+
+static MemberDesc export_desc(Fp32Host *h, const double *ts_static)
+{
     MemberDesc md{};
     md.maxi = h->d.maxi; md.maxj = h->d.maxj; md.maxk = h->d.maxk; md.L = h->d.L; md.NI = h->d.NI; md.NJ = h->d.NJ;
     md.ieos = h->p.ieos;
     for (int n = 0; n < 5; ++n) md.ec[n] = h->p.ec[n];
     md.ts_static = ts_static;
-    md.mk = D.mk;
+    md.mk = h->data.mk;
     md.k1 = h->k1_dev;
-    int r = fp32_export(md, D.plan_buf[D.steps & 1], ts_cur, rho, s);
-    if (r) return r;
+    return md;
+}
+
+static int member_status(Fp32Data &D, cudaStream_t s)
+{
     unsigned int st = 0;
     cudaError_t e = cudaMemcpyAsync(&st, D.status, sizeof(st), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -2069,6 +2098,28 @@ int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double 
     if (st & 1u) return GB_GO_ENONFINITE;
     if (st & 6u) return GB_GO_ERANGE;
     return 0;
+}
+
+int fp32_member_rho(Fp32Member *f, double *rho, const double *ts_static, cudaStream_t s)
+{
+    Fp32Host *h = host_of(f);
+    Fp32Data &D = h->data;
+    const MemberDesc md = export_desc(h, ts_static);
+    const size_t ncell = (size_t)md.maxj * md.maxk * (md.maxi + 2);
+    k_rho_fp32<<<(int)std::min<size_t>((ncell + 255) / 256, 4096), 256, 0, s>>>(md, D.plan_buf[D.steps & 1], rho);
+    count_launches(1);
+    if (launch_status()) return GB_GO_ECUDA;
+    return member_status(D, s);
+}
+
+int fp32_member_export(Fp32Member *f, double *ts_cur, double *rho, const double *ts_static, cudaStream_t s)
+{
+    Fp32Host *h = host_of(f);
+    Fp32Data &D = h->data;
+    const MemberDesc md = export_desc(h, ts_static);
+    int r = fp32_export(md, D.plan_buf[D.steps & 1], ts_cur, rho, s);
+    if (r) return r;
+    return member_status(D, s);
 }
 
 }  // namespace gbgo

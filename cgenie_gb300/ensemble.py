@@ -110,35 +110,69 @@ class Ensemble:
 
     def add_many(self, members, steps=None, **kw) -> list:
         """Admit several members in one call per tile shape (gb_ens_add_many: host preparation
-        on up to 16 threads inside the library, one synchronisation).  All or nothing: when a
-        call fails, the members this method admitted before it leave again.  `steps`: per
-        member, its remaining-step count (set_remaining), or None.  Returns the ids in order."""
+        on up to 16 threads inside the library, one synchronisation).  The calls run on a worker
+        thread in order, smallest group first, while this thread builds the next group's
+        arguments (ctypes releases the GIL during a call).  All or nothing: when a call fails,
+        the members this method admitted before it leave again.  `steps`: per member, its
+        remaining-step count (set_remaining), or None.  Returns the ids in order."""
+        from concurrent.futures import ThreadPoolExecutor
+
         from .abi import GbDims, GbGrid, GbParams
         members = list(members)
         ids = [None] * len(members)
         groups = {}
         for n, m in enumerate(members):
             groups.setdefault(self._tile_for(m), []).append(n)
-        try:
-            for tile, idx in groups.items():
-                if tile != self._current_tile:
-                    self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
-                    self._current_tile = tile
-                k = len(idx)
-                refs = [GridRefs(members[n], precision=abi.GB_GO_FP32FLUX, **kw) for n in idx]
-                tss = [np.ascontiguousarray(members[n].ts, dtype=np.float64) for n in idx]
-                us = [np.ascontiguousarray(members[n].u, dtype=np.float64) for n in idx]
-                dims = (GbDims * k)(*[r.dims for r in refs])
-                params = (GbParams * k)(*[r.params for r in refs])
-                grids = (GbGrid * k)(*[r.grid for r in refs])
-                out = (C.c_int32 * k)()
-                vp = C.c_void_p
-                self._check(self.lib.gb_ens_add_many(self.e, k, dims, params, grids,
-                                                     (vp * k)(*[abi.addr(a) for a in tss]),
-                                                     (vp * k)(*[abi.addr(a) for a in us]), out), "gb_ens_add_many")
-                for n, mid in zip(idx, out):
+        vp = C.c_void_p
+
+        def arguments(idx):
+            k = len(idx)
+            refs = [GridRefs(members[n], precision=abi.GB_GO_FP32FLUX, **kw) for n in idx]
+            tss = [np.ascontiguousarray(members[n].ts, dtype=np.float64) for n in idx]
+            us = [np.ascontiguousarray(members[n].u, dtype=np.float64) for n in idx]
+            return (refs, tss, us, (GbDims * k)(*[r.dims for r in refs]), (GbParams * k)(*[r.params for r in refs]),
+                    (GbGrid * k)(*[r.grid for r in refs]), (vp * k)(*[abi.addr(a) for a in tss]),
+                    (vp * k)(*[abi.addr(a) for a in us]))
+
+        def call(tile, idx, args):
+            if tile != self._current_tile:
+                self.set_tuning(tile_i=tile[0], tile_j=tile[1], use_graph=self.use_graph)
+                self._current_tile = tile
+            out = (C.c_int32 * len(idx))()
+            _, _, _, dims, params, grids, tsp, up = args
+            rc = self.lib.gb_ens_add_many(self.e, len(idx), dims, params, grids, tsp, up, out)
+            return rc, list(out)
+
+        order = sorted(groups.items(), key=lambda g: len(g[1]))
+        pending = None   # (indices, arguments kept alive, future) of the call in flight
+
+        def collect():
+            # the call in flight: its ids are recorded (admitted or not) before anything else
+            nonlocal pending
+            pidx, _, fut = pending
+            pending = None
+            rc, out = fut.result()
+            if rc == 0:
+                for n, mid in zip(pidx, out):
                     ids[n] = int(mid)
                     self.members[int(mid)] = members[n]
+            self._check(rc, "gb_ens_add_many")
+
+        try:
+            with ThreadPoolExecutor(max_workers=1) as pool:
+                try:
+                    for tile, idx in order:
+                        args = arguments(idx)
+                        if pending is not None:
+                            collect()
+                        pending = (idx, args, pool.submit(call, tile, idx, args))
+                    collect()
+                finally:
+                    if pending is not None:
+                        try:
+                            collect()
+                        except Exception:
+                            pass
         except BaseException:
             for mid in ids:
                 if mid is not None:
