@@ -404,7 +404,7 @@ struct Prepared {
     // [copied, zeroed), then the arrays the device fills
     size_t o_blob, o_mj, o_rvol, o_mk, o_dsj, o_tmax, o_gmax, o_k1, o_tref, o_gtop, o_ptab, o_ediff1;
     size_t o_mlddec, o_mldketau, o_rhos, copied;
-    size_t o_rho, o_cost, o_icosd, o_gmaxu, o_diag, o_status, o_cd, o_scale, o_mld, o_mldk, zeroed;
+    size_t o_rho, o_cost, o_icosd, o_gmaxu, o_diag, o_status, o_cd, o_scale, o_ext, o_mld, o_mldk, zeroed;
     size_t o_buf0, o_buf1, o_static, o_stage, o_vel, o_coef, o_coefl, o_stencil, total;
     std::vector<char> host;        // the copied segment
     int rc = GB_GO_OK;
@@ -484,7 +484,13 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     const int L = dims->maxl, NI = pm.d.NI, NJ = pm.d.NJ, maxi = dims->maxi, maxj = dims->maxj, maxk = dims->maxk;
     const size_t ntop = (size_t)L * NI * NJ;
     fp32_gtop(pm.d, pm.p, pm.blob, ts + ntop * (maxk + 1), pm.gtop);
-    fp32_tracer_maxima(pm.d, grid->k1, ts, pm.gtop.data(), pm.tref, pm.tmax, pm.gmax);
+    // the offsets and maxima of the tracers are found on the device (the set-up's extrema
+    // kernel reads the uploaded state); the forcing's maxima here
+    pm.tref.assign(L, 0.0f);
+    pm.tmax.assign(L, 0.0);
+    pm.gmax.assign(L, 0.0);
+    for (size_t c = 0; c < (size_t)dims->maxi * dims->maxj; ++c)
+        for (int l = 0; l < L; ++l) pm.gmax[l] = std::max(pm.gmax[l], (double)std::fabs(pm.gtop[c * (L + 2) + l]));
     for (int j = 1; j <= maxj; ++j)
         for (int i = 1; i <= maxi; ++i) {
             const int k1 = grid->k1[i + (size_t)NI * j];
@@ -530,6 +536,7 @@ int prepare_member(gb_ens *e, const gb_ens_tuning &tuning, const gb_go_dims *dim
     pm.o_status = take(4);
     pm.o_cd = take(2 * 8);
     pm.o_scale = take((size_t)L * 4);
+    pm.o_ext = take((size_t)2 * L * 8);
     pm.o_mld = take(mldon ? ncol * 8 : 0);
     pm.o_mldk = take(mldon ? ncol * 4 : 0);
     pm.zeroed = off;
@@ -680,6 +687,7 @@ static int commit_member(gb_ens *e, Prepared &pm, int32_t *member_id, SetupItem 
     item->tmax = m->tmaxd;
     item->gmax = m->gmaxd;
     item->tref = m->tref;
+    item->ext = (unsigned long long *)(b + pm.o_ext);
     item->scale = m->scale;
     MemberDesc &md = m->desc;
     md.maxi = dims->maxi; md.maxj = dims->maxj; md.maxk = maxk; md.L = L;

@@ -245,15 +245,18 @@ struct SetupItem {
     double *buf0, *buf1;
     float *coef, *coefl;
     unsigned long long *cd;
-    const double *tmax, *gmax;
-    const float *tref;
+    double *tmax;               // written by the set-up: max over wet cells of |T - tref|
+    const double *gmax;
+    float *tref;                // written by the set-up: the per-tracer offsets
+    unsigned long long *ext;    // 2 L words, zeroed: order keys of the wet maxima and (inverted) minima
     int32_t *scale;
 };
 // Device part of the set-up of n ensemble members (items in device memory; stream order, no
-// synchronisation), five launches in all: both state buffers from the uploaded ts; the transfer
+// synchronisation), six launches in all: both state buffers from the uploaded ts; the transfer
 // coefficients from u as fp32_build_static builds them (words 0-5, then the divergence pair);
 // their largest face sums and divergence into cd[0], cd[1] (double bits, cd zeroed beforehand);
-// the fixed-point scales from cd and the per-tracer maxima (fp32_transfer_bound,
+// the extremes of every tracer over the wet cells (ext); then the offsets and maxima of
+// fp32_tracer_maxima from them and the fixed-point scales from cd (fp32_transfer_bound,
 // fp32_scale_of).  max_elems / max_cells: the largest state (L x cells) and interior cell count
 // of the items.
 int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t max_cells, cudaStream_t s);

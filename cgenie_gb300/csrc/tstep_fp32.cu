@@ -1658,10 +1658,65 @@ __global__ void k_setup_stats_many(const SetupItem *it)
     coef_stats_cells(I.d, I.p, I.m, I.u, I.coef, I.cd, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
                      (size_t)gridDim.x * blockDim.x);
 }
+// order key of a double: unsigned comparison of keys is the comparison of the values
+__device__ __forceinline__ unsigned long long order_key_u(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k)
+{
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// the extremes of every tracer over the member's wet interior cells: ext[2l] the largest key,
+// ext[2l+1] the largest inverted key (the smallest value); shared-memory maxima per block
+__global__ void __launch_bounds__(256) k_setup_extrema_many(const SetupItem *it)
+{
+    __shared__ unsigned long long sh[2 * kFp32MaxL];
+    const SetupItem &I = it[blockIdx.y];
+    const int L = I.d.L, maxi = I.d.maxi, maxj = I.d.maxj, NI = I.d.NI, NJ = I.d.NJ;
+    for (int e = threadIdx.x; e < 2 * L; e += blockDim.x) sh[e] = 0ull;
+    __syncthreads();
+    const size_t nij = (size_t)maxi * maxj, n = nij * I.d.maxk * L;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(e % L);
+        const size_t c = e / L;
+        const int i = (int)(c % maxi) + 1, j = (int)((c / maxi) % maxj) + 1, k = (int)(c / nij) + 1;
+        if (k < I.m.k1[i + (size_t)NI * j]) continue;
+        const double v = I.ts_static[(size_t)l + (size_t)L * ((size_t)i + (size_t)NI * ((size_t)j + (size_t)NJ * k))];
+        const unsigned long long key = order_key_u(v);
+        atomicMax(&sh[2 * l], key);
+        atomicMax(&sh[2 * l + 1], ~key);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * L; e += blockDim.x)
+        if (sh[e]) atomicMax(&I.ext[e], sh[e]);
+}
+
+// the offsets and maxima of fp32_tracer_maxima from the extremes, then the scales
 __global__ void k_setup_scales_many(const SetupItem *it)
 {
     const SetupItem &I = it[blockIdx.x];
-    member_scales(I.cd, I.tmax, I.gmax, I.tref, I.d.L, I.scale);
+    const int L = I.d.L;
+    for (int l = threadIdx.x; l < L; l += blockDim.x) {
+        const unsigned long long kh = I.ext[2 * l], kl = I.ext[2 * l + 1];
+        float tr = 0.0f;
+        double tm = 0.0;
+        if (kh != 0ull) {   // the tracer has wet cells
+            const double hi = key_value(kh), lo = key_value(~kl);
+            if (l >= 2 && ((lo > 0.0 && lo > __dmul_rn(0.5, hi)) || (hi < 0.0 && hi < __dmul_rn(0.5, lo)))) {
+                int ex = 0;
+                const double f = frexp(__dmul_rn(0.5, __dadd_rn(lo, hi)), &ex);
+                tr = (float)ldexp(rint(__dmul_rn(f, 256.0)), ex - 8);
+            }
+            tm = fmax(fabs(__dadd_rn(lo, -(double)tr)), fabs(__dadd_rn(hi, -(double)tr)));
+        }
+        I.tref[l] = tr;
+        I.tmax[l] = tm;
+    }
+    __syncthreads();
+    member_scales(I.cd, I.tmax, I.gmax, I.tref, L, I.scale);
 }
 
 int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t max_cells, cudaStream_t s)
@@ -1675,8 +1730,9 @@ int fp32_setup_many(const SetupItem *items_dev, int n, size_t max_elems, size_t 
         k_setup_coef_many<<<dim3(cb, nq), 256, 0, s>>>(it);
         k_setup_div_many<<<dim3(cb, nq), 256, 0, s>>>(it);
         k_setup_stats_many<<<dim3(cb, nq), 256, 0, s>>>(it);
+        k_setup_extrema_many<<<dim3(pb, nq), 256, 0, s>>>(it);
         k_setup_scales_many<<<nq, 64, 0, s>>>(it);
-        count_launches(5);
+        count_launches(6);
     }
     return launch_status();
 }
