@@ -41,6 +41,7 @@ class Request:
     finished: float = math.nan
     cell_updates: int = 0
     member_id: int = -1
+    steps_left: int = 0
     result: Optional[dict] = None
 
 
@@ -145,6 +146,7 @@ class Server:
             req.member_id = mid
             req.admitted = now
             req.cell_updates = self._wet(m) * req.maxl * req.steps
+            req.steps_left = req.steps     # the library's remaining-step count, kept on the host
             active[mid] = req
 
     def run(self, requests, clock: Callable[[], float] = time.perf_counter, time_scale: float = 1.0):
@@ -176,14 +178,16 @@ class Server:
                             time.sleep(min(wait / time_scale, 0.01))
                     continue
             # launch the batch up to the next completion (at most `chunk` steps) ...
-            nxt = min(ens.remaining(mid) for mid in active)
-            n = max(1, min(self.chunk, nxt))
+            left = {mid: req.steps_left for mid, req in active.items()}
+            n = max(1, min(self.chunk, min(left.values())))
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(self.stream)
             ens.step(n)
             ev[1].record(self.stream)
             events.append(ev)
             steps_run += n
+            for req in active.values():   # the members of this chunk (admissions below join later)
+                req.steps_left -= n
             # ... and while it runs, admit the arrivals (they join at the next step boundary)
             now = stamp()
             while pending and pending[0].arrival <= now:
@@ -191,7 +195,7 @@ class Server:
             self._admit(waiting, active, stamp)
             max_active = max(max_active, len(active))
             ens.sync()
-            for mid in [mid for mid in active if ens.remaining(mid) == 0]:
+            for mid in [mid for mid, req in active.items() if req.steps_left == 0]:
                 req = active.pop(mid)
                 if self.keep:
                     req.result = ens.download(mid)
