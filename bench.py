@@ -1064,6 +1064,7 @@ def run_c3(args, rank, world, local, dist):
     alg = sum(algorithmic_bytes(m) for m in mems)
     achieved = alg / (total_ms * 1e-3 / args.steps) / 1e9
     traffic = profile_traffic("k_step_fp32", w["name"])
+    l2_bytes = profile_traffic("l2_bytes_transfer_kernels", w["name"])
     if rank == 0:
         line = {
             "metric": "tracer cell-updates/s", "value": value, "unit": "tracer cell-updates/s",
@@ -1089,7 +1090,11 @@ def run_c3(args, rank, world, local, dist):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
                          "algorithmic_bytes_per_launch": alg,
-                         "note": "achieved = algorithmic bytes of a step (16 L + 24 per wet cell, k1) / step time"},
+                         "note": "achieved = algorithmic bytes of a step (16 L + 24 per wet cell, k1) / step time",
+                         "l2": None if l2_bytes is None else {
+                             "bytes_per_step": l2_bytes, "gbs": l2_bytes / (total_ms * 1e-3 / args.steps) / 1e9,
+                             "note": "L2 traffic of the two transfer kernels per step (ncu, 64-member capture scaled "
+                                     "to this ensemble) over the measured step time"}},
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
