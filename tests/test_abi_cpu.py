@@ -74,3 +74,18 @@ def test_autotune_candidates_start_with_planner_choice():
         assert all(64 <= tx * ty <= 128 for tx, ty in c[1:])
     assert autotune.lookup({"36x36x16": [12, 9, 1.0]}, 36, 36, 16) == (12, 9)
     assert autotune.lookup({}, 36, 36, 16) is None
+
+
+def test_host_memory_calls_refuse_bad_arguments_without_gpu():
+    """gb_ens_host_alloc / gb_ens_host_free validate their arguments before any CUDA call:
+    a zero size or NULL result pointer, and a pointer the allocator did not return, are
+    GB_GO_EINVAL."""
+    from cgenie_gb300 import build, goldstein
+    build.build()
+    lib = goldstein.load_library()
+    p = C.c_void_p()
+    assert lib.gb_ens_host_alloc(C.c_size_t(0), C.byref(p)) == abi.GB_GO_EINVAL
+    assert lib.gb_ens_host_alloc(C.c_size_t(64), None) == abi.GB_GO_EINVAL
+    buf = (C.c_char * 64)()
+    assert lib.gb_ens_host_free(C.cast(buf, C.c_void_p)) == abi.GB_GO_EINVAL
+    assert lib.gb_ens_host_free(None) == abi.GB_GO_EINVAL
