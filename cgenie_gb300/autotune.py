@@ -61,6 +61,15 @@ def lookup(table: Dict[str, list], maxi: int, maxj: int, maxk: int) -> Optional[
     return (int(v[0]), int(v[1])) if v else None
 
 
+BATCH_KEY = "batch"   # [packing, ctas_per_sm, rate]: the launch-wide settings of a mixed batch
+
+
+def batch_entry(table: Dict[str, list]) -> Tuple[int, int]:
+    """The autotuned member packing and CTA cap of the batch, (0, 0) when none is stored."""
+    v = table.get(BATCH_KEY)
+    return (int(v[0]), int(v[1])) if v else (0, 0)
+
+
 def make_members(shape: Shape, members: int = 64, seed: int = 5):
     """Seeded members of one grid shape with 2-24 tracers (the ensemble's mix)."""
     import numpy as np
@@ -72,11 +81,14 @@ def make_members(shape: Shape, members: int = 64, seed: int = 5):
             for _ in range(members)]
 
 
-def time_shape(mems, tile: Tuple[int, int], steps: int = 30) -> float:
-    """Tracer cell-updates/s of the batched step (CUDA graph) on `mems` with one tile shape;
-    0 when the shape does not fit the kernel limits on some member."""
+def time_shape(mems, tile: Tuple[int, int], steps: int = 30, packing: int = 0, ctas_per_sm: int = 0,
+               use_table: bool = False) -> float:
+    """Tracer cell-updates/s of the batched step (CUDA graph) on `mems` with one tile shape
+    ((0, 0) with use_table: the table's tiles per member), member packing and CTA cap; 0 when
+    the shape does not fit the kernel limits on some member."""
     from .ensemble import Ensemble
-    ens = Ensemble(tile_i=tile[0], tile_j=tile[1], use_graph=True, use_table=False)
+    ens = Ensemble(tile_i=tile[0], tile_j=tile[1], use_graph=True, use_table=use_table, packing=packing,
+                   ctas_per_sm=ctas_per_sm)
     try:
         ens.add_many(mems)
     except Exception:
@@ -122,5 +134,37 @@ def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), m
     return table
 
 
+def tune_batch(members: int = 96, steps: int = 30, path: str = TABLE_PATH, verbose: bool = True,
+               packings: Iterable[int] = (0, 1, 2), caps: Iterable[int] = (0, 3, 4)) -> Dict[str, list]:
+    """Member packing and CTA cap of a mixed batch (the three grid shapes, 2-24 tracers, the
+    stored tiles): every combination is timed and the best stored when it beats the default
+    (members packed together, no cap) by more than run-to-run noise."""
+    table = load_table(path)
+    shapes = ((18, 18, 16), (36, 36, 16), (36, 36, 32))
+    mems = []
+    for n, shape in enumerate(shapes):
+        mems += make_members(shape, members // len(shapes), seed=11 + n)
+    rates = {}
+    for pk in packings:
+        for cap in caps:
+            rates[(pk, cap)] = time_shape(mems, (0, 0), steps=steps, packing=pk, ctas_per_sm=cap, use_table=True)
+            if verbose:
+                print(f"packing {pk} ctas_per_sm {cap}: {rates[(pk, cap)]:.3e} cell-updates/s", flush=True)
+    best = max(rates, key=rates.get)
+    if best == (0, 0) or rates[best] < NOISE * rates[(0, 0)]:
+        table.pop(BATCH_KEY, None)
+    else:
+        table[BATCH_KEY] = [best[0], best[1], rates[best]]
+    with open(path, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    if verbose:
+        print(f"batch: best packing {best[0]}, ctas_per_sm {best[1]} ({rates[best]:.3e})", flush=True)
+    return table
+
+
 if __name__ == "__main__":
-    tune()
+    import sys
+    if "--batch" in sys.argv:
+        tune_batch()
+    else:
+        tune()

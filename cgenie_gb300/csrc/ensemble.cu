@@ -235,7 +235,7 @@ struct gb_ens {
     int cocap = 0;
     int *work = nullptr;                // device work counters (two, by step parity)
     bool dirty = true;
-    gb_ens_tuning tuning{0, 0, 0, 0};
+    gb_ens_tuning tuning{0, 0, 0, 0, GB_ENS_PACK_MEMBERS, 0};
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     std::string last_error;
@@ -363,6 +363,9 @@ extern "C" int gb_ens_set_tuning(gb_ens *e, const gb_ens_tuning *t)
     // over the kernel limits for a member falls back to the chosen one
     if (t->tile_i < 0 || t->tile_j < 0 || t->tile_i > 4096 || t->tile_j > 4096)
         return efail(e, GB_GO_EINVAL, "tile sizes must be in 0..4096");
+    if (t->ctas_per_sm < 0 || t->ctas_per_sm > 32) return efail(e, GB_GO_EINVAL, "ctas_per_sm must be in 0..32");
+    if (t->packing < GB_ENS_PACK_MEMBERS || t->packing > GB_ENS_PACK_ROUND_ROBIN || t->reserved != 0)
+        return efail(e, GB_GO_EINVAL, "unknown packing");
     e->tuning = *t;
     e->dirty = true;
     return GB_GO_OK;
@@ -971,17 +974,44 @@ static int rebuild(gb_ens *e)
         ++slot;
     }
     std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
-    // transfer items (member, patch, group) with a patch's groups and a member's patches next to
-    // each other: items taken together share the coefficients and ring columns in L2.  The co
-    // column list holds at most every wet column of the batch.
+    // transfer items (member, patch, group), T-S items first, in the tuning's packing order.
+    // GB_ENS_PACK_MEMBERS: a patch's groups and a member's patches next to each other (items
+    // taken together share the coefficients and ring columns in L2).  The co column list holds
+    // at most every wet column of the batch.
     std::vector<int4> it;
-    for (auto &o : order)
-        for (size_t n = 0; n < o.second->poff.size(); ++n) it.push_back(make_int4(o.second->slot, o.second->poff[n], 0, 0));
+    auto add_items = [&](bool ts) {
+        struct Cand {
+            double cost;
+            size_t rank;
+            int4 item;
+        };
+        std::vector<Cand> c;
+        size_t rank = 0;
+        for (auto &o : order) {
+            const Member *m = o.second;
+            const int ng = fp32_group_count(m->d.L);
+            for (size_t n = 0; n < m->poff.size(); ++n)
+                for (int g = ts ? 0 : 1; g < (ts ? 1 : ng); ++g) {
+                    int g0, gl;
+                    fp32_group(m->d.L, g, &g0, &gl);
+                    // cost: the patch's estimate times the group's share of the tracers
+                    const double w = m->pcost[n] * (double)gl / (double)m->d.L;
+                    // round robin: patch index first, then the member order
+                    const size_t rr = (n << 20) + (rank << 5) + (size_t)g;
+                    c.push_back(Cand{w, e->tuning.packing == GB_ENS_PACK_ROUND_ROBIN ? rr : c.size(),
+                                     make_int4(m->slot, m->poff[n], g, 0)});
+                }
+            ++rank;
+        }
+        if (e->tuning.packing == GB_ENS_PACK_ITEMS)
+            std::stable_sort(c.begin(), c.end(), [](const Cand &a, const Cand &b) { return a.cost > b.cost; });
+        else if (e->tuning.packing == GB_ENS_PACK_ROUND_ROBIN)
+            std::stable_sort(c.begin(), c.end(), [](const Cand &a, const Cand &b) { return a.rank < b.rank; });
+        for (const Cand &x : c) it.push_back(x.item);
+    };
+    add_items(true);
     const int n_ts = (int)it.size();
-    for (auto &o : order)
-        for (size_t n = 0; n < o.second->poff.size(); ++n)
-            for (int g = 1; g < fp32_group_count(o.second->d.L); ++g)
-                it.push_back(make_int4(o.second->slot, o.second->poff[n], g, 0));
+    add_items(false);
     int cocap = 0;
     for (auto &o : order) cocap += o.second->wet_cols;
     if ((int)it.size() > e->cap_items) {
@@ -1042,6 +1072,7 @@ static Fp32Batch batch_of(gb_ens *e)
     b.stencil_list = e->stencil_list;
     b.n_stencil = e->n_stencil;
     b.stencil_blocks = e->stencil_blocks;
+    b.ctas_per_sm = e->tuning.ctas_per_sm;
     return b;
 }
 

@@ -304,6 +304,7 @@ struct Fp32Batch {
     bool co_general = false;   // some member has iconv = 1, ieos != 0, imld = 1 or maxk > 32
     const int *stencil_list = nullptr;   // descriptor indices of the members with a stencil
     int n_stencil = 0, stencil_blocks = 1;   // their count; blocks per member of the prepass
+    int ctas_per_sm = 0;        // cap on resident CTAs per SM of the transfer kernels (0: none)
 };
 // s2/fork/join: a second stream and two events to run the two item kinds side by side
 // (s2 null: one stream).

@@ -939,7 +939,7 @@ int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).tota
 template <bool ISO, bool TS>
 static void launch_step_instance(const MemberDesc *descs, const int4 *items, int nitems, int P,
                                  const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap,
-                                 int nsm, cudaStream_t s)
+                                 int nsm, int ctas_cap, cudaStream_t s)
 {
     if (nitems <= 0) return;
     const int smem_bytes = fp32_smem_layout(P).total;
@@ -947,6 +947,7 @@ static void launch_step_instance(const MemberDesc *descs, const int4 *items, int
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
+    if (ctas_cap > 0) per_sm = std::min(per_sm, ctas_cap);
     if (per_sm < 1) per_sm = 1;
     const int grid = std::max(1, std::min(nitems, nsm * per_sm));
     kern<<<grid, kFp32Threads, smem_bytes, s>>>(descs, items, nitems, step_ctr, rel, work, P, colist, cocount, cocap);
@@ -974,14 +975,14 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
     cudaStream_t sb = two ? s2 : s;
     if (b.iso) {
         launch_step_instance<true, true>(b.descs, b.items, b.n_ts, P, step_ctr, rel, b.work, b.colist,
-                                         b.cocount, b.cocap, nsm, s);
+                                         b.cocount, b.cocap, nsm, b.ctas_per_sm, s);
         launch_step_instance<true, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel, b.work + 2,
-                                          b.colist, b.cocount, b.cocap, nsm, sb);
+                                          b.colist, b.cocount, b.cocap, nsm, b.ctas_per_sm, sb);
     } else {
         launch_step_instance<false, true>(b.descs, b.items, b.n_ts, P, step_ctr, rel, b.work, b.colist,
-                                          b.cocount, b.cocap, nsm, s);
+                                          b.cocount, b.cocap, nsm, b.ctas_per_sm, s);
         launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel,
-                                           b.work + 2, b.colist, b.cocount, b.cocap, nsm, sb);
+                                           b.work + 2, b.colist, b.cocount, b.cocap, nsm, b.ctas_per_sm, sb);
     }
     if (two) {
         cudaEventRecord(join, s2);

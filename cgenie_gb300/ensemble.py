@@ -47,7 +47,10 @@ def host_copy(a) -> np.ndarray:
 
 class Ensemble:
     def __init__(self, device: int = -1, hbm_budget_bytes: int = 0, *, tile_i: int = 0, tile_j: int = 0,
-                 use_graph: bool = False, stream: Optional[int] = None, use_table: bool = True):
+                 use_graph: bool = False, stream: Optional[int] = None, use_table: bool = True,
+                 packing: Optional[int] = None, ctas_per_sm: Optional[int] = None):
+        """packing / ctas_per_sm: the batch's member packing (abi.GB_ENS_PACK_*) and cap on resident
+        CTAs per SM; None = the autotuned values of the tuning table (else 0 and 0)."""
         self.lib = load_library()
         e = C.c_void_p()
         rc = self.lib.gb_ens_create(int(device), C.c_size_t(hbm_budget_bytes), C.byref(e))
@@ -59,8 +62,11 @@ class Ensemble:
         self.tile = (int(tile_i), int(tile_j))
         self.use_graph = bool(use_graph)
         self._current_tile = None
-        from .autotune import load_table
+        from .autotune import batch_entry, load_table
         self.table = load_table() if use_table else {}
+        tuned = batch_entry(self.table)
+        self.packing = int(tuned[0] if packing is None else packing)
+        self.ctas_per_sm = int(tuned[1] if ctas_per_sm is None else ctas_per_sm)
         self.set_tuning(tile_i=tile_i, tile_j=tile_j, use_graph=use_graph)
         if stream is not None:
             self._check(self.lib.gb_ens_set_stream(self.e, C.c_void_p(stream)), "gb_ens_set_stream")
@@ -70,8 +76,11 @@ class Ensemble:
             detail = self.lib.gb_ens_last_error(self.e).decode() if self.e else ""
             raise GoldsteinError(rc, what, detail)
 
-    def set_tuning(self, tile_i=0, tile_j=0, ctas_per_sm=0, use_graph=False):
-        t = GbEnsTuning(int(tile_i), int(tile_j), int(ctas_per_sm), int(bool(use_graph)))
+    def set_tuning(self, tile_i=0, tile_j=0, ctas_per_sm=None, use_graph=False, packing=None):
+        """gb_ens_set_tuning; ctas_per_sm / packing None: the ensemble's batch settings."""
+        cps = self.ctas_per_sm if ctas_per_sm is None else int(ctas_per_sm)
+        pk = self.packing if packing is None else int(packing)
+        t = GbEnsTuning(int(tile_i), int(tile_j), cps, int(bool(use_graph)), pk, 0)
         self._check(self.lib.gb_ens_set_tuning(self.e, C.byref(t)), "gb_ens_set_tuning")
 
     def close(self):

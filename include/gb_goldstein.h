@@ -208,9 +208,21 @@ typedef struct gb_ens gb_ens;
 
 typedef struct gb_ens_tuning {
     int32_t tile_i, tile_j;   /* columns per work item (0 = autotuned default) */
-    int32_t ctas_per_sm;      /* persistent CTAs per SM (0 = default) */
+    int32_t ctas_per_sm;      /* at most this many persistent CTAs per SM for the transfer
+                                 kernels (0 = as many as fit) */
     int32_t use_graph;        /* capture a multi-step launch in a CUDA graph */
+    int32_t packing;          /* order of the work items in the launch (member packing):
+                                 GB_ENS_PACK_MEMBERS, GB_ENS_PACK_ITEMS or GB_ENS_PACK_ROUND_ROBIN */
+    int32_t reserved;         /* 0 */
 } gb_ens_tuning;
+
+/* Member packing: members by decreasing work, each member's patches together and a patch's
+ * tracer groups together (neighbouring items share coefficients and ring columns in L2) */
+#define GB_ENS_PACK_MEMBERS     0
+/* work items by decreasing cost over the whole batch (longest first, the shortest tail) */
+#define GB_ENS_PACK_ITEMS       1
+/* the n-th patch of every member, then the (n+1)-th (DRAM traffic spread over members) */
+#define GB_ENS_PACK_ROUND_ROBIN 2
 
 int  gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out);
 void gb_ens_destroy(gb_ens *e);

@@ -37,7 +37,7 @@ def test_struct_layouts():
     assert C.sizeof(abi.GbParams) == (7 + 3) * 8 + 8 * 4 + 8
     # 19 pointers, dphi and rdphi, 3 pointers of the mixed-layer scheme
     assert C.sizeof(abi.GbGrid) == 19 * 8 + 2 * 8 + 3 * 8
-    assert C.sizeof(abi.GbEnsTuning) == 16
+    assert C.sizeof(abi.GbEnsTuning) == 24
     assert C.sizeof(abi.GbBgDims) == 24
     assert C.sizeof(abi.GbBgParams) == 24
     assert C.sizeof(abi.GbEaDims) == 8

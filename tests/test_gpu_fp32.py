@@ -375,3 +375,33 @@ def test_ensemble_mapped_host_arrays(gpu_lib):
     assert a.lib.gb_ens_host_free(C.c_void_p(junk.ctypes.data)) != 0
     a.close()
     b.close()
+
+
+def test_ensemble_packing_and_cta_cap_do_not_change_results(gpu_lib):
+    """The member packing (order of the work items) and the cap on resident CTAs per SM change
+    only which CTA takes which item: every member's result is bit-identical, and a bad value is
+    refused."""
+    from cgenie_gb300 import abi
+    from cgenie_gb300.ensemble import Ensemble
+    from cgenie_gb300.goldstein import GoldsteinError
+    mems = [grid.make_member(c) for c in grid.ensemble_configs(n=12, seed=29)]
+    ref = None
+    for packing, cap in ((abi.GB_ENS_PACK_MEMBERS, 0), (abi.GB_ENS_PACK_ITEMS, 0), (abi.GB_ENS_PACK_ROUND_ROBIN, 2),
+                         (abi.GB_ENS_PACK_ITEMS, 1)):
+        e = Ensemble(use_graph=True, packing=packing, ctas_per_sm=cap)
+        ids = e.add_many(mems)
+        e.step(9)
+        out = e.download_many(ids)
+        e.close()
+        if ref is None:
+            ref = out
+            continue
+        for a, b in zip(ref, out):
+            for k in ("ts", "rho", "cost"):
+                assert np.array_equal(a[k], b[k]), (packing, cap, k)
+    e = Ensemble()
+    with pytest.raises(GoldsteinError):
+        e.set_tuning(packing=7)
+    with pytest.raises(GoldsteinError):
+        e.set_tuning(ctas_per_sm=-1)
+    e.close()
