@@ -57,8 +57,10 @@ def load_table(path: str = TABLE_PATH) -> Dict[str, list]:
 
 
 def lookup(table: Dict[str, list], maxi: int, maxj: int, maxk: int) -> Optional[Tuple[int, int]]:
+    """The stored tile of a grid shape; None when none is stored or the planner's own choice
+    (stored as 0, 0) won."""
     v = table.get(f"{maxi}x{maxj}x{maxk}")
-    return (int(v[0]), int(v[1])) if v else None
+    return (int(v[0]), int(v[1])) if v and (int(v[0]), int(v[1])) != (0, 0) else None
 
 
 BATCH_KEY = "batch"   # [packing, ctas_per_sm, rate]: the launch-wide settings of a mixed batch
@@ -107,8 +109,9 @@ def time_shape(mems, tile: Tuple[int, int], steps: int = 30, packing: int = 0, c
 
 def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), members: int = 64,
          steps: int = 30, path: str = TABLE_PATH, verbose: bool = True) -> Dict[str, list]:
-    """Time every candidate tile of each shape (the planner's choice included) and store the
-    shapes whose best tile beats the planner's."""
+    """Time every candidate tile of each shape (the planner's choice included) and store, per
+    shape, the best tile when it beats the planner's by more than run-to-run noise, else the
+    planner's (0, 0); with the rate."""
     table = load_table(path)
     for shape in shapes:
         mems = make_members(shape, members)
@@ -124,7 +127,7 @@ def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), m
         key = f"{shape[0]}x{shape[1]}x{shape[2]}"
         planner = next(r for t, r in rates if t == (0, 0))
         if best[0] == (0, 0) or best[1] < NOISE * planner:
-            table.pop(key, None)     # the planner's choice is as good: no entry
+            table[key] = [0, 0, planner]     # the planner's choice is as good
         else:
             table[key] = [best[0][0], best[0][1], best[1]]
         if verbose:
@@ -137,8 +140,8 @@ def tune(shapes: Iterable[Shape] = ((18, 18, 16), (36, 36, 16), (36, 36, 32)), m
 def tune_batch(members: int = 96, steps: int = 30, path: str = TABLE_PATH, verbose: bool = True,
                packings: Iterable[int] = (0, 1, 2), caps: Iterable[int] = (0, 3, 4)) -> Dict[str, list]:
     """Member packing and CTA cap of a mixed batch (the three grid shapes, 2-24 tracers, the
-    stored tiles): every combination is timed and the best stored when it beats the default
-    (members packed together, no cap) by more than run-to-run noise."""
+    stored tiles): every combination is timed; the best is stored when it beats the default
+    (members packed together, no cap) by more than run-to-run noise, else the default."""
     table = load_table(path)
     shapes = ((18, 18, 16), (36, 36, 16), (36, 36, 32))
     mems = []
@@ -152,9 +155,8 @@ def tune_batch(members: int = 96, steps: int = 30, path: str = TABLE_PATH, verbo
                 print(f"packing {pk} ctas_per_sm {cap}: {rates[(pk, cap)]:.3e} cell-updates/s", flush=True)
     best = max(rates, key=rates.get)
     if best == (0, 0) or rates[best] < NOISE * rates[(0, 0)]:
-        table.pop(BATCH_KEY, None)
-    else:
-        table[BATCH_KEY] = [best[0], best[1], rates[best]]
+        best = (0, 0)
+    table[BATCH_KEY] = [best[0], best[1], rates[best]]
     with open(path, "w") as f:
         json.dump(table, f, indent=1, sort_keys=True)
     if verbose:
