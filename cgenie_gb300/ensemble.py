@@ -175,7 +175,8 @@ class Ensemble:
                         if pending is not None:
                             collect()
                         pending = (idx, args, pool.submit(call, tile, idx, args))
-                    collect()
+                    if pending is not None:
+                        collect()
                 finally:
                     if pending is not None:
                         try:

@@ -36,3 +36,11 @@ def test_no_undefined_module_names():
     problems = {os.path.relpath(p, ROOT): undefined_globals(p) for p in paths}
     problems = {k: v for k, v in problems.items() if v}
     assert not problems, problems
+
+
+def test_ensemble_add_many_of_nothing_calls_nothing():
+    """Ensemble.add_many([]) returns [] without a library call (no GPU needed)."""
+    from cgenie_gb300.ensemble import Ensemble
+    e = object.__new__(Ensemble)
+    e.members, e.tile, e.table, e._current_tile, e.use_graph = {}, (0, 0), {}, None, False
+    assert e.add_many([]) == []
