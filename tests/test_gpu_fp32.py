@@ -405,3 +405,54 @@ def test_ensemble_packing_and_cta_cap_do_not_change_results(gpu_lib):
     with pytest.raises(GoldsteinError):
         e.set_tuning(ctas_per_sm=-1)
     e.close()
+
+
+def _with_mask(m, k1):
+    """Member m with the interior mask k1 (maxj, maxi) and the periodic halo columns."""
+    import dataclasses
+    full = m.k1.copy()
+    full[1:-1, 1:-1] = k1
+    full[:, 0] = full[:, m.maxi]
+    full[:, m.maxi + 1] = full[:, 1]
+    return dataclasses.replace(m, k1=full)
+
+
+def test_ensemble_degenerate_members(gpu_lib):
+    """Edge cases in one batch: a member without any wet column, a member with one wet column,
+    the smallest grid (2x2x2, T and S), and the largest member shape (64 levels, 32 tracers),
+    next to an ordinary member.  Each equals its FP64 run within the split-precision bars (the
+    land-only member exactly its upload), and the ordinary member equals its run in a batch of
+    its own bit for bit."""
+    from cgenie_gb300.ensemble import Ensemble
+    from cgenie_gb300.goldstein import new_member_run
+    from test_gpu_long import per_tracer_errors
+    base = grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=8, maxl=5, seed=71, tracer_kind="bgc"))
+    land = _with_mask(base, np.full((base.maxj, base.maxi), base.maxk + 1, dtype=np.int32))
+    one = np.full((base.maxj, base.maxi), base.maxk + 1, dtype=np.int32)
+    one[4, 5] = 1
+    single = _with_mask(base, one)
+    tiny = grid.make_member(grid.MemberConfig(maxi=2, maxj=2, maxk=2, maxl=2, seed=72))
+    big = grid.make_member(grid.MemberConfig(maxi=10, maxj=8, maxk=64, maxl=32, seed=58, tracer_kind="bgc", noise=1.0))
+    normal = grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=16, maxl=7, seed=73, tracer_kind="bgc"))
+    mems = [land, single, tiny, big, normal]
+    e = Ensemble(use_graph=True)
+    ids = e.add_many(mems)
+    e.step(12)
+    outs = e.download_many(ids)
+    solo = Ensemble(use_graph=True)
+    sid = solo.add_many([normal])
+    solo.step(12)
+    assert np.array_equal(solo.download_many(sid)[0]["ts"], outs[4]["ts"])
+    solo.close()
+    assert np.array_equal(outs[0]["ts"], land.ts)
+    for m, out, mid in zip(mems[1:], outs[1:], ids[1:]):
+        g = new_member_run(m, precision=abi.GB_GO_FP64)
+        g.tstepo(12)
+        ref = g.download()
+        g.close()
+        if (m.k1[1:-1, 1:-1] <= m.maxk).any():
+            err = per_tracer_errors(m, out["ts"], ref["ts"])
+            assert np.all(err[:2] <= 1e-11) and np.all(err <= 1e-6), (m.maxi, m.maxk, m.maxl, err)
+        assert np.array_equal(out["cost"], ref["cost"])
+        assert e.status(mid) == 0
+    e.close()
