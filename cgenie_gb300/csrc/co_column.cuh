@@ -351,40 +351,23 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
 
 
 // ---------------------------------------------------------------------------
-// Warp-parallel adjustment of one column with maxk <= 32 and ieos = 0.
+// Convective adjustment of the columns with maxk <= 32 and ieos = 0 in two phases.
 //
-// co's working list kk (position -> level, the sentinel 0 below the lowest active
-// position) is held one position per lane (position p = lane + 1), each position
-// carrying the record of its level: thickness dzm, T, S, double-float density and the
-// exact FP64 key once computed.  A round evaluates every pair (p, p-1) at once
-// (ballot), so co's walk down a stable stretch (goldstein.f90:2715-2719), and the scan
-// for the bottom of an unstable stretch (2727-2731), each take one round; a merge
-// (2732-2746) shifts the records below it with one shuffle.  Decisions, merge order and
-// arithmetic are co's; the fill (2748-2765) is computed from the final list.
+// Decisions (k_co_decide): one lane per column runs co (goldstein.f90:2657-2777) on T and S,
+// with the list kk held as a bit mask of the active levels (a merge of positions n..m clears
+// the levels it absorbs), so the walk down a stable stretch (2715-2719), the scan for the
+// bottom of an unstable stretch (2727-2731) and the step back up after a merge are bit
+// operations.  The lanes advance in rounds: each lane walks to its next merge, then every
+// lane that has one mixes T and S (2732-2746) at once, so a round's FP64 instructions serve
+// all the merging columns of the warp (GB300's FP64 pipe costs per warp instruction, not per
+// active lane).  Each merge is logged: the top level, the absorbed levels in co's order with
+// the thicknesses co used, and the summed thickness.
+// Tracers (k_co_mix): one lane per (column, tracer l >= 2) replays its column's log in co's
+// order and arithmetic, then the fill (2748-2765) from the final list.
+// Densities are co's FP64 eos values, compared as integer order keys.  Each merge divides by
+// its summed thickness through co_div with the reciprocal computed once per merge.
 
-struct CoRec {
-    int kk;            // level at this position
-    double dzm, t, s;  // thickness, T and S of that level
-    float rdh, rdl, rm;
-    long long key;     // exact order key of its FP64 density, kNoKey until needed
-};
-
-__device__ __forceinline__ CoRec co_rec_up(const CoRec &r, int d)
-{
-    const unsigned F = 0xffffffffu;
-    CoRec o;
-    o.kk = __shfl_up_sync(F, r.kk, d);
-    o.dzm = __shfl_up_sync(F, r.dzm, d);
-    o.t = __shfl_up_sync(F, r.t, d);
-    o.s = __shfl_up_sync(F, r.s, d);
-    o.rdh = __shfl_up_sync(F, r.rdh, d);
-    o.rdl = __shfl_up_sync(F, r.rdl, d);
-    o.rm = __shfl_up_sync(F, r.rm, d);
-    o.key = __shfl_up_sync(F, r.key, d);
-    return o;
-}
-
-// bits of positions lo..hi (position p = bit p-1)
+// bits of levels lo..hi (level l = bit l-1)
 __device__ __forceinline__ unsigned co_bits(int lo, int hi)
 {
     if (hi < lo) return 0u;
@@ -392,142 +375,41 @@ __device__ __forceinline__ unsigned co_bits(int lo, int hi)
     return up & ~((1u << (lo - 1)) - 1u);
 }
 
-// tv: shared memory, tv[lev * 32 + l]; ts0: T of the column at level 0 (S follows), level
-// stride s0; wc (lanes < L): this lane's tracer at level 0, level stride lstride.  Loads
-// the column, adjusts it, writes back the levels that changed; returns the number of
-// filled levels.
-__device__ inline int co_warp32(double *tv, const EosCoef &ec, int maxk, int L, int k1, const double *dz,
-                                int lane, const double *ts0, size_t s0, double *wc, size_t lstride)
+// Merge log of a column (one slot of kCoLogBytes per list entry): header {int nm, unsigned
+// final mask}; per merge k: dtot[k] (summed thickness), y[k] = RN(1 / dtot[k]), dtop[k] (the
+// top level's thickness before it), x[k] (top level), cnt[k] (levels absorbed); per absorbed
+// level in co's order: its thickness and level.  maxk <= 32: at most 31 merges and 31
+// absorbed levels.
+constexpr int kCoLogBytes = (int)kCoLogSlotBytes;
+constexpr int kCoLogDtot = 16, kCoLogY = 264, kCoLogDtop = 512, kCoLogEdz = 760, kCoLogX = 1008, kCoLogCnt = 1039,
+              kCoLogElev = 1070;
+static_assert(kCoLogElev + 31 <= kCoLogBytes, "merge log layout");
+
+// RN(a / b) given y = RN(1 / b): q0 = a y, then two residual corrections q <- q + (a - b q) y
+// (fma).  The first makes q faithful, the second correctly rounded (Markstein's theorem:
+// P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119; the remainder a - b q of a faithful q is
+// exact).  Five FP64 operations instead of a division; operands outside the range where every
+// intermediate stays normal (and a = 0, whose sign the corrections would lose) divide.
+__device__ __forceinline__ double co_div(double a, double b, double y)
 {
-    const unsigned F = 0xffffffffu;
-    const int p = lane + 1;
-    CoDf ecd[4];
-#pragma unroll
-    for (int n = 0; n < 4; ++n) ecd[n] = co_split(ec.ec[n]);
-    CoRec rec;
-    rec.kk = p;
-    rec.dzm = 0.0;
-    rec.t = 0.0;
-    rec.s = 0.0;
-    rec.rdh = rec.rdl = rec.rm = 0.0f;
-    rec.key = kNoKey;
-    if (p >= k1 && p <= maxk) {
-        const double2 v = *reinterpret_cast<const double2 *>(ts0 + (size_t)p * s0);
-        rec.t = v.x;
-        rec.s = v.y;
-        rec.dzm = dz[p];
-        float mg;
-        const CoDf r = eos_df(ecd, v.x, v.y, mg);
-        rec.rdh = r.hi;
-        rec.rdl = r.lo;
-        rec.rm = mg;
+    const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
+    if (ea < 512 || ea > 1535 || eb < 768 || eb > 1279) return __ddiv_rn(a, b);
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
+    return __fma_rn(__fma_rn(-b, q1, a), y, q1);
+}
+
+// Tracer l of a member's column: its value at level 0 and the level stride (group-planar
+// layout: tracer groups in planes of NI*NJ*(maxk+2) cells of gp values).
+__device__ __forceinline__ double *co_tracer(double *W, int L, size_t plane, size_t cell, size_t NIJ, int l, size_t &lstride)
+{
+    int g0 = 0, gl = 2, gp = 2, pl = 0;
+    for (int g = 0; g < fp32_ngroups(L); ++g) {
+        fp32_plane(L, g, &g0, &gl, &gp, &pl);
+        if (l < g0 + gl) break;
     }
-    int sp = k1 - 1;   // sentinel position
-    // bit p-1 set iff rho(kk[p]) < rho(kk[p-1]) or p-1 is the sentinel, for p in [sp+2, lim];
-    // positions outside that range read as stable
-    auto stable_mask = [&](int lim) -> unsigned {
-        const float bh = __shfl_up_sync(F, rec.rdh, 1), bl = __shfl_up_sync(F, rec.rdl, 1);
-        const float bm = __shfl_up_sync(F, rec.rm, 1);
-        int st = 1;
-        if (p >= sp + 2 && p <= lim) {
-            const float d = __fadd_rn(__fsub_rn(rec.rdh, bh), __fsub_rn(rec.rdl, bl));
-            const float tol = __fmul_rn(0x1p-40f, __fadd_rn(rec.rm, bm));
-            st = d < -tol ? 1 : (d > tol ? 0 : 2);
-        }
-        if (__any_sync(F, st == 2)) {
-            const double bt = __shfl_up_sync(F, rec.t, 1), bs = __shfl_up_sync(F, rec.s, 1);
-            // equal T and S: equal densities, not stable
-            if (st == 2 && __double_as_longlong(rec.t) == __double_as_longlong(bt) &&
-                __double_as_longlong(rec.s) == __double_as_longlong(bs))
-                st = 0;
-            const int above = __shfl_down_sync(F, st, 1);
-            if ((st == 2 || (lane < 31 && above == 2)) && rec.key == kNoKey)
-                rec.key = order_key(eos_rn(ec, rec.t, rec.s, 0.0));
-            const long long bk = __shfl_up_sync(F, rec.key, 1);
-            if (st == 2) st = rec.key < bk ? 1 : 0;
-        }
-        return __ballot_sync(F, st == 1);
-    };
-    unsigned stab = stable_mask(maxk);
-    // no unstable pair: co changes nothing
-    if ((~stab & co_bits(k1 + 1, maxk)) == 0u) return 0;
-    if (lane < L)
-        for (int lev = k1; lev <= maxk; lev += 8) {
-            double v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (lev + u <= maxk) v[u] = wc[(size_t)(lev + u) * lstride];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
-        }
-    __syncwarp();
-    unsigned modified = 0u;
-    int m = maxk, lastmix = 0;
-    bool fresh = true;   // stab holds the pairs of the current list up to m
-    while (m > sp + 1 || (lastmix != 0 && m != maxk)) {
-        if (!fresh) stab = stable_mask(m);
-        fresh = false;
-        if (lastmix == 0) {
-            // walk down the stable pairs to the highest unstable one
-            const unsigned un = ~stab & co_bits(sp + 2, m);
-            if (un == 0u) break;
-            m = 32 - __clz(un);
-        } else if ((stab >> (m - 1)) & 1u) {
-            m = (m == maxk) ? m - 1 : m + 1;
-            lastmix = 0;
-            continue;
-        }
-        // merge positions n..m: n = the highest stable position below m (sp+1 always is)
-        const int n = 32 - __clz(stab & co_bits(sp + 1, m - 1));
-        const int d = m - n, lm = m - 1;
-        const int km = __shfl_sync(F, rec.kk, lm);
-        const double d0 = __shfl_sync(F, rec.dzm, lm);
-        double dtot = d0, acc = 0.0;
-        if (lane < L) acc = __dmul_rn(tv[km * 32 + lane], d0);
-        for (int ni = 1; ni <= d; ++ni) {
-            const int lv = __shfl_sync(F, rec.kk, lm - ni);
-            const double dzv = __shfl_sync(F, rec.dzm, lm - ni);
-            dtot = __dadd_rn(dtot, dzv);
-            if (lane < L) acc = __dadd_rn(acc, __dmul_rn(tv[lv * 32 + lane], dzv));
-        }
-        if (lane < L) tv[km * 32 + lane] = __ddiv_rn(acc, dtot);
-        __syncwarp();
-        modified |= 1u << (km - 1);
-        if (lane == lm) {
-            rec.dzm = dtot;
-            rec.t = tv[km * 32];
-            rec.s = tv[km * 32 + 1];
-            float mg;
-            const CoDf r = eos_df(ecd, rec.t, rec.s, mg);
-            rec.rdh = r.hi;
-            rec.rdl = r.lo;
-            rec.rm = mg;
-            rec.key = kNoKey;
-        }
-        // positions sp+d .. m-1 take the records d below (sp+d becomes the sentinel)
-        const CoRec sh = co_rec_up(rec, d);
-        if (p >= sp + d && p <= m - 1) rec = sh;
-        sp += d;
-        lastmix = 1;
-    }
-    // fill: every level of [k1, maxk-1] no longer in the list takes the values of the
-    // lowest listed level above it
-    const unsigned act = __reduce_or_sync(F, (p >= sp + 1 && p <= maxk) ? (1u << (rec.kk - 1)) : 0u);
-    const unsigned fillm = ~act & co_bits(k1, maxk - 1);
-    for (unsigned f = fillm; f; f &= f - 1u) {
-        const int lev = __ffs(f);
-        const int src = __ffs(act & ~((1u << lev) - 1u));
-        if (lane < L) tv[lev * 32 + lane] = tv[src * 32 + lane];
-    }
-    modified |= fillm;
-    __syncwarp();
-    if (lane < L)
-        for (unsigned f = modified; f; f &= f - 1u) {
-            const int lev = __ffs(f);
-            wc[(size_t)lev * lstride] = tv[lev * 32 + lane];
-        }
-    return __popc(fillm);
+    lstride = NIJ * (size_t)gp;
+    return W + (size_t)pl * plane + (size_t)(l - g0) + cell * (size_t)gp;
 }
 
 // ---------------------------------------------------------------------------

@@ -230,9 +230,13 @@ struct gb_ens {
     int *stencil_list = nullptr;        // device: descriptor slots of the members with a stencil
     int cap_stencil = 0, n_stencil = 0, stencil_blocks = 1;
     int kmax = 1;                       // largest maxk of the members
+    int lmax = 2;                       // largest L of the members
     int2 *colist = nullptr;             // columns listed for the exact convective adjustment
-    int *cocount = nullptr;             // two counters, by step parity
+    int *cocount = nullptr;             // list and slot counters, two each by step parity
     int cocap = 0;
+    unsigned char *colog = nullptr;     // merge logs of the two-phase adjustment (cocap slots)
+    int2 *comap = nullptr;              // its second-phase slots
+    int mapcap = 0;
     int *work = nullptr;                // device work counters (two, by step parity)
     bool dirty = true;
     gb_ens_tuning tuning{0, 0, 0, 0, GB_ENS_PACK_MEMBERS, 0};
@@ -282,7 +286,8 @@ static size_t member_bytes(const gb_go_dims *d, const gb_go_params *p)
     const size_t nplan = (size_t)fp32_planar_width(d->maxl) * (d->maxi + 2) * (d->maxj + 2) * (d->maxk + 2);
     return 2 * nplan * 8 + 2 * nts * 8 + nrho * 8 + 16 * ncell * 4 + ncol * (d->maxl + 2) * 4 + (size_t)d->maxj * d->maxk * 8 +
            ncol * 12 + (size_t)(d->maxi + 2) * (d->maxj + 2) * 4 + ncol * (31 + (size_t)d->maxk) * 4 + ned * 8 + nst * 4 + (size_t)d->maxl * 4 +
-           (p && p->imld == 1 ? ncol * 28 + ((size_t)d->maxk + 1) * 16 + 1024 : 0) + 4096;
+           (p && p->imld == 1 ? ncol * 28 + ((size_t)d->maxk + 1) * 16 + 1024 : 0) +
+           ncol * (kCoLogSlotBytes + 8 * (size_t)fp32_co_slots(d->maxl)) + 4096;
 }
 
 extern "C" size_t gb_ens_member_bytes(const gb_go_dims *dims, const gb_go_params *params)
@@ -318,8 +323,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
     if (x == cudaSuccess) x = cudaStreamCreateWithFlags(&e->s2, cudaStreamNonBlocking);
     if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
     if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
-    if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 2 * sizeof(int));
-    if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 2 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 4 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 4 * sizeof(int));
     if (x != cudaSuccess) {
         gb_ens_destroy(e);
         return x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;
@@ -348,6 +353,8 @@ extern "C" void gb_ens_destroy(gb_ens *e)
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->join) cudaEventDestroy(e->join);
     cudaFree(e->cocount);
+    cudaFree(e->colog);
+    cudaFree(e->comap);
     cudaFree(e->colist);
     cudaFree(e->stencil_list);
     cudaFree(e->descs);
@@ -947,7 +954,7 @@ static int rebuild(gb_ens *e)
     std::vector<std::pair<double, Member *>> order;
     int max_slots = 1;
     bool any_iso = false, co_general = false;
-    int kmax = 1;
+    int kmax = 1, lmax = 2;
     int slot = 0;
     std::vector<int> slist;   // members with a stencil
     int sblocks = 1;
@@ -971,6 +978,7 @@ static int rebuild(gb_ens *e)
         }
         co_general = co_general || !fp32_co_fast(m->desc.iconv, m->desc.ieos, m->desc.imld, m->d.maxk);
         kmax = std::max(kmax, m->d.maxk);
+        lmax = std::max(lmax, m->d.L);
         ++slot;
     }
     std::stable_sort(order.begin(), order.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
@@ -1036,9 +1044,20 @@ static int rebuild(gb_ens *e)
     e->n_ts = n_ts;
     if (cocap > e->cocap) {
         if (e->colist) cudaFreeAsync(e->colist, s);
+        if (e->colog) cudaFreeAsync(e->colog, s);
         e->colist = nullptr;
+        e->colog = nullptr;
         ETRY(e, cudaMallocAsync(&e->colist, (size_t)cocap * sizeof(int2), s));
+        ETRY(e, cudaMallocAsync(&e->colog, (size_t)cocap * kCoLogSlotBytes, s));
         e->cocap = cocap;
+    }
+    // second-phase slots: at most L - 2 per listed column
+    if ((size_t)e->cocap * fp32_co_slots(lmax) > (size_t)e->mapcap) {
+        if (e->comap) cudaFreeAsync(e->comap, s);
+        e->comap = nullptr;
+        const int mapcap = e->cocap * fp32_co_slots(lmax);
+        ETRY(e, cudaMallocAsync(&e->comap, (size_t)mapcap * sizeof(int2), s));
+        e->mapcap = mapcap;
     }
     e->max_slots = max_slots;
     e->any_iso = any_iso;
@@ -1046,6 +1065,7 @@ static int rebuild(gb_ens *e)
     e->n_stencil = (int)slist.size();
     e->stencil_blocks = sblocks;
     e->kmax = kmax;
+    e->lmax = lmax;
     e->dirty = false;
     if (e->graph) {
         cudaGraphExecDestroy(e->graph);
@@ -1063,10 +1083,14 @@ static Fp32Batch batch_of(gb_ens *e)
     b.n_bgc = e->nitems - e->n_ts;
     b.max_slots = e->max_slots;
     b.kmax = e->kmax;
+    b.lmax = e->lmax;
     b.work = e->work;
     b.colist = e->colist;
     b.cocount = e->cocount;
     b.cocap = e->cocap;
+    b.colog = e->colog;
+    b.comap = e->comap;
+    b.mapcap = e->mapcap;
     b.iso = e->any_iso;
     b.co_general = e->co_general;
     b.stencil_list = e->stencil_list;

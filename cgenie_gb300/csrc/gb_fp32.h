@@ -146,8 +146,11 @@ struct Fp32Data {
     int4 *items = nullptr;      // work items when stepped alone: (0, patch, group)
     int nitems = 0;
     int2 *colist = nullptr;     // columns for the exact convective adjustment (capacity cocap)
-    int *cocount = nullptr;     // their count, two by step parity
+    int *cocount = nullptr;     // their count and the second phase's slot count, two each by step parity
     int cocap = 0;
+    unsigned char *colog = nullptr;   // merge logs (cocap slots)
+    int2 *comap = nullptr;      // second-phase slots (capacity mapcap)
+    int mapcap = 0;
     int n_ts = 0;               // items[0, n_ts): T-S groups
     cudaStream_t s2 = nullptr;  // second stream and events: the two kinds of items side by side
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -296,10 +299,14 @@ struct Fp32Batch {
     const int4 *items = nullptr;
     int n_ts = 0, n_bgc = 0;
     int max_slots = 1, kmax = 1;
+    int lmax = kFp32MaxL;       // the largest L of the members (shared memory of the adjustment)
     int *work = nullptr;
     int2 *colist = nullptr;
-    int *cocount = nullptr;
+    int *cocount = nullptr;     // list counts, then slot counts, by step parity
     int cocap = 0;
+    unsigned char *colog = nullptr;   // merge logs of the two-phase adjustment (cocap slots)
+    int2 *comap = nullptr;      // (list entry, tracer) slots of its second phase
+    int mapcap = 0;
     bool iso = false;
     bool co_general = false;   // some member has iconv = 1, ieos != 0, imld = 1 or maxk > 32
     const int *stencil_list = nullptr;   // descriptor indices of the members with a stencil
@@ -311,6 +318,9 @@ struct Fp32Batch {
 int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStream_t s, cudaStream_t s2,
                 cudaEvent_t fork, cudaEvent_t join);
 int fp32_launches_per_step(const Fp32Batch &b);   // kernels fp32_launch starts
+// scratch of the two-phase adjustment: merge-log bytes per listed column, and slots per column
+constexpr size_t kCoLogSlotBytes = 1152;
+inline int fp32_co_slots(int L) { return L > 2 ? L - 2 : 1; }
 // columns the warp-parallel adjustment takes (the others run co's serial form)
 __host__ __device__ inline bool fp32_co_fast(int iconv, int ieos, int imld, int maxk)
 {

@@ -799,31 +799,316 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
 
 // Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step listed
 // (every column with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  A list
-// entry is (member, word offset of the column's record); warps take entries in turn.
-// GENERAL = false: columns of members with iconv = 0, ieos = 0, maxk <= 32, adjusted by
-// co_warp32 (one list position per lane); GENERAL = true: the others, by co_warp (the column
-// staged in shared memory, one lane per tracer; kmax: the largest maxk of the batch), with
-// coshuffle (iconv = 1) on one lane.
-template <bool GENERAL>
+// entry is (member, word offset of the column's record).  Columns of members with iconv = 0,
+// ieos = 0, imld = 0 and maxk <= 32 take the two phases k_co_decide and k_co_mix; the others
+// take k_co_serial, one entry per warp, by co_warp (the column staged in shared memory, one
+// lane per tracer), with coshuffle (iconv = 1) and the mixed layer on one lane.
+
+// A list entry's column as the adjustment kernels see it.
+struct CoCol {
+    double *W;             // group-planar FP64 state the step wrote
+    const double *dz;      // dz[lev]
+    double *cost;          // the column's cost entry
+    size_t cell, NIJ, plane;
+    int maxk, L, k1;
+};
+
+__device__ __forceinline__ CoCol co_col(const MemberDesc &md, int2 ent, long long step)
+{
+    const int32_t *ticol = md.ptab + ent.y;
+    const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
+    CoCol c;
+    c.W = md.buf[(int)((step + md.parity) & 1) ^ 1];
+    c.dz = md.mk;
+    c.cost = md.cost + ticol[3];
+    c.NIJ = (size_t)md.NI * md.NJ;
+    c.cell = (size_t)i + (size_t)md.NI * j;
+    c.plane = c.NIJ * (size_t)(md.maxk + 2);
+    c.maxk = md.maxk;
+    c.L = md.L;
+    c.k1 = (ticol[2] >> 16) & 0xffff;
+    return c;
+}
+
+constexpr int kCoDecideThreads = 64;
+constexpr int kCoDecideWarpBytes = 33 * 32 * (8 + 8);   // per warp: thickness, double-float density
+
+// Decisions of co for the columns with maxk <= 32, ieos = 0, iconv = 0, imld = 0: one lane
+// per list entry (co_column.cuh).  T and S are adjusted in place and the merges logged in
+// colog; a column with merges and L > 2 reserves L - 2 slots of comap (entry, tracer) for
+// k_co_mix, counted in cocount[2 + (step & 1)].  Shared memory per warp, [level][lane] for
+// levels 0..32: the thickness of the stretch a level heads and its double-float density (on
+// the FP32 pipes: GB300's FP64 pipe takes ~15 SM cycles per warp instruction).  A pair is
+// decided by the pair densities when their difference exceeds 2^-39 M, M the largest
+// magnitude of the column's eos terms (M is convex in (T, S), so no mixed level exceeds
+// it); otherwise equal T and S are equal densities and the rest compare exact FP64 eos
+// values (goldstein.f90:3048-3061).  T and S are read and written in place.
+__global__ void __launch_bounds__(kCoDecideThreads)
+k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
+            const long long *__restrict__ step_ctr, int rel, unsigned char *__restrict__ colog, int2 *__restrict__ comap,
+            int mapcap)
+{
+    extern __shared__ double cosm[];
+    const unsigned F = 0xffffffffu;
+    const long long step = *step_ctr + rel;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarp = blockDim.x >> 5;
+    const int ncol = min(cocount[step & 1], cocap);
+    int *nslot = cocount + 2 + (int)(step & 1);
+    // the lists of the next step start empty (that step's kernels run after this one)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cocount[(step + 1) & 1] = 0;
+        cocount[2 + ((step + 1) & 1)] = 0;
+    }
+    unsigned char *wsm = reinterpret_cast<unsigned char *>(cosm) + (size_t)warp * kCoDecideWarpBytes;
+    double *dzm = reinterpret_cast<double *>(wsm) + lane;
+    float2 *dd = reinterpret_cast<float2 *>(wsm + 33 * 32 * 8) + lane;
+    for (int base = (blockIdx.x * nwarp + warp) * 32; base < ncol; base += gridDim.x * nwarp * 32) {
+        const int e = base + lane;
+        bool valid = false;
+        const MemberDesc *mdp = nullptr;
+        CoCol c{};
+        if (e < ncol) {
+            const int2 ent = colist[e];
+            mdp = mds + ent.x;
+            if (fp32_co_fast(mdp->iconv, mdp->ieos, mdp->imld, mdp->maxk)) {
+                valid = true;
+                c = co_col(*mdp, ent, step);
+            }
+        }
+        // T and S of level l in the state (plane 0: two values per cell)
+        double *TS = valid ? c.W + 2 * c.cell : nullptr;
+        const size_t tstr = 2 * c.NIJ;
+        auto ts_at = [&](int l) -> double2 { return *reinterpret_cast<const double2 *>(TS + (size_t)l * tstr); };
+        auto ts_set = [&](int l, double2 v) { *reinterpret_cast<double2 *>(TS + (size_t)l * tstr) = v; };
+        CoDf ecd[4];
+#pragma unroll
+        for (int n = 0; n < 4; ++n) ecd[n] = co_split(valid ? mdp->ec[n] : 0.0);
+        const int k1 = valid ? c.k1 : 1, maxk = valid ? c.maxk : 1;
+        float mmax = 0.0f;
+        if (valid) {
+            for (int l0 = k1; l0 <= maxk; l0 += 8) {
+                double2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (l0 + u <= maxk) v[u] = *reinterpret_cast<const double2 *>(TS + (size_t)(l0 + u) * tstr);
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (l0 + u <= maxk) {
+                        float mg;
+                        const CoDf r = eos_df(ecd, v[u].x, v[u].y, mg);
+                        dd[(l0 + u) * 32] = make_float2(r.hi, r.lo);
+                        dzm[(l0 + u) * 32] = c.dz[l0 + u];
+                        mmax = fmaxf(mmax, mg);
+                    }
+            }
+        }
+        const float tol = __fmul_rn(0x1p-39f, mmax);   // >= 2^-40 (M_a + M_b)
+        // rho(a) < rho(b) for active levels a above b: co's stable pair
+        auto stable = [&](int a, int b) -> bool {
+            const float2 da = dd[a * 32], db = dd[b * 32];
+            const float d = __fadd_rn(__fsub_rn(da.x, db.x), __fsub_rn(da.y, db.y));
+            if (d < -tol) return true;
+            if (d > tol) return false;
+            const double2 va = ts_at(a), vb = ts_at(b);
+            // equal T and S: equal densities, not stable
+            if (__double_as_longlong(va.x) == __double_as_longlong(vb.x) && __double_as_longlong(va.y) == __double_as_longlong(vb.y))
+                return false;
+            EosCoef ec;
+            for (int n = 0; n < 4; ++n) ec.ec[n] = mdp->ec[n];
+            ec.ec[4] = 0.0;
+            ec.ieos = 0;
+            return order_key(eos_rn(ec, va.x, va.y, 0.0)) < order_key(eos_rn(ec, vb.x, vb.y, 0.0));
+        };
+        unsigned mask = valid ? co_bits(k1, maxk) : 0u;   // active levels (co's list)
+        auto below = [&](int x) -> int {
+            const unsigned m = mask & ((1u << (x - 1)) - 1u);
+            return m ? 32 - __clz(m) : 0;
+        };
+        auto above = [&](int x) -> int { return __ffs(mask & ~((1u << x) - 1u)); };
+        unsigned char *log = valid ? colog + (size_t)e * kCoLogBytes : nullptr;
+        double *ldt = reinterpret_cast<double *>(log + kCoLogDtot), *ly = reinterpret_cast<double *>(log + kCoLogY);
+        double *ldp = reinterpret_cast<double *>(log + kCoLogDtop), *ledz = reinterpret_cast<double *>(log + kCoLogEdz);
+        int x = maxk, lastmix = 0, nm = 0, ne = 0, guard = 0;
+        bool done = !valid;
+        for (;;) {
+            // walk to this column's next merge (levels nl..x), or to the end of co's loop
+            bool ready = false;
+            int nl = 0;
+            while (!done && !ready) {
+                if (++guard > 2048) {   // co ends within maxk^2 steps; a longer walk is a fault
+                    atomicOr(mdp->status, 4u);
+                    done = true;
+                    break;
+                }
+                const int b = below(x);
+                if (!(b > 0 || (lastmix != 0 && x != maxk))) {
+                    done = true;
+                    break;
+                }
+                if (b <= 0 || stable(x, b)) {
+                    x = (lastmix == 0 || x == maxk) ? b : above(x);
+                    lastmix = 0;
+                    continue;
+                }
+                nl = b;
+                for (;;) {
+                    const int bb = below(nl);
+                    if (bb <= 0 || stable(nl, bb)) break;
+                    nl = bb;
+                }
+                ready = true;
+            }
+            if (!__any_sync(F, ready)) break;
+            if (ready) {
+                // mix T and S of level x, then of the active levels below it down to nl
+                const unsigned sm = mask & co_bits(nl, x - 1);
+                const double dtop = dzm[x * 32];
+                const double2 vx = ts_at(x);
+                double at = __dmul_rn(vx.x, dtop), as = __dmul_rn(vx.y, dtop), dtot = dtop;
+                int cnt = 0;
+                for (unsigned f = sm; f;) {
+                    const int l = 32 - __clz(f);
+                    f &= ~(1u << (l - 1));
+                    const double dzl = dzm[l * 32];
+                    const double2 vl = ts_at(l);
+                    dtot = __dadd_rn(dtot, dzl);
+                    at = __dadd_rn(at, __dmul_rn(vl.x, dzl));
+                    as = __dadd_rn(as, __dmul_rn(vl.y, dzl));
+                    ledz[ne] = dzl;
+                    log[kCoLogElev + ne] = (unsigned char)l;
+                    ++ne;
+                    ++cnt;
+                }
+                const double y = __drcp_rn(dtot);
+                const double nt = co_div(at, dtot, y), ns = co_div(as, dtot, y);
+                ts_set(x, make_double2(nt, ns));
+                dzm[x * 32] = dtot;
+                float mg;
+                const CoDf r = eos_df(ecd, nt, ns, mg);
+                dd[x * 32] = make_float2(r.hi, r.lo);
+                mask &= ~sm;
+                ldt[nm] = dtot;
+                ly[nm] = y;
+                ldp[nm] = dtop;
+                log[kCoLogX + nm] = (unsigned char)x;
+                log[kCoLogCnt + nm] = (unsigned char)cnt;
+                ++nm;
+                lastmix = 1;
+            }
+        }
+        int need = 0;
+        if (valid) {
+            // fill: every level of [k1, maxk-1] no longer active takes T and S of the lowest
+            // active level above it
+            const unsigned fillm = ~mask & co_bits(k1, maxk - 1);
+            for (unsigned f = fillm; f; f &= f - 1u) {
+                const int lev = __ffs(f);
+                ts_set(lev, ts_at(__ffs(mask & ~((1u << lev) - 1u))));
+            }
+            const int filled = __popc(fillm);
+            if (filled > 0) *c.cost = add_count_rn(*c.cost, filled);
+            *reinterpret_cast<int *>(log) = nm;
+            *reinterpret_cast<unsigned *>(log + 4) = mask;
+            if (nm > 0) need = c.L - 2;
+        }
+        // slots of the other tracers: one reservation per warp
+        int incl = need;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(F, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int tot = __shfl_sync(F, incl, 31);
+        int wb = 0;
+        if (lane == 31 && tot > 0) wb = atomicAdd(nslot, tot);
+        wb = __shfl_sync(F, wb, 31);
+        for (int l = 0; l < need; ++l) {
+            const int at = wb + incl - need + l;
+            if (at < mapcap) comap[at] = make_int2(e, l + 2);
+            else atomicOr(mdp->status, 4u);
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int kCoMixThreads = 256;
+
+// The other tracers of the columns k_co_decide adjusted: one thread per (list entry, tracer)
+// slot replays the entry's merge log in place, in co's order and arithmetic
+// (goldstein.f90:2732-2746), then the fill (2748-2765).
+__global__ void __launch_bounds__(kCoMixThreads)
+k_co_mix(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, const int *__restrict__ cocount,
+         const long long *__restrict__ step_ctr, int rel, const unsigned char *__restrict__ colog,
+         const int2 *__restrict__ comap, int mapcap)
+{
+    const long long step = *step_ctr + rel;
+    const int n = min(cocount[2 + (int)(step & 1)], mapcap);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int2 sl = comap[t];
+        const int2 ent = colist[sl.x];
+        const CoCol c = co_col(mds[ent.x], ent, step);
+        size_t ls;
+        double *w = co_tracer(c.W, c.L, c.plane, c.cell, c.NIJ, sl.y, ls);
+        const unsigned char *log = colog + (size_t)sl.x * kCoLogBytes;
+        const int nm = *reinterpret_cast<const int *>(log);
+        const unsigned mask = *reinterpret_cast<const unsigned *>(log + 4);
+        const double *ldt = reinterpret_cast<const double *>(log + kCoLogDtot);
+        const double *ly = reinterpret_cast<const double *>(log + kCoLogY);
+        const double *ldp = reinterpret_cast<const double *>(log + kCoLogDtop);
+        const double *ledz = reinterpret_cast<const double *>(log + kCoLogEdz);
+        // the next merge's and the next absorbed level's log entries are read one ahead (every
+        // index stays inside the slot), so their loads overlap the FP64 chain
+        int ei = 0, lv = log[kCoLogElev];
+        double dzv = ledz[0];
+        int x = log[kCoLogX], cnt = log[kCoLogCnt];
+        double dtop = ldp[0], dtot = ldt[0], y = ly[0];
+        for (int k = 0; k < nm; ++k) {
+            const int xn = log[kCoLogX + k + 1], cntn = log[kCoLogCnt + k + 1];
+            const double dtopn = ldp[k + 1], dtotn = ldt[k + 1], yn = ly[k + 1];
+            double acc = __dmul_rn(w[(size_t)x * ls], dtop);
+            for (int q = 0; q < cnt; ++q) {
+                const int l = lv;
+                const double dz = dzv;
+                ++ei;
+                lv = log[kCoLogElev + ei];
+                dzv = ledz[ei];
+                acc = __dadd_rn(acc, __dmul_rn(w[(size_t)l * ls], dz));
+            }
+            w[(size_t)x * ls] = co_div(acc, dtot, y);
+            x = xn;
+            cnt = cntn;
+            dtop = dtopn;
+            dtot = dtotn;
+            y = yn;
+        }
+        const unsigned fillm = ~mask & co_bits(c.k1, c.maxk - 1);
+        for (unsigned f = fillm; f; f &= f - 1u) {
+            const int lev = __ffs(f);
+            w[(size_t)lev * ls] = w[(size_t)__ffs(mask & ~((1u << lev) - 1u)) * ls];
+        }
+    }
+}
+
+// The serial form for the other listed columns.  kmax: the largest maxk of the batch (shared
+// memory layout).
 __global__ void __launch_bounds__(kFp32Threads)
-k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
-          const long long *__restrict__ step_ctr, int rel, int kmax)
+k_co_serial(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
+            const long long *__restrict__ step_ctr, int rel, int kmax)
 {
     extern __shared__ double cosm[];
     const long long step = *step_ctr + rel;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    double *tv = cosm + (size_t)warp * (kmax + 1) * 32;
-    CoWarpState *cs = GENERAL ? reinterpret_cast<CoWarpState *>(cosm + (size_t)nwarp * (kmax + 1) * 32) + warp : nullptr;
     const int ncol = min(cocount[step & 1], cocap);
-    // the list of the next step starts empty (that step's kernel runs after this one)
-    if (blockIdx.x == 0 && threadIdx.x == 0) cocount[(step + 1) & 1] = 0;
+    double *tv = cosm + (size_t)warp * (kmax + 1) * 32;
+    CoWarpState *cs = reinterpret_cast<CoWarpState *>(cosm + (size_t)nwarp * (kmax + 1) * 32) + warp;
     for (int e = blockIdx.x * nwarp + warp; e < ncol; e += gridDim.x * nwarp) {
         const int2 ent = colist[e];
         const MemberDesc &md = mds[ent.x];
         const int32_t *ticol = md.ptab + ent.y;
         const int maxk = md.maxk, L = md.L, NI = md.NI, NJ = md.NJ, mkn = maxk + 2;
-        // this instance takes either the warp-parallel columns or the others
-        if (fp32_co_fast(md.iconv, md.ieos, md.imld, maxk) == GENERAL) continue;
+        // the two-phase form takes the others
+        if (fp32_co_fast(md.iconv, md.ieos, md.imld, maxk)) continue;
         const int k1c = (ticol[2] >> 16) & 0xffff, cl0 = ticol[3];
         const int i = ticol[4] & 0xffff, j = (ticol[4] >> 16) & 0xffff;
         const int par = (int)((step + md.parity) & 1);
@@ -833,7 +1118,7 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         EosCoef ec;
         for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
         ec.ieos = md.ieos;
-        if (GENERAL && (md.iconv == 1 || md.imld != 0)) {
+        if (md.iconv == 1 || md.imld != 0) {
             // coshuffle (iconv = 1), co and the mixed layer (imld = 1) on one lane, in the
             // order of tstepo (goldstein.f90:2311-2389)
             if (lane == 0) {
@@ -907,14 +1192,6 @@ k_co_fp32(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, i
         const size_t NIJ = (size_t)NI * NJ;
         const double *wc = W + wofs + ((size_t)i + (size_t)NI * j) * gpw;
         const size_t lstride = NIJ * gpw;
-        if (!GENERAL) {
-            // T and S are plane 0, two values per cell
-            const int filled = co_warp32(tv, ec, maxk, L, k1c, dz, lane, W + 2 * ((size_t)i + (size_t)NI * j), 2 * NIJ,
-                                         const_cast<double *>(wc), lstride);
-            if (lane == 0 && filled > 0) md.cost[cl0] = add_count_rn(md.cost[cl0], filled);
-            __syncwarp();
-            continue;
-        }
         if (lane < L)
             for (int lev = k1c; lev <= maxk; lev += 8) {
                 double v[8];
@@ -988,23 +1265,35 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         cudaEventRecord(join, s2);
         cudaStreamWaitEvent(s, join, 0);
     }
-    // the adjustment: warp-parallel columns, then (if the batch has any) the serial ones
-    for (int general = 0; general <= (b.co_general ? 1 : 0); ++general) {
-        auto kern = general ? k_co_fp32<true> : k_co_fp32<false>;
-        const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) +
-                                                   (general ? (int)sizeof(CoWarpState) : 0));
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
+    // the adjustment: decisions of the two-phase columns (with T and S), their other tracers,
+    // then (if the batch has any) the serial columns
+    {
+        const int smem = (kCoDecideThreads / 32) * kCoDecideWarpBytes;
+        cudaFuncSetAttribute(k_co_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        // one block per 64 list entries of the capacity: blocks past the step's count exit, and
+        // the others are scheduled as SMs free up (a deep column's warp delays only itself)
+        const int grid = std::max(1, (b.cocap + kCoDecideThreads - 1) / kCoDecideThreads);
+        k_co_decide<<<grid, kCoDecideThreads, smem, s>>>(b.descs, b.colist, b.cocount, b.cocap, step_ctr,
+                                                                            rel, b.colog, b.comap, b.mapcap);
+        int mper_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mper_sm, k_co_mix, kCoMixThreads, 0);
+        k_co_mix<<<nsm * std::max(1, mper_sm), kCoMixThreads, 0, s>>>(b.descs, b.colist, b.cocount, step_ctr, rel, b.colog,
+                                                                     b.comap, b.mapcap);
+    }
+    if (b.co_general) {
+        const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
+        cudaFuncSetAttribute(k_co_serial, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
         int co_per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, kern, kFp32Threads, co_smem);
-        kern<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
-                                                                         step_ctr, rel, b.kmax);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, k_co_serial, kFp32Threads, co_smem);
+        k_co_serial<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
+                                                                               step_ctr, rel, b.kmax);
     }
     return launch_status();
 }
 
 int fp32_launches_per_step(const Fp32Batch &b)
 {
-    return (b.n_stencil > 0) + (b.n_ts > 0) + (b.n_bgc > 0) + 1 + (b.co_general ? 1 : 0);
+    return (b.n_stencil > 0) + (b.n_ts > 0) + (b.n_bgc > 0) + 2 + (b.co_general ? 1 : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1858,8 +2147,11 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&D.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&D.ptab, std::max<size_t>(1, plan.words.size()) * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc(&D.colist, std::max(1, D.cocap) * sizeof(int2));
-    if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 4 * sizeof(int));
+    D.mapcap = std::max(1, D.cocap) * fp32_co_slots(d.L);
+    if (e == cudaSuccess) e = cudaMalloc(&D.colog, std::max(1, D.cocap) * kCoLogSlotBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&D.comap, (size_t)D.mapcap * sizeof(int2));
     if (e == cudaSuccess) e = cudaMalloc(&D.items, std::max(1, D.nitems) * sizeof(int4));
     if ((p.diso || p.iediff) && e == cudaSuccess) {
         e = cudaMalloc(&D.stencil, (size_t)kStencilWords * ncell * sizeof(float));
@@ -1899,7 +2191,7 @@ void fp32_member_free(Fp32Member *f)
     Fp32Data &D = h->data;
     cudaFree(D.coef); cudaFree(D.coefl); cudaFree(D.plan_buf[0]); cudaFree(D.plan_buf[1]); cudaFree(D.rvol); cudaFree(D.gtop); cudaFree(D.scale); cudaFree(D.tref); cudaFree(D.gmax); cudaFree(D.mk); cudaFree(D.mj);
     cudaFree(D.status); cudaFree(D.dev); cudaFree(D.items); cudaFree(D.step_ctr); cudaFree(D.ptab); cudaFree(D.work);
-    cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.stencil); cudaFree(D.stencil_list); cudaFree(D.rhos);
+    cudaFree(D.colist); cudaFree(D.cocount); cudaFree(D.colog); cudaFree(D.comap); cudaFree(D.stencil); cudaFree(D.stencil_list); cudaFree(D.rhos);
     if (D.s2) cudaStreamDestroy(D.s2);
     if (D.fork) cudaEventDestroy(D.fork);
     if (D.join) cudaEventDestroy(D.join);
@@ -2075,10 +2367,14 @@ int fp32_member_step(Fp32Member *f, double *ts_buf[2], int *cur, double *rho, co
         bt.n_bgc = D.nitems - D.n_ts;
         bt.max_slots = D.max_slots;
         bt.kmax = h->d.maxk;
+        bt.lmax = h->d.L;
         bt.work = D.work;
         bt.colist = D.colist;
         bt.cocount = D.cocount;
         bt.cocap = D.cocap;
+        bt.colog = D.colog;
+        bt.comap = D.comap;
+        bt.mapcap = D.mapcap;
         bt.iso = D.stencil != nullptr;
         bt.co_general = !fp32_co_fast(h->p.iconv, h->p.ieos, h->p.imld, h->d.maxk);
         if (D.stencil) {

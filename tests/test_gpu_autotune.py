@@ -14,4 +14,5 @@ def test_tune_writes_a_usable_table(gpu_lib, tmp_path):
     stored = json.loads(path.read_text())
     assert stored == table
     for key, v in stored.items():
-        assert key == "18x18x16" and v[2] > 0 and 64 <= v[0] * v[1] <= 128
+        # (0, 0): the planner's own tile was kept (no candidate beat it by more than the noise)
+        assert key == "18x18x16" and v[2] > 0 and ((v[0], v[1]) == (0, 0) or 64 <= v[0] * v[1] <= 128)
