@@ -887,11 +887,17 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
         const int k1 = valid ? c.k1 : 1, maxk = valid ? c.maxk : 1;
         float mmax = 0.0f;
         if (valid) {
+            // levels in blocks of 8, the next block's loads issued before this block's densities
+            double2 v[8], vn[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (k1 + u <= maxk) vn[u] = ts_at(k1 + u);
             for (int l0 = k1; l0 <= maxk; l0 += 8) {
-                double2 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = vn[u];
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
-                    if (l0 + u <= maxk) v[u] = *reinterpret_cast<const double2 *>(TS + (size_t)(l0 + u) * tstr);
+                    if (l0 + 8 + u <= maxk) vn[u] = ts_at(l0 + 8 + u);
 #pragma unroll
                 for (int u = 0; u < 8; ++u)
                     if (l0 + u <= maxk) {
@@ -930,6 +936,8 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
         double *ldt = reinterpret_cast<double *>(log + kCoLogDtot), *ly = reinterpret_cast<double *>(log + kCoLogY);
         double *ldp = reinterpret_cast<double *>(log + kCoLogDtop), *ledz = reinterpret_cast<double *>(log + kCoLogEdz);
         int x = maxk, lastmix = 0, nm = 0, ne = 0, guard = 0;
+        int xlast = 0;               // level of the last merge and its new T and S
+        double2 tslast = make_double2(0.0, 0.0);
         bool done = !valid;
         for (;;) {
             // walk to this column's next merge (levels nl..x), or to the end of co's loop
@@ -964,14 +972,19 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
                 // mix T and S of level x, then of the active levels below it down to nl
                 const unsigned sm = mask & co_bits(nl, x - 1);
                 const double dtop = dzm[x * 32];
-                const double2 vx = ts_at(x);
+                // the last merge's level (the next merge's top, usually) is held in registers; the
+                // absorbed levels' loads go out before the FP64 chain, one ahead
+                const double2 vx = x == xlast ? tslast : ts_at(x);
+                int l = sm ? 32 - __clz(sm) : 0;
+                double2 vn = l ? ts_at(l) : make_double2(0.0, 0.0);
                 double at = __dmul_rn(vx.x, dtop), as = __dmul_rn(vx.y, dtop), dtot = dtop;
                 int cnt = 0;
                 for (unsigned f = sm; f;) {
-                    const int l = 32 - __clz(f);
                     f &= ~(1u << (l - 1));
+                    const double2 vl = vn;
+                    const int ln = f ? 32 - __clz(f) : 0;
+                    if (ln) vn = ts_at(ln);
                     const double dzl = dzm[l * 32];
-                    const double2 vl = ts_at(l);
                     dtot = __dadd_rn(dtot, dzl);
                     at = __dadd_rn(at, __dmul_rn(vl.x, dzl));
                     as = __dadd_rn(as, __dmul_rn(vl.y, dzl));
@@ -979,10 +992,13 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
                     log[kCoLogElev + ne] = (unsigned char)l;
                     ++ne;
                     ++cnt;
+                    l = ln;
                 }
                 const double y = __drcp_rn(dtot);
                 const double nt = co_div(at, dtot, y), ns = co_div(as, dtot, y);
                 ts_set(x, make_double2(nt, ns));
+                xlast = x;
+                tslast = make_double2(nt, ns);
                 dzm[x * 32] = dtot;
                 float mg;
                 const CoDf r = eos_df(ecd, nt, ns, mg);
@@ -1002,9 +1018,13 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
             // fill: every level of [k1, maxk-1] no longer active takes T and S of the lowest
             // active level above it
             const unsigned fillm = ~mask & co_bits(k1, maxk - 1);
-            for (unsigned f = fillm; f; f &= f - 1u) {
-                const int lev = __ffs(f);
-                ts_set(lev, ts_at(__ffs(mask & ~((1u << lev) - 1u))));
+            for (unsigned f = fillm; f;) {
+                // the filled levels below one active level take its values: one load per group
+                const int src = __ffs(mask & ~((1u << __ffs(f)) - 1u));
+                const double2 v = src == xlast ? tslast : ts_at(src);
+                const unsigned grp = f & ((1u << (src - 1)) - 1u);
+                for (unsigned g = grp; g; g &= g - 1u) ts_set(__ffs(g), v);
+                f &= ~grp;
             }
             const int filled = __popc(fillm);
             if (filled > 0) *c.cost = add_count_rn(*c.cost, filled);
