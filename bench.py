@@ -1088,7 +1088,7 @@ def run_c3(args, rank, world, local, dist):
                             f"second of two identical jobs (the first absorbs first-use costs)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_fp32 + k_rescale",
+                         "kernel": "batched step: k_step_fp32 (T-S and tracer-group instances) + k_co_decide + k_co_mix + k_rescale",
                          "algorithmic_bytes_per_launch": alg,
                          "note": "achieved = algorithmic bytes of a step (16 L + 24 per wet cell, k1) / step time",
                          "l2": None if l2_bytes is None else {
