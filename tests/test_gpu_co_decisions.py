@@ -74,11 +74,8 @@ def crafted_member(seed, ieos=0, maxk=12, maxl=4):
     return m
 
 
-@pytest.mark.parametrize("precision", [abi.GB_GO_FP32FLUX, abi.GB_GO_FP64], ids=["fp32flux", "fp64"])
-@pytest.mark.parametrize("seed,ieos", [(81, 0), (82, 0), (83, 1)], ids=["a", "b", "ieos1"])
-def test_co_decisions_bit_exact(gpu_lib, oracle, precision, seed, ieos):
+def run_and_compare(oracle, m, precision):
     from cgenie_gb300.goldstein import new_member_run
-    m = crafted_member(seed, ieos)
     ref = oracle.OracleState(m)
     ref.step(1)
     g = new_member_run(m, precision=precision)
@@ -96,3 +93,19 @@ def test_co_decisions_bit_exact(gpu_lib, oracle, precision, seed, ieos):
     assert np.array_equal(out["cost"].view(np.int64), ref.cost.view(np.int64))
     # the crafted columns do convect
     assert np.sum(ref.cost != m.cost) > 20
+
+
+@pytest.mark.parametrize("precision", [abi.GB_GO_FP32FLUX, abi.GB_GO_FP64], ids=["fp32flux", "fp64"])
+@pytest.mark.parametrize("seed,ieos", [(81, 0), (82, 0), (83, 1)], ids=["a", "b", "ieos1"])
+def test_co_decisions_bit_exact(gpu_lib, oracle, precision, seed, ieos):
+    run_and_compare(oracle, crafted_member(seed, ieos), precision)
+
+
+# The split-precision form's two-phase adjustment at its limits: 32 levels (the longest
+# merge logs: a column of exact ties merges 31 levels at once, a random one makes many
+# merges), 24 and 32 tracers (30 replay slots per column over four tracer groups), and
+# 3 tracers (one slot).
+@pytest.mark.parametrize("precision", [abi.GB_GO_FP32FLUX, abi.GB_GO_FP64], ids=["fp32flux", "fp64"])
+@pytest.mark.parametrize("seed,maxk,maxl", [(84, 32, 24), (85, 32, 32), (86, 16, 3)], ids=["k32l24", "k32l32", "k16l3"])
+def test_co_decisions_deep_columns_bit_exact(gpu_lib, oracle, precision, seed, maxk, maxl):
+    run_and_compare(oracle, crafted_member(seed, 0, maxk=maxk, maxl=maxl), precision)
