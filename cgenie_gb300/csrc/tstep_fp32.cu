@@ -830,15 +830,17 @@ __device__ __forceinline__ CoCol co_col(const MemberDesc &md, int2 ent, long lon
     return c;
 }
 
-constexpr int kCoDecideThreads = 64;
-constexpr int kCoDecideWarpBytes = 33 * 32 * (8 + 8);   // per warp: thickness, double-float density
+constexpr int kCoDecideThreads = 32;
+constexpr int kCoDecideWarpBytes = 33 * 32 * (8 + 1);   // per warp: double-float density, merge index
 
 // Decisions of co for the columns with maxk <= 32, ieos = 0, iconv = 0, imld = 0: one lane
 // per list entry (co_column.cuh).  T and S are adjusted in place and the merges logged in
 // colog; a column with merges and L > 2 reserves L - 2 slots of comap (entry, tracer) for
 // k_co_mix, counted in cocount[2 + (step & 1)].  Shared memory per warp, [level][lane] for
-// levels 0..32: the thickness of the stretch a level heads and its double-float density (on
-// the FP32 pipes: GB300's FP64 pipe takes ~15 SM cycles per warp instruction).  A pair is
+// levels 0..32: a level's double-float density (on the FP32 pipes: GB300's FP64 pipe takes
+// ~15 SM cycles per warp instruction) and the index of the last merge it headed, whose logged
+// sum is its thickness (dz otherwise); 9.5 KB per warp, so a step's batches are resident at
+// once.  A pair is
 // decided by the pair densities when their difference exceeds 2^-39 M, M the largest
 // magnitude of the column's eos terms (M is convex in (T, S), so no mixed level exceeds
 // it); otherwise equal T and S are equal densities and the rest compare exact FP64 eos
@@ -861,8 +863,8 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
         cocount[2 + ((step + 1) & 1)] = 0;
     }
     unsigned char *wsm = reinterpret_cast<unsigned char *>(cosm) + (size_t)warp * kCoDecideWarpBytes;
-    double *dzm = reinterpret_cast<double *>(wsm) + lane;
-    float2 *dd = reinterpret_cast<float2 *>(wsm + 33 * 32 * 8) + lane;
+    float2 *dd = reinterpret_cast<float2 *>(wsm) + lane;
+    unsigned char *tix = wsm + 33 * 32 * 8 + lane;   // the last merge a level headed, 0xff: none
     for (int base = (blockIdx.x * nwarp + warp) * 32; base < ncol; base += gridDim.x * nwarp * 32) {
         const int e = base + lane;
         bool valid = false;
@@ -904,7 +906,7 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
                         float mg;
                         const CoDf r = eos_df(ecd, v[u].x, v[u].y, mg);
                         dd[(l0 + u) * 32] = make_float2(r.hi, r.lo);
-                        dzm[(l0 + u) * 32] = c.dz[l0 + u];
+                        tix[(l0 + u) * 32] = 0xff;
                         mmax = fmaxf(mmax, mg);
                     }
             }
@@ -936,8 +938,16 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
         double *ldt = reinterpret_cast<double *>(log + kCoLogDtot), *ly = reinterpret_cast<double *>(log + kCoLogY);
         double *ldp = reinterpret_cast<double *>(log + kCoLogDtop), *ledz = reinterpret_cast<double *>(log + kCoLogEdz);
         int x = maxk, lastmix = 0, nm = 0, ne = 0, guard = 0;
-        int xlast = 0;               // level of the last merge and its new T and S
+        int xlast = 0;               // level of the last merge, its new T and S and thickness
         double2 tslast = make_double2(0.0, 0.0);
+        double dtlast = 0.0;
+        // thickness of the stretch level l heads: dz, or the summed thickness of the last merge
+        // it headed (the log's, or registers for the latest merge)
+        auto dzm_of = [&](int l) -> double {
+            if (l == xlast) return dtlast;
+            const int k = tix[l * 32];
+            return k == 0xff ? c.dz[l] : ldt[k];
+        };
         bool done = !valid;
         for (;;) {
             // walk to this column's next merge (levels nl..x), or to the end of co's loop
@@ -971,7 +981,7 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
             if (ready) {
                 // mix T and S of level x, then of the active levels below it down to nl
                 const unsigned sm = mask & co_bits(nl, x - 1);
-                const double dtop = dzm[x * 32];
+                const double dtop = dzm_of(x);
                 // the last merge's level (the next merge's top, usually) is held in registers; the
                 // absorbed levels' loads go out before the FP64 chain, one ahead
                 const double2 vx = x == xlast ? tslast : ts_at(x);
@@ -984,7 +994,7 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
                     const double2 vl = vn;
                     const int ln = f ? 32 - __clz(f) : 0;
                     if (ln) vn = ts_at(ln);
-                    const double dzl = dzm[l * 32];
+                    const double dzl = dzm_of(l);
                     dtot = __dadd_rn(dtot, dzl);
                     at = __dadd_rn(at, __dmul_rn(vl.x, dzl));
                     as = __dadd_rn(as, __dmul_rn(vl.y, dzl));
@@ -999,7 +1009,8 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
                 ts_set(x, make_double2(nt, ns));
                 xlast = x;
                 tslast = make_double2(nt, ns);
-                dzm[x * 32] = dtot;
+                dtlast = dtot;
+                tix[x * 32] = (unsigned char)nm;
                 float mg;
                 const CoDf r = eos_df(ecd, nt, ns, mg);
                 dd[x * 32] = make_float2(r.hi, r.lo);
@@ -1290,8 +1301,8 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
     {
         const int smem = (kCoDecideThreads / 32) * kCoDecideWarpBytes;
         cudaFuncSetAttribute(k_co_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        // one block per 64 list entries of the capacity: blocks past the step's count exit, and
-        // the others are scheduled as SMs free up (a deep column's warp delays only itself)
+        // one one-warp block per 32 list entries of the capacity: blocks past the step's count
+        // exit, and the others are scheduled as SMs free up (a deep column's warp delays only itself)
         const int grid = std::max(1, (b.cocap + kCoDecideThreads - 1) / kCoDecideThreads);
         k_co_decide<<<grid, kCoDecideThreads, smem, s>>>(b.descs, b.colist, b.cocount, b.cocap, step_ctr,
                                                                             rel, b.colog, b.comap, b.mapcap);

@@ -456,3 +456,35 @@ def test_ensemble_degenerate_members(gpu_lib):
         assert np.array_equal(out["cost"], ref["cost"])
         assert e.status(mid) == 0
     e.close()
+
+
+def test_ensemble_adjustment_scratch_grows(gpu_lib):
+    """The two-phase adjustment's merge logs and tracer slots are sized by the batch (listable
+    columns x (largest L - 2)); members with more tracers admitted later grow them.  Every
+    member equals its run alone, bit for bit, before and after the growth."""
+    from cgenie_gb300.ensemble import Ensemble
+    small = [grid.make_member(grid.MemberConfig(maxi=18, maxj=18, maxk=16, maxl=2, seed=s, noise=2.0)) for s in (701, 702)]
+    big = [grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=32, maxl=l, seed=s, noise=2.0, tracer_kind="bgc"))
+           for s, l in ((703, 24), (704, 32))]
+
+    def alone(m, steps):
+        e = Ensemble(use_graph=True)
+        i = e.add_many([m])
+        e.step(steps)
+        out = e.download_many(i)[0]["ts"]
+        e.close()
+        return out
+
+    e = Ensemble(use_graph=True)
+    ids = e.add_many(small)
+    e.step(6)
+    for i, m in zip(ids, small):
+        assert np.array_equal(e.download_many([i])[0]["ts"], alone(m, 6))
+    bid = e.add_many(big)
+    e.step(6)
+    for i, m in zip(ids, small):
+        assert np.array_equal(e.download_many([i])[0]["ts"], alone(m, 12))
+    for i, m in zip(bid, big):
+        assert np.array_equal(e.download_many([i])[0]["ts"], alone(m, 6))
+    assert all(e.status(i) == 0 for i in ids + bid)
+    e.close()
