@@ -232,7 +232,7 @@ struct gb_ens {
     int kmax = 1;                       // largest maxk of the members
     int lmax = 2;                       // largest L of the members
     int2 *colist = nullptr;             // columns listed for the exact convective adjustment
-    int *cocount = nullptr;             // list and slot counters, two each by step parity
+    int *cocount = nullptr;             // list and (front, back) slot counters, two each by step parity
     int cocap = 0;
     unsigned char *colog = nullptr;     // merge logs of the two-phase adjustment (cocap slots)
     int2 *comap = nullptr;              // its second-phase slots
@@ -323,8 +323,8 @@ extern "C" int gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out)
     if (x == cudaSuccess) x = cudaStreamCreateWithFlags(&e->s2, cudaStreamNonBlocking);
     if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
     if (x == cudaSuccess) x = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
-    if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 4 * sizeof(int));
-    if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 4 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMalloc(&e->cocount, 6 * sizeof(int));
+    if (x == cudaSuccess) x = cudaMemset(e->cocount, 0, 6 * sizeof(int));
     if (x != cudaSuccess) {
         gb_ens_destroy(e);
         return x == cudaErrorMemoryAllocation ? GB_GO_ENOMEM : GB_GO_ECUDA;

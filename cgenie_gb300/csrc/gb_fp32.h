@@ -146,7 +146,7 @@ struct Fp32Data {
     int4 *items = nullptr;      // work items when stepped alone: (0, patch, group)
     int nitems = 0;
     int2 *colist = nullptr;     // columns for the exact convective adjustment (capacity cocap)
-    int *cocount = nullptr;     // their count and the second phase's slot count, two each by step parity
+    int *cocount = nullptr;     // their count and the second phase's two slot counts, two each by step parity
     int cocap = 0;
     unsigned char *colog = nullptr;   // merge logs (cocap slots)
     int2 *comap = nullptr;      // second-phase slots (capacity mapcap)
@@ -302,7 +302,7 @@ struct Fp32Batch {
     int lmax = kFp32MaxL;       // the largest L of the members (shared memory of the adjustment)
     int *work = nullptr;
     int2 *colist = nullptr;
-    int *cocount = nullptr;     // list counts, then slot counts, by step parity
+    int *cocount = nullptr;     // list counts, then front and back slot counts, two each by step parity
     int cocap = 0;
     unsigned char *colog = nullptr;   // merge logs of the two-phase adjustment (cocap slots)
     int2 *comap = nullptr;      // (list entry, tracer) slots of its second phase

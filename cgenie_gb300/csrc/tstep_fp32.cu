@@ -836,7 +836,8 @@ constexpr int kCoDecideWarpBytes = 33 * 32 * (8 + 1);   // per warp: double-floa
 // Decisions of co for the columns with maxk <= 32, ieos = 0, iconv = 0, imld = 0: one lane
 // per list entry (co_column.cuh).  T and S are adjusted in place and the merges logged in
 // colog; a column with merges and L > 2 reserves L - 2 slots of comap (entry, tracer) for
-// k_co_mix, counted in cocount[2 + (step & 1)].  Shared memory per warp, [level][lane] for
+// k_co_mix: from the front (count cocount[2 + (step & 1)]) with at most two merges, else from
+// the back (count cocount[4 + (step & 1)]).  Shared memory per warp, [level][lane] for
 // levels 0..32: a level's double-float density (on the FP32 pipes: GB300's FP64 pipe takes
 // ~15 SM cycles per warp instruction) and the index of the last merge it headed, whose logged
 // sum is its thickness (dz otherwise); 9.5 KB per warp, so a step's batches are resident at
@@ -856,11 +857,14 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarp = blockDim.x >> 5;
     const int ncol = min(cocount[step & 1], cocap);
-    int *nslot = cocount + 2 + (int)(step & 1);
+    // slots of columns with at most two merges from the front of comap, the others from the
+    // back, so that a warp of k_co_mix replays logs of similar length
+    int *nslot = cocount + 2 + (int)(step & 1), *nslotb = cocount + 4 + (int)(step & 1);
     // the lists of the next step start empty (that step's kernels run after this one)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         cocount[(step + 1) & 1] = 0;
         cocount[2 + ((step + 1) & 1)] = 0;
+        cocount[4 + ((step + 1) & 1)] = 0;
     }
     unsigned char *wsm = reinterpret_cast<unsigned char *>(cosm) + (size_t)warp * kCoDecideWarpBytes;
     float2 *dd = reinterpret_cast<float2 *>(wsm) + lane;
@@ -1043,21 +1047,26 @@ k_co_decide(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
             *reinterpret_cast<unsigned *>(log + 4) = mask;
             if (nm > 0) need = c.L - 2;
         }
-        // slots of the other tracers: one reservation per warp
-        int incl = need;
+        // slots of the other tracers: one reservation per warp and class
+        const bool back = nm > 2;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(F, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int tot = __shfl_sync(F, incl, 31);
-        int wb = 0;
-        if (lane == 31 && tot > 0) wb = atomicAdd(nslot, tot);
-        wb = __shfl_sync(F, wb, 31);
-        for (int l = 0; l < need; ++l) {
-            const int at = wb + incl - need + l;
-            if (at < mapcap) comap[at] = make_int2(e, l + 2);
-            else atomicOr(mdp->status, 4u);
+        for (int cls = 0; cls < 2; ++cls) {
+            const int nd = (cls == 1) == back ? need : 0;
+            int incl = nd;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(F, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int tot = __shfl_sync(F, incl, 31);
+            int wb = 0;
+            if (lane == 31 && tot > 0) wb = atomicAdd(cls ? nslotb : nslot, tot);
+            wb = __shfl_sync(F, wb, 31);
+            for (int l = 0; l < nd; ++l) {
+                const int at = wb + incl - nd + l;
+                if (at < mapcap) comap[cls ? mapcap - 1 - at : at] = make_int2(e, l + 2);
+                else atomicOr(mdp->status, 4u);
+            }
         }
         __syncwarp();
     }
@@ -1074,9 +1083,9 @@ k_co_mix(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, co
          const int2 *__restrict__ comap, int mapcap)
 {
     const long long step = *step_ctr + rel;
-    const int n = min(cocount[2 + (int)(step & 1)], mapcap);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int2 sl = comap[t];
+    const int nf = min(cocount[2 + (int)(step & 1)], mapcap), nb = min(cocount[4 + (int)(step & 1)], mapcap - nf);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf + nb; t += gridDim.x * blockDim.x) {
+        const int2 sl = comap[t < nf ? t : mapcap - 1 - (t - nf)];
         const int2 ent = colist[sl.x];
         const CoCol c = co_col(mds[ent.x], ent, step);
         size_t ls;
@@ -2178,8 +2187,8 @@ int fp32_member_init(Fp32Member *f, const Dims &d, const PhysParams &p, const Me
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&D.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&D.ptab, std::max<size_t>(1, plan.words.size()) * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc(&D.colist, std::max(1, D.cocap) * sizeof(int2));
-    if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 4 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&D.cocount, 6 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(D.cocount, 0, 6 * sizeof(int));
     D.mapcap = std::max(1, D.cocap) * fp32_co_slots(d.L);
     if (e == cudaSuccess) e = cudaMalloc(&D.colog, std::max(1, D.cocap) * kCoLogSlotBytes);
     if (e == cudaSuccess) e = cudaMalloc(&D.comap, (size_t)D.mapcap * sizeof(int2));
