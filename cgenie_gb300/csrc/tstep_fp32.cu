@@ -797,8 +797,9 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
     return launch_status();
 }
 
-// Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step listed
-// (every column with iconv = 1 or ieos != 0), on the FP64 state the step wrote.  A list
+// Exact convective adjustment (goldstein.f90:2657-2841) of the columns the step listed (those
+// its FP32 prescreen cannot prove stable, and every column of members with iconv = 1,
+// ieos != 0 or imld = 1), on the FP64 state the step wrote.  A list
 // entry is (member, word offset of the column's record).  Columns of members with iconv = 0,
 // ieos = 0, imld = 0 and maxk <= 32 take the two phases k_co_decide and k_co_mix; the others
 // take k_co_serial, one entry per warp, by co_warp (the column staged in shared memory, one
