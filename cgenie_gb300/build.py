@@ -33,6 +33,7 @@ SOURCES = {
     "momentum.cu": ["-fmad=false"],
     "restart.cu": ["-fmad=false"],
     "timeseries.cu": ["-fmad=false"],
+    "trace.cu": [],
 }
 
 

@@ -448,6 +448,7 @@ extern "C" const char *gb_bg_last_error(const gb_bg *h) { return h ? h->last_err
 extern "C" int gb_bg_upload(gb_bg *h, const double *vocn, const double *mass, const double *volume, const double *rmass,
                             const double *vbio_part)
 {
+    gbgo::TraceRange tr_("bg_upload");
     if (!h || !vocn || !mass || !volume || !rmass || (h->d.n_l_sed > 0 && !vbio_part))
         return bfail(h, GB_GO_EINVAL, "upload: NULL array");
     BG_TRY(h, cudaSetDevice(h->device));
@@ -491,6 +492,7 @@ extern "C" int gb_bg_set_increments(gb_bg *h, const double *vdocn, const double 
 
 extern "C" int gb_bg_tracercoupling(gb_bg *h, gb_go_handle *ocean)
 {
+    gbgo::TraceRange tr_("bg_tracercoupling");
     if (!h || !ocean) return bfail(h, GB_GO_EINVAL, "tracercoupling: NULL handle");
     if (!h->have_state || !h->have_inc) return bfail(h, GB_GO_ENOTREADY, "tracercoupling before upload/set_increments");
     OceanState o{};
@@ -548,6 +550,7 @@ extern "C" int gb_bg_tracercoupling(gb_bg *h, gb_go_handle *ocean)
 
 extern "C" int gb_bg_download(gb_bg *h, double *vocn, double *mass, double *rmass, double *vbio_part)
 {
+    gbgo::TraceRange tr_("bg_download");
     if (!h) return GB_GO_EINVAL;
     if (!h->have_state) return bfail(h, GB_GO_ENOTREADY, "download before upload");
     BG_TRY(h, cudaSetDevice(h->device));

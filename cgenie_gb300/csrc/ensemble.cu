@@ -746,6 +746,7 @@ extern "C" int gb_ens_add(gb_ens *e, const gb_go_dims *dims, const gb_go_params 
 extern "C" int gb_ens_add_many(gb_ens *e, int32_t n, const gb_go_dims *dims, const gb_go_params *params,
                                const gb_go_grid *grids, const double *const *ts, const double *const *u, int32_t *ids)
 {
+    gbgo::TraceRange tr_("ens_add_many");
     if (!e || n < 0 || (n > 0 && (!dims || !params || !grids || !ts || !u || !ids))) return GB_GO_EINVAL;
     if (n == 0) return GB_GO_OK;
     ETRY(e, cudaSetDevice(e->device));
@@ -1121,6 +1122,7 @@ static int launch_steps(gb_ens *e, int nsteps)
 
 extern "C" int gb_ens_step(gb_ens *e, int32_t nsteps)
 {
+    gbgo::TraceRange tr_("ens_step");
     if (!e || nsteps < 0) return GB_GO_EINVAL;
     ETRY(e, cudaSetDevice(e->device));
     if (e->dirty) {
@@ -1295,6 +1297,7 @@ __global__ void k_member_download_many(const DownloadItem *it)
 extern "C" int gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, double *const *ts, double *const *rho,
                                     double *const *cost)
 {
+    gbgo::TraceRange tr_("ens_download_many");
     if (!e || n < 0 || (n > 0 && !ids)) return GB_GO_EINVAL;
     std::vector<Member *> ms;
     for (int32_t q = 0; q < n; ++q) {

@@ -521,6 +521,7 @@ int ocean_state_reloaded(gb_go_handle *h)
 
 extern "C" int gb_go_upload_state(gb_go_handle *h, const double *ts, const double *ts1, const double *rho)
 {
+    gbgo::TraceRange tr_("go_upload_state");
     if (!h || !ts || !ts1 || !rho) return fail(h, GB_GO_EINVAL, "upload_state: NULL array");
     CUDA_TRY(h, cudaSetDevice(h->device));
     const size_t nts = (size_t)h->d.L * h->d.NI * h->d.NJ * (h->d.maxk + 2);
@@ -594,6 +595,7 @@ extern "C" int gb_go_set_diag(gb_go_handle *h, const double *cost, const int32_t
 
 extern "C" int gb_go_tstepo(gb_go_handle *h, int32_t nsteps)
 {
+    gbgo::TraceRange tr_("go_tstepo");
     if (!h || nsteps < 0) return fail(h, GB_GO_EINVAL, "tstepo: bad arguments");
     if (!h->state_ready || !h->vel_ready) return fail(h, GB_GO_ENOTREADY, "tstepo before upload_state/set_velocity");
     CUDA_TRY(h, cudaSetDevice(h->device));
@@ -664,6 +666,7 @@ extern "C" int gb_go_download_mld(gb_go_handle *h, double *mld, int32_t *mldk)
 extern "C" int gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *rho, double *cost, int32_t *icosd,
                               double *dmax, int32_t *limps)
 {
+    gbgo::TraceRange tr_("go_download");
     if (!h) return GB_GO_EINVAL;
     if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "download before upload_state");
     CUDA_TRY(h, cudaSetDevice(h->device));
@@ -709,6 +712,7 @@ extern "C" int gb_go_download(gb_go_handle *h, double *ts, double *ts1, double *
 
 extern "C" int gb_go_inventory(gb_go_handle *h, double *out)
 {
+    gbgo::TraceRange tr_("go_inventory");
     if (!h || !out) return GB_GO_EINVAL;
     if (!h->state_ready) return fail(h, GB_GO_ENOTREADY, "inventory before upload_state");
     CUDA_TRY(h, cudaSetDevice(h->device));

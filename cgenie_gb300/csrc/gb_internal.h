@@ -22,6 +22,19 @@
 
 namespace gbgo {
 
+// An NVTX range of the library's domain ("cgenie_gb300") for the lifetime of the object: the
+// public calls open one named after the call (no-op unless a profiler is attached).
+struct TraceRange {
+    explicit TraceRange(const char *name);
+    ~TraceRange();
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+
+}  // namespace gbgo
+
+namespace gbgo {
+
 constexpr int kMaxK = 64;
 
 // Fortran-indexed metric pointers (device).

@@ -978,6 +978,7 @@ static int launch_step(const MoDev &a, cudaStream_t s, double *ocean_u);
 
 extern "C" int gb_mo_step(gb_mo *h, gb_go_handle *ocean)
 {
+    gbgo::TraceRange tr_("mo_step");
     if (!h || !ocean) return mfail(h, GB_GO_EINVAL, "step: NULL handle");
     if (!h->have_wind) return mfail(h, GB_GO_ENOTREADY, "step before set_wind");
     OceanState o{};

@@ -540,6 +540,7 @@ extern "C" int gb_rs_write_fields(const char *path, int32_t maxi, int32_t maxj, 
                                   const double *temp, const double *salinity, const double *uvel, const double *vvel,
                                   const double *evap, const double *late, const double *sens)
 {
+    gbgo::TraceRange tr_("rs_write_fields");
     if (!path || !cal || !lon || !lat || !depths1 || !temp || !salinity || !uvel || !vvel)
         return rs_fail(GB_GO_EINVAL, "write_fields: NULL argument");
     if (int r = check_dims(maxi, maxj, maxk)) return r;
@@ -594,6 +595,7 @@ extern "C" int gb_rs_write_goldstein(gb_go_handle *ocean, const char *path, cons
                                      const double *nclon1, const double *nclat1, const double *ncdepth,
                                      const double *evap, const double *late, const double *sens)
 {
+    gbgo::TraceRange tr_("rs_write_goldstein");
     if (!ocean || !path || !cal || !nclon1 || !nclat1 || !ncdepth) return rs_fail(GB_GO_EINVAL, "write_goldstein: NULL argument");
     OceanState o;
     if (int r = pack_fields(ocean, nullptr, o)) return r;   // validation and export only
@@ -624,6 +626,7 @@ extern "C" int gb_rs_read_goldstein(const char *path, int32_t maxi, int32_t maxj
                                     gb_rs_calendar *cal, double *temp, double *salinity, double *uvel, double *vvel,
                                     double *evap, double *late, double *sens)
 {
+    gbgo::TraceRange tr_("rs_read_goldstein");
     if (!path) return rs_fail(GB_GO_EINVAL, "read_goldstein: NULL path");
     if (int r = check_dims(maxi, maxj, maxk)) return r;
     NcFile f;

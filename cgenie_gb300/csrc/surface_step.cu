@@ -564,12 +564,14 @@ static int step_grids(gb_ea *const *hs, int n, int nsteps)
 
 extern "C" int gb_ea_step(gb_ea *h, int32_t nsteps)
 {
+    gbgo::TraceRange tr_("ea_step");
     if (!h) return GB_GO_EINVAL;
     return step_grids(&h, 1, nsteps);
 }
 
 extern "C" int gb_ea_step_many(gb_ea *const *handles, int32_t n, int32_t nsteps)
 {
+    gbgo::TraceRange tr_("ea_step_many");
     if (!handles || n < 1 || !handles[0]) return GB_GO_EINVAL;
     return step_grids(handles, n, nsteps);
 }

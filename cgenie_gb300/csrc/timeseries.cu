@@ -331,6 +331,7 @@ extern "C" void gb_ts_destroy(gb_ts_handle *h)
 extern "C" int gb_ts_diagnose(gb_ts_handle *h, gb_go_handle *ocean, double *sums, double *avn, double *avs, double *ext,
                               int32_t *iposa, double *opsi, double *opsip, double *opsia)
 {
+    gbgo::TraceRange tr_("ts_diagnose");
     if (!h || !ocean) return GB_GO_EINVAL;
     OceanState o{};
     if (ocean_state(ocean, &o) != GB_GO_OK) return tsfail(h, GB_GO_EINVAL, "bad ocean handle");

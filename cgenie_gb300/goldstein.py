@@ -45,6 +45,8 @@ EXPORTED = [
     "gb_rs_write_goldstein", "gb_rs_pack_goldstein", "gb_rs_write_fields", "gb_rs_read_goldstein", "gb_rs_goldstein_name",
     "gb_rs_calendar_step", "gb_rs_calendar_after_read", "gb_rs_last_error",
     "gb_ts_create", "gb_ts_destroy", "gb_ts_diagnose", "gb_ts_format", "gb_ts_last_error",
+    "gb_tr_resume", "gb_tr_pause", "gb_tr_domain_create", "gb_tr_string_handle_create", "gb_tr_task_begin",
+    "gb_tr_task_end",
 ]
 
 _lib = None
@@ -105,6 +107,16 @@ def load_library(path: str = LIB_PATH):
                                C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]
     L.gb_ts_last_error.argtypes = [vp]
     L.gb_ts_last_error.restype = C.c_char_p
+    L.gb_tr_resume.argtypes = []
+    L.gb_tr_pause.argtypes = []
+    L.gb_tr_domain_create.argtypes = [C.c_char_p]
+    L.gb_tr_domain_create.restype = vp
+    L.gb_tr_string_handle_create.argtypes = [C.c_char_p]
+    L.gb_tr_string_handle_create.restype = vp
+    L.gb_tr_task_begin.argtypes = [vp, vp]
+    L.gb_tr_task_begin.restype = None
+    L.gb_tr_task_end.argtypes = [vp]
+    L.gb_tr_task_end.restype = None
     L.gb_ens_add.argtypes = [vp, P(GbDims), P(GbParams), P(GbGrid), dp, dp, ip]
     L.gb_ens_add_many.argtypes = [vp, C.c_int32, P(GbDims), P(GbParams), P(GbGrid), P(vp), P(vp), ip]
     L.gb_ens_remove.argtypes = [vp, C.c_int32]

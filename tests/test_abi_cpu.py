@@ -16,7 +16,7 @@ def header_functions():
     for h in sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo|rs|ts)_[a-z0-9_]+)\s*\(", src))
+        names |= set(re.findall(r"\b(gb_(?:go|ens|bg|ea|mo|rs|ts|tr)_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 
@@ -89,3 +89,26 @@ def test_host_memory_calls_refuse_bad_arguments_without_gpu():
     buf = (C.c_char * 64)()
     assert lib.gb_ens_host_free(C.cast(buf, C.c_void_p)) == abi.GB_GO_EINVAL
     assert lib.gb_ens_host_free(None) == abi.GB_GO_EINVAL
+
+
+def test_trace_calls_without_gpu():
+    """The ITT-shaped tracing calls (include/gb_trace.h) work without a GPU or a profiler:
+    domains are one per name, NULL names are refused, tasks nest and close, and the collection
+    window calls report the missing device instead of failing."""
+    from cgenie_gb300 import build, goldstein
+    build.build()
+    L = goldstein.load_library()
+    d = L.gb_tr_domain_create(b"genie")
+    assert d and L.gb_tr_domain_create(b"genie") == d and L.gb_tr_domain_create(b"other") != d
+    assert not L.gb_tr_domain_create(None) and not L.gb_tr_domain_create(b"")
+    assert not L.gb_tr_string_handle_create(None)
+    step, status = L.gb_tr_string_handle_create(b"timestep"), L.gb_tr_string_handle_create(b"status")
+    assert step and status
+    L.gb_tr_task_begin(d, step)
+    L.gb_tr_task_begin(d, status)
+    L.gb_tr_task_end(d)
+    L.gb_tr_task_end(d)
+    L.gb_tr_task_begin(None, None)   # the library's own domain, unnamed
+    L.gb_tr_task_end(None)
+    assert L.gb_tr_resume() in (abi.GB_GO_OK, abi.GB_GO_ECUDA)
+    assert L.gb_tr_pause() in (abi.GB_GO_OK, abi.GB_GO_ECUDA)
