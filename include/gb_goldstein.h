@@ -294,6 +294,11 @@ int  gb_ens_download_many(gb_ens *e, int32_t n, const int32_t *ids, double *cons
 int  gb_ens_set_mld_wind(gb_ens *e, int32_t member_id, const double *mldketau);
 int  gb_ens_download_mld(gb_ens *e, int32_t member_id, double *mld, int32_t *mldk);
 int  gb_ens_inventory(gb_ens *e, int32_t member_id, double *out);
+/* The member's status word: bit 0 (1) a non-finite tracer value; bit 1 (2) a scaled transfer
+ * beyond the fixed-point range; bit 2 (4) the convective adjustment did not complete (a full
+ * column list or slot map, or a decision walk past its bound: none can happen with the sizes
+ * the library allocates, so it marks a fault).  0: healthy.  Bits are sticky; the other members
+ * of the batch are unaffected. */
 int  gb_ens_status(gb_ens *e, int32_t member_id, int32_t *status);
 int  gb_ens_sync(gb_ens *e);
 int  gb_ens_count(gb_ens *e, int32_t *active, size_t *bytes_in_use);
