@@ -1302,12 +1302,9 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel,
                                            b.work + 2, b.colist, b.cocount, b.cocap, nsm, b.ctas_per_sm, sb);
     }
-    if (two) {
-        cudaEventRecord(join, s2);
-        cudaStreamWaitEvent(s, join, 0);
-    }
-    // the adjustment: decisions of the two-phase columns (with T and S), their other tracers,
-    // then (if the batch has any) the serial columns
+    // the adjustment's decisions need only T, S and the column list, which the T-S items
+    // complete: they run while the other tracer groups are still stepping (k_co_decide writes T
+    // and S in place, plane 0 of the new state, which the group items neither read nor write)
     {
         const int smem = (kCoDecideThreads / 32) * kCoDecideWarpBytes;
         cudaFuncSetAttribute(k_co_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -1316,6 +1313,13 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         const int grid = std::max(1, (b.cocap + kCoDecideThreads - 1) / kCoDecideThreads);
         k_co_decide<<<grid, kCoDecideThreads, smem, s>>>(b.descs, b.colist, b.cocount, b.cocap, step_ctr,
                                                                             rel, b.colog, b.comap, b.mapcap);
+    }
+    if (two) {
+        cudaEventRecord(join, s2);
+        cudaStreamWaitEvent(s, join, 0);
+    }
+    // then the other tracers of the two-phase columns, and (if the batch has any) the serial columns
+    {
         int mper_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mper_sm, k_co_mix, kCoMixThreads, 0);
         k_co_mix<<<nsm * std::max(1, mper_sm), kCoMixThreads, 0, s>>>(b.descs, b.colist, b.cocount, step_ctr, rel, b.colog,
