@@ -124,10 +124,12 @@ class GbEaGrid(C.Structure):
 
 class GbEnsTuning(C.Structure):
     _fields_ = [("tile_i", C.c_int32), ("tile_j", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("use_graph", C.c_int32), ("packing", C.c_int32), ("reserved", C.c_int32)]
+                ("use_graph", C.c_int32), ("packing", C.c_int32), ("co_form", C.c_int32)]
 
 
 GB_ENS_PACK_MEMBERS, GB_ENS_PACK_ITEMS, GB_ENS_PACK_ROUND_ROBIN = 0, 1, 2
+GB_ENS_CO_AUTO, GB_ENS_CO_WARP, GB_ENS_CO_TWO_PHASE = 0, 1, 2
+GB_ENS_CO_TWO_PHASE_MIN = 100000
 
 
 def addr(a: np.ndarray) -> int:

@@ -364,8 +364,11 @@ __device__ inline int co_warp(double *tv, CoWarpState *cs, const EosCoef &ec, in
 // the thicknesses co used, and the summed thickness.
 // Tracers (k_co_mix): one lane per (column, tracer l >= 2) replays its column's log in co's
 // order and arithmetic, then the fill (2748-2765) from the final list.
-// Densities are co's FP64 eos values, compared as integer order keys.  Each merge divides by
-// its summed thickness through co_div with the reciprocal computed once per merge.
+// Density decisions as in the one-warp-per-column form below (double-float densities, exact
+// FP64 eos where they are closer than their error bound, equal T and S as equal densities).
+// Each merge divides by its summed thickness through co_div with the reciprocal computed once
+// per merge.  The two-phase form pays a fixed latency per batch of 32 columns, so it serves
+// large batches; the one-warp-per-column form below serves small ones.
 
 // bits of levels lo..hi (level l = bit l-1)
 __device__ __forceinline__ unsigned co_bits(int lo, int hi)
@@ -373,6 +376,179 @@ __device__ __forceinline__ unsigned co_bits(int lo, int hi)
     if (hi < lo) return 0u;
     const unsigned up = hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u);
     return up & ~((1u << (lo - 1)) - 1u);
+}
+
+// ---------------------------------------------------------------------------
+// The one-warp-per-column form (small batches) of the columns with maxk <= 32 and ieos = 0.
+//
+// co's working list kk (position -> level, the sentinel 0 below the lowest active
+// position) is held one position per lane (position p = lane + 1), each position
+// carrying the record of its level: thickness dzm, T, S, double-float density and the
+// exact FP64 key once computed.  A round evaluates every pair (p, p-1) at once
+// (ballot), so co's walk down a stable stretch (goldstein.f90:2715-2719), and the scan
+// for the bottom of an unstable stretch (2727-2731), each take one round; a merge
+// (2732-2746) shifts the records below it with one shuffle.  Decisions, merge order and
+// arithmetic are co's; the fill (2748-2765) is computed from the final list.
+
+struct CoRec {
+    int kk;            // level at this position
+    double dzm, t, s;  // thickness, T and S of that level
+    float rdh, rdl, rm;
+    long long key;     // exact order key of its FP64 density, kNoKey until needed
+};
+
+__device__ __forceinline__ CoRec co_rec_up(const CoRec &r, int d)
+{
+    const unsigned F = 0xffffffffu;
+    CoRec o;
+    o.kk = __shfl_up_sync(F, r.kk, d);
+    o.dzm = __shfl_up_sync(F, r.dzm, d);
+    o.t = __shfl_up_sync(F, r.t, d);
+    o.s = __shfl_up_sync(F, r.s, d);
+    o.rdh = __shfl_up_sync(F, r.rdh, d);
+    o.rdl = __shfl_up_sync(F, r.rdl, d);
+    o.rm = __shfl_up_sync(F, r.rm, d);
+    o.key = __shfl_up_sync(F, r.key, d);
+    return o;
+}
+
+
+// tv: shared memory, tv[lev * 32 + l]; ts0: T of the column at level 0 (S follows), level
+// stride s0; wc (lanes < L): this lane's tracer at level 0, level stride lstride.  Loads
+// the column, adjusts it, writes back the levels that changed; returns the number of
+// filled levels.
+__device__ inline int co_warp32(double *tv, const EosCoef &ec, int maxk, int L, int k1, const double *dz,
+                                int lane, const double *ts0, size_t s0, double *wc, size_t lstride)
+{
+    const unsigned F = 0xffffffffu;
+    const int p = lane + 1;
+    CoDf ecd[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) ecd[n] = co_split(ec.ec[n]);
+    CoRec rec;
+    rec.kk = p;
+    rec.dzm = 0.0;
+    rec.t = 0.0;
+    rec.s = 0.0;
+    rec.rdh = rec.rdl = rec.rm = 0.0f;
+    rec.key = kNoKey;
+    if (p >= k1 && p <= maxk) {
+        const double2 v = *reinterpret_cast<const double2 *>(ts0 + (size_t)p * s0);
+        rec.t = v.x;
+        rec.s = v.y;
+        rec.dzm = dz[p];
+        float mg;
+        const CoDf r = eos_df(ecd, v.x, v.y, mg);
+        rec.rdh = r.hi;
+        rec.rdl = r.lo;
+        rec.rm = mg;
+    }
+    int sp = k1 - 1;   // sentinel position
+    // bit p-1 set iff rho(kk[p]) < rho(kk[p-1]) or p-1 is the sentinel, for p in [sp+2, lim];
+    // positions outside that range read as stable
+    auto stable_mask = [&](int lim) -> unsigned {
+        const float bh = __shfl_up_sync(F, rec.rdh, 1), bl = __shfl_up_sync(F, rec.rdl, 1);
+        const float bm = __shfl_up_sync(F, rec.rm, 1);
+        int st = 1;
+        if (p >= sp + 2 && p <= lim) {
+            const float d = __fadd_rn(__fsub_rn(rec.rdh, bh), __fsub_rn(rec.rdl, bl));
+            const float tol = __fmul_rn(0x1p-40f, __fadd_rn(rec.rm, bm));
+            st = d < -tol ? 1 : (d > tol ? 0 : 2);
+        }
+        if (__any_sync(F, st == 2)) {
+            const double bt = __shfl_up_sync(F, rec.t, 1), bs = __shfl_up_sync(F, rec.s, 1);
+            // equal T and S: equal densities, not stable
+            if (st == 2 && __double_as_longlong(rec.t) == __double_as_longlong(bt) &&
+                __double_as_longlong(rec.s) == __double_as_longlong(bs))
+                st = 0;
+            const int above = __shfl_down_sync(F, st, 1);
+            if ((st == 2 || (lane < 31 && above == 2)) && rec.key == kNoKey)
+                rec.key = order_key(eos_rn(ec, rec.t, rec.s, 0.0));
+            const long long bk = __shfl_up_sync(F, rec.key, 1);
+            if (st == 2) st = rec.key < bk ? 1 : 0;
+        }
+        return __ballot_sync(F, st == 1);
+    };
+    unsigned stab = stable_mask(maxk);
+    // no unstable pair: co changes nothing
+    if ((~stab & co_bits(k1 + 1, maxk)) == 0u) return 0;
+    if (lane < L)
+        for (int lev = k1; lev <= maxk; lev += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (lev + u <= maxk) v[u] = wc[(size_t)(lev + u) * lstride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (lev + u <= maxk) tv[(lev + u) * 32 + lane] = v[u];
+        }
+    __syncwarp();
+    unsigned modified = 0u;
+    int m = maxk, lastmix = 0;
+    bool fresh = true;   // stab holds the pairs of the current list up to m
+    while (m > sp + 1 || (lastmix != 0 && m != maxk)) {
+        if (!fresh) stab = stable_mask(m);
+        fresh = false;
+        if (lastmix == 0) {
+            // walk down the stable pairs to the highest unstable one
+            const unsigned un = ~stab & co_bits(sp + 2, m);
+            if (un == 0u) break;
+            m = 32 - __clz(un);
+        } else if ((stab >> (m - 1)) & 1u) {
+            m = (m == maxk) ? m - 1 : m + 1;
+            lastmix = 0;
+            continue;
+        }
+        // merge positions n..m: n = the highest stable position below m (sp+1 always is)
+        const int n = 32 - __clz(stab & co_bits(sp + 1, m - 1));
+        const int d = m - n, lm = m - 1;
+        const int km = __shfl_sync(F, rec.kk, lm);
+        const double d0 = __shfl_sync(F, rec.dzm, lm);
+        double dtot = d0, acc = 0.0;
+        if (lane < L) acc = __dmul_rn(tv[km * 32 + lane], d0);
+        for (int ni = 1; ni <= d; ++ni) {
+            const int lv = __shfl_sync(F, rec.kk, lm - ni);
+            const double dzv = __shfl_sync(F, rec.dzm, lm - ni);
+            dtot = __dadd_rn(dtot, dzv);
+            if (lane < L) acc = __dadd_rn(acc, __dmul_rn(tv[lv * 32 + lane], dzv));
+        }
+        if (lane < L) tv[km * 32 + lane] = __ddiv_rn(acc, dtot);
+        __syncwarp();
+        modified |= 1u << (km - 1);
+        if (lane == lm) {
+            rec.dzm = dtot;
+            rec.t = tv[km * 32];
+            rec.s = tv[km * 32 + 1];
+            float mg;
+            const CoDf r = eos_df(ecd, rec.t, rec.s, mg);
+            rec.rdh = r.hi;
+            rec.rdl = r.lo;
+            rec.rm = mg;
+            rec.key = kNoKey;
+        }
+        // positions sp+d .. m-1 take the records d below (sp+d becomes the sentinel)
+        const CoRec sh = co_rec_up(rec, d);
+        if (p >= sp + d && p <= m - 1) rec = sh;
+        sp += d;
+        lastmix = 1;
+    }
+    // fill: every level of [k1, maxk-1] no longer in the list takes the values of the
+    // lowest listed level above it
+    const unsigned act = __reduce_or_sync(F, (p >= sp + 1 && p <= maxk) ? (1u << (rec.kk - 1)) : 0u);
+    const unsigned fillm = ~act & co_bits(k1, maxk - 1);
+    for (unsigned f = fillm; f; f &= f - 1u) {
+        const int lev = __ffs(f);
+        const int src = __ffs(act & ~((1u << lev) - 1u));
+        if (lane < L) tv[lev * 32 + lane] = tv[src * 32 + lane];
+    }
+    modified |= fillm;
+    __syncwarp();
+    if (lane < L)
+        for (unsigned f = modified; f; f &= f - 1u) {
+            const int lev = __ffs(f);
+            wc[(size_t)lev * lstride] = tv[lev * 32 + lane];
+        }
+    return __popc(fillm);
 }
 
 // Merge log of a column (one slot of kCoLogBytes per list entry): header {int nm, unsigned

@@ -371,8 +371,9 @@ extern "C" int gb_ens_set_tuning(gb_ens *e, const gb_ens_tuning *t)
     if (t->tile_i < 0 || t->tile_j < 0 || t->tile_i > 4096 || t->tile_j > 4096)
         return efail(e, GB_GO_EINVAL, "tile sizes must be in 0..4096");
     if (t->ctas_per_sm < 0 || t->ctas_per_sm > 32) return efail(e, GB_GO_EINVAL, "ctas_per_sm must be in 0..32");
-    if (t->packing < GB_ENS_PACK_MEMBERS || t->packing > GB_ENS_PACK_ROUND_ROBIN || t->reserved != 0)
+    if (t->packing < GB_ENS_PACK_MEMBERS || t->packing > GB_ENS_PACK_ROUND_ROBIN)
         return efail(e, GB_GO_EINVAL, "unknown packing");
+    if (t->co_form < GB_ENS_CO_AUTO || t->co_form > GB_ENS_CO_TWO_PHASE) return efail(e, GB_GO_EINVAL, "unknown co_form");
     e->tuning = *t;
     e->dirty = true;
     return GB_GO_OK;
@@ -1098,6 +1099,7 @@ static Fp32Batch batch_of(gb_ens *e)
     b.n_stencil = e->n_stencil;
     b.stencil_blocks = e->stencil_blocks;
     b.ctas_per_sm = e->tuning.ctas_per_sm;
+    b.co_form = e->tuning.co_form;
     return b;
 }
 

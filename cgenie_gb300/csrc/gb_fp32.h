@@ -2,6 +2,7 @@
 // batched ensemble (a single grid is a batch of one member).
 #pragma once
 
+#include "gb_goldstein.h"
 #include "gb_internal.h"
 
 #include <cuda_runtime.h>
@@ -312,12 +313,19 @@ struct Fp32Batch {
     const int *stencil_list = nullptr;   // descriptor indices of the members with a stencil
     int n_stencil = 0, stencil_blocks = 1;   // their count; blocks per member of the prepass
     int ctas_per_sm = 0;        // cap on resident CTAs per SM of the transfer kernels (0: none)
+    int co_form = 0;            // GB_ENS_CO_*: the adjustment's form (0: by the list capacity)
 };
 // s2/fork/join: a second stream and two events to run the two item kinds side by side
 // (s2 null: one stream).
 int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStream_t s, cudaStream_t s2,
                 cudaEvent_t fork, cudaEvent_t join);
 int fp32_launches_per_step(const Fp32Batch &b);   // kernels fp32_launch starts
+// the adjustment runs in two phases (else one warp per column): by the batch's form, or for
+// GB_ENS_CO_AUTO from GB_ENS_CO_TWO_PHASE_MIN listable columns
+inline bool fp32_co_two_phase(const Fp32Batch &b)
+{
+    return b.co_form == GB_ENS_CO_TWO_PHASE || (b.co_form == GB_ENS_CO_AUTO && b.cocap >= GB_ENS_CO_TWO_PHASE_MIN);
+}
 // scratch of the two-phase adjustment: merge-log bytes per listed column, and slots per column
 constexpr size_t kCoLogSlotBytes = 1152;
 inline int fp32_co_slots(int L) { return L > 2 ? L - 2 : 1; }

@@ -34,6 +34,8 @@
 #include "../../include/gb_goldstein.h"
 
 #include <cuda_runtime.h>
+#include <mutex>
+#include <vector>
 
 #include <algorithm>
 #include <climits>
@@ -1131,6 +1133,39 @@ k_co_mix(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, co
     }
 }
 
+// The one-warp-per-column form (small batches) of the columns with maxk <= 32, ieos = 0,
+// iconv = 0, imld = 0: warps take list entries in turn; co_warp32 (co_column.cuh) holds one
+// list position per lane and mixes the column's tracers one lane each.  kmax: the largest maxk
+// of the batch (shared memory: (kmax+1) x 32 tracer values per warp).
+__global__ void __launch_bounds__(kFp32Threads)
+k_co_warp(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist, int *__restrict__ cocount, int cocap,
+          const long long *__restrict__ step_ctr, int rel, int kmax)
+{
+    extern __shared__ double cosm[];
+    const long long step = *step_ctr + rel;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int ncol = min(cocount[step & 1], cocap);
+    // the list of the next step starts empty (that step's kernels run after this one)
+    if (blockIdx.x == 0 && threadIdx.x == 0) cocount[(step + 1) & 1] = 0;
+    double *tv = cosm + (size_t)warp * (kmax + 1) * 32;
+    for (int e = blockIdx.x * nwarp + warp; e < ncol; e += gridDim.x * nwarp) {
+        const int2 ent = colist[e];
+        const MemberDesc &md = mds[ent.x];
+        if (!fp32_co_fast(md.iconv, md.ieos, md.imld, md.maxk)) continue;
+        const CoCol c = co_col(md, ent, step);
+        EosCoef ec;
+        for (int n = 0; n < 5; ++n) ec.ec[n] = md.ec[n];
+        ec.ieos = 0;
+        // this lane's tracer (lanes < L) at level 0 and its level stride
+        size_t lstride = 0;
+        double *wc = lane < c.L ? co_tracer(c.W, c.L, c.plane, c.cell, c.NIJ, lane, lstride) : nullptr;
+        // T and S are plane 0, two values per cell
+        const int filled = co_warp32(tv, ec, c.maxk, c.L, c.k1, c.dz, lane, c.W + 2 * c.cell, 2 * c.NIJ, wc, lstride);
+        if (lane == 0 && filled > 0) *c.cost = add_count_rn(*c.cost, filled);
+        __syncwarp();
+    }
+}
+
 // The serial form for the other listed columns.  kmax: the largest maxk of the batch (shared
 // memory layout).
 __global__ void __launch_bounds__(kFp32Threads)
@@ -1254,6 +1289,48 @@ k_co_serial(const MemberDesc *__restrict__ mds, const int2 *__restrict__ colist,
 
 int fp32_smem_bytes(int max_slots) { return fp32_smem_layout(max_slots + 1).total; }
 
+// Resident CTAs per SM of a kernel at a block size and dynamic shared memory size, with the
+// kernel's shared-memory limit raised to at least that size first.  Both are runtime calls
+// costing microseconds on every launch of a step that is not replayed from a CUDA graph, so the
+// process remembers, per device and kernel, the largest limit it has set (it is only ever
+// raised: a launch with less shared memory stays valid) and the occupancy of every size asked.
+static int resident_ctas(const void *fn, int threads, int smem)
+{
+    struct Limit {
+        int dev;
+        const void *fn;
+        int smem;
+    };
+    struct Occ {
+        int dev;
+        const void *fn;
+        int threads, smem, per_sm;
+    };
+    static std::mutex mu;
+    static std::vector<Limit> limits;
+    static std::vector<Occ> occ;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem > 0) {
+        Limit *lim = nullptr;
+        for (Limit &x : limits)
+            if (x.dev == dev && x.fn == fn) lim = &x;
+        if (!lim) {
+            limits.push_back({dev, fn, 0});
+            lim = &limits.back();
+        }
+        if (smem > lim->smem && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess)
+            lim->smem = smem;
+    }
+    for (const Occ &x : occ)
+        if (x.dev == dev && x.fn == fn && x.threads == threads && x.smem == smem) return x.per_sm;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    occ.push_back({dev, fn, threads, smem, per_sm});
+    return per_sm;
+}
+
 template <bool ISO, bool TS>
 static void launch_step_instance(const MemberDesc *descs, const int4 *items, int nitems, int P,
                                  const long long *step_ctr, int rel, int *work, int2 *colist, int *cocount, int cocap,
@@ -1262,9 +1339,7 @@ static void launch_step_instance(const MemberDesc *descs, const int4 *items, int
     if (nitems <= 0) return;
     const int smem_bytes = fp32_smem_layout(P).total;
     auto kern = k_step_fp32<ISO, TS>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFp32Threads, smem_bytes);
+    int per_sm = resident_ctas((const void *)kern, kFp32Threads, smem_bytes);
     if (ctas_cap > 0) per_sm = std::min(per_sm, ctas_cap);
     if (per_sm < 1) per_sm = 1;
     const int grid = std::max(1, std::min(nitems, nsm * per_sm));
@@ -1302,12 +1377,14 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         launch_step_instance<false, false>(b.descs, b.items + b.n_ts, b.n_bgc, P, step_ctr, rel,
                                            b.work + 2, b.colist, b.cocount, b.cocap, nsm, b.ctas_per_sm, sb);
     }
-    // the adjustment's decisions need only T, S and the column list, which the T-S items
-    // complete: they run while the other tracer groups are still stepping (k_co_decide writes T
-    // and S in place, plane 0 of the new state, which the group items neither read nor write)
-    {
+    // the adjustment's form: two phases for large batches, one warp per column for small ones
+    const bool two_phase = fp32_co_two_phase(b);
+    // the two-phase decisions need only T, S and the column list, which the T-S items complete:
+    // they run while the other tracer groups are still stepping (k_co_decide writes T and S in
+    // place, plane 0 of the new state, which the group items neither read nor write)
+    if (two_phase) {
         const int smem = (kCoDecideThreads / 32) * kCoDecideWarpBytes;
-        cudaFuncSetAttribute(k_co_decide, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        resident_ctas((const void *)k_co_decide, kCoDecideThreads, smem);
         // one one-warp block per 32 list entries of the capacity: blocks past the step's count
         // exit, and the others are scheduled as SMs free up (a deep column's warp delays only itself)
         const int grid = std::max(1, (b.cocap + kCoDecideThreads - 1) / kCoDecideThreads);
@@ -1318,18 +1395,22 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
         cudaEventRecord(join, s2);
         cudaStreamWaitEvent(s, join, 0);
     }
-    // then the other tracers of the two-phase columns, and (if the batch has any) the serial columns
-    {
-        int mper_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mper_sm, k_co_mix, kCoMixThreads, 0);
+    // then the other tracers of the two-phase columns (or the one-warp-per-column form), and (if
+    // the batch has any) the serial columns
+    if (!two_phase) {
+        const int kst = std::min(b.kmax, 32) + 1;
+        const int wsmem = (kFp32Threads / 32) * kst * 32 * (int)sizeof(double);
+        const int wper_sm = resident_ctas((const void *)k_co_warp, kFp32Threads, wsmem);
+        k_co_warp<<<nsm * std::max(1, wper_sm), kFp32Threads, wsmem, s>>>(b.descs, b.colist, b.cocount, b.cocap, step_ctr,
+                                                                        rel, std::min(b.kmax, 32));
+    } else {
+        const int mper_sm = resident_ctas((const void *)k_co_mix, kCoMixThreads, 0);
         k_co_mix<<<nsm * std::max(1, mper_sm), kCoMixThreads, 0, s>>>(b.descs, b.colist, b.cocount, step_ctr, rel, b.colog,
                                                                      b.comap, b.mapcap);
     }
     if (b.co_general) {
         const int co_smem = (kFp32Threads / 32) * ((b.kmax + 1) * 32 * (int)sizeof(double) + (int)sizeof(CoWarpState));
-        cudaFuncSetAttribute(k_co_serial, cudaFuncAttributeMaxDynamicSharedMemorySize, co_smem);
-        int co_per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&co_per_sm, k_co_serial, kFp32Threads, co_smem);
+        const int co_per_sm = resident_ctas((const void *)k_co_serial, kFp32Threads, co_smem);
         k_co_serial<<<nsm * std::max(1, co_per_sm), kFp32Threads, co_smem, s>>>(b.descs, b.colist, b.cocount, b.cocap,
                                                                                step_ctr, rel, b.kmax);
     }
@@ -1338,7 +1419,7 @@ int fp32_launch(const Fp32Batch &b, const long long *step_ctr, int rel, cudaStre
 
 int fp32_launches_per_step(const Fp32Batch &b)
 {
-    return (b.n_stencil > 0) + (b.n_ts > 0) + (b.n_bgc > 0) + 2 + (b.co_general ? 1 : 0);
+    return (b.n_stencil > 0) + (b.n_ts > 0) + (b.n_bgc > 0) + (fp32_co_two_phase(b) ? 2 : 1) + (b.co_general ? 1 : 0);
 }
 
 // ---------------------------------------------------------------------------

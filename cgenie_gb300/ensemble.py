@@ -48,9 +48,10 @@ def host_copy(a) -> np.ndarray:
 class Ensemble:
     def __init__(self, device: int = -1, hbm_budget_bytes: int = 0, *, tile_i: int = 0, tile_j: int = 0,
                  use_graph: bool = False, stream: Optional[int] = None, use_table: bool = True,
-                 packing: Optional[int] = None, ctas_per_sm: Optional[int] = None):
+                 packing: Optional[int] = None, ctas_per_sm: Optional[int] = None, co_form: int = 0):
         """packing / ctas_per_sm: the batch's member packing (abi.GB_ENS_PACK_*) and cap on resident
-        CTAs per SM; None = the autotuned values of the tuning table (else 0 and 0)."""
+        CTAs per SM; None = the autotuned values of the tuning table (else 0 and 0).  co_form: the
+        convective adjustment's form (abi.GB_ENS_CO_*; 0: by the batch's size)."""
         self.lib = load_library()
         e = C.c_void_p()
         rc = self.lib.gb_ens_create(int(device), C.c_size_t(hbm_budget_bytes), C.byref(e))
@@ -67,6 +68,7 @@ class Ensemble:
         tuned = batch_entry(self.table)
         self.packing = int(tuned[0] if packing is None else packing)
         self.ctas_per_sm = int(tuned[1] if ctas_per_sm is None else ctas_per_sm)
+        self.co_form = int(co_form)
         self.set_tuning(tile_i=tile_i, tile_j=tile_j, use_graph=use_graph)
         if stream is not None:
             self._check(self.lib.gb_ens_set_stream(self.e, C.c_void_p(stream)), "gb_ens_set_stream")
@@ -80,7 +82,7 @@ class Ensemble:
         """gb_ens_set_tuning; ctas_per_sm / packing None: the ensemble's batch settings."""
         cps = self.ctas_per_sm if ctas_per_sm is None else int(ctas_per_sm)
         pk = self.packing if packing is None else int(packing)
-        t = GbEnsTuning(int(tile_i), int(tile_j), cps, int(bool(use_graph)), pk, 0)
+        t = GbEnsTuning(int(tile_i), int(tile_j), cps, int(bool(use_graph)), pk, self.co_form)
         self._check(self.lib.gb_ens_set_tuning(self.e, C.byref(t)), "gb_ens_set_tuning")
 
     def close(self):

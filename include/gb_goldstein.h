@@ -213,7 +213,8 @@ typedef struct gb_ens_tuning {
     int32_t use_graph;        /* capture a multi-step launch in a CUDA graph */
     int32_t packing;          /* order of the work items in the launch (member packing):
                                  GB_ENS_PACK_MEMBERS, GB_ENS_PACK_ITEMS or GB_ENS_PACK_ROUND_ROBIN */
-    int32_t reserved;         /* 0 */
+    int32_t co_form;          /* convective adjustment of the maxk <= 32, ieos = 0 columns:
+                                 GB_ENS_CO_AUTO, GB_ENS_CO_WARP or GB_ENS_CO_TWO_PHASE */
 } gb_ens_tuning;
 
 /* Member packing: members by decreasing work, each member's patches together and a patch's
@@ -223,6 +224,15 @@ typedef struct gb_ens_tuning {
 #define GB_ENS_PACK_ITEMS       1
 /* the n-th patch of every member, then the (n+1)-th (DRAM traffic spread over members) */
 #define GB_ENS_PACK_ROUND_ROBIN 2
+
+/* The adjustment's form: one warp per listed column (small batches), or two phases (a lane per
+ * column for the decisions on T and S, a lane per column and tracer replaying the logged merges;
+ * large batches).  AUTO: two phases from GB_ENS_CO_TWO_PHASE_MIN listable (wet) columns in the
+ * batch.  Every form gives the same results bit for bit. */
+#define GB_ENS_CO_AUTO          0
+#define GB_ENS_CO_WARP          1
+#define GB_ENS_CO_TWO_PHASE     2
+#define GB_ENS_CO_TWO_PHASE_MIN 100000
 
 int  gb_ens_create(int device, size_t hbm_budget_bytes, gb_ens **out);
 void gb_ens_destroy(gb_ens *e);

@@ -9,6 +9,8 @@ Bars, per tracer, over wet cells, error = max|x - x_oracle| / max|x_oracle|:
     drift <= 1e-12 relative
   * the kernel equals the CPU emulation of the same scheme (tests/fp32_emul.py)
     to 1e-13 (tracers other than T, S) -- a spec check of the kernel itself."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -193,11 +195,15 @@ def test_ensemble_alone_equals_in_mix(gpu_lib):
     mix.close()
 
 
-def test_ensemble_matches_oracle_per_member(gpu_lib, oracle):
+CO_FORMS = pytest.mark.parametrize("co_form", [abi.GB_ENS_CO_WARP, abi.GB_ENS_CO_TWO_PHASE], ids=["warp", "two_phase"])
+
+
+@CO_FORMS
+def test_ensemble_matches_oracle_per_member(gpu_lib, oracle, co_form):
     from cgenie_gb300.ensemble import Ensemble
     cfgs = grid.ensemble_configs(n=6, seed=11)
     mems = [grid.make_member(c) for c in cfgs]
-    ens = Ensemble(use_graph=True)
+    ens = Ensemble(use_graph=True, co_form=co_form)
     ids = [ens.add(m) for m in mems]
     inv0 = [ens.inventory(i) for i in ids]
     ens.step(20)
@@ -216,8 +222,9 @@ def test_ensemble_matches_oracle_per_member(gpu_lib, oracle):
     ens.close()
 
 
-def test_ensemble_mixed_adjustment_forms(gpu_lib, oracle):
-    """One batch with members of both adjustment forms: warp-parallel (ieos = 0,
+@CO_FORMS
+def test_ensemble_mixed_adjustment_forms(gpu_lib, oracle, co_form):
+    """One batch with members of both adjustment paths: warp-parallel or two-phase (ieos = 0,
     iconv = 0, maxk <= 32) and serial (ieos = 1 with coshuffle; 40 levels), and a member
     with the local vertical diffusivity (iediff = 1)."""
     from cgenie_gb300.ensemble import Ensemble
@@ -228,7 +235,7 @@ def test_ensemble_mixed_adjustment_forms(gpu_lib, oracle):
             grid.make_member(grid.MemberConfig(maxi=16, maxj=12, maxk=40, maxl=4, seed=63, noise=2.0)),
             grid.make_member(grid.MemberConfig(maxi=18, maxj=14, maxk=16, maxl=4, seed=64, iediff=1,
                                                ediffpow2=1.0, tracer_kind="bgc"))]
-    ens = Ensemble(use_graph=True)
+    ens = Ensemble(use_graph=True, co_form=co_form)
     ids = [ens.add(m) for m in mems]
     ens.step(25)
     for m, i in zip(mems, ids):
@@ -404,6 +411,9 @@ def test_ensemble_packing_and_cta_cap_do_not_change_results(gpu_lib):
         e.set_tuning(packing=7)
     with pytest.raises(GoldsteinError):
         e.set_tuning(ctas_per_sm=-1)
+    e.co_form = 3
+    with pytest.raises(GoldsteinError):
+        e.set_tuning()
     e.close()
 
 
@@ -468,14 +478,14 @@ def test_ensemble_adjustment_scratch_grows(gpu_lib):
            for s, l in ((703, 24), (704, 32))]
 
     def alone(m, steps):
-        e = Ensemble(use_graph=True)
+        e = Ensemble(use_graph=True, co_form=abi.GB_ENS_CO_TWO_PHASE)
         i = e.add_many([m])
         e.step(steps)
         out = e.download_many(i)[0]["ts"]
         e.close()
         return out
 
-    e = Ensemble(use_graph=True)
+    e = Ensemble(use_graph=True, co_form=abi.GB_ENS_CO_TWO_PHASE)
     ids = e.add_many(small)
     e.step(6)
     for i, m in zip(ids, small):
@@ -488,3 +498,25 @@ def test_ensemble_adjustment_scratch_grows(gpu_lib):
         assert np.array_equal(e.download_many([i])[0]["ts"], alone(m, 6))
     assert all(e.status(i) == 0 for i in ids + bid)
     e.close()
+
+
+def test_ensemble_adjustment_forms_agree(gpu_lib):
+    """The one-warp-per-column and two-phase adjustments give the same state and convection
+    counts bit for bit, on convecting members of every shape and tracer count (and both at
+    once in the automatic form's choice for this small batch)."""
+    from cgenie_gb300.ensemble import Ensemble
+    cfgs = grid.ensemble_configs(n=9, seed=21)
+    mems = [grid.make_member(dataclasses.replace(c, noise=2.0)) for c in cfgs]
+    outs = {}
+    for form in (abi.GB_ENS_CO_WARP, abi.GB_ENS_CO_TWO_PHASE, abi.GB_ENS_CO_AUTO):
+        e = Ensemble(use_graph=True, co_form=form)
+        ids = e.add_many(mems)
+        e.step(30)
+        outs[form] = [e.download(i) for i in ids]
+        assert all(e.status(i) == 0 for i in ids)
+        e.close()
+    for a, b, c in zip(*outs.values()):
+        for k in ("ts", "cost"):
+            assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), k
+    # the members do convect
+    assert sum(int(np.sum(o["cost"] != m.cost)) for o, m in zip(outs[abi.GB_ENS_CO_WARP], mems)) > 100
