@@ -213,7 +213,8 @@ struct Fp32Col {
 // face transfers of level k from the slabs of k and k+1 (the bottom face carried
 // in registers) and writes its column's FP64 update.  Three slab buffers make one
 // barrier per level enough.  The group of T and S also flags the columns whose FP32
-// density profile may be unstable; k_co_fp32 then adjusts those columns exactly.
+// density profile may be unstable; the adjustment kernels (k_co_warp or k_co_decide and
+// k_co_mix, and k_co_serial) then adjust those columns exactly.
 
 // FP32 slab pitch per slot (kGroup tracers + 1: consecutive slots hit distinct banks)
 constexpr int kGP = 9;
@@ -803,9 +804,10 @@ int fp32_rescale(const MemberDesc *descs, int n, cudaStream_t s)
 // its FP32 prescreen cannot prove stable, and every column of members with iconv = 1,
 // ieos != 0 or imld = 1), on the FP64 state the step wrote.  A list
 // entry is (member, word offset of the column's record).  Columns of members with iconv = 0,
-// ieos = 0, imld = 0 and maxk <= 32 take the two phases k_co_decide and k_co_mix; the others
-// take k_co_serial, one entry per warp, by co_warp (the column staged in shared memory, one
-// lane per tracer), with coshuffle (iconv = 1) and the mixed layer on one lane.
+// ieos = 0, imld = 0 and maxk <= 32 take k_co_warp (one warp per column; small batches) or the
+// two phases k_co_decide and k_co_mix (large batches; fp32_co_two_phase); the others take
+// k_co_serial, one entry per warp, by co_warp (the column staged in shared memory, one lane per
+// tracer), with coshuffle (iconv = 1) and the mixed layer on one lane.
 
 // A list entry's column as the adjustment kernels see it.
 struct CoCol {
