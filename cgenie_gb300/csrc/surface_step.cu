@@ -37,6 +37,7 @@ struct EaArgs {
     const int32_t *k1;
     double *tq, *tq1;
     const double *src, *vel, *pptn;
+    double *dth, *ddy;   // sea ice: variceth, varicedy (2, maxi, maxj)
 };
 
 __device__ __forceinline__ double clamp01(double x)
@@ -240,6 +241,13 @@ __global__ void __launch_bounds__(kThreads) k_surface_step(const EaArgs *__restr
         const size_t x = (size_t)(l - 1) + 2 * ((size_t)(i - 1) + (size_t)maxi * (j - 1));
         a.tq[x] = tq[r];
         a.tq1[x] = tq1[r];
+        if (ice && upd[r]) {
+            // the thermal and dynamical parts of the step's ice change, purely diagnostic
+            // (gold_seaice.f90:1046-1056)
+            const double th = a.tsc * dt * a.src[x];
+            a.dth[x] = th;
+            a.ddy[x] = tq[r] - tq1[r] - th;
+        }
     }
 }
 
@@ -319,6 +327,7 @@ struct gb_ea {
     double *rc = nullptr, *cv = nullptr, *dsv = nullptr, *rdsv = nullptr, *rds = nullptr, *diffa = nullptr;
     int32_t *k1 = nullptr;
     double *tq = nullptr, *tq1 = nullptr, *src = nullptr, *vel = nullptr, *pptn = nullptr;
+    double *dth = nullptr, *ddy = nullptr;   // sea ice: variceth, varicedy
     bool have_state = false, have_forcing = false;
     int cluster_max = 8;   // 16 where the device schedules clusters of 16 (gb_ea_create)
     EaArgs *dargs = nullptr;   // kernel arguments in device memory (capacity cap_args grids)
@@ -392,6 +401,10 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     up(&h->src, nullptr, n2);
     up(&h->vel, nullptr, n2);
     up(&h->pptn, nullptr, (size_t)maxi * maxj);
+    up(&h->dth, nullptr, n2);
+    up(&h->ddy, nullptr, n2);
+    if (e == cudaSuccess) e = cudaMemset(h->dth, 0, n2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(h->ddy, 0, n2 * sizeof(double));
     const size_t nk = (size_t)(maxi + 2) * (maxj + 2);
     if (e == cudaSuccess) e = cudaMalloc(&h->k1, nk * sizeof(int32_t));
     if (e == cudaSuccess && p.kind != GB_EA_EMBM)
@@ -436,7 +449,7 @@ extern "C" void gb_ea_destroy(gb_ea *h)
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn, h->dargs};
+    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn, h->dth, h->ddy, h->dargs};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -505,6 +518,8 @@ static EaArgs args_of(const gb_ea *h, int nsteps)
     a.src = h->src;
     a.vel = h->vel;
     a.pptn = h->pptn;
+    a.dth = h->dth;
+    a.ddy = h->ddy;
     return a;
 }
 
@@ -584,6 +599,18 @@ extern "C" int gb_ea_download(gb_ea *h, double *tq, double *tq1)
     const size_t n2 = 2 * (size_t)h->d.maxi * h->d.maxj;
     if (tq) EA_TRY(h, cudaMemcpyAsync(tq, h->tq, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     if (tq1) EA_TRY(h, cudaMemcpyAsync(tq1, h->tq1, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_download_seaice_diag(gb_ea *h, double *variceth, double *varicedy)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (h->p.kind == GB_EA_EMBM) return efail(h, GB_GO_EINVAL, "download_seaice_diag: an EMBM handle has no ice");
+    EA_TRY(h, cudaSetDevice(h->device));
+    const size_t n2 = 2 * (size_t)h->d.maxi * h->d.maxj;
+    if (variceth) EA_TRY(h, cudaMemcpyAsync(variceth, h->dth, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (varicedy) EA_TRY(h, cudaMemcpyAsync(varicedy, h->ddy, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     EA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
 }

@@ -183,6 +183,14 @@ class SurfaceStepper:
         self._check(self.lib.gb_ea_download(self.h, dptr(tq), dptr(tq1)), "gb_ea_download")
         return tq, tq1
 
+    def download_seaice_diag(self):
+        """(variceth, varicedy) [j, i, l] of the last tstipsic step (gold_seaice.f90:1046-1056)."""
+        c = self.case
+        th = np.zeros((c.maxj, c.maxi, 2))
+        dy = np.zeros((c.maxj, c.maxi, 2))
+        self._check(self.lib.gb_ea_download_seaice_diag(self.h, dptr(th), dptr(dy)), "gb_ea_download_seaice_diag")
+        return th, dy
+
 
 def step_many(steppers, nsteps: int = 1):
     """One launch advancing every stepper (same kind and shape, one device) by nsteps."""

@@ -81,6 +81,13 @@ int gb_ea_step(gb_ea *h, int32_t nsteps);
    errors are reported on handles[0]. */
 int gb_ea_step_many(gb_ea *const *handles, int32_t n, int32_t nsteps);
 int gb_ea_download(gb_ea *h, double *tq, double *tq1);
+/* Sea ice: the diagnostic split of the last tstipsic's ice change, variceth = tsc*dtsic*dtha
+   (thermal) and varicedy = varice - varice1 - variceth (dynamical), (2, maxi, maxj) each, as
+   gold_seaice.f90:1046-1056 sets them on the ocean cells; other cells keep their previous
+   values (0 from creation, as initialise_seaice, gold_seaice.f90:329-330).  tstepsic (kind
+   GB_EA_SEAICE_EXPLICIT) does not set them: they stay 0.  Either pointer may be NULL.
+   GB_GO_EINVAL for an EMBM handle. */
+int gb_ea_download_seaice_diag(gb_ea *h, double *variceth, double *varicedy);
 const char *gb_ea_last_error(const gb_ea *h);
 
 #ifdef __cplusplus

@@ -3,7 +3,8 @@
 Independent NumPy restatement of the 2-D surface steppers, written from the Fortran
 separately from oracle/surface_oracle.c:
   tstipa    src/embm/embm.f90:2039-2138
-  tstipsic  src/goldsteinseaice/gold_seaice.f90:937-1058 (without the diagnostics of :1047-1055)
+  tstipsic  src/goldsteinseaice/gold_seaice.f90:937-1058 (its diagnostics of :1046-1056 in
+            seaice_diag)
   tstepsic  src/goldsteinseaice/gold_seaice.f90:844-929 (as whole-array face fluxes: the
             reference's west/south carries are the east/north fluxes of the neighbours)
 Arrays are [j, i] views (C order) of the Fortran (i, j) fields; tq is [j, i, l].  Every cell's
@@ -90,6 +91,19 @@ def step(kind, maxk, dt, dphi, rdphi, betaz, betam, diffmod0, ppmin, ppmax, diff
             tq[..., l] = t
         if kind == 0:
             tq1[...] = tq
+
+
+
+def seaice_diag(maxk, dt, tsc, k1, tq, tq1, dtha, variceth, varicedy):
+    """The thermal and dynamical parts of the last tstipsic's ice change on the ocean cells
+    (gold_seaice.f90:1046-1056): variceth = tsc*dtsic*dtha, varicedy = varice - varice1 -
+    variceth; tq (varice after the step), tq1, dtha, variceth, varicedy [j, i, l]; the last two
+    are updated in place (other cells keep their values)."""
+    maxj, maxi = tq.shape[:2]
+    wet = (k1[1:maxj + 1, 1:maxi + 1] <= maxk)[..., None]
+    th = tsc * dt * dtha
+    variceth[...] = np.where(wet, th, variceth)
+    varicedy[...] = np.where(wet, tq - tq1 - th, varicedy)
 
 
 def tstepsic(maxk, dt, rdphi, diffsic, tsc, sica, sich, rc, cv, rdsv, rds, k1, tq, tq1, dtha, vel):

@@ -114,3 +114,70 @@ def test_step_many_rejects_mixed_shapes(gpu_lib):
     assert e.value.code == abi.GB_GO_EINVAL
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("cfg", [dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=25, land_frac=0.5),
+                                 dict(maxi=180, maxj=90, maxk=8, maxl=2, seed=26, land_frac=0.4)],
+                         ids=["36x36", "180x90"])
+def test_seaice_diagnostics_bitexact(gpu_lib, cfg):
+    """variceth / varicedy of tstipsic (gold_seaice.f90:1046-1056) against the NumPy oracle,
+    over two calls (the second starts from the first's ice, with new forcing); land cells stay 0."""
+    from oracle import surface_np as snp
+    m = grid.make_member(grid.MemberConfig(**cfg))
+    c = surface.seaice_case(m, seed=8)
+    s = surface.SurfaceStepper(c.copy())
+    ref = c.copy()
+    th_ref, dy_ref = np.zeros_like(c.tq), np.zeros_like(c.tq)
+    rng = np.random.default_rng(9)
+    for call in range(2):
+        if call:
+            ref.tq1 = ref.tq.copy()
+            ref.source = ref.source * rng.uniform(0.5, 1.5, ref.source.shape)
+        s.upload_state(ref.tq, ref.tq1)
+        s.set_forcing(source=ref.source)
+        s.step(1)
+        tq1_before = ref.tq1.copy()
+        ol.surface_step(ref, 1)
+        snp.seaice_diag(ref.maxk, ref.dt, ref.tsc, ref.k1, ref.tq, tq1_before, ref.source, th_ref, dy_ref)
+        th, dy = s.download_seaice_diag()
+        assert np.array_equal(th.view(np.uint64), th_ref.view(np.uint64))
+        assert np.array_equal(dy.view(np.uint64), dy_ref.view(np.uint64))
+    dry = m.k1[1:-1, 1:-1] > m.maxk
+    assert dry.any() and not th[dry].any() and not dy[dry].any()
+    assert np.abs(dy).max() > 0 and np.abs(th).max() > 0
+    s.close()
+
+
+def test_seaice_diagnostics_forms(gpu_lib):
+    """The explicit step leaves the diagnostics at 0 (tstepsic does not set them); batched
+    implicit steps set each grid's own; an EMBM handle has none."""
+    from cgenie_gb300.goldstein import GoldsteinError
+    from oracle import surface_np as snp
+    m = grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=8, maxl=2, seed=27, land_frac=0.3))
+    s = surface.SurfaceStepper(surface.seaice_case(m, seed=10, explicit=True))
+    s.upload_state()
+    s.set_forcing()
+    s.step(1)
+    th, dy = s.download_seaice_diag()
+    assert not th.any() and not dy.any()
+    s.close()
+    cases = [surface.seaice_case(grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=8, maxl=2, seed=80 + n,
+                                                                    land_frac=0.3)), seed=90 + n) for n in range(3)]
+    steppers = [surface.SurfaceStepper(c.copy()) for c in cases]
+    for st in steppers:
+        st.upload_state()
+        st.set_forcing()
+    surface.step_many(steppers, 1)
+    for st, c in zip(steppers, cases):
+        ref = c.copy()
+        ol.surface_step(ref, 1)
+        th_ref, dy_ref = np.zeros_like(c.tq), np.zeros_like(c.tq)
+        snp.seaice_diag(c.maxk, c.dt, c.tsc, c.k1, ref.tq, c.tq1, c.source, th_ref, dy_ref)
+        th, dy = st.download_seaice_diag()
+        assert np.array_equal(th, th_ref) and np.array_equal(dy, dy_ref)
+        st.close()
+    e_ = surface.SurfaceStepper(surface.embm_case(m, seed=11))
+    with pytest.raises(GoldsteinError) as e:
+        e_.download_seaice_diag()
+    assert e.value.code == abi.GB_GO_EINVAL
+    e_.close()

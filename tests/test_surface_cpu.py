@@ -78,3 +78,20 @@ def test_explicit_seaice_restatements_agree(cfg):
                  b.k1, b.tq, b.tq1, b.source, b.vel)
     assert np.array_equal(a.tq, b.tq)
     assert not np.array_equal(a.tq, c.tq)
+
+
+def test_seaice_diag_splits_the_change():
+    """tstipsic's diagnostics (gold_seaice.f90:1046-1056): the thermal part is the source
+    term's contribution, the dynamical part the rest of the change; land cells keep their
+    values."""
+    m = grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=16, maxl=2, seed=5, land_frac=0.5))
+    c = surface.seaice_case(m, seed=6)
+    a = c.copy()
+    np_step(a, 1)
+    th, dy = np.full_like(c.tq, 7.0), np.full_like(c.tq, 7.0)
+    snp.seaice_diag(c.maxk, c.dt, c.tsc, c.k1, a.tq, c.tq1, c.source, th, dy)
+    wet = m.k1[1:-1, 1:-1] <= m.maxk
+    assert np.array_equal(th[wet], (c.tsc * c.dt * c.source)[wet])
+    np.testing.assert_allclose((th + dy)[wet], (a.tq - c.tq1)[wet], rtol=0, atol=1e-12 * np.abs(a.tq).max())
+    assert (th[~wet] == 7.0).all() and (dy[~wet] == 7.0).all()
+    assert np.abs(dy[wet]).max() > 0
