@@ -116,6 +116,12 @@ class GbEaParams(C.Structure):
                 ("sich_thresh", C.c_double)]
 
 
+class GbEaSeaicePost(C.Structure):
+    """gb_ea_seaice_post: the constants of step_seaice's post-processing."""
+    _fields_ = [("rhoio", C.c_double), ("rhoice", C.c_double), ("hlf", C.c_double), ("hmin", C.c_double),
+                ("rdtdim", C.c_double), ("m2mm", C.c_double)]
+
+
 class GbEaGrid(C.Structure):
     """gb_ea_grid: j metrics with their Fortran bounds, diffa (EMBM) or k1 (sea ice)."""
     _fields_ = [("rc", _dp), ("cv", _dp), ("dsv", _dp), ("rdsv", _dp), ("rds", _dp), ("diffa", _dp),

@@ -38,6 +38,8 @@ struct EaArgs {
     double *tq, *tq1;
     const double *src, *vel, *pptn;
     double *dth, *ddy;   // sea ice: variceth, varicedy (2, maxi, maxj)
+    double rhoio, rhoice, hlf, hmin, rdtdim, m2mm;   // sea ice: step_seaice's post-processing
+    double *fx, *fw;     // sea ice: fx_delta, fw_delta (maxi, maxj)
 };
 
 __device__ __forceinline__ double clamp01(double x)
@@ -305,6 +307,35 @@ __global__ void __launch_bounds__(256) k_seaice_explicit(const EaArgs *__restric
     }
 }
 
+// step_seaice's post-processing of a sea-ice step (gold_seaice.f90:599-619), one thread per
+// cell: the area is held in [0, 1]; ice thinner than hmin is removed, its latent heat and
+// water returned to the ocean as fluxes; varice1 = varice.  Land cells keep fx = fw = 0
+// (gold_seaice.f90:578-579).
+__global__ void __launch_bounds__(256) k_seaice_post(const EaArgs *__restrict__ args)
+{
+    const EaArgs a = args[blockIdx.y];
+    const int maxi = a.maxi;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= maxi * a.maxj) return;
+    const int i = c % maxi + 1, j = c / maxi + 1;
+    if (a.maxk < a.k1[i + (size_t)(maxi + 2) * j]) return;
+    const size_t x = 2 * (size_t)c;
+    double fw = -(a.rhoio * a.src[x]);
+    double fx = 0.0;
+    double h = a.tq[x];
+    double ar = clamp01(a.tq[x + 1]);
+    if (h < a.hmin) {
+        fx = -(((h * a.rhoice) * a.hlf) * a.rdtdim);
+        fw = fw + (h * a.rhoio) * a.rdtdim;
+        h = 0.0;
+        ar = 0.0;
+    }
+    a.tq[x] = a.tq1[x] = h;
+    a.tq[x + 1] = a.tq1[x + 1] = ar;
+    a.fx[c] = fx;
+    a.fw[c] = fw * a.m2mm;   // m/s to mm/s
+}
+
 // rows per block and blocks per tracer (the cluster size, at most kClusterMax)
 void split_rows(int maxj, int *R, int *C, int cmax = kClusterMax)
 {
@@ -328,6 +359,9 @@ struct gb_ea {
     int32_t *k1 = nullptr;
     double *tq = nullptr, *tq1 = nullptr, *src = nullptr, *vel = nullptr, *pptn = nullptr;
     double *dth = nullptr, *ddy = nullptr;   // sea ice: variceth, varicedy
+    double *fx = nullptr, *fw = nullptr;     // sea ice: fx_delta, fw_delta
+    bool post = false;                        // sea ice: post-process each step
+    gb_ea_seaice_post pp{};
     bool have_state = false, have_forcing = false;
     int cluster_max = 8;   // 16 where the device schedules clusters of 16 (gb_ea_create)
     EaArgs *dargs = nullptr;   // kernel arguments in device memory (capacity cap_args grids)
@@ -405,6 +439,10 @@ extern "C" int gb_ea_create(const gb_ea_dims *dims, const gb_ea_params *params, 
     up(&h->ddy, nullptr, n2);
     if (e == cudaSuccess) e = cudaMemset(h->dth, 0, n2 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(h->ddy, 0, n2 * sizeof(double));
+    up(&h->fx, nullptr, n2 / 2);
+    up(&h->fw, nullptr, n2 / 2);
+    if (e == cudaSuccess) e = cudaMemset(h->fx, 0, n2 / 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(h->fw, 0, n2 / 2 * sizeof(double));
     const size_t nk = (size_t)(maxi + 2) * (maxj + 2);
     if (e == cudaSuccess) e = cudaMalloc(&h->k1, nk * sizeof(int32_t));
     if (e == cudaSuccess && p.kind != GB_EA_EMBM)
@@ -449,7 +487,7 @@ extern "C" void gb_ea_destroy(gb_ea *h)
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn, h->dth, h->ddy, h->dargs};
+    void *ptrs[] = {h->rc, h->cv, h->dsv, h->rdsv, h->rds, h->diffa, h->k1, h->tq, h->tq1, h->src, h->vel, h->pptn, h->dth, h->ddy, h->fx, h->fw, h->dargs};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -520,6 +558,14 @@ static EaArgs args_of(const gb_ea *h, int nsteps)
     a.pptn = h->pptn;
     a.dth = h->dth;
     a.ddy = h->ddy;
+    a.rhoio = h->pp.rhoio;
+    a.rhoice = h->pp.rhoice;
+    a.hlf = h->pp.hlf;
+    a.hmin = h->pp.hmin;
+    a.rdtdim = h->pp.rdtdim;
+    a.m2mm = h->pp.m2mm;
+    a.fx = h->fx;
+    a.fw = h->fw;
     return a;
 }
 
@@ -532,12 +578,13 @@ static int step_grids(gb_ea *const *hs, int n, int nsteps)
         const gb_ea *g = hs[m];
         if (!g) return efail(h, GB_GO_EINVAL, "step: NULL handle");
         if (g->device != h->device || g->p.kind != h->p.kind || g->d.maxi != h->d.maxi || g->d.maxj != h->d.maxj ||
-            g->cluster_max != h->cluster_max)
-            return efail(h, GB_GO_EINVAL, "step_many: grids differ in device, kind or shape");
+            g->cluster_max != h->cluster_max || g->post != h->post)
+            return efail(h, GB_GO_EINVAL, "step_many: grids differ in device, kind, shape or post-processing");
         if (!g->have_state || !g->have_forcing) return efail(h, GB_GO_ENOTREADY, "step before upload_state/set_forcing");
     }
-    if (h->p.kind != GB_EA_EMBM && nsteps > 1)
-        return efail(h, GB_GO_EINVAL, "step: sea ice takes one step per call (step_seaice post-processes between steps)");
+    if (h->p.kind != GB_EA_EMBM && nsteps > 1 && !h->post)
+        return efail(h, GB_GO_EINVAL,
+                     "step: sea ice takes one step per call unless its post-processing is on (gb_ea_set_seaice_post)");
     if (nsteps == 0 || n == 0) return GB_GO_OK;
     EA_TRY(h, cudaSetDevice(h->device));
     if (n > h->cap_args) {
@@ -548,30 +595,38 @@ static int step_grids(gb_ea *const *hs, int n, int nsteps)
         h->cap_args = n;
     }
     std::vector<EaArgs> args((size_t)n);
-    for (int m = 0; m < n; ++m) args[m] = args_of(hs[m], nsteps);
+    // with the sea-ice post-processing on, every step is a step launch and a post launch
+    const bool post = h->post && h->p.kind != GB_EA_EMBM;
+    for (int m = 0; m < n; ++m) args[m] = args_of(hs[m], post ? 1 : nsteps);
     EA_TRY(h, cudaMemcpyAsync(h->dargs, args.data(), (size_t)n * sizeof(EaArgs), cudaMemcpyHostToDevice, h->stream));
-    if (h->p.kind == GB_EA_SEAICE_EXPLICIT) {
-        const int ncell = h->d.maxi * h->d.maxj;
-        k_seaice_explicit<<<dim3((ncell + 255) / 256, n), 256, 0, h->stream>>>(h->dargs);
-    } else {
-        int R = 0, C = 0;
-        split_rows(h->d.maxj, &R, &C, h->cluster_max);
-        const int cells = h->d.maxi * R;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(2 * C, n);
-        cfg.blockDim = dim3(std::min(kThreads, (cells + 31) / 32 * 32));
-        cfg.dynamicSmemBytes = smem_bytes(h->d.maxi, R);
-        cfg.stream = h->stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = C;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        EA_TRY(h, cudaLaunchKernelEx(&cfg, k_surface_step, (const EaArgs *)h->dargs, R));
+    const int ncell = h->d.maxi * h->d.maxj;
+    for (int s = 0; s < (post ? nsteps : 1); ++s) {
+        if (h->p.kind == GB_EA_SEAICE_EXPLICIT) {
+            k_seaice_explicit<<<dim3((ncell + 255) / 256, n), 256, 0, h->stream>>>(h->dargs);
+        } else {
+            int R = 0, C = 0;
+            split_rows(h->d.maxj, &R, &C, h->cluster_max);
+            const int cells = h->d.maxi * R;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(2 * C, n);
+            cfg.blockDim = dim3(std::min(kThreads, (cells + 31) / 32 * 32));
+            cfg.dynamicSmemBytes = smem_bytes(h->d.maxi, R);
+            cfg.stream = h->stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = C;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            EA_TRY(h, cudaLaunchKernelEx(&cfg, k_surface_step, (const EaArgs *)h->dargs, R));
+        }
+        count_launches(1);
+        if (post) {
+            k_seaice_post<<<dim3((ncell + 255) / 256, n), 256, 0, h->stream>>>(h->dargs);
+            count_launches(1);
+        }
     }
-    count_launches(1);
     EA_TRY(h, cudaGetLastError());
     EA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
@@ -611,6 +666,27 @@ extern "C" int gb_ea_download_seaice_diag(gb_ea *h, double *variceth, double *va
     const size_t n2 = 2 * (size_t)h->d.maxi * h->d.maxj;
     if (variceth) EA_TRY(h, cudaMemcpyAsync(variceth, h->dth, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     if (varicedy) EA_TRY(h, cudaMemcpyAsync(varicedy, h->ddy, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EA_TRY(h, cudaStreamSynchronize(h->stream));
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_set_seaice_post(gb_ea *h, const gb_ea_seaice_post *post)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (h->p.kind == GB_EA_EMBM) return efail(h, GB_GO_EINVAL, "set_seaice_post: an EMBM handle has no ice");
+    h->post = post != nullptr;
+    if (post) h->pp = *post;
+    return GB_GO_OK;
+}
+
+extern "C" int gb_ea_download_seaice_fluxes(gb_ea *h, double *fx_delta, double *fw_delta)
+{
+    if (!h) return GB_GO_EINVAL;
+    if (h->p.kind == GB_EA_EMBM) return efail(h, GB_GO_EINVAL, "download_seaice_fluxes: an EMBM handle has no ice");
+    EA_TRY(h, cudaSetDevice(h->device));
+    const size_t n1 = (size_t)h->d.maxi * h->d.maxj;
+    if (fx_delta) EA_TRY(h, cudaMemcpyAsync(fx_delta, h->fx, n1 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (fw_delta) EA_TRY(h, cudaMemcpyAsync(fw_delta, h->fw, n1 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     EA_TRY(h, cudaStreamSynchronize(h->stream));
     return GB_GO_OK;
 }

@@ -40,6 +40,8 @@ EXPORTED = [
     "gb_ea_create", "gb_ea_destroy", "gb_ea_upload_state", "gb_ea_set_forcing", "gb_ea_step", "gb_ea_step_many",
     "gb_ea_download",
     "gb_ea_download_seaice_diag",
+    "gb_ea_set_seaice_post",
+    "gb_ea_download_seaice_fluxes",
     "gb_ea_last_error",
     "gb_mo_create", "gb_mo_destroy", "gb_mo_set_wind", "gb_mo_upload_velocity", "gb_mo_step", "gb_mo_download",
     "gb_mo_last_error",
@@ -158,6 +160,8 @@ def load_library(path: str = LIB_PATH):
     L.gb_ea_step_many.argtypes = [P(vp), C.c_int32, C.c_int32]
     L.gb_ea_download.argtypes = [vp, dp, dp]
     L.gb_ea_download_seaice_diag.argtypes = [vp, dp, dp]
+    L.gb_ea_set_seaice_post.argtypes = [vp, C.POINTER(abi.GbEaSeaicePost)]
+    L.gb_ea_download_seaice_fluxes.argtypes = [vp, dp, dp]
     L.gb_ea_last_error.argtypes = [vp]
     L.gb_ea_last_error.restype = C.c_char_p
     L.gb_mo_create.argtypes = [vp, vp, vp, C.c_int, P(vp)]

@@ -127,6 +127,14 @@ def seaice_case(member, seed: int = 0, explicit: bool = False) -> SurfaceCase:
                        diffsic=2000.0 / (rsc * usc), tsc=tsc, sica_thresh=0.9, sich_thresh=2.5)
 
 
+def seaice_post_constants(case: SurfaceCase) -> abi.GbEaSeaicePost:
+    """The reference's post-processing constants for a sea-ice case: rhoio = rhoice/rho0,
+    rhoice = 913, rho0 = 1000, hmin = 0.01 (gold_seaice_lib.f90:33-34; gold_seaice.f90:304),
+    rdtdim = 1/(tsc*dtsic) (gold_seaice.f90:262), hlf = 3.34e5 (gold_seaice_lib.f90:38), m2mm = 1000."""
+    return abi.GbEaSeaicePost(rhoio=913.0 / 1.0e3, rhoice=913.0, hlf=3.34e5, hmin=0.01,
+                              rdtdim=1.0 / (case.tsc * case.dt), m2mm=1000.0)
+
+
 class SurfaceStepper:
     """A device-resident surface grid (gb_ea handle)."""
 
@@ -182,6 +190,20 @@ class SurfaceStepper:
         tq1 = np.zeros((c.maxj, c.maxi, 2))
         self._check(self.lib.gb_ea_download(self.h, dptr(tq), dptr(tq1)), "gb_ea_download")
         return tq, tq1
+
+    def set_seaice_post(self, post: Optional[abi.GbEaSeaicePost]):
+        """Post-process every sea-ice step as step_seaice does (gold_seaice.f90:599-619), or
+        stop (None); with it on, step(n) takes n step_seaice steps."""
+        self._check(self.lib.gb_ea_set_seaice_post(self.h, None if post is None else C.byref(post)),
+                    "gb_ea_set_seaice_post")
+
+    def download_seaice_fluxes(self):
+        """(fx_delta, fw_delta) [j, i] of the last post-processed step."""
+        c = self.case
+        fx = np.zeros((c.maxj, c.maxi))
+        fw = np.zeros((c.maxj, c.maxi))
+        self._check(self.lib.gb_ea_download_seaice_fluxes(self.h, dptr(fx), dptr(fw)), "gb_ea_download_seaice_fluxes")
+        return fx, fw
 
     def download_seaice_diag(self):
         """(variceth, varicedy) [j, i, l] of the last tstipsic step (gold_seaice.f90:1046-1056)."""

@@ -74,9 +74,27 @@ int gb_ea_upload_state(gb_ea *h, const double *tq, const double *tq1);
    `vel` (2, maxi, maxj) -- u(1,i,j) on the east face, u(2,i,j) on the north face; pptn NULL. */
 int gb_ea_set_forcing(gb_ea *h, const double *source, const double *vel, const double *pptn);
 /* EMBM: nsteps tstipa steps with the same forcing, each ending with tq1 = tq
-   (embm.f90:2137).  Sea ice: nsteps = 1, one tstipsic; tq1 is left as it was (step_seaice
-   post-processes the ice and copies it, gold_seaice.f90:604-619). */
+   (embm.f90:2137).  Sea ice without post-processing: nsteps = 1, one tstipsic (or tstepsic);
+   tq1 is left as it was, for the caller's step_seaice to post-process the ice and copy it
+   (gold_seaice.f90:599-619).  Sea ice with post-processing (gb_ea_set_seaice_post): nsteps
+   step_seaice steps with the same forcing, each the transport step followed by that
+   post-processing on the device. */
 int gb_ea_step(gb_ea *h, int32_t nsteps);
+
+/* step_seaice's post-processing of each sea-ice step (gold_seaice.f90:599-619) on the ocean
+   cells: varice(2) held in [0, 1]; where varice(1) < hmin the ice is removed with
+   fx_delta = -varice(1)*rhoice*hlf*rdtdim and fw_delta += varice(1)*rhoio*rdtdim, after
+   fw_delta = -rhoio*dtha(1); fw_delta is then converted by m2mm; varice1 = varice.  The
+   constants are the reference's (gold_seaice.f90:262, 304; gold_seaice_lib.f90:33-34, 38). */
+typedef struct {
+    double rhoio, rhoice, hlf, hmin, rdtdim, m2mm;
+} gb_ea_seaice_post;
+/* Turn the post-processing on for the handle's following steps (post copied), or off (NULL).
+   GB_GO_EINVAL for an EMBM handle.  Grids stepped together must agree on it. */
+int gb_ea_set_seaice_post(gb_ea *h, const gb_ea_seaice_post *post);
+/* fx_delta, fw_delta (maxi, maxj) of the last post-processed step: 0 on land and before the
+   first post-processed step.  Either pointer may be NULL. */
+int gb_ea_download_seaice_fluxes(gb_ea *h, double *fx_delta, double *fw_delta);
 /* The same for n grids of one kind and shape on one device (an ensemble), in one launch:
    errors are reported on handles[0]. */
 int gb_ea_step_many(gb_ea *const *handles, int32_t n, int32_t nsteps);

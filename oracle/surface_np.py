@@ -5,6 +5,7 @@ separately from oracle/surface_oracle.c:
   tstipa    src/embm/embm.f90:2039-2138
   tstipsic  src/goldsteinseaice/gold_seaice.f90:937-1058 (its diagnostics of :1046-1056 in
             seaice_diag)
+  step_seaice's post-processing  gold_seaice.f90:599-619 (seaice_post)
   tstepsic  src/goldsteinseaice/gold_seaice.f90:844-929 (as whole-array face fluxes: the
             reference's west/south carries are the east/north fluxes of the neighbours)
 Arrays are [j, i] views (C order) of the Fortran (i, j) fields; tq is [j, i, l].  Every cell's
@@ -104,6 +105,29 @@ def seaice_diag(maxk, dt, tsc, k1, tq, tq1, dtha, variceth, varicedy):
     th = tsc * dt * dtha
     variceth[...] = np.where(wet, th, variceth)
     varicedy[...] = np.where(wet, tq - tq1 - th, varicedy)
+
+
+
+def seaice_post(maxk, k1, tq, tq1, dtha, rhoio, rhoice, hlf, hmin, rdtdim, m2mm):
+    """step_seaice's post-processing of a sea-ice step (gold_seaice.f90:599-619) on the ocean
+    cells: tq (varice) and tq1 (varice1) [j, i, l] updated in place; returns (fx_delta,
+    fw_delta) [j, i], 0 on land (gold_seaice.f90:578-579)."""
+    maxj, maxi = tq.shape[:2]
+    wet = k1[1:maxj + 1, 1:maxi + 1] <= maxk
+    h = tq[..., 0]
+    a = tq[..., 1]
+    m = np.where(1.0 < a, 1.0, a)                 # MAX(0.0, MIN(1.0, varice(2)))
+    a = np.where(0.0 > m, 0.0, m)
+    fw = -(rhoio * dtha[..., 0])
+    thin = h < hmin
+    fx = np.where(thin, -(((h * rhoice) * hlf) * rdtdim), 0.0)
+    fw = np.where(thin, fw + (h * rhoio) * rdtdim, fw)
+    h = np.where(thin, 0.0, h)
+    a = np.where(thin, 0.0, a)
+    new = np.stack([h, a], axis=-1)
+    tq[...] = np.where(wet[..., None], new, tq)
+    tq1[...] = np.where(wet[..., None], new, tq1)
+    return np.where(wet, fx, 0.0), np.where(wet, fw * m2mm, 0.0)
 
 
 def tstepsic(maxk, dt, rdphi, diffsic, tsc, sica, sich, rc, cv, rdsv, rds, k1, tq, tq1, dtha, vel):

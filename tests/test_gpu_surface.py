@@ -181,3 +181,101 @@ def test_seaice_diagnostics_forms(gpu_lib):
         e_.download_seaice_diag()
     assert e.value.code == abi.GB_GO_EINVAL
     e_.close()
+
+
+def _post_case(m, seed, explicit):
+    """A sea-ice case with thin ice (under hmin) and areas above 1 on some ocean cells."""
+    c = surface.seaice_case(m, seed=seed, explicit=explicit)
+    rng = np.random.default_rng(seed + 1)
+    thin = rng.random(c.tq.shape[:2]) < 0.2
+    c.tq[..., 0] = np.where(thin, c.tq[..., 0] * 0.003, c.tq[..., 0])
+    c.tq[..., 1] = np.where(rng.random(c.tq.shape[:2]) < 0.1, c.tq[..., 1] + 0.3, c.tq[..., 1])
+    c.tq1 = c.tq.copy()
+    return c
+
+
+def _ref_post_steps(c, nsteps, post):
+    """nsteps step_seaice steps on the oracles: transport, diagnostics, post-processing."""
+    from oracle import surface_np as snp
+    ref = c.copy()
+    th, dy = np.zeros_like(c.tq), np.zeros_like(c.tq)
+    fx = fw = None
+    for _ in range(nsteps):
+        before = ref.tq1.copy()
+        ol.surface_step(ref, 1)
+        if ref.kind == abi.GB_EA_SEAICE:
+            snp.seaice_diag(ref.maxk, ref.dt, ref.tsc, ref.k1, ref.tq, before, ref.source, th, dy)
+        fx, fw = snp.seaice_post(ref.maxk, ref.k1, ref.tq, ref.tq1, ref.source, post.rhoio, post.rhoice, post.hlf,
+                                 post.hmin, post.rdtdim, post.m2mm)
+    return ref, th, dy, fx, fw
+
+
+def _bits_equal(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+@pytest.mark.parametrize("explicit", [False, True], ids=["tstipsic", "tstepsic"])
+@pytest.mark.parametrize("cfg", [dict(maxi=36, maxj=36, maxk=16, maxl=2, seed=28, land_frac=0.5),
+                                 dict(maxi=180, maxj=90, maxk=8, maxl=2, seed=29, land_frac=0.4)],
+                         ids=["36x36", "180x90"])
+def test_seaice_post_steps_bitexact(gpu_lib, cfg, explicit):
+    """Several step_seaice steps in one call (transport + gold_seaice.f90:599-619 on the device)
+    against the oracles step by step: ice, fluxes and diagnostics bit for bit."""
+    m = grid.make_member(grid.MemberConfig(**cfg))
+    c = _post_case(m, 30, explicit)
+    post = surface.seaice_post_constants(c)
+    s = surface.SurfaceStepper(c.copy())
+    s.set_seaice_post(post)
+    s.upload_state()
+    s.set_forcing()
+    s.step(3)
+    tq, tq1 = s.download()
+    fx, fw = s.download_seaice_fluxes()
+    th, dy = s.download_seaice_diag()
+    s.close()
+    ref, th_ref, dy_ref, fx_ref, fw_ref = _ref_post_steps(c, 3, post)
+    assert _bits_equal(tq, ref.tq) and _bits_equal(tq1, ref.tq1)
+    assert _bits_equal(fx, fx_ref) and _bits_equal(fw, fw_ref)
+    assert _bits_equal(th, th_ref) and _bits_equal(dy, dy_ref)
+    wet = m.k1[1:-1, 1:-1] <= m.maxk
+    assert (fx[wet] != 0).any() and (fw[wet] != 0).any() and not fx[~wet].any() and not fw[~wet].any()
+    assert (tq[..., 1] <= 1.0).all() and (tq[..., 1] >= 0.0).all()
+
+
+def test_seaice_post_many_and_errors(gpu_lib):
+    """Batched post-processed steps equal the oracles per grid; grids that differ in
+    post-processing cannot step together; EMBM has none; without it sea ice takes one step."""
+    from cgenie_gb300.goldstein import GoldsteinError
+    cases = [_post_case(grid.make_member(grid.MemberConfig(maxi=36, maxj=36, maxk=8, maxl=2, seed=40 + n,
+                                                           land_frac=0.3)), 50 + n, False) for n in range(3)]
+    post = surface.seaice_post_constants(cases[0])
+    steppers = [surface.SurfaceStepper(c.copy()) for c in cases]
+    for st in steppers:
+        st.set_seaice_post(post)
+        st.upload_state()
+        st.set_forcing()
+    surface.step_many(steppers, 2)
+    for st, c in zip(steppers, cases):
+        ref, _, _, fx_ref, fw_ref = _ref_post_steps(c, 2, post)
+        tq, tq1 = st.download()
+        fx, fw = st.download_seaice_fluxes()
+        assert _bits_equal(tq, ref.tq) and _bits_equal(tq1, ref.tq1)
+        assert _bits_equal(fx, fx_ref) and _bits_equal(fw, fw_ref)
+    steppers[1].set_seaice_post(None)
+    with pytest.raises(GoldsteinError) as e:
+        surface.step_many(steppers, 1)
+    assert e.value.code == abi.GB_GO_EINVAL
+    with pytest.raises(GoldsteinError) as e:
+        steppers[1].step(2)
+    assert e.value.code == abi.GB_GO_EINVAL
+    for st in steppers:
+        st.close()
+    m = grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=8, maxl=2, seed=41))
+    e_ = surface.SurfaceStepper(surface.embm_case(m, seed=1))
+    with pytest.raises(GoldsteinError) as e:
+        e_.set_seaice_post(post)
+    assert e.value.code == abi.GB_GO_EINVAL
+    with pytest.raises(GoldsteinError) as e:
+        e_.download_seaice_fluxes()
+    assert e.value.code == abi.GB_GO_EINVAL
+    e_.close()

@@ -95,3 +95,29 @@ def test_seaice_diag_splits_the_change():
     np.testing.assert_allclose((th + dy)[wet], (a.tq - c.tq1)[wet], rtol=0, atol=1e-12 * np.abs(a.tq).max())
     assert (th[~wet] == 7.0).all() and (dy[~wet] == 7.0).all()
     assert np.abs(dy[wet]).max() > 0
+
+
+def test_seaice_post_known_answers():
+    """step_seaice's post-processing (gold_seaice.f90:599-619) on hand-set cells: area held in
+    [0, 1], thin ice removed with its heat and water, varice1 = varice, land untouched."""
+    m = grid.make_member(grid.MemberConfig(maxi=12, maxj=10, maxk=8, maxl=2, seed=4, land_frac=0.3))
+    c = surface.seaice_case(m, seed=6)
+    wet = np.argwhere(m.k1[1:-1, 1:-1] <= m.maxk)
+    dry = np.argwhere(m.k1[1:-1, 1:-1] > m.maxk)
+    (j0, i0), (j1, i1) = wet[0], wet[1]
+    tq = np.zeros_like(c.tq)
+    tq[j0, i0] = (0.005, 1.4)    # thin: removed
+    tq[j1, i1] = (0.5, -0.2)     # area clamped to 0
+    jd, id_ = dry[0]
+    tq[jd, id_] = (0.001, 2.0)   # land: untouched
+    tq1 = np.full_like(tq, 9.0)
+    dtha = np.full_like(tq, 2e-9)
+    p = surface.seaice_post_constants(c)
+    fx, fw = snp.seaice_post(c.maxk, c.k1, tq, tq1, dtha, p.rhoio, p.rhoice, p.hlf, p.hmin, p.rdtdim, p.m2mm)
+    assert tuple(tq[j0, i0]) == (0.0, 0.0) and tuple(tq1[j0, i0]) == (0.0, 0.0)
+    assert fx[j0, i0] == -(0.005 * 913.0 * 3.34e5 * p.rdtdim)
+    assert fw[j0, i0] == (-(p.rhoio * 2e-9) + 0.005 * p.rhoio * p.rdtdim) * 1000.0
+    assert tuple(tq[j1, i1]) == (0.5, 0.0) and fx[j1, i1] == 0.0
+    assert fw[j1, i1] == -(p.rhoio * 2e-9) * 1000.0
+    assert tuple(tq[jd, id_]) == (0.001, 2.0) and tuple(tq1[jd, id_]) == (9.0, 9.0)
+    assert fx[jd, id_] == 0.0 and fw[jd, id_] == 0.0
