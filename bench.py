@@ -17,6 +17,9 @@ Workloads (seeded synthetic members with the reference's grid formulas):
       the model calls it; `value` is air cell-updates/s
   ea36e the EMBM step of a 256-member ensemble of 36x36 surface grids, one launch per step
       for all members (gb_ea_step_many)
+  ice64 step_seaice on a 64x64 grid: the implicit sea-ice transport (tstipsic) with its
+      diagnostics, then the post-processing (area clamp, thin-ice removal and its fluxes), two
+      launches per step; `value` is ice cell-updates/s (two tracers per cell)
   ocean36 the device-resident ocean step of a 36x36x16 basin with 8 tracers: momentum, then
       tstepo (split-precision form), and the BIOGEM tracer coupling every 5th step; `value` is
       tracer cell-updates/s of the whole step
@@ -67,6 +70,7 @@ WORKLOADS = {
     "bg5": dict(name="biogem_tracercoupling_360x180x32_L24_sed8", factory="config_c5", n_l_sed=8),
     "ea64": dict(name="embm_tstipa_64x64", maxi=64, maxj=64),
     "ea36e": dict(name="embm_tstipa_ensemble256_36x36", maxi=36, maxj=36, members=256),
+    "ice64": dict(name="seaice_step_seaice_64x64", maxi=64, maxj=64, kind="ice"),
     "mo36": dict(name="momentum_36x36x16_2islands", maxi=36, maxj=36, maxk=16),
     "rs5": dict(name="goldstein_restart_write_360x180x32_L24", factory="config_c5"),
     "rs5s": dict(name="goldstein_restart_write_360x180x32_L2", factory="config_c5", maxl=2),
@@ -345,19 +349,35 @@ def run_bg(args, rank, world, local, dist):
 def _ea_case(w, member: int = 0):
     from cgenie_gb300 import grid, surface
     m = grid.make_member(grid.MemberConfig(maxi=w["maxi"], maxj=w["maxj"], maxk=8, maxl=2, seed=21 + 7919 * member))
+    if w.get("kind") == "ice":
+        return surface.seaice_case(m, seed=22 + 7919 * member)
     return surface.embm_case(m, seed=22 + 7919 * member)
+
+
+def _ice_oracle_steps(c, n):
+    """n step_seaice steps on the oracles: transport (C restatement), post-processing (NumPy)."""
+    from cgenie_gb300 import surface
+    from oracle import oracle_lib
+    from oracle import surface_np as snp
+    p = surface.seaice_post_constants(c)
+    for _ in range(n):
+        oracle_lib.surface_step(c, 1)
+        snp.seaice_post(c.maxk, c.k1, c.tq, c.tq1, c.source, p.rhoio, p.rhoice, p.hlf, p.hmin, p.rdtdim, p.m2mm)
 
 
 def ea_cpu_rate(case, target_s: float = 10.0):
     """The oracle's tstipa (serial, 1 core): (cell-updates/s, steps)."""
+    from cgenie_gb300 import abi
     from oracle import oracle_lib
     c = case.copy()
+    run = (lambda k: _ice_oracle_steps(c, k)) if case.kind == abi.GB_EA_SEAICE else \
+        (lambda k: oracle_lib.surface_step(c, k))
     t0 = time.perf_counter()
-    oracle_lib.surface_step(c, 10)
+    run(10)
     per = (time.perf_counter() - t0) / 10
     n = max(10, min(100000, int(target_s / max(per, 1e-9))))
     t0 = time.perf_counter()
-    oracle_lib.surface_step(c, n)
+    run(n)
     dt = time.perf_counter() - t0
     return case.maxi * case.maxj * 2 * n / dt, n
 
@@ -378,6 +398,10 @@ def run_ea(args, rank, world, local, dist):
     for st in steppers:
         st.upload_state()
         st.set_forcing()
+    ice = w.get("kind") == "ice"
+    if ice:
+        for st in steppers:
+            st.set_seaice_post(surface.seaice_post_constants(case))
     s = steppers[0]
     step = (lambda: s.step(1)) if nmem == 1 else (lambda: surface.step_many(steppers, 1))
     for _ in range(args.warmup):
@@ -400,10 +424,11 @@ def run_ea(args, rank, world, local, dist):
     # end to end: the step's forcing (tqa, uatm, pptn) from pinned host memory, the step, tq back
     src_h = torch.from_numpy(np.ascontiguousarray(case.source)).pin_memory()
     vel_h = torch.from_numpy(np.ascontiguousarray(case.vel)).pin_memory()
-    pp_h = torch.from_numpy(np.ascontiguousarray(case.pptn)).pin_memory()
+    pp_h = None if ice else torch.from_numpy(np.ascontiguousarray(case.pptn)).pin_memory()
     tq_h = torch.empty(tuple(case.tq.shape), dtype=torch.float64).pin_memory()
+    fl_h = torch.empty((2, case.maxj, case.maxi), dtype=torch.float64).pin_memory()   # fx_delta, fw_delta
     dp = C.POINTER(C.c_double)
-    ptr = lambda t: C.cast(t.data_ptr(), dp)   # noqa: E731
+    ptr = lambda t: None if t is None else C.cast(t.data_ptr(), dp)   # noqa: E731
     e2e_steps = args.steps if nmem == 1 else max(1, args.steps // 10)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -412,26 +437,35 @@ def run_ea(args, rank, world, local, dist):
         step()
         for st in steppers:
             st.lib.gb_ea_download(st.h, ptr(tq_h), None)
+            if ice:
+                st.lib.gb_ea_download_seaice_fluxes(st.h, ptr(fl_h[0]), ptr(fl_h[1]))
     e2e_s = time.perf_counter() - t0
     peak, peak_kind = measured_peaks()
-    alg = 13 * 8 * case.maxi * case.maxj * nmem   # read tq, tq1, tqa, uatm (2 each), pptn; write tq, tq1
+    # EMBM: read tq, tq1, tqa, uatm (2 each), pptn; write tq, tq1.  Sea ice: the transport reads
+    # tq, tq1, dtha, u (2 each) and writes tq, variceth, varicedy; the post-processing reads tq,
+    # dtha(1) and writes tq, tq1, fx_delta, fw_delta (23 doubles per cell)
+    alg = (23 if ice else 13) * 8 * case.maxi * case.maxj * nmem
     achieved = alg / (dev_s / args.steps) / 1e9
+    unit = "ice cell-updates/s" if ice else "air cell-updates/s"
     if rank == 0:
         line = {
-            "metric": "air cell-updates/s", "value": value, "unit": "air cell-updates/s", "n_gpus": world,
+            "metric": unit, "value": value, "unit": unit, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fields on the reference's sin-latitude grid)",
             "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2, "grids": nmem,
-                       "timing": "host clock around the synchronous C-ABI step calls (one launch each)",
+                       "timing": "host clock around the synchronous C-ABI step calls (%s each)"
+                                 % ("two launches" if ice else "one launch"),
                        "l2": "not flushed: the grid (0.3 MB) lives in L2, as in the model",
                        "parallelism": f"replicas{world}"},
-            "e2e": {"value": world * units * e2e_steps / e2e_s, "unit": "air cell-updates/s",
-                    "h2d_bytes_per_step": int(src_h.numel() + vel_h.numel() + pp_h.numel()) * 8 * nmem,
-                    "d2h_bytes_per_step": int(tq_h.numel()) * 8 * nmem,
-                    "note": "per step and grid: tqa + uatm + pptn H2D (pinned), step, tq D2H"},
+            "e2e": {"value": world * units * e2e_steps / e2e_s, "unit": unit,
+                    "h2d_bytes_per_step": int(src_h.numel() + vel_h.numel() + (0 if ice else pp_h.numel())) * 8 * nmem,
+                    "d2h_bytes_per_step": int(tq_h.numel() + (fl_h.numel() if ice else 0)) * 8 * nmem,
+                    "note": ("per step and grid: dtha + u H2D (pinned), step_seaice, tq + fx_delta + fw_delta D2H"
+                             if ice else "per step and grid: tqa + uatm + pptn H2D (pinned), step, tq D2H")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "peak_source": peak_kind, "kernel": "k_surface_step",
+                         "traffic": None, "peak_source": peak_kind,
+                         "kernel": "k_surface_step + k_seaice_post (one step)" if ice else "k_surface_step",
                          "algorithmic_bytes_per_launch": alg,
                          "note": "latency-bound: one cluster of 8 blocks per tracer, 5 cluster-barrier-separated "
                                  "sweeps per step; the HBM roofline does not bind a 0.3 MB grid"},
@@ -440,8 +474,9 @@ def run_ea(args, rank, world, local, dist):
         }
         if not args.no_cpu_baseline:
             v, n = ea_cpu_rate(case)
-            line["cpu_baseline"] = {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
-                                    "sample": f"{n} steps of the same grid, oracle C restatement, -O2"}
+            line["cpu_baseline"] = {"value": v, "unit": unit, "cores": 1, "kind": "port",
+                                    "sample": f"{n} steps of the same grid, oracle C restatement, -O2"
+                                              + (" + NumPy post-processing" if ice else "")}
         print(json.dumps(line))
     for st in steppers:
         st.close()
@@ -824,17 +859,19 @@ def run_reference(args, rank, world):
         }
         print(json.dumps(line))
         return
-    if args.workload in ("ea64", "ea36e"):
+    if args.workload in ("ea64", "ea36e", "ice64"):
         case = _ea_case(w)
         v, n = ea_cpu_rate(case, target_s=min(10.0, 0.01 * max(args.steps, 1)))
+        unit = "ice cell-updates/s" if w.get("kind") == "ice" else "air cell-updates/s"
         line = {
-            "metric": "air cell-updates/s", "value": v, "unit": "air cell-updates/s", "impl": "reference",
+            "metric": unit, "value": v, "unit": unit, "impl": "reference",
             "n_gpus": world, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * case.maxi * case.maxj * 2 / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": w["name"], "maxi": case.maxi, "maxj": case.maxj, "tracers": 2},
-            "cpu_baseline": {"value": v, "unit": "air cell-updates/s", "cores": 1, "kind": "port",
-                             "sample": f"{n} steps, oracle C restatement, serial (the reference routine is serial)"},
-            "e2e": {"value": v, "unit": "air cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_baseline": {"value": v, "unit": unit, "cores": 1, "kind": "port",
+                             "sample": f"{n} steps, oracle C restatement" + (" + NumPy post-processing" if w.get("kind") == "ice" else "")
+                                       + ", serial (the reference routine is serial)"},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
         return
@@ -1167,7 +1204,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    if args.workload in ("ea64", "ea36e"):
+    if args.workload in ("ea64", "ea36e", "ice64"):
         run_ea(args, rank, world, local, dist)
         if dist:
             dist.destroy_process_group()
